@@ -1,0 +1,306 @@
+"""Benchmark: LM iterations/s of the GB300 bundle-adjustment solver.
+
+Workload (default): benchmark configuration 1 — one synthetic BAL problem,
+250 cameras on a random walk, 60,000 points, ~296k observations, 50 LM
+iterations (tolerances off so all 50 run), PCG capped at 100 iterations
+(residual criterion 1e-6).  A step is one full solve.  `value` = LM
+iterations/s of the mixed-precision form with the problem resident in HBM
+(re-solved from its initial point on the device, L2 flushed between steps);
+`forms` also reports the plain FP64 form; `e2e` = the same metric through the
+public C ABI call (gba_solve) with host buffers, host prep and transfers
+inside the timed region.
+
+--impl reference times the CPU oracle (the C restatement of the reference's
+Ceres path: exact Schur + dense Cholesky) on this host's cores instead.
+
+Multi-GPU (torchrun, N>1): replicas only — each rank solves its own copy of
+the workload (weak scaling); value = all ranks' LM iterations / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "LM iters/s and solves/s per GB300 (mixed vs plain FP64 GPU); p50/p99 latency"
+UNIT = "LM iter/s"
+
+
+def workload_options(precision: str) -> dict:
+    return dict(max_num_iterations=50, function_tolerance=0.0, gradient_tolerance=0.0, parameter_tolerance=0.0,
+                max_linear_solver_iterations=100, pcg_tolerance=1e-6, precision=precision, loss="trivial")
+
+
+def config_dict(problem, extra=None) -> dict:
+    d = {"workload": "config1: synthetic BAL, 250 cams random walk, 60k points, "
+                     f"{problem.num_observations()} obs, 50 LM iters, PCG<=100",
+         "num_cameras": problem.num_cameras(), "num_points": problem.num_points(),
+         "num_observations": problem.num_observations(), "lm_iterations": 50, "pcg_cap": 100,
+         "l2": "flushed between steps (256 MiB write on the solver stream, outside the timed events)",
+         "parallelism": "replicas"}
+    if extra:
+        d.update(extra)
+    return d
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown," \
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown," \
+             "clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, index: int = 0):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.index), "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return {"hbm_gbs": 6800.0, "fallback": True}
+
+
+def cpu_baseline(seconds_budget: float = 20.0) -> dict:
+    """The oracle (C restatement of the reference path, exact Schur + dense
+    Cholesky, OpenMP on all host cores) on a bounded sample of the workload:
+    the first LM iterations of the same problem."""
+    from oracle import oracle_py as O
+    from slamplay_gb300 import BALProblem
+
+    b = BALProblem.synthetic(1, seed=0)
+    iters = 2
+    t0 = time.perf_counter()
+    res = O.solve(O.Problem.from_bal(b), max_num_iterations=iters, function_tolerance=0.0, gradient_tolerance=0.0,
+                  parameter_tolerance=0.0, linear_solver="dense_schur")
+    dt = time.perf_counter() - t0
+    cores = os.cpu_count() or 1
+    return {"value": res["num_iterations"] / dt, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"config1 problem, first {res['num_iterations']} LM iterations (+ initial evaluation), "
+                      f"oracle dense-Schur LM, {dt:.1f} s"}
+
+
+def run_reference(args) -> None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    for _ in range(args.warmup):
+        pass  # the CPU oracle has no warm-up state worth timing
+    vals = []
+    for _ in range(args.steps):
+        cb = cpu_baseline()
+        vals.append(cb["value"])
+    v = statistics.median(vals)
+    from slamplay_gb300 import BALProblem
+
+    b = BALProblem.synthetic(1, seed=0)
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * 2 / v if v else None,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config_dict(b, {"reference": "CPU oracle port (Ceres' path restated: LM + exact Schur + "
+                                                   "dense Cholesky); the Ceres build is unavailable here"}),
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cb["cores"], "kind": "port", "sample": cb["sample"]},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def launches_per_solve(s) -> int:
+    # setup: sync, init, table, eval x2 (2 kernels each), scale, post, gather
+    return 10 + 10 * s.num_iterations + 3 * s.num_linear_solver_iterations
+
+
+def run_gpu(args) -> None:
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    from slamplay_gb300 import BALProblem, Solver
+
+    problem = BALProblem.synthetic(1, seed=0)
+    stream = torch.cuda.Stream()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def timed_form(precision: str):
+        s = Solver(device=local, stream=stream.cuda_stream, **workload_options(precision))
+        p0 = problem.copy()
+        first = s.solve(p0)  # uploads the problem, builds the graph
+        iters = first.num_iterations
+        for _ in range(args.warmup):
+            s.solve_resident(1)
+        s.synchronize()
+        times = []
+        for _ in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(1)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            s.solve_resident(1)
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+        return s, first, iters, times
+
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    t_wall0 = time.perf_counter()
+    sm, first_m, iters_m, times_m = timed_form("mixed")
+    t_wall1 = time.perf_counter()
+    clk = clocks.stop()
+    torch.cuda.synchronize()
+    sp, first_p, iters_p, times_p = timed_form("fp64")
+    ms_m = sum(times_m) / len(times_m)
+    ms_p = sum(times_p) / len(times_p)
+    if dist:
+        t = torch.tensor([ms_m, ms_p], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_m, ms_p = t.tolist()
+    value = world * iters_m / (ms_m * 1e-3)
+    value_p = world * iters_p / (ms_p * 1e-3)
+
+    # e2e through gba_solve: host arrays in, host prep + H2D + solve + D2H
+    e2e_times = []
+    h2d = d2h = 0
+    for _ in range(max(1, min(args.steps, 5))):
+        p = problem.copy()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        su = sm.solve(p)
+        e2e_times.append(time.perf_counter() - t0)
+    no, nc, np_ = problem.num_observations(), problem.num_cameras(), problem.num_points()
+    h2d = 24 * no + 8 * (9 * nc + 3 * np_)
+    d2h = 8 * (9 * nc + 3 * np_)
+    e2e_s = statistics.median(e2e_times)
+    e2e_val = world * su.num_iterations / e2e_s
+
+    # per-kernel device times (host-driven pass with CUDA events per launch)
+    sm.set_profiling(True)
+    sm.solve(problem.copy())
+    sm.set_profiling(False)
+    prof = [e for e in sm.profile() if e["launches"] > 0]
+    top = max(prof, key=lambda e: e["total_ms"]) if prof else None
+    peaks = measured_peaks()
+    roof = None
+    if top:
+        avg_ms = top["total_ms"] / top["launches"]
+        bytes_per = top["bytes"] / top["launches"]
+        ach = bytes_per / (avg_ms * 1e-3) / 1e9
+        peak = peaks.get("hbm_gbs", 6800.0)
+        roof = {"kernel": top["name"], "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
+                "frac": ach / peak, "traffic": None, "bytes_per_launch": bytes_per, "avg_launch_ms": avg_ms,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if not peaks.get("fallback")
+                else "fallback 6.8 TB/s"}
+    if rank == 0:
+        cb = cpu_baseline() if world == 1 else None
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_m, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64 (mixed)", "data": "synthetic",
+            "config": config_dict(problem),
+            "forms": {
+                "mixed": {"lm_iters_per_s": value, "solves_per_s": world * 1e3 / ms_m, "ms_per_solve": ms_m,
+                          "lm_iterations": iters_m, "pcg_iterations": first_m.num_linear_solver_iterations,
+                          "final_cost": first_m.final_cost},
+                "fp64": {"lm_iters_per_s": value_p, "solves_per_s": world * 1e3 / ms_p, "ms_per_solve": ms_p,
+                         "lm_iterations": iters_p, "pcg_iterations": first_p.num_linear_solver_iterations,
+                         "final_cost": first_p.final_cost},
+                "mixed_vs_fp64_final_cost_rel": abs(first_m.final_cost - first_p.final_cost) / first_p.final_cost,
+            },
+            "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "ms_per_step": 1e3 * e2e_s},
+            "roofline": roof,
+            "kernels": prof,
+            "cpu_baseline": cb,
+            "gpu_launches": args.steps * launches_per_solve(first_m),
+            "clocks": clk,
+            "wall_s_timed": t_wall1 - t_wall0,
+        }
+        print(json.dumps(line), flush=True)
+    sm.close()
+    sp.close()
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gba", choices=["gba", "reference"])
+    args = ap.parse_args()
+    from slamplay_gb300 import build as B
+
+    B.build()
+    if args.impl == "reference":
+        from oracle import oracle_py
+
+        oracle_py.ensure_built()
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

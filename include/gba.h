@@ -1,0 +1,329 @@
+/*
+ * gba.h — C ABI of the GB300-native bundle-adjustment solver (libgba.so).
+ *
+ * Drop-in replacement for the Ceres solve in slamplay's
+ * backend/slam_ba_simple_g2o_ceres/test_bundle_adjustment_ceres.cpp:58-101
+ * (`void SolveBA(BALProblem&)`).  The problem keeps the BALProblem layout of
+ * utils/datasets/BALProblem.h:31-119:
+ *   parameters  = double[9*nc + 3*np], cameras first (BALProblem.h:80,82);
+ *                 camera = [angle-axis(3), translation(3), f, k1, k2]
+ *                 (utils/camera/SnavelyReprojectionError.h:55-59), point = xyz;
+ *   camera_index, point_index = int32[no] (BALProblem.h:67-69);
+ *   observations = double[2*no], interleaved u,v (BALProblem.h:71).
+ * One residual block per observation, r = predict(camera, point) - (u, v)
+ * (SnavelyReprojectionError.h:42-53), optional Huber loss
+ * (test_bundle_adjustment_ceres.cpp:78), additive update of all 9 camera
+ * parameters (no manifold, test_bundle_adjustment_ceres.cpp:86).
+ *
+ * Memory: every pointer in this header is caller-owned HOST memory.  The
+ * library copies in, solves on one GPU, and copies `parameters` back in place.
+ * Threading: a gba_handle owns one CUDA stream and is used from one host
+ * thread at a time.  Every entry point returns a gba_status; the message of
+ * the last failure is available from gba_last_error().
+ */
+#ifndef GBA_H_
+#define GBA_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBA_ABI_VERSION 1
+
+/* ------------------------------------------------------------------------ */
+/* Status codes.  The reference has none: BALProblem prints parse errors and  */
+/* carries on (utils/datasets/BALProblem.cpp:60-64, :81-84); Ceres reports    */
+/* failures only through Solver::Summary::termination_type.                  */
+/* ------------------------------------------------------------------------ */
+typedef enum gba_status {
+  GBA_OK = 0,
+  GBA_ERR_INVALID_ARGUMENT = 1, /* null pointer, bad size, index out of range */
+  GBA_ERR_OUT_OF_MEMORY = 2,    /* device or host allocation failed / footprint too large */
+  GBA_ERR_NON_FINITE = 3,       /* NaN/Inf in observations or parameters */
+  GBA_ERR_CUDA = 4,             /* CUDA runtime error (message in gba_last_error) */
+  GBA_ERR_TIMEOUT = 5,          /* a bounded device-side wait gave up */
+  GBA_ERR_IO = 6,               /* file could not be opened / parsed */
+  GBA_ERR_NO_DEVICE = 7,        /* no CUDA device or the kernels' image cannot load */
+  GBA_ERR_QUEUE_FULL = 8,       /* serving: admission refused, queue at capacity */
+  GBA_ERR_NOT_FOUND = 9,        /* serving: unknown ticket */
+  GBA_ERR_INTERNAL = 10
+} gba_status;
+
+/* Ceres::TerminationType equivalents (Solver::Summary::termination_type). */
+typedef enum gba_termination {
+  GBA_TERMINATION_CONVERGENCE = 0,
+  GBA_TERMINATION_NO_CONVERGENCE = 1, /* max_num_iterations reached */
+  GBA_TERMINATION_FAILURE = 2         /* evaluation failed / too many invalid steps */
+} gba_termination;
+
+/* Which test ended the minimiser (Ceres' Summary::message, as a code). */
+typedef enum gba_termination_reason {
+  GBA_REASON_NONE = 0,
+  GBA_REASON_MAX_ITERATIONS = 1,
+  GBA_REASON_FUNCTION_TOLERANCE = 2,
+  GBA_REASON_GRADIENT_TOLERANCE = 3,
+  GBA_REASON_PARAMETER_TOLERANCE = 4,
+  GBA_REASON_MIN_TRUST_REGION_RADIUS = 5,
+  GBA_REASON_INVALID_STEPS = 6,
+  GBA_REASON_EVALUATION_FAILED = 7
+} gba_termination_reason;
+
+typedef enum gba_loss {
+  GBA_LOSS_TRIVIAL = 0, /* rho(s) = s                       (no LossFunction)     */
+  GBA_LOSS_HUBER = 1,   /* ceres::HuberLoss(a), test_bundle_adjustment_ceres.cpp:78 */
+  GBA_LOSS_CAUCHY = 2   /* ceres::CauchyLoss(a), backend/ceres/test_ceres_bundle_adjuster_simple.cpp:192-193 */
+} gba_loss;
+
+typedef enum gba_precision {
+  GBA_PRECISION_FP64 = 0,  /* plain: every kernel in FP64 */
+  GBA_PRECISION_MIXED = 1  /* FP32 Jacobians / Schur products / PCG mat-vecs with
+                              compensated sums; FP64 cost, step ratio, dots, norms
+                              and the 3x3 / 9x9 block inverses */
+} gba_precision;
+
+typedef enum gba_pcg_criterion {
+  GBA_PCG_RESIDUAL = 0,        /* stop when |r_k| <= pcg_tolerance * |r_0|          */
+  GBA_PCG_QUADRATIC_MODEL = 1  /* Ceres ITERATIVE_SCHUR's eta (Nash-Sofer) test    */
+} gba_pcg_criterion;
+
+/* ------------------------------------------------------------------------ */
+/* Options.  Defaults (gba_options_init) are Ceres 2.2's Solver::Options     */
+/* defaults for the fields the reference leaves unset                        */
+/* (test_bundle_adjustment_ceres.cpp:96-98), plus the GPU-side knobs.         */
+/* ------------------------------------------------------------------------ */
+typedef struct gba_options {
+  uint32_t abi_version;               /* = GBA_ABI_VERSION                          */
+  int32_t max_num_iterations;         /* 50                                          */
+  double function_tolerance;          /* 1e-6                                        */
+  double gradient_tolerance;          /* 1e-10                                       */
+  double parameter_tolerance;         /* 1e-8                                        */
+  double initial_trust_region_radius; /* 1e4                                         */
+  double max_trust_region_radius;     /* 1e16                                        */
+  double min_trust_region_radius;     /* 1e-32                                       */
+  double min_relative_decrease;       /* 1e-3                                        */
+  double min_lm_diagonal;             /* 1e-6                                        */
+  double max_lm_diagonal;             /* 1e32                                        */
+  int32_t max_num_consecutive_invalid_steps; /* 5                                    */
+  int32_t jacobi_scaling;             /* 1                                           */
+  int32_t loss;                       /* gba_loss, GBA_LOSS_TRIVIAL                  */
+  double loss_scale;                  /* a of Huber/Cauchy, 1.0                      */
+  int32_t precision;                  /* gba_precision, GBA_PRECISION_FP64           */
+  int32_t pcg_criterion;              /* gba_pcg_criterion, GBA_PCG_RESIDUAL         */
+  int32_t max_linear_solver_iterations; /* PCG cap, 500                              */
+  int32_t min_linear_solver_iterations; /* 0                                         */
+  double pcg_tolerance;               /* relative residual for GBA_PCG_RESIDUAL, 1e-10 */
+  double eta;                         /* forcing term for GBA_PCG_QUADRATIC_MODEL, 0.1 */
+  int32_t minimizer_progress_to_stdout; /* 0                                         */
+  int32_t device;                     /* CUDA device ordinal, 0                      */
+  void *stream;                       /* cudaStream_t to run on; NULL = own stream   */
+  int32_t chunk_observations;         /* point-segment tile (obs per CTA), 0 = auto  */
+  int32_t reorder_points;             /* 1 = group points by first camera (locality) */
+  int32_t use_graphs;                 /* 1 = run the LM loop as one CUDA graph       */
+  int32_t reserved[8];
+} gba_options;
+
+/* Per-solve report, the subset of ceres::Solver::Summary the reference
+ * prints with FullReport() (test_bundle_adjustment_ceres.cpp:101). */
+typedef struct gba_summary {
+  double initial_cost;            /* 0.5 * sum rho(|r|^2) at the start            */
+  double final_cost;              /* cost at the returned parameters              */
+  int32_t num_iterations;         /* LM iterations after iteration 0              */
+  int32_t num_successful_steps;
+  int32_t num_unsuccessful_steps;
+  int32_t num_invalid_steps;
+  int64_t num_linear_solver_iterations; /* PCG iterations, summed                 */
+  int32_t termination_type;       /* gba_termination                              */
+  int32_t termination_reason;     /* gba_termination_reason                       */
+  double final_trust_region_radius;
+  double gradient_max_norm;       /* at the returned parameters                   */
+  double setup_time_s;            /* host prep + H2D + device setup               */
+  double solve_time_s;            /* device LM loop (CUDA events)                 */
+  double total_time_s;            /* wall time of the call                        */
+  /* Optional per-iteration trace, caller-allocated; may be NULL.  Entry k is
+   * iteration k (0 = initial point): cost, trust radius, PCG iterations and
+   * step_is_successful, as in Ceres' IterationSummary. */
+  int32_t trace_capacity;
+  int32_t trace_length;
+  double *trace_cost;
+  double *trace_radius;
+  int32_t *trace_linear_iterations;
+  int32_t *trace_successful;
+} gba_summary;
+
+/* A problem in the BALProblem layout (see header comment). */
+typedef struct gba_problem_view {
+  int32_t num_cameras;
+  int32_t num_points;
+  int32_t num_observations;
+  const int32_t *camera_index;  /* [num_observations]                 */
+  const int32_t *point_index;   /* [num_observations]                 */
+  const double *observations;   /* [2 * num_observations] u,v         */
+  double *parameters;           /* [9*num_cameras + 3*num_points] in/out */
+} gba_problem_view;
+
+typedef struct gba_handle gba_handle;
+
+/* ---- lifecycle --------------------------------------------------------- */
+/* Fills `o` with the defaults listed in gba_options. */
+void gba_options_init(gba_options *o);
+/* Creates a solver bound to o->device.  Fails with GBA_ERR_NO_DEVICE when no
+ * GPU is present or the sm_103a kernels cannot load. */
+gba_status gba_create(const gba_options *o, gba_handle **out);
+void gba_destroy(gba_handle *h);
+/* Message of the last failure on `h` (or of the last failed gba_create when
+ * h == NULL).  Valid until the next call on the same handle. */
+const char *gba_last_error(const gba_handle *h);
+/* Version string "gba <abi> sm_103a". */
+const char *gba_version(void);
+
+/* ---- solving ----------------------------------------------------------- */
+/* Replaces ceres::Solve(options, &problem, &summary) as called at
+ * test_bundle_adjustment_ceres.cpp:100 for the problem built at :70-87.
+ * p->parameters is updated in place with the best accepted iterate. */
+gba_status gba_solve(gba_handle *h, const gba_problem_view *p, gba_summary *s);
+
+/* Solves `n` independent problems together: one work list over all
+ * (problem, point-segment) tiles, one LM iteration per graph launch, each
+ * problem with its own trust region and termination.  summaries[i] may be
+ * NULL-filled (pass summaries == NULL to skip reports). */
+gba_status gba_batch_solve(gba_handle *h, const gba_problem_view *problems, int32_t n,
+                           gba_summary *summaries);
+
+/* ---- serving (continuous batching) ------------------------------------- */
+/* Starts the serving loop on the handle: problems submitted with gba_submit
+ * are admitted while their estimated device footprint fits in
+ * `device_budget_bytes` (0 = 90% of free memory) and at most `max_live`
+ * solves are on the device at once; live solves advance one LM iteration
+ * per step, finished ones free their slot immediately. */
+gba_status gba_server_start(gba_handle *h, size_t device_budget_bytes, int32_t max_live,
+                            int32_t max_queue);
+/* Queues a solve.  The view's arrays must stay valid until gba_poll reports
+ * it done; parameters are written back in place then. */
+gba_status gba_submit(gba_handle *h, const gba_problem_view *p, uint64_t *ticket);
+/* done = 1 when the ticket's solve finished (summary filled, ticket freed). */
+gba_status gba_poll(gba_handle *h, uint64_t ticket, gba_summary *s, int32_t *done);
+/* Blocks until every submitted problem is done, then stops the loop. */
+gba_status gba_server_stop(gba_handle *h);
+
+typedef struct gba_server_stats {
+  int64_t submitted, admitted, completed, rejected;
+  int32_t live, queued, peak_live;
+  int64_t steps;                 /* batched LM iterations run */
+  size_t device_bytes_in_use, device_bytes_peak;
+} gba_server_stats;
+gba_status gba_server_get_stats(gba_handle *h, gba_server_stats *st);
+
+/* Estimated device footprint of one problem in bytes (the admission rule). */
+size_t gba_estimate_footprint(int32_t num_cameras, int32_t num_points, int32_t num_observations,
+                              int32_t precision);
+
+/* ---- kernel-level entry points (parity tests, profiling) --------------- */
+/* Evaluates residuals and Jacobians on the GPU at p->parameters, in the
+ * original observation order: residuals[2*i+k] and jacobians[24*i + 12*k + j]
+ * (row k = u,v; columns 0..8 camera, 9..11 point), as
+ * ceres::AutoDiffCostFunction<SnavelyReprojectionError,2,9,3>
+ * (utils/camera/SnavelyReprojectionError.h:89-92) would produce before the
+ * loss.  cost = 0.5 * sum rho(|r_i|^2) with the handle's loss.  Either
+ * output pointer may be NULL. */
+gba_status gba_evaluate(gba_handle *h, const gba_problem_view *p, double *residuals,
+                        double *jacobians, double *cost);
+
+/* One LM linear solve at p->parameters with trust radius `radius` and the
+ * Jacobi scaling of that point: writes the parameter update delta
+ * (9*nc+3*np, in parameter units) that Ceres' LevenbergMarquardtStrategy +
+ * Schur solver would produce, and the model cost change.  pcg_iterations may
+ * be NULL. */
+gba_status gba_compute_step(gba_handle *h, const gba_problem_view *p, double radius,
+                            double *delta, double *model_cost_change, int32_t *pcg_iterations);
+
+/* Re-runs the problem (or batch) last solved on this handle `repeats` times
+ * from its uploaded initial point, entirely on the device: no host prep and
+ * no transfers, results stay in device memory.  Asynchronous on the handle's
+ * stream (gba_options.stream when given).  For benchmarks with inputs
+ * resident in HBM; no counterpart in the reference. */
+gba_status gba_solve_resident(gba_handle *h, int32_t repeats);
+/* Waits for all work queued on the handle's stream. */
+gba_status gba_synchronize(gba_handle *h);
+
+/* Per-kernel device times of the last gba_solve / gba_batch_solve when
+ * profiling is on: kernel names, launches and total milliseconds. */
+gba_status gba_set_profiling(gba_handle *h, int32_t on);
+int32_t gba_profile_count(const gba_handle *h);
+gba_status gba_profile_entry(const gba_handle *h, int32_t i, const char **name,
+                             int64_t *launches, double *total_ms, double *bytes);
+
+/* ---- BALProblem I/O and preparation (host only, no GPU needed) --------- */
+/* Header of a BAL text file (BALProblem.cpp:87-89). */
+gba_status gba_bal_read_header(const char *path, int32_t *nc, int32_t *np, int32_t *no);
+/* Reads the body into caller-allocated arrays sized from the header
+ * (BALProblem.cpp:78-114). */
+gba_status gba_bal_read(const char *path, const gba_problem_view *out);
+/* Writes a BAL text file as BALProblem::WriteToFile (BALProblem.cpp:141-183). */
+gba_status gba_bal_write(const char *path, const gba_problem_view *p);
+/* Writes camera centres + points as BALProblem::WriteToPLYFile (BALProblem.cpp:185-228). */
+gba_status gba_bal_write_ply(const char *path, const gba_problem_view *p);
+/* BALProblem::Normalize (BALProblem.cpp:263-303). */
+gba_status gba_bal_normalize(const gba_problem_view *p);
+/* BALProblem::Perturb (BALProblem.cpp:305-336).  seed == 0 draws from the C
+ * library's rand() exactly as the reference does; otherwise a private
+ * generator seeded with `seed` is used. */
+gba_status gba_bal_perturb(const gba_problem_view *p, double rotation_sigma,
+                           double translation_sigma, double point_sigma, uint64_t seed);
+/* Angle-axis <-> quaternion (utils/geometry/rotation.h:73-131), for the
+ * BALProblem use_quaternions layout (BALProblem.cpp:117-138). */
+void gba_angle_axis_to_quaternion(const double *angle_axis, double *quaternion);
+void gba_quaternion_to_angle_axis(const double *quaternion, double *angle_axis);
+/* Rodrigues rotation R(w)*pt with the reference's small-angle branch
+ * (utils/geometry/rotation.h:133-199). */
+void gba_angle_axis_rotate_point(const double *angle_axis, const double *pt, double *result);
+
+/* ---- synthetic problems (seeded; host only) ---------------------------- */
+/* Problem families of the benchmark configurations:
+ *   GBA_SYNTH_RING     16-camera ring, uniform points, uniform 4..10 views;
+ *   GBA_SYNTH_WALK     random-walk trajectory, box of points, geometric views;
+ *   GBA_SYNTH_LOOPS    several random-walk loops with coincident starts, Zipf views;
+ *   GBA_SYNTH_WINDOW   short random-walk segment (local-BA window), uniform views. */
+typedef enum gba_synth_layout {
+  GBA_SYNTH_RING = 0,
+  GBA_SYNTH_WALK = 1,
+  GBA_SYNTH_LOOPS = 2,
+  GBA_SYNTH_WINDOW = 3
+} gba_synth_layout;
+
+typedef struct gba_synth_spec {
+  int32_t layout;           /* gba_synth_layout                         */
+  int32_t num_cameras;
+  int32_t num_points;
+  int32_t min_views, max_views;
+  int32_t view_distribution; /* 0 uniform, 1 geometric tail, 2 Zipf     */
+  double view_param;         /* p of the geometric tail / s of Zipf     */
+  double focal;              /* 500                                     */
+  double k1_range, k2_range; /* 0.05, 0.005                             */
+  double pixel_noise;        /* 0.5 px                                  */
+  double rotation_noise;     /* 0.01 rad                                */
+  double translation_noise;  /* 0.1                                     */
+  double point_noise;        /* 0.1                                     */
+  double focal_noise;        /* 0.01 (relative)                         */
+  uint64_t seed;
+} gba_synth_spec;
+
+/* Fills `spec` for benchmark configuration 0, 1 or 2 (single problems) or,
+ * for config 3, problem `index` of the 1,024-window batch, and for config 4
+ * request `index` of the serving stream. */
+gba_status gba_synth_preset(int32_t config, int32_t index, uint64_t seed, gba_synth_spec *spec);
+/* Sizes of the problem `spec` generates. */
+gba_status gba_synth_size(const gba_synth_spec *spec, int32_t *nc, int32_t *np, int32_t *no);
+/* Generates it into caller-allocated arrays: observations are projections of
+ * the true scene plus pixel noise; parameters hold the perturbed initial
+ * guess; `truth` (may be NULL) receives the true parameters. */
+gba_status gba_synth_generate(const gba_synth_spec *spec, const gba_problem_view *out,
+                              double *truth);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBA_H_ */

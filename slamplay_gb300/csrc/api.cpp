@@ -1,0 +1,240 @@
+// api.cpp — the extern "C" surface of libgba (declared in include/gba.h).
+#include <cstring>
+#include <memory>
+#include <new>
+#include <string>
+
+#include "engine.h"
+#include "gba.h"
+#include "server.h"
+
+struct gba_handle {
+  std::unique_ptr<gba::Engine> engine;
+  std::unique_ptr<gba::Server> server;
+  std::string last_error;
+};
+
+namespace {
+thread_local std::string g_create_error;
+
+gba_status fail(gba_handle *h, gba_status st, const std::string &msg) {
+  if (h) h->last_error = msg;
+  return st;
+}
+}  // namespace
+
+const char *gba_io_last_error(void);
+
+extern "C" {
+
+void gba_options_init(gba_options *o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof *o);
+  o->abi_version = GBA_ABI_VERSION;
+  o->max_num_iterations = 50;
+  o->function_tolerance = 1e-6;
+  o->gradient_tolerance = 1e-10;
+  o->parameter_tolerance = 1e-8;
+  o->initial_trust_region_radius = 1e4;
+  o->max_trust_region_radius = 1e16;
+  o->min_trust_region_radius = 1e-32;
+  o->min_relative_decrease = 1e-3;
+  o->min_lm_diagonal = 1e-6;
+  o->max_lm_diagonal = 1e32;
+  o->max_num_consecutive_invalid_steps = 5;
+  o->jacobi_scaling = 1;
+  o->loss = GBA_LOSS_TRIVIAL;
+  o->loss_scale = 1.0;
+  o->precision = GBA_PRECISION_FP64;
+  o->pcg_criterion = GBA_PCG_RESIDUAL;
+  o->max_linear_solver_iterations = 500;
+  o->min_linear_solver_iterations = 0;
+  o->pcg_tolerance = 1e-10;
+  o->eta = 0.1;
+  o->minimizer_progress_to_stdout = 0;
+  o->device = 0;
+  o->stream = nullptr;
+  o->chunk_observations = 0;
+  o->reorder_points = 1;
+  o->use_graphs = 1;
+}
+
+const char *gba_version(void) { return "gba 1 sm_103a"; }
+
+gba_status gba_create(const gba_options *o, gba_handle **out) {
+  if (!out) return GBA_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  gba_options opt;
+  if (o) {
+    opt = *o;
+    if (opt.abi_version != GBA_ABI_VERSION) {
+      g_create_error = "gba_options.abi_version mismatch (call gba_options_init)";
+      return GBA_ERR_INVALID_ARGUMENT;
+    }
+  } else {
+    gba_options_init(&opt);
+  }
+  if (opt.max_num_iterations < 0 || opt.max_linear_solver_iterations < 0 || opt.loss < 0 || opt.loss > 2 ||
+      opt.precision < 0 || opt.precision > 1 || !(opt.initial_trust_region_radius > 0) ||
+      !(opt.loss_scale > 0) || opt.max_num_consecutive_invalid_steps < 1) {
+    g_create_error = "invalid solver options";
+    return GBA_ERR_INVALID_ARGUMENT;
+  }
+  gba_handle *h = new (std::nothrow) gba_handle();
+  if (!h) return GBA_ERR_OUT_OF_MEMORY;
+  h->engine.reset(new gba::Engine(opt));
+  std::string err;
+  const gba_status st = h->engine->init(&err);
+  if (st != GBA_OK) {
+    g_create_error = err;
+    delete h;
+    return st;
+  }
+  *out = h;
+  return GBA_OK;
+}
+
+void gba_destroy(gba_handle *h) {
+  if (!h) return;
+  if (h->server) h->server->stop();
+  delete h;
+}
+
+const char *gba_last_error(const gba_handle *h) {
+  if (!h) return g_create_error.c_str();
+  return h->last_error.c_str();
+}
+
+gba_status gba_solve(gba_handle *h, const gba_problem_view *p, gba_summary *s) {
+  if (!h) return GBA_ERR_INVALID_ARGUMENT;
+  if (!p) return fail(h, GBA_ERR_INVALID_ARGUMENT, "null problem");
+  if (h->server && h->server->running()) return fail(h, GBA_ERR_INVALID_ARGUMENT, "handle is serving");
+  std::string err;
+  const gba_status st = h->engine->solve(p, 1, s, &err);
+  if (st != GBA_OK) return fail(h, st, err);
+  return GBA_OK;
+}
+
+gba_status gba_batch_solve(gba_handle *h, const gba_problem_view *problems, int32_t n, gba_summary *summaries) {
+  if (!h) return GBA_ERR_INVALID_ARGUMENT;
+  if (!problems || n <= 0) return fail(h, GBA_ERR_INVALID_ARGUMENT, "empty batch");
+  if (h->server && h->server->running()) return fail(h, GBA_ERR_INVALID_ARGUMENT, "handle is serving");
+  std::string err;
+  const gba_status st = h->engine->solve(problems, n, summaries, &err);
+  if (st != GBA_OK) return fail(h, st, err);
+  return GBA_OK;
+}
+
+gba_status gba_evaluate(gba_handle *h, const gba_problem_view *p, double *residuals, double *jacobians,
+                        double *cost) {
+  if (!h) return GBA_ERR_INVALID_ARGUMENT;
+  if (!p) return fail(h, GBA_ERR_INVALID_ARGUMENT, "null problem");
+  std::string err;
+  const gba_status st = h->engine->evaluate(p, residuals, jacobians, cost, &err);
+  if (st != GBA_OK) return fail(h, st, err);
+  return GBA_OK;
+}
+
+gba_status gba_compute_step(gba_handle *h, const gba_problem_view *p, double radius, double *delta,
+                            double *model_cost_change, int32_t *pcg_iterations) {
+  if (!h) return GBA_ERR_INVALID_ARGUMENT;
+  if (!p || !delta || !(radius > 0)) return fail(h, GBA_ERR_INVALID_ARGUMENT, "invalid step arguments");
+  std::string err;
+  int it = 0;
+  const gba_status st = h->engine->compute_step(p, radius, delta, model_cost_change, &it, &err);
+  if (pcg_iterations) *pcg_iterations = it;
+  if (st != GBA_OK) return fail(h, st, err);
+  return GBA_OK;
+}
+
+gba_status gba_solve_resident(gba_handle *h, int32_t repeats) {
+  if (!h || repeats < 0) return GBA_ERR_INVALID_ARGUMENT;
+  std::string err;
+  for (int32_t r = 0; r < repeats; ++r) {
+    const gba_status st = h->engine->rerun(&err);
+    if (st != GBA_OK) return fail(h, st, err);
+  }
+  return GBA_OK;
+}
+
+gba_status gba_synchronize(gba_handle *h) {
+  if (!h) return GBA_ERR_INVALID_ARGUMENT;
+  const cudaError_t e = cudaStreamSynchronize(h->engine->stream());
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(h, GBA_ERR_CUDA, cudaGetErrorString(e));
+  }
+  return GBA_OK;
+}
+
+gba_status gba_set_profiling(gba_handle *h, int32_t on) {
+  if (!h) return GBA_ERR_INVALID_ARGUMENT;
+  h->engine->set_profiling(on != 0);
+  return GBA_OK;
+}
+
+int32_t gba_profile_count(const gba_handle *h) { return h ? (int32_t)h->engine->profile().size() : 0; }
+
+gba_status gba_profile_entry(const gba_handle *h, int32_t i, const char **name, int64_t *launches,
+                             double *total_ms, double *bytes) {
+  if (!h || i < 0 || i >= (int32_t)h->engine->profile().size()) return GBA_ERR_INVALID_ARGUMENT;
+  const gba::ProfileEntry &e = h->engine->profile()[i];
+  if (name) *name = e.name.c_str();
+  if (launches) *launches = e.launches;
+  if (total_ms) *total_ms = e.total_ms;
+  if (bytes) *bytes = e.bytes;
+  return GBA_OK;
+}
+
+size_t gba_estimate_footprint(int32_t nc, int32_t np, int32_t no, int32_t precision) {
+  return gba::Server::estimate_footprint(nc, np, no, precision == GBA_PRECISION_MIXED);
+}
+
+gba_status gba_server_start(gba_handle *h, size_t budget, int32_t max_live, int32_t max_queue) {
+  if (!h) return GBA_ERR_INVALID_ARGUMENT;
+  if (h->server && h->server->running()) return fail(h, GBA_ERR_INVALID_ARGUMENT, "server already running");
+  h->server.reset(new gba::Server(h->engine->options()));
+  std::string err;
+  const gba_status st = h->server->start(budget, max_live, max_queue, &err);
+  if (st != GBA_OK) {
+    h->server.reset();
+    return fail(h, st, err);
+  }
+  return GBA_OK;
+}
+
+gba_status gba_submit(gba_handle *h, const gba_problem_view *p, uint64_t *ticket) {
+  if (!h || !ticket) return GBA_ERR_INVALID_ARGUMENT;
+  if (!h->server || !h->server->running()) return fail(h, GBA_ERR_INVALID_ARGUMENT, "server not started");
+  std::string err;
+  const gba_status st = h->server->submit(p, ticket, &err);
+  if (st != GBA_OK) return fail(h, st, err);
+  return GBA_OK;
+}
+
+gba_status gba_poll(gba_handle *h, uint64_t ticket, gba_summary *s, int32_t *done) {
+  if (!h || !done) return GBA_ERR_INVALID_ARGUMENT;
+  if (!h->server) return fail(h, GBA_ERR_INVALID_ARGUMENT, "server not started");
+  std::string err;
+  const gba_status st = h->server->poll(ticket, s, done, &err);
+  if (st != GBA_OK) return fail(h, st, err);
+  return GBA_OK;
+}
+
+gba_status gba_server_stop(gba_handle *h) {
+  if (!h) return GBA_ERR_INVALID_ARGUMENT;
+  if (!h->server) return GBA_OK;
+  std::string err;
+  const gba_status st = h->server->drain_and_stop(&err);
+  if (st != GBA_OK) return fail(h, st, err);
+  return GBA_OK;
+}
+
+gba_status gba_server_get_stats(gba_handle *h, gba_server_stats *st) {
+  if (!h || !st) return GBA_ERR_INVALID_ARGUMENT;
+  std::memset(st, 0, sizeof *st);
+  if (h->server) h->server->stats(st);
+  return GBA_OK;
+}
+
+}  // extern "C"

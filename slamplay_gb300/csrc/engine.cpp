@@ -1,0 +1,780 @@
+// engine.cpp — device workspace, uploads, the LM loop as one CUDA graph
+// (conditional WHILE nodes for the LM loop and the nested PCG loop, set from
+// the kernels themselves), a host-driven variant with per-kernel event
+// timing, and result download.
+#include "engine.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+
+#include "kernels.h"
+
+namespace gba {
+
+cudaError_t probe_kernel_image();
+void launch_cost_only(const DeviceBatch &b, cudaStream_t s);
+
+namespace {
+
+inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+struct Carver {
+  char *base;
+  size_t off;
+  template <typename T>
+  T *take(size_t n) {
+    off = align_up(off, 256);
+    T *p = base ? reinterpret_cast<T *>(base + off) : nullptr;
+    off += n * sizeof(T);
+    return p;
+  }
+};
+
+enum ProfSlot {
+  PF_EVAL = 0,
+  PF_POST,
+  PF_POINT,
+  PF_SCHUR,
+  PF_MATVEC,
+  PF_REDUCE,
+  PF_UPDATE,
+  PF_BACKSUB,
+  PF_CANDIDATE,
+  PF_DECIDE,
+  PF_TABLE,
+  PF_SETUP_MISC,
+  PF_COUNT
+};
+const char *kProfNames[PF_COUNT] = {"eval_jacobian",  "post_eval",    "point_prepare", "camera_schur",
+                                    "schur_matvec",   "camera_reduce", "pcg_update",   "back_substitute",
+                                    "candidate_cost", "decide",        "camera_table", "setup_misc"};
+
+double now_s() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+}  // namespace
+
+Engine::Engine(const gba_options &o) : o_(o) {
+  mixed_ = o.precision == GBA_PRECISION_MIXED;
+  device_ = o.device;
+  trace_cap_ = std::max(1, o.max_num_iterations + 1);
+  profile_.resize(PF_COUNT);
+  for (int i = 0; i < PF_COUNT; ++i) profile_[i].name = kProfNames[i];
+}
+
+Engine::~Engine() {
+  cudaSetDevice(device_);
+  destroy_graph();
+  if (d_arena_) cudaFree(d_arena_);
+  if (h_stage_) cudaFreeHost(h_stage_);
+  for (cudaStream_t &s : cap_)
+    if (s) cudaStreamDestroy(s);
+  if (own_stream_ && stream_) cudaStreamDestroy(stream_);
+  for (cudaEvent_t e : {ev_start_, ev_stop_, pev_[0], pev_[1]})
+    if (e) cudaEventDestroy(e);
+}
+
+gba_status Engine::check(cudaError_t e, const char *what, std::string *err) {
+  if (e == cudaSuccess) return GBA_OK;
+  *err = std::string(what) + ": " + cudaGetErrorString(e);
+  cudaGetLastError();
+  if (e == cudaErrorMemoryAllocation) return GBA_ERR_OUT_OF_MEMORY;
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver || e == cudaErrorNoKernelImageForDevice ||
+      e == cudaErrorInvalidDevice)
+    return GBA_ERR_NO_DEVICE;
+  return GBA_ERR_CUDA;
+}
+
+gba_status Engine::init(std::string *err) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    *err = "no CUDA device available";
+    return GBA_ERR_NO_DEVICE;
+  }
+  if (device_ < 0 || device_ >= n) {
+    *err = "device ordinal out of range";
+    return GBA_ERR_INVALID_ARGUMENT;
+  }
+  gba_status st;
+  if ((st = check(cudaSetDevice(device_), "cudaSetDevice", err)) != GBA_OK) return st;
+  if ((st = check(probe_kernel_image(), "loading the sm_103a kernels", err)) != GBA_OK) return st;
+  if (o_.stream) {
+    stream_ = static_cast<cudaStream_t>(o_.stream);
+  } else {
+    if ((st = check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "stream", err)) != GBA_OK) return st;
+    own_stream_ = true;
+  }
+  for (cudaStream_t &s : cap_)
+    if ((st = check(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "stream", err)) != GBA_OK) return st;
+  for (cudaEvent_t *e : {&ev_start_, &ev_stop_, &pev_[0], &pev_[1]})
+    if ((st = check(cudaEventCreate(e), "event", err)) != GBA_OK) return st;
+  return GBA_OK;
+}
+
+// Arena order: [upload | download | work].  The pinned host staging buffer
+// mirrors [upload | download] at the same offsets, so one H2D copy uploads
+// a whole batch and one D2H copy returns its results.
+size_t Engine::layout(const HostBatch &hb, char *base, DeviceBatch *db, size_t *upload_bytes,
+                      size_t *download_off, size_t *download_bytes) {
+  Carver cv{base, 0};
+  DeviceBatch &b = *db;
+  const size_t P = hb.P, nc = hb.nc, np = hb.np, no = hb.no, nch = hb.nchunks, ns = hb.nseg;
+  const size_t nb = hb.cam_blocks;
+  b.num_problems = hb.P;
+  b.nc = hb.nc;
+  b.np = hb.np;
+  b.no = hb.no;
+  b.nchunks = hb.nchunks;
+  b.nseg = hb.nseg;
+  b.cam_blocks = hb.cam_blocks;
+  // upload
+  b.prob = cv.take<ProblemInfo>(P);
+  b.chunk = cv.take<ChunkInfo>(nch);
+  b.obs_cam = cv.take<int32_t>(no);
+  b.obs_pt = cv.take<int32_t>(no);
+  b.obs_uv = cv.take<double2>(no);
+  b.obs_seg = cv.take<uint16_t>(no);
+  b.obs_slot = cv.take<uint16_t>(no);
+  b.pt_obs_begin = cv.take<int32_t>(np + 1);
+  b.pt_problem = cv.take<int32_t>(np);
+  b.cam_problem = cv.take<int32_t>(nc);
+  b.pt_used = cv.take<uint8_t>(np);
+  b.cam_used = cv.take<uint8_t>(nc);
+  b.seg_pos = cv.take<uint16_t>(ns);
+  b.seg_cam = cv.take<int32_t>(ns);
+  b.cam_seg_begin = cv.take<int32_t>(nc + 1);
+  b.cam_seg_list = cv.take<int32_t>(ns);
+  b.cam_obs_begin = cv.take<int32_t>(nc + 1);
+  b.cam_obs_list = cv.take<int32_t>(no);
+  b.camblk = cv.take<int4>(nb);
+  b.cam_init = cv.take<double>(9 * nc);
+  b.pt_init = cv.take<double>(4 * np);
+  *upload_bytes = align_up(cv.off, 256);
+  // download
+  cv.off = *upload_bytes;
+  *download_off = cv.off;
+  double *out_cam = cv.take<double>(9 * nc);
+  double *out_pt = cv.take<double>(4 * np);
+  (void)out_cam;
+  (void)out_pt;
+  b.lm = cv.take<LMState>(P);
+  b.trace_cap = trace_cap_;
+  b.trace_cost = cv.take<double>(P * trace_cap_);
+  b.trace_radius = cv.take<double>(P * trace_cap_);
+  b.trace_pcg = cv.take<int32_t>(P * trace_cap_);
+  b.trace_succ = cv.take<int32_t>(P * trace_cap_);
+  b.status = cv.take<int32_t>(8);
+  *download_bytes = align_up(cv.off, 256) - *download_off;
+  cv.off = *download_off + *download_bytes;
+  // work
+  const size_t rs = mixed_ ? sizeof(float) : sizeof(double);
+  b.cam_param[0] = cv.take<double>(9 * nc);
+  b.cam_param[1] = cv.take<double>(9 * nc);
+  b.pt_param[0] = cv.take<double>(4 * np);
+  b.pt_param[1] = cv.take<double>(4 * np);
+  b.cam_table = cv.take<double>(kCamTable * nc);
+  b.jac = cv.take<char>(13 * no * 2 * rs);
+  b.pt_C = cv.take<double>(6 * np);
+  b.pt_g = cv.take<double>(3 * np);
+  b.pt_scale = cv.take<double>(3 * np);
+  b.pt_t = cv.take<double>(3 * np);
+  b.pt_Cinv = cv.take<char>(6 * np * rs);
+  b.pt_Cinv64 = cv.take<double>(6 * np);
+  b.pt_colnorm = cv.take<double>(3 * np);
+  b.cam_B = cv.take<double>(45 * nc);
+  b.cam_g = cv.take<double>(9 * nc);
+  b.cam_scale = cv.take<double>(9 * nc);
+  b.cam_Minv = cv.take<double>(81 * nc);
+  b.cam_D2 = cv.take<double>(9 * nc);
+  b.pcg_x = cv.take<double>(9 * nc);
+  b.pcg_r = cv.take<double>(9 * nc);
+  b.pcg_z = cv.take<double>(9 * nc);
+  b.pcg_p = cv.take<double>(9 * nc);
+  b.pcg_q = cv.take<double>(9 * nc);
+  b.pcg_v = cv.take<double>(9 * nc);
+  b.cam_colnorm = cv.take<double>(9 * nc);
+  b.seg_partial = cv.take<double>(9 * ns);
+  b.chunk_scal = cv.take<double>(kChunkScal * nch);
+  b.cam_scal = cv.take<double>(kCamScal * nc);
+  b.blk_scal = cv.take<double>(kBlkScal * nb);
+  b.prob_counter = cv.take<uint32_t>(4 * P);
+  b.global_counter = cv.take<uint32_t>(8);
+  b.opt.function_tolerance = o_.function_tolerance;
+  b.opt.gradient_tolerance = o_.gradient_tolerance;
+  b.opt.parameter_tolerance = o_.parameter_tolerance;
+  b.opt.initial_radius = o_.initial_trust_region_radius;
+  b.opt.max_radius = o_.max_trust_region_radius;
+  b.opt.min_radius = o_.min_trust_region_radius;
+  b.opt.min_relative_decrease = o_.min_relative_decrease;
+  b.opt.min_diagonal = o_.min_lm_diagonal;
+  b.opt.max_diagonal = o_.max_lm_diagonal;
+  b.opt.loss_scale = o_.loss_scale;
+  b.opt.pcg_tolerance = o_.pcg_tolerance;
+  b.opt.eta = o_.eta;
+  b.opt.max_iterations = o_.max_num_iterations;
+  b.opt.max_invalid_steps = o_.max_num_consecutive_invalid_steps;
+  b.opt.jacobi_scaling = o_.jacobi_scaling;
+  b.opt.loss = o_.loss;
+  b.opt.pcg_criterion = o_.pcg_criterion;
+  b.opt.max_pcg_iterations = o_.max_linear_solver_iterations;
+  b.opt.min_pcg_iterations = o_.min_linear_solver_iterations;
+  b.opt.mixed = mixed_ ? 1 : 0;
+  b.lm_cond = 0;
+  b.pcg_cond = 0;
+  b.use_cond = 0;
+  return align_up(cv.off, 256);
+}
+
+gba_status Engine::ensure_capacity(size_t dev_bytes, size_t host_bytes, std::string *err) {
+  gba_status st;
+  if (dev_bytes > d_cap_) {
+    destroy_graph();
+    if (d_arena_) cudaFree(d_arena_);
+    d_arena_ = nullptr;
+    d_cap_ = 0;
+    const size_t want = align_up(dev_bytes + dev_bytes / 8, 1 << 20);
+    if ((st = check(cudaMalloc(&d_arena_, want), "device workspace", err)) != GBA_OK) {
+      d_arena_ = nullptr;
+      return st;
+    }
+    d_cap_ = want;
+  }
+  if (host_bytes > h_cap_) {
+    if (h_stage_) cudaFreeHost(h_stage_);
+    h_stage_ = nullptr;
+    h_cap_ = 0;
+    const size_t want = align_up(host_bytes + host_bytes / 8, 1 << 20);
+    if ((st = check(cudaMallocHost(&h_stage_, want), "pinned staging", err)) != GBA_OK) {
+      h_stage_ = nullptr;
+      return st;
+    }
+    h_cap_ = want;
+  }
+  return GBA_OK;
+}
+
+template <typename T>
+static void put(T *dst, const std::vector<T> &src) {
+  if (!src.empty()) std::memcpy(dst, src.data(), src.size() * sizeof(T));
+}
+
+gba_status Engine::upload(const HostBatch &hb, std::string *err) {
+  gba_status st;
+  if ((st = check(cudaSetDevice(device_), "cudaSetDevice", err)) != GBA_OK) return st;
+  DeviceBatch probe{};
+  size_t ub, doff, dbytes;
+  const size_t total = layout(hb, nullptr, &probe, &ub, &doff, &dbytes);
+  if ((st = ensure_capacity(total, doff + dbytes, err)) != GBA_OK) return st;
+  upload_bytes_ = ub;
+  download_off_ = doff;
+  download_bytes_ = dbytes;
+  layout(hb, d_arena_, &db_, &ub, &doff, &dbytes);
+  DeviceBatch hdb{};
+  layout(hb, h_stage_, &hdb, &ub, &doff, &dbytes);
+  put(const_cast<ProblemInfo *>(hdb.prob), hb.prob);
+  put(const_cast<ChunkInfo *>(hdb.chunk), hb.chunk);
+  put(const_cast<int32_t *>(hdb.obs_cam), hb.obs_cam);
+  put(const_cast<int32_t *>(hdb.obs_pt), hb.obs_pt);
+  if (!hb.obs_uv.empty()) std::memcpy(const_cast<double2 *>(hdb.obs_uv), hb.obs_uv.data(), hb.obs_uv.size() * sizeof(double));
+  put(const_cast<uint16_t *>(hdb.obs_seg), hb.obs_seg);
+  put(const_cast<uint16_t *>(hdb.obs_slot), hb.obs_slot);
+  put(const_cast<int32_t *>(hdb.pt_obs_begin), hb.pt_obs_begin);
+  put(const_cast<int32_t *>(hdb.pt_problem), hb.pt_problem);
+  put(const_cast<int32_t *>(hdb.cam_problem), hb.cam_problem);
+  put(const_cast<uint8_t *>(hdb.pt_used), hb.pt_used);
+  put(const_cast<uint8_t *>(hdb.cam_used), hb.cam_used);
+  put(const_cast<uint16_t *>(hdb.seg_pos), hb.seg_pos);
+  put(const_cast<int32_t *>(hdb.seg_cam), hb.seg_cam);
+  put(const_cast<int32_t *>(hdb.cam_seg_begin), hb.cam_seg_begin);
+  put(const_cast<int32_t *>(hdb.cam_seg_list), hb.cam_seg_list);
+  put(const_cast<int32_t *>(hdb.cam_obs_begin), hb.cam_obs_begin);
+  put(const_cast<int32_t *>(hdb.cam_obs_list), hb.cam_obs_list);
+  put(const_cast<int4 *>(hdb.camblk), hb.camblk);
+  put(const_cast<double *>(hdb.cam_init), hb.cam_param);
+  put(const_cast<double *>(hdb.pt_init), hb.pt_param);
+  if ((st = check(cudaMemcpyAsync(d_arena_, h_stage_, upload_bytes_, cudaMemcpyHostToDevice, stream_),
+                  "upload", err)) != GBA_OK)
+    return st;
+  // current batch shape + pointers + options = graph key
+  DeviceBatch k = db_;
+  cur_key_.assign(reinterpret_cast<const char *>(&k), reinterpret_cast<const char *>(&k) + sizeof k);
+  return GBA_OK;
+}
+
+void Engine::destroy_graph() {
+  if (exec_) cudaGraphExecDestroy(exec_);
+  if (graph_) cudaGraphDestroy(graph_);
+  exec_ = nullptr;
+  graph_ = nullptr;
+  graph_key_.clear();
+}
+
+void Engine::prof_begin(cudaStream_t s) {
+  if (profiling_) cudaEventRecord(pev_[0], s);
+}
+void Engine::prof_end(cudaStream_t s, int entry, double bytes) {
+  if (!profiling_) return;
+  cudaEventRecord(pev_[1], s);
+  cudaEventSynchronize(pev_[1]);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, pev_[0], pev_[1]);
+  profile_[entry].launches += 1;
+  profile_[entry].total_ms += ms;
+  profile_[entry].bytes += bytes;
+}
+
+// Algorithmic bytes of one launch of the main kernels (what the kernel
+// must read and write at least once; cached gathers counted once per
+// distinct item).  Used for the achieved-bandwidth figures.
+static double bytes_matvec(const DeviceBatch &b) {
+  const double rs = b.opt.mixed ? 4.0 : 8.0;
+  return (double)b.no * (24.0 * rs + 8.0) + (double)b.np * (4.0 + 6.0 * rs) +
+         (double)b.nseg * (6.0 + 72.0 + 144.0) + (double)b.nchunks * 32.0;
+}
+static double bytes_eval(const DeviceBatch &b) {
+  const double rs = b.opt.mixed ? 4.0 : 8.0;
+  // K1: uv, cam, pt in; 13 pairs out; points in/out; K1c: list, 10 pairs in
+  return (double)b.no * (24.0 + 26.0 * rs) + (double)b.np * (32.0 + 72.0 + 4.0 + 24.0) +
+         (double)b.nc * (kCamTable * 8.0) + (double)b.no * (4.0 + 20.0 * rs) + (double)b.nc * (54.0 * 8.0);
+}
+static double bytes_schur(const DeviceBatch &b) {
+  const double rs = b.opt.mixed ? 4.0 : 8.0;
+  return (double)b.no * (4.0 + 4.0 + 24.0 * rs) + (double)b.np * (6.0 * rs + 24.0) +
+         (double)b.nc * (45.0 + 9.0 + 81.0 + 9.0 * 6.0) * 8.0;
+}
+static double bytes_backsub(const DeviceBatch &b) {
+  const double rs = b.opt.mixed ? 4.0 : 8.0;
+  return (double)b.no * (26.0 * rs + 8.0) + (double)b.np * (24.0 + 48.0 + 24.0 + 64.0);
+}
+static double bytes_cost(const DeviceBatch &b) {
+  return (double)b.no * 24.0 + (double)b.np * 32.0 + (double)b.nc * 15.0 * 8.0;
+}
+
+void Engine::enqueue_setup(cudaStream_t s) {
+  cudaMemsetAsync(db_.prob_counter, 0, 4 * sizeof(uint32_t) * (size_t)db_.num_problems, s);
+  cudaMemsetAsync(db_.global_counter, 0, 8 * sizeof(uint32_t), s);
+  cudaMemsetAsync(db_.status, 0, 8 * sizeof(int32_t), s);
+  launch_sync_param_buffers(db_, s);
+  launch_init_state(db_, s);
+  launch_camera_table(db_, s);
+  launch_eval_jacobian(db_, mixed_, true, s);
+  launch_scale_init(db_, s);
+  launch_eval_jacobian(db_, mixed_, false, s);
+  launch_post_eval(db_, s);
+}
+
+void Engine::enqueue_lm_head(cudaStream_t s) {
+  prof_begin(s);
+  launch_point_prepare(db_, mixed_, s);
+  prof_end(s, PF_POINT, (double)db_.np * (48.0 + 24.0 + 48.0 + 24.0 + 48.0 + (mixed_ ? 24.0 : 48.0)));
+  prof_begin(s);
+  launch_camera_schur(db_, mixed_, s);
+  prof_end(s, PF_SCHUR, bytes_schur(db_));
+}
+
+void Engine::enqueue_lm_tail(cudaStream_t s) {
+  prof_begin(s);
+  launch_back_substitute(db_, mixed_, s);
+  prof_end(s, PF_BACKSUB, bytes_backsub(db_));
+  prof_begin(s);
+  launch_candidate_cost(db_, s);
+  prof_end(s, PF_CANDIDATE, bytes_cost(db_));
+  prof_begin(s);
+  launch_decide(db_, s);
+  prof_end(s, PF_DECIDE, 0.0);
+  prof_begin(s);
+  launch_camera_table(db_, s);
+  prof_end(s, PF_TABLE, (double)db_.nc * (72.0 + kCamTable * 8.0));
+  prof_begin(s);
+  launch_eval_jacobian(db_, mixed_, false, s);
+  prof_end(s, PF_EVAL, bytes_eval(db_));
+  prof_begin(s);
+  launch_post_eval(db_, s);
+  prof_end(s, PF_POST, 0.0);
+}
+
+gba_status Engine::build_graph(std::string *err) {
+  destroy_graph();
+  gba_status st;
+  cudaGraphConditionalHandle lmh = 0, pcgh = 0;
+  if ((st = check(cudaGraphCreate(&graph_, 0), "cudaGraphCreate", err)) != GBA_OK) return st;
+  if ((st = check(cudaGraphConditionalHandleCreate(&lmh, graph_, 1, cudaGraphCondAssignDefault),
+                  "conditional handle", err)) != GBA_OK)
+    return st;
+  db_.use_cond = 1;
+  db_.lm_cond = lmh;
+  db_.pcg_cond = 0;
+  const bool prof = profiling_;
+  profiling_ = false;
+  auto fail = [&](cudaError_t e, const char *what) {
+    profiling_ = prof;
+    cudaStreamCaptureStatus cs;
+    for (cudaStream_t s : {cap_[1], cap_[0], stream_}) {
+      if (cudaStreamIsCapturing(s, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) {
+        cudaGraph_t g = nullptr;
+        cudaStreamEndCapture(s, &g);
+        if (g && g != graph_) cudaGraphDestroy(g);
+      }
+    }
+    cudaGetLastError();
+    const gba_status r = check(e, what, err);
+    destroy_graph();
+    db_.use_cond = 0;
+    return r;
+  };
+  cudaError_t e = cudaStreamBeginCaptureToGraph(stream_, graph_, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return fail(e, "capture setup");
+  enqueue_setup(stream_);
+  // LM while node
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t cg = nullptr;
+  const cudaGraphNode_t *deps = nullptr;
+  size_t ndeps = 0;
+  e = cudaStreamGetCaptureInfo(stream_, &cs, nullptr, &cg, &deps, nullptr, &ndeps);
+  if (e != cudaSuccess) return fail(e, "capture info");
+  cudaGraphNodeParams lp = {};
+  lp.type = cudaGraphNodeTypeConditional;
+  lp.conditional.handle = lmh;
+  lp.conditional.type = cudaGraphCondTypeWhile;
+  lp.conditional.size = 1;
+  cudaGraphNode_t lmnode;
+  e = cudaGraphAddNode(&lmnode, cg, deps, nullptr, ndeps, &lp);
+  if (e != cudaSuccess) return fail(e, "LM conditional node");
+  cudaGraph_t lmbody = lp.conditional.phGraph_out[0];
+  e = cudaStreamUpdateCaptureDependencies(stream_, &lmnode, nullptr, 1, cudaStreamSetCaptureDependencies);
+  if (e != cudaSuccess) return fail(e, "capture dependencies");
+  e = cudaGraphConditionalHandleCreate(&pcgh, lmbody, 1, cudaGraphCondAssignDefault);
+  if (e != cudaSuccess) return fail(e, "PCG conditional handle");
+  db_.pcg_cond = pcgh;
+  // LM body
+  e = cudaStreamBeginCaptureToGraph(cap_[0], lmbody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return fail(e, "capture LM body");
+  enqueue_lm_head(cap_[0]);
+  e = cudaStreamGetCaptureInfo(cap_[0], &cs, nullptr, &cg, &deps, nullptr, &ndeps);
+  if (e != cudaSuccess) return fail(e, "capture info (LM body)");
+  cudaGraphNodeParams pp = {};
+  pp.type = cudaGraphNodeTypeConditional;
+  pp.conditional.handle = pcgh;
+  pp.conditional.type = cudaGraphCondTypeWhile;
+  pp.conditional.size = 1;
+  cudaGraphNode_t pcgnode;
+  e = cudaGraphAddNode(&pcgnode, cg, deps, nullptr, ndeps, &pp);
+  if (e != cudaSuccess) return fail(e, "PCG conditional node");
+  cudaGraph_t pcgbody = pp.conditional.phGraph_out[0];
+  e = cudaStreamUpdateCaptureDependencies(cap_[0], &pcgnode, nullptr, 1, cudaStreamSetCaptureDependencies);
+  if (e != cudaSuccess) return fail(e, "capture dependencies (LM body)");
+  e = cudaStreamBeginCaptureToGraph(cap_[1], pcgbody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return fail(e, "capture PCG body");
+  launch_pcg_iteration(db_, mixed_, cap_[1]);
+  cudaGraph_t tmp = nullptr;
+  e = cudaStreamEndCapture(cap_[1], &tmp);
+  if (e != cudaSuccess) return fail(e, "end capture PCG body");
+  enqueue_lm_tail(cap_[0]);
+  e = cudaStreamEndCapture(cap_[0], &tmp);
+  if (e != cudaSuccess) return fail(e, "end capture LM body");
+  char *out = d_arena_ + download_off_;
+  launch_gather_results(db_, reinterpret_cast<double *>(out),
+                        reinterpret_cast<double *>(out + align_up(sizeof(double) * 9 * (size_t)db_.nc, 256)), stream_);
+  e = cudaStreamEndCapture(stream_, &tmp);
+  if (e != cudaSuccess) return fail(e, "end capture");
+  e = cudaGraphInstantiate(&exec_, graph_, 0);
+  if (e != cudaSuccess) return fail(e, "cudaGraphInstantiate");
+  profiling_ = prof;
+  graph_key_ = cur_key_;
+  return GBA_OK;
+}
+
+gba_status Engine::run_host_driven(std::string *err) {
+  gba_status st;
+  db_.use_cond = 0;
+  db_.lm_cond = 0;
+  db_.pcg_cond = 0;
+  int32_t *hstat = reinterpret_cast<int32_t *>(h_stage_ + (reinterpret_cast<char *>(db_.status) - d_arena_));
+  auto read_status = [&]() -> gba_status {
+    gba_status s2 = check(cudaMemcpyAsync(hstat, db_.status, 8 * sizeof(int32_t), cudaMemcpyDeviceToHost, stream_),
+                          "status read", err);
+    if (s2 != GBA_OK) return s2;
+    return check(cudaStreamSynchronize(stream_), "solver kernels", err);
+  };
+  prof_begin(stream_);
+  cudaMemsetAsync(db_.prob_counter, 0, 4 * sizeof(uint32_t) * (size_t)db_.num_problems, stream_);
+  cudaMemsetAsync(db_.global_counter, 0, 8 * sizeof(uint32_t), stream_);
+  cudaMemsetAsync(db_.status, 0, 8 * sizeof(int32_t), stream_);
+  launch_sync_param_buffers(db_, stream_);
+  launch_init_state(db_, stream_);
+  prof_end(stream_, PF_SETUP_MISC, 0.0);
+  prof_begin(stream_);
+  launch_camera_table(db_, stream_);
+  prof_end(stream_, PF_TABLE, (double)db_.nc * (72.0 + kCamTable * 8.0));
+  prof_begin(stream_);
+  launch_eval_jacobian(db_, mixed_, true, stream_);
+  launch_scale_init(db_, stream_);
+  prof_end(stream_, PF_SETUP_MISC, 0.0);
+  prof_begin(stream_);
+  launch_eval_jacobian(db_, mixed_, false, stream_);
+  prof_end(stream_, PF_EVAL, bytes_eval(db_));
+  prof_begin(stream_);
+  launch_post_eval(db_, stream_);
+  prof_end(stream_, PF_POST, 0.0);
+  if ((st = read_status()) != GBA_OK) return st;
+  int bodies = 0;
+  while (hstat[1] && hstat[0] == 0) {
+    if (++bodies > o_.max_num_iterations + 2) break;
+    enqueue_lm_head(stream_);
+    if ((st = read_status()) != GBA_OK) return st;
+    int pcg = 0;
+    while (hstat[2] && pcg <= o_.max_linear_solver_iterations) {
+      ++pcg;
+      prof_begin(stream_);
+      launch_schur_matvec(db_, mixed_, stream_);
+      prof_end(stream_, PF_MATVEC, bytes_matvec(db_));
+      prof_begin(stream_);
+      launch_camera_reduce(db_, stream_);
+      prof_end(stream_, PF_REDUCE, (double)db_.nseg * 72.0 + (double)db_.nc * (45.0 + 9.0 * 5.0) * 8.0);
+      prof_begin(stream_);
+      launch_pcg_update(db_, stream_);
+      prof_end(stream_, PF_UPDATE, (double)db_.nc * (81.0 + 9.0 * 8.0) * 8.0);
+      if ((st = read_status()) != GBA_OK) return st;
+    }
+    enqueue_lm_tail(stream_);
+    if ((st = read_status()) != GBA_OK) return st;
+  }
+  char *out = d_arena_ + download_off_;
+  launch_gather_results(db_, reinterpret_cast<double *>(out),
+                        reinterpret_cast<double *>(out + align_up(sizeof(double) * 9 * (size_t)db_.nc, 256)), stream_);
+  return check(cudaGetLastError(), "kernel launch", err);
+}
+
+gba_status Engine::rerun(std::string *err) {
+  if (!d_arena_ || cur_key_.empty()) {
+    *err = "no problem has been uploaded on this handle";
+    return GBA_ERR_INVALID_ARGUMENT;
+  }
+  return run_solve(err);
+}
+
+gba_status Engine::run_solve(std::string *err) {
+  gba_status st;
+  if ((st = check(cudaEventRecord(ev_start_, stream_), "event", err)) != GBA_OK) return st;
+  if (o_.use_graphs && !profiling_) {
+    if (!exec_ || graph_key_ != cur_key_) {
+      if ((st = build_graph(err)) != GBA_OK) return st;
+    }
+    if ((st = check(cudaGraphLaunch(exec_, stream_), "cudaGraphLaunch", err)) != GBA_OK) return st;
+  } else {
+    if ((st = run_host_driven(err)) != GBA_OK) return st;
+  }
+  return check(cudaEventRecord(ev_stop_, stream_), "event", err);
+}
+
+gba_status Engine::download(const HostBatch &hb, const gba_problem_view *v, gba_summary *s, std::string *err) {
+  gba_status st;
+  if ((st = check(cudaMemcpyAsync(h_stage_ + download_off_, d_arena_ + download_off_, download_bytes_,
+                                  cudaMemcpyDeviceToHost, stream_),
+                  "download", err)) != GBA_OK)
+    return st;
+  if ((st = check(cudaStreamSynchronize(stream_), "solver kernels", err)) != GBA_OK) return st;
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, ev_start_, ev_stop_);
+  last_solve_ms_ = ms;
+  DeviceBatch hdb{};
+  size_t ub, doff, dbytes;
+  layout(hb, h_stage_, &hdb, &ub, &doff, &dbytes);
+  const int32_t *hstat = hdb.status;
+  if (hstat[0] != 0) {
+    *err = "device-side loop guard tripped (internal error)";
+    return GBA_ERR_INTERNAL;
+  }
+  const double *out_cam = reinterpret_cast<const double *>(h_stage_ + download_off_);
+  const double *out_pt =
+      reinterpret_cast<const double *>(h_stage_ + download_off_ + align_up(sizeof(double) * 9 * (size_t)hb.nc, 256));
+  for (int p = 0; p < hb.P; ++p) {
+    if (v[p].parameters) scatter_parameters(hb, p, out_cam, out_pt, v[p].parameters);
+    if (!s) continue;
+    const LMState &L = hdb.lm[p];
+    gba_summary &S = s[p];
+    S.initial_cost = L.initial_cost;
+    S.final_cost = L.x_cost;
+    S.num_iterations = L.iteration;
+    S.num_successful_steps = L.successful_steps;
+    S.num_unsuccessful_steps = L.unsuccessful_steps;
+    S.num_invalid_steps = L.invalid_steps;
+    S.num_linear_solver_iterations = L.total_pcg_iterations;
+    S.termination_type = L.termination_type < 0 ? GBA_TERMINATION_NO_CONVERGENCE : L.termination_type;
+    S.termination_reason = L.termination_reason;
+    S.final_trust_region_radius = L.radius;
+    S.gradient_max_norm = L.gradient_max_norm;
+    S.solve_time_s = ms * 1e-3;
+    const int n = std::min(L.iteration + 1, trace_cap_);
+    S.trace_length = std::min(n, S.trace_capacity > 0 ? S.trace_capacity : 0);
+    for (int k = 0; k < S.trace_length; ++k) {
+      const size_t i = (size_t)p * trace_cap_ + k;
+      if (S.trace_cost) S.trace_cost[k] = hdb.trace_cost[i];
+      if (S.trace_radius) S.trace_radius[k] = hdb.trace_radius[i];
+      if (S.trace_linear_iterations) S.trace_linear_iterations[k] = hdb.trace_pcg[i];
+      if (S.trace_successful) S.trace_successful[k] = hdb.trace_succ[i];
+    }
+  }
+  return GBA_OK;
+}
+
+gba_status Engine::solve(const gba_problem_view *v, int n, gba_summary *s, std::string *err) {
+  const double t0 = now_s();
+  PrepOptions po;
+  po.reorder_points = o_.reorder_points != 0;
+  HostBatch hb;
+  gba_status st = prepare_batch(v, n, po, &hb, err);
+  if (st != GBA_OK) return st;
+  if ((st = upload(hb, err)) != GBA_OK) return st;
+  const double t1 = now_s();
+  if ((st = run_solve(err)) != GBA_OK) return st;
+  if ((st = download(hb, v, s, err)) != GBA_OK) return st;
+  const double t2 = now_s();
+  if (s)
+    for (int p = 0; p < n; ++p) {
+      s[p].setup_time_s = t1 - t0;
+      s[p].total_time_s = t2 - t0;
+    }
+  if (o_.minimizer_progress_to_stdout && s) {
+    for (int p = 0; p < n; ++p) {
+      std::printf("problem %d: iter  cost  tr_radius  pcg  success\n", p);
+      for (int k = 0; k < s[p].trace_length; ++k)
+        std::printf("%4d % .6e % .2e %4d %d\n", k, s[p].trace_cost ? s[p].trace_cost[k] : 0.0,
+                    s[p].trace_radius ? s[p].trace_radius[k] : 0.0,
+                    s[p].trace_linear_iterations ? s[p].trace_linear_iterations[k] : 0,
+                    s[p].trace_successful ? s[p].trace_successful[k] : 0);
+    }
+  }
+  return GBA_OK;
+}
+
+gba_status Engine::evaluate(const gba_problem_view *v, double *residuals, double *jacobians, double *cost,
+                            std::string *err) {
+  PrepOptions po;
+  po.reorder_points = o_.reorder_points != 0;
+  HostBatch hb;
+  gba_status st = prepare_batch(v, 1, po, &hb, err);
+  if (st != GBA_OK) return st;
+  if ((st = upload(hb, err)) != GBA_OK) return st;
+  const int loss = db_.opt.loss;
+  db_.opt.loss = GBA_LOSS_TRIVIAL;
+  db_.use_cond = 0;
+  cudaMemsetAsync(db_.prob_counter, 0, 4 * sizeof(uint32_t) * (size_t)db_.num_problems, stream_);
+  cudaMemsetAsync(db_.global_counter, 0, 8 * sizeof(uint32_t), stream_);
+  cudaMemsetAsync(db_.status, 0, 8 * sizeof(int32_t), stream_);
+  launch_sync_param_buffers(db_, stream_);
+  launch_init_state(db_, stream_);
+  launch_camera_table(db_, stream_);
+  launch_eval_jacobian(db_, mixed_, true, stream_);
+  db_.opt.loss = loss;
+  launch_cost_only(db_, stream_);
+  if ((st = check(cudaStreamSynchronize(stream_), "evaluate kernels", err)) != GBA_OK) return st;
+  const size_t no = hb.no;
+  const size_t pair = mixed_ ? sizeof(float2) : sizeof(double2);
+  std::vector<char> jac(13 * no * pair);
+  std::vector<double> cs((size_t)kChunkScal * hb.nchunks);
+  if (no && (st = check(cudaMemcpy(jac.data(), db_.jac, jac.size(), cudaMemcpyDeviceToHost), "download", err)) != GBA_OK)
+    return st;
+  if (!cs.empty() && (st = check(cudaMemcpy(cs.data(), db_.chunk_scal, cs.size() * sizeof(double), cudaMemcpyDeviceToHost),
+                                 "download", err)) != GBA_OK)
+    return st;
+  auto get = [&](int k, size_t o, int comp) -> double {
+    if (mixed_) {
+      const float2 f = reinterpret_cast<const float2 *>(jac.data())[k * no + o];
+      return comp ? f.y : f.x;
+    }
+    const double2 d = reinterpret_cast<const double2 *>(jac.data())[k * no + o];
+    return comp ? d.y : d.x;
+  };
+  for (size_t o = 0; o < no; ++o) {
+    const size_t i = hb.obs_orig[o];
+    for (int row = 0; row < 2; ++row) {
+      if (residuals) residuals[2 * i + row] = get(12, o, row);
+      if (jacobians)
+        for (int k = 0; k < 12; ++k) jacobians[24 * i + 12 * row + k] = get(k, o, row);
+    }
+  }
+  if (cost) {
+    double c = 0.0;
+    for (int ch = 0; ch < hb.nchunks; ++ch) c += cs[(size_t)kChunkScal * ch + kCS_COST];
+    *cost = c;
+  }
+  return GBA_OK;
+}
+
+gba_status Engine::compute_step(const gba_problem_view *v, double radius, double *delta, double *model,
+                                int *pcg_iterations, std::string *err) {
+  PrepOptions po;
+  po.reorder_points = o_.reorder_points != 0;
+  HostBatch hb;
+  gba_status st = prepare_batch(v, 1, po, &hb, err);
+  if (st != GBA_OK) return st;
+  if ((st = upload(hb, err)) != GBA_OK) return st;
+  db_.use_cond = 0;
+  int32_t *hstat = reinterpret_cast<int32_t *>(h_stage_ + (reinterpret_cast<char *>(db_.status) - d_arena_));
+  auto read_status = [&]() -> gba_status {
+    gba_status s2 = check(cudaMemcpyAsync(hstat, db_.status, 8 * sizeof(int32_t), cudaMemcpyDeviceToHost, stream_),
+                          "status read", err);
+    if (s2 != GBA_OK) return s2;
+    return check(cudaStreamSynchronize(stream_), "kernels", err);
+  };
+  cudaMemsetAsync(db_.prob_counter, 0, 4 * sizeof(uint32_t) * (size_t)db_.num_problems, stream_);
+  cudaMemsetAsync(db_.global_counter, 0, 8 * sizeof(uint32_t), stream_);
+  cudaMemsetAsync(db_.status, 0, 8 * sizeof(int32_t), stream_);
+  launch_sync_param_buffers(db_, stream_);
+  launch_init_state(db_, stream_);
+  launch_camera_table(db_, stream_);
+  launch_eval_jacobian(db_, mixed_, true, stream_);
+  launch_scale_init(db_, stream_);
+  launch_eval_jacobian(db_, mixed_, false, stream_);
+  launch_post_eval(db_, stream_);
+  if ((st = read_status()) != GBA_OK) return st;
+  // force the problem active with the requested radius
+  LMState L;
+  if ((st = check(cudaMemcpy(&L, db_.lm, sizeof L, cudaMemcpyDeviceToHost), "state", err)) != GBA_OK) return st;
+  L.radius = radius;
+  L.active = 1;
+  if ((st = check(cudaMemcpy(db_.lm, &L, sizeof L, cudaMemcpyHostToDevice), "state", err)) != GBA_OK) return st;
+  launch_point_prepare(db_, mixed_, stream_);
+  launch_camera_schur(db_, mixed_, stream_);
+  if ((st = read_status()) != GBA_OK) return st;
+  int pcg = 0;
+  while (hstat[2] && pcg <= o_.max_linear_solver_iterations) {
+    ++pcg;
+    launch_pcg_iteration(db_, mixed_, stream_);
+    if ((st = read_status()) != GBA_OK) return st;
+  }
+  launch_back_substitute(db_, mixed_, stream_);
+  launch_candidate_cost(db_, stream_);
+  launch_decide(db_, stream_);
+  if ((st = check(cudaStreamSynchronize(stream_), "step kernels", err)) != GBA_OK) return st;
+  if ((st = check(cudaMemcpy(&L, db_.lm, sizeof L, cudaMemcpyDeviceToHost), "state", err)) != GBA_OK) return st;
+  std::vector<double> c0(9 * (size_t)hb.nc), c1(9 * (size_t)hb.nc), p0(4 * (size_t)hb.np), p1(4 * (size_t)hb.np);
+  if (hb.nc) {
+    cudaMemcpy(c0.data(), db_.cam_param[0], c0.size() * 8, cudaMemcpyDeviceToHost);
+    cudaMemcpy(c1.data(), db_.cam_param[1], c1.size() * 8, cudaMemcpyDeviceToHost);
+  }
+  if (hb.np) {
+    cudaMemcpy(p0.data(), db_.pt_param[0], p0.size() * 8, cudaMemcpyDeviceToHost);
+    cudaMemcpy(p1.data(), db_.pt_param[1], p1.size() * 8, cudaMemcpyDeviceToHost);
+  }
+  if ((st = check(cudaGetLastError(), "download", err)) != GBA_OK) return st;
+  const size_t n = 9 * (size_t)hb.nc + 3 * (size_t)hb.np;
+  std::vector<double> x0(n), x1(n);
+  scatter_parameters(hb, 0, c0.data(), p0.data(), x0.data());
+  scatter_parameters(hb, 0, c1.data(), p1.data(), x1.data());
+  for (size_t k = 0; k < n; ++k) delta[k] = x1[k] - x0[k];
+  if (model) *model = L.model_cost_change;
+  if (pcg_iterations) *pcg_iterations = L.pcg_iterations;
+  if (!L.last_linear_ok) {
+    *err = "linear solve failed";
+    return GBA_ERR_INTERNAL;
+  }
+  return GBA_OK;
+}
+
+}  // namespace gba

@@ -1,0 +1,88 @@
+// engine.h — one GPU solver instance (behind a gba_handle).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "gba_internal.h"
+#include "prep.h"
+
+namespace gba {
+
+struct ProfileEntry {
+  std::string name;
+  long long launches = 0;
+  double total_ms = 0.0;
+  double bytes = 0.0;  // algorithmic bytes moved, summed over launches
+};
+
+class Engine {
+ public:
+  explicit Engine(const gba_options &o);
+  ~Engine();
+  gba_status init(std::string *err);
+
+  gba_status solve(const gba_problem_view *v, int n, gba_summary *s, std::string *err);
+  gba_status evaluate(const gba_problem_view *v, double *residuals, double *jacobians, double *cost,
+                      std::string *err);
+  gba_status compute_step(const gba_problem_view *v, double radius, double *delta, double *model,
+                          int *pcg_iterations, std::string *err);
+
+  void set_profiling(bool on) { profiling_ = on; }
+  const std::vector<ProfileEntry> &profile() const { return profile_; }
+  const gba_options &options() const { return o_; }
+  cudaStream_t stream() const { return stream_; }
+  size_t device_bytes() const { return d_cap_; }
+
+  // Prepared-batch level entry points (used by the serving loop).
+  gba_status upload(const HostBatch &hb, std::string *err);
+  gba_status run_solve(std::string *err);
+  // Re-runs the last uploaded batch from its initial point (device only,
+  // asynchronous on the handle's stream).
+  gba_status rerun(std::string *err);
+  gba_status download(const HostBatch &hb, const gba_problem_view *v, gba_summary *s, std::string *err);
+
+ private:
+  gba_status ensure_capacity(size_t dev_bytes, size_t host_bytes, std::string *err);
+  size_t layout(const HostBatch &hb, char *dbase, DeviceBatch *db, size_t *upload_bytes,
+                size_t *download_off, size_t *download_bytes);
+  gba_status build_graph(std::string *err);
+  void destroy_graph();
+  gba_status run_host_driven(std::string *err);
+  gba_status check(cudaError_t e, const char *what, std::string *err);
+  void enqueue_setup(cudaStream_t s);
+  void enqueue_lm_head(cudaStream_t s);
+  void enqueue_lm_tail(cudaStream_t s);
+  // profiling helpers (host-driven mode)
+  void prof_begin(cudaStream_t s);
+  void prof_end(cudaStream_t s, int entry, double bytes);
+
+  gba_options o_;
+  bool mixed_ = false;
+  bool profiling_ = false;
+  int device_ = 0;
+  cudaStream_t stream_ = nullptr;
+  bool own_stream_ = false;
+  cudaStream_t cap_[2] = {nullptr, nullptr};
+  char *d_arena_ = nullptr;
+  size_t d_cap_ = 0;
+  char *h_stage_ = nullptr;
+  size_t h_cap_ = 0;
+  DeviceBatch db_{};
+  size_t upload_bytes_ = 0, download_off_ = 0, download_bytes_ = 0;
+  // graph cache: valid while the arena and the batch shape are unchanged
+  cudaGraph_t graph_ = nullptr;
+  cudaGraphExec_t exec_ = nullptr;
+  std::vector<long long> graph_key_;
+  std::vector<long long> cur_key_;
+  // events
+  cudaEvent_t ev_start_ = nullptr, ev_stop_ = nullptr;
+  cudaEvent_t pev_[2] = {nullptr, nullptr};
+  std::vector<ProfileEntry> profile_;
+  double last_setup_ms_ = 0.0, last_solve_ms_ = 0.0;
+  int trace_cap_ = 0;
+};
+
+}  // namespace gba

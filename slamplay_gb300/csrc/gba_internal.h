@@ -1,0 +1,162 @@
+// gba_internal.h — definitions shared by the host library and the CUDA
+// kernels of libgba (not part of the public ABI).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+#include <vector_types.h>
+
+#include "gba.h"
+
+namespace gba {
+
+// Point-segment tile: one CTA of the chunk kernels processes one chunk, one
+// thread per observation.  A chunk is a run of consecutive points (in the
+// internal point order) whose observations fit in kChunkCap.
+constexpr int kChunkCap = 256;
+constexpr int kChunkCapLarge = 1024;  // problems with a point seen > 256 times
+
+// Per-chunk metadata (all indices global over the batch).
+struct ChunkInfo {
+  int32_t obs_begin;
+  int32_t obs_count;
+  int32_t pt_begin;
+  int32_t pt_count;
+  int32_t seg_begin;  // first camera segment of this chunk
+  int32_t seg_count;  // number of distinct cameras observed in this chunk
+  int32_t problem;
+  int32_t pad;
+};
+
+// Per-problem ranges inside the batch arrays.
+struct ProblemInfo {
+  int32_t cam_begin, cam_count;
+  int32_t pt_begin, pt_count;
+  int32_t obs_begin, obs_count;
+  int32_t chunk_begin, chunk_count;
+  int32_t seg_begin, seg_count;
+  int32_t cam_block_begin, cam_block_count;  // camera-kernel CTAs of this problem
+};
+
+// Solver options as the kernels need them (copied from gba_options).
+struct DeviceOptions {
+  double function_tolerance, gradient_tolerance, parameter_tolerance;
+  double initial_radius, max_radius, min_radius, min_relative_decrease;
+  double min_diagonal, max_diagonal;
+  double loss_scale;
+  double pcg_tolerance, eta;
+  int32_t max_iterations, max_invalid_steps, jacobi_scaling, loss;
+  int32_t pcg_criterion, max_pcg_iterations, min_pcg_iterations, mixed;
+};
+
+// LM / trust-region state of one problem, resident on the device.
+// Follows Ceres' TrustRegionMinimizer + LevenbergMarquardtStrategy.
+struct LMState {
+  double radius;
+  double decrease_factor;
+  double x_cost;           // cost at the current point
+  double x_norm;           // |x| over parameter blocks that appear in a residual
+  double gradient_max_norm;
+  double candidate_cost;
+  double model_cost_change;
+  double step_norm;
+  double minimum_cost;
+  double relative_decrease;
+  double initial_cost;
+  // PCG scalars
+  double rz, pq, alpha, beta, r0_norm, rr, q0;
+  int32_t iteration;       // LM iteration index (0 = initial point)
+  int32_t active;          // 1 while the problem is still iterating
+  int32_t need_jacobian;   // 1 after an accepted step
+  int32_t parity;          // which parameter buffer holds the current point
+  int32_t termination_type, termination_reason;
+  int32_t successful_steps, unsuccessful_steps, invalid_steps, invalid_run;
+  int32_t pcg_active, pcg_iterations, linear_ok, last_linear_ok;
+  int64_t total_pcg_iterations;
+};
+
+// Everything a kernel may touch, as raw device pointers.  Built by the host
+// (solver.cpp) and passed by value to every launch.
+struct DeviceBatch {
+  int32_t num_problems, nc, np, no, nchunks, nseg;
+  int32_t cam_blocks;        // camera blocks of the PCG kernels (kCamPerBlock cameras each)
+  const ProblemInfo *prob;
+  const ChunkInfo *chunk;
+  // observations, internal (point-major) order
+  const int32_t *obs_cam;    // global camera
+  const int32_t *obs_pt;     // global internal point
+  const double2 *obs_uv;
+  const uint16_t *obs_seg;   // local camera-segment index inside its chunk
+  const uint16_t *obs_slot;  // position in the chunk's camera-sorted order
+  const int32_t *pt_obs_begin;  // np + 1
+  const int32_t *pt_problem;
+  const int32_t *cam_problem;
+  const uint8_t *pt_used, *cam_used;
+  const uint16_t *seg_pos;   // start (sorted position) of each segment in its chunk
+  const int32_t *seg_cam;
+  const int32_t *cam_seg_begin, *cam_seg_list;
+  const int32_t *cam_obs_begin, *cam_obs_list;
+  // parameters: the uploaded initial point, and two working buffers of
+  // which LMState::parity picks the current one
+  const double *cam_init;    // nc * 9
+  const double *pt_init;     // np * 4 (xyz + pad)
+  double *cam_param[2];      // nc * 9
+  double *pt_param[2];       // np * 4
+  double *cam_table;         // nc * kCamTable: R, dR/dw, t, f, k1, k2 of one buffer
+  // Jacobian (scaled, loss-corrected), SoA by column pair; element type by mode
+  void *jac;                 // 13 * no of double2 (FP64) or float2 (mixed)
+  // per point
+  double *pt_C;              // 6 sym (J_p^T J_p)
+  double *pt_g;              // 3
+  double *pt_scale;          // 3
+  double *pt_t;              // 3: Cinv g_p
+  void *pt_Cinv;             // 6 sym, double (FP64) or float (mixed)
+  double *pt_Cinv64;         // 6 sym, double (both modes, for the back-substitution)
+  // per camera
+  double *cam_B;             // 45 sym packed (J_c^T J_c)
+  double *cam_g;             // 9
+  double *cam_scale;         // 9
+  double *cam_Minv;          // 81 block-Jacobi inverse of S_ii
+  double *cam_D2;            // 9: squared LM diagonal of the camera parameters
+  double *pcg_x, *pcg_r, *pcg_z, *pcg_p, *pcg_q, *pcg_v;  // 9 * nc each
+  double *cam_colnorm;       // 9 * nc: column norms of the first evaluation
+  double *pt_colnorm;        // 3 * np
+  double *seg_partial;       // 9 * nseg
+  // per chunk / per camera / per camera-block scalars (deterministic partials)
+  double *chunk_scal;        // kChunkScal per chunk
+  double *cam_scal;          // kCamScal per camera
+  double *blk_scal;          // kBlkScal per camera block
+  const int4 *camblk;        // camera blocks: (problem, first camera, count, 0)
+  LMState *lm;
+  DeviceOptions opt;
+  // cross-CTA completion counters (last-block reductions)
+  uint32_t *prob_counter;    // 4 per problem
+  uint32_t *global_counter;  // 8
+  int32_t *status;           // [0] error word, [1] any LM active, [2] any PCG active
+  // per-iteration trace, [num_problems][trace_cap]
+  int32_t trace_cap;
+  double *trace_cost, *trace_radius;
+  int32_t *trace_pcg, *trace_succ;
+  // graph conditional handles (0 when the host drives the loops)
+  unsigned long long lm_cond, pcg_cond;
+  int32_t use_cond;
+};
+
+constexpr int kCamTable = 44;    // R(9) dR(27) t(3) f k1 k2 + pad
+// chunk_scal slots
+constexpr int kChunkScal = 6;
+constexpr int kCS_COST = 0, kCS_GMAX = 1, kCS_XN2 = 2, kCS_MODEL = 3, kCS_STEP2 = 4, kCS_BAD = 5;
+// cam_scal slots
+constexpr int kCamScal = 6;
+constexpr int kCC_GMAX = 0, kCC_XN2 = 1, kCC_STEP2 = 2, kCC_RZ = 3, kCC_RR = 4;
+// blk_scal slots (PCG partials of one camera block)
+constexpr int kBlkScal = 4;
+constexpr int kBS_PQ = 0, kBS_RZ = 1, kBS_RR = 2, kBS_QX = 3;
+// cameras per CTA in the warp-per-camera PCG kernels
+constexpr int kCamPerBlock = 8;
+// prob_counter slots (4 per problem) and global_counter slots
+constexpr int kPC_SCHUR = 0, kPC_REDUCE = 1, kPC_UPDATE = 2;
+constexpr int kGC_SCHUR = 0, kGC_UPDATE = 1, kGC_POST = 2, kGC_LMBODIES = 3;
+
+}  // namespace gba

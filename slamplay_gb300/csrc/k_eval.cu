@@ -1,0 +1,546 @@
+// k_eval.cu — evaluation kernels of the GB300 bundle-adjustment solver.
+//
+//  K0  k_camera_table   per camera: R, dR/dw (dual-number Rodrigues), t, f, k1, k2
+//  K1  k_eval_chunk     per point-segment chunk, one thread per observation:
+//                       residual, analytic Jacobian (== the dual-number
+//                       Jacobian of SnavelyReprojectionError.h:42-87),
+//                       loss corrector, Jacobi scaling, J stored SoA; point
+//                       blocks J_p^T J_p and J_p^T r reduced per point in
+//                       shared memory (points own contiguous observations).
+//  K1c k_eval_camera    per camera (CTA): J_c^T J_c (45) and J_c^T r over the
+//                       camera's observations, fixed-order CTA reduction.
+//  K7  k_post_eval      per problem: cost, gradient max-norm, |x|, Ceres'
+//                       termination tests, LM-loop condition.
+//  K5b k_candidate      per camera: candidate camera + its table (R only).
+//  K2  k_cost_chunk     per chunk: candidate cost in FP64.
+#include <cuda_runtime.h>
+
+#include "kernels.cuh"
+#include "kernels.h"
+
+namespace gba {
+
+// ---------------------------------------------------------------------------
+__global__ void k_init_state(DeviceBatch B) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= B.num_problems) return;
+  LMState L;
+  memset(&L, 0, sizeof L);
+  L.radius = B.opt.initial_radius;
+  L.decrease_factor = 2.0;
+  L.active = B.prob[p].obs_count > 0 ? 1 : 0;
+  L.termination_type = L.active ? -1 : GBA_TERMINATION_CONVERGENCE;
+  L.need_jacobian = 1;
+  L.parity = 0;
+  L.linear_ok = 1;
+  L.last_linear_ok = 1;
+  B.lm[p] = L;
+}
+
+void launch_init_state(const DeviceBatch &b, cudaStream_t s) {
+  k_init_state<<<(b.num_problems + 127) / 128, 128, 0, s>>>(b);
+}
+
+// ---------------------------------------------------------------------------
+// K0
+__global__ void k_camera_table(DeviceBatch B) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= B.nc) return;
+  const LMState *L = B.lm + B.cam_problem[c];
+  if (!L->active || !L->need_jacobian) return;
+  camera_table_entry(B.cam_param[L->parity] + 9 * (size_t)c, B.cam_table + (size_t)kCamTable * c,
+                     true);
+}
+
+void launch_camera_table(const DeviceBatch &b, cudaStream_t s) {
+  k_camera_table<<<(b.nc + 127) / 128, 128, 0, s>>>(b);
+}
+
+// ---------------------------------------------------------------------------
+// Residual + Jacobian of one observation.  Jc[k] = (d r_u, d r_v)/d cam_k,
+// Jp[k] = (d r_u, d r_v)/d X_k, r = corrected residual; scaled by the Jacobi
+// scaling.  Returns 0.5*rho(|r|^2) (FP64).  *bad = 1 on a non-finite value.
+template <bool MIXED>
+__device__ __forceinline__ double eval_observation(const DeviceBatch &B, int64_t o, int c, int j,
+                                                   const double *X, bool unit_scale,
+                                                   typename Prec<MIXED>::real2 *Jc,
+                                                   typename Prec<MIXED>::real2 *Jp,
+                                                   typename Prec<MIXED>::real2 &r, bool &bad) {
+  typedef typename Prec<MIXED>::real real;
+  const double *tab = B.cam_table + (size_t)kCamTable * c;
+  Proj pr;
+  project(tab, X, B.obs_uv[o], pr);
+  // d prediction / dP = f * M * dxy  (x' = -P_x/P_z, y' = -P_y/P_z)
+  const real iz = (real)(1.0 / pr.P[2]);
+  const real xp = (real)pr.xp, yp = (real)pr.yp, r2 = (real)pr.r2, dist = (real)pr.dist;
+  const real f = (real)pr.f, k1 = (real)pr.k1, k2 = (real)pr.k2;
+  const real g = k1 + (real)2 * k2 * r2;
+  const real m00 = dist + (real)2 * g * xp * xp;
+  const real m01 = (real)2 * g * xp * yp;
+  const real m11 = dist + (real)2 * g * yp * yp;
+  const real A00 = -f * m00 * iz, A01 = -f * m01 * iz, A02 = -f * (m00 * xp + m01 * yp) * iz;
+  const real A10 = -f * m01 * iz, A11 = -f * m11 * iz, A12 = -f * (m01 * xp + m11 * yp) * iz;
+  real ju[12], jv[12];
+  const real Xr[3] = {(real)X[0], (real)X[1], (real)X[2]};
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    // dP/dw_k = dR_k X
+    const double *d = tab + 9 + 9 * k;
+    const real q0 = (real)d[0] * Xr[0] + (real)d[1] * Xr[1] + (real)d[2] * Xr[2];
+    const real q1 = (real)d[3] * Xr[0] + (real)d[4] * Xr[1] + (real)d[5] * Xr[2];
+    const real q2 = (real)d[6] * Xr[0] + (real)d[7] * Xr[1] + (real)d[8] * Xr[2];
+    ju[k] = A00 * q0 + A01 * q1 + A02 * q2;
+    jv[k] = A10 * q0 + A11 * q1 + A12 * q2;
+    // dP/dX_k = R[:,k]
+    const real c0 = (real)tab[k], c1 = (real)tab[3 + k], c2 = (real)tab[6 + k];
+    ju[9 + k] = A00 * c0 + A01 * c1 + A02 * c2;
+    jv[9 + k] = A10 * c0 + A11 * c1 + A12 * c2;
+  }
+  ju[3] = A00, ju[4] = A01, ju[5] = A02;
+  jv[3] = A10, jv[4] = A11, jv[5] = A12;
+  ju[6] = dist * xp, jv[6] = dist * yp;
+  ju[7] = f * r2 * xp, jv[7] = f * r2 * yp;
+  ju[8] = f * (r2 * r2) * xp, jv[8] = f * (r2 * r2) * yp;
+  // robust-loss corrector (FP64 scalars)
+  const int loss = B.opt.loss;
+  const double cost = block_cost(loss, B.opt.loss_scale, pr.ru, pr.rv);
+  double ru = pr.ru, rv = pr.rv;
+  if (loss != GBA_LOSS_TRIVIAL) {
+    const Corrector cr = make_corrector(loss, B.opt.loss_scale, ru, rv);
+    const real s1 = (real)cr.sqrt_rho1, al = (real)cr.alpha_sq_norm;
+    const real rur = (real)ru, rvr = (real)rv;
+#pragma unroll
+    for (int k = 0; k < 12; ++k) {
+      const real rJ = rur * ju[k] + rvr * jv[k];
+      ju[k] = s1 * (ju[k] - al * rur * rJ);
+      jv[k] = s1 * (jv[k] - al * rvr * rJ);
+    }
+    ru *= cr.residual_scaling;
+    rv *= cr.residual_scaling;
+  }
+  bool ok = isfinite(ru) && isfinite(rv) && isfinite(cost);
+  if (!unit_scale) {
+    const double *sc = B.cam_scale + 9 * (size_t)c;
+    const double *sp = B.pt_scale + 3 * (size_t)j;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      const real s = (real)sc[k];
+      ju[k] *= s;
+      jv[k] *= s;
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const real s = (real)sp[k];
+      ju[9 + k] *= s;
+      jv[9 + k] *= s;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    Jc[k] = mk2(ju[k], jv[k]);
+    ok = ok && isfinite((double)ju[k]) && isfinite((double)jv[k]);
+  }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    Jp[k] = mk2(ju[9 + k], jv[9 + k]);
+    ok = ok && isfinite((double)ju[9 + k]) && isfinite((double)jv[9 + k]);
+  }
+  r = mk2((real)ru, (real)rv);
+  bad = !ok;
+  return cost;
+}
+
+// ---------------------------------------------------------------------------
+// K1
+template <bool MIXED, bool NORMS>
+__global__ void __launch_bounds__(kChunkCap) k_eval_chunk(DeviceBatch B) {
+  typedef typename Prec<MIXED>::real real;
+  typedef typename Prec<MIXED>::real2 real2;
+  typedef typename Acc<MIXED>::type Acc;
+  __shared__ real sm[kChunkCap][9];
+  __shared__ double red[kChunkCap / 32];
+  const int t = threadIdx.x;
+  for (int ch = blockIdx.x; ch < B.nchunks; ch += gridDim.x) {
+    const ChunkInfo ci = B.chunk[ch];
+    const LMState *L = B.lm + ci.problem;
+    if (!L->active || !L->need_jacobian) continue;  // uniform over the CTA
+    const int parity = L->parity;
+    double cost = 0.0;
+    bool bad = false;
+    if (t < ci.obs_count) {
+      const int64_t o = ci.obs_begin + t;
+      const int c = B.obs_cam[o], j = B.obs_pt[o];
+      const double *Xp = B.pt_param[parity] + 4 * (size_t)j;
+      const double X[3] = {Xp[0], Xp[1], Xp[2]};
+      real2 Jc[9], Jp[3], r;
+      cost = eval_observation<MIXED>(B, o, c, j, X, NORMS, Jc, Jp, r, bad);
+#pragma unroll
+      for (int k = 0; k < 9; ++k) jstore(B.jac, B.no, k, o, Jc[k]);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) jstore(B.jac, B.no, 9 + k, o, Jp[k]);
+      jstore(B.jac, B.no, 12, o, r);
+      // point-block contributions: C (sym3) and g
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+#pragma unroll
+        for (int b = a; b < 3; ++b) sm[t][sym3(a, b)] = Jp[a].x * Jp[b].x + Jp[a].y * Jp[b].y;
+        sm[t][6 + a] = Jp[a].x * r.x + Jp[a].y * r.y;
+      }
+    }
+    __syncthreads();
+    double gmax = 0.0, xn2 = 0.0;
+    if (t < ci.pt_count) {
+      const int jj = ci.pt_begin + t;
+      const int b0 = B.pt_obs_begin[jj] - ci.obs_begin, b1 = B.pt_obs_begin[jj + 1] - ci.obs_begin;
+      Acc acc[9];
+#pragma unroll
+      for (int q = 0; q < 9; ++q) acc[q].init();
+      for (int k = b0; k < b1; ++k) {
+#pragma unroll
+        for (int q = 0; q < 9; ++q) acc[q].add(sm[k][q]);
+      }
+      if (NORMS) {
+        B.pt_colnorm[3 * (size_t)jj + 0] = acc[0].value();
+        B.pt_colnorm[3 * (size_t)jj + 1] = acc[3].value();
+        B.pt_colnorm[3 * (size_t)jj + 2] = acc[5].value();
+      } else {
+#pragma unroll
+        for (int q = 0; q < 6; ++q) B.pt_C[6 * (size_t)jj + q] = acc[q].value();
+        if (B.pt_used[jj]) {
+          const double *x = B.pt_param[parity] + 4 * (size_t)jj;
+#pragma unroll
+          for (int q = 0; q < 3; ++q) {
+            const double gq = acc[6 + q].value();
+            B.pt_g[3 * (size_t)jj + q] = gq;
+            const double gu = gq / B.pt_scale[3 * (size_t)jj + q];
+            gmax = fmax(gmax, fabs(x[q] - (x[q] - gu)));
+            xn2 += x[q] * x[q];
+          }
+        } else {
+#pragma unroll
+          for (int q = 0; q < 3; ++q) B.pt_g[3 * (size_t)jj + q] = 0.0;
+        }
+      }
+    }
+    if (!NORMS) {
+      const double cs = block_sum(cost, red);
+      const double gm = block_max(gmax, red);
+      const double xs = block_sum(xn2, red);
+      const double bd = block_max(bad ? 1.0 : 0.0, red);
+      if (t == 0) {
+        double *cs_out = B.chunk_scal + (size_t)kChunkScal * ch;
+        cs_out[kCS_COST] = cs;
+        cs_out[kCS_GMAX] = gm;
+        cs_out[kCS_XN2] = xs;
+        cs_out[kCS_BAD] = bd;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// K1c: one CTA per camera.
+constexpr int kCamThreads = 128;
+
+template <bool MIXED, bool NORMS>
+__global__ void __launch_bounds__(kCamThreads) k_eval_camera(DeviceBatch B) {
+  typedef typename Prec<MIXED>::real real;
+  typedef typename Prec<MIXED>::real2 real2;
+  typedef typename Acc<MIXED>::type Acc;
+  constexpr int NV = NORMS ? 9 : 54;
+  __shared__ double part[kCamThreads / 32][NV];
+  const int c = blockIdx.x;
+  const LMState *L = B.lm + B.cam_problem[c];
+  if (!L->active || !L->need_jacobian) return;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  Acc acc[NV];
+#pragma unroll
+  for (int q = 0; q < NV; ++q) acc[q].init();
+  const int e = B.cam_obs_begin[c + 1];
+  for (int k = B.cam_obs_begin[c] + t; k < e; k += kCamThreads) {
+    const int64_t o = B.cam_obs_list[k];
+    real2 J[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) J[q] = jload<real2>(B.jac, B.no, q, o);
+    if (NORMS) {
+#pragma unroll
+      for (int q = 0; q < 9; ++q) acc[q].add(J[q].x * J[q].x + J[q].y * J[q].y);
+    } else {
+      const real2 r = jload<real2>(B.jac, B.no, 12, o);
+#pragma unroll
+      for (int a = 0; a < 9; ++a) {
+#pragma unroll
+        for (int b = a; b < 9; ++b) acc[sym9(a, b)].add(J[a].x * J[b].x + J[a].y * J[b].y);
+        acc[45 + a].add(J[a].x * r.x + J[a].y * r.y);
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < NV; ++q) {
+    const double v = warp_sum(acc[q].value());
+    if (lane == 0) part[warp][q] = v;
+  }
+  __syncthreads();
+  if (t < NV) {
+    double s = 0.0;
+    for (int w = 0; w < kCamThreads / 32; ++w) s += part[w][t];
+    part[0][t] = s;  // each t reads its own column only before writing it
+  }
+  __syncthreads();
+  if (t == 0) {
+    if (NORMS) {
+      for (int q = 0; q < 9; ++q) B.cam_colnorm[9 * (size_t)c + q] = part[0][q];
+    } else {
+      for (int q = 0; q < 45; ++q) B.cam_B[45 * (size_t)c + q] = part[0][q];
+      double gmax = 0.0, xn2 = 0.0;
+      const bool used = B.cam_used[c] != 0;
+      const double *x = B.cam_param[L->parity] + 9 * (size_t)c;
+      for (int q = 0; q < 9; ++q) {
+        const double gq = used ? part[0][45 + q] : 0.0;
+        B.cam_g[9 * (size_t)c + q] = gq;
+        if (used) {
+          const double gu = gq / B.cam_scale[9 * (size_t)c + q];
+          gmax = fmax(gmax, fabs(x[q] - (x[q] - gu)));
+          xn2 += x[q] * x[q];
+        }
+      }
+      B.cam_scal[(size_t)kCamScal * c + kCC_GMAX] = gmax;
+      B.cam_scal[(size_t)kCamScal * c + kCC_XN2] = xn2;
+    }
+  }
+}
+
+void launch_eval_jacobian(const DeviceBatch &b, bool mixed, bool norms, cudaStream_t s) {
+  const int gc = b.nchunks;
+  if (mixed) {
+    if (norms) {
+      k_eval_chunk<true, true><<<gc, kChunkCap, 0, s>>>(b);
+      k_eval_camera<true, true><<<b.nc, kCamThreads, 0, s>>>(b);
+    } else {
+      k_eval_chunk<true, false><<<gc, kChunkCap, 0, s>>>(b);
+      k_eval_camera<true, false><<<b.nc, kCamThreads, 0, s>>>(b);
+    }
+  } else {
+    if (norms) {
+      k_eval_chunk<false, true><<<gc, kChunkCap, 0, s>>>(b);
+      k_eval_camera<false, true><<<b.nc, kCamThreads, 0, s>>>(b);
+    } else {
+      k_eval_chunk<false, false><<<gc, kChunkCap, 0, s>>>(b);
+      k_eval_camera<false, false><<<b.nc, kCamThreads, 0, s>>>(b);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Jacobi scaling s = 1 / (1 + sqrt(|J_col|^2)) of the first evaluation, kept
+// for the whole solve.
+__global__ void k_scale_init(DeviceBatch B) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t ncam = 9 * (int64_t)B.nc, npt = 3 * (int64_t)B.np;
+  if (i < ncam) {
+    B.cam_scale[i] = B.opt.jacobi_scaling ? 1.0 / (1.0 + sqrt(B.cam_colnorm[i])) : 1.0;
+  } else if (i < ncam + npt) {
+    const int64_t k = i - ncam;
+    B.pt_scale[k] = B.opt.jacobi_scaling ? 1.0 / (1.0 + sqrt(B.pt_colnorm[k])) : 1.0;
+  }
+}
+
+void launch_scale_init(const DeviceBatch &b, cudaStream_t s) {
+  const int64_t n = 9 * (int64_t)b.nc + 3 * (int64_t)b.np;
+  k_scale_init<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(b);
+}
+
+// Sets the LM-loop condition once every problem's CTA of this launch is
+// done: any problem still active, and never more LM bodies than the
+// iteration cap allows (a runaway loop cannot happen).
+__device__ void finish_lm_body(const DeviceBatch &B, bool count_body) {
+  __shared__ int flag;
+  if (last_block_done(B.global_counter + kGC_POST, gridDim.x, &flag)) {
+    if (threadIdx.x == 0) {
+      int any = 0;
+      for (int p = 0; p < B.num_problems; ++p) any |= B.lm[p].active;
+      uint32_t bodies = B.global_counter[kGC_LMBODIES];
+      if (count_body) B.global_counter[kGC_LMBODIES] = ++bodies;
+      if (bodies > (uint32_t)B.opt.max_iterations + 2u) {
+        if (any) B.status[0] = GBA_ERR_INTERNAL;
+        any = 0;
+      }
+      B.status[1] = any;
+      if (B.use_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)B.lm_cond, any ? 1u : 0u);
+    }
+  }
+}
+
+// K7: one CTA per problem.
+__global__ void __launch_bounds__(256) k_post_eval(DeviceBatch B, int count_body) {
+  __shared__ double red[8];
+  const int p = blockIdx.x;
+  LMState *L = B.lm + p;
+  if (L->active && L->need_jacobian) {
+    const ProblemInfo pi = B.prob[p];
+    const double *cs = B.chunk_scal;
+    const double cost = block_range_sum(cs + kCS_COST, pi.chunk_begin, pi.chunk_begin + pi.chunk_count, kChunkScal, red);
+    const double bad = block_range_max(cs + kCS_BAD, pi.chunk_begin, pi.chunk_begin + pi.chunk_count, kChunkScal, red);
+    const double gp = block_range_max(cs + kCS_GMAX, pi.chunk_begin, pi.chunk_begin + pi.chunk_count, kChunkScal, red);
+    const double gc = block_range_max(B.cam_scal + kCC_GMAX, pi.cam_begin, pi.cam_begin + pi.cam_count, kCamScal, red);
+    const double xc = block_range_sum(B.cam_scal + kCC_XN2, pi.cam_begin, pi.cam_begin + pi.cam_count, kCamScal, red);
+    const double xp = block_range_sum(cs + kCS_XN2, pi.chunk_begin, pi.chunk_begin + pi.chunk_count, kChunkScal, red);
+    if (threadIdx.x == 0) {
+      const DeviceOptions &o = B.opt;
+      L->need_jacobian = 0;
+      L->x_cost = cost;
+      L->gradient_max_norm = fmax(gp, gc);
+      L->x_norm = sqrt(xc + xp);
+      const int it = L->iteration;
+      if (bad != 0.0 || !isfinite(cost)) {
+        L->active = 0;
+        L->termination_type = GBA_TERMINATION_FAILURE;
+        L->termination_reason = GBA_REASON_EVALUATION_FAILED;
+        if (it == 0) L->initial_cost = cost;
+      } else {
+        if (it == 0) {
+          L->initial_cost = cost;
+          L->minimum_cost = cost;
+          trace_put(B, p, 0, cost, L->radius, 0, 1);
+        } else {
+          L->minimum_cost = cost;
+          trace_put(B, p, it, cost, L->radius, L->pcg_iterations, 1);
+        }
+        if (it >= o.max_iterations) {
+          L->active = 0;
+          L->termination_type = GBA_TERMINATION_NO_CONVERGENCE;
+          L->termination_reason = GBA_REASON_MAX_ITERATIONS;
+        } else if (L->gradient_max_norm <= o.gradient_tolerance) {
+          L->active = 0;
+          L->termination_type = GBA_TERMINATION_CONVERGENCE;
+          L->termination_reason = GBA_REASON_GRADIENT_TOLERANCE;
+        } else if (L->radius <= o.min_radius) {
+          L->active = 0;
+          L->termination_type = GBA_TERMINATION_CONVERGENCE;
+          L->termination_reason = GBA_REASON_MIN_TRUST_REGION_RADIUS;
+        }
+      }
+    }
+  }
+  finish_lm_body(B, count_body != 0);
+}
+
+void launch_post_eval(const DeviceBatch &b, cudaStream_t s) {
+  k_post_eval<<<b.num_problems, 256, 0, s>>>(b, 1);
+}
+
+// ---------------------------------------------------------------------------
+// K5b: candidate cameras x + step * scale (step = -y_c from the PCG), the
+// camera part of |x - x_cand|^2, and the candidate camera tables (R only).
+__global__ void k_candidate_cameras(DeviceBatch B) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= B.nc) return;
+  const LMState *L = B.lm + B.cam_problem[c];
+  if (!L->active || !L->linear_ok) return;
+  const double *x = B.cam_param[L->parity] + 9 * (size_t)c;
+  double *xc = B.cam_param[L->parity ^ 1] + 9 * (size_t)c;
+  double cand[9];
+  double s2 = 0.0;
+  const bool used = B.cam_used[c] != 0;
+  for (int q = 0; q < 9; ++q) {
+    const double step = -B.pcg_x[9 * (size_t)c + q];
+    cand[q] = used ? x[q] + step * B.cam_scale[9 * (size_t)c + q] : x[q];
+    const double d = x[q] - cand[q];
+    s2 += d * d;
+    xc[q] = cand[q];
+  }
+  B.cam_scal[(size_t)kCamScal * c + kCC_STEP2] = used ? s2 : 0.0;
+  camera_table_entry(cand, B.cam_table + (size_t)kCamTable * c, false);
+}
+
+// K2: candidate cost, FP64 in both precision modes.
+__global__ void __launch_bounds__(kChunkCap) k_cost_chunk(DeviceBatch B) {
+  __shared__ double red[kChunkCap / 32];
+  const int t = threadIdx.x;
+  for (int ch = blockIdx.x; ch < B.nchunks; ch += gridDim.x) {
+    const ChunkInfo ci = B.chunk[ch];
+    const LMState *L = B.lm + ci.problem;
+    if (!L->active || !L->linear_ok) continue;
+    const int parity = L->parity ^ 1;
+    double cost = 0.0;
+    bool bad = false;
+    if (t < ci.obs_count) {
+      const int64_t o = ci.obs_begin + t;
+      const int c = B.obs_cam[o], j = B.obs_pt[o];
+      const double *Xp = B.pt_param[parity] + 4 * (size_t)j;
+      const double X[3] = {Xp[0], Xp[1], Xp[2]};
+      Proj pr;
+      project(B.cam_table + (size_t)kCamTable * c, X, B.obs_uv[o], pr);
+      cost = block_cost(B.opt.loss, B.opt.loss_scale, pr.ru, pr.rv);
+      bad = !(isfinite(pr.ru) && isfinite(pr.rv) && isfinite(cost));
+    }
+    const double cs = block_sum(cost, red);
+    const double bd = block_max(bad ? 1.0 : 0.0, red);
+    if (t == 0) {
+      B.chunk_scal[(size_t)kChunkScal * ch + kCS_COST] = cs;
+      B.chunk_scal[(size_t)kChunkScal * ch + kCS_BAD] = bd;
+    }
+  }
+}
+
+void launch_candidate_cost(const DeviceBatch &b, cudaStream_t s) {
+  k_candidate_cameras<<<(b.nc + 127) / 128, 128, 0, s>>>(b);
+  k_cost_chunk<<<b.nchunks, kChunkCap, 0, s>>>(b);
+}
+
+// Cost at the second parameter buffer with the current camera tables (the
+// kernel-level evaluate entry point, where both buffers hold the same point).
+void launch_cost_only(const DeviceBatch &b, cudaStream_t s) {
+  if (b.nchunks > 0) k_cost_chunk<<<b.nchunks, kChunkCap, 0, s>>>(b);
+}
+
+// Fails with cudaErrorNoKernelImageForDevice when the sm_103a image cannot
+// run on the current device.
+cudaError_t probe_kernel_image() {
+  cudaFuncAttributes a;
+  return cudaFuncGetAttributes(&a, k_init_state);
+}
+
+// ---------------------------------------------------------------------------
+// Starts a solve from the uploaded initial point: both working buffers get
+// the initial parameters (blocks a problem never updates then hold the same
+// values in both), so a solve can be re-run without a new upload.
+__global__ void k_sync_params(DeviceBatch B) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nc9 = 9 * (int64_t)B.nc, np4 = 4 * (int64_t)B.np;
+  if (i < nc9) {
+    const double v = B.cam_init[i];
+    B.cam_param[0][i] = v;
+    B.cam_param[1][i] = v;
+  } else if (i < nc9 + np4) {
+    const double v = B.pt_init[i - nc9];
+    B.pt_param[0][i - nc9] = v;
+    B.pt_param[1][i - nc9] = v;
+  }
+}
+
+__global__ void k_gather_results(DeviceBatch B, double *out_cam, double *out_pt) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nc9 = 9 * (int64_t)B.nc, np4 = 4 * (int64_t)B.np;
+  if (i < nc9) {
+    const int par = B.lm[B.cam_problem[i / 9]].parity;
+    out_cam[i] = B.cam_param[par][i];
+  } else if (i < nc9 + np4) {
+    const int64_t k = i - nc9;
+    const int par = B.lm[B.pt_problem[k / 4]].parity;
+    out_pt[k] = B.pt_param[par][k];
+  }
+}
+
+void launch_gather_results(const DeviceBatch &b, double *out_cam, double *out_pt, cudaStream_t s) {
+  const int64_t n = 9 * (int64_t)b.nc + 4 * (int64_t)b.np;
+  if (n > 0) k_gather_results<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(b, out_cam, out_pt);
+}
+
+void launch_sync_param_buffers(const DeviceBatch &b, cudaStream_t s) {
+  const int64_t n = 9 * (int64_t)b.nc + 4 * (int64_t)b.np;
+  k_sync_params<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(b);
+}
+
+}  // namespace gba

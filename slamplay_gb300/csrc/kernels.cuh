@@ -1,0 +1,387 @@
+// kernels.cuh — device helpers shared by the libgba kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cfloat>
+#include <cstdint>
+
+#include "gba_internal.h"
+
+namespace gba {
+
+// ---------------------------------------------------------------------------
+// Storage type of the Jacobian / Schur products per precision mode.
+// ---------------------------------------------------------------------------
+template <bool MIXED>
+struct Prec;
+template <>
+struct Prec<false> {
+  typedef double real;
+  typedef double2 real2;
+};
+template <>
+struct Prec<true> {
+  typedef float real;
+  typedef float2 real2;
+};
+
+__device__ __forceinline__ double2 mk2(double a, double b) { return make_double2(a, b); }
+__device__ __forceinline__ float2 mk2(float a, float b) { return make_float2(a, b); }
+
+// Packed symmetric indices: 3x3 as (00 01 02 11 12 22), 9x9 upper row-major.
+__host__ __device__ __forceinline__ int sym3(int i, int j) {
+  if (i > j) {
+    const int t = i;
+    i = j;
+    j = t;
+  }
+  return i * 3 - (i * (i - 1)) / 2 + (j - i);
+}
+__host__ __device__ __forceinline__ int sym9(int i, int j) {
+  if (i > j) {
+    const int t = i;
+    i = j;
+    j = t;
+  }
+  return i * 9 - (i * (i - 1)) / 2 + (j - i);
+}
+
+// ---------------------------------------------------------------------------
+// Compensated (Kahan) summation for the FP32 segmented sums of the mixed
+// form.  Written so the compiler cannot fold the compensation away (no
+// fast-math is used anywhere in libgba).
+// ---------------------------------------------------------------------------
+struct KahanF {
+  float s, c;
+  __device__ __forceinline__ void init() { s = 0.f, c = 0.f; }
+  __device__ __forceinline__ void add(float x) {
+    const float y = __fsub_rn(x, c);
+    const float t = __fadd_rn(s, y);
+    c = __fsub_rn(__fsub_rn(t, s), y);
+    s = t;
+  }
+  __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+
+// Plain FP64 accumulator with the same interface.
+struct SumD {
+  double s;
+  __device__ __forceinline__ void init() { s = 0.0; }
+  __device__ __forceinline__ void add(double x) { s += x; }
+  __device__ __forceinline__ double value() const { return s; }
+};
+
+template <bool MIXED>
+struct Acc;
+template <>
+struct Acc<false> {
+  typedef SumD type;
+};
+template <>
+struct Acc<true> {
+  typedef KahanF type;
+};
+
+// ---------------------------------------------------------------------------
+// Deterministic reductions: fixed xor-butterfly inside a warp, then warp
+// results combined in warp order.  Results depend only on blockDim.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// Sum over the CTA; result valid in every thread.  `red` needs blockDim/32
+// doubles.  Contains __syncthreads(): call from all threads.
+__device__ __forceinline__ double block_sum(double v, double *red) {
+  v = warp_sum(v);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  double s = 0.0;
+  for (int w = 0; w < nw; ++w) s += red[w];
+  __syncthreads();
+  return s;
+}
+__device__ __forceinline__ double block_max(double v, double *red) {
+  v = warp_max(v);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  double s = 0.0;
+  for (int w = 0; w < nw; ++w) s = fmax(s, red[w]);
+  __syncthreads();
+  return s;
+}
+
+// Strided sum of a[begin..end) by the whole CTA in a fixed order.
+__device__ __forceinline__ double block_range_sum(const double *a, int begin, int end, int stride,
+                                                  double *red) {
+  double s = 0.0;
+  for (int i = begin + threadIdx.x; i < end; i += blockDim.x) s += a[(size_t)i * stride];
+  return block_sum(s, red);
+}
+__device__ __forceinline__ double block_range_max(const double *a, int begin, int end, int stride,
+                                                  double *red) {
+  double s = 0.0;
+  for (int i = begin + threadIdx.x; i < end; i += blockDim.x) s = fmax(s, a[(size_t)i * stride]);
+  return block_max(s, red);
+}
+
+// "Last CTA done" detection without waiting: each CTA fences its writes and
+// bumps a counter; the CTA that brings it to `total` sees everyone's results
+// and resets the counter.  Returns true in every thread of the last CTA.
+__device__ __forceinline__ bool last_block_done(uint32_t *counter, uint32_t total, int *flag) {
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const uint32_t prev = atomicAdd(counter, 1u);
+    *flag = (prev == total - 1u);
+    if (*flag) *counter = 0u;
+  }
+  __syncthreads();
+  const bool last = *flag != 0;
+  if (last) __threadfence();
+  return last;
+}
+
+// ---------------------------------------------------------------------------
+// Camera table: R and dR/dw_k of the Rodrigues formula, evaluated exactly as
+// utils/geometry/rotation.h:133-199 does on forward-mode duals (theta^2 >
+// DBL_EPSILON branch and first-order branch), once per camera.  Per
+// observation R*X and dR_k*X then reproduce the dual-number Jacobian of the
+// rotation, including its rounding near the branch point.
+// ---------------------------------------------------------------------------
+struct J3 {
+  double a, d0, d1, d2;
+};
+__device__ __forceinline__ J3 j3c(double a) { return J3{a, 0.0, 0.0, 0.0}; }
+__device__ __forceinline__ J3 j3add(J3 x, J3 y) { return J3{x.a + y.a, x.d0 + y.d0, x.d1 + y.d1, x.d2 + y.d2}; }
+__device__ __forceinline__ J3 j3sub(J3 x, J3 y) { return J3{x.a - y.a, x.d0 - y.d0, x.d1 - y.d1, x.d2 - y.d2}; }
+__device__ __forceinline__ J3 j3mul(J3 x, J3 y) {
+  return J3{x.a * y.a, x.a * y.d0 + x.d0 * y.a, x.a * y.d1 + x.d1 * y.a, x.a * y.d2 + x.d2 * y.a};
+}
+
+// Fills tab[0..8] = R (row-major), tab[9 + 9k + 3i + j] = dR_k[i][j].
+__device__ inline void rotation_and_derivatives(const double *aa_in, double *tab) {
+  const J3 aa[3] = {J3{aa_in[0], 1.0, 0.0, 0.0}, J3{aa_in[1], 0.0, 1.0, 0.0}, J3{aa_in[2], 0.0, 0.0, 1.0}};
+  const J3 theta2 = j3add(j3add(j3mul(aa[0], aa[0]), j3mul(aa[1], aa[1])), j3mul(aa[2], aa[2]));
+  if (theta2.a > DBL_EPSILON) {
+    // theta = sqrt(theta2), c = cos, s = sin, inv = 1/theta (dual rules)
+    const double th = sqrt(theta2.a);
+    const double fth = 1.0 / (2.0 * th);
+    const J3 theta{th, theta2.d0 * fth, theta2.d1 * fth, theta2.d2 * fth};
+    double sv, cv;
+    sincos(theta.a, &sv, &cv);
+    const double mcs = -sv;
+    const J3 c{cv, mcs * theta.d0, mcs * theta.d1, mcs * theta.d2};
+    const J3 s{sv, cv * theta.d0, cv * theta.d1, cv * theta.d2};
+    const double fi = -1.0 / (theta.a * theta.a);
+    const J3 inv{1.0 / theta.a, theta.d0 * fi, theta.d1 * fi, theta.d2 * fi};
+    const J3 w[3] = {j3mul(aa[0], inv), j3mul(aa[1], inv), j3mul(aa[2], inv)};
+    const J3 omc = j3sub(j3c(1.0), c);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const J3 pt[3] = {j3c(j == 0 ? 1.0 : 0.0), j3c(j == 1 ? 1.0 : 0.0), j3c(j == 2 ? 1.0 : 0.0)};
+      const J3 wx[3] = {j3sub(j3mul(w[1], pt[2]), j3mul(w[2], pt[1])),
+                        j3sub(j3mul(w[2], pt[0]), j3mul(w[0], pt[2])),
+                        j3sub(j3mul(w[0], pt[1]), j3mul(w[1], pt[0]))};
+      const J3 dot = j3add(j3add(j3mul(w[0], pt[0]), j3mul(w[1], pt[1])), j3mul(w[2], pt[2]));
+      const J3 tmp = j3mul(dot, omc);
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        const J3 res = j3add(j3add(j3mul(pt[i], c), j3mul(wx[i], s)), j3mul(w[i], tmp));
+        tab[3 * i + j] = res.a;
+        tab[9 + 0 + 3 * i + j] = res.d0;
+        tab[9 + 9 + 3 * i + j] = res.d1;
+        tab[9 + 18 + 3 * i + j] = res.d2;
+      }
+    }
+  } else {
+    // R X = X + w x X:  R = I + [w]_x,  dR_k X = e_k x X
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const J3 pt[3] = {j3c(j == 0 ? 1.0 : 0.0), j3c(j == 1 ? 1.0 : 0.0), j3c(j == 2 ? 1.0 : 0.0)};
+      const J3 wx[3] = {j3sub(j3mul(aa[1], pt[2]), j3mul(aa[2], pt[1])),
+                        j3sub(j3mul(aa[2], pt[0]), j3mul(aa[0], pt[2])),
+                        j3sub(j3mul(aa[0], pt[1]), j3mul(aa[1], pt[0]))};
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        const J3 res = j3add(pt[i], wx[i]);
+        tab[3 * i + j] = res.a;
+        tab[9 + 0 + 3 * i + j] = res.d0;
+        tab[9 + 9 + 3 * i + j] = res.d1;
+        tab[9 + 18 + 3 * i + j] = res.d2;
+      }
+    }
+  }
+}
+
+// R only (candidate-point cost evaluation).  Must produce bit-identical R to
+// rotation_and_derivatives, so it runs the same code and drops the rest.
+__device__ inline void camera_table_entry(const double *cam, double *tab, bool derivatives) {
+  double t[kCamTable];
+  rotation_and_derivatives(cam, t);
+  const int n = derivatives ? 36 : 9;
+  for (int k = 0; k < n; ++k) tab[k] = t[k];
+  tab[36] = cam[3];
+  tab[37] = cam[4];
+  tab[38] = cam[5];
+  tab[39] = cam[6];
+  tab[40] = cam[7];
+  tab[41] = cam[8];
+}
+
+// ---------------------------------------------------------------------------
+// Snavely projection (utils/camera/SnavelyReprojectionError.h:61-87) on the
+// camera table: P = R X + t; x' = -P_x/P_z; d = 1 + r2 (k1 + k2 r2);
+// prediction = f d x'.  Residual = prediction - observation (:49-50).
+// ---------------------------------------------------------------------------
+struct Proj {
+  double P[3];
+  double xp, yp, r2, dist, f, k1, k2;
+  double ru, rv;
+};
+
+__device__ __forceinline__ void project(const double *tab, const double *X, double2 uv, Proj &o) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+    o.P[i] = tab[3 * i + 0] * X[0] + tab[3 * i + 1] * X[1] + tab[3 * i + 2] * X[2] + tab[36 + i];
+  o.xp = -o.P[0] / o.P[2];
+  o.yp = -o.P[1] / o.P[2];
+  o.f = tab[39];
+  o.k1 = tab[40];
+  o.k2 = tab[41];
+  o.r2 = o.xp * o.xp + o.yp * o.yp;
+  o.dist = 1.0 + o.r2 * (o.k1 + o.k2 * o.r2);
+  o.ru = o.f * o.dist * o.xp - uv.x;
+  o.rv = o.f * o.dist * o.yp - uv.y;
+}
+
+// Ceres robust-loss rho(s) (LossFunction::Evaluate) for trivial, Huber(a),
+// Cauchy(a).
+__device__ __forceinline__ void loss_rho(int loss, double a, double s, double rho[3]) {
+  if (loss == GBA_LOSS_HUBER) {
+    const double b = a * a;
+    if (s > b) {
+      const double r = sqrt(s);
+      rho[0] = 2.0 * a * r - b;
+      rho[1] = fmax(DBL_MIN, a / r);
+      rho[2] = -rho[1] / (2.0 * s);
+    } else {
+      rho[0] = s;
+      rho[1] = 1.0;
+      rho[2] = 0.0;
+    }
+  } else if (loss == GBA_LOSS_CAUCHY) {
+    const double b = a * a, c = 1.0 / b;
+    const double sum = 1.0 + s * c;
+    const double inv = 1.0 / sum;
+    rho[0] = b * log(sum);
+    rho[1] = fmax(DBL_MIN, inv);
+    rho[2] = -c * (inv * inv);
+  } else {
+    rho[0] = s;
+    rho[1] = 1.0;
+    rho[2] = 0.0;
+  }
+}
+
+__device__ __forceinline__ double block_cost(int loss, double a, double ru, double rv) {
+  const double s = ru * ru + rv * rv;
+  if (loss == GBA_LOSS_TRIVIAL) return 0.5 * s;
+  double rho[3];
+  loss_rho(loss, a, s, rho);
+  return 0.5 * rho[0];
+}
+
+// Corrector of a residual block: r' = residual_scaling * r and
+// J' = sqrt_rho1 (J - alpha_sq_norm r r^T J).
+struct Corrector {
+  double sqrt_rho1, residual_scaling, alpha_sq_norm;
+};
+__device__ __forceinline__ Corrector make_corrector(int loss, double a, double ru, double rv) {
+  Corrector c{1.0, 1.0, 0.0};
+  if (loss == GBA_LOSS_TRIVIAL) return c;
+  const double s = ru * ru + rv * rv;
+  double rho[3];
+  loss_rho(loss, a, s, rho);
+  c.sqrt_rho1 = sqrt(rho[1]);
+  if (s == 0.0 || rho[2] <= 0.0) {
+    c.residual_scaling = c.sqrt_rho1;
+    c.alpha_sq_norm = 0.0;
+  } else {
+    const double D = 1.0 + 2.0 * s * rho[2] / rho[1];
+    const double alpha = 1.0 - sqrt(D);
+    c.residual_scaling = c.sqrt_rho1 / (1.0 - alpha);
+    c.alpha_sq_norm = alpha / s;
+  }
+  return c;
+}
+
+// Loads / stores of one observation's Jacobian columns from the SoA layout:
+// column k (k = 0..8 camera, 9..11 point) as a (d/du, d/dv) pair at
+// jac[k * no + o]; the corrected residual pair at jac[12 * no + o].
+template <typename R2>
+__device__ __forceinline__ R2 jload(const void *jac, int64_t no, int k, int64_t o) {
+  return reinterpret_cast<const R2 *>(jac)[(int64_t)k * no + o];
+}
+template <typename R2>
+__device__ __forceinline__ void jstore(void *jac, int64_t no, int k, int64_t o, R2 v) {
+  reinterpret_cast<R2 *>(jac)[(int64_t)k * no + o] = v;
+}
+
+// 3x3 symmetric positive-definite inverse via Cholesky (FP64).  In/out in the
+// packed sym3 order.  Returns false when not positive definite.
+__device__ __forceinline__ bool spd_inverse3(const double *C, double *Ci) {
+  const double l00s = C[0];
+  if (!(l00s > 0.0)) return false;
+  const double l00 = sqrt(l00s);
+  const double l10 = C[1] / l00;
+  const double l20 = C[2] / l00;
+  const double l11s = C[3] - l10 * l10;
+  if (!(l11s > 0.0)) return false;
+  const double l11 = sqrt(l11s);
+  const double l21 = (C[4] - l20 * l10) / l11;
+  const double l22s = C[5] - l20 * l20 - l21 * l21;
+  if (!(l22s > 0.0)) return false;
+  const double l22 = sqrt(l22s);
+  // Y = L^{-1}
+  const double y00 = 1.0 / l00;
+  const double y11 = 1.0 / l11;
+  const double y22 = 1.0 / l22;
+  const double y10 = -(l10 * y00) / l11;
+  const double y21 = -(l21 * y11) / l22;
+  const double y20 = -(l20 * y00 + l21 * y10) / l22;
+  // Ci = Y^T Y
+  Ci[0] = y00 * y00 + y10 * y10 + y20 * y20;
+  Ci[1] = y10 * y11 + y20 * y21;
+  Ci[2] = y20 * y22;
+  Ci[3] = y11 * y11 + y21 * y21;
+  Ci[4] = y21 * y22;
+  Ci[5] = y22 * y22;
+  return isfinite(Ci[0]) && isfinite(Ci[3]) && isfinite(Ci[5]);
+}
+
+// ---------------------------------------------------------------------------
+// Trace helper (LM iteration `it` of problem p).
+__device__ __forceinline__ void trace_put(const DeviceBatch &B, int p, int it, double cost,
+                                          double radius, int pcg, int succ) {
+  if (it < 0 || it >= B.trace_cap) return;
+  const size_t k = (size_t)p * B.trace_cap + it;
+  B.trace_cost[k] = cost;
+  B.trace_radius[k] = radius;
+  B.trace_pcg[k] = pcg;
+  B.trace_succ[k] = succ;
+}
+
+}  // namespace gba

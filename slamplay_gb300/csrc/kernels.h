@@ -1,0 +1,45 @@
+// kernels.h — host-side launchers of the libgba kernels (one per kernel
+// family; the precision mode picks the template instance).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "gba_internal.h"
+
+namespace gba {
+
+// LM state initialisation (per problem).
+void launch_init_state(const DeviceBatch &b, cudaStream_t s);
+// K0: camera tables (R, dR/dw, t, f, k1, k2) of the current parameters.
+void launch_camera_table(const DeviceBatch &b, cudaStream_t s);
+// K1 + K1c: residuals, scaled & corrected Jacobian, point blocks (chunk
+// kernel) and camera blocks (camera kernel).  norms = first pass of the
+// solve: unscaled column norms only.
+void launch_eval_jacobian(const DeviceBatch &b, bool mixed, bool norms, cudaStream_t s);
+// Jacobi scaling from the column norms of the first pass.
+void launch_scale_init(const DeviceBatch &b, cudaStream_t s);
+// K7: per-problem cost / gradient / |x| after a Jacobian evaluation, the
+// trust-region termination tests, and the LM loop condition.
+void launch_post_eval(const DeviceBatch &b, cudaStream_t s);
+// K3a: damped point blocks, their FP64 inverses, Cinv g_p.
+void launch_point_prepare(const DeviceBatch &b, bool mixed, cudaStream_t s);
+// K3b: camera-diagonal Schur blocks, reduced rhs, block-Jacobi inverse, PCG init.
+void launch_camera_schur(const DeviceBatch &b, bool mixed, cudaStream_t s);
+// K4a-c: one PCG iteration (implicit Schur mat-vec, camera reduce, update).
+void launch_pcg_iteration(const DeviceBatch &b, bool mixed, cudaStream_t s);
+void launch_schur_matvec(const DeviceBatch &b, bool mixed, cudaStream_t s);
+void launch_camera_reduce(const DeviceBatch &b, cudaStream_t s);
+void launch_pcg_update(const DeviceBatch &b, cudaStream_t s);
+// K5: point back-substitution, model cost change, candidate points.
+void launch_back_substitute(const DeviceBatch &b, bool mixed, cudaStream_t s);
+// K5b + K2: candidate cameras (+ their tables) and the candidate cost.
+void launch_candidate_cost(const DeviceBatch &b, cudaStream_t s);
+// K6: accept / reject, trust-region radius update, termination tests.
+void launch_decide(const DeviceBatch &b, cudaStream_t s);
+// Copies the uploaded initial parameters into both working buffers.
+void launch_sync_param_buffers(const DeviceBatch &b, cudaStream_t s);
+// Gathers each problem's current parameters (the buffer its parity selects)
+// into out_cam (9 per camera) / out_pt (4 per point).
+void launch_gather_results(const DeviceBatch &b, double *out_cam, double *out_pt, cudaStream_t s);
+
+}  // namespace gba

@@ -1,0 +1,272 @@
+// prep.cpp — host-side layout of a batch of BAL problems.
+//
+// Input: the BALProblem arrays of each problem (utils/datasets/BALProblem.h:
+// 109-118), in any observation order.  Output: observations sorted by
+// (internal point, camera, input index) — point-major as BAL files usually
+// are (data/bal/ladybug49.txt) — with every point's observations contiguous;
+// chunks of whole points; per chunk the camera-sorted order of its
+// observations and its camera segments; per camera its segments and its
+// observations.  All orderings are deterministic functions of the input.
+#include "prep.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+
+namespace gba {
+
+static std::string fmt(const char *f, long long a, long long b = 0, long long c = 0) {
+  char buf[256];
+  std::snprintf(buf, sizeof buf, f, a, b, c);
+  return buf;
+}
+
+gba_status validate_problem(const gba_problem_view *v, std::string *err) {
+  if (!v) {
+    *err = "null problem view";
+    return GBA_ERR_INVALID_ARGUMENT;
+  }
+  if (v->num_cameras < 0 || v->num_points < 0 || v->num_observations < 0) {
+    *err = "negative problem size";
+    return GBA_ERR_INVALID_ARGUMENT;
+  }
+  if (v->num_observations > 0 &&
+      (!v->camera_index || !v->point_index || !v->observations))
+    return *err = "null observation array", GBA_ERR_INVALID_ARGUMENT;
+  if ((v->num_cameras > 0 || v->num_points > 0) && !v->parameters)
+    return *err = "null parameter array", GBA_ERR_INVALID_ARGUMENT;
+  const int nc = v->num_cameras, np = v->num_points;
+  for (int i = 0; i < v->num_observations; ++i) {
+    const int c = v->camera_index[i], p = v->point_index[i];
+    if (c < 0 || c >= nc) {
+      *err = fmt("observation %lld: camera index %lld out of range [0, %lld)", i, c, nc);
+      return GBA_ERR_INVALID_ARGUMENT;
+    }
+    if (p < 0 || p >= np) {
+      *err = fmt("observation %lld: point index %lld out of range [0, %lld)", i, p, np);
+      return GBA_ERR_INVALID_ARGUMENT;
+    }
+    if (!std::isfinite(v->observations[2 * i]) || !std::isfinite(v->observations[2 * i + 1])) {
+      *err = fmt("observation %lld is not finite", i);
+      return GBA_ERR_NON_FINITE;
+    }
+  }
+  const long long npar = 9LL * nc + 3LL * np;
+  for (long long k = 0; k < npar; ++k)
+    if (!std::isfinite(v->parameters[k])) {
+      *err = fmt("parameter %lld is not finite", k);
+      return GBA_ERR_NON_FINITE;
+    }
+  return GBA_OK;
+}
+
+gba_status prepare_batch(const gba_problem_view *views, int n, const PrepOptions &opt, HostBatch *out,
+                         std::string *err) {
+  HostBatch &hb = *out;
+  hb = HostBatch();
+  if (n <= 0 || !views) {
+    *err = "empty batch";
+    return GBA_ERR_INVALID_ARGUMENT;
+  }
+  const int cap = opt.chunk_cap;
+  long long tc = 0, tp = 0, to = 0;
+  for (int p = 0; p < n; ++p) {
+    const gba_status st = validate_problem(&views[p], err);
+    if (st != GBA_OK) {
+      if (n > 1) *err = fmt("problem %lld: ", p) + *err;
+      return st;
+    }
+    tc += views[p].num_cameras;
+    tp += views[p].num_points;
+    to += views[p].num_observations;
+  }
+  if (tc > (1LL << 30) || tp > (1LL << 30) || to > (1LL << 30)) {
+    *err = "batch too large for 32-bit indices";
+    return GBA_ERR_INVALID_ARGUMENT;
+  }
+  hb.P = n;
+  hb.nc = (int)tc;
+  hb.np = (int)tp;
+  hb.no = (int)to;
+  hb.prob.resize(n);
+  hb.obs_cam.resize(to);
+  hb.obs_pt.resize(to);
+  hb.obs_uv.resize(2 * to);
+  hb.obs_seg.resize(to);
+  hb.obs_slot.resize(to);
+  hb.obs_orig.resize(to);
+  hb.pt_obs_begin.assign(tp + 1, 0);
+  hb.pt_problem.resize(tp);
+  hb.cam_problem.resize(tc);
+  hb.pt_used.assign(tp, 0);
+  hb.cam_used.assign(tc, 0);
+  hb.pt_orig.resize(tp);
+  hb.cam_param.resize(9 * tc);
+  hb.pt_param.assign(4 * tp, 0.0);
+  hb.cam_obs_begin.assign(tc + 1, 0);
+  hb.cam_obs_list.resize(to);
+
+  int cam0 = 0, pt0 = 0, obs0 = 0;
+  std::vector<int32_t> deg, key, order, inv, fill, cams;
+  std::vector<std::pair<int, int>> tmp;
+  for (int p = 0; p < n; ++p) {
+    const gba_problem_view &v = views[p];
+    const int nc = v.num_cameras, np = v.num_points, no = v.num_observations;
+    ProblemInfo &pi = hb.prob[p];
+    pi.cam_begin = cam0;
+    pi.cam_count = nc;
+    pi.pt_begin = pt0;
+    pi.pt_count = np;
+    pi.obs_begin = obs0;
+    pi.obs_count = no;
+    pi.chunk_begin = (int)hb.chunk.size();
+    pi.seg_begin = (int)hb.seg_cam.size();
+    // degrees, first camera of each point
+    deg.assign(np, 0);
+    key.assign(np, nc);
+    for (int i = 0; i < no; ++i) {
+      const int c = v.camera_index[i], j = v.point_index[i];
+      ++deg[j];
+      if (c < key[j]) key[j] = c;
+      hb.cam_used[cam0 + c] = 1;
+    }
+    // internal point order: by first camera (locality of the camera
+    // segments in the chunk kernels), stable in the input index
+    order.resize(np);
+    if (opt.reorder_points) {
+      fill.assign(nc + 2, 0);
+      for (int j = 0; j < np; ++j) ++fill[key[j] + 1];
+      for (int c = 0; c <= nc; ++c) fill[c + 1] += fill[c];
+      for (int j = 0; j < np; ++j) order[fill[key[j]]++] = j;
+    } else {
+      for (int j = 0; j < np; ++j) order[j] = j;
+    }
+    inv.resize(np);
+    for (int ji = 0; ji < np; ++ji) inv[order[ji]] = ji;
+    // CSR by internal point, observations stable in input index
+    for (int ji = 0; ji < np; ++ji) {
+      const int j = order[ji];
+      hb.pt_orig[pt0 + ji] = j;
+      hb.pt_problem[pt0 + ji] = p;
+      hb.pt_used[pt0 + ji] = deg[j] > 0;
+      hb.pt_obs_begin[pt0 + ji + 1] = deg[j];
+      for (int q = 0; q < 3; ++q) hb.pt_param[4 * (size_t)(pt0 + ji) + q] = v.parameters[9 * (size_t)nc + 3 * (size_t)j + q];
+    }
+    hb.pt_obs_begin[pt0] = obs0;
+    for (int ji = 0; ji < np; ++ji) hb.pt_obs_begin[pt0 + ji + 1] += hb.pt_obs_begin[pt0 + ji];
+    fill.assign(hb.pt_obs_begin.begin() + pt0, hb.pt_obs_begin.begin() + pt0 + np + 1);
+    for (int i = 0; i < no; ++i) hb.obs_orig[fill[inv[v.point_index[i]]]++] = i;
+    // within a point: by camera, then input index (insertion sort, stable)
+    for (int ji = 0; ji < np; ++ji) {
+      const int b = hb.pt_obs_begin[pt0 + ji], e = hb.pt_obs_begin[pt0 + ji + 1];
+      for (int k = b + 1; k < e; ++k) {
+        const int x = hb.obs_orig[k];
+        const int cx = v.camera_index[x];
+        int m = k - 1;
+        while (m >= b && v.camera_index[hb.obs_orig[m]] > cx) {
+          hb.obs_orig[m + 1] = hb.obs_orig[m];
+          --m;
+        }
+        hb.obs_orig[m + 1] = x;
+      }
+    }
+    for (int k = obs0; k < obs0 + no; ++k) {
+      const int i = hb.obs_orig[k];
+      hb.obs_cam[k] = cam0 + v.camera_index[i];
+      hb.obs_pt[k] = pt0 + inv[v.point_index[i]];
+      hb.obs_uv[2 * (size_t)k] = v.observations[2 * (size_t)i];
+      hb.obs_uv[2 * (size_t)k + 1] = v.observations[2 * (size_t)i + 1];
+    }
+    for (int c = 0; c < nc; ++c) {
+      hb.cam_problem[cam0 + c] = p;
+      for (int q = 0; q < 9; ++q) hb.cam_param[9 * (size_t)(cam0 + c) + q] = v.parameters[9 * (size_t)c + q];
+    }
+    // chunks of whole points
+    int ji = 0;
+    while (ji < np) {
+      ChunkInfo ci;
+      std::memset(&ci, 0, sizeof ci);
+      ci.problem = p;
+      ci.pt_begin = pt0 + ji;
+      ci.obs_begin = hb.pt_obs_begin[pt0 + ji];
+      int nobs = 0, npts = 0;
+      while (ji < np && npts < cap) {
+        const int d = hb.pt_obs_begin[pt0 + ji + 1] - hb.pt_obs_begin[pt0 + ji];
+        if (d > cap) {
+          *err = fmt("point %lld is observed %lld times; at most %lld observations per point are supported",
+                     order[ji], d, cap);
+          return GBA_ERR_INVALID_ARGUMENT;
+        }
+        if (nobs + d > cap) break;
+        nobs += d;
+        ++npts;
+        ++ji;
+      }
+      ci.obs_count = nobs;
+      ci.pt_count = npts;
+      // camera-sorted order of the chunk's observations, stable
+      tmp.resize(nobs);
+      for (int k = 0; k < nobs; ++k) tmp[k] = std::make_pair(hb.obs_cam[ci.obs_begin + k], k);
+      std::stable_sort(tmp.begin(), tmp.end(),
+                       [](const std::pair<int, int> &a, const std::pair<int, int> &b) { return a.first < b.first; });
+      ci.seg_begin = (int)hb.seg_cam.size();
+      int segs = 0;
+      for (int k = 0; k < nobs; ++k) {
+        if (k == 0 || tmp[k].first != tmp[k - 1].first) {
+          hb.seg_pos.push_back((uint16_t)k);
+          hb.seg_cam.push_back(tmp[k].first);
+          ++segs;
+        }
+        hb.obs_slot[ci.obs_begin + tmp[k].second] = (uint16_t)k;
+        hb.obs_seg[ci.obs_begin + tmp[k].second] = (uint16_t)(segs - 1);
+      }
+      ci.seg_count = segs;
+      hb.chunk.push_back(ci);
+    }
+    pi.chunk_count = (int)hb.chunk.size() - pi.chunk_begin;
+    pi.seg_count = (int)hb.seg_cam.size() - pi.seg_begin;
+    // camera blocks of the PCG kernels
+    pi.cam_block_begin = (int)hb.camblk.size();
+    for (int c = 0; c < nc; c += kCamPerBlock) {
+      int4 b;
+      b.x = p;
+      b.y = cam0 + c;
+      b.z = std::min(kCamPerBlock, nc - c);
+      b.w = 0;
+      hb.camblk.push_back(b);
+    }
+    pi.cam_block_count = (int)hb.camblk.size() - pi.cam_block_begin;
+    cam0 += nc;
+    pt0 += np;
+    obs0 += no;
+  }
+  hb.nchunks = (int)hb.chunk.size();
+  hb.nseg = (int)hb.seg_cam.size();
+  hb.cam_blocks = (int)hb.camblk.size();
+  // per camera: its segments (chunk order) and its observations (internal order)
+  hb.cam_seg_begin.assign(hb.nc + 1, 0);
+  for (int s = 0; s < hb.nseg; ++s) ++hb.cam_seg_begin[hb.seg_cam[s] + 1];
+  for (int c = 0; c < hb.nc; ++c) hb.cam_seg_begin[c + 1] += hb.cam_seg_begin[c];
+  hb.cam_seg_list.resize(hb.nseg);
+  fill.assign(hb.cam_seg_begin.begin(), hb.cam_seg_begin.end());
+  for (int s = 0; s < hb.nseg; ++s) hb.cam_seg_list[fill[hb.seg_cam[s]]++] = s;
+  for (int k = 0; k < hb.no; ++k) ++hb.cam_obs_begin[hb.obs_cam[k] + 1];
+  for (int c = 0; c < hb.nc; ++c) hb.cam_obs_begin[c + 1] += hb.cam_obs_begin[c];
+  fill.assign(hb.cam_obs_begin.begin(), hb.cam_obs_begin.end());
+  for (int k = 0; k < hb.no; ++k) hb.cam_obs_list[fill[hb.obs_cam[k]]++] = k;
+  return GBA_OK;
+}
+
+void scatter_parameters(const HostBatch &hb, int p, const double *cam_param, const double *pt_param,
+                        double *out) {
+  const ProblemInfo &pi = hb.prob[p];
+  std::memcpy(out, cam_param + 9 * (size_t)pi.cam_begin, sizeof(double) * 9 * (size_t)pi.cam_count);
+  double *pts = out + 9 * (size_t)pi.cam_count;
+  for (int ji = 0; ji < pi.pt_count; ++ji) {
+    const int j = hb.pt_orig[pi.pt_begin + ji];
+    for (int q = 0; q < 3; ++q) pts[3 * (size_t)j + q] = pt_param[4 * (size_t)(pi.pt_begin + ji) + q];
+  }
+}
+
+}  // namespace gba

@@ -1,0 +1,51 @@
+// prep.h — host-side preparation of a batch of BAL problems into the
+// device layout (observation orderings, point-segment chunks, camera
+// segments).  Pure host code, testable without a GPU.
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "gba_internal.h"
+
+namespace gba {
+
+struct PrepOptions {
+  int chunk_cap = kChunkCap;  // observations per chunk (CTA)
+  bool reorder_points = true; // group points by their first camera
+};
+
+struct HostBatch {
+  int P = 0, nc = 0, np = 0, no = 0, nchunks = 0, nseg = 0, cam_blocks = 0;
+  std::vector<ProblemInfo> prob;
+  std::vector<ChunkInfo> chunk;
+  std::vector<int32_t> obs_cam, obs_pt;
+  std::vector<double> obs_uv;  // 2 per observation
+  std::vector<uint16_t> obs_seg, obs_slot;
+  std::vector<int32_t> pt_obs_begin, pt_problem, cam_problem;
+  std::vector<uint8_t> pt_used, cam_used;
+  std::vector<uint16_t> seg_pos;
+  std::vector<int32_t> seg_cam;
+  std::vector<int32_t> cam_seg_begin, cam_seg_list, cam_obs_begin, cam_obs_list;
+  std::vector<int4> camblk;
+  // output mapping
+  std::vector<int32_t> obs_orig;  // internal observation -> index in its problem's input
+  std::vector<int32_t> pt_orig;   // internal point -> point index in its problem's input
+  // initial parameters in the internal layout
+  std::vector<double> cam_param;  // 9 per camera
+  std::vector<double> pt_param;   // 4 per point
+};
+
+// Validates and lays out `n` problems.  Returns GBA_OK or an error with a
+// message in *err.
+gba_status prepare_batch(const gba_problem_view *views, int n, const PrepOptions &opt, HostBatch *out,
+                         std::string *err);
+
+// Checks one problem view (sizes, pointers, indices, finiteness).
+gba_status validate_problem(const gba_problem_view *v, std::string *err);
+
+// Writes the internal-layout parameters of problem p back to the caller's array.
+void scatter_parameters(const HostBatch &hb, int p, const double *cam_param, const double *pt_param,
+                        double *out);
+
+}  // namespace gba

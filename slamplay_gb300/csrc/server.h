@@ -1,0 +1,75 @@
+// server.h — continuous-batching request loop over several engine slots.
+#pragma once
+
+#include <condition_variable>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "engine.h"
+
+namespace gba {
+
+class Server {
+ public:
+  explicit Server(const gba_options &o) : o_(o) {}
+  ~Server() { stop(); }
+
+  // Estimated device bytes of one problem (admission rule).
+  static size_t estimate_footprint(int nc, int np, int no, bool mixed);
+
+  gba_status start(size_t budget, int max_live, int max_queue, std::string *err);
+  gba_status submit(const gba_problem_view *p, uint64_t *ticket, std::string *err);
+  gba_status poll(uint64_t ticket, gba_summary *s, int32_t *done, std::string *err);
+  gba_status drain_and_stop(std::string *err);
+  void stop();
+  bool running() const { return running_; }
+  void stats(gba_server_stats *st);
+
+ private:
+  struct Request {
+    uint64_t ticket;
+    gba_problem_view view;
+    size_t footprint;
+    gba_summary summary;
+    gba_status status = GBA_OK;
+    std::string error;
+    bool done = false;
+  };
+  struct Slot {
+    std::unique_ptr<Engine> engine;
+    std::vector<std::shared_ptr<Request>> reqs;
+    std::vector<gba_problem_view> views;
+    HostBatch hb;
+    cudaEvent_t done_ev = nullptr;
+    size_t bytes = 0;
+    bool busy = false;
+    double t_start = 0.0;
+  };
+  void loop();
+  bool launch_cohort(Slot &s, std::vector<std::shared_ptr<Request>> &&reqs);
+  void retire(Slot &s);
+
+  gba_options o_;
+  std::thread thread_;
+  std::mutex mu_;
+  std::condition_variable cv_;
+  std::condition_variable done_cv_;
+  std::deque<std::shared_ptr<Request>> queue_;
+  std::map<uint64_t, std::shared_ptr<Request>> tickets_;
+  std::vector<Slot> slots_;
+  uint64_t next_ticket_ = 1;
+  size_t budget_ = 0;
+  int max_live_ = 0, max_queue_ = 0;
+  bool running_ = false, stopping_ = false;
+  std::string init_error_;
+  gba_status init_status_ = GBA_OK;
+  bool init_done_ = false;
+  gba_server_stats st_{};
+};
+
+}  // namespace gba

@@ -1,0 +1,241 @@
+"""GPU bundle-adjustment solver: the Python side of include/gba.h.
+
+``solve_ba(bal_problem)`` is the drop-in for the reference's
+``void SolveBA(BALProblem&)`` (backend/slam_ba_simple_g2o_ceres/
+test_bundle_adjustment_ceres.cpp:58-101): one Snavely residual block per
+observation with HuberLoss(1.0), Levenberg-Marquardt with the points
+eliminated, parameters updated in place, and a report of the fields
+Ceres' ``Summary::FullReport()`` prints.
+"""
+from __future__ import annotations
+
+import dataclasses
+from typing import Sequence
+
+import numpy as np
+
+from . import _native as N
+from .bal_problem import BALProblem
+
+
+@dataclasses.dataclass
+class SolveSummary:
+    initial_cost: float
+    final_cost: float
+    num_iterations: int
+    num_successful_steps: int
+    num_unsuccessful_steps: int
+    num_invalid_steps: int
+    num_linear_solver_iterations: int
+    termination_type: str
+    termination_reason: str
+    final_trust_region_radius: float
+    gradient_max_norm: float
+    setup_time_s: float
+    solve_time_s: float
+    total_time_s: float
+    trace_cost: np.ndarray
+    trace_radius: np.ndarray
+    trace_linear_iterations: np.ndarray
+    trace_successful: np.ndarray
+
+    def FullReport(self) -> str:
+        return (
+            "GB300 bundle adjustment report\n"
+            f"  Initial cost          {self.initial_cost:.6e}\n"
+            f"  Final cost            {self.final_cost:.6e}\n"
+            f"  Change                {self.initial_cost - self.final_cost:.6e}\n"
+            f"  Minimizer iterations  {self.num_iterations}\n"
+            f"  Successful steps      {self.num_successful_steps}\n"
+            f"  Unsuccessful steps    {self.num_unsuccessful_steps}\n"
+            f"  Linear solver iters   {self.num_linear_solver_iterations}\n"
+            f"  Solve time (s)        {self.solve_time_s:.6f}\n"
+            f"  Total time (s)        {self.total_time_s:.6f}\n"
+            f"  Termination           {self.termination_type} ({self.termination_reason})\n")
+
+
+class _Trace:
+    def __init__(self, cap: int):
+        self.cost = np.zeros(cap)
+        self.radius = np.zeros(cap)
+        self.lin = np.zeros(cap, np.int32)
+        self.succ = np.zeros(cap, np.int32)
+
+    def attach(self, s: N.Summary) -> None:
+        s.trace_capacity = len(self.cost)
+        s.trace_cost = N.f64p(self.cost)
+        s.trace_radius = N.f64p(self.radius)
+        s.trace_linear_iterations = N.i32p(self.lin)
+        s.trace_successful = N.i32p(self.succ)
+
+
+def _summary(s: N.Summary, tr: _Trace | None) -> SolveSummary:
+    n = s.trace_length if tr is not None else 0
+    return SolveSummary(
+        initial_cost=s.initial_cost, final_cost=s.final_cost, num_iterations=s.num_iterations,
+        num_successful_steps=s.num_successful_steps, num_unsuccessful_steps=s.num_unsuccessful_steps,
+        num_invalid_steps=s.num_invalid_steps, num_linear_solver_iterations=s.num_linear_solver_iterations,
+        termination_type=N.TERMINATION.get(s.termination_type, str(s.termination_type)),
+        termination_reason=N.REASON.get(s.termination_reason, str(s.termination_reason)),
+        final_trust_region_radius=s.final_trust_region_radius, gradient_max_norm=s.gradient_max_norm,
+        setup_time_s=s.setup_time_s, solve_time_s=s.solve_time_s, total_time_s=s.total_time_s,
+        trace_cost=tr.cost[:n].copy() if tr else np.zeros(0),
+        trace_radius=tr.radius[:n].copy() if tr else np.zeros(0),
+        trace_linear_iterations=tr.lin[:n].copy() if tr else np.zeros(0, np.int32),
+        trace_successful=tr.succ[:n].copy() if tr else np.zeros(0, np.int32))
+
+
+def make_options(**kw) -> N.Options:
+    """gba_options with Ceres' defaults, overridden by keyword (loss and
+    precision accept names: loss='huber', precision='mixed')."""
+    o = N.Options()
+    N.lib().gba_options_init(N.C.byref(o))
+    for k, v in kw.items():
+        if k == "loss" and isinstance(v, str):
+            v = N.LOSS[v]
+        elif k == "precision" and isinstance(v, str):
+            v = N.PRECISION[v]
+        elif k == "pcg_criterion" and isinstance(v, str):
+            v = N.PCG_CRITERION[v]
+        elif k == "stream" and v is not None and not isinstance(v, int):
+            v = int(v)
+        if not hasattr(o, k):
+            raise TypeError(f"unknown solver option {k!r}")
+        setattr(o, k, v)
+    return o
+
+
+class Solver:
+    """One GPU solver handle (gba_handle): a CUDA stream, a device workspace
+    reused across solves and the cached LM graph."""
+
+    def __init__(self, **options):
+        self.options = make_options(**options)
+        h = N.C.c_void_p()
+        N.check(N.lib().gba_create(N.C.byref(self.options), N.C.byref(h)), None, "gba_create")
+        self._h = h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            N.lib().gba_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _cap(self) -> int:
+        return max(1, self.options.max_num_iterations + 1)
+
+    def solve(self, problem: BALProblem) -> SolveSummary:
+        """ceres::Solve replacement; problem.parameters() updated in place."""
+        v = problem.view()
+        s = N.Summary()
+        tr = _Trace(self._cap())
+        tr.attach(s)
+        N.check(N.lib().gba_solve(self._h, N.C.byref(v), N.C.byref(s)), self._h, "gba_solve")
+        return _summary(s, tr)
+
+    def batch_solve(self, problems: Sequence[BALProblem]) -> list[SolveSummary]:
+        n = len(problems)
+        views = (N.ProblemView * n)(*[p.view() for p in problems])
+        sums = (N.Summary * n)()
+        trs = [_Trace(self._cap()) for _ in range(n)]
+        for s, t in zip(sums, trs):
+            t.attach(s)
+        N.check(N.lib().gba_batch_solve(self._h, views, n, sums), self._h, "gba_batch_solve")
+        return [_summary(s, t) for s, t in zip(sums, trs)]
+
+    def evaluate(self, problem: BALProblem):
+        """(residuals [no,2], jacobians [no,2,12], cost) evaluated on the GPU."""
+        no = problem.num_observations()
+        r = np.zeros(2 * no)
+        J = np.zeros(24 * no)
+        c = N.C.c_double()
+        N.check(N.lib().gba_evaluate(self._h, N.C.byref(problem.view()), N.f64p(r), N.f64p(J), N.C.byref(c)),
+                self._h, "gba_evaluate")
+        return r.reshape(no, 2), J.reshape(no, 2, 12), c.value
+
+    def compute_step(self, problem: BALProblem, radius: float):
+        """One LM linear solve: (delta, model_cost_change, pcg_iterations)."""
+        d = np.zeros(problem.num_parameters())
+        m = N.C.c_double()
+        it = N.C.c_int32()
+        N.check(N.lib().gba_compute_step(self._h, N.C.byref(problem.view()), float(radius), N.f64p(d),
+                                         N.C.byref(m), N.C.byref(it)), self._h, "gba_compute_step")
+        return d, m.value, it.value
+
+    def solve_resident(self, repeats: int = 1) -> None:
+        """Re-run the last solved problem from its initial point on the device
+        (asynchronous; no host transfers)."""
+        N.check(N.lib().gba_solve_resident(self._h, int(repeats)), self._h, "gba_solve_resident")
+
+    def synchronize(self) -> None:
+        N.check(N.lib().gba_synchronize(self._h), self._h, "gba_synchronize")
+
+    # ---- profiling ---------------------------------------------------------
+    def set_profiling(self, on: bool) -> None:
+        N.check(N.lib().gba_set_profiling(self._h, 1 if on else 0), self._h)
+
+    def profile(self) -> list[dict]:
+        L = N.lib()
+        out = []
+        for i in range(L.gba_profile_count(self._h)):
+            name = N.C.c_char_p()
+            n = N.C.c_int64()
+            ms = N.C.c_double()
+            b = N.C.c_double()
+            N.check(L.gba_profile_entry(self._h, i, N.C.byref(name), N.C.byref(n), N.C.byref(ms), N.C.byref(b)))
+            out.append({"name": name.value.decode(), "launches": n.value, "total_ms": ms.value, "bytes": b.value})
+        return out
+
+    # ---- serving -------------------------------------------------------------
+    def start_server(self, device_budget_bytes: int = 0, max_live: int = 0, max_queue: int = 0) -> None:
+        N.check(N.lib().gba_server_start(self._h, device_budget_bytes, max_live, max_queue), self._h,
+                "gba_server_start")
+        self._pending: dict[int, BALProblem] = {}
+
+    def submit(self, problem: BALProblem) -> int:
+        t = N.C.c_uint64()
+        N.check(N.lib().gba_submit(self._h, N.C.byref(problem.view()), N.C.byref(t)), self._h, "gba_submit")
+        self._pending[t.value] = problem  # keep arrays alive until done
+        return t.value
+
+    def poll(self, ticket: int):
+        s = N.Summary()
+        done = N.C.c_int32()
+        N.check(N.lib().gba_poll(self._h, ticket, N.C.byref(s), N.C.byref(done)), self._h, "gba_poll")
+        if not done.value:
+            return None
+        self._pending.pop(ticket, None)
+        return _summary(s, None)
+
+    def stop_server(self) -> None:
+        N.check(N.lib().gba_server_stop(self._h), self._h, "gba_server_stop")
+
+    def server_stats(self) -> dict:
+        st = N.ServerStats()
+        N.check(N.lib().gba_server_get_stats(self._h, N.C.byref(st)), self._h)
+        return {k: getattr(st, k) for k, _ in N.ServerStats._fields_}
+
+
+def solve_ba(bal_problem: BALProblem, **options) -> SolveSummary:
+    """Drop-in for SolveBA(BALProblem&) (test_bundle_adjustment_ceres.cpp:58-101):
+    HuberLoss(1.0) per observation unless `loss` is given; other options are
+    Ceres' defaults unless overridden."""
+    options.setdefault("loss", "huber")
+    options.setdefault("loss_scale", 1.0)
+    with Solver(**options) as s:
+        return s.solve(bal_problem)
+
+
+def estimate_footprint(num_cameras: int, num_points: int, num_observations: int, precision: str = "fp64") -> int:
+    return int(N.lib().gba_estimate_footprint(num_cameras, num_points, num_observations, N.PRECISION[precision]))

@@ -1,0 +1,183 @@
+"""GPU kernels and solver vs the CPU oracle, through the C ABI (libgba.so).
+
+Tolerances (stated per test):
+  FP64 residual / Jacobian: |gpu - oracle| <= 1e-10 (1 + |row|_max) per entry
+  FP64 final cost: relative difference <= 1e-9 (the spec bar)
+  mixed final cost: relative difference <= 1e-6 from the FP64 oracle
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle_py as O
+from slamplay_gb300 import BALProblem, GBAError, Solver
+
+pytestmark = pytest.mark.gpu
+
+# Iteration-count runs: tolerances off so both sides run the stated number
+# of LM iterations (benchmark configurations "run N LM iterations").
+FIXED = dict(function_tolerance=0.0, gradient_tolerance=0.0, parameter_tolerance=0.0)
+
+
+def small_problem(config=0, **over):
+    return BALProblem.synthetic(config, seed=11, **over)
+
+
+def branch_problem():
+    """Cameras whose angle-axis norm sits on both sides of the reference's
+    theta^2 <= DBL_EPSILON branch (rotation.h:136), plus exactly zero."""
+    b = BALProblem.synthetic(0, seed=5, num_cameras=8, num_points=300)
+    cams = b.mutable_cameras().reshape(-1, 9)
+    rng = np.random.default_rng(3)
+    for i, th in enumerate([0.0, 1e-9, 1.0e-8, 1.45e-8, 1.5e-8, 1e-7, 1e-4, 2.0]):
+        axis = rng.normal(size=3)
+        axis /= np.linalg.norm(axis)
+        cams[i, :3] = axis * th
+    return b
+
+
+@pytest.mark.parametrize("make", [small_problem, branch_problem])
+def test_evaluate_fp64_matches_oracle(make):
+    b = make()
+    with Solver() as s:
+        r, J, cost = s.evaluate(b)
+    ro, Jo, co, ok = O.evaluate(O.Problem.from_bal(b))
+    assert ok
+    scale = 1.0 + np.abs(Jo).max(axis=2, keepdims=True)
+    assert np.all(np.abs(r - ro) <= 1e-10 * (1.0 + np.abs(ro))), np.abs(r - ro).max()
+    assert np.all(np.abs(J - Jo) <= 1e-10 * scale), np.abs(J - Jo).max()
+    assert abs(cost - co) <= 1e-12 * co
+
+
+def test_evaluate_mixed_matches_oracle():
+    b = small_problem()
+    with Solver(precision="mixed") as s:
+        r, J, cost = s.evaluate(b)
+    ro, Jo, co, _ = O.evaluate(O.Problem.from_bal(b))
+    scale = 1.0 + np.abs(Jo).max(axis=2, keepdims=True)
+    # residual stored in FP32 after an FP64 evaluation; J computed in FP32
+    assert np.all(np.abs(r - ro) <= 1e-6 * (1.0 + np.abs(ro)))
+    assert np.all(np.abs(J - Jo) <= 2e-5 * scale), np.abs(J - Jo).max()
+    assert abs(cost - co) <= 1e-12 * co  # cost is FP64 in both modes
+
+
+@pytest.mark.parametrize("loss", ["trivial", "huber"])
+def test_compute_step_matches_oracle(loss):
+    b = small_problem()
+    radius = 1e4
+    with Solver(loss=loss, pcg_tolerance=1e-12, max_linear_solver_iterations=1000) as s:
+        d, m, it = s.compute_step(b, radius)
+    p = O.Problem.from_bal(b)
+    do, mo, _, ok = O.compute_step(p, radius, loss=loss, linear_solver="pcg_schur", pcg_tolerance=1e-12,
+                                   max_linear_solver_iterations=1000)
+    assert ok and it > 0
+    rel = np.linalg.norm(d - do) / np.linalg.norm(do)
+    assert rel < 1e-8, rel
+    assert abs(m - mo) <= 1e-9 * abs(mo)
+    # and against the exact (dense Cholesky) Schur solve
+    dd, md, _, ok = O.compute_step(O.Problem.from_bal(b), radius, loss=loss, linear_solver="dense_schur")
+    assert ok
+    assert np.linalg.norm(d - dd) / np.linalg.norm(dd) < 1e-6
+
+
+def _solve_pair(b, gpu_opts, orc_opts):
+    g = b.copy()
+    with Solver(**gpu_opts) as s:
+        sg = s.solve(g)
+    po = O.Problem.from_bal(b)
+    so = O.solve(po, **orc_opts)
+    return g, sg, so
+
+
+@pytest.mark.parametrize("loss", ["trivial", "huber"])
+def test_solve_fp64_matches_oracle(loss):
+    b = small_problem()
+    opts = dict(max_num_iterations=20, loss=loss, **FIXED)
+    g, sg, so = _solve_pair(b, dict(opts, pcg_tolerance=1e-12, max_linear_solver_iterations=1000),
+                            dict(opts, linear_solver="dense_schur"))
+    assert abs(sg.initial_cost - so["initial_cost"]) <= 1e-12 * so["initial_cost"]
+    rel = abs(sg.final_cost - so["final_cost"]) / so["final_cost"]
+    assert rel <= 1e-9, (sg.final_cost, so["final_cost"], rel)
+    # the two cost histories agree until the cost stops changing
+    n = min(len(sg.trace_cost), len(so["trace_cost"]), 4)
+    np.testing.assert_allclose(sg.trace_cost[:n], so["trace_cost"][:n], rtol=1e-9)
+    dp = g.parameters() - so["parameters"]
+    print("camera RMS diff", np.sqrt(np.mean(dp[: 9 * b.num_cameras()] ** 2)),
+          "point RMS diff", np.sqrt(np.mean(dp[9 * b.num_cameras():] ** 2)))
+
+
+def test_solve_default_tolerances_same_termination():
+    b = small_problem()
+    g, sg, so = _solve_pair(b, dict(pcg_tolerance=1e-12, max_linear_solver_iterations=1000),
+                            dict(linear_solver="dense_schur"))
+    assert sg.num_iterations == so["num_iterations"]
+    assert sg.termination_type == "CONVERGENCE" and so["termination_type"] == 0
+    assert abs(sg.final_cost - so["final_cost"]) <= 1e-9 * so["final_cost"]
+
+
+def test_solve_mixed_within_1e6_of_fp64_oracle():
+    b = small_problem()
+    opts = dict(max_num_iterations=20, **FIXED)
+    g, sg, so = _solve_pair(b, dict(opts, precision="mixed", pcg_tolerance=1e-6, max_linear_solver_iterations=200),
+                            dict(opts, linear_solver="dense_schur"))
+    rel = abs(sg.final_cost - so["final_cost"]) / so["final_cost"]
+    assert rel <= 1e-6, rel
+
+
+def test_solve_is_deterministic_and_graph_equals_host_loop():
+    b = small_problem(num_points=800)
+    outs = []
+    for use_graphs in (1, 1, 0):
+        g = b.copy()
+        with Solver(max_num_iterations=10, use_graphs=use_graphs, **FIXED) as s:
+            sm = s.solve(g)
+        outs.append((g.parameters().copy(), sm.final_cost, sm.num_linear_solver_iterations))
+    for o in outs[1:]:
+        assert np.array_equal(o[0], outs[0][0])
+        assert o[1] == outs[0][1] and o[2] == outs[0][2]
+
+
+def test_batch_equals_alone_bitwise():
+    probs = [BALProblem.synthetic(3, index=i, seed=2) for i in range(4)]
+    alone = []
+    with Solver(max_num_iterations=8, **FIXED) as s:
+        for p in probs:
+            q = p.copy()
+            sm = s.solve(q)
+            alone.append((q.parameters().copy(), sm.final_cost))
+        qs = [p.copy() for p in probs]
+        sums = s.batch_solve(qs)
+    for (pa, ca), q, sm in zip(alone, qs, sums):
+        assert np.array_equal(pa, q.parameters())
+        assert ca == sm.final_cost
+
+
+def test_unobserved_blocks_unchanged():
+    b = small_problem(num_points=400)
+    # add one camera and one point that no observation uses
+    nc, np_ = b.num_cameras(), b.num_points()
+    params = np.concatenate([b.cameras(), [0.1, 0.2, 0.3, 1, 2, -10, 500, 0, 0], b.points(), [7.0, 8.0, 9.0]])
+    e = BALProblem.from_arrays(nc + 1, np_ + 1, b.camera_index(), b.point_index(), b.observations(), params)
+    before = e.parameters().copy()
+    with Solver(max_num_iterations=5) as s:
+        s.solve(e)
+    np.testing.assert_array_equal(e.parameters()[9 * nc: 9 * nc + 9], before[9 * nc: 9 * nc + 9])
+    np.testing.assert_array_equal(e.parameters()[-3:], before[-3:])
+
+
+def test_invalid_inputs_raise():
+    b = small_problem(num_points=100)
+    with Solver() as s:
+        bad = b.copy()
+        bad.camera_index()[3] = b.num_cameras()
+        with pytest.raises(GBAError) as ei:
+            s.solve(bad)
+        assert ei.value.status == 1
+        bad = b.copy()
+        bad.observations()[5] = np.nan
+        with pytest.raises(GBAError) as ei:
+            s.solve(bad)
+        assert ei.value.status == 3
+        # the handle stays usable after an error
+        ok = b.copy()
+        sm = s.solve(ok)
+        assert sm.final_cost < sm.initial_cost
