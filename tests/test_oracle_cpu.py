@@ -1,0 +1,107 @@
+"""The CPU oracle on its own: golden fixture, known answers, and independent
+cross-checks (finite differences, scipy least_squares)."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle_py as O
+from slamplay_gb300 import BALProblem
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "small_problem.npz")
+FIXED = dict(function_tolerance=0.0, gradient_tolerance=0.0, parameter_tolerance=0.0)
+
+
+def golden_problem():
+    g = np.load(GOLDEN)
+    return g, O.Problem(int(g["num_cameras"]), int(g["num_points"]), g["camera_index"], g["point_index"],
+                        g["observations"], g["parameters"])
+
+
+@pytest.mark.parametrize("loss", ["trivial", "huber"])
+def test_oracle_reproduces_golden_fixture(loss):
+    g, p = golden_problem()
+    r = O.solve(p, loss=loss, max_num_iterations=15, linear_solver="dense_schur", **FIXED)
+    np.testing.assert_allclose(r["trace_cost"], g[f"{loss}_trace_cost"], rtol=1e-12)
+    np.testing.assert_allclose(r["parameters"], g[f"{loss}_final_parameters"], rtol=1e-9, atol=1e-9)
+
+
+def test_jacobian_matches_central_differences():
+    b = BALProblem.synthetic(0, seed=2, num_points=30)
+    cams = b.cameras().reshape(-1, 9)
+    pts = b.points().reshape(-1, 3)
+    for i in range(0, b.num_observations(), 17):
+        cam = cams[b.camera_index()[i]].copy()
+        pt = pts[b.point_index()[i]].copy()
+        uv = b.observations()[2 * i: 2 * i + 2].copy()
+        r0, J = np.zeros(2), np.zeros(24)
+        O.oracle().orc_residual_jacobian(O.f64(cam), O.f64(pt), O.f64(uv), O.f64(r0), O.f64(J))
+        J = J.reshape(2, 12)
+        x = np.concatenate([cam, pt])
+        for k in range(12):
+            h = 1e-6 * max(1.0, abs(x[k]))
+            rr = []
+            for s in (+1, -1):
+                y = x.copy()
+                y[k] += s * h
+                r = np.zeros(2)
+                O.oracle().orc_residual_jacobian(O.f64(np.ascontiguousarray(y[:9])), O.f64(np.ascontiguousarray(y[9:])),
+                                                 O.f64(uv), O.f64(r), O.f64(np.zeros(24)))
+                rr.append(r)
+            fd = (rr[0] - rr[1]) / (2 * h)
+            assert np.allclose(J[:, k], fd, rtol=1e-5, atol=1e-5 * (1 + np.abs(J).max())), (k, J[:, k], fd)
+
+
+def test_zero_noise_problem_converges_to_zero_cost():
+    b, truth = BALProblem.synthetic(0, seed=5, num_points=400, pixel_noise=0.0, return_truth=True)
+    r = O.solve(O.Problem.from_bal(b), max_num_iterations=30, linear_solver="dense_schur")
+    assert r["initial_cost"] > 1e3
+    assert r["final_cost"] < 1e-12 * r["initial_cost"]
+
+
+def test_dense_and_pcg_schur_agree():
+    b = BALProblem.synthetic(0, seed=6, num_points=500)
+    a = O.solve(O.Problem.from_bal(b), max_num_iterations=10, linear_solver="dense_schur", **FIXED)
+    c = O.solve(O.Problem.from_bal(b), max_num_iterations=10, linear_solver="pcg_schur", pcg_tolerance=1e-13,
+                max_linear_solver_iterations=2000, **FIXED)
+    assert abs(a["final_cost"] - c["final_cost"]) <= 1e-10 * a["final_cost"]
+
+
+def test_huber_cost_formula():
+    b = BALProblem.synthetic(0, seed=7, num_points=100)
+    p = O.Problem.from_bal(b)
+    r, _, c_triv, _ = O.evaluate(p, "trivial")
+    _, _, c_hub, _ = O.evaluate(p, "huber", 1.0)
+    s = (r ** 2).sum(axis=1)
+    rho = np.where(s > 1.0, 2.0 * np.sqrt(s) - 1.0, s)
+    assert abs(c_triv - 0.5 * s.sum()) <= 1e-9 * c_triv
+    assert abs(c_hub - 0.5 * rho.sum()) <= 1e-9 * c_hub
+
+
+def test_final_cost_matches_scipy_least_squares():
+    scipy_opt = pytest.importorskip("scipy.optimize")
+    b = BALProblem.synthetic(0, seed=21, num_cameras=6, num_points=60)
+    p = O.Problem.from_bal(b)
+    x0 = b.parameters().copy()
+    nc = b.num_cameras()
+    ci, pi = b.camera_index(), b.point_index()
+
+    def fun(x):
+        q = O.Problem(nc, b.num_points(), ci, pi, b.observations(), x)
+        r, _, _, _ = O.evaluate(q)
+        return r.reshape(-1)
+
+    def jac(x):
+        q = O.Problem(nc, b.num_points(), ci, pi, b.observations(), x)
+        _, J, _, _ = O.evaluate(q)
+        full = np.zeros((2 * len(ci), x.size))
+        for i in range(len(ci)):
+            full[2 * i: 2 * i + 2, 9 * ci[i]: 9 * ci[i] + 9] = J[i, :, :9]
+            full[2 * i: 2 * i + 2, 9 * nc + 3 * pi[i]: 9 * nc + 3 * pi[i] + 3] = J[i, :, 9:]
+        return full
+
+    ls = scipy_opt.least_squares(fun, x0, jac=jac, method="trf", x_scale="jac", xtol=1e-15, ftol=1e-15,
+                                 gtol=1e-15, max_nfev=400)
+    r = O.solve(p, max_num_iterations=100, linear_solver="dense_schur", function_tolerance=1e-15,
+                parameter_tolerance=1e-15, gradient_tolerance=1e-15)
+    assert abs(r["final_cost"] - ls.cost) <= 1e-6 * ls.cost, (r["final_cost"], ls.cost)
