@@ -45,11 +45,13 @@ enum ProfSlot {
   PF_DECIDE,
   PF_TABLE,
   PF_SETUP_MISC,
+  PF_PERSISTENT,
   PF_COUNT
 };
-const char *kProfNames[PF_COUNT] = {"eval_jacobian",  "post_eval",    "point_prepare", "camera_schur",
-                                    "schur_matvec",   "camera_reduce", "pcg_update",   "back_substitute",
-                                    "candidate_cost", "decide",        "camera_table", "setup_misc"};
+const char *kProfNames[PF_COUNT] = {"eval_jacobian",  "post_eval",     "point_prepare", "camera_schur",
+                                    "schur_matvec",   "camera_reduce", "pcg_update",    "back_substitute",
+                                    "candidate_cost", "decide",        "camera_table",  "setup_misc",
+                                    "pcg_persistent"};
 
 double now_s() {
   return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
@@ -112,6 +114,49 @@ gba_status Engine::init(std::string *err) {
     if ((st = check(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "stream", err)) != GBA_OK) return st;
   for (cudaEvent_t *e : {&ev_start_, &ev_stop_, &pev_[0], &pev_[1]})
     if ((st = check(cudaEventCreate(e), "event", err)) != GBA_OK) return st;
+  if ((st = check(cudaDeviceGetAttribute(&sm_count_, cudaDevAttrMultiProcessorCount, device_), "SM count", err)) !=
+      GBA_OK)
+    return st;
+  int coop = 0;
+  cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device_);
+  pcg_occupancy_ = coop ? pcg_persistent_blocks_per_sm(mixed_) : 0;
+  if (pcg_occupancy_ <= 0) o_.persistent_pcg = 0;
+  return GBA_OK;
+}
+
+// Persistent PCG grid: every CTA co-resident (cooperative launch), no more
+// CTAs than there are chunks or camera blocks to hand out.
+int Engine::pcg_grid() const {
+  const int cap = sm_count_ * pcg_occupancy_;
+  const int want = std::max(std::max(db_.nchunks, db_.cam_blocks), 1);
+  return std::max(1, std::min(cap, want));
+}
+
+void Engine::enqueue_pcg(cudaStream_t s) { launch_pcg_persistent(db_, mixed_, pcg_grid(), s); }
+
+gba_status Engine::selftest_wait_timeout(int *device_status, std::string *err) {
+  gba_status st;
+  DeviceBatch b{};
+  int32_t *dstat = nullptr;
+  uint32_t *dcnt = nullptr;
+  if ((st = check(cudaMalloc(&dstat, 8 * sizeof(int32_t)), "selftest alloc", err)) != GBA_OK) return st;
+  if ((st = check(cudaMalloc(&dcnt, 8 * sizeof(uint32_t)), "selftest alloc", err)) != GBA_OK) {
+    cudaFree(dstat);
+    return st;
+  }
+  cudaMemsetAsync(dstat, 0, 8 * sizeof(int32_t), stream_);
+  cudaMemsetAsync(dcnt, 0, 8 * sizeof(uint32_t), stream_);
+  b.status = dstat;
+  b.global_counter = dcnt;
+  // ~1e5 polls of >= 32 ns: the wait gives up within milliseconds
+  cudaError_t e = launch_barrier_timeout_probe(b, 100000u, stream_);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(stream_);
+  int32_t hs[8] = {0};
+  if (e == cudaSuccess) e = cudaMemcpy(hs, dstat, sizeof hs, cudaMemcpyDeviceToHost);
+  cudaFree(dstat);
+  cudaFree(dcnt);
+  if ((st = check(e, "selftest", err)) != GBA_OK) return st;
+  *device_status = hs[0];
   return GBA_OK;
 }
 
@@ -200,7 +245,7 @@ size_t Engine::layout(const HostBatch &hb, char *base, DeviceBatch *db, size_t *
   b.seg_partial = cv.take<double>(9 * ns);
   b.chunk_scal = cv.take<double>(kChunkScal * nch);
   b.cam_scal = cv.take<double>(kCamScal * nc);
-  b.blk_scal = cv.take<double>(kBlkScal * nb);
+  b.cam_pcg = cv.take<double>(kPcgScal * nc);
   b.prob_counter = cv.take<uint32_t>(4 * P);
   b.global_counter = cv.take<uint32_t>(8);
   b.opt.function_tolerance = o_.function_tolerance;
@@ -306,9 +351,11 @@ gba_status Engine::upload(const HostBatch &hb, std::string *err) {
 }
 
 void Engine::destroy_graph() {
-  if (exec_) cudaGraphExecDestroy(exec_);
+  for (cudaGraphExec_t *x : {&exec_, &setup_exec_, &body_exec_, &gather_exec_}) {
+    if (*x) cudaGraphExecDestroy(*x);
+    *x = nullptr;
+  }
   if (graph_) cudaGraphDestroy(graph_);
-  exec_ = nullptr;
   graph_ = nullptr;
   graph_key_.clear();
 }
@@ -399,6 +446,7 @@ void Engine::enqueue_lm_tail(cudaStream_t s) {
 
 gba_status Engine::build_graph(std::string *err) {
   destroy_graph();
+  if (o_.persistent_pcg && host_loop_) return build_host_loop_graphs(err);
   gba_status st;
   cudaGraphConditionalHandle lmh = 0, pcgh = 0;
   if ((st = check(cudaGraphCreate(&graph_, 0), "cudaGraphCreate", err)) != GBA_OK) return st;
@@ -412,18 +460,13 @@ gba_status Engine::build_graph(std::string *err) {
   profiling_ = false;
   auto fail = [&](cudaError_t e, const char *what) {
     profiling_ = prof;
-    cudaStreamCaptureStatus cs;
-    for (cudaStream_t s : {cap_[1], cap_[0], stream_}) {
-      if (cudaStreamIsCapturing(s, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) {
-        cudaGraph_t g = nullptr;
-        cudaStreamEndCapture(s, &g);
-        if (g && g != graph_) cudaGraphDestroy(g);
-      }
-    }
+    end_captures();
     cudaGetLastError();
     const gba_status r = check(e, what, err);
     destroy_graph();
     db_.use_cond = 0;
+    db_.lm_cond = 0;
+    db_.pcg_cond = 0;
     return r;
   };
   cudaError_t e = cudaStreamBeginCaptureToGraph(stream_, graph_, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
@@ -447,43 +490,118 @@ gba_status Engine::build_graph(std::string *err) {
   cudaGraph_t lmbody = lp.conditional.phGraph_out[0];
   e = cudaStreamUpdateCaptureDependencies(stream_, &lmnode, nullptr, 1, cudaStreamSetCaptureDependencies);
   if (e != cudaSuccess) return fail(e, "capture dependencies");
-  e = cudaGraphConditionalHandleCreate(&pcgh, lmbody, 1, cudaGraphCondAssignDefault);
-  if (e != cudaSuccess) return fail(e, "PCG conditional handle");
-  db_.pcg_cond = pcgh;
+  if (!o_.persistent_pcg) {
+    e = cudaGraphConditionalHandleCreate(&pcgh, lmbody, 1, cudaGraphCondAssignDefault);
+    if (e != cudaSuccess) return fail(e, "PCG conditional handle");
+    db_.pcg_cond = pcgh;
+  }
   // LM body
   e = cudaStreamBeginCaptureToGraph(cap_[0], lmbody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) return fail(e, "capture LM body");
   enqueue_lm_head(cap_[0]);
-  e = cudaStreamGetCaptureInfo(cap_[0], &cs, nullptr, &cg, &deps, nullptr, &ndeps);
-  if (e != cudaSuccess) return fail(e, "capture info (LM body)");
-  cudaGraphNodeParams pp = {};
-  pp.type = cudaGraphNodeTypeConditional;
-  pp.conditional.handle = pcgh;
-  pp.conditional.type = cudaGraphCondTypeWhile;
-  pp.conditional.size = 1;
-  cudaGraphNode_t pcgnode;
-  e = cudaGraphAddNode(&pcgnode, cg, deps, nullptr, ndeps, &pp);
-  if (e != cudaSuccess) return fail(e, "PCG conditional node");
-  cudaGraph_t pcgbody = pp.conditional.phGraph_out[0];
-  e = cudaStreamUpdateCaptureDependencies(cap_[0], &pcgnode, nullptr, 1, cudaStreamSetCaptureDependencies);
-  if (e != cudaSuccess) return fail(e, "capture dependencies (LM body)");
-  e = cudaStreamBeginCaptureToGraph(cap_[1], pcgbody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
-  if (e != cudaSuccess) return fail(e, "capture PCG body");
-  launch_pcg_iteration(db_, mixed_, cap_[1]);
   cudaGraph_t tmp = nullptr;
-  e = cudaStreamEndCapture(cap_[1], &tmp);
-  if (e != cudaSuccess) return fail(e, "end capture PCG body");
+  if (o_.persistent_pcg) {
+    // one cooperative kernel node runs every PCG iteration of the LM step
+    e = launch_pcg_persistent(db_, mixed_, pcg_grid(), cap_[0]);
+    if (e != cudaSuccess) return fail(e, "persistent PCG capture");
+  } else {
+    e = cudaStreamGetCaptureInfo(cap_[0], &cs, nullptr, &cg, &deps, nullptr, &ndeps);
+    if (e != cudaSuccess) return fail(e, "capture info (LM body)");
+    cudaGraphNodeParams pp = {};
+    pp.type = cudaGraphNodeTypeConditional;
+    pp.conditional.handle = pcgh;
+    pp.conditional.type = cudaGraphCondTypeWhile;
+    pp.conditional.size = 1;
+    cudaGraphNode_t pcgnode;
+    e = cudaGraphAddNode(&pcgnode, cg, deps, nullptr, ndeps, &pp);
+    if (e != cudaSuccess) return fail(e, "PCG conditional node");
+    cudaGraph_t pcgbody = pp.conditional.phGraph_out[0];
+    e = cudaStreamUpdateCaptureDependencies(cap_[0], &pcgnode, nullptr, 1, cudaStreamSetCaptureDependencies);
+    if (e != cudaSuccess) return fail(e, "capture dependencies (LM body)");
+    e = cudaStreamBeginCaptureToGraph(cap_[1], pcgbody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return fail(e, "capture PCG body");
+    launch_pcg_iteration(db_, mixed_, cap_[1]);
+    e = cudaStreamEndCapture(cap_[1], &tmp);
+    if (e != cudaSuccess) return fail(e, "end capture PCG body");
+  }
   enqueue_lm_tail(cap_[0]);
   e = cudaStreamEndCapture(cap_[0], &tmp);
   if (e != cudaSuccess) return fail(e, "end capture LM body");
-  char *out = d_arena_ + download_off_;
-  launch_gather_results(db_, reinterpret_cast<double *>(out),
-                        reinterpret_cast<double *>(out + align_up(sizeof(double) * 9 * (size_t)db_.nc, 256)), stream_);
+  enqueue_gather(stream_);
   e = cudaStreamEndCapture(stream_, &tmp);
   if (e != cudaSuccess) return fail(e, "end capture");
   e = cudaGraphInstantiate(&exec_, graph_, 0);
-  if (e != cudaSuccess) return fail(e, "cudaGraphInstantiate");
+  if (e != cudaSuccess) {
+    if (o_.persistent_pcg) {
+      // This driver/toolkit refuses a cooperative kernel inside a conditional
+      // body: keep the persistent PCG and loop over LM bodies from the host.
+      fail(e, "cudaGraphInstantiate");
+      host_loop_ = true;
+      return build_host_loop_graphs(err);
+    }
+    return fail(e, "cudaGraphInstantiate");
+  }
   profiling_ = prof;
+  graph_key_ = cur_key_;
+  return GBA_OK;
+}
+
+void Engine::end_captures() {
+  cudaStreamCaptureStatus cs;
+  for (cudaStream_t s : {cap_[1], cap_[0], stream_}) {
+    if (cudaStreamIsCapturing(s, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) {
+      cudaGraph_t g = nullptr;
+      cudaStreamEndCapture(s, &g);
+      if (g && g != graph_) cudaGraphDestroy(g);
+    }
+  }
+}
+
+void Engine::enqueue_gather(cudaStream_t s) {
+  char *out = d_arena_ + download_off_;
+  launch_gather_results(db_, reinterpret_cast<double *>(out),
+                        reinterpret_cast<double *>(out + align_up(sizeof(double) * 9 * (size_t)db_.nc, 256)), s);
+}
+
+// Host-looped variant: a setup graph, one LM-body graph (with the persistent
+// PCG kernel) launched max_num_iterations times back to back — a body whose
+// problems have all terminated does no work — and a gather graph.
+gba_status Engine::build_host_loop_graphs(std::string *err) {
+  db_.use_cond = 0;
+  db_.lm_cond = 0;
+  db_.pcg_cond = 0;
+  const bool prof = profiling_;
+  profiling_ = false;
+  auto capture = [&](int which, cudaGraphExec_t *out) -> cudaError_t {
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return e;
+    if (which == 0) {
+      enqueue_setup(stream_);
+    } else if (which == 1) {
+      enqueue_lm_head(stream_);
+      launch_pcg_persistent(db_, mixed_, pcg_grid(), stream_);
+      enqueue_lm_tail(stream_);
+    } else {
+      enqueue_gather(stream_);
+    }
+    e = cudaStreamEndCapture(stream_, &g);
+    if (e != cudaSuccess) return e;
+    e = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    return e;
+  };
+  cudaError_t e = capture(0, &setup_exec_);
+  if (e == cudaSuccess) e = capture(1, &body_exec_);
+  if (e == cudaSuccess) e = capture(2, &gather_exec_);
+  profiling_ = prof;
+  if (e != cudaSuccess) {
+    end_captures();
+    cudaGetLastError();
+    const gba_status r = check(e, "host-loop graphs", err);
+    destroy_graph();
+    return r;
+  }
   graph_key_ = cur_key_;
   return GBA_OK;
 }
@@ -527,6 +645,25 @@ gba_status Engine::run_host_driven(std::string *err) {
     enqueue_lm_head(stream_);
     if ((st = read_status()) != GBA_OK) return st;
     int pcg = 0;
+    if (o_.persistent_pcg && hstat[2]) {
+      prof_begin(stream_);
+      if ((st = check(launch_pcg_persistent(db_, mixed_, pcg_grid(), stream_), "persistent PCG", err)) != GBA_OK)
+        return st;
+      if (profiling_) {
+        // algorithmic bytes: PCG iterations run in this launch x bytes of one
+        // iteration (mat-vec + camera reduce + update)
+        if ((st = read_status()) != GBA_OK) return st;
+        std::vector<LMState> ls((size_t)db_.num_problems);
+        cudaMemcpy(ls.data(), db_.lm, ls.size() * sizeof(LMState), cudaMemcpyDeviceToHost);
+        double iters = 0.0;
+        for (const LMState &l : ls) iters = std::max(iters, (double)l.pcg_iterations);
+        const double per_it = bytes_matvec(db_) + (double)db_.nseg * 72.0 +
+                              (double)db_.nc * (45.0 + 9.0 * 5.0) * 8.0 + (double)db_.nc * (81.0 + 9.0 * 8.0) * 8.0;
+        prof_end(stream_, PF_PERSISTENT, iters * per_it);
+      }
+      if ((st = read_status()) != GBA_OK) return st;
+      hstat[2] = 0;
+    }
     while (hstat[2] && pcg <= o_.max_linear_solver_iterations) {
       ++pcg;
       prof_begin(stream_);
@@ -561,10 +698,23 @@ gba_status Engine::run_solve(std::string *err) {
   gba_status st;
   if ((st = check(cudaEventRecord(ev_start_, stream_), "event", err)) != GBA_OK) return st;
   if (o_.use_graphs && !profiling_) {
-    if (!exec_ || graph_key_ != cur_key_) {
-      if ((st = build_graph(err)) != GBA_OK) return st;
+    if ((!exec_ && !body_exec_) || graph_key_ != cur_key_) {
+      st = build_graph(err);
+      if (st != GBA_OK && o_.persistent_pcg) {
+        // no cooperative kernel in graphs at all: three-kernel PCG instead
+        o_.persistent_pcg = 0;
+        st = build_graph(err);
+      }
+      if (st != GBA_OK) return st;
     }
-    if ((st = check(cudaGraphLaunch(exec_, stream_), "cudaGraphLaunch", err)) != GBA_OK) return st;
+    if (exec_) {
+      if ((st = check(cudaGraphLaunch(exec_, stream_), "cudaGraphLaunch", err)) != GBA_OK) return st;
+    } else {
+      if ((st = check(cudaGraphLaunch(setup_exec_, stream_), "cudaGraphLaunch", err)) != GBA_OK) return st;
+      for (int k = 0; k < o_.max_num_iterations; ++k)
+        if ((st = check(cudaGraphLaunch(body_exec_, stream_), "cudaGraphLaunch", err)) != GBA_OK) return st;
+      if ((st = check(cudaGraphLaunch(gather_exec_, stream_), "cudaGraphLaunch", err)) != GBA_OK) return st;
+    }
   } else {
     if ((st = run_host_driven(err)) != GBA_OK) return st;
   }
@@ -585,6 +735,10 @@ gba_status Engine::download(const HostBatch &hb, const gba_problem_view *v, gba_
   size_t ub, doff, dbytes;
   layout(hb, h_stage_, &hdb, &ub, &doff, &dbytes);
   const int32_t *hstat = hdb.status;
+  if (hstat[0] == GBA_ERR_TIMEOUT) {
+    *err = "a bounded device-side wait (persistent PCG grid barrier) gave up";
+    return GBA_ERR_TIMEOUT;
+  }
   if (hstat[0] != 0) {
     *err = "device-side loop guard tripped (internal error)";
     return GBA_ERR_INTERNAL;

@@ -43,12 +43,21 @@ class Engine {
   // asynchronous on the handle's stream).
   gba_status rerun(std::string *err);
   gba_status download(const HostBatch &hb, const gba_problem_view *v, gba_summary *s, std::string *err);
+  // Runs a grid barrier that cannot complete with a short spin limit; the
+  // device reports GBA_ERR_TIMEOUT in *device_status and the context stays
+  // usable.
+  gba_status selftest_wait_timeout(int *device_status, std::string *err);
 
  private:
+  int pcg_grid() const;
+  void enqueue_pcg(cudaStream_t s);
   gba_status ensure_capacity(size_t dev_bytes, size_t host_bytes, std::string *err);
   size_t layout(const HostBatch &hb, char *dbase, DeviceBatch *db, size_t *upload_bytes,
                 size_t *download_off, size_t *download_bytes);
   gba_status build_graph(std::string *err);
+  gba_status build_host_loop_graphs(std::string *err);
+  void end_captures();
+  void enqueue_gather(cudaStream_t s);
   void destroy_graph();
   gba_status run_host_driven(std::string *err);
   gba_status check(cudaError_t e, const char *what, std::string *err);
@@ -75,6 +84,10 @@ class Engine {
   // graph cache: valid while the arena and the batch shape are unchanged
   cudaGraph_t graph_ = nullptr;
   cudaGraphExec_t exec_ = nullptr;
+  // host-looped LM bodies (when a cooperative kernel cannot sit in a
+  // conditional graph body)
+  cudaGraphExec_t setup_exec_ = nullptr, body_exec_ = nullptr, gather_exec_ = nullptr;
+  bool host_loop_ = false;
   std::vector<long long> graph_key_;
   std::vector<long long> cur_key_;
   // events
@@ -83,6 +96,8 @@ class Engine {
   std::vector<ProfileEntry> profile_;
   double last_setup_ms_ = 0.0, last_solve_ms_ = 0.0;
   int trace_cap_ = 0;
+  int sm_count_ = 0;
+  int pcg_occupancy_ = 0;  // CTAs per SM of the persistent PCG kernel
 };
 
 }  // namespace gba

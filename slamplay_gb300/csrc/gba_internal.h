@@ -126,7 +126,7 @@ struct DeviceBatch {
   // per chunk / per camera / per camera-block scalars (deterministic partials)
   double *chunk_scal;        // kChunkScal per chunk
   double *cam_scal;          // kCamScal per camera
-  double *blk_scal;          // kBlkScal per camera block
+  double *cam_pcg;           // kPcgScal per camera: PCG dot-product partials
   const int4 *camblk;        // camera blocks: (problem, first camera, count, 0)
   LMState *lm;
   DeviceOptions opt;
@@ -150,13 +150,14 @@ constexpr int kCS_COST = 0, kCS_GMAX = 1, kCS_XN2 = 2, kCS_MODEL = 3, kCS_STEP2 
 // cam_scal slots
 constexpr int kCamScal = 6;
 constexpr int kCC_GMAX = 0, kCC_XN2 = 1, kCC_STEP2 = 2, kCC_RZ = 3, kCC_RR = 4;
-// blk_scal slots (PCG partials of one camera block)
-constexpr int kBlkScal = 4;
-constexpr int kBS_PQ = 0, kBS_RZ = 1, kBS_RR = 2, kBS_QX = 3;
+// cam_pcg slots (PCG partials of one camera)
+constexpr int kPcgScal = 4;
+constexpr int kPS_PQ = 0, kPS_RZ = 1, kPS_RR = 2, kPS_QX = 3;
 // cameras per CTA in the warp-per-camera PCG kernels
 constexpr int kCamPerBlock = 8;
 // prob_counter slots (4 per problem) and global_counter slots
 constexpr int kPC_SCHUR = 0, kPC_REDUCE = 1, kPC_UPDATE = 2;
-constexpr int kGC_SCHUR = 0, kGC_UPDATE = 1, kGC_POST = 2, kGC_LMBODIES = 3;
+constexpr int kGC_SCHUR = 0, kGC_UPDATE = 1, kGC_POST = 2, kGC_LMBODIES = 3, kGC_BAR_COUNT = 4, kGC_BAR_GEN = 5;
+// status words: [0] error, [1] any LM active, [2] any PCG active, [3] PCG-active problem count
 
 }  // namespace gba

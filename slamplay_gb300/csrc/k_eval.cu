@@ -359,7 +359,7 @@ __device__ void finish_lm_body(const DeviceBatch &B, bool count_body) {
   if (last_block_done(B.global_counter + kGC_POST, gridDim.x, &flag)) {
     if (threadIdx.x == 0) {
       int any = 0;
-      for (int p = 0; p < B.num_problems; ++p) any |= B.lm[p].active;
+      for (int p = 0; p < B.num_problems; ++p) any |= __ldcg(&B.lm[p].active);
       uint32_t bodies = B.global_counter[kGC_LMBODIES];
       if (count_body) B.global_counter[kGC_LMBODIES] = ++bodies;
       if (bodies > (uint32_t)B.opt.max_iterations + 2u) {
@@ -367,7 +367,7 @@ __device__ void finish_lm_body(const DeviceBatch &B, bool count_body) {
         any = 0;
       }
       B.status[1] = any;
-      if (B.use_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)B.lm_cond, any ? 1u : 0u);
+      if (B.use_cond && B.lm_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)B.lm_cond, any ? 1u : 0u);
     }
   }
 }

@@ -9,12 +9,8 @@
 //  K3a k_point_prepare   per point: C = J_p^T J_p + Dp^2, FP64 inverse, Cinv g_p
 //  K3b k_camera_schur    per camera (CTA): S_ii, reduced rhs, 9x9 FP64 inverse,
 //                        PCG start (x = 0, r = v, z = M r)
-//  K4a k_schur_matvec    per point-segment chunk: w = W^T p, t = C^-1 w,
-//                        u = W t, reduced into per-(chunk, camera) partials
-//                        through a camera-sorted shared-memory tile (no
-//                        global atomics, fixed summation order)
-//  K4b k_camera_reduce   warp per camera: q = (B + Dc^2) p - sum(partials), p.q
-//  K4c k_pcg_update      warp per camera: x, r, z = M r, r.z, r.r; PCG tests
+//  K4  (k_pcg.cu)        implicit-Schur PCG: mat-vec over point-segment
+//                        chunks, camera reduce, vector update
 //  K5  k_back_substitute per chunk: y_p = C^-1 (g_p - W^T y_c), model cost
 //                        change, candidate points
 //  K6  k_decide          per problem: Ceres' accept / reject / radius update
@@ -246,10 +242,17 @@ __global__ void __launch_bounds__(kSchurThreads) k_camera_schur(DeviceBatch B) {
   // the grid's last CTA sets the PCG loop condition
   if (last_block_done(B.global_counter + kGC_SCHUR, gridDim.x, &flag)) {
     if (t == 0) {
-      int any = 0;
-      for (int q = 0; q < B.num_problems; ++q) any |= B.lm[q].active && B.lm[q].pcg_active;
+      int any = 0, count = 0;
+      for (int q = 0; q < B.num_problems; ++q) {
+        const int a = __ldcg(&B.lm[q].active) && __ldcg(&B.lm[q].pcg_active);
+        any |= a;
+        count += a;
+      }
       B.status[2] = any;
-      if (B.use_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)B.pcg_cond, any ? 1u : 0u);
+      B.status[3] = count;
+      B.global_counter[kGC_BAR_COUNT] = 0u;  // persistent PCG barrier starts empty
+      __threadfence();
+      if (B.use_cond && B.pcg_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)B.pcg_cond, any ? 1u : 0u);
     }
   }
 }
@@ -261,279 +264,6 @@ void launch_camera_schur(const DeviceBatch &b, bool mixed, cudaStream_t s) {
     k_camera_schur<false><<<b.nc, kSchurThreads, 0, s>>>(b);
 }
 
-// ---------------------------------------------------------------------------
-// K4a: implicit Schur product, one CTA per chunk, one thread per observation.
-//   p_c  = z_c + beta p_c          (this iteration's direction, staged per
-//                                   distinct camera of the chunk)
-//   w_o  = J_p^T (J_c p_c)          per observation
-//   t_j  = C_j^-1 sum_{o in j} w_o  per point (points own contiguous obs)
-//   u_o  = J_c^T (J_p t_j)          per observation, written at its slot in
-//                                   the chunk's camera-sorted order
-//   partial(chunk, camera) = sum of u over the camera's run of slots
-template <bool MIXED>
-__global__ void __launch_bounds__(kChunkCap) k_schur_matvec(DeviceBatch B) {
-  typedef typename Prec<MIXED>::real real;
-  typedef typename Prec<MIXED>::real2 real2;
-  typedef typename Acc<MIXED>::type Acc;
-  __shared__ real pseg[kChunkCap][9];
-  __shared__ real U[kChunkCap][9];  // first holds w (3 per obs), then u (9 per slot)
-  __shared__ real tpt[kChunkCap][3];
-  const int t = threadIdx.x;
-  for (int ch = blockIdx.x; ch < B.nchunks; ch += gridDim.x) {
-    const ChunkInfo ci = B.chunk[ch];
-    const LMState *L = B.lm + ci.problem;
-    if (!L->active || !L->pcg_active) continue;
-    const double beta = L->beta;
-    for (int i = t; i < ci.seg_count * 9; i += blockDim.x) {
-      const int s = i / 9, q = i - 9 * s;
-      const size_t k = 9 * (size_t)B.seg_cam[ci.seg_begin + s] + q;
-      pseg[s][q] = (real)(B.pcg_z[k] + beta * B.pcg_p[k]);
-    }
-    __syncthreads();
-    const bool valid = t < ci.obs_count;
-    real2 Jc[9], Jp[3];
-    int lp = 0, slot = 0;
-    if (valid) {
-      const int64_t o = ci.obs_begin + t;
-      const int s = B.obs_seg[o];
-      slot = B.obs_slot[o];
-      lp = B.obs_pt[o] - ci.pt_begin;
-#pragma unroll
-      for (int q = 0; q < 9; ++q) Jc[q] = jload<real2>(B.jac, B.no, q, o);
-#pragma unroll
-      for (int q = 0; q < 3; ++q) Jp[q] = jload<real2>(B.jac, B.no, 9 + q, o);
-      real zu = 0, zv = 0;
-#pragma unroll
-      for (int q = 0; q < 9; ++q) {
-        const real x = pseg[s][q];
-        zu += Jc[q].x * x;
-        zv += Jc[q].y * x;
-      }
-#pragma unroll
-      for (int q = 0; q < 3; ++q) U[t][q] = Jp[q].x * zu + Jp[q].y * zv;
-    }
-    __syncthreads();
-    if (t < ci.pt_count) {
-      const int jj = ci.pt_begin + t;
-      const int b0 = B.pt_obs_begin[jj] - ci.obs_begin, b1 = B.pt_obs_begin[jj + 1] - ci.obs_begin;
-      Acc y0, y1, y2;
-      y0.init(), y1.init(), y2.init();
-      for (int k = b0; k < b1; ++k) {
-        y0.add(U[k][0]);
-        y1.add(U[k][1]);
-        y2.add(U[k][2]);
-      }
-      const real *Ci = reinterpret_cast<const real *>(B.pt_Cinv) + 6 * (size_t)jj;
-      const real w0 = (real)y0.value(), w1 = (real)y1.value(), w2 = (real)y2.value();
-      tpt[t][0] = Ci[0] * w0 + Ci[1] * w1 + Ci[2] * w2;
-      tpt[t][1] = Ci[1] * w0 + Ci[3] * w1 + Ci[4] * w2;
-      tpt[t][2] = Ci[2] * w0 + Ci[4] * w1 + Ci[5] * w2;
-    }
-    __syncthreads();
-    if (valid) {
-      const real t0 = tpt[lp][0], t1 = tpt[lp][1], t2 = tpt[lp][2];
-      const real eu = Jp[0].x * t0 + Jp[1].x * t1 + Jp[2].x * t2;
-      const real ev = Jp[0].y * t0 + Jp[1].y * t1 + Jp[2].y * t2;
-#pragma unroll
-      for (int q = 0; q < 9; ++q) U[slot][q] = Jc[q].x * eu + Jc[q].y * ev;
-    }
-    __syncthreads();
-    for (int i = t; i < ci.seg_count * 9; i += blockDim.x) {
-      const int s = i / 9, q = i - 9 * s;
-      const int b0 = B.seg_pos[ci.seg_begin + s];
-      const int b1 = (s + 1 < ci.seg_count) ? B.seg_pos[ci.seg_begin + s + 1] : ci.obs_count;
-      Acc a;
-      a.init();
-      for (int k = b0; k < b1; ++k) a.add(U[k][q]);
-      B.seg_partial[9 * ((size_t)ci.seg_begin + s) + q] = a.value();
-    }
-    __syncthreads();
-  }
-}
-
-// K4b: warp per camera.
-__global__ void __launch_bounds__(32 * kCamPerBlock) k_camera_reduce(DeviceBatch B) {
-  __shared__ double red[kCamPerBlock];
-  __shared__ int flag;
-  const int4 cb = B.camblk[blockIdx.x];
-  const int p = cb.x;
-  LMState *L = B.lm + p;
-  if (!L->active || !L->pcg_active) return;  // uniform per problem
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const double beta = L->beta;
-  double pq = 0.0;
-  if (warp < cb.z) {
-    const int c = cb.y + warp;
-    // direction of this iteration
-    double pc = 0.0;
-    if (lane < 9) {
-      const size_t i = 9 * (size_t)c + lane;
-      pc = B.pcg_z[i] + beta * B.pcg_p[i];
-    }
-    double acc[9];
-#pragma unroll
-    for (int q = 0; q < 9; ++q) acc[q] = 0.0;
-    const int e = B.cam_seg_begin[c + 1];
-    for (int k = B.cam_seg_begin[c] + lane; k < e; k += 32) {
-      const double *pp = B.seg_partial + 9 * (size_t)B.cam_seg_list[k];
-#pragma unroll
-      for (int q = 0; q < 9; ++q) acc[q] += pp[q];
-    }
-#pragma unroll
-    for (int q = 0; q < 9; ++q) acc[q] = warp_sum(acc[q]);
-    // (B + D^2) p, row `lane`
-    double bp = 0.0;
-    const double *Bc = B.cam_B + 45 * (size_t)c;
-    for (int k = 0; k < 9; ++k) {
-      const double pk = __shfl_sync(0xffffffffu, pc, k);
-      if (lane < 9) bp += Bc[sym9(lane, k)] * pk;
-    }
-    if (lane < 9) {
-      double mine = 0.0;
-#pragma unroll
-      for (int q = 0; q < 9; ++q)
-        if (q == lane) mine = acc[q];
-      const size_t i = 9 * (size_t)c + lane;
-      const double q = bp + B.cam_D2[i] * pc - mine;
-      B.pcg_p[i] = pc;
-      B.pcg_q[i] = q;
-      pq = pc * q;
-    }
-    pq = warp_sum(pq);
-  }
-  if (lane == 0) red[warp] = pq;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double s = 0.0;
-    for (int w = 0; w < kCamPerBlock; ++w) s += red[w];
-    B.blk_scal[(size_t)kBlkScal * blockIdx.x + kBS_PQ] = s;
-  }
-  const ProblemInfo pi = B.prob[p];
-  if (last_block_done(B.prob_counter + 4 * p + kPC_REDUCE, (uint32_t)pi.cam_block_count, &flag)) {
-    __shared__ double rr[8];
-    const double pqs = block_range_sum(B.blk_scal + kBS_PQ, pi.cam_block_begin,
-                                       pi.cam_block_begin + pi.cam_block_count, kBlkScal, rr);
-    if (threadIdx.x == 0) {
-      L->pq = pqs;
-      if (!(pqs > 0.0) || !isfinite(pqs)) {
-        // not positive definite along p: stop with the current iterate
-        if (L->pcg_iterations == 0) L->linear_ok = 0;
-        L->pcg_active = 0;
-        L->alpha = 0.0;
-      } else {
-        L->alpha = L->rz / pqs;
-      }
-    }
-  }
-}
-
-// K4c: warp per camera.
-__global__ void __launch_bounds__(32 * kCamPerBlock) k_pcg_update(DeviceBatch B) {
-  __shared__ double red[3][kCamPerBlock];
-  __shared__ int flag;
-  const int4 cb = B.camblk[blockIdx.x];
-  const int p = cb.x;
-  LMState *L = B.lm + p;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (L->active && L->pcg_active) {
-    const double alpha = L->alpha;
-    double rz = 0.0, rr = 0.0, qx = 0.0;
-    if (warp < cb.z) {
-      const int c = cb.y + warp;
-      const size_t i = 9 * (size_t)c + (lane < 9 ? lane : 0);
-      double r = 0.0, x = 0.0;
-      if (lane < 9) {
-        x = B.pcg_x[i] + alpha * B.pcg_p[i];
-        r = B.pcg_r[i] - alpha * B.pcg_q[i];
-        B.pcg_x[i] = x;
-        B.pcg_r[i] = r;
-      }
-      double z = 0.0;
-      const double *M = B.cam_Minv + 81 * (size_t)c;
-      for (int k = 0; k < 9; ++k) {
-        const double rk = __shfl_sync(0xffffffffu, r, k);
-        if (lane < 9) z += M[lane * 9 + k] * rk;
-      }
-      if (lane < 9) {
-        B.pcg_z[i] = z;
-        rz = r * z;
-        rr = r * r;
-        qx = x * (B.pcg_v[i] + r);
-      }
-      rz = warp_sum(rz);
-      rr = warp_sum(rr);
-      qx = warp_sum(qx);
-    }
-    if (lane == 0) {
-      red[0][warp] = rz;
-      red[1][warp] = rr;
-      red[2][warp] = qx;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double a = 0.0, b = 0.0, d = 0.0;
-      for (int w = 0; w < kCamPerBlock; ++w) a += red[0][w], b += red[1][w], d += red[2][w];
-      double *bs = B.blk_scal + (size_t)kBlkScal * blockIdx.x;
-      bs[kBS_RZ] = a;
-      bs[kBS_RR] = b;
-      bs[kBS_QX] = d;
-    }
-    const ProblemInfo pi = B.prob[p];
-    if (last_block_done(B.prob_counter + 4 * p + kPC_UPDATE, (uint32_t)pi.cam_block_count, &flag)) {
-      __shared__ double rr2[8];
-      const int b0 = pi.cam_block_begin, b1 = pi.cam_block_begin + pi.cam_block_count;
-      const double rzn = block_range_sum(B.blk_scal + kBS_RZ, b0, b1, kBlkScal, rr2);
-      const double rrn = block_range_sum(B.blk_scal + kBS_RR, b0, b1, kBlkScal, rr2);
-      const double qxn = block_range_sum(B.blk_scal + kBS_QX, b0, b1, kBlkScal, rr2);
-      if (threadIdx.x == 0) {
-        const DeviceOptions &o = B.opt;
-        const int it = ++L->pcg_iterations;
-        bool stop = false;
-        if (o.pcg_criterion == GBA_PCG_QUADRATIC_MODEL) {
-          // Q(x) = x'Sx - 2 v'x = -x'(v + r);  stop when i (Q_i - Q_{i-1}) / Q_i < eta
-          const double Q1 = -qxn;
-          const double zeta = it * (Q1 - L->q0) / Q1;
-          if (zeta < o.eta && it >= o.min_pcg_iterations) stop = true;
-          L->q0 = Q1;
-        } else {
-          if (sqrt(rrn) <= o.pcg_tolerance * L->r0_norm && it >= o.min_pcg_iterations) stop = true;
-        }
-        if (it >= o.max_pcg_iterations) stop = true;
-        if (!isfinite(rzn) || !(L->rz != 0.0)) stop = true;
-        L->rr = rrn;
-        L->beta = stop ? 0.0 : rzn / L->rz;
-        L->rz = rzn;
-        if (stop) L->pcg_active = 0;
-      }
-    }
-  }
-  if (last_block_done(B.global_counter + kGC_UPDATE, gridDim.x, &flag)) {
-    if (threadIdx.x == 0) {
-      int any = 0;
-      for (int q = 0; q < B.num_problems; ++q) any |= B.lm[q].active && B.lm[q].pcg_active;
-      B.status[2] = any;
-      if (B.use_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)B.pcg_cond, any ? 1u : 0u);
-    }
-  }
-}
-
-void launch_schur_matvec(const DeviceBatch &b, bool mixed, cudaStream_t s) {
-  if (mixed)
-    k_schur_matvec<true><<<b.nchunks, kChunkCap, 0, s>>>(b);
-  else
-    k_schur_matvec<false><<<b.nchunks, kChunkCap, 0, s>>>(b);
-}
-void launch_camera_reduce(const DeviceBatch &b, cudaStream_t s) {
-  k_camera_reduce<<<b.cam_blocks, 32 * kCamPerBlock, 0, s>>>(b);
-}
-void launch_pcg_update(const DeviceBatch &b, cudaStream_t s) {
-  k_pcg_update<<<b.cam_blocks, 32 * kCamPerBlock, 0, s>>>(b);
-}
-void launch_pcg_iteration(const DeviceBatch &b, bool mixed, cudaStream_t s) {
-  launch_schur_matvec(b, mixed, s);
-  launch_camera_reduce(b, s);
-  launch_pcg_update(b, s);
-}
 
 // ---------------------------------------------------------------------------
 // K5: y_p = C^-1 (g_p - W^T y_c), step = -y, model cost change

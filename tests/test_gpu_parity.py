@@ -181,3 +181,46 @@ def test_invalid_inputs_raise():
         ok = b.copy()
         sm = s.solve(ok)
         assert sm.final_cost < sm.initial_cost
+
+
+def test_persistent_pcg_bitwise_equals_three_kernel_pcg():
+    b = small_problem(num_points=900)
+    outs = []
+    for persistent in (1, 0):
+        for crit in ("residual", "quadratic_model"):
+            g = b.copy()
+            with Solver(max_num_iterations=8, persistent_pcg=persistent, pcg_criterion=crit, **FIXED) as s:
+                sm = s.solve(g)
+            outs.append((persistent, crit, g.parameters().copy(), sm.final_cost, sm.num_linear_solver_iterations))
+    for a, b2 in ((outs[0], outs[2]), (outs[1], outs[3])):
+        assert np.array_equal(a[2], b2[2]), a[1]
+        assert a[3] == b2[3] and a[4] == b2[4]
+
+
+def test_bounded_wait_reports_timeout_and_context_survives():
+    with Solver() as s:
+        assert s.selftest_wait_timeout() == 5  # GBA_ERR_TIMEOUT
+        b = small_problem(num_points=100)
+        sm = s.solve(b)
+        assert sm.final_cost < sm.initial_cost
+
+
+@pytest.mark.parametrize("loss", ["trivial", "huber"])
+def test_golden_fixture_fp64(loss):
+    import os
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "small_problem.npz"))
+    b = BALProblem.from_arrays(int(g["num_cameras"]), int(g["num_points"]), g["camera_index"], g["point_index"],
+                               g["observations"], g["parameters"])
+    with Solver(max_num_iterations=15, loss=loss, pcg_tolerance=1e-12, max_linear_solver_iterations=1000,
+                **FIXED) as s:
+        sm = s.solve(b)
+    assert abs(sm.initial_cost - g[f"{loss}_initial_cost"]) <= 1e-12 * g[f"{loss}_initial_cost"]
+    assert abs(sm.final_cost - g[f"{loss}_final_cost"]) <= 1e-9 * g[f"{loss}_final_cost"]
+    np.testing.assert_allclose(sm.trace_cost[:4], g[f"{loss}_trace_cost"][:4], rtol=1e-9)
+    if loss == "trivial":
+        with Solver(pcg_tolerance=1e-12, max_linear_solver_iterations=1000) as s:
+            d, m, _ = s.compute_step(BALProblem.from_arrays(int(g["num_cameras"]), int(g["num_points"]),
+                                                            g["camera_index"], g["point_index"], g["observations"],
+                                                            g["parameters"]), 1e4)
+        ref = g["step_radius_1e4"]
+        assert np.linalg.norm(d - ref) <= 1e-6 * np.linalg.norm(ref)
