@@ -1,0 +1,32 @@
+// bundle_adjustment_gb300 — the reference demo's main()
+// (backend/slam_ba_simple_g2o_ceres/test_bundle_adjustment_ceres.cpp:37-56)
+// with SolveBA running on the GPU through libgba:
+//   read BAL -> Normalize -> Perturb(0.1, 0.5, 0.5) -> initial.ply ->
+//   SolveBA -> final.ply
+// Usage: bundle_adjustment_gb300 bal_data.txt [--mixed]
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "gba_solve_ba.hpp"
+
+int main(int argc, char **argv) {
+  if (argc < 2) {
+    std::printf("usage: %s bal_data.txt [--mixed]\n", argv[0]);
+    return 1;
+  }
+  try {
+    slamplay_gb300::BALProblem bal_problem(argv[1]);
+    bal_problem.Normalize();
+    bal_problem.Perturb(0.1, 0.5, 0.5);
+    bal_problem.WriteToPLYFile("initial.ply");
+    slamplay_gb300::SolveBAOptions opts;
+    if (argc > 2 && std::strcmp(argv[2], "--mixed") == 0) opts.options.precision = GBA_PRECISION_MIXED;
+    const gba_status st = slamplay_gb300::SolveBA(bal_problem, opts);
+    bal_problem.WriteToPLYFile("final.ply");
+    return st == GBA_OK ? 0 : 2;
+  } catch (const std::exception &e) {
+    std::fprintf(stderr, "%s\n", e.what());
+    return 1;
+  }
+}
