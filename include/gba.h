@@ -256,6 +256,36 @@ gba_status gba_synchronize(gba_handle *h);
  * handle stays usable.  No counterpart in the reference. */
 gba_status gba_selftest_wait_timeout(gba_handle *h, int32_t *device_status);
 
+/* ---- allocation-free evaluation ----------------------------------------- */
+/* A problem whose arrays are already in DEVICE memory (BALProblem layout,
+ * cameras and points in separate arrays). */
+typedef struct gba_device_problem {
+  int32_t num_cameras;
+  int32_t num_points;
+  int32_t num_observations;
+  const int32_t *camera_index;  /* device, [num_observations]     */
+  const int32_t *point_index;   /* device, [num_observations]     */
+  const double *observations;   /* device, [2 * num_observations] */
+  const double *cameras;        /* device, [9 * num_cameras]      */
+  const double *points;         /* device, [3 * num_points]       */
+} gba_device_problem;
+
+/* Residuals (device, 2 per observation, may be NULL) and cost (device, one
+ * double) of a device-resident problem, computed without allocating any
+ * memory.  No counterpart in the reference: it exists for callers that
+ * cannot call cudaMalloc — code running during CUDA graph capture, real-time
+ * threads that must not take cudaMalloc's implicit synchronisation, hosts
+ * that own every device byte through their own pool.  Scratch lives in a
+ * fixed file-scope device array (~6.3 MB, held by every GPU that loads the
+ * library until exit); at most 16384 cameras and 16777216 observations per
+ * call, larger problems are rejected with GBA_ERR_INVALID_ARGUMENT.  The
+ * first call on a device sets up the array's address for that device (make
+ * it before any stream capture).  Calls share the array: calls that overlap
+ * on the GPU race.  Asynchronous on `stream` (a cudaStream_t, NULL = the
+ * default stream); errors via gba_last_error(NULL). */
+gba_status gba_evaluate_noalloc(const gba_device_problem *p, int32_t loss, double loss_scale,
+                                double *residuals, double *cost, void *stream);
+
 /* Per-kernel device times of the last gba_solve / gba_batch_solve when
  * profiling is on: kernel names, launches and total milliseconds. */
 gba_status gba_set_profiling(gba_handle *h, int32_t on);

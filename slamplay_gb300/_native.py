@@ -82,6 +82,15 @@ class SynthSpec(C.Structure):
     ]
 
 
+class DeviceProblem(C.Structure):
+    """gba_device_problem: device pointers (as integers) of a resident problem."""
+    _fields_ = [
+        ("num_cameras", C.c_int32), ("num_points", C.c_int32), ("num_observations", C.c_int32),
+        ("camera_index", C.c_void_p), ("point_index", C.c_void_p), ("observations", C.c_void_p),
+        ("cameras", C.c_void_p), ("points", C.c_void_p),
+    ]
+
+
 class ServerStats(C.Structure):
     _fields_ = [
         ("submitted", C.c_int64), ("admitted", C.c_int64), ("completed", C.c_int64),
@@ -120,6 +129,8 @@ _SIGS = {
     "gba_solve_resident": (C.c_int, [C.c_void_p, C.c_int32]),
     "gba_synchronize": (C.c_int, [C.c_void_p]),
     "gba_selftest_wait_timeout": (C.c_int, [C.c_void_p, _i32p]),
+    "gba_evaluate_noalloc": (C.c_int, [C.POINTER(DeviceProblem), C.c_int32, C.c_double, C.c_void_p, C.c_void_p,
+                                       C.c_void_p]),
     "gba_set_profiling": (C.c_int, [C.c_void_p, C.c_int32]),
     "gba_profile_count": (C.c_int32, [C.c_void_p]),
     "gba_profile_entry": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_char_p), C.POINTER(C.c_int64),

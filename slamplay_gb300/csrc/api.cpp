@@ -25,6 +25,11 @@ gba_status fail(gba_handle *h, gba_status st, const std::string &msg) {
 
 const char *gba_io_last_error(void);
 
+namespace gba {
+// The calling thread's handle-less error message (gba_last_error(NULL)).
+std::string &thread_error_message() { return g_create_error; }
+}  // namespace gba
+
 extern "C" {
 
 void gba_options_init(gba_options *o) {
