@@ -122,10 +122,7 @@ typedef struct gba_options {
   int32_t chunk_observations;         /* point-segment tile (obs per CTA), 0 = auto  */
   int32_t reorder_points;             /* 1 = group points by first camera (locality) */
   int32_t use_graphs;                 /* 1 = run the LM loop as one CUDA graph       */
-  int32_t persistent_pcg;             /* 1 = all PCG iterations of an LM step in one
-                                         persistent cooperative kernel (bounded grid
-                                         barriers); 0 = three kernels per iteration  */
-  int32_t reserved[7];
+  int32_t reserved[8];
 } gba_options;
 
 /* Per-solve report, the subset of ceres::Solver::Summary the reference
@@ -250,11 +247,6 @@ gba_status gba_compute_step(gba_handle *h, const gba_problem_view *p, double rad
 gba_status gba_solve_resident(gba_handle *h, int32_t repeats);
 /* Waits for all work queued on the handle's stream. */
 gba_status gba_synchronize(gba_handle *h);
-/* Failure-path self test of the bounded device-side waits: launches a grid
- * barrier that can never complete, with a spin limit of milliseconds.  The
- * kernel must give up and report GBA_ERR_TIMEOUT in *device_status, and the
- * handle stays usable.  No counterpart in the reference. */
-gba_status gba_selftest_wait_timeout(gba_handle *h, int32_t *device_status);
 
 /* ---- allocation-free evaluation ----------------------------------------- */
 /* A problem whose arrays are already in DEVICE memory (BALProblem layout,

@@ -44,7 +44,7 @@ class Options(C.Structure):
         ("pcg_tolerance", C.c_double), ("eta", C.c_double),
         ("minimizer_progress_to_stdout", C.c_int32), ("device", C.c_int32), ("stream", C.c_void_p),
         ("chunk_observations", C.c_int32), ("reorder_points", C.c_int32), ("use_graphs", C.c_int32),
-        ("persistent_pcg", C.c_int32), ("reserved", C.c_int32 * 7),
+        ("reserved", C.c_int32 * 8),
     ]
 
 
@@ -128,7 +128,6 @@ _SIGS = {
     "gba_compute_step": (C.c_int, [C.c_void_p, C.POINTER(ProblemView), C.c_double, _f64p, _f64p, _i32p]),
     "gba_solve_resident": (C.c_int, [C.c_void_p, C.c_int32]),
     "gba_synchronize": (C.c_int, [C.c_void_p]),
-    "gba_selftest_wait_timeout": (C.c_int, [C.c_void_p, _i32p]),
     "gba_evaluate_noalloc": (C.c_int, [C.POINTER(DeviceProblem), C.c_int32, C.c_double, C.c_void_p, C.c_void_p,
                                        C.c_void_p]),
     "gba_set_profiling": (C.c_int, [C.c_void_p, C.c_int32]),

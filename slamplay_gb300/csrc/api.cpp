@@ -62,7 +62,6 @@ void gba_options_init(gba_options *o) {
   o->chunk_observations = 0;
   o->reorder_points = 1;
   o->use_graphs = 1;
-  o->persistent_pcg = 1;
 }
 
 const char *gba_version(void) { return "gba 1 sm_103a"; }
@@ -160,16 +159,6 @@ gba_status gba_solve_resident(gba_handle *h, int32_t repeats) {
     const gba_status st = h->engine->rerun(&err);
     if (st != GBA_OK) return fail(h, st, err);
   }
-  return GBA_OK;
-}
-
-gba_status gba_selftest_wait_timeout(gba_handle *h, int32_t *device_status) {
-  if (!h || !device_status) return GBA_ERR_INVALID_ARGUMENT;
-  std::string err;
-  int ds = 0;
-  const gba_status st = h->engine->selftest_wait_timeout(&ds, &err);
-  *device_status = ds;
-  if (st != GBA_OK) return fail(h, st, err);
   return GBA_OK;
 }
 

@@ -38,20 +38,17 @@ enum ProfSlot {
   PF_POINT,
   PF_SCHUR,
   PF_MATVEC,
-  PF_REDUCE,
-  PF_UPDATE,
+  PF_PCGCAM,
   PF_BACKSUB,
   PF_CANDIDATE,
   PF_DECIDE,
   PF_TABLE,
   PF_SETUP_MISC,
-  PF_PERSISTENT,
   PF_COUNT
 };
-const char *kProfNames[PF_COUNT] = {"eval_jacobian",  "post_eval",     "point_prepare", "camera_schur",
-                                    "schur_matvec",   "camera_reduce", "pcg_update",    "back_substitute",
-                                    "candidate_cost", "decide",        "camera_table",  "setup_misc",
-                                    "pcg_persistent"};
+const char *kProfNames[PF_COUNT] = {"eval_jacobian",  "post_eval", "point_prepare", "camera_schur",
+                                    "schur_matvec",   "pcg_camera", "back_substitute", "candidate_cost",
+                                    "decide",         "camera_table", "setup_misc"};
 
 double now_s() {
   return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
@@ -117,47 +114,19 @@ gba_status Engine::init(std::string *err) {
   if ((st = check(cudaDeviceGetAttribute(&sm_count_, cudaDevAttrMultiProcessorCount, device_), "SM count", err)) !=
       GBA_OK)
     return st;
-  int coop = 0;
-  cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device_);
-  pcg_occupancy_ = coop ? pcg_persistent_blocks_per_sm(mixed_) : 0;
-  if (pcg_occupancy_ <= 0) o_.persistent_pcg = 0;
+  max_cluster_ = pcg_max_cluster();
   return GBA_OK;
 }
 
-// Persistent PCG grid: every CTA co-resident (cooperative launch), no more
-// CTAs than there are chunks or camera blocks to hand out.
-int Engine::pcg_grid() const {
-  const int cap = sm_count_ * pcg_occupancy_;
-  const int want = std::max(std::max(db_.nchunks, db_.cam_blocks), 1);
-  return std::max(1, std::min(cap, want));
-}
-
-void Engine::enqueue_pcg(cudaStream_t s) { launch_pcg_persistent(db_, mixed_, pcg_grid(), s); }
-
-gba_status Engine::selftest_wait_timeout(int *device_status, std::string *err) {
-  gba_status st;
-  DeviceBatch b{};
-  int32_t *dstat = nullptr;
-  uint32_t *dcnt = nullptr;
-  if ((st = check(cudaMalloc(&dstat, 8 * sizeof(int32_t)), "selftest alloc", err)) != GBA_OK) return st;
-  if ((st = check(cudaMalloc(&dcnt, 8 * sizeof(uint32_t)), "selftest alloc", err)) != GBA_OK) {
-    cudaFree(dstat);
-    return st;
-  }
-  cudaMemsetAsync(dstat, 0, 8 * sizeof(int32_t), stream_);
-  cudaMemsetAsync(dcnt, 0, 8 * sizeof(uint32_t), stream_);
-  b.status = dstat;
-  b.global_counter = dcnt;
-  // ~1e5 polls of >= 32 ns: the wait gives up within milliseconds
-  cudaError_t e = launch_barrier_timeout_probe(b, 100000u, stream_);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(stream_);
-  int32_t hs[8] = {0};
-  if (e == cudaSuccess) e = cudaMemcpy(hs, dstat, sizeof hs, cudaMemcpyDeviceToHost);
-  cudaFree(dstat);
-  cudaFree(dcnt);
-  if ((st = check(e, "selftest", err)) != GBA_OK) return st;
-  *device_status = hs[0];
-  return GBA_OK;
+// Cluster shape of the camera-side PCG kernel: one CTA per camera block
+// (kPcgBlockCams cameras) of the largest problem, capped by the device's
+// cluster limit; the remaining blocks are taken in passes.
+void Engine::pcg_cluster(const HostBatch &hb, int *cluster, int *passes) const {
+  int maxc = 1;
+  for (const ProblemInfo &pi : hb.prob) maxc = std::max(maxc, pi.cam_count);
+  const int blocks = (maxc + kPcgBlockCams - 1) / kPcgBlockCams;
+  *cluster = std::min(max_cluster_, blocks);
+  *passes = (blocks + *cluster - 1) / *cluster;
 }
 
 // Arena order: [upload | download | work].  The pinned host staging buffer
@@ -192,7 +161,7 @@ size_t Engine::layout(const HostBatch &hb, char *base, DeviceBatch *db, size_t *
   b.seg_pos = cv.take<uint16_t>(ns);
   b.seg_cam = cv.take<int32_t>(ns);
   b.cam_seg_begin = cv.take<int32_t>(nc + 1);
-  b.cam_seg_list = cv.take<int32_t>(ns);
+  b.seg_slot = cv.take<int32_t>(ns);
   b.cam_obs_begin = cv.take<int32_t>(nc + 1);
   b.cam_obs_list = cv.take<int32_t>(no);
   b.camblk = cv.take<int4>(nb);
@@ -234,6 +203,8 @@ size_t Engine::layout(const HostBatch &hb, char *base, DeviceBatch *db, size_t *
   b.cam_g = cv.take<double>(9 * nc);
   b.cam_scale = cv.take<double>(9 * nc);
   b.cam_Minv = cv.take<double>(81 * nc);
+  b.cam_Minvf = cv.take<float>(81 * nc);
+  b.cam_Bf = cv.take<float>(45 * nc);
   b.cam_D2 = cv.take<double>(9 * nc);
   b.pcg_x = cv.take<double>(9 * nc);
   b.pcg_r = cv.take<double>(9 * nc);
@@ -241,8 +212,10 @@ size_t Engine::layout(const HostBatch &hb, char *base, DeviceBatch *db, size_t *
   b.pcg_p = cv.take<double>(9 * nc);
   b.pcg_q = cv.take<double>(9 * nc);
   b.pcg_v = cv.take<double>(9 * nc);
+  b.pcg_pf = cv.take<float>(9 * nc);
   b.cam_colnorm = cv.take<double>(9 * nc);
   b.seg_partial = cv.take<double>(9 * ns);
+  pcg_cluster(hb, &b.pcg_cluster, &b.pcg_passes);
   b.chunk_scal = cv.take<double>(kChunkScal * nch);
   b.cam_scal = cv.take<double>(kCamScal * nc);
   b.cam_pcg = cv.take<double>(kPcgScal * nc);
@@ -313,6 +286,11 @@ gba_status Engine::upload(const HostBatch &hb, std::string *err) {
   DeviceBatch probe{};
   size_t ub, doff, dbytes;
   const size_t total = layout(hb, nullptr, &probe, &ub, &doff, &dbytes);
+  if (pcg_camera_smem(probe.pcg_passes) > kPcgSmemMax) {
+    *err = "a problem has more cameras than the camera-side PCG kernel supports (" +
+           std::to_string(kPcgSmemMax / pcg_camera_smem(1) * (size_t)probe.pcg_cluster * kPcgBlockCams) + ")";
+    return GBA_ERR_INVALID_ARGUMENT;
+  }
   if ((st = ensure_capacity(total, doff + dbytes, err)) != GBA_OK) return st;
   upload_bytes_ = ub;
   download_off_ = doff;
@@ -335,7 +313,7 @@ gba_status Engine::upload(const HostBatch &hb, std::string *err) {
   put(const_cast<uint16_t *>(hdb.seg_pos), hb.seg_pos);
   put(const_cast<int32_t *>(hdb.seg_cam), hb.seg_cam);
   put(const_cast<int32_t *>(hdb.cam_seg_begin), hb.cam_seg_begin);
-  put(const_cast<int32_t *>(hdb.cam_seg_list), hb.cam_seg_list);
+  put(const_cast<int32_t *>(hdb.seg_slot), hb.seg_slot);
   put(const_cast<int32_t *>(hdb.cam_obs_begin), hb.cam_obs_begin);
   put(const_cast<int32_t *>(hdb.cam_obs_list), hb.cam_obs_list);
   put(const_cast<int4 *>(hdb.camblk), hb.camblk);
@@ -351,11 +329,9 @@ gba_status Engine::upload(const HostBatch &hb, std::string *err) {
 }
 
 void Engine::destroy_graph() {
-  for (cudaGraphExec_t *x : {&exec_, &setup_exec_, &body_exec_, &gather_exec_}) {
-    if (*x) cudaGraphExecDestroy(*x);
-    *x = nullptr;
-  }
+  if (exec_) cudaGraphExecDestroy(exec_);
   if (graph_) cudaGraphDestroy(graph_);
+  exec_ = nullptr;
   graph_ = nullptr;
   graph_key_.clear();
 }
@@ -378,9 +354,17 @@ void Engine::prof_end(cudaStream_t s, int entry, double bytes) {
 // must read and write at least once; cached gathers counted once per
 // distinct item).  Used for the achieved-bandwidth figures.
 static double bytes_matvec(const DeviceBatch &b) {
+  // J_c, J_p (12 pairs) + slot / segment / point indices per observation;
+  // C^-1 + CSR per point; per segment its camera's direction, position,
+  // slot and partial; per chunk its record
   const double rs = b.opt.mixed ? 4.0 : 8.0;
   return (double)b.no * (24.0 * rs + 8.0) + (double)b.np * (4.0 + 6.0 * rs) +
-         (double)b.nseg * (6.0 + 72.0 + 144.0) + (double)b.nchunks * 32.0;
+         (double)b.nseg * (2.0 + 4.0 + 4.0 + 18.0 * rs) + (double)b.nchunks * 32.0;
+}
+static double bytes_pcg_camera(const DeviceBatch &b) {
+  // partials read once; per camera p, q, x, r, z, v (FP64), B, M^-1, D^2
+  const double rs = b.opt.mixed ? 4.0 : 8.0;
+  return (double)b.nseg * 9.0 * rs + (double)b.nc * (8.0 * 9.0 * 12.0 + (45.0 + 81.0) * rs + 72.0);
 }
 static double bytes_eval(const DeviceBatch &b) {
   const double rs = b.opt.mixed ? 4.0 : 8.0;
@@ -446,7 +430,6 @@ void Engine::enqueue_lm_tail(cudaStream_t s) {
 
 gba_status Engine::build_graph(std::string *err) {
   destroy_graph();
-  if (o_.persistent_pcg && host_loop_) return build_host_loop_graphs(err);
   gba_status st;
   cudaGraphConditionalHandle lmh = 0, pcgh = 0;
   if ((st = check(cudaGraphCreate(&graph_, 0), "cudaGraphCreate", err)) != GBA_OK) return st;
@@ -469,78 +452,47 @@ gba_status Engine::build_graph(std::string *err) {
     db_.pcg_cond = 0;
     return r;
   };
+  auto add_while = [&](cudaStream_t s, cudaGraphConditionalHandle h, cudaGraph_t *body) -> cudaError_t {
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t cg = nullptr;
+    const cudaGraphNode_t *deps = nullptr;
+    size_t ndeps = 0;
+    cudaError_t e = cudaStreamGetCaptureInfo(s, &cs, nullptr, &cg, &deps, nullptr, &ndeps);
+    if (e != cudaSuccess) return e;
+    cudaGraphNodeParams np = {};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = h;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    e = cudaGraphAddNode(&node, cg, deps, nullptr, ndeps, &np);
+    if (e != cudaSuccess) return e;
+    *body = np.conditional.phGraph_out[0];
+    return cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+  };
+  // setup, then WHILE(LM) { head; WHILE(PCG) { mat-vec; camera side } tail }, then gather
   cudaError_t e = cudaStreamBeginCaptureToGraph(stream_, graph_, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) return fail(e, "capture setup");
   enqueue_setup(stream_);
-  // LM while node
-  cudaStreamCaptureStatus cs;
-  cudaGraph_t cg = nullptr;
-  const cudaGraphNode_t *deps = nullptr;
-  size_t ndeps = 0;
-  e = cudaStreamGetCaptureInfo(stream_, &cs, nullptr, &cg, &deps, nullptr, &ndeps);
-  if (e != cudaSuccess) return fail(e, "capture info");
-  cudaGraphNodeParams lp = {};
-  lp.type = cudaGraphNodeTypeConditional;
-  lp.conditional.handle = lmh;
-  lp.conditional.type = cudaGraphCondTypeWhile;
-  lp.conditional.size = 1;
-  cudaGraphNode_t lmnode;
-  e = cudaGraphAddNode(&lmnode, cg, deps, nullptr, ndeps, &lp);
-  if (e != cudaSuccess) return fail(e, "LM conditional node");
-  cudaGraph_t lmbody = lp.conditional.phGraph_out[0];
-  e = cudaStreamUpdateCaptureDependencies(stream_, &lmnode, nullptr, 1, cudaStreamSetCaptureDependencies);
-  if (e != cudaSuccess) return fail(e, "capture dependencies");
-  if (!o_.persistent_pcg) {
-    e = cudaGraphConditionalHandleCreate(&pcgh, lmbody, 1, cudaGraphCondAssignDefault);
-    if (e != cudaSuccess) return fail(e, "PCG conditional handle");
-    db_.pcg_cond = pcgh;
-  }
-  // LM body
+  cudaGraph_t lmbody = nullptr, pcgbody = nullptr, tmp = nullptr;
+  if ((e = add_while(stream_, lmh, &lmbody)) != cudaSuccess) return fail(e, "LM conditional node");
+  if ((e = cudaGraphConditionalHandleCreate(&pcgh, lmbody, 1, cudaGraphCondAssignDefault)) != cudaSuccess)
+    return fail(e, "PCG conditional handle");
+  db_.pcg_cond = pcgh;
   e = cudaStreamBeginCaptureToGraph(cap_[0], lmbody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) return fail(e, "capture LM body");
   enqueue_lm_head(cap_[0]);
-  cudaGraph_t tmp = nullptr;
-  if (o_.persistent_pcg) {
-    // one cooperative kernel node runs every PCG iteration of the LM step
-    e = launch_pcg_persistent(db_, mixed_, pcg_grid(), cap_[0]);
-    if (e != cudaSuccess) return fail(e, "persistent PCG capture");
-  } else {
-    e = cudaStreamGetCaptureInfo(cap_[0], &cs, nullptr, &cg, &deps, nullptr, &ndeps);
-    if (e != cudaSuccess) return fail(e, "capture info (LM body)");
-    cudaGraphNodeParams pp = {};
-    pp.type = cudaGraphNodeTypeConditional;
-    pp.conditional.handle = pcgh;
-    pp.conditional.type = cudaGraphCondTypeWhile;
-    pp.conditional.size = 1;
-    cudaGraphNode_t pcgnode;
-    e = cudaGraphAddNode(&pcgnode, cg, deps, nullptr, ndeps, &pp);
-    if (e != cudaSuccess) return fail(e, "PCG conditional node");
-    cudaGraph_t pcgbody = pp.conditional.phGraph_out[0];
-    e = cudaStreamUpdateCaptureDependencies(cap_[0], &pcgnode, nullptr, 1, cudaStreamSetCaptureDependencies);
-    if (e != cudaSuccess) return fail(e, "capture dependencies (LM body)");
-    e = cudaStreamBeginCaptureToGraph(cap_[1], pcgbody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
-    if (e != cudaSuccess) return fail(e, "capture PCG body");
-    launch_pcg_iteration(db_, mixed_, cap_[1]);
-    e = cudaStreamEndCapture(cap_[1], &tmp);
-    if (e != cudaSuccess) return fail(e, "end capture PCG body");
-  }
+  if ((e = add_while(cap_[0], pcgh, &pcgbody)) != cudaSuccess) return fail(e, "PCG conditional node");
+  e = cudaStreamBeginCaptureToGraph(cap_[1], pcgbody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return fail(e, "capture PCG body");
+  launch_schur_matvec(db_, mixed_, cap_[1]);
+  if ((e = launch_pcg_camera(db_, mixed_, cap_[1])) != cudaSuccess) return fail(e, "PCG camera kernel");
+  if ((e = cudaStreamEndCapture(cap_[1], &tmp)) != cudaSuccess) return fail(e, "end capture PCG body");
   enqueue_lm_tail(cap_[0]);
-  e = cudaStreamEndCapture(cap_[0], &tmp);
-  if (e != cudaSuccess) return fail(e, "end capture LM body");
+  if ((e = cudaStreamEndCapture(cap_[0], &tmp)) != cudaSuccess) return fail(e, "end capture LM body");
   enqueue_gather(stream_);
-  e = cudaStreamEndCapture(stream_, &tmp);
-  if (e != cudaSuccess) return fail(e, "end capture");
-  e = cudaGraphInstantiate(&exec_, graph_, 0);
-  if (e != cudaSuccess) {
-    if (o_.persistent_pcg) {
-      // This driver/toolkit refuses a cooperative kernel inside a conditional
-      // body: keep the persistent PCG and loop over LM bodies from the host.
-      fail(e, "cudaGraphInstantiate");
-      host_loop_ = true;
-      return build_host_loop_graphs(err);
-    }
-    return fail(e, "cudaGraphInstantiate");
-  }
+  if ((e = cudaStreamEndCapture(stream_, &tmp)) != cudaSuccess) return fail(e, "end capture");
+  if ((e = cudaGraphInstantiate(&exec_, graph_, 0)) != cudaSuccess) return fail(e, "cudaGraphInstantiate");
   profiling_ = prof;
   graph_key_ = cur_key_;
   return GBA_OK;
@@ -561,49 +513,6 @@ void Engine::enqueue_gather(cudaStream_t s) {
   char *out = d_arena_ + download_off_;
   launch_gather_results(db_, reinterpret_cast<double *>(out),
                         reinterpret_cast<double *>(out + align_up(sizeof(double) * 9 * (size_t)db_.nc, 256)), s);
-}
-
-// Host-looped variant: a setup graph, one LM-body graph (with the persistent
-// PCG kernel) launched max_num_iterations times back to back — a body whose
-// problems have all terminated does no work — and a gather graph.
-gba_status Engine::build_host_loop_graphs(std::string *err) {
-  db_.use_cond = 0;
-  db_.lm_cond = 0;
-  db_.pcg_cond = 0;
-  const bool prof = profiling_;
-  profiling_ = false;
-  auto capture = [&](int which, cudaGraphExec_t *out) -> cudaError_t {
-    cudaGraph_t g = nullptr;
-    cudaError_t e = cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal);
-    if (e != cudaSuccess) return e;
-    if (which == 0) {
-      enqueue_setup(stream_);
-    } else if (which == 1) {
-      enqueue_lm_head(stream_);
-      launch_pcg_persistent(db_, mixed_, pcg_grid(), stream_);
-      enqueue_lm_tail(stream_);
-    } else {
-      enqueue_gather(stream_);
-    }
-    e = cudaStreamEndCapture(stream_, &g);
-    if (e != cudaSuccess) return e;
-    e = cudaGraphInstantiate(out, g, 0);
-    cudaGraphDestroy(g);
-    return e;
-  };
-  cudaError_t e = capture(0, &setup_exec_);
-  if (e == cudaSuccess) e = capture(1, &body_exec_);
-  if (e == cudaSuccess) e = capture(2, &gather_exec_);
-  profiling_ = prof;
-  if (e != cudaSuccess) {
-    end_captures();
-    cudaGetLastError();
-    const gba_status r = check(e, "host-loop graphs", err);
-    destroy_graph();
-    return r;
-  }
-  graph_key_ = cur_key_;
-  return GBA_OK;
 }
 
 gba_status Engine::run_host_driven(std::string *err) {
@@ -645,44 +554,20 @@ gba_status Engine::run_host_driven(std::string *err) {
     enqueue_lm_head(stream_);
     if ((st = read_status()) != GBA_OK) return st;
     int pcg = 0;
-    if (o_.persistent_pcg && hstat[2]) {
-      prof_begin(stream_);
-      if ((st = check(launch_pcg_persistent(db_, mixed_, pcg_grid(), stream_), "persistent PCG", err)) != GBA_OK)
-        return st;
-      if (profiling_) {
-        // algorithmic bytes: PCG iterations run in this launch x bytes of one
-        // iteration (mat-vec + camera reduce + update)
-        if ((st = read_status()) != GBA_OK) return st;
-        std::vector<LMState> ls((size_t)db_.num_problems);
-        cudaMemcpy(ls.data(), db_.lm, ls.size() * sizeof(LMState), cudaMemcpyDeviceToHost);
-        double iters = 0.0;
-        for (const LMState &l : ls) iters = std::max(iters, (double)l.pcg_iterations);
-        const double per_it = bytes_matvec(db_) + (double)db_.nseg * 72.0 +
-                              (double)db_.nc * (45.0 + 9.0 * 5.0) * 8.0 + (double)db_.nc * (81.0 + 9.0 * 8.0) * 8.0;
-        prof_end(stream_, PF_PERSISTENT, iters * per_it);
-      }
-      if ((st = read_status()) != GBA_OK) return st;
-      hstat[2] = 0;
-    }
     while (hstat[2] && pcg <= o_.max_linear_solver_iterations) {
       ++pcg;
       prof_begin(stream_);
       launch_schur_matvec(db_, mixed_, stream_);
       prof_end(stream_, PF_MATVEC, bytes_matvec(db_));
       prof_begin(stream_);
-      launch_camera_reduce(db_, stream_);
-      prof_end(stream_, PF_REDUCE, (double)db_.nseg * 72.0 + (double)db_.nc * (45.0 + 9.0 * 5.0) * 8.0);
-      prof_begin(stream_);
-      launch_pcg_update(db_, stream_);
-      prof_end(stream_, PF_UPDATE, (double)db_.nc * (81.0 + 9.0 * 8.0) * 8.0);
+      if ((st = check(launch_pcg_camera(db_, mixed_, stream_), "PCG camera kernel", err)) != GBA_OK) return st;
+      prof_end(stream_, PF_PCGCAM, bytes_pcg_camera(db_));
       if ((st = read_status()) != GBA_OK) return st;
     }
     enqueue_lm_tail(stream_);
     if ((st = read_status()) != GBA_OK) return st;
   }
-  char *out = d_arena_ + download_off_;
-  launch_gather_results(db_, reinterpret_cast<double *>(out),
-                        reinterpret_cast<double *>(out + align_up(sizeof(double) * 9 * (size_t)db_.nc, 256)), stream_);
+  enqueue_gather(stream_);
   return check(cudaGetLastError(), "kernel launch", err);
 }
 
@@ -698,23 +583,10 @@ gba_status Engine::run_solve(std::string *err) {
   gba_status st;
   if ((st = check(cudaEventRecord(ev_start_, stream_), "event", err)) != GBA_OK) return st;
   if (o_.use_graphs && !profiling_) {
-    if ((!exec_ && !body_exec_) || graph_key_ != cur_key_) {
-      st = build_graph(err);
-      if (st != GBA_OK && o_.persistent_pcg) {
-        // no cooperative kernel in graphs at all: three-kernel PCG instead
-        o_.persistent_pcg = 0;
-        st = build_graph(err);
-      }
-      if (st != GBA_OK) return st;
+    if (!exec_ || graph_key_ != cur_key_) {
+      if ((st = build_graph(err)) != GBA_OK) return st;
     }
-    if (exec_) {
-      if ((st = check(cudaGraphLaunch(exec_, stream_), "cudaGraphLaunch", err)) != GBA_OK) return st;
-    } else {
-      if ((st = check(cudaGraphLaunch(setup_exec_, stream_), "cudaGraphLaunch", err)) != GBA_OK) return st;
-      for (int k = 0; k < o_.max_num_iterations; ++k)
-        if ((st = check(cudaGraphLaunch(body_exec_, stream_), "cudaGraphLaunch", err)) != GBA_OK) return st;
-      if ((st = check(cudaGraphLaunch(gather_exec_, stream_), "cudaGraphLaunch", err)) != GBA_OK) return st;
-    }
+    if ((st = check(cudaGraphLaunch(exec_, stream_), "cudaGraphLaunch", err)) != GBA_OK) return st;
   } else {
     if ((st = run_host_driven(err)) != GBA_OK) return st;
   }
@@ -735,10 +607,6 @@ gba_status Engine::download(const HostBatch &hb, const gba_problem_view *v, gba_
   size_t ub, doff, dbytes;
   layout(hb, h_stage_, &hdb, &ub, &doff, &dbytes);
   const int32_t *hstat = hdb.status;
-  if (hstat[0] == GBA_ERR_TIMEOUT) {
-    *err = "a bounded device-side wait (persistent PCG grid barrier) gave up";
-    return GBA_ERR_TIMEOUT;
-  }
   if (hstat[0] != 0) {
     *err = "device-side loop guard tripped (internal error)";
     return GBA_ERR_INTERNAL;

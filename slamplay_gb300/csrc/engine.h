@@ -43,19 +43,13 @@ class Engine {
   // asynchronous on the handle's stream).
   gba_status rerun(std::string *err);
   gba_status download(const HostBatch &hb, const gba_problem_view *v, gba_summary *s, std::string *err);
-  // Runs a grid barrier that cannot complete with a short spin limit; the
-  // device reports GBA_ERR_TIMEOUT in *device_status and the context stays
-  // usable.
-  gba_status selftest_wait_timeout(int *device_status, std::string *err);
 
  private:
-  int pcg_grid() const;
-  void enqueue_pcg(cudaStream_t s);
+  void pcg_cluster(const HostBatch &hb, int *cluster, int *passes) const;
   gba_status ensure_capacity(size_t dev_bytes, size_t host_bytes, std::string *err);
   size_t layout(const HostBatch &hb, char *dbase, DeviceBatch *db, size_t *upload_bytes,
                 size_t *download_off, size_t *download_bytes);
   gba_status build_graph(std::string *err);
-  gba_status build_host_loop_graphs(std::string *err);
   void end_captures();
   void enqueue_gather(cudaStream_t s);
   void destroy_graph();
@@ -84,10 +78,6 @@ class Engine {
   // graph cache: valid while the arena and the batch shape are unchanged
   cudaGraph_t graph_ = nullptr;
   cudaGraphExec_t exec_ = nullptr;
-  // host-looped LM bodies (when a cooperative kernel cannot sit in a
-  // conditional graph body)
-  cudaGraphExec_t setup_exec_ = nullptr, body_exec_ = nullptr, gather_exec_ = nullptr;
-  bool host_loop_ = false;
   std::vector<long long> graph_key_;
   std::vector<long long> cur_key_;
   // events
@@ -97,7 +87,7 @@ class Engine {
   double last_setup_ms_ = 0.0, last_solve_ms_ = 0.0;
   int trace_cap_ = 0;
   int sm_count_ = 0;
-  int pcg_occupancy_ = 0;  // CTAs per SM of the persistent PCG kernel
+  int max_cluster_ = 8;    // largest cluster the camera-side PCG kernel may use
 };
 
 }  // namespace gba

@@ -95,7 +95,8 @@ struct DeviceBatch {
   const uint8_t *pt_used, *cam_used;
   const uint16_t *seg_pos;   // start (sorted position) of each segment in its chunk
   const int32_t *seg_cam;
-  const int32_t *cam_seg_begin, *cam_seg_list;
+  const int32_t *cam_seg_begin;  // nc + 1: each camera's run of partials (camera-major)
+  const int32_t *seg_slot;       // camera-major position of each segment's partial
   const int32_t *cam_obs_begin, *cam_obs_list;
   // parameters: the uploaded initial point, and two working buffers of
   // which LMState::parity picks the current one
@@ -118,11 +119,14 @@ struct DeviceBatch {
   double *cam_g;             // 9
   double *cam_scale;         // 9
   double *cam_Minv;          // 81 block-Jacobi inverse of S_ii
+  float *cam_Minvf;          // 81, FP32 copy (mixed form)
+  float *cam_Bf;             // 45, FP32 copy of cam_B (mixed form)
   double *cam_D2;            // 9: squared LM diagonal of the camera parameters
   double *pcg_x, *pcg_r, *pcg_z, *pcg_p, *pcg_q, *pcg_v;  // 9 * nc each
+  float *pcg_pf;             // 9 * nc, FP32 copy of the direction (mixed form)
   double *cam_colnorm;       // 9 * nc: column norms of the first evaluation
   double *pt_colnorm;        // 3 * np
-  double *seg_partial;       // 9 * nseg
+  void *seg_partial;         // 9 * nseg, double (FP64) or float (mixed)
   // per chunk / per camera / per camera-block scalars (deterministic partials)
   double *chunk_scal;        // kChunkScal per chunk
   double *cam_scal;          // kCamScal per camera
@@ -141,6 +145,8 @@ struct DeviceBatch {
   // graph conditional handles (0 when the host drives the loops)
   unsigned long long lm_cond, pcg_cond;
   int32_t use_cond;
+  int32_t pcg_cluster;       // CTAs per cluster of the camera-side PCG kernel
+  int32_t pcg_passes;        // camera blocks per CTA of that kernel (largest problem)
 };
 
 constexpr int kCamTable = 44;    // R(9) dR(27) t(3) f k1 k2 + pad
@@ -153,8 +159,12 @@ constexpr int kCC_GMAX = 0, kCC_XN2 = 1, kCC_STEP2 = 2, kCC_RZ = 3, kCC_RR = 4;
 // cam_pcg slots (PCG partials of one camera)
 constexpr int kPcgScal = 4;
 constexpr int kPS_PQ = 0, kPS_RZ = 1, kPS_RR = 2, kPS_QX = 3;
-// cameras per CTA in the warp-per-camera PCG kernels
+// cameras per CTA in the warp-per-camera camera kernels
 constexpr int kCamPerBlock = 8;
+// cameras per block of the camera-side PCG kernel (one thread per coordinate)
+constexpr int kPcgBlockCams = 32;
+// dynamic shared memory the camera-side PCG kernel may use (36 doubles per pass)
+constexpr size_t kPcgSmemMax = 96 * 1024;
 // prob_counter slots (4 per problem) and global_counter slots
 constexpr int kPC_SCHUR = 0, kPC_REDUCE = 1, kPC_UPDATE = 2;
 constexpr int kGC_SCHUR = 0, kGC_UPDATE = 1, kGC_POST = 2, kGC_LMBODIES = 3, kGC_BAR_COUNT = 4, kGC_BAR_GEN = 5;

@@ -210,12 +210,17 @@ __global__ void __launch_bounds__(kSchurThreads) k_camera_schur(DeviceBatch B) {
       B.pcg_v[i] = vec[t];
       B.pcg_r[i] = vec[t];
       B.pcg_x[i] = 0.0;
-      B.pcg_p[i] = 0.0;
+      B.pcg_p[i] = z;  // first direction p0 = z0
       B.pcg_z[i] = z;
+      if (MIXED) B.pcg_pf[i] = (float)z;
       rz = vec[t] * z;
       rr = vec[t] * vec[t];
     }
-    if (t < 81) B.cam_Minv[81 * (size_t)c + t] = Minv[t];
+    if (t < 81) {
+      B.cam_Minv[81 * (size_t)c + t] = Minv[t];
+      if (MIXED) B.cam_Minvf[81 * (size_t)c + t] = (float)Minv[t];
+    }
+    if (MIXED && t < 45) B.cam_Bf[45 * (size_t)c + t] = (float)B.cam_B[45 * (size_t)c + t];
     const double rzs = block_sum(rz, red);
     const double rrs = block_sum(rr, red);
     if (t == 0) {

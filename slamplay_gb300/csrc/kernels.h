@@ -25,16 +25,14 @@ void launch_post_eval(const DeviceBatch &b, cudaStream_t s);
 void launch_point_prepare(const DeviceBatch &b, bool mixed, cudaStream_t s);
 // K3b: camera-diagonal Schur blocks, reduced rhs, block-Jacobi inverse, PCG init.
 void launch_camera_schur(const DeviceBatch &b, bool mixed, cudaStream_t s);
-// K4a-c: one PCG iteration (implicit Schur mat-vec, camera reduce, update).
+// K4a-b: one PCG iteration (implicit Schur mat-vec, camera-side update).
 void launch_pcg_iteration(const DeviceBatch &b, bool mixed, cudaStream_t s);
 void launch_schur_matvec(const DeviceBatch &b, bool mixed, cudaStream_t s);
-void launch_camera_reduce(const DeviceBatch &b, cudaStream_t s);
-void launch_pcg_update(const DeviceBatch &b, cudaStream_t s);
-// All PCG iterations of one LM step in one persistent cooperative kernel.
-cudaError_t launch_pcg_persistent(const DeviceBatch &b, bool mixed, int grid, cudaStream_t s);
-int pcg_persistent_blocks_per_sm(bool mixed);
-// Self test of the bounded wait: a barrier that can never complete.
-cudaError_t launch_barrier_timeout_probe(const DeviceBatch &b, unsigned spin_limit, cudaStream_t s);
+// K4b alone (one thread-block cluster per problem).
+cudaError_t launch_pcg_camera(const DeviceBatch &b, bool mixed, cudaStream_t s);
+// Largest cluster size the camera-side kernel may use on this device.
+int pcg_max_cluster();
+size_t pcg_camera_smem(int passes);
 // K5: point back-substitution, model cost change, candidate points.
 void launch_back_substitute(const DeviceBatch &b, bool mixed, cudaStream_t s);
 // K5b + K2: candidate cameras (+ their tables) and the candidate cost.

@@ -248,9 +248,11 @@ gba_status prepare_batch(const gba_problem_view *views, int n, const PrepOptions
   hb.cam_seg_begin.assign(hb.nc + 1, 0);
   for (int s = 0; s < hb.nseg; ++s) ++hb.cam_seg_begin[hb.seg_cam[s] + 1];
   for (int c = 0; c < hb.nc; ++c) hb.cam_seg_begin[c + 1] += hb.cam_seg_begin[c];
-  hb.cam_seg_list.resize(hb.nseg);
+  // each segment's partial goes to its camera-major position, so a camera's
+  // partials are contiguous for the camera reduce
+  hb.seg_slot.resize(hb.nseg);
   fill.assign(hb.cam_seg_begin.begin(), hb.cam_seg_begin.end());
-  for (int s = 0; s < hb.nseg; ++s) hb.cam_seg_list[fill[hb.seg_cam[s]]++] = s;
+  for (int s = 0; s < hb.nseg; ++s) hb.seg_slot[s] = fill[hb.seg_cam[s]]++;
   for (int k = 0; k < hb.no; ++k) ++hb.cam_obs_begin[hb.obs_cam[k] + 1];
   for (int c = 0; c < hb.nc; ++c) hb.cam_obs_begin[c + 1] += hb.cam_obs_begin[c];
   fill.assign(hb.cam_obs_begin.begin(), hb.cam_obs_begin.end());

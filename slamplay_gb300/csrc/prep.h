@@ -26,7 +26,7 @@ struct HostBatch {
   std::vector<uint8_t> pt_used, cam_used;
   std::vector<uint16_t> seg_pos;
   std::vector<int32_t> seg_cam;
-  std::vector<int32_t> cam_seg_begin, cam_seg_list, cam_obs_begin, cam_obs_list;
+  std::vector<int32_t> cam_seg_begin, seg_slot, cam_obs_begin, cam_obs_list;
   std::vector<int4> camblk;
   // output mapping
   std::vector<int32_t> obs_orig;  // internal observation -> index in its problem's input

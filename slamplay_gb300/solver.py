@@ -181,13 +181,6 @@ class Solver:
     def synchronize(self) -> None:
         N.check(N.lib().gba_synchronize(self._h), self._h, "gba_synchronize")
 
-    def selftest_wait_timeout(self) -> int:
-        """Runs a device-side wait that cannot complete; returns the status
-        the device reported (GBA_ERR_TIMEOUT = 5 when the bound works)."""
-        ds = N.C.c_int32()
-        N.check(N.lib().gba_selftest_wait_timeout(self._h, N.C.byref(ds)), self._h, "gba_selftest_wait_timeout")
-        return ds.value
-
     # ---- profiling ---------------------------------------------------------
     def set_profiling(self, on: bool) -> None:
         N.check(N.lib().gba_set_profiling(self._h, 1 if on else 0), self._h)
