@@ -286,9 +286,9 @@ gba_status Engine::upload(const HostBatch &hb, std::string *err) {
   DeviceBatch probe{};
   size_t ub, doff, dbytes;
   const size_t total = layout(hb, nullptr, &probe, &ub, &doff, &dbytes);
-  if (pcg_camera_smem(probe.pcg_passes) > kPcgSmemMax) {
+  if (pcg_camera_smem(probe.pcg_passes, probe.pcg_cluster) > kPcgSmemMax) {
     *err = "a problem has more cameras than the camera-side PCG kernel supports (" +
-           std::to_string(kPcgSmemMax / pcg_camera_smem(1) * (size_t)probe.pcg_cluster * kPcgBlockCams) + ")";
+           std::to_string(kPcgSmemMax / pcg_camera_smem(1, 1) * kPcgBlockCams) + ")";
     return GBA_ERR_INVALID_ARGUMENT;
   }
   if ((st = ensure_capacity(total, doff + dbytes, err)) != GBA_OK) return st;

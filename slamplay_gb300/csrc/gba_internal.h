@@ -163,8 +163,9 @@ constexpr int kPS_PQ = 0, kPS_RZ = 1, kPS_RR = 2, kPS_QX = 3;
 constexpr int kCamPerBlock = 8;
 // cameras per block of the camera-side PCG kernel (one thread per coordinate)
 constexpr int kPcgBlockCams = 32;
-// dynamic shared memory the camera-side PCG kernel may use (36 doubles per pass)
-constexpr size_t kPcgSmemMax = 96 * 1024;
+// dynamic shared memory the camera-side PCG kernel may use (4 doubles per
+// camera block of the largest problem: 204,800 cameras)
+constexpr size_t kPcgSmemMax = 200 * 1024;
 // prob_counter slots (4 per problem) and global_counter slots
 constexpr int kPC_SCHUR = 0, kPC_REDUCE = 1, kPC_UPDATE = 2;
 constexpr int kGC_SCHUR = 0, kGC_UPDATE = 1, kGC_POST = 2, kGC_LMBODIES = 3, kGC_BAR_COUNT = 4, kGC_BAR_GEN = 5;

@@ -159,17 +159,21 @@ __global__ void __launch_bounds__(kChunkCap) k_schur_matvec(DeviceBatch B) {
 // more blocks than the cluster has CTAs takes several passes.
 //
 // Every problem-wide dot product is summed in a fixed order that depends
-// only on the problem's camera count: lanes -> warp (xor butterfly); then
-// the (block, warp) values of all blocks, read over distributed shared
-// memory from the CTA that owns each block, strided over the lanes of one
-// warp in (block, warp) order and combined by a second butterfly.  All CTAs
-// therefore hold the same alpha, beta and stopping decision, and the result
-// depends neither on the cluster size nor on the other problems of a batch.
+// only on the problem's camera count: the 288 per-thread values of a block
+// are staged in shared memory and warp 0 adds them (nine per lane in a fixed
+// pairwise tree, then a xor butterfly) -- one warp of FP64 additions instead
+// of nine, since GB300 issues FP64 at a small fraction of its FP32 rate; the
+// block value is pushed into the shared memory of every CTA of the cluster
+// (remote stores, one lane per destination) at the block's slot; after a
+// cluster barrier every CTA adds the slots of all blocks in block order,
+// strided over the lanes of one warp, and combines them with a butterfly.  All CTAs therefore hold the same alpha, beta and stopping
+// decision, and the result depends neither on the cluster size nor on the
+// other problems of a batch.  After the second barrier no CTA touches
+// another CTA's shared memory, so the kernel needs two cluster barriers.
 //
-// The three cluster barriers are split into arrive / wait so that the loads
-// of the next phase overlap the wait.
+// The state of the first kPcgRegPasses passes stays in registers between
+// the phases; every load of a pass is issued before the first barrier.
 constexpr int kPcgThreads = 9 * kPcgBlockCams;  // 288
-constexpr int kPcgWarps = kPcgThreads / 32;     // 9
 
 namespace {
 
@@ -180,41 +184,166 @@ __device__ __forceinline__ void cluster_wait() {
   asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
 }
 
-// Sum of NV values per (block, warp) over all blocks of the problem: block b
-// lives in CTA rank b % cs at pass slot b / cs, value v of warp w at
-// blk[(slot * kPcgWarps + w) * NV + v].  Called by one whole warp; returns
-// the sums in every lane.
+// Fixed-order sum of NV values per block slot, slots 0..n-1 of the local
+// array blk (slot e at blk[NV * e]).  Called by one whole warp; the sums are
+// returned in every lane.
 template <int NV>
-__device__ __forceinline__ void blocks_sum(cg::cluster_group &cl, const double *blk, int nblk, int cs, double *out) {
+__device__ __forceinline__ void slots_sum(const double *blk, int n, double *out) {
   const int lane = threadIdx.x & 31;
   double v[NV];
 #pragma unroll
   for (int k = 0; k < NV; ++k) v[k] = 0.0;
-  const int n = nblk * kPcgWarps;
   for (int e = lane; e < n; e += 32) {
-    const int b = e / kPcgWarps, w = e - kPcgWarps * b;
-    const double *src = cl.map_shared_rank(blk, b % cs) + ((b / cs) * kPcgWarps + w) * NV;
 #pragma unroll
-    for (int k = 0; k < NV; ++k) v[k] += src[k];
+    for (int k = 0; k < NV; ++k) v[k] += blk[NV * e + k];
   }
 #pragma unroll
   for (int k = 0; k < NV; ++k) out[k] = warp_sum(v[k]);
 }
 
-// Loads a fixed-size batch of partials before adding them, so that several
-// memory round trips overlap while the additions keep their serial order.
-template <typename real, typename AccT>
-__device__ __forceinline__ void sum_partials(AccT &acc, const real *part, int s0, int s1) {
-  constexpr int U = 32;
-  int s = s0;
-  for (; s + U <= s1; s += U) {
-    real v[U];
+// Block value of NV per-thread values v (all threads call it together):
+// staged in red[NV][kPcgThreads], summed by warp 0 and pushed to slot b of
+// every CTA of the cluster.
+template <int NV>
+__device__ __forceinline__ void block_push(cg::cluster_group &cl, double (*red)[kPcgThreads], const double *v,
+                                           double *slots, int b, int cs) {
+  const int tid = threadIdx.x, lane = tid & 31;
 #pragma unroll
-    for (int u = 0; u < U; ++u) v[u] = part[9 * (size_t)(s + u)];
+  for (int k = 0; k < NV; ++k) red[k][tid] = v[k];
+  __syncthreads();
+  if (tid < 32) {
+    double s[NV];
 #pragma unroll
-    for (int u = 0; u < U; ++u) acc.add(v[u]);
+    for (int k = 0; k < NV; ++k) {
+      const double *r = red[k] + lane;
+      s[k] = (((r[0] + r[32]) + (r[64] + r[96])) + ((r[128] + r[160]) + (r[192] + r[224]))) + r[256];
+      s[k] = warp_sum(s[k]);
+    }
+    if (lane < cs) {
+      double *dst = cl.map_shared_rank(slots + NV * b, lane);
+#pragma unroll
+      for (int k = 0; k < NV; ++k) dst[k] = s[k];
+    }
   }
-  for (; s < s1; ++s) acc.add(part[9 * (size_t)s]);
+  __syncthreads();  // red may be reused
+}
+
+// One camera coordinate of a pass: everything the three phases need.
+template <typename real>
+struct CamCoord {
+  bool valid;
+  int c;
+  double p, q, x, r, v, z;
+  real m[9];  // row of the block-Jacobi preconditioner
+};
+
+// Phase 1 of one coordinate: loads the pass state and computes
+// q = (B + Dc^2) p - sum of partials.  Returns p.q (0 when not valid).
+template <bool MIXED>
+__device__ __forceinline__ double pcg_phase1(const DeviceBatch &B, const ProblemInfo &pi, int k, int q,
+                                             CamCoord<typename Prec<MIXED>::real> &st) {
+  typedef typename Prec<MIXED>::real real;
+  typedef typename Acc<MIXED>::type Acc;
+  st.valid = k < pi.cam_count;
+  st.c = pi.cam_begin + (st.valid ? k : 0);
+  if (!st.valid) return 0.0;
+  const int c = st.c;
+  const size_t i = 9 * (size_t)c + q;
+  const real *Bc = reinterpret_cast<const real *>(MIXED ? (const void *)B.cam_Bf : (const void *)B.cam_B) + 45 * (size_t)c;
+  const real *pv = reinterpret_cast<const real *>(MIXED ? (const void *)B.pcg_pf : (const void *)B.pcg_p) + 9 * (size_t)c;
+  const real *M = reinterpret_cast<const real *>(MIXED ? (const void *)B.cam_Minvf : (const void *)B.cam_Minv) +
+                  81 * (size_t)c + 9 * q;
+  const real *part = reinterpret_cast<const real *>(B.seg_partial) + q;
+  const int s0 = B.cam_seg_begin[c], s1 = B.cam_seg_begin[c + 1];
+  st.p = B.pcg_p[i];
+  st.x = B.pcg_x[i];
+  st.r = B.pcg_r[i];
+  st.v = B.pcg_v[i];
+  const real d2 = (real)B.cam_D2[i];
+  real brow[9], prow[9];
+#pragma unroll
+  for (int kk = 0; kk < 9; ++kk) {
+    brow[kk] = Bc[sym9(q, kk)];
+    prow[kk] = pv[kk];
+    st.m[kk] = M[kk];
+  }
+  // the camera's partials: the first kBatch in one round trip, then batches.
+  // FP64: four interleaved accumulators (partial s to accumulator
+  // (s - s0) % 4) shorten the chain of 64-cycle additions fourfold; mixed:
+  // one compensated FP32 sum (its chain is short and each extra accumulator
+  // would cost FP64 conversions)
+  constexpr int kBatch = MIXED ? 64 : 32;
+  constexpr int kAcc = MIXED ? 1 : 4;
+  Acc a[kAcc];
+#pragma unroll
+  for (int u = 0; u < kAcc; ++u) a[u].init();
+  for (int s = s0; s < s1; s += kBatch) {
+    real pv2[kBatch];
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) pv2[u] = (s + u < s1) ? part[9 * (size_t)(s + u)] : (real)0;
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u)
+      if (s + u < s1) a[u % kAcc].add(pv2[u]);
+  }
+  double asum = a[0].value();
+  if (kAcc == 4) asum = (a[0].value() + a[1 % kAcc].value()) + (a[2 % kAcc].value() + a[3 % kAcc].value());
+  real bp = 0;
+#pragma unroll
+  for (int kk = 0; kk < 9; ++kk) bp += brow[kk] * prow[kk];
+  st.q = (double)(bp + d2 * (real)st.p - (real)asum);
+  B.pcg_q[i] = st.q;
+  return st.p * st.q;
+}
+
+// Phase 1 for a coordinate whose state is not kept in registers: the same
+// arithmetic, with q stored for phase 2.
+template <bool MIXED>
+__device__ __forceinline__ void pcg_reload(const DeviceBatch &B, int q, CamCoord<typename Prec<MIXED>::real> &st) {
+  typedef typename Prec<MIXED>::real real;
+  if (!st.valid) return;
+  const size_t i = 9 * (size_t)st.c + q;
+  const real *M = reinterpret_cast<const real *>(MIXED ? (const void *)B.cam_Minvf : (const void *)B.cam_Minv) +
+                  81 * (size_t)st.c + 9 * q;
+  st.p = B.pcg_p[i];
+  st.q = B.pcg_q[i];
+  st.x = B.pcg_x[i];
+  st.r = B.pcg_r[i];
+  st.v = B.pcg_v[i];
+#pragma unroll
+  for (int kk = 0; kk < 9; ++kk) st.m[kk] = M[kk];
+}
+
+// Phase 2 of one coordinate (all threads of the CTA call it together):
+// x += alpha p, r -= alpha q, z = M r; returns r.z, r.r, x.(v + r).
+template <bool MIXED>
+__device__ __forceinline__ void pcg_phase2(const DeviceBatch &B, int q, int lc, double alpha,
+                                           CamCoord<typename Prec<MIXED>::real> &st, typename Prec<MIXED>::real *sv,
+                                           bool sync_before, double *d3) {
+  typedef typename Prec<MIXED>::real real;
+  if (st.valid) {
+    st.x = st.x + alpha * st.p;
+    st.r = st.r - alpha * st.q;
+  } else {
+    st.x = st.r = 0.0;
+  }
+  if (sync_before) __syncthreads();  // the previous pass has finished reading sv
+  sv[threadIdx.x] = (real)st.r;
+  __syncthreads();
+  d3[0] = d3[1] = d3[2] = 0.0;
+  if (st.valid) {
+    const real *rv = sv + 9 * lc;
+    real z = 0;
+#pragma unroll
+    for (int kk = 0; kk < 9; ++kk) z += st.m[kk] * rv[kk];
+    st.z = (double)z;
+    const size_t i = 9 * (size_t)st.c + q;
+    B.pcg_x[i] = st.x;
+    B.pcg_r[i] = st.r;
+    B.pcg_z[i] = st.z;
+    d3[0] = st.r * st.z;
+    d3[1] = st.r * st.r;
+    d3[2] = st.x * (st.v + st.r);
+  }
 }
 
 }  // namespace
@@ -222,10 +351,11 @@ __device__ __forceinline__ void sum_partials(AccT &acc, const real *part, int s0
 template <bool MIXED>
 __global__ void __launch_bounds__(kPcgThreads) k_pcg_camera(DeviceBatch B) {
   typedef typename Prec<MIXED>::real real;
-  typedef typename Acc<MIXED>::type Acc;
-  // per pass: kPcgWarps p.q values, then kPcgWarps x (r.z, r.r, x.(v + r))
+  constexpr int kRegPasses = MIXED ? 4 : 2;
+  // slots: [nblk_max] p.q, then [nblk_max][3] r.z, r.r, x.(v + r)
   extern __shared__ double blk[];
   __shared__ real sv[kPcgThreads];  // the block's r, staged for z = M r
+  __shared__ double red[3][kPcgThreads];
   __shared__ double tot[4];
   __shared__ int flag;
   cg::cluster_group cl = cg::this_cluster();
@@ -234,8 +364,9 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg_camera(DeviceBatch B) {
   const int prob = blockIdx.x / cs;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int lc = tid / 9, q = tid - 9 * lc;  // camera in the block, coordinate
+  const int nslots = B.pcg_passes * cs;
   double *blk1 = blk;
-  double *blk3 = blk + kPcgWarps * B.pcg_passes;
+  double *blk3 = blk + nslots;
   LMState *L = B.lm + prob;
   if (prob < B.num_problems && pcg_live(L)) {  // uniform over the cluster
     const ProblemInfo pi = B.prob[prob];
@@ -244,103 +375,59 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg_camera(DeviceBatch B) {
     // barrier: rank 0 overwrites them after the second one
     const double rz_old = L->rz, q0 = L->q0, r0_norm = L->r0_norm;
     const int its = L->pcg_iterations;
-    const real *part = reinterpret_cast<const real *>(B.seg_partial) + q;
-    const real *pdir = reinterpret_cast<const real *>(MIXED ? (const void *)B.pcg_pf : (const void *)B.pcg_p);
-    // ---- q = (B + Dc^2) p - sum of partials, and p.q ---------------------
-    for (int j = 0, b = rank; b < nblk; ++j, b += cs) {
-      const int k = b * kPcgBlockCams + lc;
-      const bool valid = k < pi.cam_count;
-      double pq = 0.0;
-      if (valid) {
-        const int c = pi.cam_begin + k;
-        const size_t i = 9 * (size_t)c + q;
-        const double pc = B.pcg_p[i];
-        const real d2 = (real)B.cam_D2[i];
-        const int s0 = B.cam_seg_begin[c], s1 = B.cam_seg_begin[c + 1];
-        const real *Bc = reinterpret_cast<const real *>(MIXED ? (const void *)B.cam_Bf : (const void *)B.cam_B) +
-                         45 * (size_t)c;
-        const real *pv = pdir + 9 * (size_t)c;
-        real brow[9], prow[9];
+    CamCoord<real> st[kRegPasses];
+    // ---- phase 1: q = (B + Dc^2) p - sum of partials, and p.q --------------
+    auto push1 = [&](int b, double pq) { block_push<1>(cl, red, &pq, blk1, b, cs); };
 #pragma unroll
-        for (int kk = 0; kk < 9; ++kk) brow[kk] = Bc[sym9(q, kk)], prow[kk] = pv[kk];
-        Acc a;
-        a.init();
-        sum_partials<real, Acc>(a, part, s0, s1);
-        real bp = 0;
-#pragma unroll
-        for (int kk = 0; kk < 9; ++kk) bp += brow[kk] * prow[kk];
-        const double qv = (double)(bp + d2 * (real)pc - (real)a.value());
-        B.pcg_q[i] = qv;
-        pq = pc * qv;
-      }
-      pq = warp_sum(pq);
-      if (lane == 0) blk1[j * kPcgWarps + warp] = pq;
+    for (int j = 0; j < kRegPasses; ++j) {
+      const int b = rank + j * cs;
+      if (b < nblk) push1(b, pcg_phase1<MIXED>(B, pi, b * kPcgBlockCams + lc, q, st[j]));
+    }
+    for (int b = rank + kRegPasses * cs; b < nblk; b += cs) {
+      CamCoord<real> t;
+      push1(b, pcg_phase1<MIXED>(B, pi, b * kPcgBlockCams + lc, q, t));
     }
     cluster_arrive();
     cluster_wait();
     if (warp == 0) {
       double t[1];
-      blocks_sum<1>(cl, blk1, nblk, cs, t);
+      slots_sum<1>(blk1, nblk, t);
       if (lane == 0) tot[0] = t[0];
     }
     __syncthreads();
     const double pqs = tot[0];
     const bool good = pqs > 0.0 && isfinite(pqs);
     const double alpha = good ? rz_old / pqs : 0.0;
-    // ---- x += alpha p, r -= alpha q, z = M r, and the three dot products ----
+    // ---- phase 2: x += alpha p, r -= alpha q, z = M r, three dot products --
+    auto push3 = [&](int b, double *d3) { block_push<3>(cl, red, d3, blk3, b, cs); };
     if (good) {
-      for (int j = 0, b = rank; b < nblk; ++j, b += cs) {
-        const int k = b * kPcgBlockCams + lc;
-        const bool valid = k < pi.cam_count;
-        const int c = pi.cam_begin + (valid ? k : 0);
-        const size_t i = 9 * (size_t)c + q;
-        double x = 0.0, r = 0.0, v = 0.0;
-        real mrow[9];
-        if (valid) {
-          const real *M = reinterpret_cast<const real *>(MIXED ? (const void *)B.cam_Minvf
-                                                               : (const void *)B.cam_Minv) +
-                          81 * (size_t)c + 9 * q;
 #pragma unroll
-          for (int kk = 0; kk < 9; ++kk) mrow[kk] = M[kk];
-          x = B.pcg_x[i] + alpha * B.pcg_p[i];
-          r = B.pcg_r[i] - alpha * B.pcg_q[i];
-          v = B.pcg_v[i];
+      for (int j = 0; j < kRegPasses; ++j) {
+        const int b = rank + j * cs;
+        if (b < nblk) {
+          double d3[3];
+          pcg_phase2<MIXED>(B, q, lc, alpha, st[j], sv, j > 0, d3);
+          push3(b, d3);
         }
-        if (j > 0) __syncthreads();  // the previous pass has finished reading sv
-        sv[tid] = (real)r;
-        __syncthreads();
-        double rz = 0.0, rr = 0.0, qx = 0.0;
-        if (valid) {
-          const real *rv = sv + 9 * lc;
-          real z = 0;
-#pragma unroll
-          for (int kk = 0; kk < 9; ++kk) z += mrow[kk] * rv[kk];
-          B.pcg_x[i] = x;
-          B.pcg_r[i] = r;
-          B.pcg_z[i] = (double)z;
-          rz = r * (double)z;
-          rr = r * r;
-          qx = x * (v + r);
-        }
-        rz = warp_sum(rz);
-        rr = warp_sum(rr);
-        qx = warp_sum(qx);
-        if (lane == 0) {
-          double *d = blk3 + (j * kPcgWarps + warp) * 3;
-          d[0] = rz, d[1] = rr, d[2] = qx;
-        }
+      }
+      for (int b = rank + kRegPasses * cs; b < nblk; b += cs) {
+        CamCoord<real> t;
+        t.valid = b * kPcgBlockCams + lc < pi.cam_count;
+        t.c = pi.cam_begin + (t.valid ? b * kPcgBlockCams + lc : 0);
+        pcg_reload<MIXED>(B, q, t);
+        double d3[3];
+        pcg_phase2<MIXED>(B, q, lc, alpha, t, sv, true, d3);
+        push3(b, d3);
       }
     }
     cluster_arrive();
-    cluster_wait();
+    cluster_wait();  // after this barrier no CTA touches another's shared memory
     if (warp == 0) {
       double t[3] = {0.0, 0.0, 0.0};
-      if (good) blocks_sum<3>(cl, blk3, nblk, cs, t);
+      if (good) slots_sum<3>(blk3, nblk, t);
       if (lane == 0) tot[1] = t[0], tot[2] = t[1], tot[3] = t[2];
     }
     __syncthreads();
-    // this CTA has read all the distributed shared memory it needs
-    cluster_arrive();
     const double rzn = tot[1], rrn = tot[2], qxn = tot[3];
     // ---- stopping test and the next direction (identical in every CTA) ------
     const DeviceOptions &o = B.opt;
@@ -361,13 +448,21 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg_camera(DeviceBatch B) {
     }
     const double beta = stop ? 0.0 : rzn / rz_old;
     if (!stop) {
-      for (int b = rank; b < nblk; b += cs) {
+      auto next_dir = [&](size_t i, double z, double p) {
+        const double pn = z + beta * p;
+        B.pcg_p[i] = pn;
+        if (MIXED) B.pcg_pf[i] = (float)pn;
+      };
+#pragma unroll
+      for (int j = 0; j < kRegPasses; ++j) {
+        const int b = rank + j * cs;
+        if (b < nblk && st[j].valid) next_dir(9 * (size_t)st[j].c + q, st[j].z, st[j].p);
+      }
+      for (int b = rank + kRegPasses * cs; b < nblk; b += cs) {
         const int k = b * kPcgBlockCams + lc;
         if (k < pi.cam_count) {
           const size_t i = 9 * (size_t)(pi.cam_begin + k) + q;
-          const double pn = B.pcg_z[i] + beta * B.pcg_p[i];
-          B.pcg_p[i] = pn;
-          if (MIXED) B.pcg_pf[i] = (float)pn;
+          next_dir(i, B.pcg_z[i], B.pcg_p[i]);
         }
       }
     }
@@ -390,14 +485,13 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg_camera(DeviceBatch B) {
         if (B.use_cond && B.pcg_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)B.pcg_cond, stop ? 0u : 1u);
       }
     }
-    cluster_wait();  // no CTA leaves while another may still read its shared memory
   } else if (B.num_problems == 1 && blockIdx.x == 0 && tid == 0) {
     B.status[2] = 0;
     if (B.use_cond && B.pcg_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)B.pcg_cond, 0u);
   }
   if (B.num_problems == 1) return;
   // several problems: the last cluster to finish sets the PCG loop condition
-  if (cs > 1 && (blockIdx.x % cs) != 0) return;
+  if (cs > 1 && rank != 0) return;
   if (last_block_done(B.global_counter + kGC_UPDATE, (uint32_t)(gridDim.x / cs), &flag)) {
     if (tid == 0) {
       int any = 0;
@@ -420,7 +514,7 @@ cudaError_t launch_pcg_camera(const DeviceBatch &b, bool mixed, cudaStream_t s) 
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(b.num_problems * b.pcg_cluster));
   cfg.blockDim = dim3(kPcgThreads);
-  cfg.dynamicSmemBytes = pcg_camera_smem(b.pcg_passes);
+  cfg.dynamicSmemBytes = pcg_camera_smem(b.pcg_passes, b.pcg_cluster);
   cfg.stream = s;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -438,7 +532,11 @@ void launch_pcg_iteration(const DeviceBatch &b, bool mixed, cudaStream_t s) {
   launch_pcg_camera(b, mixed, s);
 }
 
-size_t pcg_camera_smem(int passes) { return sizeof(double) * 4 * kPcgWarps * (size_t)(passes > 0 ? passes : 1); }
+// Slots of every camera block of the largest problem (passes x cluster size),
+// four doubles per block.
+size_t pcg_camera_smem(int passes, int cluster) {
+  return sizeof(double) * 4 * (size_t)(passes > 0 ? passes : 1) * (size_t)(cluster > 0 ? cluster : 1);
+}
 
 // Largest cluster the camera kernel may use on this device (16 when the
 // non-portable size is allowed, else 8).
