@@ -46,7 +46,7 @@ enum ProfSlot {
   PF_SETUP_MISC,
   PF_COUNT
 };
-const char *kProfNames[PF_COUNT] = {"eval_jacobian",  "post_eval", "point_prepare", "camera_schur",
+const char *kProfNames[PF_COUNT] = {"eval_jacobian",  "post_eval", "point_schur",  "camera_schur",
                                     "schur_matvec",   "pcg_camera", "back_substitute", "candidate_cost",
                                     "decide",         "camera_table", "setup_misc"};
 
@@ -115,6 +115,7 @@ gba_status Engine::init(std::string *err) {
       GBA_OK)
     return st;
   max_cluster_ = pcg_max_cluster();
+  point_schur_init();
   return GBA_OK;
 }
 
@@ -191,10 +192,12 @@ size_t Engine::layout(const HostBatch &hb, char *base, DeviceBatch *db, size_t *
   b.pt_param[0] = cv.take<double>(4 * np);
   b.pt_param[1] = cv.take<double>(4 * np);
   b.cam_table = cv.take<double>(kCamTable * nc);
+  b.cam_tablef = cv.take<float>(kCamTable * nc);
   b.jac = cv.take<char>(13 * no * 2 * rs);
   b.pt_C = cv.take<double>(6 * np);
   b.pt_g = cv.take<double>(3 * np);
   b.pt_scale = cv.take<double>(3 * np);
+  b.pt_scalef = cv.take<float>(3 * np);
   b.pt_t = cv.take<double>(3 * np);
   b.pt_Cinv = cv.take<char>(6 * np * rs);
   b.pt_Cinv64 = cv.take<double>(6 * np);
@@ -202,6 +205,7 @@ size_t Engine::layout(const HostBatch &hb, char *base, DeviceBatch *db, size_t *
   b.cam_B = cv.take<double>(45 * nc);
   b.cam_g = cv.take<double>(9 * nc);
   b.cam_scale = cv.take<double>(9 * nc);
+  b.cam_scalef = cv.take<float>(9 * nc);
   b.cam_Minv = cv.take<double>(81 * nc);
   b.cam_Minvf = cv.take<float>(81 * nc);
   b.cam_Bf = cv.take<float>(45 * nc);
@@ -215,6 +219,7 @@ size_t Engine::layout(const HostBatch &hb, char *base, DeviceBatch *db, size_t *
   b.pcg_pf = cv.take<float>(9 * nc);
   b.cam_colnorm = cv.take<double>(9 * nc);
   b.seg_partial = cv.take<double>(9 * ns);
+  b.schur_partial = cv.take<char>(54 * ns * rs);
   pcg_cluster(hb, &b.pcg_cluster, &b.pcg_passes);
   b.chunk_scal = cv.take<double>(kChunkScal * nch);
   b.cam_scal = cv.take<double>(kCamScal * nc);
@@ -372,10 +377,17 @@ static double bytes_eval(const DeviceBatch &b) {
   return (double)b.no * (24.0 + 26.0 * rs) + (double)b.np * (32.0 + 72.0 + 4.0 + 24.0) +
          (double)b.nc * (kCamTable * 8.0) + (double)b.no * (4.0 + 20.0 * rs) + (double)b.nc * (54.0 * 8.0);
 }
-static double bytes_schur(const DeviceBatch &b) {
+static double bytes_point_schur(const DeviceBatch &b) {
+  // J_c, J_p, slot and point index per observation; C, g in and C^-1 (both
+  // precisions), t out per point; 54 partials per segment
   const double rs = b.opt.mixed ? 4.0 : 8.0;
-  return (double)b.no * (4.0 + 4.0 + 24.0 * rs) + (double)b.np * (6.0 * rs + 24.0) +
-         (double)b.nc * (45.0 + 9.0 + 81.0 + 9.0 * 6.0) * 8.0;
+  return (double)b.no * (24.0 * rs + 2.0 + 4.0) + (double)b.np * (48.0 + 24.0 + 6.0 * rs + 48.0 + 24.0) +
+         (double)b.nseg * (54.0 * rs + 8.0);
+}
+static double bytes_schur(const DeviceBatch &b) {
+  // partials in; B, g in; D^2, M^-1 (both precisions), PCG start vectors out
+  const double rs = b.opt.mixed ? 4.0 : 8.0;
+  return (double)b.nseg * 54.0 * rs + (double)b.nc * ((45.0 + 9.0) * 8.0 + 9.0 * 8.0 + 81.0 * (8.0 + rs) + 5.0 * 72.0);
 }
 static double bytes_backsub(const DeviceBatch &b) {
   const double rs = b.opt.mixed ? 4.0 : 8.0;
@@ -401,7 +413,7 @@ void Engine::enqueue_setup(cudaStream_t s) {
 void Engine::enqueue_lm_head(cudaStream_t s) {
   prof_begin(s);
   launch_point_prepare(db_, mixed_, s);
-  prof_end(s, PF_POINT, (double)db_.np * (48.0 + 24.0 + 48.0 + 24.0 + 48.0 + (mixed_ ? 24.0 : 48.0)));
+  prof_end(s, PF_POINT, bytes_point_schur(db_));
   prof_begin(s);
   launch_camera_schur(db_, mixed_, s);
   prof_end(s, PF_SCHUR, bytes_schur(db_));

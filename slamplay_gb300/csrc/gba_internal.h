@@ -105,12 +105,14 @@ struct DeviceBatch {
   double *cam_param[2];      // nc * 9
   double *pt_param[2];       // np * 4
   double *cam_table;         // nc * kCamTable: R, dR/dw, t, f, k1, k2 of one buffer
+  float *cam_tablef;         // nc * kCamTable: FP32 copy for the mixed-form Jacobian
   // Jacobian (scaled, loss-corrected), SoA by column pair; element type by mode
   void *jac;                 // 13 * no of double2 (FP64) or float2 (mixed)
   // per point
   double *pt_C;              // 6 sym (J_p^T J_p)
   double *pt_g;              // 3
   double *pt_scale;          // 3
+  float *pt_scalef;          // 3, FP32 copy
   double *pt_t;              // 3: Cinv g_p
   void *pt_Cinv;             // 6 sym, double (FP64) or float (mixed)
   double *pt_Cinv64;         // 6 sym, double (both modes, for the back-substitution)
@@ -118,6 +120,7 @@ struct DeviceBatch {
   double *cam_B;             // 45 sym packed (J_c^T J_c)
   double *cam_g;             // 9
   double *cam_scale;         // 9
+  float *cam_scalef;         // 9, FP32 copy
   double *cam_Minv;          // 81 block-Jacobi inverse of S_ii
   float *cam_Minvf;          // 81, FP32 copy (mixed form)
   float *cam_Bf;             // 45, FP32 copy of cam_B (mixed form)
@@ -127,6 +130,7 @@ struct DeviceBatch {
   double *cam_colnorm;       // 9 * nc: column norms of the first evaluation
   double *pt_colnorm;        // 3 * np
   void *seg_partial;         // 9 * nseg, double (FP64) or float (mixed)
+  void *schur_partial;       // 54 * nseg: per segment 45 packed Schur-block and 9 rhs partials
   // per chunk / per camera / per camera-block scalars (deterministic partials)
   double *chunk_scal;        // kChunkScal per chunk
   double *cam_scal;          // kCamScal per camera

@@ -48,8 +48,12 @@ __global__ void k_camera_table(DeviceBatch B) {
   if (c >= B.nc) return;
   const LMState *L = B.lm + B.cam_problem[c];
   if (!L->active || !L->need_jacobian) return;
-  camera_table_entry(B.cam_param[L->parity] + 9 * (size_t)c, B.cam_table + (size_t)kCamTable * c,
-                     true);
+  double *tab = B.cam_table + (size_t)kCamTable * c;
+  camera_table_entry(B.cam_param[L->parity] + 9 * (size_t)c, tab, true);
+  if (B.opt.mixed) {
+    float *tf = B.cam_tablef + (size_t)kCamTable * c;
+    for (int k = 0; k < kCamTable; ++k) tf[k] = (float)tab[k];
+  }
 }
 
 void launch_camera_table(const DeviceBatch &b, cudaStream_t s) {
@@ -68,10 +72,14 @@ __device__ __forceinline__ double eval_observation(const DeviceBatch &B, int64_t
                                                    typename Prec<MIXED>::real2 &r, bool &bad) {
   typedef typename Prec<MIXED>::real real;
   const double *tab = B.cam_table + (size_t)kCamTable * c;
+  // the Jacobian reads the table and the scales in its own precision (an
+  // FP32 copy in the mixed form: no FP64 conversions per observation)
+  const real *tr = reinterpret_cast<const real *>(MIXED ? (const void *)(B.cam_tablef + (size_t)kCamTable * c)
+                                                        : (const void *)tab);
   Proj pr;
   project(tab, X, B.obs_uv[o], pr);
   // d prediction / dP = f * M * dxy  (x' = -P_x/P_z, y' = -P_y/P_z)
-  const real iz = (real)(1.0 / pr.P[2]);
+  const real iz = (real)pr.iz;
   const real xp = (real)pr.xp, yp = (real)pr.yp, r2 = (real)pr.r2, dist = (real)pr.dist;
   const real f = (real)pr.f, k1 = (real)pr.k1, k2 = (real)pr.k2;
   const real g = k1 + (real)2 * k2 * r2;
@@ -85,14 +93,14 @@ __device__ __forceinline__ double eval_observation(const DeviceBatch &B, int64_t
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     // dP/dw_k = dR_k X
-    const double *d = tab + 9 + 9 * k;
-    const real q0 = (real)d[0] * Xr[0] + (real)d[1] * Xr[1] + (real)d[2] * Xr[2];
-    const real q1 = (real)d[3] * Xr[0] + (real)d[4] * Xr[1] + (real)d[5] * Xr[2];
-    const real q2 = (real)d[6] * Xr[0] + (real)d[7] * Xr[1] + (real)d[8] * Xr[2];
+    const real *d = tr + 9 + 9 * k;
+    const real q0 = d[0] * Xr[0] + d[1] * Xr[1] + d[2] * Xr[2];
+    const real q1 = d[3] * Xr[0] + d[4] * Xr[1] + d[5] * Xr[2];
+    const real q2 = d[6] * Xr[0] + d[7] * Xr[1] + d[8] * Xr[2];
     ju[k] = A00 * q0 + A01 * q1 + A02 * q2;
     jv[k] = A10 * q0 + A11 * q1 + A12 * q2;
     // dP/dX_k = R[:,k]
-    const real c0 = (real)tab[k], c1 = (real)tab[3 + k], c2 = (real)tab[6 + k];
+    const real c0 = tr[k], c1 = tr[3 + k], c2 = tr[6 + k];
     ju[9 + k] = A00 * c0 + A01 * c1 + A02 * c2;
     jv[9 + k] = A10 * c0 + A11 * c1 + A12 * c2;
   }
@@ -120,30 +128,30 @@ __device__ __forceinline__ double eval_observation(const DeviceBatch &B, int64_t
   }
   bool ok = isfinite(ru) && isfinite(rv) && isfinite(cost);
   if (!unit_scale) {
-    const double *sc = B.cam_scale + 9 * (size_t)c;
-    const double *sp = B.pt_scale + 3 * (size_t)j;
+    const real *sc = reinterpret_cast<const real *>(MIXED ? (const void *)B.cam_scalef : (const void *)B.cam_scale) +
+                     9 * (size_t)c;
+    const real *sp = reinterpret_cast<const real *>(MIXED ? (const void *)B.pt_scalef : (const void *)B.pt_scale) +
+                     3 * (size_t)j;
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
-      const real s = (real)sc[k];
-      ju[k] *= s;
-      jv[k] *= s;
+      ju[k] *= sc[k];
+      jv[k] *= sc[k];
     }
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      const real s = (real)sp[k];
-      ju[9 + k] *= s;
-      jv[9 + k] *= s;
+      ju[9 + k] *= sp[k];
+      jv[9 + k] *= sp[k];
     }
   }
 #pragma unroll
   for (int k = 0; k < 9; ++k) {
     Jc[k] = mk2(ju[k], jv[k]);
-    ok = ok && isfinite((double)ju[k]) && isfinite((double)jv[k]);
+    ok = ok && isfinite(ju[k]) && isfinite(jv[k]);
   }
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     Jp[k] = mk2(ju[9 + k], jv[9 + k]);
-    ok = ok && isfinite((double)ju[9 + k]) && isfinite((double)jv[9 + k]);
+    ok = ok && isfinite(ju[9 + k]) && isfinite(jv[9 + k]);
   }
   r = mk2((real)ru, (real)rv);
   bad = !ok;
@@ -340,9 +348,11 @@ __global__ void k_scale_init(DeviceBatch B) {
   const int64_t ncam = 9 * (int64_t)B.nc, npt = 3 * (int64_t)B.np;
   if (i < ncam) {
     B.cam_scale[i] = B.opt.jacobi_scaling ? 1.0 / (1.0 + sqrt(B.cam_colnorm[i])) : 1.0;
+    B.cam_scalef[i] = (float)B.cam_scale[i];
   } else if (i < ncam + npt) {
     const int64_t k = i - ncam;
     B.pt_scale[k] = B.opt.jacobi_scaling ? 1.0 / (1.0 + sqrt(B.pt_colnorm[k])) : 1.0;
+    B.pt_scalef[k] = (float)B.pt_scale[k];
   }
 }
 

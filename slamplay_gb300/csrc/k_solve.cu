@@ -6,9 +6,12 @@
 // matrix S = B + Dc^2 - W C^-1 W^T is never formed: it is applied implicitly
 // inside a block-Jacobi PCG.
 //
-//  K3a k_point_prepare   per point: C = J_p^T J_p + Dp^2, FP64 inverse, Cinv g_p
-//  K3b k_camera_schur    per camera (CTA): S_ii, reduced rhs, 9x9 FP64 inverse,
-//                        PCG start (x = 0, r = v, z = M r)
+//  K3a k_point_schur     per chunk: C = J_p^T J_p + Dp^2, FP64 inverse, Cinv g_p,
+//                        and per (camera segment) the partial Schur diagonal
+//                        block and reduced rhs of the chunk's observations
+//  K3b k_camera_schur    per camera (CTA): S_ii and the reduced rhs from the
+//                        partials, parallel FP64 9x9 inverse, PCG start
+//                        (x = 0, r = v, z = M r)
 //  K4  (k_pcg.cu)        implicit-Schur PCG: mat-vec over point-segment
 //                        chunks, camera reduce, vector update
 //  K5  k_back_substitute per chunk: y_p = C^-1 (g_p - W^T y_c), model cost
@@ -29,183 +32,267 @@ __device__ __forceinline__ double lm_d2(double colnorm2, double radius, const De
 }
 
 // ---------------------------------------------------------------------------
-// K3a
-template <bool MIXED>
-__global__ void k_point_prepare(DeviceBatch B) {
-  typedef typename Prec<MIXED>::real real;
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= B.np) return;
-  LMState *L = B.lm + B.pt_problem[j];
-  if (!L->active) return;
-  const double radius = L->radius;
-  double C[6];
-#pragma unroll
-  for (int q = 0; q < 6; ++q) C[q] = B.pt_C[6 * (size_t)j + q];
-  C[0] += lm_d2(C[0], radius, B.opt);
-  C[3] += lm_d2(C[3], radius, B.opt);
-  C[5] += lm_d2(C[5], radius, B.opt);
-  double Ci[6];
-  if (!spd_inverse3(C, Ci)) {
-    L->linear_ok = 0;  // benign race: every writer stores 0
-    for (int q = 0; q < 6; ++q) Ci[q] = 0.0;
-  }
-  real *cio = reinterpret_cast<real *>(B.pt_Cinv) + 6 * (size_t)j;
-#pragma unroll
-  for (int q = 0; q < 6; ++q) {
-    cio[q] = (real)Ci[q];
-    B.pt_Cinv64[6 * (size_t)j + q] = Ci[q];
-  }
-  const double *g = B.pt_g + 3 * (size_t)j;
-  B.pt_t[3 * (size_t)j + 0] = Ci[0] * g[0] + Ci[1] * g[1] + Ci[2] * g[2];
-  B.pt_t[3 * (size_t)j + 1] = Ci[1] * g[0] + Ci[3] * g[1] + Ci[4] * g[2];
-  B.pt_t[3 * (size_t)j + 2] = Ci[2] * g[0] + Ci[4] * g[1] + Ci[5] * g[2];
-}
+// K3a: one CTA per point-segment chunk.
+//   1. per point (thread < pt_count): C = J_p^T J_p + Dp^2, its FP64 inverse,
+//      t = C^-1 g_p (kept for the back-substitution and the reduced rhs);
+//   2. per observation: the 2x2 A = J_p C^-1 J_p^T and e = J_p t, staged
+//      with J_c at the observation's slot in the chunk's camera-sorted order;
+//   3. per (camera segment, entry): the segment's share of the camera's
+//      Schur diagonal block, sum_obs J_c^T A J_c (45 packed entries), and of
+//      the reduced rhs, sum_obs J_c^T e (9), each summed over the segment's
+//      observations in slot order and written to the camera-major partial
+//      record of the segment (54 values).
+// Observations are read coalesced in point order; no global atomics.
+template <typename real>
+struct PointSchurSmem {
+  real jc[kChunkCap][18];  // J_c by slot (u, v interleaved per column)
+  real ae[kChunkCap][5];   // A00 A01 A11 e_u e_v by slot
+  real ci[kChunkCap][6];   // C^-1 by chunk point
+  real tp[kChunkCap][3];   // C^-1 g_p by chunk point
+};
 
-void launch_point_prepare(const DeviceBatch &b, bool mixed, cudaStream_t s) {
-  if (mixed)
-    k_point_prepare<true><<<(b.np + 255) / 256, 256, 0, s>>>(b);
-  else
-    k_point_prepare<false><<<(b.np + 255) / 256, 256, 0, s>>>(b);
-}
-
-// ---------------------------------------------------------------------------
-// 9x9 SPD inverse by Cholesky, FP64, one thread.  A and Ainv row-major.
-__device__ bool spd_inverse9(const double *A, double *Ainv) {
-  double L[45];  // packed lower by rows: L[i][j] at i*(i+1)/2 + j
-#define LL(i, j) L[(i) * ((i) + 1) / 2 + (j)]
-  for (int i = 0; i < 9; ++i) {
-    for (int j = 0; j <= i; ++j) {
-      double s = A[i * 9 + j];
-      for (int k = 0; k < j; ++k) s -= LL(i, k) * LL(j, k);
-      if (i == j) {
-        if (!(s > 0.0)) return false;
-        LL(i, i) = sqrt(s);
-      } else {
-        LL(i, j) = s / LL(j, j);
-      }
-    }
+__device__ __forceinline__ void sym9_pair(int e, int &a, int &b) {
+  a = 0;
+  int r = 9;
+  while (e >= r) {
+    e -= r;
+    --r;
+    ++a;
   }
-  // Y = L^{-1}, in place of L (lower)
-  double Y[45];
-  for (int j = 0; j < 9; ++j) {
-    for (int i = j; i < 9; ++i) {
-      double s = (i == j) ? 1.0 : 0.0;
-      for (int k = j; k < i; ++k) s -= LL(i, k) * Y[k * (k + 1) / 2 + j];
-      Y[i * (i + 1) / 2 + j] = s / LL(i, i);
-    }
-  }
-  for (int i = 0; i < 9; ++i)
-    for (int j = 0; j < 9; ++j) {
-      double s = 0.0;
-      const int k0 = i > j ? i : j;
-      for (int k = k0; k < 9; ++k) s += Y[k * (k + 1) / 2 + i] * Y[k * (k + 1) / 2 + j];
-      Ainv[i * 9 + j] = s;
-    }
-#undef LL
-  for (int q = 0; q < 81; ++q)
-    if (!isfinite(Ainv[q])) return false;
-  return true;
+  b = a + e;
 }
-
-// ---------------------------------------------------------------------------
-// K3b: one CTA per camera.
-constexpr int kSchurThreads = 128;
 
 template <bool MIXED>
-__global__ void __launch_bounds__(kSchurThreads) k_camera_schur(DeviceBatch B) {
+__global__ void __launch_bounds__(kChunkCap) k_point_schur(DeviceBatch B) {
   typedef typename Prec<MIXED>::real real;
   typedef typename Prec<MIXED>::real2 real2;
   typedef typename Acc<MIXED>::type Acc;
-  __shared__ double part[kSchurThreads / 32][54];
-  __shared__ double S[81];
-  __shared__ double Minv[81];
-  __shared__ double vec[9];
-  __shared__ double red[kSchurThreads / 32];
-  __shared__ int flag, okflag;
-  const int c = blockIdx.x;
-  const int p = B.cam_problem[c];
-  LMState *L = B.lm + p;
-  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-  const bool work = L->active != 0;
-  if (work) {
-    Acc acc[54];
-#pragma unroll
-    for (int q = 0; q < 54; ++q) acc[q].init();
-    const int e = B.cam_obs_begin[c + 1];
-    for (int k = B.cam_obs_begin[c] + t; k < e; k += kSchurThreads) {
-      const int64_t o = B.cam_obs_list[k];
-      const int j = B.obs_pt[o];
-      real2 Jc[9], Jp[3];
+  extern __shared__ __align__(16) unsigned char k3_smem[];
+  PointSchurSmem<real> &sm = *reinterpret_cast<PointSchurSmem<real> *>(k3_smem);
+  const int t = threadIdx.x;
+  for (int ch = blockIdx.x; ch < B.nchunks; ch += gridDim.x) {
+    const ChunkInfo ci = B.chunk[ch];
+    LMState *L = B.lm + ci.problem;
+    if (!L->active) continue;  // uniform over the CTA
+    const bool valid = t < ci.obs_count;
+    real2 Jc[9], Jp[3];
+    int lp = 0, slot = 0;
+    if (valid) {
+      const int64_t o = ci.obs_begin + t;
 #pragma unroll
       for (int q = 0; q < 9; ++q) Jc[q] = jload<real2>(B.jac, B.no, q, o);
 #pragma unroll
       for (int q = 0; q < 3; ++q) Jp[q] = jload<real2>(B.jac, B.no, 9 + q, o);
-      const real *Ci = reinterpret_cast<const real *>(B.pt_Cinv) + 6 * (size_t)j;
-      const real c0 = Ci[0], c1 = Ci[1], c2 = Ci[2], c3 = Ci[3], c4 = Ci[4], c5 = Ci[5];
-      // h = Cinv J_p^T rows
+      slot = B.obs_slot[o];
+      lp = B.obs_pt[o] - ci.pt_begin;
+    }
+    if (t < ci.pt_count) {
+      const int j = ci.pt_begin + t;
+      const double radius = L->radius;
+      double C[6];
+#pragma unroll
+      for (int q = 0; q < 6; ++q) C[q] = B.pt_C[6 * (size_t)j + q];
+      C[0] += lm_d2(C[0], radius, B.opt);
+      C[3] += lm_d2(C[3], radius, B.opt);
+      C[5] += lm_d2(C[5], radius, B.opt);
+      double Ci[6];
+      if (!spd_inverse3(C, Ci)) {
+        L->linear_ok = 0;  // benign race: every writer stores 0
+#pragma unroll
+        for (int q = 0; q < 6; ++q) Ci[q] = 0.0;
+      }
+      real *cio = reinterpret_cast<real *>(B.pt_Cinv) + 6 * (size_t)j;
+#pragma unroll
+      for (int q = 0; q < 6; ++q) {
+        cio[q] = (real)Ci[q];
+        B.pt_Cinv64[6 * (size_t)j + q] = Ci[q];
+        sm.ci[t][q] = (real)Ci[q];
+      }
+      const double *g = B.pt_g + 3 * (size_t)j;
+      const double g0 = g[0], g1 = g[1], g2 = g[2];
+      const double t0 = Ci[0] * g0 + Ci[1] * g1 + Ci[2] * g2;
+      const double t1 = Ci[1] * g0 + Ci[3] * g1 + Ci[4] * g2;
+      const double t2 = Ci[2] * g0 + Ci[4] * g1 + Ci[5] * g2;
+      B.pt_t[3 * (size_t)j + 0] = t0;
+      B.pt_t[3 * (size_t)j + 1] = t1;
+      B.pt_t[3 * (size_t)j + 2] = t2;
+      sm.tp[t][0] = (real)t0, sm.tp[t][1] = (real)t1, sm.tp[t][2] = (real)t2;
+    }
+    // the first (segment, entry) task of this thread: its metadata now
+    int f_b0 = 0, f_b1 = 0, f_slot = 0;
+    if (t < ci.seg_count * 54) {
+      const int sg = t / 54;
+      f_b0 = B.seg_pos[ci.seg_begin + sg];
+      f_b1 = (sg + 1 < ci.seg_count) ? B.seg_pos[ci.seg_begin + sg + 1] : ci.obs_count;
+      f_slot = B.seg_slot[ci.seg_begin + sg];
+    }
+    __syncthreads();
+    if (valid) {
+      const real c0 = sm.ci[lp][0], c1 = sm.ci[lp][1], c2 = sm.ci[lp][2];
+      const real c3 = sm.ci[lp][3], c4 = sm.ci[lp][4], c5 = sm.ci[lp][5];
       const real hu0 = c0 * Jp[0].x + c1 * Jp[1].x + c2 * Jp[2].x;
       const real hu1 = c1 * Jp[0].x + c3 * Jp[1].x + c4 * Jp[2].x;
       const real hu2 = c2 * Jp[0].x + c4 * Jp[1].x + c5 * Jp[2].x;
       const real hv0 = c0 * Jp[0].y + c1 * Jp[1].y + c2 * Jp[2].y;
       const real hv1 = c1 * Jp[0].y + c3 * Jp[1].y + c4 * Jp[2].y;
       const real hv2 = c2 * Jp[0].y + c4 * Jp[1].y + c5 * Jp[2].y;
-      const real a00 = Jp[0].x * hu0 + Jp[1].x * hu1 + Jp[2].x * hu2;
-      const real a01 = Jp[0].x * hv0 + Jp[1].x * hv1 + Jp[2].x * hv2;
-      const real a11 = Jp[0].y * hv0 + Jp[1].y * hv1 + Jp[2].y * hv2;
-      const double *tp = B.pt_t + 3 * (size_t)j;
-      const real t0 = (real)tp[0], t1 = (real)tp[1], t2 = (real)tp[2];
-      const real eu = Jp[0].x * t0 + Jp[1].x * t1 + Jp[2].x * t2;
-      const real ev = Jp[0].y * t0 + Jp[1].y * t1 + Jp[2].y * t2;
-      real gu[9], gv[9];
+      const real t0 = sm.tp[lp][0], t1 = sm.tp[lp][1], t2 = sm.tp[lp][2];
+      sm.ae[slot][0] = Jp[0].x * hu0 + Jp[1].x * hu1 + Jp[2].x * hu2;
+      sm.ae[slot][1] = Jp[0].x * hv0 + Jp[1].x * hv1 + Jp[2].x * hv2;
+      sm.ae[slot][2] = Jp[0].y * hv0 + Jp[1].y * hv1 + Jp[2].y * hv2;
+      sm.ae[slot][3] = Jp[0].x * t0 + Jp[1].x * t1 + Jp[2].x * t2;
+      sm.ae[slot][4] = Jp[0].y * t0 + Jp[1].y * t1 + Jp[2].y * t2;
 #pragma unroll
-      for (int b = 0; b < 9; ++b) {
-        gu[b] = a00 * Jc[b].x + a01 * Jc[b].y;
-        gv[b] = a01 * Jc[b].x + a11 * Jc[b].y;
-      }
-#pragma unroll
-      for (int a = 0; a < 9; ++a) {
-#pragma unroll
-        for (int b = a; b < 9; ++b) acc[sym9(a, b)].add(Jc[a].x * gu[b] + Jc[a].y * gv[b]);
-        acc[45 + a].add(Jc[a].x * eu + Jc[a].y * ev);
-      }
+      for (int q = 0; q < 9; ++q) sm.jc[slot][2 * q] = Jc[q].x, sm.jc[slot][2 * q + 1] = Jc[q].y;
     }
+    __syncthreads();
+    real *part = reinterpret_cast<real *>(B.schur_partial);
+    for (int i = t; i < ci.seg_count * 54; i += blockDim.x) {
+      const int sg = i / 54, en = i - 54 * sg;
+      int b0 = f_b0, b1 = f_b1, sl = f_slot;
+      if (i != t) {
+        b0 = B.seg_pos[ci.seg_begin + sg];
+        b1 = (sg + 1 < ci.seg_count) ? B.seg_pos[ci.seg_begin + sg + 1] : ci.obs_count;
+        sl = B.seg_slot[ci.seg_begin + sg];
+      }
+      Acc acc;
+      acc.init();
+      if (en < 45) {
+        int a, b;
+        sym9_pair(en, a, b);
+        for (int k = b0; k < b1; ++k) {
+          const real ua = sm.jc[k][2 * a], va = sm.jc[k][2 * a + 1];
+          const real ub = sm.jc[k][2 * b], vb = sm.jc[k][2 * b + 1];
+          const real A00 = sm.ae[k][0], A01 = sm.ae[k][1], A11 = sm.ae[k][2];
+          acc.add(ua * (A00 * ub + A01 * vb) + va * (A01 * ub + A11 * vb));
+        }
+      } else {
+        const int a = en - 45;
+        for (int k = b0; k < b1; ++k) acc.add(sm.jc[k][2 * a] * sm.ae[k][3] + sm.jc[k][2 * a + 1] * sm.ae[k][4]);
+      }
+      part[54 * (size_t)sl + en] = (real)acc.value();
+    }
+    __syncthreads();
+  }
+}
+
+size_t point_schur_smem(bool mixed) {
+  return mixed ? sizeof(PointSchurSmem<float>) : sizeof(PointSchurSmem<double>);
+}
+
+void launch_point_prepare(const DeviceBatch &b, bool mixed, cudaStream_t s) {
+  if (mixed)
+    k_point_schur<true><<<b.nchunks, kChunkCap, point_schur_smem(true), s>>>(b);
+  else
+    k_point_schur<false><<<b.nchunks, kChunkCap, point_schur_smem(false), s>>>(b);
+}
+
+// ---------------------------------------------------------------------------
+// In-place Gauss-Jordan inverse of a 9x9 SPD matrix in shared memory, one
+// thread per entry (threads 0..80; every thread of the CTA must call it).
+// Diagonal pivots in order: for an SPD matrix every pivot is a Schur
+// complement pivot, positive exactly when the matrix is positive definite,
+// so no row exchange is needed.  Step k maps
+//   a_kk -> 1/p,  a_kj -> a_kj / p,  a_ik -> -a_ik / p,
+//   a_ij -> a_ij - a_ik a_kj / p  (p = a_kk);
+// after nine steps the buffer holds A^-1.  Two buffers alternate so one
+// barrier per step suffices.  Returns false (in every thread) when a pivot
+// is not positive or an entry is not finite.
+__device__ bool spd_inverse9_gj(double (*buf)[81]) {
+  const int t = threadIdx.x;
+  const int i = t / 9, j = t - 9 * (t / 9);
+  int cur = 0;
+  bool ok = true;
+  for (int k = 0; k < 9; ++k) {
+    const double p = buf[cur][10 * k];
+    if (!(p > 0.0)) ok = false;  // uniform: every thread reads the same pivot
+    if (ok && t < 81) {
+      const double pinv = recip_nr(p);
+      double v;
+      if (i == k && j == k)
+        v = pinv;
+      else if (i == k)
+        v = buf[cur][t] * pinv;
+      else if (j == k)
+        v = -buf[cur][t] * pinv;
+      else
+        v = fma(-(buf[cur][9 * i + k] * pinv), buf[cur][9 * k + j], buf[cur][t]);
+      buf[cur ^ 1][t] = v;
+    }
+    __syncthreads();
+    cur ^= 1;
+  }
+  const bool fin = t >= 81 || isfinite(buf[cur][t]);
+  return __syncthreads_and(fin ? 1 : 0) && ok;
+}
+
+// ---------------------------------------------------------------------------
+// K3b: one CTA per camera: S_ii = B + Dc^2 - sum of the segment partials,
+// reduced rhs v = g_c - sum of the rhs partials, the FP64 inverse of S_ii
+// (block-Jacobi preconditioner), and the PCG start (x = 0, r = v, z = M r).
+constexpr int kSchurThreads = 96;
+
+template <bool MIXED>
+__global__ void __launch_bounds__(kSchurThreads) k_camera_schur(DeviceBatch B) {
+  typedef typename Prec<MIXED>::real real;
+  typedef typename Acc<MIXED>::type Acc;
+  __shared__ double buf[2][81];
+  __shared__ double sums[54];
+  __shared__ double vec[9];
+  __shared__ double red[kSchurThreads / 32];
+  __shared__ int flag;
+  const int c = blockIdx.x;
+  const int p = B.cam_problem[c];
+  LMState *L = B.lm + p;
+  const int t = threadIdx.x;
+  const bool work = L->active != 0;
+  if (work) {
+    // sums of the camera's segment partials, in segment order (FP64: four
+    // interleaved accumulators, combined pairwise)
+    if (t < 54) {
+      const real *part = reinterpret_cast<const real *>(B.schur_partial) + t;
+      const int s0 = B.cam_seg_begin[c], s1 = B.cam_seg_begin[c + 1];
+      constexpr int kBatch = 16;
+      constexpr int kAcc = MIXED ? 1 : 4;
+      Acc a[kAcc];
 #pragma unroll
-    for (int q = 0; q < 54; ++q) {
-      const double v = warp_sum(acc[q].value());
-      if (lane == 0) part[warp][q] = v;
+      for (int u = 0; u < kAcc; ++u) a[u].init();
+      for (int s = s0; s < s1; s += kBatch) {
+        real v[kBatch];
+#pragma unroll
+        for (int u = 0; u < kBatch; ++u) v[u] = (s + u < s1) ? part[54 * (size_t)(s + u)] : (real)0;
+#pragma unroll
+        for (int u = 0; u < kBatch; ++u)
+          if (s + u < s1) a[u % kAcc].add(v[u]);
+      }
+      double sum = a[0].value();
+      if (kAcc == 4) sum = (a[0].value() + a[1 % kAcc].value()) + (a[2 % kAcc].value() + a[3 % kAcc].value());
+      sums[t] = sum;
     }
     __syncthreads();
     const double radius = L->radius;
     if (t < 81) {
       const int a = t / 9, b = t % 9;
-      double s = 0.0;
-      for (int w = 0; w < kSchurThreads / 32; ++w) s += part[w][sym9(a, b)];
-      double v = B.cam_B[45 * (size_t)c + sym9(a, b)] - s;
+      double v = B.cam_B[45 * (size_t)c + sym9(a, b)] - sums[sym9(a, b)];
       if (a == b) {
         const double d2 = lm_d2(B.cam_B[45 * (size_t)c + sym9(a, a)], radius, B.opt);
         v += d2;
         B.cam_D2[9 * (size_t)c + a] = d2;
       }
-      S[t] = v;
+      buf[0][t] = v;
     }
-    if (t < 9) {
-      double s = 0.0;
-      for (int w = 0; w < kSchurThreads / 32; ++w) s += part[w][45 + t];
-      vec[t] = B.cam_g[9 * (size_t)c + t] - s;
-    }
+    if (t < 9) vec[t] = B.cam_g[9 * (size_t)c + t] - sums[45 + t];
     __syncthreads();
-    if (t == 0) {
-      okflag = spd_inverse9(S, Minv) ? 1 : 0;
-      if (!okflag) {
-        L->linear_ok = 0;
-        for (int q = 0; q < 81; ++q) Minv[q] = 0.0;
-      }
+    const bool ok = spd_inverse9_gj(buf);  // result in buf[1] (nine steps)
+    if (!ok) {
+      if (t == 0) L->linear_ok = 0;
+      if (t < 81) buf[1][t] = 0.0;
     }
     __syncthreads();
     double rz = 0.0, rr = 0.0;
     if (t < 9) {
       double z = 0.0;
-      for (int k = 0; k < 9; ++k) z += Minv[t * 9 + k] * vec[k];
+      for (int k = 0; k < 9; ++k) z += buf[1][t * 9 + k] * vec[k];
       const size_t i = 9 * (size_t)c + t;
       B.pcg_v[i] = vec[t];
       B.pcg_r[i] = vec[t];
@@ -217,8 +304,8 @@ __global__ void __launch_bounds__(kSchurThreads) k_camera_schur(DeviceBatch B) {
       rr = vec[t] * vec[t];
     }
     if (t < 81) {
-      B.cam_Minv[81 * (size_t)c + t] = Minv[t];
-      if (MIXED) B.cam_Minvf[81 * (size_t)c + t] = (float)Minv[t];
+      B.cam_Minv[81 * (size_t)c + t] = buf[1][t];
+      if (MIXED) B.cam_Minvf[81 * (size_t)c + t] = (float)buf[1][t];
     }
     if (MIXED && t < 45) B.cam_Bf[45 * (size_t)c + t] = (float)B.cam_B[45 * (size_t)c + t];
     const double rzs = block_sum(rz, red);
@@ -255,8 +342,6 @@ __global__ void __launch_bounds__(kSchurThreads) k_camera_schur(DeviceBatch B) {
       }
       B.status[2] = any;
       B.status[3] = count;
-      B.global_counter[kGC_BAR_COUNT] = 0u;  // persistent PCG barrier starts empty
-      __threadfence();
       if (B.use_cond && B.pcg_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)B.pcg_cond, any ? 1u : 0u);
     }
   }
@@ -269,6 +354,12 @@ void launch_camera_schur(const DeviceBatch &b, bool mixed, cudaStream_t s) {
     k_camera_schur<false><<<b.nc, kSchurThreads, 0, s>>>(b);
 }
 
+// Large dynamic shared memory of the point-Schur kernel (FP64 form).
+void point_schur_init() {
+  cudaFuncSetAttribute(k_point_schur<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)point_schur_smem(true));
+  cudaFuncSetAttribute(k_point_schur<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)point_schur_smem(false));
+}
+
 
 // ---------------------------------------------------------------------------
 // K5: y_p = C^-1 (g_p - W^T y_c), step = -y, model cost change
@@ -276,10 +367,14 @@ void launch_camera_schur(const DeviceBatch &b, bool mixed, cudaStream_t s) {
 // arithmetic in both modes (the acceptance ratio is FP64).
 template <bool MIXED>
 __global__ void __launch_bounds__(kChunkCap) k_back_substitute(DeviceBatch B) {
+  // mixed form: the inner products with the FP32 Jacobian run in FP32; the
+  // point step y = C^-1 (g_p - W^T y_c), the candidate points and the model
+  // cost change stay FP64
+  typedef typename Prec<MIXED>::real real;
   typedef typename Prec<MIXED>::real2 real2;
-  __shared__ double yseg[kChunkCap][9];
-  __shared__ double W[kChunkCap][3];
-  __shared__ double ypt[kChunkCap][3];
+  __shared__ real yseg[kChunkCap][9];
+  __shared__ real W[kChunkCap][3];
+  __shared__ real ypt[kChunkCap][3];
   __shared__ double red[kChunkCap / 32];
   const int t = threadIdx.x;
   for (int ch = blockIdx.x; ch < B.nchunks; ch += gridDim.x) {
@@ -289,11 +384,12 @@ __global__ void __launch_bounds__(kChunkCap) k_back_substitute(DeviceBatch B) {
     const int parity = L->parity;
     for (int i = t; i < ci.seg_count * 9; i += blockDim.x) {
       const int s = i / 9, q = i - 9 * s;
-      yseg[s][q] = B.pcg_x[9 * (size_t)B.seg_cam[ci.seg_begin + s] + q];
+      yseg[s][q] = (real)B.pcg_x[9 * (size_t)B.seg_cam[ci.seg_begin + s] + q];
     }
     __syncthreads();
     const bool valid = t < ci.obs_count;
-    double Jpu[3], Jpv[3], zu = 0.0, zv = 0.0, ru = 0.0, rv = 0.0;
+    real Jpu[3], Jpv[3], zu = 0, zv = 0;
+    double ru = 0.0, rv = 0.0;
     int lp = 0;
     if (valid) {
       const int64_t o = ci.obs_begin + t;
@@ -302,8 +398,8 @@ __global__ void __launch_bounds__(kChunkCap) k_back_substitute(DeviceBatch B) {
 #pragma unroll
       for (int q = 0; q < 9; ++q) {
         const real2 J = jload<real2>(B.jac, B.no, q, o);
-        zu += (double)J.x * yseg[s][q];
-        zv += (double)J.y * yseg[s][q];
+        zu += J.x * yseg[s][q];
+        zv += J.y * yseg[s][q];
       }
 #pragma unroll
       for (int q = 0; q < 3; ++q) {
@@ -321,15 +417,15 @@ __global__ void __launch_bounds__(kChunkCap) k_back_substitute(DeviceBatch B) {
     if (t < ci.pt_count) {
       const int jj = ci.pt_begin + t;
       const int b0 = B.pt_obs_begin[jj] - ci.obs_begin, b1 = B.pt_obs_begin[jj + 1] - ci.obs_begin;
-      double w0 = 0.0, w1 = 0.0, w2 = 0.0;
+      real w0 = 0, w1 = 0, w2 = 0;
       for (int k = b0; k < b1; ++k) w0 += W[k][0], w1 += W[k][1], w2 += W[k][2];
       const double *g = B.pt_g + 3 * (size_t)jj;
-      const double a0 = g[0] - w0, a1 = g[1] - w1, a2 = g[2] - w2;
+      const double a0 = g[0] - (double)w0, a1 = g[1] - (double)w1, a2 = g[2] - (double)w2;
       const double *Ci = B.pt_Cinv64 + 6 * (size_t)jj;
       const double y0 = Ci[0] * a0 + Ci[1] * a1 + Ci[2] * a2;
       const double y1 = Ci[1] * a0 + Ci[3] * a1 + Ci[4] * a2;
       const double y2 = Ci[2] * a0 + Ci[4] * a1 + Ci[5] * a2;
-      ypt[t][0] = y0, ypt[t][1] = y1, ypt[t][2] = y2;
+      ypt[t][0] = (real)y0, ypt[t][1] = (real)y1, ypt[t][2] = (real)y2;
       const double *x = B.pt_param[parity] + 4 * (size_t)jj;
       double *xc = B.pt_param[parity ^ 1] + 4 * (size_t)jj;
       const double *sc = B.pt_scale + 3 * (size_t)jj;
@@ -346,8 +442,8 @@ __global__ void __launch_bounds__(kChunkCap) k_back_substitute(DeviceBatch B) {
     __syncthreads();
     double model = 0.0;
     if (valid) {
-      const double m0 = -(zu + Jpu[0] * ypt[lp][0] + Jpu[1] * ypt[lp][1] + Jpu[2] * ypt[lp][2]);
-      const double m1 = -(zv + Jpv[0] * ypt[lp][0] + Jpv[1] * ypt[lp][1] + Jpv[2] * ypt[lp][2]);
+      const double m0 = -(double)(zu + Jpu[0] * ypt[lp][0] + Jpu[1] * ypt[lp][1] + Jpu[2] * ypt[lp][2]);
+      const double m1 = -(double)(zv + Jpv[0] * ypt[lp][0] + Jpv[1] * ypt[lp][1] + Jpv[2] * ypt[lp][2]);
       model = m0 * (ru + m0 / 2.0) + m1 * (rv + m1 / 2.0);
     }
     const double ms = block_sum(model, red);

@@ -26,6 +26,22 @@ struct Prec<true> {
   typedef float2 real2;
 };
 
+// 1/a: the FP32 hardware reciprocal refined by two Newton-Raphson steps
+// x <- x + x (1 - a x), each of which doubles the number of correct bits
+// (about 23 -> 46 -> FP64 rounding).  Falls back to a division outside the
+// FP32 normal range.
+__device__ __forceinline__ double recip_nr(double a) {
+  const double aa = fabs(a);
+  if (!(aa > 1e-30 && aa < 1e30)) return 1.0 / a;
+  float xf;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(xf) : "f"((float)a));
+  double x = (double)xf;
+  double e = fma(-a, x, 1.0);
+  x = fma(x, e, x);
+  e = fma(-a, x, 1.0);
+  return fma(x, e, x);
+}
+
 __device__ __forceinline__ double2 mk2(double a, double b) { return make_double2(a, b); }
 __device__ __forceinline__ float2 mk2(float a, float b) { return make_float2(a, b); }
 
@@ -248,6 +264,7 @@ __device__ inline void camera_table_entry(const double *cam, double *tab, bool d
 // ---------------------------------------------------------------------------
 struct Proj {
   double P[3];
+  double iz;  // 1 / P_z
   double xp, yp, r2, dist, f, k1, k2;
   double ru, rv;
 };
@@ -256,8 +273,10 @@ __device__ __forceinline__ void project(const double *tab, const double *X, doub
 #pragma unroll
   for (int i = 0; i < 3; ++i)
     o.P[i] = tab[3 * i + 0] * X[0] + tab[3 * i + 1] * X[1] + tab[3 * i + 2] * X[2] + tab[36 + i];
-  o.xp = -o.P[0] / o.P[2];
-  o.yp = -o.P[1] / o.P[2];
+  // one reciprocal of P_z (within an FP64 rounding of -P_x / P_z, -P_y / P_z)
+  o.iz = recip_nr(o.P[2]);
+  o.xp = -o.P[0] * o.iz;
+  o.yp = -o.P[1] * o.iz;
   o.f = tab[39];
   o.k1 = tab[40];
   o.k2 = tab[41];
@@ -340,35 +359,29 @@ __device__ __forceinline__ void jstore(void *jac, int64_t no, int k, int64_t o, 
   reinterpret_cast<R2 *>(jac)[(int64_t)k * no + o] = v;
 }
 
-// 3x3 symmetric positive-definite inverse via Cholesky (FP64).  In/out in the
-// packed sym3 order.  Returns false when not positive definite.
+// Inverse of a symmetric 3x3 block (packed 00 01 02 11 12 22) by cofactors
+// and one reciprocal of the determinant (GB300 issues FP64 square roots and
+// divisions slowly; a Cholesky inverse needs three and nine of them).
+// Positive definiteness by Sylvester's criterion: the leading principal
+// minors C00, C00 C11 - C01^2 and det C must be positive, which is exactly
+// when a Cholesky factorisation succeeds.
 __device__ __forceinline__ bool spd_inverse3(const double *C, double *Ci) {
-  const double l00s = C[0];
-  if (!(l00s > 0.0)) return false;
-  const double l00 = sqrt(l00s);
-  const double l10 = C[1] / l00;
-  const double l20 = C[2] / l00;
-  const double l11s = C[3] - l10 * l10;
-  if (!(l11s > 0.0)) return false;
-  const double l11 = sqrt(l11s);
-  const double l21 = (C[4] - l20 * l10) / l11;
-  const double l22s = C[5] - l20 * l20 - l21 * l21;
-  if (!(l22s > 0.0)) return false;
-  const double l22 = sqrt(l22s);
-  // Y = L^{-1}
-  const double y00 = 1.0 / l00;
-  const double y11 = 1.0 / l11;
-  const double y22 = 1.0 / l22;
-  const double y10 = -(l10 * y00) / l11;
-  const double y21 = -(l21 * y11) / l22;
-  const double y20 = -(l20 * y00 + l21 * y10) / l22;
-  // Ci = Y^T Y
-  Ci[0] = y00 * y00 + y10 * y10 + y20 * y20;
-  Ci[1] = y10 * y11 + y20 * y21;
-  Ci[2] = y20 * y22;
-  Ci[3] = y11 * y11 + y21 * y21;
-  Ci[4] = y21 * y22;
-  Ci[5] = y22 * y22;
+  const double a = C[0], b = C[1], c = C[2], d = C[3], e = C[4], f = C[5];
+  const double m00 = d * f - e * e;
+  const double m01 = c * e - b * f;
+  const double m02 = b * e - c * d;
+  const double m11 = a * f - c * c;
+  const double m12 = b * c - a * e;
+  const double m22 = a * d - b * b;
+  const double det = a * m00 + b * m01 + c * m02;
+  if (!(a > 0.0) || !(m22 > 0.0) || !(det > 0.0)) return false;
+  const double id = recip_nr(det);
+  Ci[0] = m00 * id;
+  Ci[1] = m01 * id;
+  Ci[2] = m02 * id;
+  Ci[3] = m11 * id;
+  Ci[4] = m12 * id;
+  Ci[5] = m22 * id;
   return isfinite(Ci[0]) && isfinite(Ci[3]) && isfinite(Ci[5]);
 }
 

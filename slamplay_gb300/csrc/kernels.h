@@ -32,6 +32,7 @@ void launch_schur_matvec(const DeviceBatch &b, bool mixed, cudaStream_t s);
 cudaError_t launch_pcg_camera(const DeviceBatch &b, bool mixed, cudaStream_t s);
 // Largest cluster size the camera-side kernel may use on this device.
 int pcg_max_cluster();
+void point_schur_init();
 size_t pcg_camera_smem(int passes, int cluster);
 // K5: point back-substitution, model cost change, candidate points.
 void launch_back_substitute(const DeviceBatch &b, bool mixed, cudaStream_t s);
