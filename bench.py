@@ -44,6 +44,7 @@ def config_dict(problem, extra=None) -> dict:
                      f"{problem.num_observations()} obs, 50 LM iters, PCG<=100",
          "num_cameras": problem.num_cameras(), "num_points": problem.num_points(),
          "num_observations": problem.num_observations(), "lm_iterations": 50, "pcg_cap": 100,
+         "pcg": "residual criterion 1e-6, at most 100 iterations per LM step",
          "l2": "flushed between steps (256 MiB write on the solver stream, outside the timed events)",
          "parallelism": "replicas"}
     if extra:
@@ -155,8 +156,24 @@ def run_reference(args) -> None:
 
 
 def launches_per_solve(s) -> int:
-    # setup: sync, init, table, eval x2 (2 kernels each), scale, post, gather
-    return 10 + 10 * s.num_iterations + 3 * s.num_linear_solver_iterations
+    """Kernels of one solve: setup (parameter sync, LM state, camera table,
+    two evaluations of two kernels each, Jacobi scale, post-evaluation) and
+    the gather = 10; per LM iteration point/Schur chunk, camera Schur, back-
+    substitution, candidate cameras, candidate cost, decide, camera table,
+    evaluation (chunk + camera), post-evaluation = 10; per PCG iteration the
+    mat-vec and the camera-side kernel = 2."""
+    return 10 + 10 * s.num_iterations + 2 * s.num_linear_solver_iterations
+
+
+def ncu_traffic(kernel: str):
+    """DRAM bytes per launch of `kernel` on this workload from the committed
+    ncu summary (dram__bytes_read.sum + dram__bytes_write.sum), or None."""
+    p = os.path.join(ROOT, "profiles", "dram_traffic_config1.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        d = json.load(f)
+    return d.get("kernels", {}).get(kernel)
 
 
 def run_gpu(args) -> None:
@@ -238,18 +255,24 @@ def run_gpu(args) -> None:
     sm.solve(problem.copy())
     sm.set_profiling(False)
     prof = [e for e in sm.profile() if e["launches"] > 0]
-    top = max(prof, key=lambda e: e["total_ms"]) if prof else None
     peaks = measured_peaks()
+    peak = peaks.get("hbm_gbs", 6800.0)
+    for e in prof:
+        e["avg_us"] = 1e3 * e["total_ms"] / e["launches"]
+        e["gbs"] = e["bytes"] / e["launches"] / (e["avg_us"] * 1e-6) / 1e9 if e["avg_us"] > 0 else None
+    top = max(prof, key=lambda e: e["total_ms"]) if prof else None
     roof = None
     if top:
         avg_ms = top["total_ms"] / top["launches"]
         bytes_per = top["bytes"] / top["launches"]
         ach = bytes_per / (avg_ms * 1e-3) / 1e9
-        peak = peaks.get("hbm_gbs", 6800.0)
         roof = {"kernel": top["name"], "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
-                "frac": ach / peak, "traffic": None, "bytes_per_launch": bytes_per, "avg_launch_ms": avg_ms,
+                "frac": ach / peak, "traffic": ncu_traffic(top["name"]), "bytes_per_launch": bytes_per,
+                "avg_launch_ms": avg_ms,
+                "timing": "CUDA events around each launch on the solver stream, host-driven pass of the same "
+                          "solve (kernels inside the conditional graph cannot be bracketed one by one)",
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if not peaks.get("fallback")
-                else "fallback 6.8 TB/s"}
+                else "fallback 6.8 TB/s (of fallback)"}
     if rank == 0:
         cb = cpu_baseline() if world == 1 else None
         line = {
@@ -283,17 +306,36 @@ def run_gpu(args) -> None:
         dist.destroy_process_group()
 
 
+def run_profile_solve(args) -> None:
+    """One solve of the workload with the host driving the loops (every
+    kernel a plain stream launch, as ncu needs: it cannot profile kernels of
+    a graph with conditional nodes).  No event timing: ncu times the
+    kernels itself."""
+    from slamplay_gb300 import BALProblem, Solver
+
+    problem = BALProblem.synthetic(1, seed=0)
+    with Solver(use_graphs=0, **workload_options(args.precision)) as s:
+        sm = s.solve(problem.copy())
+    print(json.dumps({"precision": args.precision, "lm_iterations": sm.num_iterations,
+                      "pcg_iterations": sm.num_linear_solver_iterations, "final_cost": sm.final_cost}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gba", choices=["gba", "reference"])
+    ap.add_argument("--profile-solve", action="store_true",
+                    help="one host-driven solve with per-kernel event timing (the command profiled with ncu)")
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     args = ap.parse_args()
     from slamplay_gb300 import build as B
 
     B.build()
-    if args.impl == "reference":
+    if args.profile_solve:
+        run_profile_solve(args)
+    elif args.impl == "reference":
         from oracle import oracle_py
 
         oracle_py.ensure_built()

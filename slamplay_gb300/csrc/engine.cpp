@@ -341,8 +341,15 @@ void Engine::destroy_graph() {
   graph_key_.clear();
 }
 
+// Profiling runs one launch at a time and waits for it, so the GPU is idle
+// when the next launch is queued.  A short delay kernel ahead of the start
+// event keeps the GPU busy while the host queues the event and the measured
+// kernel: the event pair then brackets the kernel's device time only, not
+// the host's launch latency.
 void Engine::prof_begin(cudaStream_t s) {
-  if (profiling_) cudaEventRecord(pev_[0], s);
+  if (!profiling_) return;
+  launch_prof_delay(s);
+  cudaEventRecord(pev_[0], s);
 }
 void Engine::prof_end(cudaStream_t s, int entry, double bytes) {
   if (!profiling_) return;
@@ -497,8 +504,13 @@ gba_status Engine::build_graph(std::string *err) {
   if ((e = add_while(cap_[0], pcgh, &pcgbody)) != cudaSuccess) return fail(e, "PCG conditional node");
   e = cudaStreamBeginCaptureToGraph(cap_[1], pcgbody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) return fail(e, "capture PCG body");
-  launch_schur_matvec(db_, mixed_, cap_[1]);
-  if ((e = launch_pcg_camera(db_, mixed_, cap_[1])) != cudaSuccess) return fail(e, "PCG camera kernel");
+  // kPcgUnroll PCG iterations per body (a finished PCG turns the extra
+  // launches into early exits); inside the body each kernel is a
+  // programmatic dependent of the one before it
+  for (int u = 0; u < kPcgUnroll; ++u) {
+    if ((e = launch_schur_matvec(db_, mixed_, cap_[1], pdl_ && u > 0)) != cudaSuccess) return fail(e, "mat-vec kernel");
+    if ((e = launch_pcg_camera(db_, mixed_, cap_[1], pdl_)) != cudaSuccess) return fail(e, "PCG camera kernel");
+  }
   if ((e = cudaStreamEndCapture(cap_[1], &tmp)) != cudaSuccess) return fail(e, "end capture PCG body");
   enqueue_lm_tail(cap_[0]);
   if ((e = cudaStreamEndCapture(cap_[0], &tmp)) != cudaSuccess) return fail(e, "end capture LM body");
@@ -569,10 +581,10 @@ gba_status Engine::run_host_driven(std::string *err) {
     while (hstat[2] && pcg <= o_.max_linear_solver_iterations) {
       ++pcg;
       prof_begin(stream_);
-      launch_schur_matvec(db_, mixed_, stream_);
+      if ((st = check(launch_schur_matvec(db_, mixed_, stream_, false), "mat-vec kernel", err)) != GBA_OK) return st;
       prof_end(stream_, PF_MATVEC, bytes_matvec(db_));
       prof_begin(stream_);
-      if ((st = check(launch_pcg_camera(db_, mixed_, stream_), "PCG camera kernel", err)) != GBA_OK) return st;
+      if ((st = check(launch_pcg_camera(db_, mixed_, stream_, false), "PCG camera kernel", err)) != GBA_OK) return st;
       prof_end(stream_, PF_PCGCAM, bytes_pcg_camera(db_));
       if ((st = read_status()) != GBA_OK) return st;
     }
@@ -596,7 +608,12 @@ gba_status Engine::run_solve(std::string *err) {
   if ((st = check(cudaEventRecord(ev_start_, stream_), "event", err)) != GBA_OK) return st;
   if (o_.use_graphs && !profiling_) {
     if (!exec_ || graph_key_ != cur_key_) {
-      if ((st = build_graph(err)) != GBA_OK) return st;
+      st = build_graph(err);
+      if (st != GBA_OK && pdl_) {
+        pdl_ = false;  // a driver without programmatic edges in conditional bodies
+        st = build_graph(err);
+      }
+      if (st != GBA_OK) return st;
     }
     if ((st = check(cudaGraphLaunch(exec_, stream_), "cudaGraphLaunch", err)) != GBA_OK) return st;
   } else {

@@ -88,6 +88,7 @@ class Engine {
   int trace_cap_ = 0;
   int sm_count_ = 0;
   int max_cluster_ = 8;    // largest cluster the camera-side PCG kernel may use
+  bool pdl_ = true;        // programmatic dependent launches inside the PCG body
 };
 
 }  // namespace gba

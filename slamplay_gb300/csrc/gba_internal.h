@@ -165,6 +165,8 @@ constexpr int kPcgScal = 4;
 constexpr int kPS_PQ = 0, kPS_RZ = 1, kPS_RR = 2, kPS_QX = 3;
 // cameras per CTA in the warp-per-camera camera kernels
 constexpr int kCamPerBlock = 8;
+// PCG iterations per body of the graph's PCG loop
+constexpr int kPcgUnroll = 2;
 // cameras per block of the camera-side PCG kernel (one thread per coordinate)
 constexpr int kPcgBlockCams = 32;
 // dynamic shared memory the camera-side PCG kernel may use (4 doubles per

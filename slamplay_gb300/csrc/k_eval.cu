@@ -505,6 +505,16 @@ void launch_cost_only(const DeviceBatch &b, cudaStream_t s) {
   if (b.nchunks > 0) k_cost_chunk<<<b.nchunks, kChunkCap, 0, s>>>(b);
 }
 
+// Busy-waits about 40 microseconds of SM clock (a fixed cycle count, so it
+// always ends), used by the profiling pass only.
+__global__ void k_prof_delay(long long cycles) {
+  const long long t0 = clock64();
+  while (clock64() - t0 < cycles) {
+  }
+}
+
+void launch_prof_delay(cudaStream_t s) { k_prof_delay<<<1, 1, 0, s>>>(80000LL); }
+
 // Fails with cudaErrorNoKernelImageForDevice when the sm_103a image cannot
 // run on the current device.
 cudaError_t probe_kernel_image() {

@@ -46,6 +46,17 @@ struct MatvecSmem {
 
 __device__ __forceinline__ bool pcg_live(const LMState *L) { return L->active != 0 && L->pcg_active != 0; }
 
+// Programmatic dependent launch: the two PCG kernels alternate, each launched
+// as a dependent of the other, so that one starts (and issues every load that
+// does not depend on the other's results) while the other is still running.
+// wait: returns once the preceding kernel of the stream has completed and
+// its writes are visible (immediately when there is no such dependency).
+// A kernel lets its dependent launch only after its own wait has returned:
+// the dependent's early loads may then read anything the kernel before the
+// preceding one wrote.
+__device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -59,7 +70,6 @@ __global__ void __launch_bounds__(kChunkCap) k_schur_matvec(DeviceBatch B) {
   const int t = threadIdx.x;
   for (int ch = blockIdx.x; ch < B.nchunks; ch += gridDim.x) {
     const ChunkInfo ci = B.chunk[ch];
-    if (!pcg_live(B.lm + ci.problem)) continue;  // uniform over the CTA
     const bool valid = t < ci.obs_count;
     // every load that depends only on the chunk is issued before the first
     // barrier, so one memory round trip covers them all
@@ -93,6 +103,12 @@ __global__ void __launch_bounds__(kChunkCap) k_schur_matvec(DeviceBatch B) {
       f_b1 = (sg + 1 < ci.seg_count) ? B.seg_pos[ci.seg_begin + sg + 1] : ci.obs_count;
       f_slot = B.seg_slot[ci.seg_begin + sg];
     }
+    // everything above is fixed during the PCG; from here on the kernel reads
+    // what the previous camera-side kernel wrote (and overwrites the partials
+    // it read)
+    pdl_wait();
+    pdl_launch_dependents();
+    if (!pcg_live(B.lm + ci.problem)) continue;  // uniform over the CTA
     // stage the direction p of the chunk's cameras
     const real *pdir = reinterpret_cast<const real *>(MIXED ? (const void *)B.pcg_pf : (const void *)B.pcg_p);
     for (int i = t; i < ci.seg_count * 9; i += blockDim.x) {
@@ -267,6 +283,7 @@ __device__ __forceinline__ double pcg_phase1(const DeviceBatch &B, const Problem
     prow[kk] = pv[kk];
     st.m[kk] = M[kk];
   }
+  pdl_wait();  // the partials come from the mat-vec kernel
   // the camera's partials: the first kBatch in one round trip, then batches.
   // FP64: four interleaved accumulators (partial s to accumulator
   // (s - s0) % 4) shorten the chain of 64-cycle additions fourfold; mixed:
@@ -387,6 +404,8 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg_camera(DeviceBatch B) {
       CamCoord<real> t;
       push1(b, pcg_phase1<MIXED>(B, pi, b * kPcgBlockCams + lc, q, t));
     }
+    pdl_wait();  // every thread, whether or not it had a camera coordinate
+    pdl_launch_dependents();
     cluster_arrive();
     cluster_wait();
     if (warp == 0) {
@@ -486,10 +505,14 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg_camera(DeviceBatch B) {
       }
     }
   } else if (B.num_problems == 1 && blockIdx.x == 0 && tid == 0) {
+    pdl_wait();
+    pdl_launch_dependents();
     B.status[2] = 0;
     if (B.use_cond && B.pcg_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)B.pcg_cond, 0u);
   }
   if (B.num_problems == 1) return;
+  pdl_wait();
+  pdl_launch_dependents();
   // several problems: the last cluster to finish sets the PCG loop condition
   if (cs > 1 && rank != 0) return;
   if (last_block_done(B.global_counter + kGC_UPDATE, (uint32_t)(gridDim.x / cs), &flag)) {
@@ -503,33 +526,44 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg_camera(DeviceBatch B) {
 }
 
 // ---------------------------------------------------------------------------
-void launch_schur_matvec(const DeviceBatch &b, bool mixed, cudaStream_t s) {
-  if (mixed)
-    k_schur_matvec<true><<<b.nchunks, kChunkCap, 0, s>>>(b);
-  else
-    k_schur_matvec<false><<<b.nchunks, kChunkCap, 0, s>>>(b);
+// pdl: launch as a programmatic dependent of the preceding kernel of the
+// stream (which must be the other PCG kernel).
+cudaError_t launch_schur_matvec(const DeviceBatch &b, bool mixed, cudaStream_t s, bool pdl) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)b.nchunks);
+  cfg.blockDim = dim3(kChunkCap);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = pdl ? 1 : 0;
+  if (mixed) return cudaLaunchKernelEx(&cfg, k_schur_matvec<true>, b);
+  return cudaLaunchKernelEx(&cfg, k_schur_matvec<false>, b);
 }
 
-cudaError_t launch_pcg_camera(const DeviceBatch &b, bool mixed, cudaStream_t s) {
+cudaError_t launch_pcg_camera(const DeviceBatch &b, bool mixed, cudaStream_t s, bool pdl) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(b.num_problems * b.pcg_cluster));
   cfg.blockDim = dim3(kPcgThreads);
   cfg.dynamicSmemBytes = pcg_camera_smem(b.pcg_passes, b.pcg_cluster);
   cfg.stream = s;
-  cudaLaunchAttribute attr[1];
+  cudaLaunchAttribute attr[2];
   attr[0].id = cudaLaunchAttributeClusterDimension;
   attr[0].val.clusterDim.x = (unsigned)b.pcg_cluster;
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
+  attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[1].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
-  cfg.numAttrs = 1;
+  cfg.numAttrs = pdl ? 2 : 1;
   if (mixed) return cudaLaunchKernelEx(&cfg, k_pcg_camera<true>, b);
   return cudaLaunchKernelEx(&cfg, k_pcg_camera<false>, b);
 }
 
 void launch_pcg_iteration(const DeviceBatch &b, bool mixed, cudaStream_t s) {
-  launch_schur_matvec(b, mixed, s);
-  launch_pcg_camera(b, mixed, s);
+  launch_schur_matvec(b, mixed, s, false);
+  launch_pcg_camera(b, mixed, s, false);
 }
 
 // Slots of every camera block of the largest problem (passes x cluster size),
