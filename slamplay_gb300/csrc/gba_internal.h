@@ -168,7 +168,7 @@ constexpr int kCamPerBlock = 8;
 // PCG iterations per body of the graph's PCG loop
 constexpr int kPcgUnroll = 2;
 // cameras per block of the camera-side PCG kernel (one thread per coordinate)
-constexpr int kPcgBlockCams = 32;
+constexpr int kPcgBlockCams = 16;
 // dynamic shared memory the camera-side PCG kernel may use (4 doubles per
 // camera block of the largest problem: 204,800 cameras)
 constexpr size_t kPcgSmemMax = 200 * 1024;

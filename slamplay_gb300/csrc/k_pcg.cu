@@ -170,15 +170,15 @@ __global__ void __launch_bounds__(kChunkCap) k_schur_matvec(DeviceBatch B) {
 
 // ---------------------------------------------------------------------------
 // K4b: one cluster per problem.  A CTA works on camera blocks of
-// kPcgBlockCams cameras with one thread per camera coordinate (9 per camera,
-// so a block is exactly nine full warps and no lane idles); a problem with
-// more blocks than the cluster has CTAs takes several passes.
+// kPcgBlockCams cameras with one thread per camera coordinate (9 per
+// camera); a problem with more blocks than the cluster has CTAs takes
+// several passes.
 //
 // Every problem-wide dot product is summed in a fixed order that depends
-// only on the problem's camera count: the 288 per-thread values of a block
-// are staged in shared memory and warp 0 adds them (nine per lane in a fixed
-// pairwise tree, then a xor butterfly) -- one warp of FP64 additions instead
-// of nine, since GB300 issues FP64 at a small fraction of its FP32 rate; the
+// only on the problem's camera count: the per-thread values of a block are
+// staged in shared memory and warp 0 adds them (in thread order per lane,
+// then a xor butterfly) -- one warp of FP64 additions instead of one per
+// warp, since GB300 issues FP64 at a small fraction of its FP32 rate; the
 // block value is pushed into the shared memory of every CTA of the cluster
 // (remote stores, one lane per destination) at the block's slot; after a
 // cluster barrier every CTA adds the slots of all blocks in block order,
@@ -189,7 +189,7 @@ __global__ void __launch_bounds__(kChunkCap) k_schur_matvec(DeviceBatch B) {
 //
 // The state of the first kPcgRegPasses passes stays in registers between
 // the phases; every load of a pass is issued before the first barrier.
-constexpr int kPcgThreads = 9 * kPcgBlockCams;  // 288
+constexpr int kPcgThreads = 9 * kPcgBlockCams;
 
 namespace {
 
@@ -228,11 +228,14 @@ __device__ __forceinline__ void block_push(cg::cluster_group &cl, double (*red)[
   for (int k = 0; k < NV; ++k) red[k][tid] = v[k];
   __syncthreads();
   if (tid < 32) {
+    constexpr int kWarps = (kPcgThreads + 31) / 32;
     double s[NV];
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
-      const double *r = red[k] + lane;
-      s[k] = (((r[0] + r[32]) + (r[64] + r[96])) + ((r[128] + r[160]) + (r[192] + r[224]))) + r[256];
+      s[k] = 0.0;
+#pragma unroll
+      for (int w = 0; w < kWarps; ++w)
+        if (lane + 32 * w < kPcgThreads) s[k] += red[k][lane + 32 * w];
       s[k] = warp_sum(s[k]);
     }
     if (lane < cs) {
