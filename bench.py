@@ -275,6 +275,10 @@ def run_gpu(args) -> None:
                 else "fallback 6.8 TB/s (of fallback)"}
     if rank == 0:
         cb = cpu_baseline() if world == 1 else None
+        extra_forms = {}
+        if world == 1 and not args.no_extra_forms:
+            extra_forms["batched"] = batched_form()
+            extra_forms["serving"] = serving_form()
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_m, "higher_is_better": True, "scaling": "weak",
@@ -288,6 +292,7 @@ def run_gpu(args) -> None:
                          "lm_iterations": iters_p, "pcg_iterations": first_p.num_linear_solver_iterations,
                          "final_cost": first_p.final_cost},
                 "mixed_vs_fp64_final_cost_rel": abs(first_m.final_cost - first_p.final_cost) / first_p.final_cost,
+                **extra_forms,
             },
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": 1e3 * e2e_s},
@@ -304,6 +309,95 @@ def run_gpu(args) -> None:
     if dist:
         dist.barrier()
         dist.destroy_process_group()
+
+
+PCG_SMALL = dict(pcg_criterion="residual", pcg_tolerance=1e-6, max_linear_solver_iterations=100)
+
+
+def batched_form(n_problems: int = 1024, repeats: int = 2, seq_sample: int = 32) -> dict:
+    """Configuration 3: 1,024 local-BA windows (5-40 cameras, 200-5,000
+    points, 2-8 views) solved as one batch (every LM iteration of every
+    problem in one graph launch), to convergence or 50 iterations, PCG as in
+    configuration 1.  Timed re-runs from the initial point on the device;
+    beside it the plain FP64 solver on the same problems one at a time
+    (first `seq_sample` problems)."""
+    from slamplay_gb300 import BALProblem, Solver
+
+    probs = [BALProblem.synthetic(3, index=i, seed=0) for i in range(n_problems)]
+    out = {"workload": f"config3: {n_problems} problems, {sum(p.num_observations() for p in probs)} obs",
+           "pcg": "residual 1e-6, <= 100"}
+    for prec in ("mixed", "fp64"):
+        with Solver(precision=prec, max_num_iterations=50, **PCG_SMALL) as s:
+            sums = s.batch_solve([p.copy() for p in probs])
+            ts = []
+            for _ in range(repeats):
+                t0 = time.perf_counter()
+                s.solve_resident(1)
+                s.synchronize()
+                ts.append(time.perf_counter() - t0)
+        its = sum(x.num_iterations for x in sums)
+        t = min(ts)
+        out[prec] = {"solves_per_s": n_problems / t, "lm_iters_per_s": its / t, "s_per_batch": t,
+                     "lm_iterations": its, "converged": sum(1 for x in sums if x.termination_type == "CONVERGENCE")}
+    with Solver(precision="fp64", max_num_iterations=50, **PCG_SMALL) as s:
+        t0 = time.perf_counter()
+        its = sum(s.solve(p.copy()).num_iterations for p in probs[:seq_sample])
+        dt = time.perf_counter() - t0
+    out["sequential_fp64"] = {"solves_per_s": seq_sample / dt, "lm_iters_per_s": its / dt,
+                              "sample": f"first {seq_sample} problems, one gba_solve each"}
+    out["mixed_batched_vs_sequential_fp64_solves"] = out["mixed"]["solves_per_s"] / out["sequential_fp64"]["solves_per_s"]
+    return out
+
+
+def serving_form(n_requests: int = 60, rate_mult: float = 2.0, seq_sample: int = 16) -> dict:
+    """Configuration 4: requests generated as configuration 1 with 10-400
+    cameras and 1k-150k points (log-uniform), solved to relative cost
+    decrease < 1e-6 or 50 iterations.  A sequential plain FP64 loop sets the
+    reference rate; the mixed-precision server then takes `n_requests`
+    Poisson arrivals at `rate_mult` x that rate (continuous batching over
+    four engine slots); latency = completion seen by the client - submit."""
+    import numpy as np
+
+    from slamplay_gb300 import BALProblem, Solver
+
+    reqs = [BALProblem.synthetic(4, index=i, seed=0) for i in range(n_requests)]
+    opts = dict(max_num_iterations=50, function_tolerance=1e-6, **PCG_SMALL)
+    with Solver(precision="fp64", **opts) as s:
+        t0 = time.perf_counter()
+        for r in reqs[:seq_sample]:
+            s.solve(r.copy())
+        seq = seq_sample / (time.perf_counter() - t0)
+    rate = seq * rate_mult
+    rng = np.random.default_rng(1)
+    gaps = rng.exponential(1.0 / rate, size=n_requests)
+    work = [r.copy() for r in reqs]
+    sub_t, done_t = {}, {}
+    with Solver(precision="mixed", **opts) as s:
+        s.start_server()
+        t_start = time.perf_counter()
+        next_t, i, pending = t_start, 0, set()
+        while i < n_requests or pending:
+            now = time.perf_counter()
+            while i < n_requests and now >= next_t:
+                tk = s.submit(work[i])
+                sub_t[tk] = now
+                pending.add(tk)
+                next_t += gaps[i]
+                i += 1
+            for tk in list(pending):
+                if s.poll(tk) is not None:
+                    done_t[tk] = time.perf_counter()
+                    pending.discard(tk)
+            time.sleep(0.0002)
+        total = time.perf_counter() - t_start
+        st = s.server_stats()
+        s.stop_server()
+    lat = np.array([done_t[k] - sub_t[k] for k in done_t])
+    return {"workload": f"config4: {n_requests} Poisson requests, mean "
+                        f"{int(np.mean([r.num_observations() for r in reqs]))} obs",
+            "arrival_rate_per_s": rate, "solves_per_s": n_requests / total, "p50_ms": 1e3 * float(np.percentile(lat, 50)),
+            "p99_ms": 1e3 * float(np.percentile(lat, 99)), "peak_live": st.get("peak_live"),
+            "sequential_fp64_solves_per_s": seq, "sequential_sample": f"first {seq_sample} requests"}
 
 
 def run_profile_solve(args) -> None:
@@ -329,6 +423,8 @@ def main():
     ap.add_argument("--profile-solve", action="store_true",
                     help="one host-driven solve with per-kernel event timing (the command profiled with ncu)")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--no-extra-forms", action="store_true",
+                    help="skip the batched (configuration 3) and serving (configuration 4) forms")
     args = ap.parse_args()
     from slamplay_gb300 import build as B
 
