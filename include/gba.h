@@ -122,7 +122,10 @@ typedef struct gba_options {
   int32_t chunk_observations;         /* point-segment tile (obs per CTA), 0 = auto  */
   int32_t reorder_points;             /* 1 = group points by first camera (locality) */
   int32_t use_graphs;                 /* 1 = run the LM loop as one CUDA graph       */
-  int32_t reserved[8];
+  int32_t pcg_unroll;                 /* PCG iterations per graph body, 0 = auto (2) */
+  int32_t autotune;                   /* 1 = run gba_autotune on the first solve of a
+                                         new problem-size bucket                     */
+  int32_t reserved[6];
 } gba_options;
 
 /* Per-solve report, the subset of ceres::Solver::Summary the reference
@@ -247,6 +250,29 @@ gba_status gba_compute_step(gba_handle *h, const gba_problem_view *p, double rad
 gba_status gba_solve_resident(gba_handle *h, int32_t repeats);
 /* Waits for all work queued on the handle's stream. */
 gba_status gba_synchronize(gba_handle *h);
+
+/* ---- autotuner ------------------------------------------------------------
+ * Times short trial solves (3 LM iterations, tolerances off, PCG capped at
+ * 20 iterations) of the given problem(s) over a grid of launch shapes --
+ * point-segment tile size (observations per CTA: 256, 192, 128) x PCG
+ * iterations per graph body (1, 2, 4) -- on a scratch engine, keeps the
+ * fastest, and sets it on the handle (later solves use it).  The problems
+ * are not modified.  Results are cached per size bucket (number of
+ * problems, log2 of observations and cameras, precision) for the process.
+ * No counterpart in the reference (Ceres has no launch shapes to tune). */
+#define GBA_TUNE_MAX_TRIALS 16
+typedef struct gba_tune_result {
+  int32_t chunk_observations; /* chosen tile size                           */
+  int32_t pcg_unroll;         /* chosen PCG iterations per graph body       */
+  int32_t num_trials;         /* 0 when the answer came from the cache      */
+  int32_t from_cache;
+  double best_ms;             /* device time of the chosen trial solve      */
+  double trial_ms[GBA_TUNE_MAX_TRIALS];
+  int32_t trial_chunk[GBA_TUNE_MAX_TRIALS];
+  int32_t trial_unroll[GBA_TUNE_MAX_TRIALS];
+} gba_tune_result;
+gba_status gba_autotune(gba_handle *h, const gba_problem_view *problems, int32_t num_problems,
+                        gba_tune_result *result);
 
 /* ---- allocation-free evaluation ----------------------------------------- */
 /* A problem whose arrays are already in DEVICE memory (BALProblem layout,

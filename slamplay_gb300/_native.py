@@ -44,7 +44,7 @@ class Options(C.Structure):
         ("pcg_tolerance", C.c_double), ("eta", C.c_double),
         ("minimizer_progress_to_stdout", C.c_int32), ("device", C.c_int32), ("stream", C.c_void_p),
         ("chunk_observations", C.c_int32), ("reorder_points", C.c_int32), ("use_graphs", C.c_int32),
-        ("reserved", C.c_int32 * 8),
+        ("pcg_unroll", C.c_int32), ("autotune", C.c_int32), ("reserved", C.c_int32 * 6),
     ]
 
 
@@ -100,6 +100,14 @@ class ServerStats(C.Structure):
     ]
 
 
+class TuneResult(C.Structure):
+    _fields_ = [
+        ("chunk_observations", C.c_int32), ("pcg_unroll", C.c_int32), ("num_trials", C.c_int32),
+        ("from_cache", C.c_int32), ("best_ms", C.c_double), ("trial_ms", C.c_double * 16),
+        ("trial_chunk", C.c_int32 * 16), ("trial_unroll", C.c_int32 * 16),
+    ]
+
+
 class GBAError(RuntimeError):
     def __init__(self, status: int, message: str):
         super().__init__(f"{STATUS.get(status, status)}: {message}")
@@ -111,6 +119,7 @@ _lib = None
 
 # name -> (restype, argtypes)
 _SIGS = {
+    "gba_autotune": (C.c_int, [C.c_void_p, C.POINTER(ProblemView), C.c_int32, C.POINTER(TuneResult)]),
     "gba_options_init": (None, [C.POINTER(Options)]),
     "gba_create": (C.c_int, [C.POINTER(Options), C.POINTER(C.c_void_p)]),
     "gba_destroy": (None, [C.c_void_p]),

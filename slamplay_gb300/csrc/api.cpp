@@ -28,7 +28,19 @@ const char *gba_io_last_error(void);
 namespace gba {
 // The calling thread's handle-less error message (gba_last_error(NULL)).
 std::string &thread_error_message() { return g_create_error; }
+gba_status autotune(Engine &target, const gba_problem_view *problems, int n, gba_tune_result *out, std::string *err);
+bool tune_cached(const gba_problem_view *problems, int n, int precision);
 }  // namespace gba
+
+namespace {
+// gba_options.autotune: tune on the first solve of a new size bucket.
+gba_status maybe_autotune(gba_handle *h, const gba_problem_view *p, int n, std::string *err) {
+  const gba_options &o = h->engine->options();
+  if (!o.autotune) return GBA_OK;
+  gba_tune_result r;
+  return gba::autotune(*h->engine, p, n, &r, err);
+}
+}  // namespace
 
 extern "C" {
 
@@ -62,6 +74,8 @@ void gba_options_init(gba_options *o) {
   o->chunk_observations = 0;
   o->reorder_points = 1;
   o->use_graphs = 1;
+  o->pcg_unroll = 0;
+  o->autotune = 0;
 }
 
 const char *gba_version(void) { return "gba 1 sm_103a"; }
@@ -115,7 +129,8 @@ gba_status gba_solve(gba_handle *h, const gba_problem_view *p, gba_summary *s) {
   if (!p) return fail(h, GBA_ERR_INVALID_ARGUMENT, "null problem");
   if (h->server && h->server->running()) return fail(h, GBA_ERR_INVALID_ARGUMENT, "handle is serving");
   std::string err;
-  const gba_status st = h->engine->solve(p, 1, s, &err);
+  gba_status st = maybe_autotune(h, p, 1, &err);
+  if (st == GBA_OK) st = h->engine->solve(p, 1, s, &err);
   if (st != GBA_OK) return fail(h, st, err);
   return GBA_OK;
 }
@@ -125,7 +140,23 @@ gba_status gba_batch_solve(gba_handle *h, const gba_problem_view *problems, int3
   if (!problems || n <= 0) return fail(h, GBA_ERR_INVALID_ARGUMENT, "empty batch");
   if (h->server && h->server->running()) return fail(h, GBA_ERR_INVALID_ARGUMENT, "handle is serving");
   std::string err;
-  const gba_status st = h->engine->solve(problems, n, summaries, &err);
+  gba_status st = maybe_autotune(h, problems, n, &err);
+  if (st == GBA_OK) st = h->engine->solve(problems, n, summaries, &err);
+  if (st != GBA_OK) return fail(h, st, err);
+  return GBA_OK;
+}
+
+gba_status gba_autotune(gba_handle *h, const gba_problem_view *problems, int32_t n, gba_tune_result *result) {
+  if (!h) return GBA_ERR_INVALID_ARGUMENT;
+  if (!problems || n <= 0 || !result) return fail(h, GBA_ERR_INVALID_ARGUMENT, "empty batch or null result");
+  if (h->server && h->server->running()) return fail(h, GBA_ERR_INVALID_ARGUMENT, "handle is serving");
+  for (int i = 0; i < n; ++i) {
+    std::string verr;
+    const gba_status vs = gba::validate_problem(&problems[i], &verr);
+    if (vs != GBA_OK) return fail(h, vs, verr);
+  }
+  std::string err;
+  const gba_status st = gba::autotune(*h->engine, problems, n, result, &err);
   if (st != GBA_OK) return fail(h, st, err);
   return GBA_OK;
 }

@@ -119,6 +119,20 @@ gba_status Engine::init(std::string *err) {
   return GBA_OK;
 }
 
+PrepOptions Engine::prep_options() const {
+  PrepOptions po;
+  po.reorder_points = o_.reorder_points != 0;
+  if (o_.chunk_observations > 0) po.chunk_cap = std::max(32, std::min(kChunkCap, (int)o_.chunk_observations));
+  return po;
+}
+
+void Engine::set_tuning(int chunk_observations, int pcg_unroll) {
+  o_.chunk_observations = chunk_observations;
+  o_.pcg_unroll = pcg_unroll;
+  destroy_graph();
+  cur_key_.clear();
+}
+
 // Cluster shape of the camera-side PCG kernel: one CTA per camera block
 // (kPcgBlockCams cameras) of the largest problem, capped by the device's
 // cluster limit; the remaining blocks are taken in passes.
@@ -504,10 +518,11 @@ gba_status Engine::build_graph(std::string *err) {
   if ((e = add_while(cap_[0], pcgh, &pcgbody)) != cudaSuccess) return fail(e, "PCG conditional node");
   e = cudaStreamBeginCaptureToGraph(cap_[1], pcgbody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) return fail(e, "capture PCG body");
-  // kPcgUnroll PCG iterations per body (a finished PCG turns the extra
+  // pcg_unroll (default kPcgUnroll) PCG iterations per body (a finished PCG turns the extra
   // launches into early exits); inside the body each kernel is a
   // programmatic dependent of the one before it
-  for (int u = 0; u < kPcgUnroll; ++u) {
+  const int unroll = o_.pcg_unroll > 0 ? std::min(o_.pcg_unroll, 8) : kPcgUnroll;
+  for (int u = 0; u < unroll; ++u) {
     if ((e = launch_schur_matvec(db_, mixed_, cap_[1], pdl_ && u > 0)) != cudaSuccess) return fail(e, "mat-vec kernel");
     if ((e = launch_pcg_camera(db_, mixed_, cap_[1], pdl_)) != cudaSuccess) return fail(e, "PCG camera kernel");
   }
@@ -675,8 +690,7 @@ gba_status Engine::download(const HostBatch &hb, const gba_problem_view *v, gba_
 
 gba_status Engine::solve(const gba_problem_view *v, int n, gba_summary *s, std::string *err) {
   const double t0 = now_s();
-  PrepOptions po;
-  po.reorder_points = o_.reorder_points != 0;
+  PrepOptions po = prep_options();
   HostBatch hb;
   gba_status st = prepare_batch(v, n, po, &hb, err);
   if (st != GBA_OK) return st;
@@ -705,8 +719,7 @@ gba_status Engine::solve(const gba_problem_view *v, int n, gba_summary *s, std::
 
 gba_status Engine::evaluate(const gba_problem_view *v, double *residuals, double *jacobians, double *cost,
                             std::string *err) {
-  PrepOptions po;
-  po.reorder_points = o_.reorder_points != 0;
+  PrepOptions po = prep_options();
   HostBatch hb;
   gba_status st = prepare_batch(v, 1, po, &hb, err);
   if (st != GBA_OK) return st;
@@ -759,8 +772,7 @@ gba_status Engine::evaluate(const gba_problem_view *v, double *residuals, double
 
 gba_status Engine::compute_step(const gba_problem_view *v, double radius, double *delta, double *model,
                                 int *pcg_iterations, std::string *err) {
-  PrepOptions po;
-  po.reorder_points = o_.reorder_points != 0;
+  PrepOptions po = prep_options();
   HostBatch hb;
   gba_status st = prepare_batch(v, 1, po, &hb, err);
   if (st != GBA_OK) return st;

@@ -33,6 +33,10 @@ class Engine {
   void set_profiling(bool on) { profiling_ = on; }
   const std::vector<ProfileEntry> &profile() const { return profile_; }
   const gba_options &options() const { return o_; }
+  // Launch shapes chosen by the autotuner (takes effect on the next upload).
+  void set_tuning(int chunk_observations, int pcg_unroll);
+  double last_solve_ms() const { return last_solve_ms_; }
+  PrepOptions prep_options() const;
   cudaStream_t stream() const { return stream_; }
   size_t device_bytes() const { return d_cap_; }
 

@@ -124,8 +124,7 @@ bool Server::launch_cohort(Slot &s, std::vector<std::shared_ptr<Request>> &&reqs
   s.views.clear();
   for (auto &r : s.reqs) s.views.push_back(r->view);
   std::string err;
-  PrepOptions po;
-  po.reorder_points = o_.reorder_points != 0;
+  const PrepOptions po = s.engine->prep_options();
   gba_status st = prepare_batch(s.views.data(), (int)s.views.size(), po, &s.hb, &err);
   if (st == GBA_OK) st = s.engine->upload(s.hb, &err);
   if (st == GBA_OK) st = s.engine->run_solve(&err);

@@ -154,6 +154,21 @@ class Solver:
         N.check(N.lib().gba_batch_solve(self._h, views, n, sums), self._h, "gba_batch_solve")
         return [_summary(s, t) for s, t in zip(sums, trs)]
 
+    def autotune(self, problems: BALProblem | Sequence[BALProblem]) -> dict:
+        """Picks the fastest launch shapes (tile size, PCG iterations per
+        graph body) for these problems by timed trial solves; later solves on
+        this handle use them.  The problems are not modified."""
+        if isinstance(problems, BALProblem):
+            problems = [problems]
+        views = (N.ProblemView * len(problems))(*[p.view() for p in problems])
+        r = N.TuneResult()
+        N.check(N.lib().gba_autotune(self._h, views, len(problems), N.C.byref(r)), self._h, "gba_autotune")
+        n = min(r.num_trials, 16)
+        return {"chunk_observations": r.chunk_observations, "pcg_unroll": r.pcg_unroll, "best_ms": r.best_ms,
+                "from_cache": bool(r.from_cache),
+                "trials": [{"chunk_observations": r.trial_chunk[i], "pcg_unroll": r.trial_unroll[i],
+                            "ms": r.trial_ms[i]} for i in range(n)]}
+
     def evaluate(self, problem: BALProblem):
         """(residuals [no,2], jacobians [no,2,12], cost) evaluated on the GPU."""
         no = problem.num_observations()

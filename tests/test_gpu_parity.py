@@ -225,3 +225,23 @@ def test_golden_fixture_fp64(loss):
                                                             g["parameters"]), 1e4)
         ref = g["step_radius_1e4"]
         assert np.linalg.norm(d - ref) <= 1e-6 * np.linalg.norm(ref)
+
+
+def test_autotune_picks_a_shape_and_keeps_the_solution():
+    """The tuner's launch shapes change which thread adds which partial,
+    never what is solved: FP64 final cost within 1e-9 relative of the
+    untuned solve; the problem is not modified by tuning; the second call
+    for the same size bucket comes from the cache."""
+    b = small_problem(num_points=1200)
+    before = b.parameters().copy()
+    opts = dict(max_num_iterations=10, pcg_tolerance=1e-12, max_linear_solver_iterations=500, **FIXED)
+    with Solver(**opts) as s:
+        ref = s.solve(b.copy())
+    with Solver(**opts) as s:
+        r = s.autotune(b)
+        assert np.array_equal(b.parameters(), before)
+        assert r["chunk_observations"] in (128, 192, 256) and r["pcg_unroll"] in (1, 2, 4)
+        assert len(r["trials"]) == 9 and min(t["ms"] for t in r["trials"]) == r["best_ms"]
+        tuned = s.solve(b.copy())
+        assert s.autotune(b)["from_cache"]
+    assert abs(tuned.final_cost - ref.final_cost) <= 1e-9 * ref.final_cost
