@@ -125,7 +125,9 @@ struct DeviceBatch {
   float *cam_Minvf;          // 81, FP32 copy (mixed form)
   float *cam_Bf;             // 45, FP32 copy of cam_B (mixed form)
   double *cam_D2;            // 9: squared LM diagonal of the camera parameters
-  double *pcg_x, *pcg_r, *pcg_z, *pcg_p, *pcg_q, *pcg_v;  // 9 * nc each
+  // PCG vectors, 9 * nc each: x, r, z (= u = M r), p, q (= s = S p), v (rhs),
+  // w (= S u, kept for camera blocks beyond the register-held passes)
+  double *pcg_x, *pcg_r, *pcg_z, *pcg_p, *pcg_q, *pcg_v, *pcg_w;
   float *pcg_pf;             // 9 * nc, FP32 copy of the direction (mixed form)
   double *cam_colnorm;       // 9 * nc: column norms of the first evaluation
   double *pt_colnorm;        // 3 * np

@@ -2,28 +2,37 @@
 // reduced camera system  S x = v,  S = B + Dc^2 - W C^-1 W^T,  with the
 // block-Jacobi preconditioner M = blockdiag(S_ii)^-1 (built by K3b).
 //
+// The PCG is the Chronopoulos-Gear single-reduction form of preconditioned
+// CG: the same iterates as the textbook recurrence in exact arithmetic, but
+// the mat-vec is applied to the preconditioned residual u = M r and both dot
+// products of an iteration come from one reduction, so the camera side needs
+// one cluster barrier per iteration instead of two:
+//   w_k = S u_k;  gamma_k = r_k.u_k;  delta_k = u_k.w_k;
+//   beta_k = gamma_k / gamma_{k-1};  alpha_k = gamma_k / (delta_k - beta_k gamma_k / alpha_{k-1})
+//   (k = 0: beta = 0, alpha = gamma / delta);
+//   p_k = u_k + beta_k p_{k-1};  s_k = w_k + beta_k s_{k-1}  (s = S p);
+//   x_{k+1} = x_k + alpha_k p_k;  r_{k+1} = r_k - alpha_k s_k;  u_{k+1} = M r_{k+1}.
+// The stopping test of call k looks at r_k and x_k (residual ratio, or Ceres'
+// quadratic-model test on Q(x_k) = -x_k.(v + r_k)), i.e. one mat-vec after
+// the textbook loop would have tested them; x is only updated when the loop
+// goes on, so the returned x_k is the same iterate.
+//
 // One PCG iteration is two kernels:
 //   K4a k_schur_matvec  mat-vec over point-segment chunks (one CTA per chunk,
-//       one thread per observation): w = J_p^T J_c p, t_j = C_j^-1 sum_j w,
-//       u = J_c^T J_p t_j written at the observation's slot in the chunk's
+//       one thread per observation): y = J_p^T J_c u, t_j = C_j^-1 sum_j y,
+//       J_c^T J_p t_j written at the observation's slot in the chunk's
 //       camera-sorted order, summed per camera run into one partial per
 //       (chunk, camera), stored at the camera's contiguous (camera-major)
 //       position.  No global atomics; every sum has a fixed order.
 //   K4b k_pcg_camera    everything on the camera side, one thread-block
 //       cluster per problem (up to 16 CTAs, one thread per camera
-//       coordinate):
-//         q = (B + Dc^2) p - sum of the camera's partials;   p.q
-//         alpha = r.z / p.q;  x += alpha p;  r -= alpha q;  z = M r;
-//         r.z, r.r, x.(v + r);  stopping test (residual ratio or Ceres'
-//         quadratic-model test);  beta;  p = z + beta p.
-//       The problem-wide dot products are reduced inside the cluster (warp
-//       -> CTA shared memory -> every CTA reads all CTAs' sums over
-//       distributed shared memory in rank order), so every CTA holds the
-//       same alpha / beta / decision without any global atomic or spin.
+//       coordinate): w = (B + Dc^2) u - sum of the camera's partials; the
+//       four dot products r.u, u.w, r.r, x.(v + r) in one cluster
+//       reduction; stopping test; alpha, beta; p, s, x, r, u = M r.
 // GB300 runs FP64 at 1/55 of FP32 throughput and with 64-cycle dependent
 // latency, so in the mixed form the matrix-like inner work (partial sums,
-// (B + Dc^2) p, M r) runs in FP32 with compensated sums while the vectors
-// x, r, z, p, q and every dot product stay FP64.
+// (B + Dc^2) u, M r) runs in FP32 with compensated sums while the vectors
+// x, r, u, p, s and every dot product stay FP64.
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
@@ -109,8 +118,8 @@ __global__ void __launch_bounds__(kChunkCap) k_schur_matvec(DeviceBatch B) {
     pdl_wait();
     pdl_launch_dependents();
     if (!pcg_live(B.lm + ci.problem)) continue;  // uniform over the CTA
-    // stage the direction p of the chunk's cameras
-    const real *pdir = reinterpret_cast<const real *>(MIXED ? (const void *)B.pcg_pf : (const void *)B.pcg_p);
+    // stage the vector u of the chunk's cameras
+    const real *pdir = reinterpret_cast<const real *>(MIXED ? (const void *)B.pcg_pf : (const void *)B.pcg_z);
     for (int i = t; i < ci.seg_count * 9; i += blockDim.x) {
       const int sg = i / 9, q = i - 9 * sg;
       sm.pseg[sg][q] = pdir[9 * (size_t)B.seg_cam[ci.seg_begin + sg] + q];
@@ -174,22 +183,24 @@ __global__ void __launch_bounds__(kChunkCap) k_schur_matvec(DeviceBatch B) {
 // camera); a problem with more blocks than the cluster has CTAs takes
 // several passes.
 //
-// Every problem-wide dot product is summed in a fixed order that depends
-// only on the problem's camera count: the per-thread values of a block are
-// staged in shared memory and warp 0 adds them (in thread order per lane,
-// then a xor butterfly) -- one warp of FP64 additions instead of one per
-// warp, since GB300 issues FP64 at a small fraction of its FP32 rate; the
-// block value is pushed into the shared memory of every CTA of the cluster
-// (remote stores, one lane per destination) at the block's slot; after a
-// cluster barrier every CTA adds the slots of all blocks in block order,
-// strided over the lanes of one warp, and combines them with a butterfly.  All CTAs therefore hold the same alpha, beta and stopping
+// The four problem-wide dot products are summed in a fixed order that
+// depends only on the problem's camera count: the per-thread values of a
+// block are staged in shared memory and warp 0 adds them (in thread order
+// per lane, then a xor butterfly) -- one warp of FP64 additions instead of
+// one per warp, since GB300 issues FP64 at a small fraction of its FP32
+// rate; the block values are pushed into the shared memory of every CTA of
+// the cluster (remote stores, one lane per destination) at the block's
+// slot; after the cluster barrier every CTA adds the slots of all blocks in
+// block order, strided over the lanes of one warp, and combines them with a
+// butterfly.  All CTAs therefore hold the same alpha, beta and stopping
 // decision, and the result depends neither on the cluster size nor on the
-// other problems of a batch.  After the second barrier no CTA touches
-// another CTA's shared memory, so the kernel needs two cluster barriers.
+// other problems of a batch.  After the barrier no CTA touches another
+// CTA's shared memory.
 //
-// The state of the first kPcgRegPasses passes stays in registers between
-// the phases; every load of a pass is issued before the first barrier.
+// The state of the first kPcgRegPasses passes stays in registers across the
+// barrier; every load of a pass is issued before it.
 constexpr int kPcgThreads = 9 * kPcgBlockCams;
+constexpr int kPcgNv = 4;  // r.u, u.w, r.r, x.(v + r)
 
 namespace {
 
@@ -247,43 +258,46 @@ __device__ __forceinline__ void block_push(cg::cluster_group &cl, double (*red)[
   __syncthreads();  // red may be reused
 }
 
-// One camera coordinate of a pass: everything the three phases need.
+// One camera coordinate of a pass.
 template <typename real>
 struct CamCoord {
   bool valid;
   int c;
-  double p, q, x, r, v, z;
+  double x, r, u, p, s, v, w;
   real m[9];  // row of the block-Jacobi preconditioner
 };
 
-// Phase 1 of one coordinate: loads the pass state and computes
-// q = (B + Dc^2) p - sum of partials.  Returns p.q (0 when not valid).
+// Phase 1 of one coordinate: loads the pass state, waits for the mat-vec,
+// computes w = (B + Dc^2) u - sum of partials and the four dot-product terms.
 template <bool MIXED>
-__device__ __forceinline__ double pcg_phase1(const DeviceBatch &B, const ProblemInfo &pi, int k, int q,
-                                             CamCoord<typename Prec<MIXED>::real> &st) {
+__device__ __forceinline__ void pcg_phase1(const DeviceBatch &B, const ProblemInfo &pi, int k, int q, bool first,
+                                           CamCoord<typename Prec<MIXED>::real> &st, double *d) {
   typedef typename Prec<MIXED>::real real;
   typedef typename Acc<MIXED>::type Acc;
+  d[0] = d[1] = d[2] = d[3] = 0.0;
   st.valid = k < pi.cam_count;
   st.c = pi.cam_begin + (st.valid ? k : 0);
-  if (!st.valid) return 0.0;
+  if (!st.valid) return;
   const int c = st.c;
   const size_t i = 9 * (size_t)c + q;
   const real *Bc = reinterpret_cast<const real *>(MIXED ? (const void *)B.cam_Bf : (const void *)B.cam_B) + 45 * (size_t)c;
-  const real *pv = reinterpret_cast<const real *>(MIXED ? (const void *)B.pcg_pf : (const void *)B.pcg_p) + 9 * (size_t)c;
+  const real *uv = reinterpret_cast<const real *>(MIXED ? (const void *)B.pcg_pf : (const void *)B.pcg_z) + 9 * (size_t)c;
   const real *M = reinterpret_cast<const real *>(MIXED ? (const void *)B.cam_Minvf : (const void *)B.cam_Minv) +
                   81 * (size_t)c + 9 * q;
   const real *part = reinterpret_cast<const real *>(B.seg_partial) + q;
   const int s0 = B.cam_seg_begin[c], s1 = B.cam_seg_begin[c + 1];
-  st.p = B.pcg_p[i];
+  st.u = B.pcg_z[i];
   st.x = B.pcg_x[i];
   st.r = B.pcg_r[i];
   st.v = B.pcg_v[i];
+  st.p = first ? 0.0 : B.pcg_p[i];
+  st.s = first ? 0.0 : B.pcg_q[i];
   const real d2 = (real)B.cam_D2[i];
-  real brow[9], prow[9];
+  real brow[9], urow[9];
 #pragma unroll
   for (int kk = 0; kk < 9; ++kk) {
     brow[kk] = Bc[sym9(q, kk)];
-    prow[kk] = pv[kk];
+    urow[kk] = uv[kk];
     st.m[kk] = M[kk];
   }
   pdl_wait();  // the partials come from the mat-vec kernel
@@ -296,73 +310,56 @@ __device__ __forceinline__ double pcg_phase1(const DeviceBatch &B, const Problem
   constexpr int kAcc = MIXED ? 1 : 4;
   Acc a[kAcc];
 #pragma unroll
-  for (int u = 0; u < kAcc; ++u) a[u].init();
+  for (int uu = 0; uu < kAcc; ++uu) a[uu].init();
   for (int s = s0; s < s1; s += kBatch) {
     real pv2[kBatch];
 #pragma unroll
-    for (int u = 0; u < kBatch; ++u) pv2[u] = (s + u < s1) ? part[9 * (size_t)(s + u)] : (real)0;
+    for (int uu = 0; uu < kBatch; ++uu) pv2[uu] = (s + uu < s1) ? part[9 * (size_t)(s + uu)] : (real)0;
 #pragma unroll
-    for (int u = 0; u < kBatch; ++u)
-      if (s + u < s1) a[u % kAcc].add(pv2[u]);
+    for (int uu = 0; uu < kBatch; ++uu)
+      if (s + uu < s1) a[uu % kAcc].add(pv2[uu]);
   }
   double asum = a[0].value();
   if (kAcc == 4) asum = (a[0].value() + a[1 % kAcc].value()) + (a[2 % kAcc].value() + a[3 % kAcc].value());
-  real bp = 0;
+  real bu = 0;
 #pragma unroll
-  for (int kk = 0; kk < 9; ++kk) bp += brow[kk] * prow[kk];
-  st.q = (double)(bp + d2 * (real)st.p - (real)asum);
-  B.pcg_q[i] = st.q;
-  return st.p * st.q;
-}
-
-// Phase 1 for a coordinate whose state is not kept in registers: the same
-// arithmetic, with q stored for phase 2.
-template <bool MIXED>
-__device__ __forceinline__ void pcg_reload(const DeviceBatch &B, int q, CamCoord<typename Prec<MIXED>::real> &st) {
-  typedef typename Prec<MIXED>::real real;
-  if (!st.valid) return;
-  const size_t i = 9 * (size_t)st.c + q;
-  const real *M = reinterpret_cast<const real *>(MIXED ? (const void *)B.cam_Minvf : (const void *)B.cam_Minv) +
-                  81 * (size_t)st.c + 9 * q;
-  st.p = B.pcg_p[i];
-  st.q = B.pcg_q[i];
-  st.x = B.pcg_x[i];
-  st.r = B.pcg_r[i];
-  st.v = B.pcg_v[i];
-#pragma unroll
-  for (int kk = 0; kk < 9; ++kk) st.m[kk] = M[kk];
+  for (int kk = 0; kk < 9; ++kk) bu += brow[kk] * urow[kk];
+  st.w = (double)(bu + d2 * (real)st.u - (real)asum);
+  d[0] = st.r * st.u;
+  d[1] = st.u * st.w;
+  d[2] = st.r * st.r;
+  d[3] = st.x * (st.v + st.r);
 }
 
 // Phase 2 of one coordinate (all threads of the CTA call it together):
-// x += alpha p, r -= alpha q, z = M r; returns r.z, r.r, x.(v + r).
+// p, s, x, r and u = M r.
 template <bool MIXED>
-__device__ __forceinline__ void pcg_phase2(const DeviceBatch &B, int q, int lc, double alpha,
-                                           CamCoord<typename Prec<MIXED>::real> &st, typename Prec<MIXED>::real *sv,
-                                           bool sync_before, double *d3) {
+__device__ __forceinline__ void pcg_phase2(const DeviceBatch &B, int q, int lc, double alpha, double beta,
+                                           CamCoord<typename Prec<MIXED>::real> &st,
+                                           typename Prec<MIXED>::real *sv, bool sync_before) {
   typedef typename Prec<MIXED>::real real;
+  double r = 0.0;
   if (st.valid) {
+    st.p = st.u + beta * st.p;
+    st.s = st.w + beta * st.s;
     st.x = st.x + alpha * st.p;
-    st.r = st.r - alpha * st.q;
-  } else {
-    st.x = st.r = 0.0;
+    r = st.r - alpha * st.s;
   }
   if (sync_before) __syncthreads();  // the previous pass has finished reading sv
-  sv[threadIdx.x] = (real)st.r;
+  sv[threadIdx.x] = (real)r;
   __syncthreads();
-  d3[0] = d3[1] = d3[2] = 0.0;
   if (st.valid) {
     const real *rv = sv + 9 * lc;
-    real z = 0;
+    real u = 0;
 #pragma unroll
-    for (int kk = 0; kk < 9; ++kk) z += st.m[kk] * rv[kk];
-    st.z = (double)z;
+    for (int kk = 0; kk < 9; ++kk) u += st.m[kk] * rv[kk];
     const size_t i = 9 * (size_t)st.c + q;
+    B.pcg_p[i] = st.p;
+    B.pcg_q[i] = st.s;
     B.pcg_x[i] = st.x;
-    B.pcg_r[i] = st.r;
-    B.pcg_z[i] = st.z;
-    d3[0] = st.r * st.z;
-    d3[1] = st.r * st.r;
-    d3[2] = st.x * (st.v + st.r);
+    B.pcg_r[i] = r;
+    B.pcg_z[i] = (double)u;
+    if (MIXED) B.pcg_pf[i] = (float)u;
   }
 }
 
@@ -371,12 +368,12 @@ __device__ __forceinline__ void pcg_phase2(const DeviceBatch &B, int q, int lc, 
 template <bool MIXED>
 __global__ void __launch_bounds__(kPcgThreads) k_pcg_camera(DeviceBatch B) {
   typedef typename Prec<MIXED>::real real;
-  constexpr int kRegPasses = MIXED ? 4 : 2;
-  // slots: [nblk_max] p.q, then [nblk_max][3] r.z, r.r, x.(v + r)
+  constexpr int kRegPasses = MIXED ? 2 : 1;
+  // slots: [nblk_max][kPcgNv]
   extern __shared__ double blk[];
-  __shared__ real sv[kPcgThreads];  // the block's r, staged for z = M r
-  __shared__ double red[3][kPcgThreads];
-  __shared__ double tot[4];
+  __shared__ real sv[kPcgThreads];  // the block's r, staged for u = M r
+  __shared__ double red[kPcgNv][kPcgThreads];
+  __shared__ double tot[kPcgNv];
   __shared__ int flag;
   cg::cluster_group cl = cg::this_cluster();
   const int cs = (int)cl.num_blocks();
@@ -384,122 +381,104 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg_camera(DeviceBatch B) {
   const int prob = blockIdx.x / cs;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int lc = tid / 9, q = tid - 9 * lc;  // camera in the block, coordinate
-  const int nslots = B.pcg_passes * cs;
-  double *blk1 = blk;
-  double *blk3 = blk + nslots;
   LMState *L = B.lm + prob;
   if (prob < B.num_problems && pcg_live(L)) {  // uniform over the cluster
     const ProblemInfo pi = B.prob[prob];
     const int nblk = (pi.cam_count + kPcgBlockCams - 1) / kPcgBlockCams;
-    // every LMState field this kernel reads is read before the first cluster
-    // barrier: rank 0 overwrites them after the second one
-    const double rz_old = L->rz, q0 = L->q0, r0_norm = L->r0_norm;
-    const int its = L->pcg_iterations;
+    // every LMState field this kernel reads is read before the cluster
+    // barrier: rank 0 overwrites them after it
+    const double gamma_old = L->rz, alpha_old = L->alpha, q_old = L->q0, r0_norm = L->r0_norm;
+    const int k = L->pcg_iterations;  // completed iterations = this call's index
     CamCoord<real> st[kRegPasses];
-    // ---- phase 1: q = (B + Dc^2) p - sum of partials, and p.q --------------
-    auto push1 = [&](int b, double pq) { block_push<1>(cl, red, &pq, blk1, b, cs); };
+    // ---- w = S u and the four dot products ---------------------------------
 #pragma unroll
     for (int j = 0; j < kRegPasses; ++j) {
       const int b = rank + j * cs;
-      if (b < nblk) push1(b, pcg_phase1<MIXED>(B, pi, b * kPcgBlockCams + lc, q, st[j]));
+      if (b < nblk) {
+        double d[kPcgNv];
+        pcg_phase1<MIXED>(B, pi, b * kPcgBlockCams + lc, q, k == 0, st[j], d);
+        block_push<kPcgNv>(cl, red, d, blk, b, cs);
+      }
     }
     for (int b = rank + kRegPasses * cs; b < nblk; b += cs) {
       CamCoord<real> t;
-      push1(b, pcg_phase1<MIXED>(B, pi, b * kPcgBlockCams + lc, q, t));
+      double d[kPcgNv];
+      pcg_phase1<MIXED>(B, pi, b * kPcgBlockCams + lc, q, k == 0, t, d);
+      block_push<kPcgNv>(cl, red, d, blk, b, cs);
+      if (t.valid) B.pcg_w[9 * (size_t)t.c + q] = t.w;  // w of passes not held in registers
     }
     pdl_wait();  // every thread, whether or not it had a camera coordinate
     pdl_launch_dependents();
     cluster_arrive();
-    cluster_wait();
+    cluster_wait();  // after this barrier no CTA touches another's shared memory
     if (warp == 0) {
-      double t[1];
-      slots_sum<1>(blk1, nblk, t);
-      if (lane == 0) tot[0] = t[0];
+      double t[kPcgNv];
+      slots_sum<kPcgNv>(blk, nblk, t);
+      if (lane == 0) {
+#pragma unroll
+        for (int v = 0; v < kPcgNv; ++v) tot[v] = t[v];
+      }
     }
     __syncthreads();
-    const double pqs = tot[0];
-    const bool good = pqs > 0.0 && isfinite(pqs);
-    const double alpha = good ? rz_old / pqs : 0.0;
-    // ---- phase 2: x += alpha p, r -= alpha q, z = M r, three dot products --
-    auto push3 = [&](int b, double *d3) { block_push<3>(cl, red, d3, blk3, b, cs); };
-    if (good) {
+    const double gamma = tot[0], delta = tot[1], rr = tot[2], qx = tot[3];
+    // ---- stopping test on (x_k, r_k), then alpha_k, beta_k -----------------
+    const DeviceOptions &o = B.opt;
+    const double qk = -qx;  // Q(x_k) = x'Sx - 2 v'x = -x.(v + r)
+    bool stop = false;
+    if (k >= 1) {
+      if (o.pcg_criterion == GBA_PCG_QUADRATIC_MODEL) {
+        const double zeta = k * (qk - q_old) / qk;
+        if (zeta < o.eta && k >= o.min_pcg_iterations) stop = true;
+      } else {
+        if (sqrt(rr) <= o.pcg_tolerance * r0_norm && k >= o.min_pcg_iterations) stop = true;
+      }
+    }
+    if (k >= o.max_pcg_iterations) stop = true;
+    const double beta = k == 0 ? 0.0 : gamma / gamma_old;
+    const double denom = k == 0 ? delta : delta - beta * gamma / alpha_old;
+    const bool good = denom > 0.0 && isfinite(denom) && isfinite(gamma) && gamma != 0.0;
+    if (!good) stop = true;
+    const double alpha = good ? gamma / denom : 0.0;
+    if (!stop) {
 #pragma unroll
       for (int j = 0; j < kRegPasses; ++j) {
         const int b = rank + j * cs;
-        if (b < nblk) {
-          double d3[3];
-          pcg_phase2<MIXED>(B, q, lc, alpha, st[j], sv, j > 0, d3);
-          push3(b, d3);
-        }
+        if (b < nblk) pcg_phase2<MIXED>(B, q, lc, alpha, beta, st[j], sv, j > 0);
       }
       for (int b = rank + kRegPasses * cs; b < nblk; b += cs) {
         CamCoord<real> t;
-        t.valid = b * kPcgBlockCams + lc < pi.cam_count;
-        t.c = pi.cam_begin + (t.valid ? b * kPcgBlockCams + lc : 0);
-        pcg_reload<MIXED>(B, q, t);
-        double d3[3];
-        pcg_phase2<MIXED>(B, q, lc, alpha, t, sv, true, d3);
-        push3(b, d3);
-      }
-    }
-    cluster_arrive();
-    cluster_wait();  // after this barrier no CTA touches another's shared memory
-    if (warp == 0) {
-      double t[3] = {0.0, 0.0, 0.0};
-      if (good) slots_sum<3>(blk3, nblk, t);
-      if (lane == 0) tot[1] = t[0], tot[2] = t[1], tot[3] = t[2];
-    }
-    __syncthreads();
-    const double rzn = tot[1], rrn = tot[2], qxn = tot[3];
-    // ---- stopping test and the next direction (identical in every CTA) ------
-    const DeviceOptions &o = B.opt;
-    const int it = its + (good ? 1 : 0);
-    bool stop = !good;
-    double q1 = q0;
-    if (good) {
-      if (o.pcg_criterion == GBA_PCG_QUADRATIC_MODEL) {
-        // Q(x) = x'Sx - 2 v'x = -x'(v + r);  stop when i (Q_i - Q_{i-1}) / Q_i < eta
-        q1 = -qxn;
-        const double zeta = it * (q1 - q0) / q1;
-        if (zeta < o.eta && it >= o.min_pcg_iterations) stop = true;
-      } else {
-        if (sqrt(rrn) <= o.pcg_tolerance * r0_norm && it >= o.min_pcg_iterations) stop = true;
-      }
-      if (it >= o.max_pcg_iterations) stop = true;
-      if (!isfinite(rzn) || !(rz_old != 0.0)) stop = true;
-    }
-    const double beta = stop ? 0.0 : rzn / rz_old;
-    if (!stop) {
-      auto next_dir = [&](size_t i, double z, double p) {
-        const double pn = z + beta * p;
-        B.pcg_p[i] = pn;
-        if (MIXED) B.pcg_pf[i] = (float)pn;
-      };
+        const int kk = b * kPcgBlockCams + lc;
+        t.valid = kk < pi.cam_count;
+        t.c = pi.cam_begin + (t.valid ? kk : 0);
+        if (t.valid) {
+          const size_t i = 9 * (size_t)t.c + q;
+          const real *M = reinterpret_cast<const real *>(MIXED ? (const void *)B.cam_Minvf
+                                                               : (const void *)B.cam_Minv) +
+                          81 * (size_t)t.c + 9 * q;
+          t.u = B.pcg_z[i];
+          t.x = B.pcg_x[i];
+          t.r = B.pcg_r[i];
+          t.w = B.pcg_w[i];  // stored in phase 1
+          t.p = k == 0 ? 0.0 : B.pcg_p[i];
+          t.s = k == 0 ? 0.0 : B.pcg_q[i];
 #pragma unroll
-      for (int j = 0; j < kRegPasses; ++j) {
-        const int b = rank + j * cs;
-        if (b < nblk && st[j].valid) next_dir(9 * (size_t)st[j].c + q, st[j].z, st[j].p);
-      }
-      for (int b = rank + kRegPasses * cs; b < nblk; b += cs) {
-        const int k = b * kPcgBlockCams + lc;
-        if (k < pi.cam_count) {
-          const size_t i = 9 * (size_t)(pi.cam_begin + k) + q;
-          next_dir(i, B.pcg_z[i], B.pcg_p[i]);
+          for (int m = 0; m < 9; ++m) t.m[m] = M[m];
         }
+        pcg_phase2<MIXED>(B, q, lc, alpha, beta, t, sv, true);
       }
     }
     if (rank == 0 && tid == 0) {
-      L->pq = pqs;
-      L->alpha = alpha;
-      if (good) {
-        L->pcg_iterations = it;
-        L->rr = rrn;
-        L->rz = rzn;
-        L->q0 = q1;
+      if (!stop) {
+        L->pcg_iterations = k + 1;
+        L->rz = gamma;
+        L->alpha = alpha;
         L->beta = beta;
-      } else if (its == 0) {
+        L->q0 = qk;
+      } else if (k == 0 && !good) {
         L->linear_ok = 0;  // S not positive definite along the first direction
       }
+      L->pq = delta;
+      L->rr = rr;
       if (stop) L->pcg_active = 0;
       if (B.num_problems == 1) {
         // the only problem decides the loop: no cross-cluster count needed
@@ -570,9 +549,9 @@ void launch_pcg_iteration(const DeviceBatch &b, bool mixed, cudaStream_t s) {
 }
 
 // Slots of every camera block of the largest problem (passes x cluster size),
-// four doubles per block.
+// kPcgNv doubles per block.
 size_t pcg_camera_smem(int passes, int cluster) {
-  return sizeof(double) * 4 * (size_t)(passes > 0 ? passes : 1) * (size_t)(cluster > 0 ? cluster : 1);
+  return sizeof(double) * kPcgNv * (size_t)(passes > 0 ? passes : 1) * (size_t)(cluster > 0 ? cluster : 1);
 }
 
 // Largest cluster the camera kernel may use on this device (16 when the
