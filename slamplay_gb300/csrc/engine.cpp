@@ -114,8 +114,8 @@ gba_status Engine::init(std::string *err) {
   if ((st = check(cudaDeviceGetAttribute(&sm_count_, cudaDevAttrMultiProcessorCount, device_), "SM count", err)) !=
       GBA_OK)
     return st;
-  max_cluster_ = pcg_max_cluster();
   point_schur_init();
+  pcg_init();
   return GBA_OK;
 }
 
@@ -131,17 +131,6 @@ void Engine::set_tuning(int chunk_observations, int pcg_unroll) {
   o_.pcg_unroll = pcg_unroll;
   destroy_graph();
   cur_key_.clear();
-}
-
-// Cluster shape of the camera-side PCG kernel: one CTA per camera block
-// (kPcgBlockCams cameras) of the largest problem, capped by the device's
-// cluster limit; the remaining blocks are taken in passes.
-void Engine::pcg_cluster(const HostBatch &hb, int *cluster, int *passes) const {
-  int maxc = 1;
-  for (const ProblemInfo &pi : hb.prob) maxc = std::max(maxc, pi.cam_count);
-  const int blocks = (maxc + kPcgBlockCams - 1) / kPcgBlockCams;
-  *cluster = std::min(max_cluster_, blocks);
-  *passes = (blocks + *cluster - 1) / *cluster;
 }
 
 // Arena order: [upload | download | work].  The pinned host staging buffer
@@ -228,19 +217,18 @@ size_t Engine::layout(const HostBatch &hb, char *base, DeviceBatch *db, size_t *
   b.pcg_r = cv.take<double>(9 * nc);
   b.pcg_z = cv.take<double>(9 * nc);
   b.pcg_p = cv.take<double>(9 * nc);
-  b.pcg_q = cv.take<double>(9 * nc);
   b.pcg_v = cv.take<double>(9 * nc);
-  b.pcg_w = cv.take<double>(9 * nc);
-  b.pcg_pf = cv.take<float>(9 * nc);
   b.cam_colnorm = cv.take<double>(9 * nc);
   b.seg_partial = cv.take<double>(9 * ns);
   b.schur_partial = cv.take<char>(54 * ns * rs);
-  pcg_cluster(hb, &b.pcg_cluster, &b.pcg_passes);
+  b.seg_grad = cv.take<double>(mixed_ ? 9 * ns : 0);
   b.chunk_scal = cv.take<double>(kChunkScal * nch);
   b.cam_scal = cv.take<double>(kCamScal * nc);
-  b.cam_pcg = cv.take<double>(kPcgScal * nc);
+  b.chunk_red = cv.take<double>(2 * nch);
+  b.blk_red = cv.take<double>(3 * nb);
   b.prob_counter = cv.take<uint32_t>(4 * P);
   b.global_counter = cv.take<uint32_t>(8);
+  b.chunk_counter = cv.take<uint32_t>(nch);
   b.opt.function_tolerance = o_.function_tolerance;
   b.opt.gradient_tolerance = o_.gradient_tolerance;
   b.opt.parameter_tolerance = o_.parameter_tolerance;
@@ -306,11 +294,6 @@ gba_status Engine::upload(const HostBatch &hb, std::string *err) {
   DeviceBatch probe{};
   size_t ub, doff, dbytes;
   const size_t total = layout(hb, nullptr, &probe, &ub, &doff, &dbytes);
-  if (pcg_camera_smem(probe.pcg_passes, probe.pcg_cluster) > kPcgSmemMax) {
-    *err = "a problem has more cameras than the camera-side PCG kernel supports (" +
-           std::to_string(kPcgSmemMax / pcg_camera_smem(1, 1) * kPcgBlockCams) + ")";
-    return GBA_ERR_INVALID_ARGUMENT;
-  }
   if ((st = ensure_capacity(total, doff + dbytes, err)) != GBA_OK) return st;
   upload_bytes_ = ub;
   download_off_ = doff;
@@ -395,9 +378,12 @@ static double bytes_pcg_camera(const DeviceBatch &b) {
 }
 static double bytes_eval(const DeviceBatch &b) {
   const double rs = b.opt.mixed ? 4.0 : 8.0;
-  // K1: uv, cam, pt in; 13 pairs out; points in/out; K1c: list, 10 pairs in
+  // K1: uv, cam, pt in; 13 pairs out; points in/out; K1c: list, 10 pairs in.
+  // Mixed form: K1 also reads the slot per observation and writes 9 FP64
+  // gradient partials per segment, which K1c reads instead of r.
+  const double seg = b.opt.mixed ? (double)b.nseg * (2.0 + 4.0 + 2.0 * 72.0) + (double)b.no * (2.0 - 2.0 * rs) : 0.0;
   return (double)b.no * (24.0 + 26.0 * rs) + (double)b.np * (32.0 + 72.0 + 4.0 + 24.0) +
-         (double)b.nc * (kCamTable * 8.0) + (double)b.no * (4.0 + 20.0 * rs) + (double)b.nc * (54.0 * 8.0);
+         (double)b.nc * (kCamTable * 8.0) + (double)b.no * (4.0 + 20.0 * rs) + (double)b.nc * (54.0 * 8.0) + seg;
 }
 static double bytes_point_schur(const DeviceBatch &b) {
   // J_c, J_p, slot and point index per observation; C, g in and C^-1 (both
@@ -419,9 +405,16 @@ static double bytes_cost(const DeviceBatch &b) {
   return (double)b.no * 24.0 + (double)b.np * 32.0 + (double)b.nc * 15.0 * 8.0;
 }
 
-void Engine::enqueue_setup(cudaStream_t s) {
+// Every completion counter starts at zero (the last CTA at a counter resets
+// it, so they stay zero between kernels).
+void Engine::zero_counters(cudaStream_t s) {
   cudaMemsetAsync(db_.prob_counter, 0, 4 * sizeof(uint32_t) * (size_t)db_.num_problems, s);
   cudaMemsetAsync(db_.global_counter, 0, 8 * sizeof(uint32_t), s);
+  if (db_.nchunks > 0) cudaMemsetAsync(db_.chunk_counter, 0, sizeof(uint32_t) * (size_t)db_.nchunks, s);
+}
+
+void Engine::enqueue_setup(cudaStream_t s) {
+  zero_counters(s);
   cudaMemsetAsync(db_.status, 0, 8 * sizeof(int32_t), s);
   launch_sync_param_buffers(db_, s);
   launch_init_state(db_, s);
@@ -568,8 +561,7 @@ gba_status Engine::run_host_driven(std::string *err) {
     return check(cudaStreamSynchronize(stream_), "solver kernels", err);
   };
   prof_begin(stream_);
-  cudaMemsetAsync(db_.prob_counter, 0, 4 * sizeof(uint32_t) * (size_t)db_.num_problems, stream_);
-  cudaMemsetAsync(db_.global_counter, 0, 8 * sizeof(uint32_t), stream_);
+  zero_counters(stream_);
   cudaMemsetAsync(db_.status, 0, 8 * sizeof(int32_t), stream_);
   launch_sync_param_buffers(db_, stream_);
   launch_init_state(db_, stream_);
@@ -728,8 +720,7 @@ gba_status Engine::evaluate(const gba_problem_view *v, double *residuals, double
   const int loss = db_.opt.loss;
   db_.opt.loss = GBA_LOSS_TRIVIAL;
   db_.use_cond = 0;
-  cudaMemsetAsync(db_.prob_counter, 0, 4 * sizeof(uint32_t) * (size_t)db_.num_problems, stream_);
-  cudaMemsetAsync(db_.global_counter, 0, 8 * sizeof(uint32_t), stream_);
+  zero_counters(stream_);
   cudaMemsetAsync(db_.status, 0, 8 * sizeof(int32_t), stream_);
   launch_sync_param_buffers(db_, stream_);
   launch_init_state(db_, stream_);
@@ -786,8 +777,7 @@ gba_status Engine::compute_step(const gba_problem_view *v, double radius, double
     if (s2 != GBA_OK) return s2;
     return check(cudaStreamSynchronize(stream_), "kernels", err);
   };
-  cudaMemsetAsync(db_.prob_counter, 0, 4 * sizeof(uint32_t) * (size_t)db_.num_problems, stream_);
-  cudaMemsetAsync(db_.global_counter, 0, 8 * sizeof(uint32_t), stream_);
+  zero_counters(stream_);
   cudaMemsetAsync(db_.status, 0, 8 * sizeof(int32_t), stream_);
   launch_sync_param_buffers(db_, stream_);
   launch_init_state(db_, stream_);

@@ -49,7 +49,6 @@ class Engine {
   gba_status download(const HostBatch &hb, const gba_problem_view *v, gba_summary *s, std::string *err);
 
  private:
-  void pcg_cluster(const HostBatch &hb, int *cluster, int *passes) const;
   gba_status ensure_capacity(size_t dev_bytes, size_t host_bytes, std::string *err);
   size_t layout(const HostBatch &hb, char *dbase, DeviceBatch *db, size_t *upload_bytes,
                 size_t *download_off, size_t *download_bytes);
@@ -60,6 +59,7 @@ class Engine {
   gba_status run_host_driven(std::string *err);
   gba_status check(cudaError_t e, const char *what, std::string *err);
   void enqueue_setup(cudaStream_t s);
+  void zero_counters(cudaStream_t s);
   void enqueue_lm_head(cudaStream_t s);
   void enqueue_lm_tail(cudaStream_t s);
   // profiling helpers (host-driven mode)
@@ -91,7 +91,6 @@ class Engine {
   double last_setup_ms_ = 0.0, last_solve_ms_ = 0.0;
   int trace_cap_ = 0;
   int sm_count_ = 0;
-  int max_cluster_ = 8;    // largest cluster the camera-side PCG kernel may use
   bool pdl_ = true;        // programmatic dependent launches inside the PCG body
 };
 

@@ -80,7 +80,7 @@ struct LMState {
 // (solver.cpp) and passed by value to every launch.
 struct DeviceBatch {
   int32_t num_problems, nc, np, no, nchunks, nseg;
-  int32_t cam_blocks;        // camera blocks of the PCG kernels (kCamPerBlock cameras each)
+  int32_t cam_blocks;        // camera blocks of the PCG camera kernel (kPcgBlockCams cameras each)
   const ProblemInfo *prob;
   const ChunkInfo *chunk;
   // observations, internal (point-major) order
@@ -125,18 +125,16 @@ struct DeviceBatch {
   float *cam_Minvf;          // 81, FP32 copy (mixed form)
   float *cam_Bf;             // 45, FP32 copy of cam_B (mixed form)
   double *cam_D2;            // 9: squared LM diagonal of the camera parameters
-  // PCG vectors, 9 * nc each: x, r, z (= u = M r), p, q (= s = S p), v (rhs),
-  // w (= S u, kept for camera blocks beyond the register-held passes)
-  double *pcg_x, *pcg_r, *pcg_z, *pcg_p, *pcg_q, *pcg_v, *pcg_w;
-  float *pcg_pf;             // 9 * nc, FP32 copy of the direction (mixed form)
+  // PCG vectors, 9 * nc each: x, r, z (= M r), p (direction), v (rhs)
+  double *pcg_x, *pcg_r, *pcg_z, *pcg_p, *pcg_v;
   double *cam_colnorm;       // 9 * nc: column norms of the first evaluation
   double *pt_colnorm;        // 3 * np
   void *seg_partial;         // 9 * nseg, double (FP64) or float (mixed)
   void *schur_partial;       // 54 * nseg: per segment 45 packed Schur-block and 9 rhs partials
+  double *seg_grad;          // 9 * nseg: per segment FP64 J_c^T r (mixed form: the camera gradient)
   // per chunk / per camera / per camera-block scalars (deterministic partials)
   double *chunk_scal;        // kChunkScal per chunk
   double *cam_scal;          // kCamScal per camera
-  double *cam_pcg;           // kPcgScal per camera: PCG dot-product partials
   const int4 *camblk;        // camera blocks: (problem, first camera, count, 0)
   LMState *lm;
   DeviceOptions opt;
@@ -151,8 +149,12 @@ struct DeviceBatch {
   // graph conditional handles (0 when the host drives the loops)
   unsigned long long lm_cond, pcg_cond;
   int32_t use_cond;
-  int32_t pcg_cluster;       // CTAs per cluster of the camera-side PCG kernel
-  int32_t pcg_passes;        // camera blocks per CTA of that kernel (largest problem)
+  // PCG reductions: per chunk its share of p.q, then per group of kRedGroup
+  // chunks ([nchunks + first chunk of the group]); per camera block its
+  // r.z, r.r, x.(v + r)
+  double *chunk_red;         // 2 * nchunks
+  uint32_t *chunk_counter;   // nchunks (one per group, at its first chunk)
+  double *blk_red;           // 3 * cam_blocks
 };
 
 constexpr int kCamTable = 44;    // R(9) dR(27) t(3) f k1 k2 + pad
@@ -161,22 +163,19 @@ constexpr int kChunkScal = 6;
 constexpr int kCS_COST = 0, kCS_GMAX = 1, kCS_XN2 = 2, kCS_MODEL = 3, kCS_STEP2 = 4, kCS_BAD = 5;
 // cam_scal slots
 constexpr int kCamScal = 6;
-constexpr int kCC_GMAX = 0, kCC_XN2 = 1, kCC_STEP2 = 2, kCC_RZ = 3, kCC_RR = 4;
-// cam_pcg slots (PCG partials of one camera)
-constexpr int kPcgScal = 4;
-constexpr int kPS_PQ = 0, kPS_RZ = 1, kPS_RR = 2, kPS_QX = 3;
-// cameras per CTA in the warp-per-camera camera kernels
-constexpr int kCamPerBlock = 8;
+constexpr int kCC_GMAX = 0, kCC_XN2 = 1, kCC_STEP2 = 2, kCC_RZ = 3, kCC_RR = 4, kCC_YG = 5;
 // PCG iterations per body of the graph's PCG loop
 constexpr int kPcgUnroll = 2;
-// cameras per block of the camera-side PCG kernel (one thread per coordinate)
-constexpr int kPcgBlockCams = 16;
-// dynamic shared memory the camera-side PCG kernel may use (4 doubles per
-// camera block of the largest problem: 204,800 cameras)
-constexpr size_t kPcgSmemMax = 200 * 1024;
+// cameras per block of the camera-side PCG kernel
+constexpr int kPcgBlockCams = 8;
+// p.q of the PCG: problems of up to kRedDirect chunks have their chunk
+// values summed by the camera kernel directly, larger ones in groups of
+// kRedGroup chunks first
+constexpr int kRedDirect = 2048;
+constexpr int kRedGroup = 64;
 // prob_counter slots (4 per problem) and global_counter slots
 constexpr int kPC_SCHUR = 0, kPC_REDUCE = 1, kPC_UPDATE = 2;
-constexpr int kGC_SCHUR = 0, kGC_UPDATE = 1, kGC_POST = 2, kGC_LMBODIES = 3, kGC_BAR_COUNT = 4, kGC_BAR_GEN = 5;
+constexpr int kGC_SCHUR = 0, kGC_UPDATE = 1, kGC_POST = 2, kGC_LMBODIES = 3;
 // status words: [0] error, [1] any LM active, [2] any PCG active, [3] PCG-active problem count
 
 }  // namespace gba

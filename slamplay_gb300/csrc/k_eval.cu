@@ -8,7 +8,9 @@
 //                       blocks J_p^T J_p and J_p^T r reduced per point in
 //                       shared memory (points own contiguous observations).
 //  K1c k_eval_camera    per camera (CTA): J_c^T J_c (45) and J_c^T r over the
-//                       camera's observations, fixed-order CTA reduction.
+//                       camera's observations, fixed-order CTA reduction (the
+//                       mixed form's J_c^T r: a sum of K1's FP64 segment
+//                       partials).
 //  K7  k_post_eval      per problem: cost, gradient max-norm, |x|, Ceres'
 //                       termination tests, LM-loop condition.
 //  K5b k_candidate      per camera: candidate camera + its table (R only).
@@ -160,12 +162,24 @@ __device__ __forceinline__ double eval_observation(const DeviceBatch &B, int64_t
 
 // ---------------------------------------------------------------------------
 // K1
+// The mixed form's gradient (G64): the Jacobian is computed in FP64 and only
+// stored in FP32.  The gradient J^T r is a sum of large terms that cancel
+// towards zero as the solve converges, so it is formed from the FP64
+// Jacobian in FP64: per point (g_p) here, and per camera as one FP64 partial
+// per (chunk, camera segment) in seg_grad, summed per camera by K1c.  The
+// LM fixed point (g = 0) is then the FP64 one; the FP32 copies only feed the
+// Schur products and the PCG, i.e. the accuracy of each step, not where the
+// steps lead.
 template <bool MIXED, bool NORMS>
 __global__ void __launch_bounds__(kChunkCap) k_eval_chunk(DeviceBatch B) {
   typedef typename Prec<MIXED>::real real;
   typedef typename Prec<MIXED>::real2 real2;
   typedef typename Acc<MIXED>::type Acc;
+  constexpr bool G64 = MIXED && !NORMS;
   __shared__ real sm[kChunkCap][9];
+  // G64: per observation its FP64 J_c^T r (9, at its camera-sorted slot) and
+  // J_p^T r (3, at its position)
+  __shared__ double gsm[G64 ? kChunkCap : 1][12];
   __shared__ double red[kChunkCap / 32];
   const int t = threadIdx.x;
   for (int ch = blockIdx.x; ch < B.nchunks; ch += gridDim.x) {
@@ -181,7 +195,26 @@ __global__ void __launch_bounds__(kChunkCap) k_eval_chunk(DeviceBatch B) {
       const double *Xp = B.pt_param[parity] + 4 * (size_t)j;
       const double X[3] = {Xp[0], Xp[1], Xp[2]};
       real2 Jc[9], Jp[3], r;
-      cost = eval_observation<MIXED>(B, o, c, j, X, NORMS, Jc, Jp, r, bad);
+      if (G64) {
+        double2 Jc64[9], Jp64[3], r64;
+        cost = eval_observation<false>(B, o, c, j, X, false, Jc64, Jp64, r64, bad);
+        const int slot = B.obs_slot[o];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+          Jc[k] = mk2((real)Jc64[k].x, (real)Jc64[k].y);
+          gsm[slot][k] = Jc64[k].x * r64.x + Jc64[k].y * r64.y;
+          bad = bad || !isfinite((float)Jc[k].x) || !isfinite((float)Jc[k].y);
+        }
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          Jp[k] = mk2((real)Jp64[k].x, (real)Jp64[k].y);
+          gsm[t][9 + k] = Jp64[k].x * r64.x + Jp64[k].y * r64.y;
+          bad = bad || !isfinite((float)Jp[k].x) || !isfinite((float)Jp[k].y);
+        }
+        r = mk2((real)r64.x, (real)r64.y);
+      } else {
+        cost = eval_observation<MIXED>(B, o, c, j, X, NORMS, Jc, Jp, r, bad);
+      }
 #pragma unroll
       for (int k = 0; k < 9; ++k) jstore(B.jac, B.no, k, o, Jc[k]);
 #pragma unroll
@@ -195,7 +228,29 @@ __global__ void __launch_bounds__(kChunkCap) k_eval_chunk(DeviceBatch B) {
         sm[t][6 + a] = Jp[a].x * r.x + Jp[a].y * r.y;
       }
     }
+    // G64: the first (segment, coordinate) camera-gradient sum of this thread
+    int f_b0 = 0, f_b1 = 0, f_slot = 0;
+    if (G64 && t < ci.seg_count * 9) {
+      const int sg = t / 9;
+      f_b0 = B.seg_pos[ci.seg_begin + sg];
+      f_b1 = (sg + 1 < ci.seg_count) ? B.seg_pos[ci.seg_begin + sg + 1] : ci.obs_count;
+      f_slot = B.seg_slot[ci.seg_begin + sg];
+    }
     __syncthreads();
+    if (G64) {
+      for (int i = t; i < ci.seg_count * 9; i += blockDim.x) {
+        const int sg = i / 9, q = i - 9 * sg;
+        int b0 = f_b0, b1 = f_b1, slot9 = f_slot;
+        if (i != t) {
+          b0 = B.seg_pos[ci.seg_begin + sg];
+          b1 = (sg + 1 < ci.seg_count) ? B.seg_pos[ci.seg_begin + sg + 1] : ci.obs_count;
+          slot9 = B.seg_slot[ci.seg_begin + sg];
+        }
+        double a = 0.0;
+        for (int k = b0; k < b1; ++k) a += gsm[k][q];
+        B.seg_grad[9 * (size_t)slot9 + q] = a;
+      }
+    }
     double gmax = 0.0, xn2 = 0.0;
     if (t < ci.pt_count) {
       const int jj = ci.pt_begin + t;
@@ -203,9 +258,14 @@ __global__ void __launch_bounds__(kChunkCap) k_eval_chunk(DeviceBatch B) {
       Acc acc[9];
 #pragma unroll
       for (int q = 0; q < 9; ++q) acc[q].init();
+      double g64[3] = {0.0, 0.0, 0.0};
       for (int k = b0; k < b1; ++k) {
 #pragma unroll
-        for (int q = 0; q < 9; ++q) acc[q].add(sm[k][q]);
+        for (int q = 0; q < (G64 ? 6 : 9); ++q) acc[q].add(sm[k][q]);
+        if (G64) {
+#pragma unroll
+          for (int q = 0; q < 3; ++q) g64[q] += gsm[k][9 + q];
+        }
       }
       if (NORMS) {
         B.pt_colnorm[3 * (size_t)jj + 0] = acc[0].value();
@@ -218,7 +278,7 @@ __global__ void __launch_bounds__(kChunkCap) k_eval_chunk(DeviceBatch B) {
           const double *x = B.pt_param[parity] + 4 * (size_t)jj;
 #pragma unroll
           for (int q = 0; q < 3; ++q) {
-            const double gq = acc[6 + q].value();
+            const double gq = G64 ? g64[q] : acc[6 + q].value();
             B.pt_g[3 * (size_t)jj + q] = gq;
             const double gu = gq / B.pt_scale[3 * (size_t)jj + q];
             gmax = fmax(gmax, fabs(x[q] - (x[q] - gu)));
@@ -275,12 +335,15 @@ __global__ void __launch_bounds__(kCamThreads) k_eval_camera(DeviceBatch B) {
 #pragma unroll
       for (int q = 0; q < 9; ++q) acc[q].add(J[q].x * J[q].x + J[q].y * J[q].y);
     } else {
-      const real2 r = jload<real2>(B.jac, B.no, 12, o);
+      // mixed form: J_c^T r comes in FP64 from the chunk kernel's segment
+      // partials (below), not from the FP32 copies
+      real2 r = mk2((real)0, (real)0);
+      if (!MIXED) r = jload<real2>(B.jac, B.no, 12, o);
 #pragma unroll
       for (int a = 0; a < 9; ++a) {
 #pragma unroll
         for (int b = a; b < 9; ++b) acc[sym9(a, b)].add(J[a].x * J[b].x + J[a].y * J[b].y);
-        acc[45 + a].add(J[a].x * r.x + J[a].y * r.y);
+        if (!MIXED) acc[45 + a].add(J[a].x * r.x + J[a].y * r.y);
       }
     }
   }
@@ -292,7 +355,23 @@ __global__ void __launch_bounds__(kCamThreads) k_eval_camera(DeviceBatch B) {
   __syncthreads();
   if (t < NV) {
     double s = 0.0;
-    for (int w = 0; w < kCamThreads / 32; ++w) s += part[w][t];
+    if (MIXED && !NORMS && t >= 45) {
+      // the camera's FP64 gradient: its segment partials in camera-major order
+      // (four interleaved accumulators, combined pairwise: a fixed order)
+      const double *gp = B.seg_grad + (t - 45);
+      const int s0 = B.cam_seg_begin[c], s1 = B.cam_seg_begin[c + 1];
+      double a4[4] = {0.0, 0.0, 0.0, 0.0};
+      for (int sg = s0; sg < s1; sg += 16) {
+        double v[16];
+#pragma unroll
+        for (int u = 0; u < 16; ++u) v[u] = (sg + u < s1) ? gp[9 * (size_t)(sg + u)] : 0.0;
+#pragma unroll
+        for (int u = 0; u < 16; ++u) a4[u % 4] += v[u];
+      }
+      s = (a4[0] + a4[1]) + (a4[2] + a4[3]);
+    } else {
+      for (int w = 0; w < kCamThreads / 32; ++w) s += part[w][t];
+    }
     part[0][t] = s;  // each t reads its own column only before writing it
   }
   __syncthreads();
@@ -461,6 +540,10 @@ __global__ void k_candidate_cameras(DeviceBatch B) {
     xc[q] = cand[q];
   }
   B.cam_scal[(size_t)kCamScal * c + kCC_STEP2] = used ? s2 : 0.0;
+  // the camera part of step.g (the mixed form's model cost change)
+  double yg = 0.0;
+  for (int q = 0; q < 9; ++q) yg += B.pcg_x[9 * (size_t)c + q] * B.cam_g[9 * (size_t)c + q];
+  B.cam_scal[(size_t)kCamScal * c + kCC_YG] = used ? -yg : 0.0;
   camera_table_entry(cand, B.cam_table + (size_t)kCamTable * c, false);
 }
 

@@ -2,44 +2,50 @@
 // reduced camera system  S x = v,  S = B + Dc^2 - W C^-1 W^T,  with the
 // block-Jacobi preconditioner M = blockdiag(S_ii)^-1 (built by K3b).
 //
-// The PCG is the Chronopoulos-Gear single-reduction form of preconditioned
-// CG: the same iterates as the textbook recurrence in exact arithmetic, but
-// the mat-vec is applied to the preconditioned residual u = M r and both dot
-// products of an iteration come from one reduction, so the camera side needs
-// one cluster barrier per iteration instead of two:
-//   w_k = S u_k;  gamma_k = r_k.u_k;  delta_k = u_k.w_k;
-//   beta_k = gamma_k / gamma_{k-1};  alpha_k = gamma_k / (delta_k - beta_k gamma_k / alpha_{k-1})
-//   (k = 0: beta = 0, alpha = gamma / delta);
-//   p_k = u_k + beta_k p_{k-1};  s_k = w_k + beta_k s_{k-1}  (s = S p);
-//   x_{k+1} = x_k + alpha_k p_k;  r_{k+1} = r_k - alpha_k s_k;  u_{k+1} = M r_{k+1}.
-// The stopping test of call k looks at r_k and x_k (residual ratio, or Ceres'
-// quadratic-model test on Q(x_k) = -x_k.(v + r_k)), i.e. one mat-vec after
-// the textbook loop would have tested them; x is only updated when the loop
-// goes on, so the returned x_k is the same iterate.
+// The recurrence is the textbook (Hestenes-Stiefel) PCG:
+//   p_k = z_k + beta_k p_{k-1}  (p_0 = z_0),   q_k = S p_k,
+//   alpha_k = (r_k.z_k) / (p_k.q_k),
+//   x_{k+1} = x_k + alpha_k p_k,  r_{k+1} = r_k - alpha_k q_k,  z_{k+1} = M r_{k+1},
+//   beta_{k+1} = (r_{k+1}.z_{k+1}) / (r_k.z_k).
+// With the mixed form's FP32 mat-vec, the single-reduction variants
+// (Chronopoulos & Gear, with the shortcut denominator or with p.s expanded
+// by bilinearity) drift measurably from the FP64 solve (final LM costs
+// 2.5e-5 apart on the 250-camera benchmark problem); this form stays within
+// 3e-7, so it pays its second reduction per iteration.
 //
-// One PCG iteration is two kernels:
-//   K4a k_schur_matvec  mat-vec over point-segment chunks (one CTA per chunk,
-//       one thread per observation): y = J_p^T J_c u, t_j = C_j^-1 sum_j y,
-//       J_c^T J_p t_j written at the observation's slot in the chunk's
-//       camera-sorted order, summed per camera run into one partial per
-//       (chunk, camera), stored at the camera's contiguous (camera-major)
-//       position.  No global atomics; every sum has a fixed order.
-//   K4b k_pcg_camera    everything on the camera side, one thread-block
-//       cluster per problem (up to 16 CTAs, one thread per camera
-//       coordinate): w = (B + Dc^2) u - sum of the camera's partials; the
-//       four dot products r.u, u.w, r.r, x.(v + r) in one cluster
-//       reduction; stopping test; alpha, beta; p, s, x, r, u = M r.
-// GB300 runs FP64 at 1/55 of FP32 throughput and with 64-cycle dependent
-// latency, so in the mixed form the matrix-like inner work (partial sums,
-// (B + Dc^2) u, M r) runs in FP32 with compensated sums while the vectors
-// x, r, u, p, s and every dot product stay FP64.
-#include <cooperative_groups.h>
+// One iteration is two kernels, each parallel over the whole GPU:
+//   K4a k_schur_matvec  one CTA per point-segment chunk, one thread per
+//       observation: forms p_k for the chunk's cameras, y = J_p^T J_c p,
+//       t_j = C_j^-1 sum_j y, J_c^T J_p t_j at the observation's slot in the
+//       chunk's camera-sorted order, summed per camera run into one partial
+//       per (chunk, camera) at the camera's contiguous (camera-major)
+//       position; and the chunk's share of p.q:
+//         p.q = sum_cameras p_c.(B_c + Dc^2) p_c - sum_segments p_c.partial,
+//       the camera term taken by the chunk that holds the camera's first
+//       segment (problems of more than kRedDirect chunks: the last CTA of
+//       each group of kRedGroup chunks also sums the group's values).
+//   K4b k_pcg_camera    one CTA per block of kPcgBlockCams cameras: p.q from
+//       the chunk (or group) values, summed by every CTA of the problem in
+//       the same order, so all hold the same alpha_k (a non-positive
+//       curvature ends the PCG); q_k = (B + Dc^2) p_k - sum of the camera's
+//       partials, x, r, z = M r, and the block's r.z, r.r and x.(v + r); the
+//       problem's last block sums them, runs the stopping test on
+//       (x_{k+1}, r_{k+1}) and stores beta_{k+1}.
+// Every cross-CTA sum either is redundant (each CTA sums the same values in
+// the same order) or is done once by the CTA that arrives last at a
+// counter; there are no spin-waits and no atomics on data, so a solve is
+// bitwise deterministic and independent of the other problems of a batch.
+// FP64 division and square root are long instruction sequences on GB300's
+// FP64 pipe (about 64 cycles per dependent operation), so the scalars are
+// formed once per CTA or per problem, with Newton-refined reciprocals.
+// GB300 runs FP64 at 1/55 of FP32 throughput, so in the mixed form the
+// matrix-like work (the mat-vec partials, M r) runs in FP32 with compensated
+// sums, while the vectors x, r, z, p, the products with B and every dot
+// product stay FP64.
 #include <cuda_runtime.h>
 
 #include "kernels.cuh"
 #include "kernels.h"
-
-namespace cg = cooperative_groups;
 
 namespace gba {
 
@@ -48,9 +54,11 @@ namespace {
 template <bool MIXED>
 struct MatvecSmem {
   typedef typename Prec<MIXED>::real real;
-  real pseg[kChunkCap][9];
-  real U[kChunkCap][9];  // first holds w (3 per obs), then u (9 per slot)
+  real pseg[kChunkCap][9];               // p of the chunk's cameras (working precision)
+  real U[kChunkCap][9];                  // first holds w (3 per obs), then u (9 per slot)
   real tpt[kChunkCap][3];
+  double p64[MIXED ? kChunkCap : 1][9];  // mixed form: p in FP64 for the dot product
+  real arow[kChunkCap][10];              // each thread's current task: row of B and Dc^2
 };
 
 __device__ __forceinline__ bool pcg_live(const LMState *L) { return L->active != 0 && L->pcg_active != 0; }
@@ -66,441 +74,399 @@ __device__ __forceinline__ bool pcg_live(const LMState *L) { return L->active !=
 __device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
+// p_k of one coordinate (both kernels evaluate exactly this expression).
+__device__ __forceinline__ double pcg_direction(int k, double beta, double z, double p_old) {
+  return k == 0 ? z : fma(beta, p_old, z);
+}
+
+// Row q of B (the working-precision copy: FP32 in the mixed form) and Dc^2_q
+// of camera c.
+template <bool MIXED>
+__device__ __forceinline__ void a_row(const DeviceBatch &B, int c, int q, typename Prec<MIXED>::real *row) {
+  typedef typename Prec<MIXED>::real real;
+  const real *Bc = reinterpret_cast<const real *>(MIXED ? (const void *)B.cam_Bf : (const void *)B.cam_B) + 45 * (size_t)c;
+#pragma unroll
+  for (int kk = 0; kk < 9; ++kk) row[kk] = Bc[sym9(q, kk)];
+  row[9] = (real)B.cam_D2[9 * (size_t)c + q];
+}
+
+// Row q of (B + Dc^2) y in FP64, from a row given by a_row.
+template <typename real>
+__device__ __forceinline__ double a_times(const real *row, const double *y, int q) {
+  double s = (double)row[9] * y[q];
+#pragma unroll
+  for (int kk = 0; kk < 9; ++kk) s = fma((double)row[kk], y[kk], s);
+  return s;
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
 // K4a
 template <bool MIXED>
-__global__ void __launch_bounds__(kChunkCap) k_schur_matvec(DeviceBatch B) {
+// (four CTAs per SM in the mixed form: 1,024 threads of at most 64 registers)
+__global__ void __launch_bounds__(kChunkCap, MIXED ? 4 : 2) k_schur_matvec(DeviceBatch B) {
   typedef typename Prec<MIXED>::real real;
   typedef typename Prec<MIXED>::real2 real2;
   typedef typename Acc<MIXED>::type Acc;
-  __shared__ MatvecSmem<MIXED> sm;
+  extern __shared__ __align__(16) unsigned char k4_smem[];
+  MatvecSmem<MIXED> &sm = *reinterpret_cast<MatvecSmem<MIXED> *>(k4_smem);
+  __shared__ double red[kChunkCap / 32];
+  __shared__ int flag;
   const int t = threadIdx.x;
-  for (int ch = blockIdx.x; ch < B.nchunks; ch += gridDim.x) {
-    const ChunkInfo ci = B.chunk[ch];
-    const bool valid = t < ci.obs_count;
-    // every load that depends only on the chunk is issued before the first
-    // barrier, so one memory round trip covers them all
-    real2 Jc[9], Jp[3];
-    int lp = 0, slot = 0, s = 0;
-    if (valid) {
-      const int64_t o = ci.obs_begin + t;
+  const int ch = blockIdx.x;
+  const ChunkInfo ci = B.chunk[ch];
+  const bool valid = t < ci.obs_count;
+  // every load that depends only on the chunk is issued before the wait, so
+  // one memory round trip covers them all
+  real2 Jc[9], Jp[3];
+  int lp = 0, slot = 0, s = 0;
+  if (valid) {
+    const int64_t o = ci.obs_begin + t;
 #pragma unroll
-      for (int q = 0; q < 9; ++q) Jc[q] = jload<real2>(B.jac, B.no, q, o);
+    for (int q = 0; q < 9; ++q) Jc[q] = jload<real2>(B.jac, B.no, q, o);
 #pragma unroll
-      for (int q = 0; q < 3; ++q) Jp[q] = jload<real2>(B.jac, B.no, 9 + q, o);
-      s = B.obs_seg[o];
-      slot = B.obs_slot[o];
-      lp = B.obs_pt[o] - ci.pt_begin;
-    }
-    int pb0 = 0, pb1 = 0;
-    real ci6[6] = {0, 0, 0, 0, 0, 0};
-    if (t < ci.pt_count) {
-      const int jj = ci.pt_begin + t;
-      pb0 = B.pt_obs_begin[jj] - ci.obs_begin;
-      pb1 = B.pt_obs_begin[jj + 1] - ci.obs_begin;
-      const real *Ci = reinterpret_cast<const real *>(B.pt_Cinv) + 6 * (size_t)jj;
-#pragma unroll
-      for (int q = 0; q < 6; ++q) ci6[q] = Ci[q];
-    }
-    // the first (segment, coordinate) this thread reduces at the end
-    int f_b0 = 0, f_b1 = 0, f_slot = 0;
-    if (t < ci.seg_count * 9) {
-      const int sg = t / 9;
-      f_b0 = B.seg_pos[ci.seg_begin + sg];
-      f_b1 = (sg + 1 < ci.seg_count) ? B.seg_pos[ci.seg_begin + sg + 1] : ci.obs_count;
-      f_slot = B.seg_slot[ci.seg_begin + sg];
-    }
-    // everything above is fixed during the PCG; from here on the kernel reads
-    // what the previous camera-side kernel wrote (and overwrites the partials
-    // it read)
-    pdl_wait();
-    pdl_launch_dependents();
-    if (!pcg_live(B.lm + ci.problem)) continue;  // uniform over the CTA
-    // stage the vector u of the chunk's cameras
-    const real *pdir = reinterpret_cast<const real *>(MIXED ? (const void *)B.pcg_pf : (const void *)B.pcg_z);
-    for (int i = t; i < ci.seg_count * 9; i += blockDim.x) {
-      const int sg = i / 9, q = i - 9 * sg;
-      sm.pseg[sg][q] = pdir[9 * (size_t)B.seg_cam[ci.seg_begin + sg] + q];
-    }
-    __syncthreads();
-    if (valid) {
-      real zu = 0, zv = 0;
-#pragma unroll
-      for (int q = 0; q < 9; ++q) {
-        const real x = sm.pseg[s][q];
-        zu += Jc[q].x * x;
-        zv += Jc[q].y * x;
-      }
-#pragma unroll
-      for (int q = 0; q < 3; ++q) sm.U[t][q] = Jp[q].x * zu + Jp[q].y * zv;
-    }
-    __syncthreads();
-    if (t < ci.pt_count) {
-      Acc y0, y1, y2;
-      y0.init(), y1.init(), y2.init();
-      for (int k = pb0; k < pb1; ++k) {
-        y0.add(sm.U[k][0]);
-        y1.add(sm.U[k][1]);
-        y2.add(sm.U[k][2]);
-      }
-      const real w0 = (real)y0.value(), w1 = (real)y1.value(), w2 = (real)y2.value();
-      sm.tpt[t][0] = ci6[0] * w0 + ci6[1] * w1 + ci6[2] * w2;
-      sm.tpt[t][1] = ci6[1] * w0 + ci6[3] * w1 + ci6[4] * w2;
-      sm.tpt[t][2] = ci6[2] * w0 + ci6[4] * w1 + ci6[5] * w2;
-    }
-    __syncthreads();
-    if (valid) {
-      const real t0 = sm.tpt[lp][0], t1 = sm.tpt[lp][1], t2 = sm.tpt[lp][2];
-      const real eu = Jp[0].x * t0 + Jp[1].x * t1 + Jp[2].x * t2;
-      const real ev = Jp[0].y * t0 + Jp[1].y * t1 + Jp[2].y * t2;
-#pragma unroll
-      for (int q = 0; q < 9; ++q) sm.U[slot][q] = Jc[q].x * eu + Jc[q].y * ev;
-    }
-    __syncthreads();
-    real *part = reinterpret_cast<real *>(B.seg_partial);
-    for (int i = t; i < ci.seg_count * 9; i += blockDim.x) {
-      const int sg = i / 9, q = i - 9 * sg;
-      int b0 = f_b0, b1 = f_b1, slot9 = f_slot;
-      if (i != t) {
-        b0 = B.seg_pos[ci.seg_begin + sg];
-        b1 = (sg + 1 < ci.seg_count) ? B.seg_pos[ci.seg_begin + sg + 1] : ci.obs_count;
-        slot9 = B.seg_slot[ci.seg_begin + sg];
-      }
-      Acc a;
-      a.init();
-      for (int k = b0; k < b1; ++k) a.add(sm.U[k][q]);
-      part[9 * (size_t)slot9 + q] = (real)a.value();
-    }
-    __syncthreads();
+    for (int q = 0; q < 3; ++q) Jp[q] = jload<real2>(B.jac, B.no, 9 + q, o);
+    s = B.obs_seg[o];
+    slot = B.obs_slot[o];
+    lp = B.obs_pt[o] - ci.pt_begin;
   }
+  int pb0 = 0, pb1 = 0;
+  real ci6[6] = {0, 0, 0, 0, 0, 0};
+  if (t < ci.pt_count) {
+    const int jj = ci.pt_begin + t;
+    pb0 = B.pt_obs_begin[jj] - ci.obs_begin;
+    pb1 = B.pt_obs_begin[jj + 1] - ci.obs_begin;
+    const real *Ci = reinterpret_cast<const real *>(B.pt_Cinv) + 6 * (size_t)jj;
+#pragma unroll
+    for (int q = 0; q < 6; ++q) ci6[q] = Ci[q];
+  }
+  // the first (segment, coordinate) this thread reduces at the end; when the
+  // segment is its camera's first, the row of B + Dc^2 for the camera term
+  // of p.q (B and Dc^2 are fixed during the PCG)
+  int f_b0 = 0, f_b1 = 0, f_slot = 0;
+  size_t f_idx = 0;  // the task's entry of the camera vectors
+  bool f_owner = false;
+  if (t < ci.seg_count * 9) {
+    const int sg = t / 9;
+    f_b0 = B.seg_pos[ci.seg_begin + sg];
+    f_b1 = (sg + 1 < ci.seg_count) ? B.seg_pos[ci.seg_begin + sg + 1] : ci.obs_count;
+    f_slot = B.seg_slot[ci.seg_begin + sg];
+    const int cam = B.seg_cam[ci.seg_begin + sg];
+    f_idx = 9 * (size_t)cam + (t - 9 * sg);
+    f_owner = f_slot == B.cam_seg_begin[cam];
+    if (f_owner) a_row<MIXED>(B, cam, t - 9 * sg, sm.arow[t]);
+  }
+  const ProblemInfo pi = B.prob[ci.problem];
+  // everything above is fixed during the PCG; from here on the kernel reads
+  // what the previous camera-side kernel wrote (and overwrites the partials
+  // it read)
+  pdl_wait();
+  pdl_launch_dependents();
+  const LMState *L = B.lm + ci.problem;
+  // the first task's z and p_{k-1} load together with the problem state
+  // (p is only used when k > 0)
+  double f_z = 0.0, f_p = 0.0;
+  if (t < ci.seg_count * 9) f_z = B.pcg_z[f_idx], f_p = B.pcg_p[f_idx];
+  // uniform over the problem's CTAs: pcg_active only changes in the camera
+  // kernel
+  if (!pcg_live(L)) return;
+  const int k = L->pcg_iterations;
+  const double beta = L->beta;
+  // stage p_k of the chunk's cameras
+  for (int i = t; i < ci.seg_count * 9; i += blockDim.x) {
+    const int sg = i / 9, q = i - 9 * sg;
+    double z = f_z, po = f_p;
+    if (i != t) {
+      const size_t idx = 9 * (size_t)B.seg_cam[ci.seg_begin + sg] + q;
+      z = B.pcg_z[idx], po = B.pcg_p[idx];
+    }
+    const double pk = pcg_direction(k, beta, z, k == 0 ? 0.0 : po);
+    sm.pseg[sg][q] = (real)pk;
+    if (MIXED) sm.p64[sg][q] = pk;
+  }
+  __syncthreads();
+  if (valid) {
+    real zu = 0, zv = 0;
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+      const real x = sm.pseg[s][q];
+      zu += Jc[q].x * x;
+      zv += Jc[q].y * x;
+    }
+#pragma unroll
+    for (int q = 0; q < 3; ++q) sm.U[t][q] = Jp[q].x * zu + Jp[q].y * zv;
+  }
+  __syncthreads();
+  if (t < ci.pt_count) {
+    Acc y0, y1, y2;
+    y0.init(), y1.init(), y2.init();
+    for (int kk = pb0; kk < pb1; ++kk) {
+      y0.add(sm.U[kk][0]);
+      y1.add(sm.U[kk][1]);
+      y2.add(sm.U[kk][2]);
+    }
+    const real w0 = (real)y0.value(), w1 = (real)y1.value(), w2 = (real)y2.value();
+    sm.tpt[t][0] = ci6[0] * w0 + ci6[1] * w1 + ci6[2] * w2;
+    sm.tpt[t][1] = ci6[1] * w0 + ci6[3] * w1 + ci6[4] * w2;
+    sm.tpt[t][2] = ci6[2] * w0 + ci6[4] * w1 + ci6[5] * w2;
+  }
+  __syncthreads();
+  if (valid) {
+    const real t0 = sm.tpt[lp][0], t1 = sm.tpt[lp][1], t2 = sm.tpt[lp][2];
+    const real eu = Jp[0].x * t0 + Jp[1].x * t1 + Jp[2].x * t2;
+    const real ev = Jp[0].y * t0 + Jp[1].y * t1 + Jp[2].y * t2;
+#pragma unroll
+    for (int q = 0; q < 9; ++q) sm.U[slot][q] = Jc[q].x * eu + Jc[q].y * ev;
+  }
+  __syncthreads();
+  real *part = reinterpret_cast<real *>(B.seg_partial);
+  double dot = 0.0;  // this thread's share of p.q
+  for (int i = t; i < ci.seg_count * 9; i += blockDim.x) {
+    const int sg = i / 9, q = i - 9 * sg;
+    int b0 = f_b0, b1 = f_b1, slot9 = f_slot;
+    bool owner = f_owner;
+    if (i != t) {  // a chunk of more than kChunkCap / 9 segments: metadata now
+      b0 = B.seg_pos[ci.seg_begin + sg];
+      b1 = (sg + 1 < ci.seg_count) ? B.seg_pos[ci.seg_begin + sg + 1] : ci.obs_count;
+      slot9 = B.seg_slot[ci.seg_begin + sg];
+      const int cam = B.seg_cam[ci.seg_begin + sg];
+      owner = slot9 == B.cam_seg_begin[cam];
+      if (owner) a_row<MIXED>(B, cam, q, sm.arow[t]);  // the thread's own row, its earlier task done
+    }
+    Acc a;
+    a.init();
+    for (int kk = b0; kk < b1; ++kk) a.add(sm.U[kk][q]);
+    const real pv = (real)a.value();
+    part[9 * (size_t)slot9 + q] = pv;
+    const double *p64 = MIXED ? sm.p64[MIXED ? sg : 0] : reinterpret_cast<const double *>(sm.pseg[sg]);
+    double d = -p64[q] * (double)pv;
+    if (owner) d = fma(p64[q], a_times(sm.arow[t], p64, q), d);  // the camera's (B + Dc^2) term
+    dot += d;
+  }
+  const double chunk_pq = block_sum(dot, red);
+  if (t == 0) B.chunk_red[ch] = chunk_pq;
+  if (pi.chunk_count <= kRedDirect) return;  // the camera kernel sums the chunk values itself
+  // a large problem: the last CTA of each group of kRedGroup chunks sums the
+  // group's values (fixed order); the camera kernel sums the group values
+  const int rel = ch - pi.chunk_begin;
+  const int g0 = pi.chunk_begin + (rel / kRedGroup) * kRedGroup;
+  const int gn = min(kRedGroup, pi.chunk_begin + pi.chunk_count - g0);
+  if (!last_block_done(B.chunk_counter + g0, (uint32_t)gn, &flag)) return;
+  const double gsum = block_sum(t < gn ? __ldcg(B.chunk_red + g0 + t) : 0.0, red);
+  if (t == 0) B.chunk_red[B.nchunks + g0] = gsum;
 }
 
 // ---------------------------------------------------------------------------
-// K4b: one cluster per problem.  A CTA works on camera blocks of
-// kPcgBlockCams cameras with one thread per camera coordinate (9 per
-// camera); a problem with more blocks than the cluster has CTAs takes
-// several passes.
-//
-// The four problem-wide dot products are summed in a fixed order that
-// depends only on the problem's camera count: the per-thread values of a
-// block are staged in shared memory and warp 0 adds them (in thread order
-// per lane, then a xor butterfly) -- one warp of FP64 additions instead of
-// one per warp, since GB300 issues FP64 at a small fraction of its FP32
-// rate; the block values are pushed into the shared memory of every CTA of
-// the cluster (remote stores, one lane per destination) at the block's
-// slot; after the cluster barrier every CTA adds the slots of all blocks in
-// block order, strided over the lanes of one warp, and combines them with a
-// butterfly.  All CTAs therefore hold the same alpha, beta and stopping
-// decision, and the result depends neither on the cluster size nor on the
-// other problems of a batch.  After the barrier no CTA touches another
-// CTA's shared memory.
-//
-// The state of the first kPcgRegPasses passes stays in registers across the
-// barrier; every load of a pass is issued before it.
-constexpr int kPcgThreads = 9 * kPcgBlockCams;
-constexpr int kPcgNv = 4;  // r.u, u.w, r.r, x.(v + r)
-
-namespace {
-
-__device__ __forceinline__ void cluster_arrive() {
-  asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");
-}
-__device__ __forceinline__ void cluster_wait() {
-  asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
-}
-
-// Fixed-order sum of NV values per block slot, slots 0..n-1 of the local
-// array blk (slot e at blk[NV * e]).  Called by one whole warp; the sums are
-// returned in every lane.
-template <int NV>
-__device__ __forceinline__ void slots_sum(const double *blk, int n, double *out) {
-  const int lane = threadIdx.x & 31;
-  double v[NV];
-#pragma unroll
-  for (int k = 0; k < NV; ++k) v[k] = 0.0;
-  for (int e = lane; e < n; e += 32) {
-#pragma unroll
-    for (int k = 0; k < NV; ++k) v[k] += blk[NV * e + k];
-  }
-#pragma unroll
-  for (int k = 0; k < NV; ++k) out[k] = warp_sum(v[k]);
-}
-
-// Block value of NV per-thread values v (all threads call it together):
-// staged in red[NV][kPcgThreads], summed by warp 0 and pushed to slot b of
-// every CTA of the cluster.
-template <int NV>
-__device__ __forceinline__ void block_push(cg::cluster_group &cl, double (*red)[kPcgThreads], const double *v,
-                                           double *slots, int b, int cs) {
-  const int tid = threadIdx.x, lane = tid & 31;
-#pragma unroll
-  for (int k = 0; k < NV; ++k) red[k][tid] = v[k];
-  __syncthreads();
-  if (tid < 32) {
-    constexpr int kWarps = (kPcgThreads + 31) / 32;
-    double s[NV];
-#pragma unroll
-    for (int k = 0; k < NV; ++k) {
-      s[k] = 0.0;
-#pragma unroll
-      for (int w = 0; w < kWarps; ++w)
-        if (lane + 32 * w < kPcgThreads) s[k] += red[k][lane + 32 * w];
-      s[k] = warp_sum(s[k]);
-    }
-    if (lane < cs) {
-      double *dst = cl.map_shared_rank(slots + NV * b, lane);
-#pragma unroll
-      for (int k = 0; k < NV; ++k) dst[k] = s[k];
-    }
-  }
-  __syncthreads();  // red may be reused
-}
-
-// One camera coordinate of a pass.
-template <typename real>
-struct CamCoord {
-  bool valid;
-  int c;
-  double x, r, u, p, s, v, w;
-  real m[9];  // row of the block-Jacobi preconditioner
-};
-
-// Phase 1 of one coordinate: loads the pass state, waits for the mat-vec,
-// computes w = (B + Dc^2) u - sum of partials and the four dot-product terms.
-template <bool MIXED>
-__device__ __forceinline__ void pcg_phase1(const DeviceBatch &B, const ProblemInfo &pi, int k, int q, bool first,
-                                           CamCoord<typename Prec<MIXED>::real> &st, double *d) {
-  typedef typename Prec<MIXED>::real real;
-  typedef typename Acc<MIXED>::type Acc;
-  d[0] = d[1] = d[2] = d[3] = 0.0;
-  st.valid = k < pi.cam_count;
-  st.c = pi.cam_begin + (st.valid ? k : 0);
-  if (!st.valid) return;
-  const int c = st.c;
-  const size_t i = 9 * (size_t)c + q;
-  const real *Bc = reinterpret_cast<const real *>(MIXED ? (const void *)B.cam_Bf : (const void *)B.cam_B) + 45 * (size_t)c;
-  const real *uv = reinterpret_cast<const real *>(MIXED ? (const void *)B.pcg_pf : (const void *)B.pcg_z) + 9 * (size_t)c;
-  const real *M = reinterpret_cast<const real *>(MIXED ? (const void *)B.cam_Minvf : (const void *)B.cam_Minv) +
-                  81 * (size_t)c + 9 * q;
-  const real *part = reinterpret_cast<const real *>(B.seg_partial) + q;
-  const int s0 = B.cam_seg_begin[c], s1 = B.cam_seg_begin[c + 1];
-  st.u = B.pcg_z[i];
-  st.x = B.pcg_x[i];
-  st.r = B.pcg_r[i];
-  st.v = B.pcg_v[i];
-  st.p = first ? 0.0 : B.pcg_p[i];
-  st.s = first ? 0.0 : B.pcg_q[i];
-  const real d2 = (real)B.cam_D2[i];
-  real brow[9], urow[9];
-#pragma unroll
-  for (int kk = 0; kk < 9; ++kk) {
-    brow[kk] = Bc[sym9(q, kk)];
-    urow[kk] = uv[kk];
-    st.m[kk] = M[kk];
-  }
-  pdl_wait();  // the partials come from the mat-vec kernel
-  // the camera's partials: the first kBatch in one round trip, then batches.
-  // FP64: four interleaved accumulators (partial s to accumulator
-  // (s - s0) % 4) shorten the chain of 64-cycle additions fourfold; mixed:
-  // one compensated FP32 sum (its chain is short and each extra accumulator
-  // would cost FP64 conversions)
-  constexpr int kBatch = MIXED ? 64 : 32;
-  constexpr int kAcc = MIXED ? 1 : 4;
-  Acc a[kAcc];
-#pragma unroll
-  for (int uu = 0; uu < kAcc; ++uu) a[uu].init();
-  for (int s = s0; s < s1; s += kBatch) {
-    real pv2[kBatch];
-#pragma unroll
-    for (int uu = 0; uu < kBatch; ++uu) pv2[uu] = (s + uu < s1) ? part[9 * (size_t)(s + uu)] : (real)0;
-#pragma unroll
-    for (int uu = 0; uu < kBatch; ++uu)
-      if (s + uu < s1) a[uu % kAcc].add(pv2[uu]);
-  }
-  double asum = a[0].value();
-  if (kAcc == 4) asum = (a[0].value() + a[1 % kAcc].value()) + (a[2 % kAcc].value() + a[3 % kAcc].value());
-  real bu = 0;
-#pragma unroll
-  for (int kk = 0; kk < 9; ++kk) bu += brow[kk] * urow[kk];
-  st.w = (double)(bu + d2 * (real)st.u - (real)asum);
-  d[0] = st.r * st.u;
-  d[1] = st.u * st.w;
-  d[2] = st.r * st.r;
-  d[3] = st.x * (st.v + st.r);
-}
-
-// Phase 2 of one coordinate (all threads of the CTA call it together):
-// p, s, x, r and u = M r.
-template <bool MIXED>
-__device__ __forceinline__ void pcg_phase2(const DeviceBatch &B, int q, int lc, double alpha, double beta,
-                                           CamCoord<typename Prec<MIXED>::real> &st,
-                                           typename Prec<MIXED>::real *sv, bool sync_before) {
-  typedef typename Prec<MIXED>::real real;
-  double r = 0.0;
-  if (st.valid) {
-    st.p = st.u + beta * st.p;
-    st.s = st.w + beta * st.s;
-    st.x = st.x + alpha * st.p;
-    r = st.r - alpha * st.s;
-  }
-  if (sync_before) __syncthreads();  // the previous pass has finished reading sv
-  sv[threadIdx.x] = (real)r;
-  __syncthreads();
-  if (st.valid) {
-    const real *rv = sv + 9 * lc;
-    real u = 0;
-#pragma unroll
-    for (int kk = 0; kk < 9; ++kk) u += st.m[kk] * rv[kk];
-    const size_t i = 9 * (size_t)st.c + q;
-    B.pcg_p[i] = st.p;
-    B.pcg_q[i] = st.s;
-    B.pcg_x[i] = st.x;
-    B.pcg_r[i] = r;
-    B.pcg_z[i] = (double)u;
-    if (MIXED) B.pcg_pf[i] = (float)u;
-  }
-}
-
-}  // namespace
+// K4b: one CTA per camera block (kPcgBlockCams cameras of one problem).  Each
+// camera coordinate has kPcgSub threads: sub-lane j sums the camera's
+// partials j, j + kPcgSub, ... (so each thread has a fraction of the loads in
+// flight), sub-lane 0 adds the kPcgSub sums in order and updates the
+// coordinate.
+constexpr int kPcgSub = 4;
+constexpr int kPcgCoords = 9 * kPcgBlockCams;
+constexpr int kPcgThreads = kPcgCoords * kPcgSub;
+constexpr int kPcgWarps = kPcgThreads / 32;
+static_assert(kPcgThreads % 32 == 0, "the block reductions combine whole warps");
 
 template <bool MIXED>
 __global__ void __launch_bounds__(kPcgThreads) k_pcg_camera(DeviceBatch B) {
   typedef typename Prec<MIXED>::real real;
-  constexpr int kRegPasses = MIXED ? 2 : 1;
-  // slots: [nblk_max][kPcgNv]
-  extern __shared__ double blk[];
-  __shared__ real sv[kPcgThreads];  // the block's r, staged for u = M r
-  __shared__ double red[kPcgNv][kPcgThreads];
-  __shared__ double tot[kPcgNv];
+  typedef typename Acc<MIXED>::type Acc;
+  __shared__ double psub[kPcgSub][kPcgCoords];  // sub-lane sums of the partials
+  __shared__ double pv[kPcgCoords];             // p_k of the block, for (B + Dc^2) p
+  __shared__ real rv[kPcgCoords];               // r_{k+1} of the block, for M r
+  __shared__ double red[kPcgWarps];
+  __shared__ double red3[kPcgWarps][3];
+  __shared__ double sc[2];
   __shared__ int flag;
-  cg::cluster_group cl = cg::this_cluster();
-  const int cs = (int)cl.num_blocks();
-  const int rank = (int)cl.block_rank();
-  const int prob = blockIdx.x / cs;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int lc = tid / 9, q = tid - 9 * lc;  // camera in the block, coordinate
+  const int4 cb = B.camblk[blockIdx.x];  // (problem, first camera, count, 0)
+  const int prob = cb.x;
+  const int t = threadIdx.x, sub = t / kPcgCoords, m = t - kPcgCoords * sub;
+  const int lc = m / 9, q = m - 9 * lc;
+  const bool valid = lc < cb.z;
+  const bool lead = valid && sub == 0;  // the thread that updates coordinate m
+  const int c = cb.y + (valid ? lc : 0);
+  const size_t i = 9 * (size_t)c + q;
   LMState *L = B.lm + prob;
-  if (prob < B.num_problems && pcg_live(L)) {  // uniform over the cluster
-    const ProblemInfo pi = B.prob[prob];
-    const int nblk = (pi.cam_count + kPcgBlockCams - 1) / kPcgBlockCams;
-    // every LMState field this kernel reads is read before the cluster
-    // barrier: rank 0 overwrites them after it
-    const double gamma_old = L->rz, alpha_old = L->alpha, q_old = L->q0, r0_norm = L->r0_norm;
-    const int k = L->pcg_iterations;  // completed iterations = this call's index
-    CamCoord<real> st[kRegPasses];
-    // ---- w = S u and the four dot products ---------------------------------
+  const ProblemInfo pi = B.prob[prob];
+  // loads of what earlier kernels wrote (the previous camera-side kernel has
+  // completed when this one starts; the problem state changes only in this
+  // kernel's last block of the problem, after every block has read it)
+  const bool live = pcg_live(L);
+  const int k = L->pcg_iterations;
+  const double beta = L->beta, rz_k = L->rz;
+  real arow[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0}, mrow[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  double x = 0.0, r = 0.0, z = 0.0, p_old = 0.0, v = 0.0;
+  int s0 = 0, s1 = 0;
+  if (valid) {
+    s0 = B.cam_seg_begin[c];
+    s1 = B.cam_seg_begin[c + 1];
+  }
+  if (lead) {
+    a_row<MIXED>(B, c, q, arow);
+    const real *M = reinterpret_cast<const real *>(MIXED ? (const void *)B.cam_Minvf : (const void *)B.cam_Minv) +
+                    81 * (size_t)c + 9 * q;
 #pragma unroll
-    for (int j = 0; j < kRegPasses; ++j) {
-      const int b = rank + j * cs;
-      if (b < nblk) {
-        double d[kPcgNv];
-        pcg_phase1<MIXED>(B, pi, b * kPcgBlockCams + lc, q, k == 0, st[j], d);
-        block_push<kPcgNv>(cl, red, d, blk, b, cs);
-      }
-    }
-    for (int b = rank + kRegPasses * cs; b < nblk; b += cs) {
-      CamCoord<real> t;
-      double d[kPcgNv];
-      pcg_phase1<MIXED>(B, pi, b * kPcgBlockCams + lc, q, k == 0, t, d);
-      block_push<kPcgNv>(cl, red, d, blk, b, cs);
-      if (t.valid) B.pcg_w[9 * (size_t)t.c + q] = t.w;  // w of passes not held in registers
-    }
-    pdl_wait();  // every thread, whether or not it had a camera coordinate
-    pdl_launch_dependents();
-    cluster_arrive();
-    cluster_wait();  // after this barrier no CTA touches another's shared memory
-    if (warp == 0) {
-      double t[kPcgNv];
-      slots_sum<kPcgNv>(blk, nblk, t);
-      if (lane == 0) {
+    for (int kk = 0; kk < 9; ++kk) mrow[kk] = M[kk];
+    x = B.pcg_x[i];
+    r = B.pcg_r[i];
+    z = B.pcg_z[i];
+    v = B.pcg_v[i];
+    p_old = B.pcg_p[i];  // used when k > 0
+  }
+  pdl_wait();  // the partials and the chunk values come from the mat-vec kernel
+  double pq = 0.0;
+  if (live) {
+    // p_k.q_k: the chunk values (or, for a large problem, the group values)
+    // in a fixed order, identical in every block of the problem
+    const bool direct = pi.chunk_count <= kRedDirect;
+    const int n = direct ? pi.chunk_count : (pi.chunk_count + kRedGroup - 1) / kRedGroup;
+    const double *cv = B.chunk_red + (direct ? pi.chunk_begin : B.nchunks + pi.chunk_begin);
+    const int stride = direct ? 1 : kRedGroup;
+    double psm = 0.0;
+#pragma unroll 8
+    for (int e = t; e < n; e += kPcgThreads) psm += __ldcg(cv + (size_t)e * stride);
+    // this sub-lane's share of the camera's partials (fixed order)
+    if (valid) {
+      constexpr int kBatch = 32;
+      const real *part = reinterpret_cast<const real *>(B.seg_partial) + q;
+      Acc a;
+      a.init();
+      for (int sg = s0 + sub; sg < s1; sg += kBatch * kPcgSub) {
+        real pp[kBatch];
 #pragma unroll
-        for (int v = 0; v < kPcgNv; ++v) tot[v] = t[v];
+        for (int uu = 0; uu < kBatch; ++uu) {
+          const int e = sg + uu * kPcgSub;
+          pp[uu] = e < s1 ? part[9 * (size_t)e] : (real)0;
+        }
+#pragma unroll
+        for (int uu = 0; uu < kBatch; ++uu)
+          if (sg + uu * kPcgSub < s1) a.add(pp[uu]);
       }
+      psub[sub][m] = a.value();
+    }
+    // p.q over the CTA (fixed order); thread 0 forms alpha once
+    psm = warp_sum(psm);
+    if ((t & 31) == 0) red[t >> 5] = psm;
+    __syncthreads();  // also publishes psub
+    if (t == 0) {
+      double s2 = 0.0;
+      for (int w = 0; w < kPcgWarps; ++w) s2 += red[w];
+      sc[0] = s2;
+      sc[1] = rz_k * recip_nr(s2);
     }
     __syncthreads();
-    const double gamma = tot[0], delta = tot[1], rr = tot[2], qx = tot[3];
-    // ---- stopping test on (x_k, r_k), then alpha_k, beta_k -----------------
-    const DeviceOptions &o = B.opt;
-    const double qk = -qx;  // Q(x_k) = x'Sx - 2 v'x = -x.(v + r)
-    bool stop = false;
-    if (k >= 1) {
-      if (o.pcg_criterion == GBA_PCG_QUADRATIC_MODEL) {
-        const double zeta = k * (qk - q_old) / qk;
-        if (zeta < o.eta && k >= o.min_pcg_iterations) stop = true;
-      } else {
-        if (sqrt(rr) <= o.pcg_tolerance * r0_norm && k >= o.min_pcg_iterations) stop = true;
-      }
+    pq = sc[0];
+  }
+  // the next mat-vec may launch now: its early loads (the Jacobian, some 100
+  // bytes per observation) would otherwise queue in front of this kernel's
+  // latency-bound loads above
+  pdl_launch_dependents();
+  const bool good = pq > 0.0 && isfinite(pq);  // else S is not positive definite along p_k
+  if (live && good) {
+    const double alpha = sc[1];
+    double p = 0.0;
+    if (lead) {
+      p = pcg_direction(k, beta, z, p_old);
+      pv[m] = p;
     }
-    if (k >= o.max_pcg_iterations) stop = true;
-    const double beta = k == 0 ? 0.0 : gamma / gamma_old;
-    const double denom = k == 0 ? delta : delta - beta * gamma / alpha_old;
-    const bool good = denom > 0.0 && isfinite(denom) && isfinite(gamma) && gamma != 0.0;
-    if (!good) stop = true;
-    const double alpha = good ? gamma / denom : 0.0;
-    if (!stop) {
+    __syncthreads();
+    double rz = 0.0, rr = 0.0, qx = 0.0;
+    if (lead) {
+      double psum = psub[0][m];
 #pragma unroll
-      for (int j = 0; j < kRegPasses; ++j) {
-        const int b = rank + j * cs;
-        if (b < nblk) pcg_phase2<MIXED>(B, q, lc, alpha, beta, st[j], sv, j > 0);
-      }
-      for (int b = rank + kRegPasses * cs; b < nblk; b += cs) {
-        CamCoord<real> t;
-        const int kk = b * kPcgBlockCams + lc;
-        t.valid = kk < pi.cam_count;
-        t.c = pi.cam_begin + (t.valid ? kk : 0);
-        if (t.valid) {
-          const size_t i = 9 * (size_t)t.c + q;
-          const real *M = reinterpret_cast<const real *>(MIXED ? (const void *)B.cam_Minvf
-                                                               : (const void *)B.cam_Minv) +
-                          81 * (size_t)t.c + 9 * q;
-          t.u = B.pcg_z[i];
-          t.x = B.pcg_x[i];
-          t.r = B.pcg_r[i];
-          t.w = B.pcg_w[i];  // stored in phase 1
-          t.p = k == 0 ? 0.0 : B.pcg_p[i];
-          t.s = k == 0 ? 0.0 : B.pcg_q[i];
+      for (int j = 1; j < kPcgSub; ++j) psum += psub[j][m];
+      const double qv = a_times(arow, pv + 9 * lc, q) - psum;
+      x = fma(alpha, p, x);
+      r = fma(-alpha, qv, r);
+      rv[m] = (real)r;
+    }
+    __syncthreads();
+    if (lead) {
+      real u = 0;
 #pragma unroll
-          for (int m = 0; m < 9; ++m) t.m[m] = M[m];
+      for (int kk = 0; kk < 9; ++kk) u += mrow[kk] * rv[9 * lc + kk];
+      z = (double)u;
+      B.pcg_p[i] = p;
+      B.pcg_x[i] = x;
+      B.pcg_r[i] = r;
+      B.pcg_z[i] = z;
+      rz = r * z, rr = r * r, qx = x * (v + r);
+    }
+    // the block's r.z, r.r, x.(v + r): warp butterflies, then the warps in
+    // order (thread 0)
+    rz = warp_sum(rz), rr = warp_sum(rr), qx = warp_sum(qx);
+    if ((t & 31) == 0) red3[t >> 5][0] = rz, red3[t >> 5][1] = rr, red3[t >> 5][2] = qx;
+    __syncthreads();
+    if (t == 0) {
+      double b3[3] = {0.0, 0.0, 0.0};
+      for (int w = 0; w < kPcgWarps; ++w) b3[0] += red3[w][0], b3[1] += red3[w][1], b3[2] += red3[w][2];
+      double *o = B.blk_red + 3 * (size_t)blockIdx.x;
+      o[0] = b3[0], o[1] = b3[1], o[2] = b3[2];
+    }
+  }
+  if (live && last_block_done(B.prob_counter + 4 * prob + kPC_UPDATE, (uint32_t)pi.cam_block_count, &flag)) {
+    // the blocks' values in block order: strided over the lanes of warp 0,
+    // then a butterfly (an order fixed by the block count)
+    if (t < 32) {
+      double a3[3] = {0.0, 0.0, 0.0};
+      if (good) {
+        for (int b = t; b < pi.cam_block_count; b += 32) {
+          const double *bv = B.blk_red + 3 * (size_t)(pi.cam_block_begin + b);
+          a3[0] += __ldcg(bv), a3[1] += __ldcg(bv + 1), a3[2] += __ldcg(bv + 2);
         }
-        pcg_phase2<MIXED>(B, q, lc, alpha, beta, t, sv, true);
+        a3[0] = warp_sum(a3[0]), a3[1] = warp_sum(a3[1]), a3[2] = warp_sum(a3[2]);
+      }
+      if (t == 0) {
+        // the stopping test on (x_{k+1}, r_{k+1}) and beta_{k+1}, without
+        // FP64 division or square root (long sequences on GB300's FP64 pipe)
+        const double rz1 = a3[0], rr1 = a3[1], qk = -a3[2];  // Q(x) = x'Sx - 2 v'x = -x.(v + r)
+        const DeviceOptions &o = B.opt;
+        const int k1 = k + 1;  // completed iterations
+        bool stop = !good;     // no update: the PCG ends with x_k (a failed solve if k = 0)
+        if (good) {
+          if (o.pcg_criterion == GBA_PCG_QUADRATIC_MODEL) {
+            // zeta = k1 (Q_k1 - Q_k) / Q_k1 < eta, multiplied through by Q_k1
+            const double lhs = k1 * (qk - L->q0), rhs = o.eta * qk;
+            const bool below = qk > 0.0 ? lhs < rhs : (qk < 0.0 ? lhs > rhs : L->q0 > 0.0);
+            if (below && k1 >= o.min_pcg_iterations) stop = true;
+          } else {
+            const double lim = o.pcg_tolerance * L->r0_norm;  // |r| <= tol |r_0|
+            if (rr1 <= lim * lim && k1 >= o.min_pcg_iterations) stop = true;
+          }
+          if (k1 >= o.max_pcg_iterations) stop = true;
+          if (!(rz1 != 0.0 && isfinite(rz1))) stop = true;
+          L->pcg_iterations = k1;
+          L->beta = rz1 * recip_nr(rz_k);
+          L->rz = rz1;
+          L->rr = rr1;
+          L->q0 = qk;
+          L->pq = pq;
+        } else if (k == 0) {
+          L->linear_ok = 0;  // S not positive definite along the first direction
+        }
+        if (stop) {
+          L->pcg_active = 0;
+          atomicSub(B.status + 3, 1);
+        }
+        if (B.num_problems == 1) {
+          // the only problem decides the loop: no grid-wide count needed
+          B.status[2] = stop ? 0 : 1;
+          if (B.use_cond && B.pcg_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)B.pcg_cond, stop ? 0u : 1u);
+        }
       }
     }
-    if (rank == 0 && tid == 0) {
-      if (!stop) {
-        L->pcg_iterations = k + 1;
-        L->rz = gamma;
-        L->alpha = alpha;
-        L->beta = beta;
-        L->q0 = qk;
-      } else if (k == 0 && !good) {
-        L->linear_ok = 0;  // S not positive definite along the first direction
-      }
-      L->pq = delta;
-      L->rr = rr;
-      if (stop) L->pcg_active = 0;
-      if (B.num_problems == 1) {
-        // the only problem decides the loop: no cross-cluster count needed
-        B.status[2] = stop ? 0 : 1;
-        if (B.use_cond && B.pcg_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)B.pcg_cond, stop ? 0u : 1u);
-      }
-    }
-  } else if (B.num_problems == 1 && blockIdx.x == 0 && tid == 0) {
-    pdl_wait();
-    pdl_launch_dependents();
+  } else if (!live && B.num_problems == 1 && blockIdx.x == 0 && t == 0) {
     B.status[2] = 0;
     if (B.use_cond && B.pcg_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)B.pcg_cond, 0u);
   }
   if (B.num_problems == 1) return;
-  pdl_wait();
-  pdl_launch_dependents();
-  // several problems: the last cluster to finish sets the PCG loop condition
-  if (cs > 1 && rank != 0) return;
-  if (last_block_done(B.global_counter + kGC_UPDATE, (uint32_t)(gridDim.x / cs), &flag)) {
-    if (tid == 0) {
-      int any = 0;
-      for (int p2 = 0; p2 < B.num_problems; ++p2) any |= __ldcg(&B.lm[p2].active) && __ldcg(&B.lm[p2].pcg_active);
+  // several problems: the grid's last CTA sets the PCG loop condition from
+  // the count of problems whose PCG is still running
+  if (last_block_done(B.global_counter + kGC_UPDATE, gridDim.x, &flag)) {
+    if (t == 0) {
+      const int any = __ldcg(B.status + 3) > 0 ? 1 : 0;
       B.status[2] = any;
       if (B.use_cond && B.pcg_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)B.pcg_cond, any ? 1u : 0u);
     }
@@ -511,9 +477,11 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg_camera(DeviceBatch B) {
 // pdl: launch as a programmatic dependent of the preceding kernel of the
 // stream (which must be the other PCG kernel).
 cudaError_t launch_schur_matvec(const DeviceBatch &b, bool mixed, cudaStream_t s, bool pdl) {
+  if (b.nchunks == 0) return cudaSuccess;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)b.nchunks);
   cfg.blockDim = dim3(kChunkCap);
+  cfg.dynamicSmemBytes = mixed ? sizeof(MatvecSmem<true>) : sizeof(MatvecSmem<false>);
   cfg.stream = s;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -525,20 +493,16 @@ cudaError_t launch_schur_matvec(const DeviceBatch &b, bool mixed, cudaStream_t s
 }
 
 cudaError_t launch_pcg_camera(const DeviceBatch &b, bool mixed, cudaStream_t s, bool pdl) {
+  if (b.cam_blocks == 0) return cudaSuccess;
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((unsigned)(b.num_problems * b.pcg_cluster));
+  cfg.gridDim = dim3((unsigned)b.cam_blocks);
   cfg.blockDim = dim3(kPcgThreads);
-  cfg.dynamicSmemBytes = pcg_camera_smem(b.pcg_passes, b.pcg_cluster);
   cfg.stream = s;
-  cudaLaunchAttribute attr[2];
-  attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = (unsigned)b.pcg_cluster;
-  attr[0].val.clusterDim.y = 1;
-  attr[0].val.clusterDim.z = 1;
-  attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[1].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
-  cfg.numAttrs = pdl ? 2 : 1;
+  cfg.numAttrs = pdl ? 1 : 0;
   if (mixed) return cudaLaunchKernelEx(&cfg, k_pcg_camera<true>, b);
   return cudaLaunchKernelEx(&cfg, k_pcg_camera<false>, b);
 }
@@ -548,24 +512,10 @@ void launch_pcg_iteration(const DeviceBatch &b, bool mixed, cudaStream_t s) {
   launch_pcg_camera(b, mixed, s, false);
 }
 
-// Slots of every camera block of the largest problem (passes x cluster size),
-// kPcgNv doubles per block.
-size_t pcg_camera_smem(int passes, int cluster) {
-  return sizeof(double) * kPcgNv * (size_t)(passes > 0 ? passes : 1) * (size_t)(cluster > 0 ? cluster : 1);
-}
-
-// Largest cluster the camera kernel may use on this device (16 when the
-// non-portable size is allowed, else 8).
-int pcg_max_cluster() {
-  cudaFuncSetAttribute(k_pcg_camera<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPcgSmemMax);
-  cudaFuncSetAttribute(k_pcg_camera<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPcgSmemMax);
-  const cudaError_t e1 = cudaFuncSetAttribute(k_pcg_camera<true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-  const cudaError_t e2 = cudaFuncSetAttribute(k_pcg_camera<false>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-  if (e1 != cudaSuccess || e2 != cudaSuccess) {
-    cudaGetLastError();
-    return 8;
-  }
-  return 16;
+// Dynamic shared memory of the mat-vec kernel (above the 48 KB static limit).
+void pcg_init() {
+  cudaFuncSetAttribute(k_schur_matvec<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(MatvecSmem<true>));
+  cudaFuncSetAttribute(k_schur_matvec<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(MatvecSmem<false>));
 }
 
 }  // namespace gba

@@ -297,9 +297,7 @@ __global__ void __launch_bounds__(kSchurThreads) k_camera_schur(DeviceBatch B) {
       B.pcg_v[i] = vec[t];
       B.pcg_r[i] = vec[t];
       B.pcg_x[i] = 0.0;
-      B.pcg_p[i] = z;  // first direction p0 = z0
-      B.pcg_z[i] = z;
-      if (MIXED) B.pcg_pf[i] = (float)z;
+      B.pcg_z[i] = z;  // the first direction p_0 = z_0 is formed by the PCG kernels
       rz = vec[t] * z;
       rr = vec[t] * vec[t];
     }
@@ -333,16 +331,14 @@ __global__ void __launch_bounds__(kSchurThreads) k_camera_schur(DeviceBatch B) {
   }
   // the grid's last CTA sets the PCG loop condition
   if (last_block_done(B.global_counter + kGC_SCHUR, gridDim.x, &flag)) {
+    double cnt = 0.0;
+    for (int q = t; q < B.num_problems; q += blockDim.x)
+      cnt += (__ldcg(&B.lm[q].active) && __ldcg(&B.lm[q].pcg_active)) ? 1.0 : 0.0;
+    const int count = (int)block_sum(cnt, red);
     if (t == 0) {
-      int any = 0, count = 0;
-      for (int q = 0; q < B.num_problems; ++q) {
-        const int a = __ldcg(&B.lm[q].active) && __ldcg(&B.lm[q].pcg_active);
-        any |= a;
-        count += a;
-      }
-      B.status[2] = any;
+      B.status[2] = count > 0 ? 1 : 0;
       B.status[3] = count;
-      if (B.use_cond && B.pcg_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)B.pcg_cond, any ? 1u : 0u);
+      if (B.use_cond && B.pcg_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)B.pcg_cond, count > 0 ? 1u : 0u);
     }
   }
 }
@@ -364,7 +360,9 @@ void point_schur_init() {
 // ---------------------------------------------------------------------------
 // K5: y_p = C^-1 (g_p - W^T y_c), step = -y, model cost change
 // -m.(r + m/2) with m = J step, candidate points x + step * scale.  FP64
-// arithmetic in both modes (the acceptance ratio is FP64).
+// arithmetic in both modes (the acceptance ratio is FP64); in the mixed form
+// m.r = step.g comes from the FP64 gradient (step_p.g_p here, step_c.g_c in
+// K5b), and only |m|^2 from the FP32 Jacobian copies.
 template <bool MIXED>
 __global__ void __launch_bounds__(kChunkCap) k_back_substitute(DeviceBatch B) {
   // mixed form: the inner products with the FP32 Jacobian run in FP32; the
@@ -413,7 +411,7 @@ __global__ void __launch_bounds__(kChunkCap) k_back_substitute(DeviceBatch B) {
       rv = r.y;
     }
     __syncthreads();
-    double s2 = 0.0;
+    double s2 = 0.0, ymodel = 0.0;
     if (t < ci.pt_count) {
       const int jj = ci.pt_begin + t;
       const int b0 = B.pt_obs_begin[jj] - ci.obs_begin, b1 = B.pt_obs_begin[jj + 1] - ci.obs_begin;
@@ -431,6 +429,7 @@ __global__ void __launch_bounds__(kChunkCap) k_back_substitute(DeviceBatch B) {
       const double *sc = B.pt_scale + 3 * (size_t)jj;
       const double y[3] = {y0, y1, y2};
       const bool used = B.pt_used[jj] != 0;
+      if (MIXED && used) ymodel = -(y0 * g[0] + y1 * g[1] + y2 * g[2]);  // step_p.g_p
 #pragma unroll
       for (int q = 0; q < 3; ++q) {
         const double cand = used ? x[q] + (-y[q]) * sc[q] : x[q];
@@ -440,11 +439,13 @@ __global__ void __launch_bounds__(kChunkCap) k_back_substitute(DeviceBatch B) {
       }
     }
     __syncthreads();
-    double model = 0.0;
+    double model = ymodel;
     if (valid) {
       const double m0 = -(double)(zu + Jpu[0] * ypt[lp][0] + Jpu[1] * ypt[lp][1] + Jpu[2] * ypt[lp][2]);
       const double m1 = -(double)(zv + Jpv[0] * ypt[lp][0] + Jpv[1] * ypt[lp][1] + Jpv[2] * ypt[lp][2]);
-      model = m0 * (ru + m0 / 2.0) + m1 * (rv + m1 / 2.0);
+      // mixed form: m.r = step.g is taken from the FP64 gradient (point part
+      // above, camera part in K5b); only |m|^2 / 2 comes from the FP32 copies
+      model += MIXED ? (m0 * m0 + m1 * m1) / 2.0 : m0 * (ru + m0 / 2.0) + m1 * (rv + m1 / 2.0);
     }
     const double ms = block_sum(model, red);
     const double ss = block_sum(s2, red);
@@ -480,7 +481,10 @@ __global__ void __launch_bounds__(256) k_decide(DeviceBatch B) {
   if (!L->active) return;
   const ProblemInfo pi = B.prob[p];
   const int c0 = pi.chunk_begin, c1 = pi.chunk_begin + pi.chunk_count;
-  const double model = -block_range_sum(B.chunk_scal + kCS_MODEL, c0, c1, kChunkScal, red);
+  // model cost change -(m.r + |m|^2 / 2) summed; the mixed form adds its
+  // camera part of m.r = step.g here
+  double model = -block_range_sum(B.chunk_scal + kCS_MODEL, c0, c1, kChunkScal, red);
+  if (B.opt.mixed) model -= block_range_sum(B.cam_scal + kCC_YG, pi.cam_begin, pi.cam_begin + pi.cam_count, kCamScal, red);
   const double cand = block_range_sum(B.chunk_scal + kCS_COST, c0, c1, kChunkScal, red);
   const double bad = block_range_max(B.chunk_scal + kCS_BAD, c0, c1, kChunkScal, red);
   const double s2p = block_range_sum(B.chunk_scal + kCS_STEP2, c0, c1, kChunkScal, red);

@@ -115,17 +115,23 @@ __device__ __forceinline__ double warp_max(double v) {
 }
 
 // Sum over the CTA; result valid in every thread.  `red` needs blockDim/32
-// doubles.  Contains __syncthreads(): call from all threads.
+// doubles.  Contains __syncthreads(): call from all threads.  Thread 0 adds
+// the warp sums in warp order and broadcasts the total (GB300 issues FP64 at
+// about two operations per clock per SM, so the total is formed once per CTA,
+// not once per thread).
 __device__ __forceinline__ double block_sum(double v, double *red) {
   v = warp_sum(v);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   __syncthreads();
   if (lane == 0) red[warp] = v;
   __syncthreads();
-  double s = 0.0;
-  for (int w = 0; w < nw; ++w) s += red[w];
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int w = 0; w < nw; ++w) s += red[w];
+    red[0] = s;
+  }
   __syncthreads();
-  return s;
+  return red[0];
 }
 __device__ __forceinline__ double block_max(double v, double *red) {
   v = warp_max(v);
@@ -133,41 +139,51 @@ __device__ __forceinline__ double block_max(double v, double *red) {
   __syncthreads();
   if (lane == 0) red[warp] = v;
   __syncthreads();
-  double s = 0.0;
-  for (int w = 0; w < nw; ++w) s = fmax(s, red[w]);
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int w = 0; w < nw; ++w) s = fmax(s, red[w]);
+    red[0] = s;
+  }
   __syncthreads();
-  return s;
+  return red[0];
 }
 
-// Strided sum of a[begin..end) by the whole CTA in a fixed order.
+// Strided sum of a[begin..end) by the whole CTA in a fixed order (L2 loads:
+// the values may come from other CTAs of the same kernel).
 __device__ __forceinline__ double block_range_sum(const double *a, int begin, int end, int stride,
                                                   double *red) {
   double s = 0.0;
-  for (int i = begin + threadIdx.x; i < end; i += blockDim.x) s += a[(size_t)i * stride];
+  for (int i = begin + threadIdx.x; i < end; i += blockDim.x) s += __ldcg(a + (size_t)i * stride);
   return block_sum(s, red);
 }
 __device__ __forceinline__ double block_range_max(const double *a, int begin, int end, int stride,
                                                   double *red) {
   double s = 0.0;
-  for (int i = begin + threadIdx.x; i < end; i += blockDim.x) s = fmax(s, a[(size_t)i * stride]);
+  for (int i = begin + threadIdx.x; i < end; i += blockDim.x) s = fmax(s, __ldcg(a + (size_t)i * stride));
   return block_max(s, red);
 }
 
-// "Last CTA done" detection without waiting: each CTA fences its writes and
-// bumps a counter; the CTA that brings it to `total` sees everyone's results
-// and resets the counter.  Returns true in every thread of the last CTA.
+// "Last CTA done" detection without waiting: each CTA bumps a counter after
+// a CTA barrier and a device-scope fence by the bumping thread (the barrier
+// orders every thread's earlier writes before that fence, the pattern of a
+// cooperative grid barrier); the CTA that brings the counter to `total`
+// fences again, so after the final barrier all its threads see every CTA's
+// results (read them with __ldcg), and resets the counter.  Returns true in
+// every thread of the last CTA.
 __device__ __forceinline__ bool last_block_done(uint32_t *counter, uint32_t total, int *flag) {
-  __threadfence();
   __syncthreads();
   if (threadIdx.x == 0) {
+    __threadfence();
     const uint32_t prev = atomicAdd(counter, 1u);
-    *flag = (prev == total - 1u);
-    if (*flag) *counter = 0u;
+    const int last = (prev == total - 1u);
+    if (last) {
+      *counter = 0u;
+      __threadfence();
+    }
+    *flag = last;
   }
   __syncthreads();
-  const bool last = *flag != 0;
-  if (last) __threadfence();
-  return last;
+  return *flag != 0;
 }
 
 // ---------------------------------------------------------------------------

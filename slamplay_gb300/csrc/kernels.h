@@ -28,13 +28,12 @@ void launch_camera_schur(const DeviceBatch &b, bool mixed, cudaStream_t s);
 // K4a-b: one PCG iteration (implicit Schur mat-vec, camera-side update).
 void launch_pcg_iteration(const DeviceBatch &b, bool mixed, cudaStream_t s);
 cudaError_t launch_schur_matvec(const DeviceBatch &b, bool mixed, cudaStream_t s, bool pdl);
-// K4b alone (one thread-block cluster per problem).
+// K4b alone (one CTA per block of kPcgBlockCams cameras).
 cudaError_t launch_pcg_camera(const DeviceBatch &b, bool mixed, cudaStream_t s, bool pdl);
-// Largest cluster size the camera-side kernel may use on this device.
-int pcg_max_cluster();
 void launch_prof_delay(cudaStream_t s);
 void point_schur_init();
-size_t pcg_camera_smem(int passes, int cluster);
+// Kernel attributes of the PCG kernels (once per device).
+void pcg_init();
 // K5: point back-substitution, model cost change, candidate points.
 void launch_back_substitute(const DeviceBatch &b, bool mixed, cudaStream_t s);
 // K5b + K2: candidate cameras (+ their tables) and the candidate cost.

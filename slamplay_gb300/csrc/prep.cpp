@@ -228,11 +228,11 @@ gba_status prepare_batch(const gba_problem_view *views, int n, const PrepOptions
     pi.seg_count = (int)hb.seg_cam.size() - pi.seg_begin;
     // camera blocks of the PCG kernels
     pi.cam_block_begin = (int)hb.camblk.size();
-    for (int c = 0; c < nc; c += kCamPerBlock) {
+    for (int c = 0; c < nc; c += kPcgBlockCams) {
       int4 b;
       b.x = p;
       b.y = cam0 + c;
-      b.z = std::min(kCamPerBlock, nc - c);
+      b.z = std::min(kPcgBlockCams, nc - c);
       b.w = 0;
       hb.camblk.push_back(b);
     }
