@@ -218,6 +218,8 @@ size_t Engine::layout(const HostBatch &hb, char *base, DeviceBatch *db, size_t *
   b.pcg_z = cv.take<double>(9 * nc);
   b.pcg_p = cv.take<double>(9 * nc);
   b.pcg_v = cv.take<double>(9 * nc);
+  b.pcg_zf = cv.take<float>(9 * nc);
+  b.pcg_pf = cv.take<float>(9 * nc);
   b.cam_colnorm = cv.take<double>(9 * nc);
   b.seg_partial = cv.take<double>(9 * ns);
   b.schur_partial = cv.take<char>(54 * ns * rs);

@@ -125,8 +125,10 @@ struct DeviceBatch {
   float *cam_Minvf;          // 81, FP32 copy (mixed form)
   float *cam_Bf;             // 45, FP32 copy of cam_B (mixed form)
   double *cam_D2;            // 9: squared LM diagonal of the camera parameters
-  // PCG vectors, 9 * nc each: x, r, z (= M r), p (direction), v (rhs)
+  // PCG vectors, 9 * nc each: x, r, z (= M r), p (direction), v (rhs); FP32
+  // copies of z and p (the mixed form's mat-vec forms its direction from them)
   double *pcg_x, *pcg_r, *pcg_z, *pcg_p, *pcg_v;
+  float *pcg_zf, *pcg_pf;
   double *cam_colnorm;       // 9 * nc: column norms of the first evaluation
   double *pt_colnorm;        // 3 * np
   void *seg_partial;         // 9 * nseg, double (FP64) or float (mixed)
@@ -152,7 +154,7 @@ struct DeviceBatch {
   // PCG reductions: per chunk its share of p.q, then per group of kRedGroup
   // chunks ([nchunks + first chunk of the group]); per camera block its
   // r.z, r.r, x.(v + r)
-  double *chunk_red;         // 2 * nchunks
+  double *chunk_red;         // 2 * nchunks (mixed form: double-float pairs, hi then lo)
   uint32_t *chunk_counter;   // nchunks (one per group, at its first chunk)
   double *blk_red;           // 3 * cam_blocks
 };

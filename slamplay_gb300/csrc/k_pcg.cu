@@ -54,11 +54,10 @@ namespace {
 template <bool MIXED>
 struct MatvecSmem {
   typedef typename Prec<MIXED>::real real;
-  real pseg[kChunkCap][9];               // p of the chunk's cameras (working precision)
-  real U[kChunkCap][9];                  // first holds w (3 per obs), then u (9 per slot)
+  real pseg[kChunkCap][9];   // p of the chunk's cameras (working precision)
+  real U[kChunkCap][9];      // first holds w (3 per obs), then u (9 per slot)
   real tpt[kChunkCap][3];
-  double p64[MIXED ? kChunkCap : 1][9];  // mixed form: p in FP64 for the dot product
-  real arow[kChunkCap][10];              // each thread's current task: row of B and Dc^2
+  real arow[kChunkCap][10];  // each thread's current task: row of B and Dc^2
 };
 
 __device__ __forceinline__ bool pcg_live(const LMState *L) { return L->active != 0 && L->pcg_active != 0; }
@@ -90,13 +89,45 @@ __device__ __forceinline__ void a_row(const DeviceBatch &B, int c, int q, typena
   row[9] = (real)B.cam_D2[9 * (size_t)c + q];
 }
 
-// Row q of (B + Dc^2) y in FP64, from a row given by a_row.
+// Row q of (B + Dc^2) y in FP64, from a row given by a_row (two chains of
+// five: FP64 operations have a long dependent latency on GB300).
 template <typename real>
 __device__ __forceinline__ double a_times(const real *row, const double *y, int q) {
-  double s = (double)row[9] * y[q];
+  double s0 = (double)row[9] * y[q], s1 = (double)row[8] * y[8];
 #pragma unroll
-  for (int kk = 0; kk < 9; ++kk) s = fma((double)row[kk], y[kk], s);
-  return s;
+  for (int kk = 0; kk < 8; kk += 2) {
+    s0 = fma((double)row[kk], y[kk], s0);
+    s1 = fma((double)row[kk + 1], y[kk + 1], s1);
+  }
+  return s0 + s1;
+}
+
+// A chunk (or group) value of p.q: FP64 in the FP64 form, a double-float
+// pair in the mixed form (stored in the double slot).
+__device__ __forceinline__ DF chunk_value_load(const DeviceBatch &B, size_t slot) {
+  const float2 v = __ldcg(reinterpret_cast<const float2 *>(B.chunk_red + slot));
+  return DF{v.x, v.y};
+}
+
+// Sums the CTA's values (fixed order: warp butterflies, then thread 0 adds
+// the warps in order) and stores the total at chunk_red[slot].  Call from
+// every thread.
+template <bool MIXED>
+__device__ __forceinline__ void chunk_value_store(const DeviceBatch &B, size_t slot, double d, DF f, DF *dfred,
+                                                  double *red) {
+  if (MIXED) {
+    f = df_warp_sum(f);
+    if ((threadIdx.x & 31) == 0) dfred[threadIdx.x >> 5] = f;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      DF s = dfred[0];
+      for (int w = 1; w < (int)(blockDim.x >> 5); ++w) s = df_add(s, dfred[w]);
+      *reinterpret_cast<float2 *>(B.chunk_red + slot) = make_float2(s.hi, s.lo);
+    }
+  } else {
+    const double v = block_sum(d, red);
+    if (threadIdx.x == 0) B.chunk_red[slot] = v;
+  }
 }
 
 }  // namespace
@@ -112,6 +143,7 @@ __global__ void __launch_bounds__(kChunkCap, MIXED ? 4 : 2) k_schur_matvec(Devic
   extern __shared__ __align__(16) unsigned char k4_smem[];
   MatvecSmem<MIXED> &sm = *reinterpret_cast<MatvecSmem<MIXED> *>(k4_smem);
   __shared__ double red[kChunkCap / 32];
+  __shared__ DF dfred[kChunkCap / 32];
   __shared__ int flag;
   const int t = threadIdx.x;
   const int ch = blockIdx.x;
@@ -164,26 +196,31 @@ __global__ void __launch_bounds__(kChunkCap, MIXED ? 4 : 2) k_schur_matvec(Devic
   pdl_wait();
   pdl_launch_dependents();
   const LMState *L = B.lm + ci.problem;
-  // the first task's z and p_{k-1} load together with the problem state
-  // (p is only used when k > 0)
-  double f_z = 0.0, f_p = 0.0;
-  if (t < ci.seg_count * 9) f_z = B.pcg_z[f_idx], f_p = B.pcg_p[f_idx];
+  // the first task's z and p_{k-1} (FP32 copies in the mixed form) load
+  // together with the problem state (p is only used when k > 0)
+  const real *zv = reinterpret_cast<const real *>(MIXED ? (const void *)B.pcg_zf : (const void *)B.pcg_z);
+  const real *pvv = reinterpret_cast<const real *>(MIXED ? (const void *)B.pcg_pf : (const void *)B.pcg_p);
+  real f_z = 0, f_p = 0;
+  if (t < ci.seg_count * 9) f_z = zv[f_idx], f_p = pvv[f_idx];
   // uniform over the problem's CTAs: pcg_active only changes in the camera
   // kernel
   if (!pcg_live(L)) return;
   const int k = L->pcg_iterations;
   const double beta = L->beta;
-  // stage p_k of the chunk's cameras
+  // stage p_k of the chunk's cameras: the FP64 form evaluates exactly the
+  // camera kernel's expression; the mixed form the same recurrence in FP32
+  // on the FP32 copies (its mat-vec input is FP32 anyway)
   for (int i = t; i < ci.seg_count * 9; i += blockDim.x) {
     const int sg = i / 9, q = i - 9 * sg;
-    double z = f_z, po = f_p;
+    real z = f_z, po = f_p;
     if (i != t) {
       const size_t idx = 9 * (size_t)B.seg_cam[ci.seg_begin + sg] + q;
-      z = B.pcg_z[idx], po = B.pcg_p[idx];
+      z = zv[idx], po = pvv[idx];
     }
-    const double pk = pcg_direction(k, beta, z, k == 0 ? 0.0 : po);
-    sm.pseg[sg][q] = (real)pk;
-    if (MIXED) sm.p64[sg][q] = pk;
+    if (MIXED)
+      sm.pseg[sg][q] = k == 0 ? z : (real)__fmaf_rn((float)beta, (float)po, (float)z);
+    else
+      sm.pseg[sg][q] = (real)pcg_direction(k, beta, (double)z, k == 0 ? 0.0 : (double)po);
   }
   __syncthreads();
   if (valid) {
@@ -206,7 +243,7 @@ __global__ void __launch_bounds__(kChunkCap, MIXED ? 4 : 2) k_schur_matvec(Devic
       y1.add(sm.U[kk][1]);
       y2.add(sm.U[kk][2]);
     }
-    const real w0 = (real)y0.value(), w1 = (real)y1.value(), w2 = (real)y2.value();
+    const real w0 = (real)y0.rvalue(), w1 = (real)y1.rvalue(), w2 = (real)y2.rvalue();
     sm.tpt[t][0] = ci6[0] * w0 + ci6[1] * w1 + ci6[2] * w2;
     sm.tpt[t][1] = ci6[1] * w0 + ci6[3] * w1 + ci6[4] * w2;
     sm.tpt[t][2] = ci6[2] * w0 + ci6[4] * w1 + ci6[5] * w2;
@@ -221,7 +258,10 @@ __global__ void __launch_bounds__(kChunkCap, MIXED ? 4 : 2) k_schur_matvec(Devic
   }
   __syncthreads();
   real *part = reinterpret_cast<real *>(B.seg_partial);
-  double dot = 0.0;  // this thread's share of p.q
+  // this thread's share of p.q: FP64 in the FP64 form, double-float in the
+  // mixed form (FP32 instructions, converted once per CTA)
+  double dot = 0.0;
+  DF dotf = df_zero();
   for (int i = t; i < ci.seg_count * 9; i += blockDim.x) {
     const int sg = i / 9, q = i - 9 * sg;
     int b0 = f_b0, b1 = f_b1, slot9 = f_slot;
@@ -237,15 +277,26 @@ __global__ void __launch_bounds__(kChunkCap, MIXED ? 4 : 2) k_schur_matvec(Devic
     Acc a;
     a.init();
     for (int kk = b0; kk < b1; ++kk) a.add(sm.U[kk][q]);
-    const real pv = (real)a.value();
+    const real pv = (real)a.rvalue();
     part[9 * (size_t)slot9 + q] = pv;
-    const double *p64 = MIXED ? sm.p64[MIXED ? sg : 0] : reinterpret_cast<const double *>(sm.pseg[sg]);
-    double d = -p64[q] * (double)pv;
-    if (owner) d = fma(p64[q], a_times(sm.arow[t], p64, q), d);  // the camera's (B + Dc^2) term
-    dot += d;
+    const real *ps = sm.pseg[sg];
+    if (MIXED) {
+      dotf = df_add(dotf, df_prod(-(float)ps[q], (float)pv));
+      if (owner) {  // the camera's (B + Dc^2) term
+        const real *ar = sm.arow[t];
+        float ap = __fmul_rn((float)ar[9], (float)ps[q]);
+#pragma unroll
+        for (int kk = 0; kk < 9; ++kk) ap = __fmaf_rn((float)ar[kk], (float)ps[kk], ap);
+        dotf = df_add(dotf, df_prod((float)ps[q], ap));
+      }
+    } else {
+      const double *p64 = reinterpret_cast<const double *>(ps);
+      double d = -p64[q] * (double)pv;
+      if (owner) d = fma(p64[q], a_times(sm.arow[t], p64, q), d);  // the camera's (B + Dc^2) term
+      dot += d;
+    }
   }
-  const double chunk_pq = block_sum(dot, red);
-  if (t == 0) B.chunk_red[ch] = chunk_pq;
+  chunk_value_store<MIXED>(B, ch, dot, dotf, dfred, red);
   if (pi.chunk_count <= kRedDirect) return;  // the camera kernel sums the chunk values itself
   // a large problem: the last CTA of each group of kRedGroup chunks sums the
   // group's values (fixed order); the camera kernel sums the group values
@@ -253,8 +304,15 @@ __global__ void __launch_bounds__(kChunkCap, MIXED ? 4 : 2) k_schur_matvec(Devic
   const int g0 = pi.chunk_begin + (rel / kRedGroup) * kRedGroup;
   const int gn = min(kRedGroup, pi.chunk_begin + pi.chunk_count - g0);
   if (!last_block_done(B.chunk_counter + g0, (uint32_t)gn, &flag)) return;
-  const double gsum = block_sum(t < gn ? __ldcg(B.chunk_red + g0 + t) : 0.0, red);
-  if (t == 0) B.chunk_red[B.nchunks + g0] = gsum;
+  double gd = 0.0;
+  DF gf = df_zero();
+  if (t < gn) {
+    if (MIXED)
+      gf = chunk_value_load(B, g0 + t);
+    else
+      gd = __ldcg(B.chunk_red + g0 + t);
+  }
+  chunk_value_store<MIXED>(B, B.nchunks + g0, gd, gf, dfred, red);
 }
 
 // ---------------------------------------------------------------------------
@@ -263,7 +321,7 @@ __global__ void __launch_bounds__(kChunkCap, MIXED ? 4 : 2) k_schur_matvec(Devic
 // partials j, j + kPcgSub, ... (so each thread has a fraction of the loads in
 // flight), sub-lane 0 adds the kPcgSub sums in order and updates the
 // coordinate.
-constexpr int kPcgSub = 4;
+constexpr int kPcgSub = 8;
 constexpr int kPcgCoords = 9 * kPcgBlockCams;
 constexpr int kPcgThreads = kPcgCoords * kPcgSub;
 constexpr int kPcgWarps = kPcgThreads / 32;
@@ -273,13 +331,15 @@ template <bool MIXED>
 __global__ void __launch_bounds__(kPcgThreads) k_pcg_camera(DeviceBatch B) {
   typedef typename Prec<MIXED>::real real;
   typedef typename Acc<MIXED>::type Acc;
-  __shared__ double psub[kPcgSub][kPcgCoords];  // sub-lane sums of the partials
-  __shared__ double pv[kPcgCoords];             // p_k of the block, for (B + Dc^2) p
-  __shared__ real rv[kPcgCoords];               // r_{k+1} of the block, for M r
+  __shared__ Acc psub[kPcgSub][kPcgCoords];  // sub-lane sums of the partials
+  __shared__ double pv[kPcgCoords];          // p_k of the block, for (B + Dc^2) p
+  __shared__ real rv[kPcgCoords];            // r_{k+1} of the block, for M r
   __shared__ double red[kPcgWarps];
+  __shared__ DF dfred[kPcgWarps];
   __shared__ double red3[kPcgWarps][3];
   __shared__ double sc[2];
   __shared__ int flag;
+  constexpr int kLeadWarps = (kPcgCoords + 31) / 32;  // the warps holding sub-lane 0
   const int4 cb = B.camblk[blockIdx.x];  // (problem, first camera, count, 0)
   const int prob = cb.x;
   const int t = threadIdx.x, sub = t / kPcgCoords, m = t - kPcgCoords * sub;
@@ -296,7 +356,8 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg_camera(DeviceBatch B) {
   const bool live = pcg_live(L);
   const int k = L->pcg_iterations;
   const double beta = L->beta, rz_k = L->rz;
-  real arow[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0}, mrow[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  double arow[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  real mrow[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   double x = 0.0, r = 0.0, z = 0.0, p_old = 0.0, v = 0.0;
   int s0 = 0, s1 = 0;
   if (valid) {
@@ -304,7 +365,10 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg_camera(DeviceBatch B) {
     s1 = B.cam_seg_begin[c + 1];
   }
   if (lead) {
-    a_row<MIXED>(B, c, q, arow);
+    real ar[10];
+    a_row<MIXED>(B, c, q, ar);
+#pragma unroll
+    for (int kk = 0; kk < 10; ++kk) arow[kk] = (double)ar[kk];  // converted before the wait
     const real *M = reinterpret_cast<const real *>(MIXED ? (const void *)B.cam_Minvf : (const void *)B.cam_Minv) +
                     81 * (size_t)c + 9 * q;
 #pragma unroll
@@ -324,12 +388,34 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg_camera(DeviceBatch B) {
     const int n = direct ? pi.chunk_count : (pi.chunk_count + kRedGroup - 1) / kRedGroup;
     const double *cv = B.chunk_red + (direct ? pi.chunk_begin : B.nchunks + pi.chunk_begin);
     const int stride = direct ? 1 : kRedGroup;
+    // (the first kCv values per thread are loaded before the partials below,
+    // so both sets of loads are in flight together); FP64 sums in the FP64
+    // form, double-float in the mixed form
+    constexpr int kCv = 4;
+    double cvl[kCv];
+    DF cvf[kCv];
+#pragma unroll
+    for (int j = 0; j < kCv; ++j) {
+      const int e = t + j * kPcgThreads;
+      cvl[j] = 0.0, cvf[j] = df_zero();
+      if (e < n) {
+        if (MIXED)
+          cvf[j] = chunk_value_load(B, (size_t)(cv - B.chunk_red) + (size_t)e * stride);
+        else
+          cvl[j] = __ldcg(cv + (size_t)e * stride);
+      }
+    }
     double psm = 0.0;
-#pragma unroll 8
-    for (int e = t; e < n; e += kPcgThreads) psm += __ldcg(cv + (size_t)e * stride);
+    DF psf = df_zero();
+    for (int e = t + kCv * kPcgThreads; e < n; e += kPcgThreads) {
+      if (MIXED)
+        psf = df_add(psf, chunk_value_load(B, (size_t)(cv - B.chunk_red) + (size_t)e * stride));
+      else
+        psm += __ldcg(cv + (size_t)e * stride);
+    }
     // this sub-lane's share of the camera's partials (fixed order)
     if (valid) {
-      constexpr int kBatch = 32;
+      constexpr int kBatch = 16;
       const real *part = reinterpret_cast<const real *>(B.seg_partial) + q;
       Acc a;
       a.init();
@@ -344,25 +430,36 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg_camera(DeviceBatch B) {
         for (int uu = 0; uu < kBatch; ++uu)
           if (sg + uu * kPcgSub < s1) a.add(pp[uu]);
       }
-      psub[sub][m] = a.value();
+      psub[sub][m] = a;
     }
     // p.q over the CTA (fixed order); thread 0 forms alpha once
-    psm = warp_sum(psm);
-    if ((t & 31) == 0) red[t >> 5] = psm;
+    if (MIXED) {
+#pragma unroll
+      for (int j = 0; j < kCv; ++j) psf = df_add(psf, cvf[j]);
+      psf = df_warp_sum(psf);
+      if ((t & 31) == 0) dfred[t >> 5] = psf;
+    } else {
+#pragma unroll
+      for (int j = 0; j < kCv; ++j) psm += cvl[j];
+      psm = warp_sum(psm);
+      if ((t & 31) == 0) red[t >> 5] = psm;
+    }
     __syncthreads();  // also publishes psub
     if (t == 0) {
       double s2 = 0.0;
-      for (int w = 0; w < kPcgWarps; ++w) s2 += red[w];
+      if (MIXED) {
+        DF sf = dfred[0];
+        for (int w = 1; w < kPcgWarps; ++w) sf = df_add(sf, dfred[w]);
+        s2 = df_value(sf);
+      } else {
+        for (int w = 0; w < kPcgWarps; ++w) s2 += red[w];
+      }
       sc[0] = s2;
       sc[1] = rz_k * recip_nr(s2);
     }
     __syncthreads();
     pq = sc[0];
   }
-  // the next mat-vec may launch now: its early loads (the Jacobian, some 100
-  // bytes per observation) would otherwise queue in front of this kernel's
-  // latency-bound loads above
-  pdl_launch_dependents();
   const bool good = pq > 0.0 && isfinite(pq);  // else S is not positive definite along p_k
   if (live && good) {
     const double alpha = sc[1];
@@ -374,9 +471,11 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg_camera(DeviceBatch B) {
     __syncthreads();
     double rz = 0.0, rr = 0.0, qx = 0.0;
     if (lead) {
-      double psum = psub[0][m];
+      // the sub-lane sums in order (compensated in the mixed form)
+      Acc comb = psub[0][m];
 #pragma unroll
-      for (int j = 1; j < kPcgSub; ++j) psum += psub[j][m];
+      for (int j = 1; j < kPcgSub; ++j) comb.merge(psub[j][m]);
+      const double psum = comb.value();
       const double qv = a_times(arow, pv + 9 * lc, q) - psum;
       x = fma(alpha, p, x);
       r = fma(-alpha, qv, r);
@@ -392,20 +491,26 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg_camera(DeviceBatch B) {
       B.pcg_x[i] = x;
       B.pcg_r[i] = r;
       B.pcg_z[i] = z;
+      if (MIXED) B.pcg_pf[i] = (float)p, B.pcg_zf[i] = (float)z;
       rz = r * z, rr = r * r, qx = x * (v + r);
     }
-    // the block's r.z, r.r, x.(v + r): warp butterflies, then the warps in
-    // order (thread 0)
-    rz = warp_sum(rz), rr = warp_sum(rr), qx = warp_sum(qx);
-    if ((t & 31) == 0) red3[t >> 5][0] = rz, red3[t >> 5][1] = rr, red3[t >> 5][2] = qx;
+    // the block's r.z, r.r, x.(v + r): warp butterflies in the warps that
+    // hold the coordinates, then those warps in order (one value per thread)
+    if ((t >> 5) < kLeadWarps) {
+      rz = warp_sum(rz), rr = warp_sum(rr), qx = warp_sum(qx);
+      if ((t & 31) == 0) red3[t >> 5][0] = rz, red3[t >> 5][1] = rr, red3[t >> 5][2] = qx;
+    }
     __syncthreads();
-    if (t == 0) {
-      double b3[3] = {0.0, 0.0, 0.0};
-      for (int w = 0; w < kPcgWarps; ++w) b3[0] += red3[w][0], b3[1] += red3[w][1], b3[2] += red3[w][2];
-      double *o = B.blk_red + 3 * (size_t)blockIdx.x;
-      o[0] = b3[0], o[1] = b3[1], o[2] = b3[2];
+    if (t < 3) {
+      double b = 0.0;
+      for (int w = 0; w < kLeadWarps; ++w) b += red3[w][t];
+      B.blk_red[3 * (size_t)blockIdx.x + t] = b;
     }
   }
+  // the next mat-vec may launch now: its early loads (the Jacobian, some 100
+  // bytes per observation) would otherwise queue in front of this kernel's
+  // latency-bound loads and stores above
+  pdl_launch_dependents();
   if (live && last_block_done(B.prob_counter + 4 * prob + kPC_UPDATE, (uint32_t)pi.cam_block_count, &flag)) {
     // the blocks' values in block order: strided over the lanes of warp 0,
     // then a butterfly (an order fixed by the block count)

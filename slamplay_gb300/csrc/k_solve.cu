@@ -298,6 +298,7 @@ __global__ void __launch_bounds__(kSchurThreads) k_camera_schur(DeviceBatch B) {
       B.pcg_r[i] = vec[t];
       B.pcg_x[i] = 0.0;
       B.pcg_z[i] = z;  // the first direction p_0 = z_0 is formed by the PCG kernels
+      if (MIXED) B.pcg_zf[i] = (float)z;
       rz = vec[t] * z;
       rr = vec[t] * vec[t];
     }

@@ -78,6 +78,13 @@ struct KahanF {
     s = t;
   }
   __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+  // the sum in the working precision, without an FP64 round trip
+  __device__ __forceinline__ float rvalue() const { return __fsub_rn(s, c); }
+  // adds another compensated sum (its value s - c)
+  __device__ __forceinline__ void merge(const KahanF &o) {
+    add(o.s);
+    add(-o.c);
+  }
 };
 
 // Plain FP64 accumulator with the same interface.
@@ -86,7 +93,54 @@ struct SumD {
   __device__ __forceinline__ void init() { s = 0.0; }
   __device__ __forceinline__ void add(double x) { s += x; }
   __device__ __forceinline__ double value() const { return s; }
+  __device__ __forceinline__ double rvalue() const { return s; }
+  __device__ __forceinline__ void merge(const SumD &o) { s += o.s; }
 };
+
+// ---------------------------------------------------------------------------
+// Double-float arithmetic: a value is the unevaluated sum hi + lo of two
+// floats (|lo| <= ulp(hi) / 2), about 48 significant bits from FP32
+// instructions.  GB300 issues FP32 some 55 times faster than FP64, so the
+// mixed form accumulates its dot products this way and converts to FP64
+// once per block.  TwoSum is Knuth's error-free addition, TwoProd the
+// FMA-based error-free product (both exact under round-to-nearest).
+// ---------------------------------------------------------------------------
+struct DF {
+  float hi, lo;
+};
+__device__ __forceinline__ DF df_zero() { return DF{0.f, 0.f}; }
+__device__ __forceinline__ DF df_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return DF{s, e};
+}
+__device__ __forceinline__ DF df_fast_two_sum(float a, float b) {  // |a| >= |b|
+  const float s = __fadd_rn(a, b);
+  return DF{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+  const DF s = df_two_sum(a.hi, b.hi);
+  const DF t = df_two_sum(a.lo, b.lo);
+  DF u = df_fast_two_sum(s.hi, __fadd_rn(s.lo, t.hi));
+  return df_fast_two_sum(u.hi, __fadd_rn(u.lo, t.lo));
+}
+__device__ __forceinline__ DF df_prod(float a, float b) {
+  const float p = __fmul_rn(a, b);
+  return DF{p, __fmaf_rn(a, b, -p)};
+}
+__device__ __forceinline__ double df_value(DF a) { return (double)a.hi + (double)a.lo; }
+// Sum over a warp (xor butterfly, result in every lane).
+__device__ __forceinline__ DF df_warp_sum(DF v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    DF w;
+    w.hi = __shfl_xor_sync(0xffffffffu, v.hi, o);
+    w.lo = __shfl_xor_sync(0xffffffffu, v.lo, o);
+    v = df_add(v, w);
+  }
+  return v;
+}
 
 template <bool MIXED>
 struct Acc;
