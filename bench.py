@@ -277,6 +277,7 @@ def run_gpu(args) -> None:
         cb = cpu_baseline() if world == 1 else None
         extra_forms = {}
         if world == 1 and not args.no_extra_forms:
+            extra_forms["large"] = large_form()
             extra_forms["batched"] = batched_form()
             extra_forms["serving"] = serving_form()
         line = {
@@ -336,9 +337,11 @@ def batched_form(n_problems: int = 1024, repeats: int = 2, seq_sample: int = 32)
             ts.append(time.perf_counter() - t0)
         return sums, min(ts)
 
+    finals = {}
     for prec in ("mixed", "fp64"):
         with Solver(precision=prec, max_num_iterations=50, **PCG_SMALL) as s:
             sums, t = timed(s)
+            finals[prec] = [x.final_cost for x in sums]
             tune = None
             if prec == "mixed":
                 t_tune = time.perf_counter()
@@ -361,6 +364,56 @@ def batched_form(n_problems: int = 1024, repeats: int = 2, seq_sample: int = 32)
     out["sequential_fp64"] = {"solves_per_s": seq_sample / dt, "lm_iters_per_s": its / dt,
                               "sample": f"first {seq_sample} problems, one gba_solve each"}
     out["mixed_batched_vs_sequential_fp64_solves"] = out["mixed"]["solves_per_s"] / out["sequential_fp64"]["solves_per_s"]
+    # accuracy of the mixed form: each problem's final cost against its FP64
+    # solve (both run to their convergence test)
+    rel = [abs(a - b) / b for a, b in zip(finals["mixed"], finals["fp64"]) if b > 0]
+    rel.sort()
+    out["mixed_vs_fp64_final_cost_rel"] = {"max": rel[-1], "median": rel[len(rel) // 2],
+                                          "p99": rel[int(0.99 * (len(rel) - 1))],
+                                          "within_1e-6": sum(1 for r in rel if r <= 1e-6), "problems": len(rel)}
+    return out
+
+
+def large_form(lm_iterations: int = 10) -> dict:
+    """Configuration 2: one large problem (1,800 cameras in six loops, 1.0M
+    points, views per point 1 + Zipf(1.5) truncated to 2-40: ~5.8M
+    observations), mixed and FP64, the first `lm_iterations` LM iterations
+    (tolerances off, PCG as in configuration 1).  Reports LM iterations/s and
+    each kernel's achieved bandwidth at a size where launch latency no longer
+    dominates (the Jacobian alone is 0.6 GB in the mixed form)."""
+    from slamplay_gb300 import BALProblem, Solver
+
+    b = BALProblem.synthetic(2, seed=0)
+    peak = measured_peaks().get("hbm_gbs", 6800.0)
+    out = {"workload": f"config2: {b.num_cameras()} cameras, {b.num_points()} points, {b.num_observations()} obs, "
+                       f"first {lm_iterations} LM iterations, PCG residual 1e-6 <= 100"}
+    finals = {}
+    for prec in ("mixed", "fp64"):
+        opts = dict(max_num_iterations=lm_iterations, function_tolerance=0.0, gradient_tolerance=0.0,
+                    parameter_tolerance=0.0, precision=prec, **PCG_SMALL)
+        with Solver(**opts) as s:
+            first = s.solve(b.copy())
+            s.synchronize()
+            t0 = time.perf_counter()
+            s.solve_resident(1)
+            s.synchronize()
+            dt = time.perf_counter() - t0
+            s.set_profiling(True)
+            s.solve(b.copy())
+            s.set_profiling(False)
+            prof = [e for e in s.profile() if e["launches"] > 0]
+        kern = {}
+        for e in prof:
+            avg = e["total_ms"] / e["launches"]
+            gbs = e["bytes"] / e["launches"] / (avg * 1e-3) / 1e9 if avg > 0 else 0.0
+            kern[e["name"]] = {"launches": e["launches"], "avg_us": 1e3 * avg, "gbs": gbs, "frac": gbs / peak,
+                               "share": e["total_ms"] / sum(x["total_ms"] for x in prof)}
+        finals[prec] = first.final_cost
+        out[prec] = {"lm_iters_per_s": first.num_iterations / dt, "s_per_solve": dt,
+                     "lm_iterations": first.num_iterations, "pcg_iterations": first.num_linear_solver_iterations,
+                     "final_cost": first.final_cost, "kernels": kern}
+    out["peak_gbs"] = peak
+    out["mixed_vs_fp64_lm_iters"] = out["mixed"]["lm_iters_per_s"] / out["fp64"]["lm_iters_per_s"]
     return out
 
 
@@ -421,14 +474,18 @@ def serving_form(n_requests: int = 48, rate_mults=(2.0, 5.0, 10.0), seq_sample: 
 
 
 def run_profile_solve(args) -> None:
-    """One solve of the workload with the host driving the loops (every
-    kernel a plain stream launch, as ncu needs: it cannot profile kernels of
-    a graph with conditional nodes).  No event timing: ncu times the
-    kernels itself."""
+    """One solve of the workload (or of configuration 0 / 2, for a bounded
+    number of LM iterations) with the host driving the loops (every kernel a
+    plain stream launch, as ncu needs: it cannot profile kernels of a graph
+    with conditional nodes).  No event timing: ncu times the kernels
+    itself."""
     from slamplay_gb300 import BALProblem, Solver
 
-    problem = BALProblem.synthetic(1, seed=0)
-    with Solver(use_graphs=0, **workload_options(args.precision)) as s:
+    problem = BALProblem.synthetic(args.config, seed=0)
+    opts = workload_options(args.precision)
+    if args.lm_iterations:
+        opts["max_num_iterations"] = args.lm_iterations
+    with Solver(use_graphs=0, **opts) as s:
         sm = s.solve(problem.copy())
     print(json.dumps({"precision": args.precision, "lm_iterations": sm.num_iterations,
                       "pcg_iterations": sm.num_linear_solver_iterations, "final_cost": sm.final_cost}), flush=True)
@@ -443,6 +500,10 @@ def main():
     ap.add_argument("--profile-solve", action="store_true",
                     help="one host-driven solve with per-kernel event timing (the command profiled with ncu)")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--config", type=int, default=1, choices=[0, 1, 2],
+                    help="with --profile-solve: the synthetic configuration to solve")
+    ap.add_argument("--lm-iterations", type=int, default=0,
+                    help="with --profile-solve: LM iterations (0 = the workload's 50)")
     ap.add_argument("--no-extra-forms", action="store_true",
                     help="skip the batched (configuration 3) and serving (configuration 4) forms")
     args = ap.parse_args()

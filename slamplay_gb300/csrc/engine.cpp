@@ -366,17 +366,22 @@ void Engine::prof_end(cudaStream_t s, int entry, double bytes) {
 // must read and write at least once; cached gathers counted once per
 // distinct item).  Used for the achieved-bandwidth figures.
 static double bytes_matvec(const DeviceBatch &b) {
-  // J_c, J_p (12 pairs) + slot / segment / point indices per observation;
-  // C^-1 + CSR per point; per segment its camera's direction, position,
-  // slot and partial; per chunk its record
+  // J_c, J_p (12 pairs) + segment / slot / point indices per observation;
+  // C^-1 + CSR per point; per segment its position, slot, camera and the
+  // camera's first-segment index, the camera's z and p_{k-1} (working
+  // precision) and its partial out; per camera the B + Dc^2 row of the
+  // chunk that owns it; per chunk its record and its value of p.q
   const double rs = b.opt.mixed ? 4.0 : 8.0;
   return (double)b.no * (24.0 * rs + 8.0) + (double)b.np * (4.0 + 6.0 * rs) +
-         (double)b.nseg * (2.0 + 4.0 + 4.0 + 18.0 * rs) + (double)b.nchunks * 32.0;
+         (double)b.nseg * (14.0 + 27.0 * rs) + (double)b.nc * 90.0 * rs + (double)b.nchunks * 40.0;
 }
 static double bytes_pcg_camera(const DeviceBatch &b) {
-  // partials read once; per camera p, q, x, r, z, v (FP64), B, M^-1, D^2
+  // partials and chunk values read once; per camera x, r, z, v, p in and
+  // x, r, z, p out (FP64; FP32 copies of z and p in the mixed form), the
+  // rows of B and M^-1, Dc^2 and the segment range
   const double rs = b.opt.mixed ? 4.0 : 8.0;
-  return (double)b.nseg * 9.0 * rs + (double)b.nc * (8.0 * 9.0 * 12.0 + (45.0 + 81.0) * rs + 72.0);
+  return (double)b.nseg * 9.0 * rs + (double)b.nchunks * 8.0 +
+         (double)b.nc * (9.0 * 8.0 * 9.0 + (b.opt.mixed ? 72.0 : 0.0) + (45.0 + 81.0) * rs + 72.0 + 8.0);
 }
 static double bytes_eval(const DeviceBatch &b) {
   const double rs = b.opt.mixed ? 4.0 : 8.0;

@@ -268,12 +268,12 @@ __global__ void __launch_bounds__(kChunkCap) k_eval_chunk(DeviceBatch B) {
         }
       }
       if (NORMS) {
-        B.pt_colnorm[3 * (size_t)jj + 0] = acc[0].value();
-        B.pt_colnorm[3 * (size_t)jj + 1] = acc[3].value();
-        B.pt_colnorm[3 * (size_t)jj + 2] = acc[5].value();
+        B.pt_colnorm[3 * (size_t)jj + 0] = (double)acc[0].rvalue();
+        B.pt_colnorm[3 * (size_t)jj + 1] = (double)acc[3].rvalue();
+        B.pt_colnorm[3 * (size_t)jj + 2] = (double)acc[5].rvalue();
       } else {
 #pragma unroll
-        for (int q = 0; q < 6; ++q) B.pt_C[6 * (size_t)jj + q] = acc[q].value();
+        for (int q = 0; q < 6; ++q) B.pt_C[6 * (size_t)jj + q] = (double)acc[q].rvalue();
         if (B.pt_used[jj]) {
           const double *x = B.pt_param[parity] + 4 * (size_t)jj;
 #pragma unroll
@@ -318,6 +318,7 @@ __global__ void __launch_bounds__(kCamThreads) k_eval_camera(DeviceBatch B) {
   typedef typename Acc<MIXED>::type Acc;
   constexpr int NV = NORMS ? 9 : 54;
   __shared__ double part[kCamThreads / 32][NV];
+  __shared__ DF partf[MIXED ? kCamThreads / 32 : 1][NV];
   const int c = blockIdx.x;
   const LMState *L = B.lm + B.cam_problem[c];
   if (!L->active || !L->need_jacobian) return;
@@ -347,12 +348,29 @@ __global__ void __launch_bounds__(kCamThreads) k_eval_camera(DeviceBatch B) {
       }
     }
   }
+  // warp sums: FP64 in the FP64 form; double-float in the mixed form (FP32
+  // instructions: 54 FP64 reductions in every warp would occupy GB300's FP64
+  // pipe for microseconds), converted once per value below
+  if (MIXED) {
 #pragma unroll
-  for (int q = 0; q < NV; ++q) {
-    const double v = warp_sum(acc[q].value());
-    if (lane == 0) part[warp][q] = v;
+    for (int q = 0; q < NV; ++q) {
+      const KahanF &kq = reinterpret_cast<const KahanF &>(acc[q]);
+      const DF v = df_warp_sum(df_fast_two_sum(kq.s, -kq.c));
+      if (lane == 0) partf[warp][q] = v;
+    }
+  } else {
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+      const double v = warp_sum(acc[q].value());
+      if (lane == 0) part[warp][q] = v;
+    }
   }
   __syncthreads();
+  if (MIXED && t < NV) {
+    DF v = partf[0][t];
+    for (int w = 1; w < kCamThreads / 32; ++w) v = df_add(v, partf[w][t]);
+    part[0][t] = df_value(v);  // read back below by this thread only
+  }
   if (t < NV) {
     double s = 0.0;
     if (MIXED && !NORMS && t >= 45) {
@@ -369,6 +387,8 @@ __global__ void __launch_bounds__(kCamThreads) k_eval_camera(DeviceBatch B) {
         for (int u = 0; u < 16; ++u) a4[u % 4] += v[u];
       }
       s = (a4[0] + a4[1]) + (a4[2] + a4[3]);
+    } else if (MIXED) {
+      s = part[0][t];
     } else {
       for (int w = 0; w < kCamThreads / 32; ++w) s += part[w][t];
     }

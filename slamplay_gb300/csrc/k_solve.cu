@@ -170,7 +170,7 @@ __global__ void __launch_bounds__(kChunkCap) k_point_schur(DeviceBatch B) {
         const int a = en - 45;
         for (int k = b0; k < b1; ++k) acc.add(sm.jc[k][2 * a] * sm.ae[k][3] + sm.jc[k][2 * a + 1] * sm.ae[k][4]);
       }
-      part[54 * (size_t)sl + en] = (real)acc.value();
+      part[54 * (size_t)sl + en] = (real)acc.rvalue();
     }
     __syncthreads();
   }

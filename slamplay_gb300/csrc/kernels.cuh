@@ -207,12 +207,14 @@ __device__ __forceinline__ double block_max(double v, double *red) {
 __device__ __forceinline__ double block_range_sum(const double *a, int begin, int end, int stride,
                                                   double *red) {
   double s = 0.0;
+#pragma unroll 8
   for (int i = begin + threadIdx.x; i < end; i += blockDim.x) s += __ldcg(a + (size_t)i * stride);
   return block_sum(s, red);
 }
 __device__ __forceinline__ double block_range_max(const double *a, int begin, int end, int stride,
                                                   double *red) {
   double s = 0.0;
+#pragma unroll 8
   for (int i = begin + threadIdx.x; i < end; i += blockDim.x) s = fmax(s, __ldcg(a + (size_t)i * stride));
   return block_max(s, red);
 }
