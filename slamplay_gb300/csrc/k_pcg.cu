@@ -73,6 +73,13 @@ __device__ __forceinline__ bool pcg_live(const LMState *L) { return L->active !=
 __device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
+// Explicit multiply-adds (no contraction left to the compiler), so the two
+// mixed-form mat-vec kernels below compute bitwise the same values.
+__device__ __forceinline__ float mad(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double mad(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+
 // p_k of one coordinate (both kernels evaluate exactly this expression).
 __device__ __forceinline__ double pcg_direction(int k, double beta, double z, double p_old) {
   return k == 0 ? z : fma(beta, p_old, z);
@@ -228,11 +235,11 @@ __global__ void __launch_bounds__(kChunkCap, MIXED ? 4 : 2) k_schur_matvec(Devic
 #pragma unroll
     for (int q = 0; q < 9; ++q) {
       const real x = sm.pseg[s][q];
-      zu += Jc[q].x * x;
-      zv += Jc[q].y * x;
+      zu = mad(Jc[q].x, x, zu);
+      zv = mad(Jc[q].y, x, zv);
     }
 #pragma unroll
-    for (int q = 0; q < 3; ++q) sm.U[t][q] = Jp[q].x * zu + Jp[q].y * zv;
+    for (int q = 0; q < 3; ++q) sm.U[t][q] = mad(Jp[q].x, zu, mul(Jp[q].y, zv));
   }
   __syncthreads();
   if (t < ci.pt_count) {
@@ -244,17 +251,17 @@ __global__ void __launch_bounds__(kChunkCap, MIXED ? 4 : 2) k_schur_matvec(Devic
       y2.add(sm.U[kk][2]);
     }
     const real w0 = (real)y0.rvalue(), w1 = (real)y1.rvalue(), w2 = (real)y2.rvalue();
-    sm.tpt[t][0] = ci6[0] * w0 + ci6[1] * w1 + ci6[2] * w2;
-    sm.tpt[t][1] = ci6[1] * w0 + ci6[3] * w1 + ci6[4] * w2;
-    sm.tpt[t][2] = ci6[2] * w0 + ci6[4] * w1 + ci6[5] * w2;
+    sm.tpt[t][0] = mad(ci6[0], w0, mad(ci6[1], w1, mul(ci6[2], w2)));
+    sm.tpt[t][1] = mad(ci6[1], w0, mad(ci6[3], w1, mul(ci6[4], w2)));
+    sm.tpt[t][2] = mad(ci6[2], w0, mad(ci6[4], w1, mul(ci6[5], w2)));
   }
   __syncthreads();
   if (valid) {
     const real t0 = sm.tpt[lp][0], t1 = sm.tpt[lp][1], t2 = sm.tpt[lp][2];
-    const real eu = Jp[0].x * t0 + Jp[1].x * t1 + Jp[2].x * t2;
-    const real ev = Jp[0].y * t0 + Jp[1].y * t1 + Jp[2].y * t2;
+    const real eu = mad(Jp[0].x, t0, mad(Jp[1].x, t1, mul(Jp[2].x, t2)));
+    const real ev = mad(Jp[0].y, t0, mad(Jp[1].y, t1, mul(Jp[2].y, t2)));
 #pragma unroll
-    for (int q = 0; q < 9; ++q) sm.U[slot][q] = Jc[q].x * eu + Jc[q].y * ev;
+    for (int q = 0; q < 9; ++q) sm.U[slot][q] = mad(Jc[q].x, eu, mul(Jc[q].y, ev));
   }
   __syncthreads();
   real *part = reinterpret_cast<real *>(B.seg_partial);
@@ -313,6 +320,151 @@ __global__ void __launch_bounds__(kChunkCap, MIXED ? 4 : 2) k_schur_matvec(Devic
       gd = __ldcg(B.chunk_red + g0 + t);
   }
   chunk_value_store<MIXED>(B, B.nchunks + g0, gd, gf, dfred, red);
+}
+
+// ---------------------------------------------------------------------------
+// K4a, mixed form, lean: the same arithmetic as k_schur_matvec<true>, but
+// the Jacobian is loaded after the wait (it stays in L2 between PCG
+// iterations) and read again for the second product instead of being held
+// in registers, so a thread needs few registers and up to kLeanCtas CTAs fit
+// per SM, and a CTA whose problem's PCG has ended loads nothing at all
+// (batches: the loop runs until the slowest problem's PCG ends).
+constexpr int kLeanCtas = 8;
+
+__global__ void __launch_bounds__(kChunkCap, kLeanCtas) k_schur_matvec_lean(DeviceBatch B) {
+  __shared__ float pseg[kChunkCap][9];  // p of the chunk's cameras
+  __shared__ float U[kChunkCap][9];     // first holds w (3 per obs), then u (9 per slot)
+  __shared__ float tpt[kChunkCap][3];
+  __shared__ double red[kChunkCap / 32];
+  __shared__ DF dfred[kChunkCap / 32];
+  __shared__ int flag;
+  const int t = threadIdx.x;
+  const int ch = blockIdx.x;
+  const ChunkInfo ci = B.chunk[ch];
+  const bool valid = t < ci.obs_count;
+  // the first task's segment (fixed during the PCG)
+  int f_b0 = 0, f_b1 = 0, f_slot = 0;
+  size_t f_idx = 0;
+  bool f_owner = false;
+  if (t < ci.seg_count * 9) {
+    const int sg = t / 9;
+    f_b0 = B.seg_pos[ci.seg_begin + sg];
+    f_b1 = (sg + 1 < ci.seg_count) ? B.seg_pos[ci.seg_begin + sg + 1] : ci.obs_count;
+    f_slot = B.seg_slot[ci.seg_begin + sg];
+    const int cam = B.seg_cam[ci.seg_begin + sg];
+    f_idx = 9 * (size_t)cam + (t - 9 * sg);
+    f_owner = f_slot == B.cam_seg_begin[cam];
+  }
+  pdl_wait();
+  pdl_launch_dependents();
+  const LMState *L = B.lm + ci.problem;
+  float f_z = 0.f, f_p = 0.f;
+  if (t < ci.seg_count * 9) f_z = B.pcg_zf[f_idx], f_p = B.pcg_pf[f_idx];
+  if (!pcg_live(L)) return;  // uniform over the problem's CTAs
+  const int k = L->pcg_iterations;
+  const float beta = (float)L->beta;
+  for (int i = t; i < ci.seg_count * 9; i += blockDim.x) {
+    const int sg = i / 9, q = i - 9 * sg;
+    float z = f_z, po = f_p;
+    if (i != t) {
+      const size_t idx = 9 * (size_t)B.seg_cam[ci.seg_begin + sg] + q;
+      z = B.pcg_zf[idx], po = B.pcg_pf[idx];
+    }
+    pseg[sg][q] = k == 0 ? z : __fmaf_rn(beta, po, z);
+  }
+  const float2 *jac = reinterpret_cast<const float2 *>(B.jac);
+  const size_t o = (size_t)ci.obs_begin + t;
+  int slot = 0, lp = 0;
+  __syncthreads();
+  if (valid) {
+    const int s = B.obs_seg[o];
+    slot = B.obs_slot[o];
+    lp = B.obs_pt[o] - ci.pt_begin;
+    float zu = 0.f, zv = 0.f;
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+      const float2 J = jac[(size_t)q * B.no + o];
+      const float x = pseg[s][q];
+      zu = mad(J.x, x, zu);
+      zv = mad(J.y, x, zv);
+    }
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      const float2 J = jac[(size_t)(9 + q) * B.no + o];
+      U[t][q] = mad(J.x, zu, mul(J.y, zv));
+    }
+  }
+  // the first task's (B + Dc^2) row, loaded now and used at the end
+  float arow[10];
+  if (f_owner) a_row<true>(B, (int)(f_idx / 9), (int)(f_idx % 9), arow);
+  __syncthreads();
+  if (t < ci.pt_count) {
+    const int jj = ci.pt_begin + t;
+    const int pb0 = B.pt_obs_begin[jj] - ci.obs_begin, pb1 = B.pt_obs_begin[jj + 1] - ci.obs_begin;
+    const float *c6 = reinterpret_cast<const float *>(B.pt_Cinv) + 6 * (size_t)jj;
+    KahanF y0, y1, y2;
+    y0.init(), y1.init(), y2.init();
+    for (int kk = pb0; kk < pb1; ++kk) {
+      y0.add(U[kk][0]);
+      y1.add(U[kk][1]);
+      y2.add(U[kk][2]);
+    }
+    const float w0 = y0.rvalue(), w1 = y1.rvalue(), w2 = y2.rvalue();
+    tpt[t][0] = mad(c6[0], w0, mad(c6[1], w1, mul(c6[2], w2)));
+    tpt[t][1] = mad(c6[1], w0, mad(c6[3], w1, mul(c6[4], w2)));
+    tpt[t][2] = mad(c6[2], w0, mad(c6[4], w1, mul(c6[5], w2)));
+  }
+  __syncthreads();
+  if (valid) {
+    const float t0 = tpt[lp][0], t1 = tpt[lp][1], t2 = tpt[lp][2];
+    const float2 P0 = jac[(size_t)9 * B.no + o], P1 = jac[(size_t)10 * B.no + o], P2 = jac[(size_t)11 * B.no + o];
+    const float eu = mad(P0.x, t0, mad(P1.x, t1, mul(P2.x, t2)));
+    const float ev = mad(P0.y, t0, mad(P1.y, t1, mul(P2.y, t2)));
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+      const float2 J = jac[(size_t)q * B.no + o];
+      U[slot][q] = mad(J.x, eu, mul(J.y, ev));
+    }
+  }
+  __syncthreads();
+  float *part = reinterpret_cast<float *>(B.seg_partial);
+  DF dotf = df_zero();
+  for (int i = t; i < ci.seg_count * 9; i += blockDim.x) {
+    const int sg = i / 9, q = i - 9 * sg;
+    int b0 = f_b0, b1 = f_b1, slot9 = f_slot;
+    bool owner = f_owner;
+    if (i != t) {  // a chunk of more than kChunkCap / 9 segments: metadata now
+      b0 = B.seg_pos[ci.seg_begin + sg];
+      b1 = (sg + 1 < ci.seg_count) ? B.seg_pos[ci.seg_begin + sg + 1] : ci.obs_count;
+      slot9 = B.seg_slot[ci.seg_begin + sg];
+      const int cam = B.seg_cam[ci.seg_begin + sg];
+      owner = slot9 == B.cam_seg_begin[cam];
+      if (owner) a_row<true>(B, cam, q, arow);
+    }
+    KahanF a;
+    a.init();
+    for (int kk = b0; kk < b1; ++kk) a.add(U[kk][q]);
+    const float pv = a.rvalue();
+    part[9 * (size_t)slot9 + q] = pv;
+    const float *ps = pseg[sg];
+    dotf = df_add(dotf, df_prod(-ps[q], pv));
+    if (owner) {  // the camera's (B + Dc^2) term
+      float ap = __fmul_rn(arow[9], ps[q]);
+#pragma unroll
+      for (int kk = 0; kk < 9; ++kk) ap = __fmaf_rn(arow[kk], ps[kk], ap);
+      dotf = df_add(dotf, df_prod(ps[q], ap));
+    }
+  }
+  chunk_value_store<true>(B, ch, 0.0, dotf, dfred, red);
+  const ProblemInfo pi = B.prob[ci.problem];
+  if (pi.chunk_count <= kRedDirect) return;  // the camera kernel sums the chunk values itself
+  const int rel = ch - pi.chunk_begin;
+  const int g0 = pi.chunk_begin + (rel / kRedGroup) * kRedGroup;
+  const int gn = min(kRedGroup, pi.chunk_begin + pi.chunk_count - g0);
+  if (!last_block_done(B.chunk_counter + g0, (uint32_t)gn, &flag)) return;
+  DF gf = df_zero();
+  if (t < gn) gf = chunk_value_load(B, g0 + t);
+  chunk_value_store<true>(B, B.nchunks + g0, 0.0, gf, dfred, red);
 }
 
 // ---------------------------------------------------------------------------
@@ -586,13 +738,18 @@ cudaError_t launch_schur_matvec(const DeviceBatch &b, bool mixed, cudaStream_t s
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)b.nchunks);
   cfg.blockDim = dim3(kChunkCap);
-  cfg.dynamicSmemBytes = mixed ? sizeof(MatvecSmem<true>) : sizeof(MatvecSmem<false>);
+  cfg.dynamicSmemBytes = (mixed && b.num_problems > 1) ? 0 : (mixed ? sizeof(MatvecSmem<true>) : sizeof(MatvecSmem<false>));
   cfg.stream = s;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
   cfg.numAttrs = pdl ? 1 : 0;
+  // mixed form: a batch runs the lean kernel (chunks of problems whose PCG
+  // has ended cost it nothing; the other kernel loads their Jacobian before
+  // it can see that), a single problem the register-prefetching one; both
+  // compute bitwise the same values
+  if (mixed && b.num_problems > 1) return cudaLaunchKernelEx(&cfg, k_schur_matvec_lean, b);
   if (mixed) return cudaLaunchKernelEx(&cfg, k_schur_matvec<true>, b);
   return cudaLaunchKernelEx(&cfg, k_schur_matvec<false>, b);
 }

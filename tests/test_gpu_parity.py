@@ -136,10 +136,14 @@ def test_solve_is_deterministic_and_graph_equals_host_loop():
         assert o[1] == outs[0][1] and o[2] == outs[0][2]
 
 
-def test_batch_equals_alone_bitwise():
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_batch_equals_alone_bitwise(precision):
+    # a problem's arithmetic depends only on itself: the same bits alone and
+    # in a batch (the mixed form's batch and single-problem mat-vec kernels
+    # differ in how they load, not in what they compute)
     probs = [BALProblem.synthetic(3, index=i, seed=2) for i in range(4)]
     alone = []
-    with Solver(max_num_iterations=8, **FIXED) as s:
+    with Solver(max_num_iterations=8, precision=precision, **FIXED) as s:
         for p in probs:
             q = p.copy()
             sm = s.solve(q)
