@@ -189,13 +189,12 @@ def test_invalid_inputs_raise():
 
 @pytest.mark.parametrize("crit", ["residual", "quadratic_model"])
 def test_many_camera_problem_matches_oracle_pcg(crit):
-    """700 cameras: more than one camera per warp of the largest PCG cluster
-    (16 CTAs x 32 warps), so the camera loops and the cluster reductions run
-    over several cameras per warp.  FP64 against the oracle's PCG Schur
-    solver with the same criterion; relative cost difference <= 1e-9 with
-    the residual criterion at 1e-12, <= 1e-8 with the quadratic-model
-    criterion at eta 1e-6 (a rounding-level change of where the model test
-    stops may move one PCG iteration)."""
+    """700 cameras: 88 blocks of the camera-side PCG kernel, whose last block
+    decides for the problem.  FP64 against the oracle's PCG Schur solver with
+    the same criterion; relative cost difference <= 1e-9 with the residual
+    criterion at 1e-12, <= 1e-8 with the quadratic-model criterion at eta
+    1e-6 (a rounding-level change of where the model test stops may move one
+    PCG iteration)."""
     b = BALProblem.synthetic(0, seed=21, num_cameras=700, num_points=6000)
     opts = dict(max_num_iterations=6, pcg_criterion=crit, **FIXED)
     tol = dict(pcg_tolerance=1e-12, max_linear_solver_iterations=1000) if crit == "residual" else dict(eta=1e-6)
@@ -208,6 +207,27 @@ def test_many_camera_problem_matches_oracle_pcg(crit):
         sh = s.solve(h)
     assert np.array_equal(h.parameters(), g.parameters())
     assert sh.num_linear_solver_iterations == sg.num_linear_solver_iterations
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_large_problem_reduction_path(precision):
+    """More than 2,048 chunks: the mat-vec first sums its p.q values in groups
+    of 64 chunks (the group's last CTA) and the camera kernel reads the group
+    sums.  The same problem in chunks of at most 32 observations (~4,000
+    chunks: the group path) and of 256 (~550 chunks: the direct path) is the
+    same solve up to the order of the sums: final costs within 1e-9 (FP64)
+    or 1e-6 (mixed) of each other, and of the FP64 oracle."""
+    b = BALProblem.synthetic(0, seed=5, num_points=20000)
+    opts = dict(max_num_iterations=6, pcg_tolerance=1e-10, max_linear_solver_iterations=300,
+                precision=precision, **FIXED)
+    with Solver(chunk_observations=32, **opts) as s:
+        grouped = s.solve(b.copy())
+    with Solver(**opts) as s:
+        direct = s.solve(b.copy())
+    so = O.solve(O.Problem.from_bal(b), max_num_iterations=6, linear_solver="dense_schur", **FIXED)
+    tol = 1e-9 if precision == "fp64" else 1e-6
+    assert abs(grouped.final_cost - direct.final_cost) <= tol * direct.final_cost
+    assert abs(grouped.final_cost - so["final_cost"]) <= tol * so["final_cost"], (grouped.final_cost, so["final_cost"])
 
 
 @pytest.mark.parametrize("loss", ["trivial", "huber"])
