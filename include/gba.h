@@ -89,6 +89,16 @@ typedef enum gba_pcg_criterion {
   GBA_PCG_QUADRATIC_MODEL = 1  /* Ceres ITERATIVE_SCHUR's eta (Nash-Sofer) test    */
 } gba_pcg_criterion;
 
+/* How the PCG applies the reduced camera matrix S = B + D^2 - W C^-1 W^T
+ * (Ceres' Solver::Options::use_explicit_schur_complement). */
+typedef enum gba_schur {
+  GBA_SCHUR_AUTO = 0,     /* explicit when the co-visible observation pairs are
+                             at most 16 per observation, else implicit          */
+  GBA_SCHUR_IMPLICIT = 1, /* every PCG iteration applies J: no S is formed      */
+  GBA_SCHUR_EXPLICIT = 2  /* the camera-camera blocks of S are formed once per LM
+                             iteration; each PCG iteration multiplies by them    */
+} gba_schur;
+
 /* ------------------------------------------------------------------------ */
 /* Options.  Defaults (gba_options_init) are Ceres 2.2's Solver::Options     */
 /* defaults for the fields the reference leaves unset                        */
@@ -125,7 +135,8 @@ typedef struct gba_options {
   int32_t pcg_unroll;                 /* PCG iterations per graph body, 0 = auto (2) */
   int32_t autotune;                   /* 1 = run gba_autotune on the first solve of a
                                          new problem-size bucket                     */
-  int32_t reserved[6];
+  int32_t schur;                      /* gba_schur, GBA_SCHUR_AUTO                   */
+  int32_t reserved[5];
 } gba_options;
 
 /* Per-solve report, the subset of ceres::Solver::Summary the reference

@@ -76,6 +76,7 @@ void gba_options_init(gba_options *o) {
   o->use_graphs = 1;
   o->pcg_unroll = 0;
   o->autotune = 0;
+  o->schur = GBA_SCHUR_AUTO;
 }
 
 const char *gba_version(void) { return "gba 1 sm_103a"; }
@@ -94,7 +95,8 @@ gba_status gba_create(const gba_options *o, gba_handle **out) {
     gba_options_init(&opt);
   }
   if (opt.max_num_iterations < 0 || opt.max_linear_solver_iterations < 0 || opt.loss < 0 || opt.loss > 2 ||
-      opt.precision < 0 || opt.precision > 1 || !(opt.initial_trust_region_radius > 0) ||
+      opt.precision < 0 || opt.precision > 1 || opt.schur < 0 || opt.schur > 2 ||
+      !(opt.initial_trust_region_radius > 0) ||
       !(opt.loss_scale > 0) || opt.max_num_consecutive_invalid_steps < 1) {
     g_create_error = "invalid solver options";
     return GBA_ERR_INVALID_ARGUMENT;
@@ -223,7 +225,7 @@ gba_status gba_profile_entry(const gba_handle *h, int32_t i, const char **name, 
 }
 
 size_t gba_estimate_footprint(int32_t nc, int32_t np, int32_t no, int32_t precision) {
-  return gba::Server::estimate_footprint(nc, np, no, precision == GBA_PRECISION_MIXED);
+  return gba::Server::estimate_footprint(nc, np, no, precision == GBA_PRECISION_MIXED, true);
 }
 
 gba_status gba_server_start(gba_handle *h, size_t budget, int32_t max_live, int32_t max_queue) {

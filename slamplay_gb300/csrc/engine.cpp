@@ -44,11 +44,12 @@ enum ProfSlot {
   PF_DECIDE,
   PF_TABLE,
   PF_SETUP_MISC,
+  PF_FORM,
   PF_COUNT
 };
 const char *kProfNames[PF_COUNT] = {"eval_jacobian",  "post_eval", "point_schur",  "camera_schur",
                                     "schur_matvec",   "pcg_camera", "back_substitute", "candidate_cost",
-                                    "decide",         "camera_table", "setup_misc"};
+                                    "decide",         "camera_table", "setup_misc", "schur_form"};
 
 double now_s() {
   return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
@@ -123,6 +124,7 @@ PrepOptions Engine::prep_options() const {
   PrepOptions po;
   po.reorder_points = o_.reorder_points != 0;
   if (o_.chunk_observations > 0) po.chunk_cap = std::max(32, std::min(kChunkCap, (int)o_.chunk_observations));
+  po.schur = o_.schur;
   return po;
 }
 
@@ -171,6 +173,18 @@ size_t Engine::layout(const HostBatch &hb, char *base, DeviceBatch *db, size_t *
   b.camblk = cv.take<int4>(nb);
   b.cam_init = cv.take<double>(9 * nc);
   b.pt_init = cv.take<double>(4 * np);
+  const bool ex = hb.explicit_schur;
+  const size_t nsb = ex ? (size_t)hb.nblk : 0, nup = ex ? (size_t)hb.nup : 0;
+  b.explicit_schur = ex ? 1 : 0;
+  b.nblk = (int32_t)nsb;
+  b.nup = (int32_t)nup;
+  b.npairs = ex ? hb.npairs : 0;
+  b.sblk_row = cv.take<int32_t>(ex ? nc + 1 : 0);
+  b.sblk_col = cv.take<int32_t>(nsb);
+  b.sblk_tr = cv.take<int32_t>(nsb);
+  b.sblk_up = cv.take<int32_t>(nup);
+  b.sblk_pair = cv.take<int32_t>(ex ? nup + 1 : 0);
+  b.spair = cv.take<int2>(ex ? (size_t)hb.npairs : 0);
   *upload_bytes = align_up(cv.off, 256);
   // download
   cv.off = *upload_bytes;
@@ -228,6 +242,11 @@ size_t Engine::layout(const HostBatch &hb, char *base, DeviceBatch *db, size_t *
   b.cam_scal = cv.take<double>(kCamScal * nc);
   b.chunk_red = cv.take<double>(2 * nch);
   b.blk_red = cv.take<double>(3 * nb);
+  b.obs_F = cv.take<char>(ex ? (size_t)kObsF * no * rs : 0);
+  b.sblk_val = cv.take<char>(81 * nsb * rs);
+  b.cam_Sii = cv.take<char>(ex ? 81 * nc * rs : 0);
+  b.pcg_q = cv.take<double>(ex ? 9 * nc : 0);
+  b.spmv_red = cv.take<double>(ex ? nc : 0);
   b.prob_counter = cv.take<uint32_t>(4 * P);
   b.global_counter = cv.take<uint32_t>(8);
   b.chunk_counter = cv.take<uint32_t>(nch);
@@ -322,6 +341,15 @@ gba_status Engine::upload(const HostBatch &hb, std::string *err) {
   put(const_cast<int32_t *>(hdb.cam_obs_begin), hb.cam_obs_begin);
   put(const_cast<int32_t *>(hdb.cam_obs_list), hb.cam_obs_list);
   put(const_cast<int4 *>(hdb.camblk), hb.camblk);
+  if (hb.explicit_schur) {
+    put(const_cast<int32_t *>(hdb.sblk_row), hb.sblk_row);
+    put(const_cast<int32_t *>(hdb.sblk_col), hb.sblk_col);
+    put(const_cast<int32_t *>(hdb.sblk_tr), hb.sblk_tr);
+    put(const_cast<int32_t *>(hdb.sblk_up), hb.sblk_up);
+    put(const_cast<int32_t *>(hdb.sblk_pair), hb.sblk_pair);
+    if (!hb.spair.empty())
+      std::memcpy(const_cast<int2 *>(hdb.spair), hb.spair.data(), hb.spair.size() * sizeof(int32_t));
+  }
   put(const_cast<double *>(hdb.cam_init), hb.cam_param);
   put(const_cast<double *>(hdb.pt_init), hb.pt_param);
   if ((st = check(cudaMemcpyAsync(d_arena_, h_stage_, upload_bytes_, cudaMemcpyHostToDevice, stream_),
@@ -365,7 +393,14 @@ void Engine::prof_end(cudaStream_t s, int entry, double bytes) {
 // Algorithmic bytes of one launch of the main kernels (what the kernel
 // must read and write at least once; cached gathers counted once per
 // distinct item).  Used for the achieved-bandwidth figures.
+static double bytes_spmv(const DeviceBatch &b) {
+  // the blocks' values and columns, the diagonal blocks, z and p_{k-1} of
+  // every camera (working precision), S p and the p.q shares out (FP64)
+  const double rs = b.opt.mixed ? 4.0 : 8.0;
+  return (double)b.nblk * (81.0 * rs + 4.0) + (double)b.nc * (81.0 * rs + 18.0 * rs + 72.0 + 8.0 + 8.0);
+}
 static double bytes_matvec(const DeviceBatch &b) {
+  if (b.explicit_schur) return bytes_spmv(b);
   // J_c, J_p (12 pairs) + segment / slot / point indices per observation;
   // C^-1 + CSR per point; per segment its position, slot, camera and the
   // camera's first-segment index, the camera's z and p_{k-1} (working
@@ -374,6 +409,13 @@ static double bytes_matvec(const DeviceBatch &b) {
   const double rs = b.opt.mixed ? 4.0 : 8.0;
   return (double)b.no * (24.0 * rs + 8.0) + (double)b.np * (4.0 + 6.0 * rs) +
          (double)b.nseg * (14.0 + 27.0 * rs) + (double)b.nc * 90.0 * rs + (double)b.nchunks * 40.0;
+}
+static double bytes_schur_form(const DeviceBatch &b) {
+  // the pairs, every observation's F once (a cached gather), per formed
+  // block its index, pair range and transpose index, and every block's 81
+  // values out
+  const double rs = b.opt.mixed ? 4.0 : 8.0;
+  return (double)b.npairs * 8.0 + (double)b.no * kObsF * rs + (double)b.nup * 12.0 + (double)b.nblk * 81.0 * rs;
 }
 static double bytes_pcg_camera(const DeviceBatch &b) {
   // partials and chunk values read once; per camera x, r, z, v, p in and
@@ -396,8 +438,9 @@ static double bytes_point_schur(const DeviceBatch &b) {
   // J_c, J_p, slot and point index per observation; C, g in and C^-1 (both
   // precisions), t out per point; 54 partials per segment
   const double rs = b.opt.mixed ? 4.0 : 8.0;
+  // (+ F per observation with the explicit Schur complement)
   return (double)b.no * (24.0 * rs + 2.0 + 4.0) + (double)b.np * (48.0 + 24.0 + 6.0 * rs + 48.0 + 24.0) +
-         (double)b.nseg * (54.0 * rs + 8.0);
+         (double)b.nseg * (54.0 * rs + 8.0) + (b.explicit_schur ? (double)b.no * kObsF * rs : 0.0);
 }
 static double bytes_schur(const DeviceBatch &b) {
   // partials in; B, g in; D^2, M^-1 (both precisions), PCG start vectors out
@@ -439,6 +482,11 @@ void Engine::enqueue_lm_head(cudaStream_t s) {
   prof_begin(s);
   launch_camera_schur(db_, mixed_, s);
   prof_end(s, PF_SCHUR, bytes_schur(db_));
+  if (db_.explicit_schur) {
+    prof_begin(s);
+    launch_schur_form(db_, mixed_, s);
+    prof_end(s, PF_FORM, bytes_schur_form(db_));
+  }
 }
 
 void Engine::enqueue_lm_tail(cudaStream_t s) {
@@ -802,6 +850,7 @@ gba_status Engine::compute_step(const gba_problem_view *v, double radius, double
   if ((st = check(cudaMemcpy(db_.lm, &L, sizeof L, cudaMemcpyHostToDevice), "state", err)) != GBA_OK) return st;
   launch_point_prepare(db_, mixed_, stream_);
   launch_camera_schur(db_, mixed_, stream_);
+  launch_schur_form(db_, mixed_, stream_);
   if ((st = read_status()) != GBA_OK) return st;
   int pcg = 0;
   while (hstat[2] && pcg <= o_.max_linear_solver_iterations) {

@@ -157,6 +157,26 @@ struct DeviceBatch {
   double *chunk_red;         // 2 * nchunks (mixed form: double-float pairs, hi then lo)
   uint32_t *chunk_counter;   // nchunks (one per group, at its first chunk)
   double *blk_red;           // 3 * cam_blocks
+  // explicit Schur complement (explicit_schur != 0): the off-diagonal
+  // camera-camera blocks by row camera, each block's transpose, the blocks
+  // on and above the diagonal with their observation pairs, per observation
+  // F = J_c^T J_p L (L L^T = C^-1 of its point), the blocks' values (9x9
+  // row-major, working precision), the diagonal blocks, S p of the current
+  // direction, and per camera its share of p.q
+  int32_t explicit_schur;
+  int32_t nblk, nup;
+  long long npairs;
+  const int32_t *sblk_row;   // nc + 1
+  const int32_t *sblk_col;   // nblk
+  const int32_t *sblk_tr;    // nblk
+  const int32_t *sblk_up;    // nup: block index
+  const int32_t *sblk_pair;  // nup + 1
+  const int2 *spair;         // npairs: (row camera's, column camera's observation)
+  void *obs_F;               // kObsF * no (9x3 row-major + pad)
+  void *sblk_val;            // 81 * nblk
+  void *cam_Sii;             // 81 * nc
+  double *pcg_q;             // 9 * nc
+  double *spmv_red;          // nc
 };
 
 constexpr int kCamTable = 44;    // R(9) dR(27) t(3) f k1 k2 + pad
@@ -175,6 +195,11 @@ constexpr int kPcgBlockCams = 8;
 // kRedGroup chunks first
 constexpr int kRedDirect = 2048;
 constexpr int kRedGroup = 64;
+// explicit Schur complement: chosen automatically up to this many ordered
+// observation pairs per observation, and supported up to kExplicitPairsMax
+constexpr long long kExplicitPairsPerObs = 16;
+constexpr long long kExplicitPairsMax = 1LL << 28;
+constexpr int kObsF = 28;  // reals per observation of obs_F (27 + pad: 16-byte rows)
 // prob_counter slots (4 per problem) and global_counter slots
 constexpr int kPC_SCHUR = 0, kPC_REDUCE = 1, kPC_UPDATE = 2;
 constexpr int kGC_SCHUR = 0, kGC_UPDATE = 1, kGC_POST = 2, kGC_LMBODIES = 3;

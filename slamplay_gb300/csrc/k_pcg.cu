@@ -30,7 +30,9 @@
 //       curvature ends the PCG); q_k = (B + Dc^2) p_k - sum of the camera's
 //       partials, x, r, z = M r, and the block's r.z, r.r and x.(v + r); the
 //       problem's last block sums them, runs the stopping test on
-//       (x_{k+1}, r_{k+1}) and stores beta_{k+1}.
+//       (x_{k+1}, r_{k+1}) and stores beta_{k+1}.  With the explicit Schur
+//       complement (k_schur.cu) q_k and the cameras' shares of p.q come
+//       from the block-sparse product instead.
 // Every cross-CTA sum either is redundant (each CTA sums the same values in
 // the same order) or is done once by the CTA that arrives last at a
 // counter; there are no spin-waits and no atomics on data, so a solve is
@@ -511,14 +513,17 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg_camera(DeviceBatch B) {
   double arow[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   real mrow[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   double x = 0.0, r = 0.0, z = 0.0, p_old = 0.0, v = 0.0;
+  // explicit Schur complement: q_k and the blocks' shares of p.q come from
+  // the block-sparse product; no partials
+  const bool ex = B.explicit_schur != 0;
   int s0 = 0, s1 = 0;
-  if (valid) {
+  if (valid && !ex) {
     s0 = B.cam_seg_begin[c];
     s1 = B.cam_seg_begin[c + 1];
   }
   if (lead) {
-    real ar[10];
-    a_row<MIXED>(B, c, q, ar);
+    real ar[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    if (!ex) a_row<MIXED>(B, c, q, ar);
 #pragma unroll
     for (int kk = 0; kk < 10; ++kk) arow[kk] = (double)ar[kk];  // converted before the wait
     const real *M = reinterpret_cast<const real *>(MIXED ? (const void *)B.cam_Minvf : (const void *)B.cam_Minv) +
@@ -532,17 +537,22 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg_camera(DeviceBatch B) {
     p_old = B.pcg_p[i];  // used when k > 0
   }
   pdl_wait();  // the partials and the chunk values come from the mat-vec kernel
-  double pq = 0.0;
+  double pq = 0.0, qex = 0.0;
   if (live) {
-    // p_k.q_k: the chunk values (or, for a large problem, the group values)
-    // in a fixed order, identical in every block of the problem
+    if (ex && lead) qex = __ldcg(B.pcg_q + i);
+    // p_k.q_k: the chunk values (or, for a large problem, the group values;
+    // with the explicit complement the cameras' values) in a fixed order,
+    // identical in every block of the problem
     const bool direct = pi.chunk_count <= kRedDirect;
-    const int n = direct ? pi.chunk_count : (pi.chunk_count + kRedGroup - 1) / kRedGroup;
-    const double *cv = B.chunk_red + (direct ? pi.chunk_begin : B.nchunks + pi.chunk_begin);
-    const int stride = direct ? 1 : kRedGroup;
+    const int n = ex ? pi.cam_count : (direct ? pi.chunk_count : (pi.chunk_count + kRedGroup - 1) / kRedGroup);
+    const double *cv = ex ? B.spmv_red + pi.cam_begin
+                          : B.chunk_red + (direct ? pi.chunk_begin : B.nchunks + pi.chunk_begin);
+    const int stride = (direct || ex) ? 1 : kRedGroup;
     // (the first kCv values per thread are loaded before the partials below,
     // so both sets of loads are in flight together); FP64 sums in the FP64
-    // form, double-float in the mixed form
+    // form and for the explicit complement's values, double-float for the
+    // mixed form's chunk values
+    const bool dfs = MIXED && !ex;
     constexpr int kCv = 4;
     double cvl[kCv];
     DF cvf[kCv];
@@ -551,7 +561,7 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg_camera(DeviceBatch B) {
       const int e = t + j * kPcgThreads;
       cvl[j] = 0.0, cvf[j] = df_zero();
       if (e < n) {
-        if (MIXED)
+        if (dfs)
           cvf[j] = chunk_value_load(B, (size_t)(cv - B.chunk_red) + (size_t)e * stride);
         else
           cvl[j] = __ldcg(cv + (size_t)e * stride);
@@ -560,7 +570,7 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg_camera(DeviceBatch B) {
     double psm = 0.0;
     DF psf = df_zero();
     for (int e = t + kCv * kPcgThreads; e < n; e += kPcgThreads) {
-      if (MIXED)
+      if (dfs)
         psf = df_add(psf, chunk_value_load(B, (size_t)(cv - B.chunk_red) + (size_t)e * stride));
       else
         psm += __ldcg(cv + (size_t)e * stride);
@@ -585,7 +595,7 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg_camera(DeviceBatch B) {
       psub[sub][m] = a;
     }
     // p.q over the CTA (fixed order); thread 0 forms alpha once
-    if (MIXED) {
+    if (dfs) {
 #pragma unroll
       for (int j = 0; j < kCv; ++j) psf = df_add(psf, cvf[j]);
       psf = df_warp_sum(psf);
@@ -599,7 +609,7 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg_camera(DeviceBatch B) {
     __syncthreads();  // also publishes psub
     if (t == 0) {
       double s2 = 0.0;
-      if (MIXED) {
+      if (dfs) {
         DF sf = dfred[0];
         for (int w = 1; w < kPcgWarps; ++w) sf = df_add(sf, dfred[w]);
         s2 = df_value(sf);
@@ -628,7 +638,7 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg_camera(DeviceBatch B) {
 #pragma unroll
       for (int j = 1; j < kPcgSub; ++j) comb.merge(psub[j][m]);
       const double psum = comb.value();
-      const double qv = a_times(arow, pv + 9 * lc, q) - psum;
+      const double qv = ex ? qex : a_times(arow, pv + 9 * lc, q) - psum;
       x = fma(alpha, p, x);
       r = fma(-alpha, qv, r);
       rv[m] = (real)r;
@@ -749,6 +759,7 @@ cudaError_t launch_schur_matvec(const DeviceBatch &b, bool mixed, cudaStream_t s
   // has ended cost it nothing; the other kernel loads their Jacobian before
   // it can see that), a single problem the register-prefetching one; both
   // compute bitwise the same values
+  if (b.explicit_schur) return launch_schur_spmv(b, mixed, s, pdl);
   if (mixed && b.num_problems > 1) return cudaLaunchKernelEx(&cfg, k_schur_matvec_lean, b);
   if (mixed) return cudaLaunchKernelEx(&cfg, k_schur_matvec<true>, b);
   return cudaLaunchKernelEx(&cfg, k_schur_matvec<false>, b);

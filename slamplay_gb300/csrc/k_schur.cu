@@ -1,0 +1,240 @@
+// k_schur.cu — the explicit Schur complement (gba_schur GBA_SCHUR_EXPLICIT).
+//
+// When the cameras' co-visibility is sparse, the reduced camera matrix
+//   S = B + Dc^2 - W C^-1 W^T
+// has few nonzero 9x9 camera-camera blocks: a 250-camera random walk has
+// about 28 per camera, 2.3 MB in FP32, where the Jacobian the implicit
+// mat-vec reads on every PCG iteration is 28 MB.  Then S is formed once per
+// LM iteration (the points eliminated into camera-camera blocks, as Ceres'
+// SPARSE_SCHUR and ITERATIVE_SCHUR with use_explicit_schur_complement do)
+// and every PCG iteration multiplies by the blocks, which stay in L2.
+//
+// With L L^T = C_j^-1 (the point's 3x3 factor) and F_a = J_c^T J_p L of an
+// observation a (9x3, formed by the point kernel K3a), the block of cameras
+// (i, k) is -sum over the points both see of F_a F_b^T.
+//
+//  K3c k_schur_form   one CTA per block on or above the diagonal (k >= i):
+//                     the sum over the block's observation pairs, in a
+//                     fixed order (three interleaved runs over the pairs'
+//                     point order, combined in order; compensated FP32 in
+//                     the mixed form), stored with its transpose as block
+//                     (k, i).  The diagonal blocks B + Dc^2 - sum F_a F_a^T
+//                     come from K3b; a camera that sees a point twice has a
+//                     block (i, i) here for the cross terms.
+//  K4a' k_schur_spmv  one CTA per camera, one warp per row of its 9x9
+//                     blocks, the lanes over the row's blocks (the last
+//                     one the diagonal block): q = S p_k with p_k = z_k +
+//                     beta_k p_{k-1} formed on the fly exactly as the
+//                     implicit mat-vec forms it, and the camera's share of
+//                     p.q for the camera kernel.  The blocks are fixed
+//                     during the PCG, so their loads are issued before the
+//                     wait on the preceding camera kernel.
+#include <cuda_runtime.h>
+
+#include "kernels.cuh"
+#include "kernels.h"
+
+namespace gba {
+
+namespace {
+
+constexpr int kFormThreads = 256;
+constexpr int kFormPairs = 32;  // pairs staged per round
+constexpr int kFormSub = 3;     // sub-lanes per block entry (243 of the 256 threads)
+
+__device__ __forceinline__ void pdl_wait_s() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_launch_dependents_s() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// 16-byte vector of the working precision
+template <bool MIXED>
+struct Vec16;
+template <>
+struct Vec16<true> {
+  typedef float4 type;
+};
+template <>
+struct Vec16<false> {
+  typedef double2 type;
+};
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// K3c
+template <bool MIXED>
+__global__ void __launch_bounds__(kFormThreads) k_schur_form(DeviceBatch B) {
+  typedef typename Prec<MIXED>::real real;
+  typedef typename Acc<MIXED>::type Acc;
+  typedef typename Vec16<MIXED>::type vec;
+  constexpr int kVec = (int)(sizeof(vec) / sizeof(real));
+  constexpr int kRowVecs = kObsF / kVec;  // 16-byte loads per F row
+  static_assert(kObsF % kVec == 0, "F rows are whole 16-byte vectors");
+  __shared__ __align__(16) real Fs[kFormPairs][2][kObsF];  // F of the row's and the column's observation
+  __shared__ Acc part[kFormSub][81];
+  const int ub = blockIdx.x, t = threadIdx.x;
+  const int blk = B.sblk_up[ub];
+  const int p0 = B.sblk_pair[ub], p1 = B.sblk_pair[ub + 1];
+  const LMState *L = B.lm + B.pt_problem[B.obs_pt[B.spair[p0].x]];  // every block has a pair
+  if (!L->active) return;  // uniform
+  // sub-lane `sub` of entry (i, k) sums the pairs sub, sub + kFormSub, ...
+  // of every round, in order
+  const int sub = t / 81, en = t - 81 * sub, ei = en / 9, ek = en - 9 * ei;
+  Acc acc;
+  acc.init();
+  for (int g = p0; g < p1; g += kFormPairs) {
+    const int n = min(kFormPairs, p1 - g);
+    for (int i = t; i < n * 2 * kRowVecs; i += kFormThreads) {
+      const int u = i / (2 * kRowVecs), r = i - 2 * kRowVecs * u;
+      const int side = r / kRowVecs, e = r - kRowVecs * side;
+      const int2 pr = B.spair[g + u];
+      const vec *src = reinterpret_cast<const vec *>(reinterpret_cast<const real *>(B.obs_F) +
+                                                     (size_t)kObsF * (side ? pr.y : pr.x));
+      *reinterpret_cast<vec *>(&Fs[u][side][kVec * e]) = src[e];
+    }
+    __syncthreads();
+    if (sub < kFormSub)
+      for (int u = sub; u < n; u += kFormSub) {
+        const real *fa = &Fs[u][0][3 * ei], *fb = &Fs[u][1][3 * ek];
+        acc.add(fa[0] * fb[0] + fa[1] * fb[1] + fa[2] * fb[2]);
+      }
+    __syncthreads();  // the stage is reused
+  }
+  if (sub < kFormSub) part[sub][en] = acc;
+  __syncthreads();
+  if (t < 81) {
+    Acc s = part[0][t];
+#pragma unroll
+    for (int j = 1; j < kFormSub; ++j) s.merge(part[j][t]);
+    const real v = -(real)s.rvalue();
+    real *vals = reinterpret_cast<real *>(B.sblk_val);
+    const int i = t / 9, k = t - 9 * i;
+    vals[81 * (size_t)blk + t] = v;
+    const int tr = B.sblk_tr[blk];
+    if (tr != blk) vals[81 * (size_t)tr + 9 * k + i] = v;
+  }
+}
+
+void launch_schur_form(const DeviceBatch &b, bool mixed, cudaStream_t s) {
+  if (!b.explicit_schur || b.nup == 0) return;
+  if (mixed)
+    k_schur_form<true><<<b.nup, kFormThreads, 0, s>>>(b);
+  else
+    k_schur_form<false><<<b.nup, kFormThreads, 0, s>>>(b);
+}
+
+// ---------------------------------------------------------------------------
+// K4a'
+constexpr int kSpmvThreads = 9 * 32;
+constexpr int kSpmvPrefetch = 2;  // blocks per lane whose values load before the wait
+
+template <bool MIXED>
+__global__ void __launch_bounds__(kSpmvThreads) k_schur_spmv(DeviceBatch B) {
+  typedef typename Prec<MIXED>::real real;
+  __shared__ double pqs[9];
+  const int c = blockIdx.x, t = threadIdx.x;
+  const int q = t >> 5, lane = t & 31;
+  const int prob = B.cam_problem[c];
+  const int r0 = B.sblk_row[c], nb = B.sblk_row[c + 1] - r0;
+  // virtual block v of the row: v < nb the off-diagonal block r0 + v, v = nb
+  // the diagonal block; lane l takes v = l, l + 32, ...
+  const real *vals = reinterpret_cast<const real *>(B.sblk_val);
+  const real *diag = reinterpret_cast<const real *>(B.cam_Sii) + 81 * (size_t)c + 9 * q;
+  real pre[kSpmvPrefetch][9];
+  int pcol[kSpmvPrefetch];
+#pragma unroll
+  for (int u = 0; u < kSpmvPrefetch; ++u) {
+    const int v = lane + 32 * u;
+    pcol[u] = -1;
+#pragma unroll
+    for (int cc = 0; cc < 9; ++cc) pre[u][cc] = 0;
+    if (v <= nb) {
+      const real *row = v < nb ? vals + 81 * (size_t)(r0 + v) + 9 * q : diag;
+      pcol[u] = v < nb ? B.sblk_col[r0 + v] : c;
+#pragma unroll
+      for (int cc = 0; cc < 9; ++cc) pre[u][cc] = row[cc];
+    }
+  }
+  pdl_wait_s();
+  pdl_launch_dependents_s();
+  const LMState *L = B.lm + prob;
+  if (!(L->active && L->pcg_active)) return;  // uniform over the CTA
+  const int k = L->pcg_iterations;
+  const double beta = L->beta;
+  const real *zv = reinterpret_cast<const real *>(MIXED ? (const void *)B.pcg_zf : (const void *)B.pcg_z);
+  const real *pvv = reinterpret_cast<const real *>(MIXED ? (const void *)B.pcg_pf : (const void *)B.pcg_p);
+  // p_k of a camera coordinate: the FP64 form evaluates the camera kernel's
+  // expression, the mixed form the same recurrence in FP32 on the FP32
+  // copies (as the implicit mat-vec)
+  auto pdir = [&](size_t idx) -> real {
+    const real z = zv[idx];
+    if (k == 0) return z;
+    if (MIXED) return (real)__fmaf_rn((float)beta, (float)pvv[idx], (float)z);
+    return (real)fma(beta, (double)pvv[idx], (double)z);
+  };
+  auto row_dot = [&](const real *row, int col) -> real {
+    real s = 0;
+#pragma unroll
+    for (int cc = 0; cc < 9; ++cc) s += row[cc] * pdir(9 * (size_t)col + cc);
+    return s;
+  };
+  // the lane's blocks in order: FP64 sums in the FP64 form, double-float in
+  // the mixed form
+  DF af = df_zero();
+  double ad = 0.0;
+#pragma unroll
+  for (int u = 0; u < kSpmvPrefetch; ++u)
+    if (pcol[u] >= 0) {
+      const real s = row_dot(pre[u], pcol[u]);
+      if (MIXED)
+        af = df_add(af, DF{(float)s, 0.f});
+      else
+        ad += (double)s;
+    }
+  for (int v = lane + 32 * kSpmvPrefetch; v <= nb; v += 32) {
+    const real *row = v < nb ? vals + 81 * (size_t)(r0 + v) + 9 * q : diag;
+    const real s = row_dot(row, v < nb ? B.sblk_col[r0 + v] : c);
+    if (MIXED)
+      af = df_add(af, DF{(float)s, 0.f});
+    else
+      ad += (double)s;
+  }
+  // the row's sum over the lanes (butterfly: a fixed order)
+  double qv;
+  if (MIXED) {
+    af = df_warp_sum(af);
+    qv = df_value(af);
+  } else {
+    qv = warp_sum(ad);
+  }
+  if (lane == 0) {
+    const size_t i = 9 * (size_t)c + q;
+    B.pcg_q[i] = qv;
+    pqs[q] = (double)pdir(i) * qv;
+  }
+  __syncthreads();
+  if (t == 0) {
+    double s = 0.0;
+#pragma unroll
+    for (int r = 0; r < 9; ++r) s += pqs[r];
+    B.spmv_red[c] = s;
+  }
+}
+
+cudaError_t launch_schur_spmv(const DeviceBatch &b, bool mixed, cudaStream_t s, bool pdl) {
+  if (b.nc == 0) return cudaSuccess;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)b.nc);
+  cfg.blockDim = dim3(kSpmvThreads);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = pdl ? 1 : 0;
+  if (mixed) return cudaLaunchKernelEx(&cfg, k_schur_spmv<true>, b);
+  return cudaLaunchKernelEx(&cfg, k_schur_spmv<false>, b);
+}
+
+}  // namespace gba

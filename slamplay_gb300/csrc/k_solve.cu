@@ -49,7 +49,24 @@ struct PointSchurSmem {
   real ae[kChunkCap][5];   // A00 A01 A11 e_u e_v by slot
   real ci[kChunkCap][6];   // C^-1 by chunk point
   real tp[kChunkCap][3];   // C^-1 g_p by chunk point
+  // last, and allocated only with the explicit Schur complement:
+  real lc[kChunkCap][6];   // L, L L^T = C^-1: l00 l10 l11 l20 l21 l22
 };
+
+// Lower Cholesky factor of a symmetric 3x3 (packed 00 01 02 11 12 22):
+// l00 l10 l11 l20 l21 l22, zero where a pivot is not positive.
+__device__ __forceinline__ void chol3(const double *A, double *L) {
+  const double l00 = A[0] > 0.0 ? sqrt(A[0]) : 0.0;
+  const double i00 = l00 > 0.0 ? recip_nr(l00) : 0.0;
+  const double l10 = A[1] * i00, l20 = A[2] * i00;
+  const double d1 = A[3] - l10 * l10;
+  const double l11 = d1 > 0.0 ? sqrt(d1) : 0.0;
+  const double i11 = l11 > 0.0 ? recip_nr(l11) : 0.0;
+  const double l21 = (A[4] - l20 * l10) * i11;
+  const double d2 = A[5] - l20 * l20 - l21 * l21;
+  const double l22 = d2 > 0.0 ? sqrt(d2) : 0.0;
+  L[0] = l00, L[1] = l10, L[2] = l11, L[3] = l20, L[4] = l21, L[5] = l22;
+}
 
 __device__ __forceinline__ void sym9_pair(int e, int &a, int &b) {
   a = 0;
@@ -117,6 +134,12 @@ __global__ void __launch_bounds__(kChunkCap) k_point_schur(DeviceBatch B) {
       B.pt_t[3 * (size_t)j + 1] = t1;
       B.pt_t[3 * (size_t)j + 2] = t2;
       sm.tp[t][0] = (real)t0, sm.tp[t][1] = (real)t1, sm.tp[t][2] = (real)t2;
+      if (B.explicit_schur) {
+        double Lc[6];
+        chol3(Ci, Lc);
+#pragma unroll
+        for (int q = 0; q < 6; ++q) sm.lc[t][q] = (real)Lc[q];
+      }
     }
     // the first (segment, entry) task of this thread: its metadata now
     int f_b0 = 0, f_b1 = 0, f_slot = 0;
@@ -144,6 +167,22 @@ __global__ void __launch_bounds__(kChunkCap) k_point_schur(DeviceBatch B) {
       sm.ae[slot][4] = Jp[0].y * t0 + Jp[1].y * t1 + Jp[2].y * t2;
 #pragma unroll
       for (int q = 0; q < 9; ++q) sm.jc[slot][2 * q] = Jc[q].x, sm.jc[slot][2 * q + 1] = Jc[q].y;
+      if (B.explicit_schur) {
+        // F = E L with E = J_c^T J_p (9x3) and L L^T = C^-1: the explicit
+        // complement's blocks are -sum F_a F_b^T over observation pairs
+        const real *Lc = sm.lc[lp];
+        real *F = reinterpret_cast<real *>(B.obs_F) + (size_t)kObsF * (ci.obs_begin + t);
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+          const real e0 = Jc[q].x * Jp[0].x + Jc[q].y * Jp[0].y;
+          const real e1 = Jc[q].x * Jp[1].x + Jc[q].y * Jp[1].y;
+          const real e2 = Jc[q].x * Jp[2].x + Jc[q].y * Jp[2].y;
+          F[3 * q + 0] = e0 * Lc[0] + e1 * Lc[1] + e2 * Lc[3];
+          F[3 * q + 1] = e1 * Lc[2] + e2 * Lc[4];
+          F[3 * q + 2] = e2 * Lc[5];
+        }
+        F[27] = (real)0;
+      }
     }
     __syncthreads();
     real *part = reinterpret_cast<real *>(B.schur_partial);
@@ -181,10 +220,13 @@ size_t point_schur_smem(bool mixed) {
 }
 
 void launch_point_prepare(const DeviceBatch &b, bool mixed, cudaStream_t s) {
+  // without the explicit Schur complement the factor rows are not allocated
+  // (more CTAs per SM in the FP64 form)
+  const size_t lcb = b.explicit_schur ? 0 : kChunkCap * 6 * (mixed ? sizeof(float) : sizeof(double));
   if (mixed)
-    k_point_schur<true><<<b.nchunks, kChunkCap, point_schur_smem(true), s>>>(b);
+    k_point_schur<true><<<b.nchunks, kChunkCap, point_schur_smem(true) - lcb, s>>>(b);
   else
-    k_point_schur<false><<<b.nchunks, kChunkCap, point_schur_smem(false), s>>>(b);
+    k_point_schur<false><<<b.nchunks, kChunkCap, point_schur_smem(false) - lcb, s>>>(b);
 }
 
 // ---------------------------------------------------------------------------
@@ -280,6 +322,7 @@ __global__ void __launch_bounds__(kSchurThreads) k_camera_schur(DeviceBatch B) {
         B.cam_D2[9 * (size_t)c + a] = d2;
       }
       buf[0][t] = v;
+      if (B.explicit_schur) reinterpret_cast<real *>(B.cam_Sii)[81 * (size_t)c + t] = (real)v;
     }
     if (t < 9) vec[t] = B.cam_g[9 * (size_t)c + t] - sums[45 + t];
     __syncthreads();

@@ -25,6 +25,11 @@ void launch_post_eval(const DeviceBatch &b, cudaStream_t s);
 void launch_point_prepare(const DeviceBatch &b, bool mixed, cudaStream_t s);
 // K3b: camera-diagonal Schur blocks, reduced rhs, block-Jacobi inverse, PCG init.
 void launch_camera_schur(const DeviceBatch &b, bool mixed, cudaStream_t s);
+// K3c: the off-diagonal camera-camera blocks of the explicit Schur complement.
+void launch_schur_form(const DeviceBatch &b, bool mixed, cudaStream_t s);
+// K4a': q = S p_k with the explicit complement (launch_schur_matvec calls it
+// when the batch forms S).
+cudaError_t launch_schur_spmv(const DeviceBatch &b, bool mixed, cudaStream_t s, bool pdl);
 // K4a-b: one PCG iteration (implicit Schur mat-vec, camera-side update).
 void launch_pcg_iteration(const DeviceBatch &b, bool mixed, cudaStream_t s);
 cudaError_t launch_schur_matvec(const DeviceBatch &b, bool mixed, cudaStream_t s, bool pdl);

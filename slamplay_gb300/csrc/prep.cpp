@@ -61,6 +61,77 @@ gba_status validate_problem(const gba_problem_view *v, std::string *err) {
   return GBA_OK;
 }
 
+// The explicit Schur complement's structure, row camera by row camera: the
+// row's co-visible cameras (sorted; the row's own camera when it observes a
+// point more than once), the transpose of every block, and for the blocks
+// on and above the diagonal (column camera >= row camera: the formation
+// kernel forms those and writes each transpose) the ordered observation
+// pairs (a of the row camera, b of the column camera, a != b, same point)
+// in point order, so the formation sums have a fixed order.  A camera's
+// observations (cam_obs_list) are in point order, so walking them and each
+// point's observations lists every block's pairs in that order.  O(pairs)
+// with a per-row lookup table.
+static void build_schur_structure(HostBatch *hbp) {
+  HostBatch &hb = *hbp;
+  std::vector<int32_t> mark(hb.nc, -1), pos(hb.nc, 0), row, cnt;
+  hb.sblk_row.assign(hb.nc + 1, 0);
+  hb.sblk_col.clear();
+  hb.sblk_up.clear();
+  hb.sblk_pair.assign(1, 0);
+  hb.spair.clear();
+  for (int c = 0; c < hb.nc; ++c) {
+    const int a0 = hb.cam_obs_begin[c], a1 = hb.cam_obs_begin[c + 1];
+    row.clear();
+    for (int ia = a0; ia < a1; ++ia) {
+      const int a = hb.cam_obs_list[ia], j = hb.obs_pt[a];
+      for (int b = hb.pt_obs_begin[j]; b < hb.pt_obs_begin[j + 1]; ++b) {
+        const int k = hb.obs_cam[b];
+        if (b != a && mark[k] != c) mark[k] = c, row.push_back(k);
+      }
+    }
+    std::sort(row.begin(), row.end());
+    const int nb = (int)row.size();
+    const int u0 = (int)(std::lower_bound(row.begin(), row.end(), c) - row.begin());  // first column >= c
+    const int nu = nb - u0;
+    cnt.assign(nu + 1, 0);
+    for (int u = u0; u < nb; ++u) pos[row[u]] = u - u0;
+    for (int ia = a0; ia < a1; ++ia) {
+      const int a = hb.cam_obs_list[ia], j = hb.obs_pt[a];
+      for (int b = hb.pt_obs_begin[j]; b < hb.pt_obs_begin[j + 1]; ++b)
+        if (b != a && hb.obs_cam[b] >= c) ++cnt[pos[hb.obs_cam[b]] + 1];
+    }
+    for (int u = 0; u < nu; ++u) cnt[u + 1] += cnt[u];
+    const size_t base = hb.spair.size() / 2;
+    for (int u = 0; u < nb; ++u) hb.sblk_col.push_back(row[u]);
+    for (int u = 0; u < nu; ++u) {
+      hb.sblk_up.push_back(hb.sblk_row[c] + u0 + u);
+      hb.sblk_pair.push_back((int32_t)(base + cnt[u + 1]));
+    }
+    hb.spair.resize(2 * (base + (size_t)cnt[nu]));
+    for (int ia = a0; ia < a1; ++ia) {
+      const int a = hb.cam_obs_list[ia], j = hb.obs_pt[a];
+      for (int b = hb.pt_obs_begin[j]; b < hb.pt_obs_begin[j + 1]; ++b)
+        if (b != a && hb.obs_cam[b] >= c) {
+          const size_t k = base + cnt[pos[hb.obs_cam[b]]]++;
+          hb.spair[2 * k] = a;
+          hb.spair[2 * k + 1] = b;
+        }
+    }
+    hb.sblk_row[c + 1] = hb.sblk_row[c] + nb;
+  }
+  hb.nblk = hb.sblk_row[hb.nc];
+  hb.nup = (long long)hb.sblk_up.size();
+  hb.npairs = (long long)(hb.spair.size() / 2);
+  // the transpose of block (c, k) is block (k, c), in row k
+  hb.sblk_tr.resize(hb.nblk);
+  for (int c = 0; c < hb.nc; ++c)
+    for (int e = hb.sblk_row[c]; e < hb.sblk_row[c + 1]; ++e) {
+      const int k = hb.sblk_col[e];
+      const auto b0 = hb.sblk_col.begin() + hb.sblk_row[k], b1 = hb.sblk_col.begin() + hb.sblk_row[k + 1];
+      hb.sblk_tr[e] = (int32_t)(std::lower_bound(b0, b1, c) - hb.sblk_col.begin());
+    }
+}
+
 gba_status prepare_batch(const gba_problem_view *views, int n, const PrepOptions &opt, HostBatch *out,
                          std::string *err) {
   HostBatch &hb = *out;
@@ -253,10 +324,29 @@ gba_status prepare_batch(const gba_problem_view *views, int n, const PrepOptions
   hb.seg_slot.resize(hb.nseg);
   fill.assign(hb.cam_seg_begin.begin(), hb.cam_seg_begin.end());
   for (int s = 0; s < hb.nseg; ++s) hb.seg_slot[s] = fill[hb.seg_cam[s]]++;
+  // explicit Schur complement: chosen by the option, AUTO when a point's
+  // ordered observation pairs (sum over points of m (m - 1)) are at most
+  // kExplicitPairsPerObs per observation (forming S then costs less than the
+  // implicit mat-vec saves over a PCG solve)
+  {
+    long long pairs = 0;
+    for (int j = 0; j < hb.np; ++j) {
+      const long long m = hb.pt_obs_begin[j + 1] - hb.pt_obs_begin[j];
+      pairs += m * (m - 1);
+    }
+    hb.explicit_schur = opt.schur == GBA_SCHUR_EXPLICIT ||
+                        (opt.schur == GBA_SCHUR_AUTO && pairs <= kExplicitPairsPerObs * (long long)hb.no);
+    if (hb.explicit_schur && pairs > kExplicitPairsMax) {
+      *err = fmt("the explicit Schur complement needs %lld observation pairs; at most %lld are supported", pairs,
+                 (long long)kExplicitPairsMax);
+      return GBA_ERR_INVALID_ARGUMENT;
+    }
+  }
   for (int k = 0; k < hb.no; ++k) ++hb.cam_obs_begin[hb.obs_cam[k] + 1];
   for (int c = 0; c < hb.nc; ++c) hb.cam_obs_begin[c + 1] += hb.cam_obs_begin[c];
   fill.assign(hb.cam_obs_begin.begin(), hb.cam_obs_begin.end());
   for (int k = 0; k < hb.no; ++k) hb.cam_obs_list[fill[hb.obs_cam[k]]++] = k;
+  if (hb.explicit_schur) build_schur_structure(&hb);
   return GBA_OK;
 }
 

@@ -13,6 +13,7 @@ namespace gba {
 struct PrepOptions {
   int chunk_cap = kChunkCap;  // observations per chunk (CTA)
   bool reorder_points = true; // group points by their first camera
+  int schur = GBA_SCHUR_AUTO; // gba_schur: whether the batch forms S explicitly
 };
 
 struct HostBatch {
@@ -28,6 +29,16 @@ struct HostBatch {
   std::vector<int32_t> seg_cam;
   std::vector<int32_t> cam_seg_begin, seg_slot, cam_obs_begin, cam_obs_list;
   std::vector<int4> camblk;
+  // explicit Schur complement (explicit_schur): the off-diagonal camera-camera
+  // blocks of S by row camera (CSR over the batch's cameras; a block with
+  // the row's own camera holds the cross terms of a camera that observes a
+  // point more than once) and each block's transpose; the blocks on and
+  // above the diagonal (sblk_up) with their observation pairs (row camera's,
+  // column camera's) of the points both see, in point order
+  bool explicit_schur = false;
+  long long nblk = 0, nup = 0, npairs = 0;
+  std::vector<int32_t> sblk_row, sblk_col, sblk_tr, sblk_up, sblk_pair;
+  std::vector<int32_t> spair;  // 2 per pair
   // output mapping
   std::vector<int32_t> obs_orig;  // internal observation -> index in its problem's input
   std::vector<int32_t> pt_orig;   // internal point -> point index in its problem's input

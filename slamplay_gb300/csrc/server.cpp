@@ -22,11 +22,20 @@ double now_s() {
 constexpr int kSlots = 4;
 }  // namespace
 
-size_t Server::estimate_footprint(int nc, int np, int no, bool mixed) {
+size_t Server::estimate_footprint(int nc, int np, int no, bool mixed, bool explicit_bound) {
   const double per_obs = 32.0 + 4.0 + 13.0 * (mixed ? 8.0 : 16.0) + 84.0;  // indices, J, segment share
   const double per_pt = 16.0 + 64.0 + 8.0 * 24.0 + (mixed ? 24.0 : 48.0);
   const double per_cam = 8.0 * (18.0 + 44.0 + 45.0 + 9.0 + 9.0 + 81.0 + 9.0 + 54.0 + 9.0 + 6.0) + 64.0;
-  const double bytes = per_obs * no + per_pt * np + per_cam * nc;
+  double bytes = per_obs * no + per_pt * np + per_cam * nc;
+  if (explicit_bound) {
+    // the explicit Schur complement as GBA_SCHUR_AUTO may choose it: at most
+    // kExplicitPairsPerObs observation pairs per observation, and at most
+    // that many (and nc^2) camera-camera blocks of 81 values
+    const double rs = mixed ? 4.0 : 8.0;
+    const double pairs = (double)kExplicitPairsPerObs * no;
+    const double blocks = std::min(pairs, (double)nc * (double)nc);
+    bytes += pairs * 8.0 + blocks * (81.0 * rs + 8.0) + (double)nc * (81.0 * rs + 80.0);
+  }
   return (size_t)(bytes * 1.15) + (1u << 20);
 }
 
@@ -58,7 +67,8 @@ gba_status Server::submit(const gba_problem_view *p, uint64_t *ticket, std::stri
   const gba_status vs = validate_problem(p, err);
   if (vs != GBA_OK) return vs;
   const bool mixed = o_.precision == GBA_PRECISION_MIXED;
-  const size_t fp = estimate_footprint(p->num_cameras, p->num_points, p->num_observations, mixed);
+  const size_t fp = estimate_footprint(p->num_cameras, p->num_points, p->num_observations, mixed,
+                                      o_.schur != GBA_SCHUR_IMPLICIT);
   std::lock_guard<std::mutex> lk(mu_);
   if (!running_ || stopping_) {
     *err = "server not running";

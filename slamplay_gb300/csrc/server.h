@@ -20,7 +20,9 @@ class Server {
   ~Server() { stop(); }
 
   // Estimated device bytes of one problem (admission rule).
-  static size_t estimate_footprint(int nc, int np, int no, bool mixed);
+  // Upper bound of one problem's device bytes; explicit_bound adds what the
+  // explicit Schur complement may take when the options allow it.
+  static size_t estimate_footprint(int nc, int np, int no, bool mixed, bool explicit_bound);
 
   gba_status start(size_t budget, int max_live, int max_queue, std::string *err);
   gba_status submit(const gba_problem_view *p, uint64_t *ticket, std::string *err);

@@ -86,8 +86,9 @@ def _summary(s: N.Summary, tr: _Trace | None) -> SolveSummary:
 
 
 def make_options(**kw) -> N.Options:
-    """gba_options with Ceres' defaults, overridden by keyword (loss and
-    precision accept names: loss='huber', precision='mixed')."""
+    """gba_options with Ceres' defaults, overridden by keyword (loss,
+    precision, pcg_criterion and schur accept names: loss='huber',
+    precision='mixed', schur='explicit')."""
     o = N.Options()
     N.lib().gba_options_init(N.C.byref(o))
     for k, v in kw.items():
@@ -97,6 +98,8 @@ def make_options(**kw) -> N.Options:
             v = N.PRECISION[v]
         elif k == "pcg_criterion" and isinstance(v, str):
             v = N.PCG_CRITERION[v]
+        elif k == "schur" and isinstance(v, str):
+            v = N.SCHUR[v]
         elif k == "stream" and v is not None and not isinstance(v, int):
             v = int(v)
         if not hasattr(o, k):

@@ -143,7 +143,7 @@ def test_batch_equals_alone_bitwise(precision):
     # differ in how they load, not in what they compute)
     probs = [BALProblem.synthetic(3, index=i, seed=2) for i in range(4)]
     alone = []
-    with Solver(max_num_iterations=8, precision=precision, **FIXED) as s:
+    with Solver(max_num_iterations=8, precision=precision, schur="implicit", **FIXED) as s:
         for p in probs:
             q = p.copy()
             sm = s.solve(q)
@@ -196,7 +196,7 @@ def test_many_camera_problem_matches_oracle_pcg(crit):
     1e-6 (a rounding-level change of where the model test stops may move one
     PCG iteration)."""
     b = BALProblem.synthetic(0, seed=21, num_cameras=700, num_points=6000)
-    opts = dict(max_num_iterations=6, pcg_criterion=crit, **FIXED)
+    opts = dict(max_num_iterations=6, pcg_criterion=crit, schur="implicit", **FIXED)
     tol = dict(pcg_tolerance=1e-12, max_linear_solver_iterations=1000) if crit == "residual" else dict(eta=1e-6)
     g, sg, so = _solve_pair(b, dict(opts, **tol), dict(opts, linear_solver="pcg_schur", **tol))
     rel = abs(sg.final_cost - so["final_cost"]) / so["final_cost"]
@@ -219,7 +219,7 @@ def test_large_problem_reduction_path(precision):
     or 1e-6 (mixed) of each other, and of the FP64 oracle."""
     b = BALProblem.synthetic(0, seed=5, num_points=20000)
     opts = dict(max_num_iterations=6, pcg_tolerance=1e-10, max_linear_solver_iterations=300,
-                precision=precision, **FIXED)
+                precision=precision, schur="implicit", **FIXED)
     with Solver(chunk_observations=32, **opts) as s:
         grouped = s.solve(b.copy())
     with Solver(**opts) as s:
