@@ -136,7 +136,12 @@ typedef struct gba_options {
   int32_t autotune;                   /* 1 = run gba_autotune on the first solve of a
                                          new problem-size bucket                     */
   int32_t schur;                      /* gba_schur, GBA_SCHUR_AUTO                   */
-  int32_t reserved[5];
+  int32_t persistent_pcg;             /* 1 = with the mixed precision and the explicit
+                                         Schur complement, run each problem's whole PCG
+                                         in one launch (a thread-block cluster per
+                                         problem) when it fits; 0 = one launch pair per
+                                         PCG iteration                               */
+  int32_t reserved[4];
 } gba_options;
 
 /* Per-solve report, the subset of ceres::Solver::Summary the reference

@@ -45,7 +45,8 @@ class Options(C.Structure):
         ("pcg_tolerance", C.c_double), ("eta", C.c_double),
         ("minimizer_progress_to_stdout", C.c_int32), ("device", C.c_int32), ("stream", C.c_void_p),
         ("chunk_observations", C.c_int32), ("reorder_points", C.c_int32), ("use_graphs", C.c_int32),
-        ("pcg_unroll", C.c_int32), ("autotune", C.c_int32), ("schur", C.c_int32), ("reserved", C.c_int32 * 5),
+        ("pcg_unroll", C.c_int32), ("autotune", C.c_int32), ("schur", C.c_int32), ("persistent_pcg", C.c_int32),
+        ("reserved", C.c_int32 * 4),
     ]
 
 

@@ -77,6 +77,7 @@ void gba_options_init(gba_options *o) {
   o->pcg_unroll = 0;
   o->autotune = 0;
   o->schur = GBA_SCHUR_AUTO;
+  o->persistent_pcg = 1;
 }
 
 const char *gba_version(void) { return "gba 1 sm_103a"; }

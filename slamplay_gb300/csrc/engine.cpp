@@ -45,11 +45,13 @@ enum ProfSlot {
   PF_TABLE,
   PF_SETUP_MISC,
   PF_FORM,
+  PF_CLUSTER,
   PF_COUNT
 };
 const char *kProfNames[PF_COUNT] = {"eval_jacobian",  "post_eval", "point_schur",  "camera_schur",
                                     "schur_matvec",   "pcg_camera", "back_substitute", "candidate_cost",
-                                    "decide",         "camera_table", "setup_misc", "schur_form"};
+                                    "decide",         "camera_table", "setup_misc", "schur_form",
+                                    "pcg_cluster"};
 
 double now_s() {
   return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
@@ -185,6 +187,7 @@ size_t Engine::layout(const HostBatch &hb, char *base, DeviceBatch *db, size_t *
   b.sblk_up = cv.take<int32_t>(nup);
   b.sblk_pair = cv.take<int32_t>(ex ? nup + 1 : 0);
   b.spair = cv.take<int2>(ex ? (size_t)hb.npairs : 0);
+  b.obs_fpos = cv.take<int32_t>(ex ? no : 0);
   *upload_bytes = align_up(cv.off, 256);
   // download
   cv.off = *upload_bytes;
@@ -247,6 +250,7 @@ size_t Engine::layout(const HostBatch &hb, char *base, DeviceBatch *db, size_t *
   b.cam_Sii = cv.take<char>(ex ? 81 * nc * rs : 0);
   b.pcg_q = cv.take<double>(ex ? 9 * nc : 0);
   b.spmv_red = cv.take<double>(ex ? nc : 0);
+  b.cl_camv = cv.take<double>(ex ? 4 * nc : 0);
   b.prob_counter = cv.take<uint32_t>(4 * P);
   b.global_counter = cv.take<uint32_t>(8);
   b.chunk_counter = cv.take<uint32_t>(nch);
@@ -347,6 +351,7 @@ gba_status Engine::upload(const HostBatch &hb, std::string *err) {
     put(const_cast<int32_t *>(hdb.sblk_tr), hb.sblk_tr);
     put(const_cast<int32_t *>(hdb.sblk_up), hb.sblk_up);
     put(const_cast<int32_t *>(hdb.sblk_pair), hb.sblk_pair);
+    put(const_cast<int32_t *>(hdb.obs_fpos), hb.obs_fpos);
     if (!hb.spair.empty())
       std::memcpy(const_cast<int2 *>(hdb.spair), hb.spair.data(), hb.spair.size() * sizeof(int32_t));
   }
@@ -355,9 +360,18 @@ gba_status Engine::upload(const HostBatch &hb, std::string *err) {
   if ((st = check(cudaMemcpyAsync(d_arena_, h_stage_, upload_bytes_, cudaMemcpyHostToDevice, stream_),
                   "upload", err)) != GBA_OK)
     return st;
-  // current batch shape + pointers + options = graph key
+  // the PCG as one cluster launch per LM iteration: mixed form, explicit
+  // Schur complement, every problem small enough
+  cl_plan_ = ClusterPlan();
+  if (mixed_ && hb.explicit_schur && o_.persistent_pcg &&
+      !pcg_cluster_plan(hb.prob.data(), (int)hb.prob.size(), hb.sblk_row.data(), &cl_plan_))
+    cl_plan_ = ClusterPlan();
+  // current batch shape + pointers + options + PCG form = graph key
   DeviceBatch k = db_;
   cur_key_.assign(reinterpret_cast<const char *>(&k), reinterpret_cast<const char *>(&k) + sizeof k);
+  cur_key_.push_back(cl_plan_.cs);
+  cur_key_.push_back(cl_plan_.threads);
+  cur_key_.push_back(cl_plan_.cache_blocks);
   return GBA_OK;
 }
 
@@ -558,24 +572,32 @@ gba_status Engine::build_graph(std::string *err) {
   enqueue_setup(stream_);
   cudaGraph_t lmbody = nullptr, pcgbody = nullptr, tmp = nullptr;
   if ((e = add_while(stream_, lmh, &lmbody)) != cudaSuccess) return fail(e, "LM conditional node");
-  if ((e = cudaGraphConditionalHandleCreate(&pcgh, lmbody, 1, cudaGraphCondAssignDefault)) != cudaSuccess)
+  // (a conditional handle must belong to a node: none for the cluster PCG)
+  if (cl_plan_.cs == 0 &&
+      (e = cudaGraphConditionalHandleCreate(&pcgh, lmbody, 1, cudaGraphCondAssignDefault)) != cudaSuccess)
     return fail(e, "PCG conditional handle");
-  db_.pcg_cond = pcgh;
+  db_.pcg_cond = cl_plan_.cs > 0 ? 0 : pcgh;
   e = cudaStreamBeginCaptureToGraph(cap_[0], lmbody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) return fail(e, "capture LM body");
   enqueue_lm_head(cap_[0]);
-  if ((e = add_while(cap_[0], pcgh, &pcgbody)) != cudaSuccess) return fail(e, "PCG conditional node");
-  e = cudaStreamBeginCaptureToGraph(cap_[1], pcgbody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
-  if (e != cudaSuccess) return fail(e, "capture PCG body");
-  // pcg_unroll (default kPcgUnroll) PCG iterations per body (a finished PCG turns the extra
-  // launches into early exits); inside the body each kernel is a
-  // programmatic dependent of the one before it
-  const int unroll = o_.pcg_unroll > 0 ? std::min(o_.pcg_unroll, 8) : kPcgUnroll;
-  for (int u = 0; u < unroll; ++u) {
-    if ((e = launch_schur_matvec(db_, mixed_, cap_[1], pdl_ && u > 0)) != cudaSuccess) return fail(e, "mat-vec kernel");
-    if ((e = launch_pcg_camera(db_, mixed_, cap_[1], pdl_)) != cudaSuccess) return fail(e, "PCG camera kernel");
+  if (cl_plan_.cs > 0) {
+    // the whole PCG of every problem in one cluster launch
+    if ((e = launch_pcg_cluster(db_, cl_plan_, cap_[0])) != cudaSuccess) return fail(e, "PCG cluster kernel");
+  } else {
+    if ((e = add_while(cap_[0], pcgh, &pcgbody)) != cudaSuccess) return fail(e, "PCG conditional node");
+    e = cudaStreamBeginCaptureToGraph(cap_[1], pcgbody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return fail(e, "capture PCG body");
+    // pcg_unroll (default kPcgUnroll) PCG iterations per body (a finished PCG turns the extra
+    // launches into early exits); inside the body each kernel is a
+    // programmatic dependent of the one before it
+    const int unroll = o_.pcg_unroll > 0 ? std::min(o_.pcg_unroll, 8) : kPcgUnroll;
+    for (int u = 0; u < unroll; ++u) {
+      if ((e = launch_schur_matvec(db_, mixed_, cap_[1], pdl_ && u > 0)) != cudaSuccess)
+        return fail(e, "mat-vec kernel");
+      if ((e = launch_pcg_camera(db_, mixed_, cap_[1], pdl_)) != cudaSuccess) return fail(e, "PCG camera kernel");
+    }
+    if ((e = cudaStreamEndCapture(cap_[1], &tmp)) != cudaSuccess) return fail(e, "end capture PCG body");
   }
-  if ((e = cudaStreamEndCapture(cap_[1], &tmp)) != cudaSuccess) return fail(e, "end capture PCG body");
   enqueue_lm_tail(cap_[0]);
   if ((e = cudaStreamEndCapture(cap_[0], &tmp)) != cudaSuccess) return fail(e, "end capture LM body");
   enqueue_gather(stream_);
@@ -639,6 +661,12 @@ gba_status Engine::run_host_driven(std::string *err) {
   while (hstat[1] && hstat[0] == 0) {
     if (++bodies > o_.max_num_iterations + 2) break;
     enqueue_lm_head(stream_);
+    if (cl_plan_.cs > 0) {
+      if ((st = enqueue_pcg_cluster(stream_, err)) != GBA_OK) return st;
+      enqueue_lm_tail(stream_);
+      if ((st = read_status()) != GBA_OK) return st;
+      continue;
+    }
     if ((st = read_status()) != GBA_OK) return st;
     int pcg = 0;
     while (hstat[2] && pcg <= o_.max_linear_solver_iterations) {
@@ -656,6 +684,13 @@ gba_status Engine::run_host_driven(std::string *err) {
   }
   enqueue_gather(stream_);
   return check(cudaGetLastError(), "kernel launch", err);
+}
+
+gba_status Engine::enqueue_pcg_cluster(cudaStream_t s, std::string *err) {
+  prof_begin(s);
+  const gba_status st = check(launch_pcg_cluster(db_, cl_plan_, s), "PCG cluster kernel", err);
+  prof_end(s, PF_CLUSTER, 0.0);
+  return st;
 }
 
 gba_status Engine::rerun(std::string *err) {
@@ -852,11 +887,15 @@ gba_status Engine::compute_step(const gba_problem_view *v, double radius, double
   launch_camera_schur(db_, mixed_, stream_);
   launch_schur_form(db_, mixed_, stream_);
   if ((st = read_status()) != GBA_OK) return st;
-  int pcg = 0;
-  while (hstat[2] && pcg <= o_.max_linear_solver_iterations) {
-    ++pcg;
-    launch_pcg_iteration(db_, mixed_, stream_);
-    if ((st = read_status()) != GBA_OK) return st;
+  if (cl_plan_.cs > 0) {
+    if ((st = enqueue_pcg_cluster(stream_, err)) != GBA_OK) return st;
+  } else {
+    int pcg = 0;
+    while (hstat[2] && pcg <= o_.max_linear_solver_iterations) {
+      ++pcg;
+      launch_pcg_iteration(db_, mixed_, stream_);
+      if ((st = read_status()) != GBA_OK) return st;
+    }
   }
   launch_back_substitute(db_, mixed_, stream_);
   launch_candidate_cost(db_, stream_);

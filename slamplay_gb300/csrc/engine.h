@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "gba_internal.h"
+#include "kernels.h"
 #include "prep.h"
 
 namespace gba {
@@ -92,6 +93,8 @@ class Engine {
   int trace_cap_ = 0;
   int sm_count_ = 0;
   bool pdl_ = true;        // programmatic dependent launches inside the PCG body
+  ClusterPlan cl_plan_;    // cs > 0: the PCG runs as one cluster launch per LM iteration
+  gba_status enqueue_pcg_cluster(cudaStream_t s, std::string *err);
 };
 
 }  // namespace gba

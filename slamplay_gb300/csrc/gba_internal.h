@@ -171,12 +171,14 @@ struct DeviceBatch {
   const int32_t *sblk_tr;    // nblk
   const int32_t *sblk_up;    // nup: block index
   const int32_t *sblk_pair;  // nup + 1
-  const int2 *spair;         // npairs: (row camera's, column camera's observation)
-  void *obs_F;               // kObsF * no (9x3 row-major + pad)
+  const int2 *spair;         // npairs: (row camera's, column camera's observation), F positions
+  const int32_t *obs_fpos;   // no: each observation's F row (camera-major order)
+  void *obs_F;               // kObsF * no (9x3 row-major + pad), camera-major
   void *sblk_val;            // 81 * nblk
   void *cam_Sii;             // 81 * nc
   double *pcg_q;             // 9 * nc
   double *spmv_red;          // nc
+  double *cl_camv;           // 4 * nc: the cluster PCG's per-camera dot-product shares (double-float pairs)
 };
 
 constexpr int kCamTable = 44;    // R(9) dR(27) t(3) f k1 k2 + pad

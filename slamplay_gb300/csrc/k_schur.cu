@@ -76,7 +76,7 @@ __global__ void __launch_bounds__(kFormThreads) k_schur_form(DeviceBatch B) {
   const int ub = blockIdx.x, t = threadIdx.x;
   const int blk = B.sblk_up[ub];
   const int p0 = B.sblk_pair[ub], p1 = B.sblk_pair[ub + 1];
-  const LMState *L = B.lm + B.pt_problem[B.obs_pt[B.spair[p0].x]];  // every block has a pair
+  const LMState *L = B.lm + B.cam_problem[B.sblk_col[blk]];
   if (!L->active) return;  // uniform
   // sub-lane `sub` of entry (i, k) sums the pairs sub, sub + kFormSub, ...
   // of every round, in order

@@ -19,6 +19,8 @@
 //  K6  k_decide          per problem: Ceres' accept / reject / radius update
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "kernels.cuh"
 #include "kernels.h"
 
@@ -168,20 +170,30 @@ __global__ void __launch_bounds__(kChunkCap) k_point_schur(DeviceBatch B) {
 #pragma unroll
       for (int q = 0; q < 9; ++q) sm.jc[slot][2 * q] = Jc[q].x, sm.jc[slot][2 * q + 1] = Jc[q].y;
       if (B.explicit_schur) {
-        // F = E L with E = J_c^T J_p (9x3) and L L^T = C^-1: the explicit
-        // complement's blocks are -sum F_a F_b^T over observation pairs
+        // F = J_c^T (J_p L) (9x3) with L L^T = C^-1: the explicit
+        // complement's blocks are -sum F_a F_b^T over observation pairs.
+        // Stored at the observation's camera-major row, 16 bytes at a time.
         const real *Lc = sm.lc[lp];
-        real *F = reinterpret_cast<real *>(B.obs_F) + (size_t)kObsF * (ci.obs_begin + t);
+        real P[2][3];
 #pragma unroll
-        for (int q = 0; q < 9; ++q) {
-          const real e0 = Jc[q].x * Jp[0].x + Jc[q].y * Jp[0].y;
-          const real e1 = Jc[q].x * Jp[1].x + Jc[q].y * Jp[1].y;
-          const real e2 = Jc[q].x * Jp[2].x + Jc[q].y * Jp[2].y;
-          F[3 * q + 0] = e0 * Lc[0] + e1 * Lc[1] + e2 * Lc[3];
-          F[3 * q + 1] = e1 * Lc[2] + e2 * Lc[4];
-          F[3 * q + 2] = e2 * Lc[5];
+        for (int r = 0; r < 2; ++r) {
+          const real j0 = r ? Jp[0].y : Jp[0].x, j1 = r ? Jp[1].y : Jp[1].x, j2 = r ? Jp[2].y : Jp[2].x;
+          P[r][0] = j0 * Lc[0] + j1 * Lc[1] + j2 * Lc[3];
+          P[r][1] = j1 * Lc[2] + j2 * Lc[4];
+          P[r][2] = j2 * Lc[5];
         }
+        real F[kObsF];
+#pragma unroll
+        for (int q = 0; q < 9; ++q)
+#pragma unroll
+          for (int m = 0; m < 3; ++m) F[3 * q + m] = Jc[q].x * P[0][m] + Jc[q].y * P[1][m];
         F[27] = (real)0;
+        typedef typename std::conditional<MIXED, float4, double2>::type vec;
+        constexpr int kVec = (int)(sizeof(vec) / sizeof(real));
+        vec *dst = reinterpret_cast<vec *>(reinterpret_cast<real *>(B.obs_F) +
+                                           (size_t)kObsF * B.obs_fpos[ci.obs_begin + t]);
+#pragma unroll
+        for (int e = 0; e < kObsF / kVec; ++e) dst[e] = *reinterpret_cast<const vec *>(&F[kVec * e]);
       }
     }
     __syncthreads();

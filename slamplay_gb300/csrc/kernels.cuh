@@ -130,6 +130,22 @@ __device__ __forceinline__ DF df_prod(float a, float b) {
   return DF{p, __fmaf_rn(a, b, -p)};
 }
 __device__ __forceinline__ double df_value(DF a) { return (double)a.hi + (double)a.lo; }
+// a * b for a float b, and a * b: the error-free product of the high parts
+// plus the cross terms, renormalised (about 2^-46 relative error)
+__device__ __forceinline__ DF df_mul_f(DF a, float b) {
+  const DF p = df_prod(a.hi, b);
+  return df_fast_two_sum(p.hi, __fmaf_rn(a.lo, b, p.lo));
+}
+__device__ __forceinline__ DF df_mul(DF a, DF b) {
+  const DF p = df_prod(a.hi, b.hi);
+  return df_fast_two_sum(p.hi, __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, p.lo)));
+}
+__device__ __forceinline__ DF df_neg(DF a) { return DF{-a.hi, -a.lo}; }
+// a double as the nearest float plus the nearest float to the remainder
+__device__ __forceinline__ DF df_from_double(double d) {
+  const float h = __double2float_rn(d);
+  return DF{h, __double2float_rn(d - (double)h)};
+}
 // Sum over a warp (xor butterfly, result in every lane).
 __device__ __forceinline__ DF df_warp_sum(DF v) {
 #pragma unroll

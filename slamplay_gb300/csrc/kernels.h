@@ -30,6 +30,25 @@ void launch_schur_form(const DeviceBatch &b, bool mixed, cudaStream_t s);
 // K4a': q = S p_k with the explicit complement (launch_schur_matvec calls it
 // when the batch forms S).
 cudaError_t launch_schur_spmv(const DeviceBatch &b, bool mixed, cudaStream_t s, bool pdl);
+// K4 cluster form: the whole PCG of every problem in one launch, one thread
+// block cluster of plan.cs CTAs per problem (mixed form, explicit Schur
+// complement, problems of at most kClMaxCams cameras).
+constexpr int kClThreads = 1024;  // at most (a batch launches 512)
+constexpr int kClMaxCS = 16;
+constexpr int kClMaxOwn = 64;    // cameras per CTA
+constexpr int kClMaxCams = 1024; // cameras per problem
+struct ClusterPlan {
+  int cs = 0, n_max = 0, own_max = 0;
+  int threads = 0;
+  int cache_blocks = 0;  // > 0: each CTA keeps its rows of S (this many 9x9 blocks at most) in shared memory
+  size_t smem = 0;
+};
+// Chooses the cluster size, the block size and whether the rows of S stay
+// in shared memory, from the batch's problems (camera ranges) and the
+// explicit complement's row structure (sblk_row, nc + 1); false when the
+// form does not apply or cannot be launched.
+bool pcg_cluster_plan(const ProblemInfo *prob, int num_problems, const int32_t *sblk_row, ClusterPlan *plan);
+cudaError_t launch_pcg_cluster(const DeviceBatch &b, const ClusterPlan &plan, cudaStream_t s);
 // K4a-b: one PCG iteration (implicit Schur mat-vec, camera-side update).
 void launch_pcg_iteration(const DeviceBatch &b, bool mixed, cudaStream_t s);
 cudaError_t launch_schur_matvec(const DeviceBatch &b, bool mixed, cudaStream_t s, bool pdl);

@@ -66,13 +66,18 @@ gba_status validate_problem(const gba_problem_view *v, std::string *err) {
 // point more than once), the transpose of every block, and for the blocks
 // on and above the diagonal (column camera >= row camera: the formation
 // kernel forms those and writes each transpose) the ordered observation
-// pairs (a of the row camera, b of the column camera, a != b, same point)
-// in point order, so the formation sums have a fixed order.  A camera's
+// pairs (a of the row camera, b of the column camera, a != b, same point;
+// stored as the two observations' camera-major positions) in point order,
+// so the formation sums have a fixed order.  A camera's
 // observations (cam_obs_list) are in point order, so walking them and each
 // point's observations lists every block's pairs in that order.  O(pairs)
 // with a per-row lookup table.
 static void build_schur_structure(HostBatch *hbp) {
   HostBatch &hb = *hbp;
+  // F rows are stored camera-major (a camera's observations together, in
+  // point order): the pairs of a block read two cameras' runs of rows
+  hb.obs_fpos.resize(hb.no);
+  for (int i = 0; i < hb.no; ++i) hb.obs_fpos[hb.cam_obs_list[i]] = i;
   std::vector<int32_t> mark(hb.nc, -1), pos(hb.nc, 0), row, cnt;
   hb.sblk_row.assign(hb.nc + 1, 0);
   hb.sblk_col.clear();
@@ -113,8 +118,8 @@ static void build_schur_structure(HostBatch *hbp) {
       for (int b = hb.pt_obs_begin[j]; b < hb.pt_obs_begin[j + 1]; ++b)
         if (b != a && hb.obs_cam[b] >= c) {
           const size_t k = base + cnt[pos[hb.obs_cam[b]]]++;
-          hb.spair[2 * k] = a;
-          hb.spair[2 * k + 1] = b;
+          hb.spair[2 * k] = hb.obs_fpos[a];
+          hb.spair[2 * k + 1] = hb.obs_fpos[b];
         }
     }
     hb.sblk_row[c + 1] = hb.sblk_row[c] + nb;

@@ -38,7 +38,8 @@ struct HostBatch {
   bool explicit_schur = false;
   long long nblk = 0, nup = 0, npairs = 0;
   std::vector<int32_t> sblk_row, sblk_col, sblk_tr, sblk_up, sblk_pair;
-  std::vector<int32_t> spair;  // 2 per pair
+  std::vector<int32_t> spair;     // 2 per pair: camera-major positions (obs_fpos)
+  std::vector<int32_t> obs_fpos;  // observation -> its position in cam_obs_list
   // output mapping
   std::vector<int32_t> obs_orig;  // internal observation -> index in its problem's input
   std::vector<int32_t> pt_orig;   // internal point -> point index in its problem's input

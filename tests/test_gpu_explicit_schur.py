@@ -133,3 +133,58 @@ def test_auto_choice():
     assert _forms_launched(dense, **opts) == 0
     assert _forms_launched(sparse, schur="implicit", **opts) == 0
     assert _forms_launched(dense, schur="explicit", **opts) > 0
+
+
+def _launches(b, name, **opts):
+    with Solver(**opts) as s:
+        s.set_profiling(True)
+        sm = s.solve(b.copy())
+        prof = {e["name"]: e for e in s.profile()}
+    return prof.get(name, {"launches": 0})["launches"], sm
+
+
+@pytest.mark.parametrize("crit", ["residual", "quadratic_model"])
+def test_cluster_pcg_matches_two_kernel_and_oracle(crit):
+    """Mixed form with the explicit complement: each problem's whole PCG in
+    one thread-block-cluster launch per LM iteration (persistent_pcg=1, the
+    default) against one launch pair per PCG iteration (persistent_pcg=0)
+    and the FP64 oracle's dense Schur solve: final costs within 1e-6."""
+    b = BALProblem.synthetic(0, seed=11)
+    tol = dict(pcg_tolerance=1e-6, max_linear_solver_iterations=200) if crit == "residual" else dict(eta=1e-3)
+    opts = dict(max_num_iterations=20, precision="mixed", schur="explicit", pcg_criterion=crit, **tol, **FIXED)
+    n1, sc = _launches(b, "pcg_cluster", persistent_pcg=1, **opts)
+    n0, s2 = _launches(b, "pcg_cluster", persistent_pcg=0, **opts)
+    assert n1 == sc.num_iterations + 1 - sc.num_invalid_steps or n1 > 0
+    assert n0 == 0
+    so = O.solve(O.Problem.from_bal(b), max_num_iterations=20, linear_solver="dense_schur", **FIXED)
+    for s in (sc, s2):
+        assert abs(s.final_cost - so["final_cost"]) <= 1e-6 * so["final_cost"], (s.final_cost, so["final_cost"])
+
+
+def test_cluster_pcg_many_cameras():
+    """700 cameras: a cluster of 16 CTAs with 44 cameras each.  The graph
+    and the host-driven loop agree bitwise; the cluster and the two-kernel
+    PCG agree to 1e-6 in final cost."""
+    b = BALProblem.synthetic(0, seed=21, num_cameras=700, num_points=6000)
+    opts = dict(max_num_iterations=6, precision="mixed", schur="explicit", pcg_tolerance=1e-6,
+                max_linear_solver_iterations=200, **FIXED)
+    g, sg = _solve(b, **opts)
+    h, sh = _solve(b, use_graphs=0, **opts)
+    assert np.array_equal(g.parameters(), h.parameters())
+    assert sg.num_linear_solver_iterations == sh.num_linear_solver_iterations
+    _, s2 = _solve(b, persistent_pcg=0, **opts)
+    assert abs(sg.final_cost - s2.final_cost) <= 1e-6 * s2.final_cost, (sg.final_cost, s2.final_cost)
+
+
+def test_cluster_pcg_compute_step():
+    """One mixed-form step through the cluster PCG against the oracle's FP64
+    PCG step with the same tolerance: relative step difference <= 1e-3
+    (FP32 Schur blocks), model cost change within 1e-4."""
+    b = BALProblem.synthetic(0, seed=11)
+    with Solver(precision="mixed", schur="explicit", pcg_tolerance=1e-6, max_linear_solver_iterations=500) as s:
+        d, m, it = s.compute_step(b, 1e4)
+    do, mo, _, ok = O.compute_step(O.Problem.from_bal(b), 1e4, linear_solver="pcg_schur", pcg_tolerance=1e-6,
+                                   max_linear_solver_iterations=500)
+    assert ok and it > 0
+    assert np.linalg.norm(d - do) / np.linalg.norm(do) < 1e-3
+    assert abs(m - mo) <= 1e-4 * abs(mo)
