@@ -12,8 +12,9 @@
 // direction is FP32 (the product's input) and the same FP32 values enter
 // p.q and the update of x, so the curvature p.Sp and the recurrences refer
 // to the direction the product used.  Per iteration:
-//   1. q = S p for the owned rows (FP32 products and per-lane sums, double-
-//      float across the lanes) and each owned camera's p.q; barrier
+//   1. q = S p for the owned rows (FP32 products and per-thread sums,
+//      double-float across the threads of a row) and each owned camera's
+//      p.q; barrier
 //   2. p.q over the problem's cameras, alpha; x, r and z = M r of the owned
 //      cameras, each owned camera's r.z, r.r, x.(v + r); barrier
 //   3. the stopping test and beta from the cameras' values, p_{k+1} =
@@ -45,7 +46,7 @@ namespace gba {
 
 namespace {
 
-constexpr int kClSub = 4;  // lanes per row of the product
+constexpr int kClSub = 8;  // lanes per (camera, row triplet) of the product
 
 // Shared-memory layout (bytes), the same on the host and the device.
 struct ClLayout {
@@ -57,7 +58,7 @@ __host__ __device__ inline ClLayout cl_layout(int n_max, int own_max, int cache_
   size_t o = 0;
   const size_t nf = 4 * 9 * (size_t)n_max, of = 4 * 9 * (size_t)own_max;
   l.zf = o, o = cl_align(o + nf);
-  l.ph = o, o = cl_align(o + nf);
+  l.ph = o, o = cl_align(o + 4 * 12 * (size_t)n_max);  // p, 12 floats per camera (three 16-byte loads)
   l.mo = o, o = cl_align(o + 4 * 81 * (size_t)own_max);
   l.xh = o, o = cl_align(o + of);
   l.xl = o, o = cl_align(o + of);
@@ -72,7 +73,8 @@ __host__ __device__ inline ClLayout cl_layout(int n_max, int own_max, int cache_
   // block, per block its column camera (in the problem) and its 81 values
   l.boff = o, o = cl_align(o + (cache_blocks > 0 ? 4 * ((size_t)own_max + 1) : 0));
   l.scol = o, o = cl_align(o + 4 * (size_t)cache_blocks);
-  l.sval = o, o = cl_align(o + 4 * 81 * (size_t)cache_blocks);
+  // per block three row triplets (rows g, g + 3, g + 6) of 27 values + pad
+  l.sval = o, o = cl_align(o + 4 * 84 * (size_t)cache_blocks);
   l.total = o;
   return l;
 }
@@ -144,8 +146,22 @@ __global__ void __launch_bounds__(kClThreads, 1) k_pcg_cluster(DeviceBatch B, in
   if (!(L->active && L->pcg_active)) return;
   const ProblemInfo pi = B.prob[prob];
   const int n = pi.cam_count, c0 = pi.cam_begin;
-  const int per = (n + cs - 1) / cs;
-  const int own0 = min(n, rank * per), own_n = min(per, n - own0);
+  // the cameras split into cs runs of about equal blocks of S (the
+  // product's work): CTA `rank` owns the cameras whose blocks before them
+  // (with the diagonal ones) lie in [bound(rank), bound(rank + 1))
+  int own0 = 0, own_end = 0;
+  {
+    const int r0 = B.sblk_row[c0];
+    const long long wtot = (long long)(B.sblk_row[c0 + n] - r0) + n;
+    const long long ta = ((long long)rank * wtot + cs - 1) / cs, tb = ((long long)(rank + 1) * wtot + cs - 1) / cs;
+    for (int cb = 0; cb < n; cb += T) {
+      const int c = cb + t;
+      const long long before = c < n ? (long long)(B.sblk_row[c0 + c] - r0) + c : wtot;
+      own0 += __syncthreads_count(before < ta);
+      own_end += __syncthreads_count(before < tb);
+    }
+  }
+  const int own_n = own_end - own0;
   const int n9 = 9 * n, o9 = 9 * own_n, a9 = 9 * own0;  // a9: first owned coordinate in the problem
   const size_t g0 = 9 * (size_t)c0;                       // the problem's first coordinate (global)
   float *zx = B.pcg_zf + g0;                              // z exchange (the problem's coordinates)
@@ -154,7 +170,7 @@ __global__ void __launch_bounds__(kClThreads, 1) k_pcg_cluster(DeviceBatch B, in
   // the start (K3b): x = 0, r = v, z = M r, p_0 = z
   for (int i = t; i < n9; i += T) {
     const float z = zx[i];
-    zf[i] = z, ph[i] = z;
+    zf[i] = z, ph[i + 3 * (i / 9)] = z;
   }
   for (int i = t; i < o9; i += T) {
     const DF v = df_from_double(B.pcg_v[g0 + a9 + i]);
@@ -184,8 +200,16 @@ __global__ void __launch_bounds__(kClThreads, 1) k_pcg_cluster(DeviceBatch B, in
       const int c = c0 + own0 + lc;
       const int r0 = B.sblk_row[c], nb = B.sblk_row[c + 1] - r0, b0 = boff[lc];
       for (int v = t; v <= nb; v += T) scol[b0 + v] = (v < nb ? B.sblk_col[r0 + v] : c) - c0;
-      for (int e = t; e < 81 * nb; e += T) sval[81 * (size_t)b0 + e] = vals[81 * (size_t)r0 + e];
-      for (int e = t; e < 81; e += T) sval[81 * (size_t)(b0 + nb) + e] = Sii[81 * (size_t)c + e];
+      // triplet layout: block b, triplet g, entry j = row (g + 3 (j / 9)), column j % 9
+      for (int e = t; e < 84 * (nb + 1); e += T) {
+        const int v = e / 84, w = e - 84 * v, g = w / 28, j = w - 28 * g;
+        float x = 0.f;
+        if (j < 27) {
+          const int el = 9 * (g + 3 * (j / 9)) + j % 9;
+          x = v < nb ? vals[81 * (size_t)(r0 + v) + el] : Sii[81 * (size_t)c + el];
+        }
+        sval[84 * (size_t)(b0 + v) + w] = x;
+      }
     }
   }
   const DeviceOptions &o = B.opt;
@@ -205,41 +229,60 @@ __global__ void __launch_bounds__(kClThreads, 1) k_pcg_cluster(DeviceBatch B, in
   const unsigned hmask = 0xffffu << (t & 16);
   __syncthreads();
   for (;;) {
-    // 1. q = S p_k for the owned rows: kClSub lanes per row over the row's
-    // blocks (the last one the diagonal block), a butterfly over the lanes
-    for (int rs = t / kClSub; rs < o9; rs += T / kClSub) {
-      const int lc = rs / 9, q = rs - 9 * lc;
+    // 1. q = S p_k for the owned rows: a thread takes rows g, g + 3, g + 6
+    // of a camera (one load of p per block for three rows) for the blocks
+    // lane, lane + kClSub, ... of the row (the last one the diagonal
+    // block); FP32 sums per thread, double-float over the kClSub lanes
+    for (int ws = t / kClSub; ws < 3 * own_n; ws += T / kClSub) {
+      const int lc = ws / 3, g = ws - 3 * lc;
       const int c = c0 + own0 + lc;
-      // per block an FP32 dot product, summed over the blocks in
-      // double-float (the diagonal and off-diagonal terms cancel strongly)
-      DF d = df_zero();
+      float a0 = 0.f, a1 = 0.f, a2 = 0.f;
       if (cached) {
         const int b0 = boff[lc], nb1 = boff[lc + 1] - b0;
         for (int v = lane; v < nb1; v += kClSub) {
-          const float *row = sval + 81 * (b0 + v) + 9 * q;
-          const float *pc = ph + 9 * scol[b0 + v];
-          float a = 0.f;
+          // the triplet's 27 values and the column camera's p: 16-byte loads
+          const float4 *r4 = reinterpret_cast<const float4 *>(sval + 84 * (b0 + v) + 28 * g);
+          const float4 *p4 = reinterpret_cast<const float4 *>(ph + 12 * scol[b0 + v]);
+          float rv[28], pv[12];
 #pragma unroll
-          for (int cc = 0; cc < 9; ++cc) a = __fmaf_rn(row[cc], pc[cc], a);
-          d = df_add(d, DF{a, 0.f});
+          for (int u = 0; u < 7; ++u) *reinterpret_cast<float4 *>(&rv[4 * u]) = r4[u];
+#pragma unroll
+          for (int u = 0; u < 3; ++u) *reinterpret_cast<float4 *>(&pv[4 * u]) = p4[u];
+#pragma unroll
+          for (int cc = 0; cc < 9; ++cc) {
+            a0 = __fmaf_rn(rv[cc], pv[cc], a0);
+            a1 = __fmaf_rn(rv[9 + cc], pv[cc], a1);
+            a2 = __fmaf_rn(rv[18 + cc], pv[cc], a2);
+          }
         }
       } else {
         const int r0 = B.sblk_row[c], nb = B.sblk_row[c + 1] - r0;
         for (int v = lane; v <= nb; v += kClSub) {
-          const float *row = v < nb ? vals + 81 * (size_t)(r0 + v) + 9 * q : Sii + 81 * (size_t)c + 9 * q;
-          const float *pc = ph + 9 * ((v < nb ? B.sblk_col[r0 + v] : c) - c0);
-          float a = 0.f;
+          const float *row = (v < nb ? vals + 81 * (size_t)(r0 + v) : Sii + 81 * (size_t)c) + 9 * g;
+          const float *pc = ph + 12 * ((v < nb ? B.sblk_col[r0 + v] : c) - c0);
 #pragma unroll
-          for (int cc = 0; cc < 9; ++cc) a = __fmaf_rn(row[cc], pc[cc], a);
-          d = df_add(d, DF{a, 0.f});
+          for (int cc = 0; cc < 9; ++cc) {
+            const float pv = pc[cc];
+            a0 = __fmaf_rn(row[cc], pv, a0);
+            a1 = __fmaf_rn(row[27 + cc], pv, a1);
+            a2 = __fmaf_rn(row[54 + cc], pv, a2);
+          }
         }
       }
+      DF d0{a0, 0.f}, d1{a1, 0.f}, d2{a2, 0.f};
 #pragma unroll
       for (int off = 1; off < kClSub; off <<= 1) {
-        const DF w{__shfl_xor_sync(gmask, d.hi, off), __shfl_xor_sync(gmask, d.lo, off)};
-        d = df_add(d, w);
+        const DF w0{__shfl_xor_sync(gmask, d0.hi, off), __shfl_xor_sync(gmask, d0.lo, off)};
+        const DF w1{__shfl_xor_sync(gmask, d1.hi, off), __shfl_xor_sync(gmask, d1.lo, off)};
+        const DF w2{__shfl_xor_sync(gmask, d2.hi, off), __shfl_xor_sync(gmask, d2.lo, off)};
+        d0 = df_add(d0, w0), d1 = df_add(d1, w1), d2 = df_add(d2, w2);
       }
-      if (lane == 0) qh[rs] = d.hi, ql[rs] = d.lo;
+      if (lane == 0) {
+        const int i = 9 * lc + g;
+        qh[i] = d0.hi, ql[i] = d0.lo;
+        qh[i + 3] = d1.hi, ql[i + 3] = d1.lo;
+        qh[i + 6] = d2.hi, ql[i + 6] = d2.lo;
+      }
     }
     __syncthreads();
     // each owned camera's p.q
@@ -248,7 +291,7 @@ __global__ void __launch_bounds__(kClThreads, 1) k_pcg_cluster(DeviceBatch B, in
       DF d = df_zero();
       if (lc < own_n && hq < 9) {
         const int i = 9 * lc + hq;
-        d = df_mul_f(DF{qh[i], ql[i]}, ph[a9 + i]);
+        d = df_mul_f(DF{qh[i], ql[i]}, ph[12 * (own0 + lc) + hq]);
       }
       d = df_group16_sum(d, hmask);
       if (lc < own_n && hq == 0) camx[4 * (own0 + lc)] = make_float2(d.hi, d.lo);
@@ -278,7 +321,7 @@ __global__ void __launch_bounds__(kClThreads, 1) k_pcg_cluster(DeviceBatch B, in
         const int i = 9 * lc + hq;
         DF r = df_zero(), x = df_zero();
         if (act) {
-          x = df_add(DF{xh[i], xl[i]}, df_mul_f(alpha, ph[a9 + i]));
+          x = df_add(DF{xh[i], xl[i]}, df_mul_f(alpha, ph[12 * (own0 + lc) + hq]));
           r = df_add(DF{rh[i], rl[i]}, df_mul(nalpha, DF{qh[i], ql[i]}));
           xh[i] = x.hi, xl[i] = x.lo;
           rh[i] = r.hi, rl[i] = r.lo;
@@ -307,10 +350,30 @@ __global__ void __launch_bounds__(kClThreads, 1) k_pcg_cluster(DeviceBatch B, in
     }
     cl.sync();
     // 3. the stopping test on (x_{k+1}, r_{k+1}) and beta_{k+1}; the new z
-    for (int i = t; i < n9; i += T) zf[i] = __ldcg(zx + i);
-    for (int e = t; e < 3 * n; e += T) {
-      const int c = e / 3, j = 1 + e - 3 * c;
-      cvs[4 * c + j] = __ldcg(camx + 4 * c + j);
+    // (four loads in flight per thread: one L2 round trip for most sizes)
+    for (int i0 = 0; i0 < n9; i0 += 4 * T) {
+      float zv[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int i = i0 + u * T + t;
+        zv[u] = i < n9 ? __ldcg(zx + i) : 0.f;
+      }
+      float2 cv[3];
+#pragma unroll
+      for (int u = 0; u < 3; ++u) {
+        const int e = (i0 / (4 * T)) * 3 * T + u * T + t;  // the cameras' slots 1..3: 3 T per round
+        cv[u] = e < 3 * n ? __ldcg(camx + 4 * (e / 3) + 1 + e % 3) : make_float2(0.f, 0.f);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int i = i0 + u * T + t;
+        if (i < n9) zf[i] = zv[u];
+      }
+#pragma unroll
+      for (int u = 0; u < 3; ++u) {
+        const int e = (i0 / (4 * T)) * 3 * T + u * T + t;
+        if (e < 3 * n) cvs[4 * (e / 3) + 1 + e % 3] = cv[u];
+      }
     }
     __syncthreads();
     if (t < 96) {  // warps 0, 1, 2: r.z, r.r, x.(v + r)
@@ -346,7 +409,10 @@ __global__ void __launch_bounds__(kClThreads, 1) k_pcg_cluster(DeviceBatch B, in
     {
       // p_{k+1} = z_{k+1} + beta p_k, rounded once to FP32
       const DF beta = scf[0];
-      for (int i = t; i < n9; i += T) ph[i] = df_add(DF{zf[i], 0.f}, df_mul_f(beta, ph[i])).hi;
+      for (int i = t; i < n9; i += T) {
+        const int ip = i + 3 * (i / 9);
+        ph[ip] = df_add(DF{zf[i], 0.f}, df_mul_f(beta, ph[ip])).hi;
+      }
     }
     __syncthreads();
   }
@@ -356,7 +422,7 @@ __global__ void __launch_bounds__(kClThreads, 1) k_pcg_cluster(DeviceBatch B, in
     B.pcg_x[gi] = df_value(DF{xh[i], xl[i]});
     B.pcg_r[gi] = df_value(DF{rh[i], rl[i]});
     B.pcg_z[gi] = (double)zf[a9 + i];
-    B.pcg_p[gi] = (double)ph[a9 + i];
+    B.pcg_p[gi] = (double)ph[12 * own0 + i + 3 * (i / 9)];
   }
   if (rank == 0 && t == 0) {
     L->pcg_iterations = k;
@@ -385,27 +451,32 @@ bool pcg_cluster_plan(const ProblemInfo *prob, int num_problems, const int32_t *
   const int target = single ? 16 : 64;
   int cs = 1;
   while (cs < kClMaxCS && (n_max + cs - 1) / cs > target) cs *= 2;
-  const int own = (n_max + cs - 1) / cs;
-  if (own > kClMaxOwn) return false;
-  const int threads = single ? 1024 : 512;
+  const int threads = 512;
   // the rows of S stay in shared memory when the CTAs of the launch fit on
   // the SMs one per SM and their rows fit next to the vectors
   int dev = 0, sms = 0, optin = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  int cache = 0;
-  if ((long long)num_problems * cs <= sms) {
-    int mb = 0;
-    for (int p = 0; p < num_problems; ++p) {
-      const int n = prob[p].cam_count, c0 = prob[p].cam_begin, per = (n + cs - 1) / cs;
-      for (int r = 0; r < cs; ++r) {
-        const int a = std::min(n, r * per), b = std::min(n, a + per);
-        mb = std::max(mb, (int)(sblk_row[c0 + b] - sblk_row[c0 + a]) + (b - a));
-      }
+  // the kernel's split of each problem's cameras (runs of about equal
+  // blocks): the largest run and its blocks
+  int own = 0, mb = 0;
+  for (int p = 0; p < num_problems; ++p) {
+    const int n = prob[p].cam_count, c0 = prob[p].cam_begin, r0 = sblk_row[c0];
+    const long long wtot = (long long)(sblk_row[c0 + n] - r0) + n;
+    int a = 0;
+    for (int r = 0; r < cs; ++r) {
+      const long long tb = ((long long)(r + 1) * wtot + cs - 1) / cs;
+      int b = a;
+      while (b < n && (long long)(sblk_row[c0 + b] - r0) + b < tb) ++b;
+      own = std::max(own, b - a);
+      mb = std::max(mb, (int)(sblk_row[c0 + b] - sblk_row[c0 + a]) + (b - a));
+      a = b;
     }
-    if (cl_layout(n_max, own, mb).total <= (size_t)optin) cache = mb;
   }
+  if (own > kClMaxOwn) return false;
+  int cache = 0;
+  if ((long long)num_problems * cs <= sms && cl_layout(n_max, own, mb).total <= (size_t)optin) cache = mb;
   const ClLayout l = cl_layout(n_max, own, cache);
   if (l.total > (size_t)optin) return false;
   if (cudaFuncSetAttribute(k_pcg_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)l.total) != cudaSuccess ||

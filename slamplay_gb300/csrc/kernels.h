@@ -33,7 +33,7 @@ cudaError_t launch_schur_spmv(const DeviceBatch &b, bool mixed, cudaStream_t s, 
 // K4 cluster form: the whole PCG of every problem in one launch, one thread
 // block cluster of plan.cs CTAs per problem (mixed form, explicit Schur
 // complement, problems of at most kClMaxCams cameras).
-constexpr int kClThreads = 1024;  // at most (a batch launches 512)
+constexpr int kClThreads = 512;
 constexpr int kClMaxCS = 16;
 constexpr int kClMaxOwn = 64;    // cameras per CTA
 constexpr int kClMaxCams = 1024; // cameras per problem
