@@ -155,14 +155,18 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
-def launches_per_solve(s) -> int:
+def launches_per_solve(s, prof_launches: dict) -> int:
     """Kernels of one solve: setup (parameter sync, LM state, camera table,
     two evaluations of two kernels each, Jacobi scale, post-evaluation) and
     the gather = 10; per LM iteration point/Schur chunk, camera Schur, back-
     substitution, candidate cameras, candidate cost, decide, camera table,
-    evaluation (chunk + camera), post-evaluation = 10; per PCG iteration the
-    mat-vec and the camera-side kernel = 2."""
-    return 10 + 10 * s.num_iterations + 2 * s.num_linear_solver_iterations
+    evaluation (chunk + camera), post-evaluation = 10, + 1 for the formation
+    of the explicit Schur complement; the PCG either as one cluster launch
+    per LM iteration or as two kernels per PCG iteration.  prof_launches:
+    launches per profile entry of a host-driven pass of the same solve."""
+    per_lm = 10 + (1 if prof_launches.get("schur_form") else 0)
+    pcg = prof_launches.get("pcg_cluster") or 2 * s.num_linear_solver_iterations
+    return 10 + per_lm * s.num_iterations + pcg
 
 
 def ncu_traffic(kernel: str):
@@ -300,7 +304,10 @@ def run_gpu(args) -> None:
             "roofline": roof,
             "kernels": prof,
             "cpu_baseline": cb,
-            "gpu_launches": args.steps * launches_per_solve(first_m),
+            "gpu_launches": args.steps * launches_per_solve(first_m, {e["name"]: e["launches"] for e in prof}),
+            "linear_solver": {"schur": "explicit" if any(e["name"] == "schur_form" for e in prof) else "implicit",
+                              "pcg": "cluster (one launch per LM iteration)"
+                              if any(e["name"] == "pcg_cluster" for e in prof) else "two kernels per PCG iteration"},
             "clocks": clk,
             "wall_s_timed": t_wall1 - t_wall0,
         }
@@ -483,11 +490,14 @@ def run_profile_solve(args) -> None:
 
     problem = BALProblem.synthetic(args.config, seed=0)
     opts = workload_options(args.precision)
+    opts["schur"] = args.schur
+    opts["persistent_pcg"] = args.persistent_pcg
     if args.lm_iterations:
         opts["max_num_iterations"] = args.lm_iterations
     with Solver(use_graphs=0, **opts) as s:
         sm = s.solve(problem.copy())
-    print(json.dumps({"precision": args.precision, "lm_iterations": sm.num_iterations,
+    print(json.dumps({"precision": args.precision, "schur": args.schur, "persistent_pcg": args.persistent_pcg,
+                      "lm_iterations": sm.num_iterations,
                       "pcg_iterations": sm.num_linear_solver_iterations, "final_cost": sm.final_cost}), flush=True)
 
 
@@ -502,6 +512,10 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--config", type=int, default=1, choices=[0, 1, 2],
                     help="with --profile-solve: the synthetic configuration to solve")
+    ap.add_argument("--schur", default="auto", choices=["auto", "implicit", "explicit"],
+                    help="with --profile-solve: the Schur complement form (gba_options.schur)")
+    ap.add_argument("--persistent-pcg", type=int, default=1, choices=[0, 1],
+                    help="with --profile-solve: the cluster PCG (1) or two kernels per PCG iteration (0)")
     ap.add_argument("--lm-iterations", type=int, default=0,
                     help="with --profile-solve: LM iterations (0 = the workload's 50)")
     ap.add_argument("--no-extra-forms", action="store_true",

@@ -686,10 +686,18 @@ gba_status Engine::run_host_driven(std::string *err) {
   return check(cudaGetLastError(), "kernel launch", err);
 }
 
+// Algorithmic bytes of one cluster-PCG launch: the blocks of S (off-diagonal
+// and diagonal) and M^-1 once (FP32), v, r, z in and x, r, z, p out per
+// camera coordinate (FP64), z in FP32; the exchanges between the CTAs stay
+// in L2.
+static double bytes_pcg_cluster(const DeviceBatch &b) {
+  return ((double)b.nblk + b.nc) * 81.0 * 4.0 + (double)b.nc * 81.0 * 4.0 + (double)b.nc * 9.0 * (3 * 8.0 + 4.0 + 4 * 8.0);
+}
+
 gba_status Engine::enqueue_pcg_cluster(cudaStream_t s, std::string *err) {
   prof_begin(s);
   const gba_status st = check(launch_pcg_cluster(db_, cl_plan_, s), "PCG cluster kernel", err);
-  prof_end(s, PF_CLUSTER, 0.0);
+  prof_end(s, PF_CLUSTER, bytes_pcg_cluster(db_));
   return st;
 }
 
