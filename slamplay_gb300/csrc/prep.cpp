@@ -9,6 +9,9 @@
 // observations.  All orderings are deterministic functions of the input.
 #include "prep.h"
 
+#include <functional>
+#include <thread>
+
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -68,73 +71,112 @@ gba_status validate_problem(const gba_problem_view *v, std::string *err) {
 // kernel forms those and writes each transpose) the ordered observation
 // pairs (a of the row camera, b of the column camera, a != b, same point;
 // stored as the two observations' camera-major positions) in point order,
-// so the formation sums have a fixed order.  A camera's
-// observations (cam_obs_list) are in point order, so walking them and each
-// point's observations lists every block's pairs in that order.  O(pairs)
-// with a per-row lookup table.
+// so the formation sums have a fixed order.  A camera's observations
+// (cam_obs_list) are in point order, so walking them and each point's
+// observations lists every block's pairs in that order.  O(pairs) with a
+// per-row lookup table; the rows are independent, so host threads take runs
+// of rows (the result does not depend on the thread count).
 static void build_schur_structure(HostBatch *hbp) {
   HostBatch &hb = *hbp;
+  const int nc = hb.nc;
   // F rows are stored camera-major (a camera's observations together, in
   // point order): the pairs of a block read two cameras' runs of rows
   hb.obs_fpos.resize(hb.no);
   for (int i = 0; i < hb.no; ++i) hb.obs_fpos[hb.cam_obs_list[i]] = i;
-  std::vector<int32_t> mark(hb.nc, -1), pos(hb.nc, 0), row, cnt;
-  hb.sblk_row.assign(hb.nc + 1, 0);
-  hb.sblk_col.clear();
-  hb.sblk_up.clear();
-  hb.sblk_pair.assign(1, 0);
-  hb.spair.clear();
-  for (int c = 0; c < hb.nc; ++c) {
-    const int a0 = hb.cam_obs_begin[c], a1 = hb.cam_obs_begin[c + 1];
-    row.clear();
-    for (int ia = a0; ia < a1; ++ia) {
-      const int a = hb.cam_obs_list[ia], j = hb.obs_pt[a];
-      for (int b = hb.pt_obs_begin[j]; b < hb.pt_obs_begin[j + 1]; ++b) {
-        const int k = hb.obs_cam[b];
-        if (b != a && mark[k] != c) mark[k] = c, row.push_back(k);
+  std::vector<std::vector<int32_t>> rows(nc), cnts(nc);  // per row: columns; pair counts of its upper blocks
+  std::vector<int32_t> first_up(nc, 0);                  // per row: index of its first column >= the row
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const int nth = (int)std::min<long long>(std::min(hw, 32u), std::max<long long>(1, (long long)hb.no / 20000));
+  auto for_rows = [&](const std::function<void(int, int, std::vector<int32_t> &, std::vector<int32_t> &)> &fn) {
+    std::vector<std::thread> th;
+    for (int w = 0; w < nth; ++w) {
+      const int c0 = (int)((long long)nc * w / nth), c1 = (int)((long long)nc * (w + 1) / nth);
+      th.emplace_back([&, c0, c1] {
+        std::vector<int32_t> mark(nc, -1), pos(nc, 0);
+        fn(c0, c1, mark, pos);
+      });
+    }
+    for (auto &x : th) x.join();
+  };
+  // 1. per row: sorted co-visible cameras, pair counts of the upper blocks
+  for_rows([&](int c0, int c1, std::vector<int32_t> &mark, std::vector<int32_t> &pos) {
+    for (int c = c0; c < c1; ++c) {
+      const int a0 = hb.cam_obs_begin[c], a1 = hb.cam_obs_begin[c + 1];
+      std::vector<int32_t> &row = rows[c];
+      for (int ia = a0; ia < a1; ++ia) {
+        const int a = hb.cam_obs_list[ia], j = hb.obs_pt[a];
+        for (int b = hb.pt_obs_begin[j]; b < hb.pt_obs_begin[j + 1]; ++b) {
+          const int k = hb.obs_cam[b];
+          if (b != a && mark[k] != c) mark[k] = c, row.push_back(k);
+        }
+      }
+      std::sort(row.begin(), row.end());
+      const int nb = (int)row.size();
+      const int u0 = (int)(std::lower_bound(row.begin(), row.end(), c) - row.begin());
+      first_up[c] = u0;
+      std::vector<int32_t> &cnt = cnts[c];
+      cnt.assign(nb - u0, 0);
+      for (int u = u0; u < nb; ++u) pos[row[u]] = u - u0;
+      for (int ia = a0; ia < a1; ++ia) {
+        const int a = hb.cam_obs_list[ia], j = hb.obs_pt[a];
+        for (int b = hb.pt_obs_begin[j]; b < hb.pt_obs_begin[j + 1]; ++b)
+          if (b != a && hb.obs_cam[b] >= c) ++cnt[pos[hb.obs_cam[b]]];
       }
     }
-    std::sort(row.begin(), row.end());
-    const int nb = (int)row.size();
-    const int u0 = (int)(std::lower_bound(row.begin(), row.end(), c) - row.begin());  // first column >= c
-    const int nu = nb - u0;
-    cnt.assign(nu + 1, 0);
-    for (int u = u0; u < nb; ++u) pos[row[u]] = u - u0;
-    for (int ia = a0; ia < a1; ++ia) {
-      const int a = hb.cam_obs_list[ia], j = hb.obs_pt[a];
-      for (int b = hb.pt_obs_begin[j]; b < hb.pt_obs_begin[j + 1]; ++b)
-        if (b != a && hb.obs_cam[b] >= c) ++cnt[pos[hb.obs_cam[b]] + 1];
+  });
+  // 2. prefix sums: the CSR, the upper blocks, their pair ranges
+  hb.sblk_row.assign(nc + 1, 0);
+  for (int c = 0; c < nc; ++c) hb.sblk_row[c + 1] = hb.sblk_row[c] + (int32_t)rows[c].size();
+  hb.nblk = hb.sblk_row[nc];
+  hb.sblk_col.resize(hb.nblk);
+  hb.sblk_up.clear();
+  hb.sblk_pair.assign(1, 0);
+  std::vector<long long> up_begin(nc + 1, 0);  // per row: its first upper block (index into sblk_up)
+  for (int c = 0; c < nc; ++c) {
+    std::copy(rows[c].begin(), rows[c].end(), hb.sblk_col.begin() + hb.sblk_row[c]);
+    up_begin[c] = (long long)hb.sblk_up.size();
+    for (size_t u = 0; u < cnts[c].size(); ++u) {
+      hb.sblk_up.push_back(hb.sblk_row[c] + first_up[c] + (int32_t)u);
+      hb.sblk_pair.push_back(hb.sblk_pair.back() + cnts[c][u]);
     }
-    for (int u = 0; u < nu; ++u) cnt[u + 1] += cnt[u];
-    const size_t base = hb.spair.size() / 2;
-    for (int u = 0; u < nb; ++u) hb.sblk_col.push_back(row[u]);
-    for (int u = 0; u < nu; ++u) {
-      hb.sblk_up.push_back(hb.sblk_row[c] + u0 + u);
-      hb.sblk_pair.push_back((int32_t)(base + cnt[u + 1]));
-    }
-    hb.spair.resize(2 * (base + (size_t)cnt[nu]));
-    for (int ia = a0; ia < a1; ++ia) {
-      const int a = hb.cam_obs_list[ia], j = hb.obs_pt[a];
-      for (int b = hb.pt_obs_begin[j]; b < hb.pt_obs_begin[j + 1]; ++b)
-        if (b != a && hb.obs_cam[b] >= c) {
-          const size_t k = base + cnt[pos[hb.obs_cam[b]]]++;
-          hb.spair[2 * k] = hb.obs_fpos[a];
-          hb.spair[2 * k + 1] = hb.obs_fpos[b];
-        }
-    }
-    hb.sblk_row[c + 1] = hb.sblk_row[c] + nb;
   }
-  hb.nblk = hb.sblk_row[hb.nc];
+  up_begin[nc] = (long long)hb.sblk_up.size();
   hb.nup = (long long)hb.sblk_up.size();
-  hb.npairs = (long long)(hb.spair.size() / 2);
-  // the transpose of block (c, k) is block (k, c), in row k
-  hb.sblk_tr.resize(hb.nblk);
-  for (int c = 0; c < hb.nc; ++c)
-    for (int e = hb.sblk_row[c]; e < hb.sblk_row[c + 1]; ++e) {
-      const int k = hb.sblk_col[e];
-      const auto b0 = hb.sblk_col.begin() + hb.sblk_row[k], b1 = hb.sblk_col.begin() + hb.sblk_row[k + 1];
-      hb.sblk_tr[e] = (int32_t)(std::lower_bound(b0, b1, c) - hb.sblk_col.begin());
+  hb.npairs = hb.sblk_pair.back();
+  hb.spair.resize(2 * (size_t)hb.npairs);
+  // 3. the pairs, in point order per block
+  for_rows([&](int c0, int c1, std::vector<int32_t> &mark, std::vector<int32_t> &pos) {
+    (void)mark;
+    std::vector<int32_t> next;
+    for (int c = c0; c < c1; ++c) {
+      const std::vector<int32_t> &row = rows[c];
+      const int u0 = first_up[c], nu = (int)row.size() - u0;
+      next.resize(nu);
+      for (int u = 0; u < nu; ++u) {
+        pos[row[u0 + u]] = u;
+        next[u] = hb.sblk_pair[up_begin[c] + u];
+      }
+      for (int ia = hb.cam_obs_begin[c]; ia < hb.cam_obs_begin[c + 1]; ++ia) {
+        const int a = hb.cam_obs_list[ia], j = hb.obs_pt[a];
+        for (int b = hb.pt_obs_begin[j]; b < hb.pt_obs_begin[j + 1]; ++b)
+          if (b != a && hb.obs_cam[b] >= c) {
+            const size_t k = (size_t)next[pos[hb.obs_cam[b]]]++;
+            hb.spair[2 * k] = hb.obs_fpos[a];
+            hb.spair[2 * k + 1] = hb.obs_fpos[b];
+          }
+      }
     }
+  });
+  // 4. the transpose of block (c, k) is block (k, c), in row k
+  hb.sblk_tr.resize(hb.nblk);
+  for_rows([&](int c0, int c1, std::vector<int32_t> &, std::vector<int32_t> &) {
+    for (int c = c0; c < c1; ++c)
+      for (int e = hb.sblk_row[c]; e < hb.sblk_row[c + 1]; ++e) {
+        const int k = hb.sblk_col[e];
+        const auto b0 = hb.sblk_col.begin() + hb.sblk_row[k], b1 = hb.sblk_col.begin() + hb.sblk_row[k + 1];
+        hb.sblk_tr[e] = (int32_t)(std::lower_bound(b0, b1, c) - hb.sblk_col.begin());
+      }
+  });
 }
 
 gba_status prepare_batch(const gba_problem_view *views, int n, const PrepOptions &opt, HostBatch *out,
