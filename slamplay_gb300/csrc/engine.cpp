@@ -250,7 +250,6 @@ size_t Engine::layout(const HostBatch &hb, char *base, DeviceBatch *db, size_t *
   b.cam_Sii = cv.take<char>(ex ? 81 * nc * rs : 0);
   b.pcg_q = cv.take<double>(ex ? 9 * nc : 0);
   b.spmv_red = cv.take<double>(ex ? nc : 0);
-  b.cl_camv = cv.take<double>(ex ? 4 * nc : 0);
   b.prob_counter = cv.take<uint32_t>(4 * P);
   b.global_counter = cv.take<uint32_t>(8);
   b.chunk_counter = cv.take<uint32_t>(nch);

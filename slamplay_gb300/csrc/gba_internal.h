@@ -178,7 +178,6 @@ struct DeviceBatch {
   void *cam_Sii;             // 81 * nc
   double *pcg_q;             // 9 * nc
   double *spmv_red;          // nc
-  double *cl_camv;           // 4 * nc: the cluster PCG's per-camera dot-product shares (double-float pairs)
 };
 
 constexpr int kCamTable = 44;    // R(9) dR(27) t(3) f k1 k2 + pad

@@ -19,10 +19,9 @@
 //      cameras, each owned camera's r.z, r.r, x.(v + r); barrier
 //   3. the stopping test and beta from the cameras' values, p_{k+1} =
 //      z_{k+1} + beta p_k for all cameras.
-// The CTAs exchange z and the per-camera values through global memory (L2:
-// one store per value, read back after the cluster barrier, whose
-// release/acquire orders them), not by storing into every CTA's shared
-// memory.  The dot products are summed per camera (a fixed tree over its
+// Each CTA stores its z and per-camera values into its own shared memory;
+// after the cluster barrier (release/acquire) the others read them from
+// there (distributed shared memory), one load per value.  The dot products are summed per camera (a fixed tree over its
 // nine coordinates) and then over the problem's cameras (a fixed tree over
 // a warp), so the result depends neither on the cluster size nor on the
 // batch: a problem gets the same bits alone and in any batch.
@@ -50,7 +49,7 @@ constexpr int kClSub = 8;  // lanes per (camera, row triplet) of the product
 
 // Shared-memory layout (bytes), the same on the host and the device.
 struct ClLayout {
-  size_t zf, ph, mo, xh, xl, rh, rl, vh, vl, qh, ql, cv, boff, scol, sval, total;
+  size_t zf, ph, mo, xh, xl, rh, rl, vh, vl, qh, ql, cv, owner, boff, scol, sval, total;
 };
 __host__ __device__ inline size_t cl_align(size_t x) { return (x + 15) & ~size_t(15); }
 __host__ __device__ inline ClLayout cl_layout(int n_max, int own_max, int cache_blocks) {
@@ -68,7 +67,8 @@ __host__ __device__ inline ClLayout cl_layout(int n_max, int own_max, int cache_
   l.vl = o, o = cl_align(o + of);
   l.qh = o, o = cl_align(o + of);
   l.ql = o, o = cl_align(o + of);
-  l.cv = o, o = cl_align(o + 8 * 4 * (size_t)n_max);  // the cameras' values, staged from global memory
+  l.cv = o, o = cl_align(o + 8 * 4 * (size_t)n_max);  // per camera: p.q, r.z, r.r, x.(v + r) (double-float)
+  l.owner = o, o = cl_align(o + 4 * (size_t)n_max);    // per camera: the rank that owns it
   // the owned rows of S (cache_blocks > 0): per owned camera its first
   // block, per block its column camera (in the problem) and its 81 values
   l.boff = o, o = cl_align(o + (cache_blocks > 0 ? 4 * ((size_t)own_max + 1) : 0));
@@ -131,6 +131,7 @@ __global__ void __launch_bounds__(kClThreads, 1) k_pcg_cluster(DeviceBatch B, in
   float *qh = reinterpret_cast<float *>(cl_smem + lay.qh);
   float *ql = reinterpret_cast<float *>(cl_smem + lay.ql);
   float2 *cvs = reinterpret_cast<float2 *>(cl_smem + lay.cv);
+  int *own_of = reinterpret_cast<int *>(cl_smem + lay.owner);
   int *boff = reinterpret_cast<int *>(cl_smem + lay.boff);
   int *scol = reinterpret_cast<int *>(cl_smem + lay.scol);
   float *sval = reinterpret_cast<float *>(cl_smem + lay.sval);
@@ -149,6 +150,8 @@ __global__ void __launch_bounds__(kClThreads, 1) k_pcg_cluster(DeviceBatch B, in
   // the cameras split into cs runs of about equal blocks of S (the
   // product's work): CTA `rank` owns the cameras whose blocks before them
   // (with the diagonal ones) lie in [bound(rank), bound(rank + 1))
+  // (bound(r) = ceil(r W / cs) <= before(c) exactly when r <= before(c) cs / W,
+  // so camera c's owner is floor(before(c) cs / W))
   int own0 = 0, own_end = 0;
   {
     const int r0 = B.sblk_row[c0];
@@ -157,6 +160,7 @@ __global__ void __launch_bounds__(kClThreads, 1) k_pcg_cluster(DeviceBatch B, in
     for (int cb = 0; cb < n; cb += T) {
       const int c = cb + t;
       const long long before = c < n ? (long long)(B.sblk_row[c0 + c] - r0) + c : wtot;
+      if (c < n) own_of[c] = (int)(before * cs / wtot);
       own0 += __syncthreads_count(before < ta);
       own_end += __syncthreads_count(before < tb);
     }
@@ -164,12 +168,10 @@ __global__ void __launch_bounds__(kClThreads, 1) k_pcg_cluster(DeviceBatch B, in
   const int own_n = own_end - own0;
   const int n9 = 9 * n, o9 = 9 * own_n, a9 = 9 * own0;  // a9: first owned coordinate in the problem
   const size_t g0 = 9 * (size_t)c0;                       // the problem's first coordinate (global)
-  float *zx = B.pcg_zf + g0;                              // z exchange (the problem's coordinates)
-  float2 *camx = reinterpret_cast<float2 *>(B.cl_camv) + 4 * (size_t)c0;  // per-camera values
 
   // the start (K3b): x = 0, r = v, z = M r, p_0 = z
   for (int i = t; i < n9; i += T) {
-    const float z = zx[i];
+    const float z = B.pcg_zf[g0 + i];
     zf[i] = z, ph[i + 3 * (i / 9)] = z;
   }
   for (int i = t; i < o9; i += T) {
@@ -294,11 +296,15 @@ __global__ void __launch_bounds__(kClThreads, 1) k_pcg_cluster(DeviceBatch B, in
         d = df_mul_f(DF{qh[i], ql[i]}, ph[12 * (own0 + lc) + hq]);
       }
       d = df_group16_sum(d, hmask);
-      if (lc < own_n && hq == 0) camx[4 * (own0 + lc)] = make_float2(d.hi, d.lo);
+      if (lc < own_n && hq == 0) cvs[4 * (own0 + lc)] = make_float2(d.hi, d.lo);
     }
     cl.sync();
     // 2. p.q, alpha, the owned update
-    for (int c = t; c < n; c += T) cvs[4 * c] = __ldcg(camx + 4 * c);
+    // the other CTAs' cameras' values, read from their shared memory
+    for (int c = t; c < n; c += T) {
+      const int r = own_of[c];
+      if (r != rank) cvs[4 * c] = *cl.map_shared_rank(cvs + 4 * c, r);
+    }
     __syncthreads();
     if (t < 32) {
       const DF s = cam_total(cvs, 0, n);
@@ -334,7 +340,7 @@ __global__ void __launch_bounds__(kClThreads, 1) k_pcg_cluster(DeviceBatch B, in
           float u = 0.f;
 #pragma unroll
           for (int kk = 0; kk < 9; ++kk) u = __fmaf_rn(m[kk], rr[kk], u);
-          zx[a9 + i] = u;
+          zf[a9 + i] = u;
           d0 = df_mul_f(r, u);
           d1 = df_mul(r, r);
           d2 = df_mul(x, df_add(DF{vh[i], vl[i]}, r));
@@ -343,39 +349,41 @@ __global__ void __launch_bounds__(kClThreads, 1) k_pcg_cluster(DeviceBatch B, in
         d1 = df_group16_sum(d1, hmask);
         d2 = df_group16_sum(d2, hmask);
         if (lc < own_n && hq == 0) {
-          float2 *dst = camx + 4 * (own0 + lc);
+          float2 *dst = cvs + 4 * (own0 + lc);
           dst[1] = make_float2(d0.hi, d0.lo), dst[2] = make_float2(d1.hi, d1.lo), dst[3] = make_float2(d2.hi, d2.lo);
         }
       }
     }
     cl.sync();
     // 3. the stopping test on (x_{k+1}, r_{k+1}) and beta_{k+1}; the new z
-    // (four loads in flight per thread: one L2 round trip for most sizes)
-    for (int i0 = 0; i0 < n9; i0 += 4 * T) {
-      float zv[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const int i = i0 + u * T + t;
-        zv[u] = i < n9 ? __ldcg(zx + i) : 0.f;
-      }
-      float2 cv[3];
-#pragma unroll
-      for (int u = 0; u < 3; ++u) {
-        const int e = (i0 / (4 * T)) * 3 * T + u * T + t;  // the cameras' slots 1..3: 3 T per round
-        cv[u] = e < 3 * n ? __ldcg(camx + 4 * (e / 3) + 1 + e % 3) : make_float2(0.f, 0.f);
-      }
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const int i = i0 + u * T + t;
-        if (i < n9) zf[i] = zv[u];
-      }
-#pragma unroll
-      for (int u = 0; u < 3; ++u) {
-        const int e = (i0 / (4 * T)) * 3 * T + u * T + t;
-        if (e < 3 * n) cvs[4 * (e / 3) + 1 + e % 3] = cv[u];
-      }
+    // the other CTAs' cameras' values (slots 1..3), then: warps 0-2 sum them
+    // while the other warps read the other CTAs' z (both from the owners'
+    // shared memory)
+    for (int e = t; e < 3 * n; e += T) {
+      const int c = e / 3, j = 1 + e - 3 * c, r = own_of[c];
+      if (r != rank) cvs[4 * c + j] = *cl.map_shared_rank(cvs + 4 * c + j, r);
     }
     __syncthreads();
+    if (t >= 96) {
+      const int tz = t - 96, Tz = T - 96;
+      for (int i0 = 0; i0 < n9; i0 += 4 * Tz) {
+        float zv[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int i = i0 + u * Tz + tz;
+          zv[u] = 0.f;
+          if (i < n9) {
+            const int r = own_of[i / 9];
+            if (r != rank) zv[u] = *cl.map_shared_rank(zf + i, r);
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int i = i0 + u * Tz + tz;
+          if (i < n9 && own_of[i / 9] != rank) zf[i] = zv[u];
+        }
+      }
+    }
     if (t < 96) {  // warps 0, 1, 2: r.z, r.r, x.(v + r)
       const DF sj = cam_total(cvs, 1 + (t >> 5), n);
       if ((t & 31) == 0) scf[1 + (t >> 5)] = sj;

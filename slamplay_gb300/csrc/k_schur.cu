@@ -14,7 +14,9 @@
 // (i, k) is -sum over the points both see of F_a F_b^T.
 //
 //  K3c k_schur_form   one CTA per block on or above the diagonal (k >= i):
-//                     the sum over the block's observation pairs, in a
+//                     the F rows of 64 pairs per round staged in shared
+//                     memory (the next round's loads in flight while this
+//                     one is summed); the sum over the block's pairs, in a
 //                     fixed order (three interleaved runs over the pairs'
 //                     point order, combined in order; compensated FP32 in
 //                     the mixed form), stored with its transpose as block
@@ -39,7 +41,7 @@ namespace gba {
 namespace {
 
 constexpr int kFormThreads = 256;
-constexpr int kFormPairs = 32;  // pairs staged per round
+constexpr int kFormPairs = 64;  // pairs staged per round
 constexpr int kFormSub = 3;     // sub-lanes per block entry (243 of the 256 threads)
 
 __device__ __forceinline__ void pdl_wait_s() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
@@ -70,6 +72,8 @@ __global__ void __launch_bounds__(kFormThreads) k_schur_form(DeviceBatch B) {
   typedef typename Vec16<MIXED>::type vec;
   constexpr int kVec = (int)(sizeof(vec) / sizeof(real));
   constexpr int kRowVecs = kObsF / kVec;  // 16-byte loads per F row
+  constexpr int kRoundVecs = kFormPairs * 2 * kRowVecs;
+  constexpr int kPer = (kRoundVecs + kFormThreads - 1) / kFormThreads;  // loads per thread per round
   static_assert(kObsF % kVec == 0, "F rows are whole 16-byte vectors");
   __shared__ __align__(16) real Fs[kFormPairs][2][kObsF];  // F of the row's and the column's observation
   __shared__ Acc part[kFormSub][81];
@@ -78,28 +82,55 @@ __global__ void __launch_bounds__(kFormThreads) k_schur_form(DeviceBatch B) {
   const int p0 = B.sblk_pair[ub], p1 = B.sblk_pair[ub + 1];
   const LMState *L = B.lm + B.cam_problem[B.sblk_col[blk]];
   if (!L->active) return;  // uniform
+  const real *F = reinterpret_cast<const real *>(B.obs_F);
+  // a round's F rows: every load issued before any is stored (one L2 round
+  // trip per round), the next round's loaded while this one is summed
+  vec buf[kPer];
+  auto load_round = [&](int g) {
+    const int n = min(kFormPairs, p1 - g);
+#pragma unroll
+    for (int u = 0; u < kPer; ++u) {
+      const int i = t + u * kFormThreads;
+      if (i < n * 2 * kRowVecs) {
+        const int pr = i / (2 * kRowVecs), r = i - 2 * kRowVecs * pr;
+        const int side = r / kRowVecs, e = r - kRowVecs * side;
+        const int2 ob = B.spair[g + pr];
+        buf[u] = reinterpret_cast<const vec *>(F + (size_t)kObsF * (side ? ob.y : ob.x))[e];
+      }
+    }
+  };
+  auto store_round = [&](int g) {
+    const int n = min(kFormPairs, p1 - g);
+#pragma unroll
+    for (int u = 0; u < kPer; ++u) {
+      const int i = t + u * kFormThreads;
+      if (i < n * 2 * kRowVecs) {
+        const int pr = i / (2 * kRowVecs), r = i - 2 * kRowVecs * pr;
+        const int side = r / kRowVecs, e = r - kRowVecs * side;
+        *reinterpret_cast<vec *>(&Fs[pr][side][kVec * e]) = buf[u];
+      }
+    }
+  };
   // sub-lane `sub` of entry (i, k) sums the pairs sub, sub + kFormSub, ...
   // of every round, in order
   const int sub = t / 81, en = t - 81 * sub, ei = en / 9, ek = en - 9 * ei;
   Acc acc;
   acc.init();
+  load_round(p0);
+  store_round(p0);
+  __syncthreads();
   for (int g = p0; g < p1; g += kFormPairs) {
     const int n = min(kFormPairs, p1 - g);
-    for (int i = t; i < n * 2 * kRowVecs; i += kFormThreads) {
-      const int u = i / (2 * kRowVecs), r = i - 2 * kRowVecs * u;
-      const int side = r / kRowVecs, e = r - kRowVecs * side;
-      const int2 pr = B.spair[g + u];
-      const vec *src = reinterpret_cast<const vec *>(reinterpret_cast<const real *>(B.obs_F) +
-                                                     (size_t)kObsF * (side ? pr.y : pr.x));
-      *reinterpret_cast<vec *>(&Fs[u][side][kVec * e]) = src[e];
-    }
-    __syncthreads();
+    const bool more = g + kFormPairs < p1;
+    if (more) load_round(g + kFormPairs);
     if (sub < kFormSub)
       for (int u = sub; u < n; u += kFormSub) {
         const real *fa = &Fs[u][0][3 * ei], *fb = &Fs[u][1][3 * ek];
         acc.add(fa[0] * fb[0] + fa[1] * fb[1] + fa[2] * fb[2]);
       }
     __syncthreads();  // the stage is reused
+    if (more) store_round(g + kFormPairs);
+    __syncthreads();
   }
   if (sub < kFormSub) part[sub][en] = acc;
   __syncthreads();
