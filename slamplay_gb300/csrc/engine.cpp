@@ -781,7 +781,7 @@ gba_status Engine::download(const HostBatch &hb, const gba_problem_view *v, gba_
 gba_status Engine::solve(const gba_problem_view *v, int n, gba_summary *s, std::string *err) {
   const double t0 = now_s();
   PrepOptions po = prep_options();
-  HostBatch hb;
+  HostBatch &hb = hb_;  // kept between solves: its storage is reused
   gba_status st = prepare_batch(v, n, po, &hb, err);
   if (st != GBA_OK) return st;
   if ((st = upload(hb, err)) != GBA_OK) return st;

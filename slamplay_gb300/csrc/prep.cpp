@@ -64,6 +64,20 @@ gba_status validate_problem(const gba_problem_view *v, std::string *err) {
   return GBA_OK;
 }
 
+// Runs fn(begin, end) over [0, n) in runs on host threads (one run when n
+// is small); fn must write disjoint outputs per index.
+static void parallel_runs(long long n, long long min_per_thread, const std::function<void(long long, long long)> &fn) {
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const long long nth = std::min<long long>(std::min(hw, 32u), std::max<long long>(1, n / std::max(1LL, min_per_thread)));
+  if (nth <= 1) {
+    fn(0, n);
+    return;
+  }
+  std::vector<std::thread> th;
+  for (long long w = 0; w < nth; ++w) th.emplace_back([&, w] { fn(n * w / nth, n * (w + 1) / nth); });
+  for (auto &x : th) x.join();
+}
+
 // The explicit Schur complement's structure, row camera by row camera: the
 // row's co-visible cameras (sorted; the row's own camera when it observes a
 // point more than once), the transpose of every block, and for the blocks
@@ -179,10 +193,27 @@ static void build_schur_structure(HostBatch *hbp) {
   });
 }
 
+void HostBatch::reset() {
+  P = nc = np = no = nchunks = nseg = cam_blocks = 0;
+  explicit_schur = false;
+  nblk = nup = npairs = 0;
+  for (auto *v : {&obs_cam, &obs_pt, &pt_obs_begin, &pt_problem, &cam_problem, &seg_cam, &cam_seg_begin, &seg_slot,
+                  &cam_obs_begin, &cam_obs_list, &sblk_row, &sblk_col, &sblk_tr, &sblk_up, &sblk_pair, &spair,
+                  &obs_fpos, &obs_orig, &pt_orig})
+    v->clear();
+  for (auto *v : {&obs_seg, &obs_slot, &seg_pos}) v->clear();
+  for (auto *v : {&obs_uv, &cam_param, &pt_param}) v->clear();
+  pt_used.clear();
+  cam_used.clear();
+  prob.clear();
+  chunk.clear();
+  camblk.clear();
+}
+
 gba_status prepare_batch(const gba_problem_view *views, int n, const PrepOptions &opt, HostBatch *out,
                          std::string *err) {
   HostBatch &hb = *out;
-  hb = HostBatch();
+  hb.reset();
   if (n <= 0 || !views) {
     *err = "empty batch";
     return GBA_ERR_INVALID_ARGUMENT;
@@ -227,7 +258,9 @@ gba_status prepare_batch(const gba_problem_view *views, int n, const PrepOptions
 
   int cam0 = 0, pt0 = 0, obs0 = 0;
   std::vector<int32_t> deg, key, order, inv, fill, cams;
-  std::vector<std::pair<int, int>> tmp;
+  // per camera of the batch, for the chunks' camera-sorted orders: the
+  // chunk that last saw it, its count, next position, segment
+  std::vector<int32_t> cmark(tc, -1), ccount(tc), cstart(tc), cseg(tc), distinct;
   for (int p = 0; p < n; ++p) {
     const gba_problem_view &v = views[p];
     const int nc = v.num_cameras, np = v.num_points, no = v.num_observations;
@@ -275,27 +308,32 @@ gba_status prepare_batch(const gba_problem_view *views, int n, const PrepOptions
     for (int ji = 0; ji < np; ++ji) hb.pt_obs_begin[pt0 + ji + 1] += hb.pt_obs_begin[pt0 + ji];
     fill.assign(hb.pt_obs_begin.begin() + pt0, hb.pt_obs_begin.begin() + pt0 + np + 1);
     for (int i = 0; i < no; ++i) hb.obs_orig[fill[inv[v.point_index[i]]]++] = i;
-    // within a point: by camera, then input index (insertion sort, stable)
-    for (int ji = 0; ji < np; ++ji) {
-      const int b = hb.pt_obs_begin[pt0 + ji], e = hb.pt_obs_begin[pt0 + ji + 1];
-      for (int k = b + 1; k < e; ++k) {
-        const int x = hb.obs_orig[k];
-        const int cx = v.camera_index[x];
-        int m = k - 1;
-        while (m >= b && v.camera_index[hb.obs_orig[m]] > cx) {
-          hb.obs_orig[m + 1] = hb.obs_orig[m];
-          --m;
+    // within a point: by camera, then input index (insertion sort, stable);
+    // points and observations are independent (host threads)
+    parallel_runs(np, 20000, [&](long long j0, long long j1) {
+      for (int ji = (int)j0; ji < (int)j1; ++ji) {
+        const int b = hb.pt_obs_begin[pt0 + ji], e = hb.pt_obs_begin[pt0 + ji + 1];
+        for (int k = b + 1; k < e; ++k) {
+          const int x = hb.obs_orig[k];
+          const int cx = v.camera_index[x];
+          int m = k - 1;
+          while (m >= b && v.camera_index[hb.obs_orig[m]] > cx) {
+            hb.obs_orig[m + 1] = hb.obs_orig[m];
+            --m;
+          }
+          hb.obs_orig[m + 1] = x;
         }
-        hb.obs_orig[m + 1] = x;
       }
-    }
-    for (int k = obs0; k < obs0 + no; ++k) {
-      const int i = hb.obs_orig[k];
-      hb.obs_cam[k] = cam0 + v.camera_index[i];
-      hb.obs_pt[k] = pt0 + inv[v.point_index[i]];
-      hb.obs_uv[2 * (size_t)k] = v.observations[2 * (size_t)i];
-      hb.obs_uv[2 * (size_t)k + 1] = v.observations[2 * (size_t)i + 1];
-    }
+    });
+    parallel_runs(no, 50000, [&](long long k0, long long k1) {
+      for (int k = obs0 + (int)k0; k < obs0 + (int)k1; ++k) {
+        const int i = hb.obs_orig[k];
+        hb.obs_cam[k] = cam0 + v.camera_index[i];
+        hb.obs_pt[k] = pt0 + inv[v.point_index[i]];
+        hb.obs_uv[2 * (size_t)k] = v.observations[2 * (size_t)i];
+        hb.obs_uv[2 * (size_t)k + 1] = v.observations[2 * (size_t)i + 1];
+      }
+    });
     for (int c = 0; c < nc; ++c) {
       hb.cam_problem[cam0 + c] = p;
       for (int q = 0; q < 9; ++q) hb.cam_param[9 * (size_t)(cam0 + c) + q] = v.parameters[9 * (size_t)c + q];
@@ -323,21 +361,31 @@ gba_status prepare_batch(const gba_problem_view *views, int n, const PrepOptions
       }
       ci.obs_count = nobs;
       ci.pt_count = npts;
-      // camera-sorted order of the chunk's observations, stable
-      tmp.resize(nobs);
-      for (int k = 0; k < nobs; ++k) tmp[k] = std::make_pair(hb.obs_cam[ci.obs_begin + k], k);
-      std::stable_sort(tmp.begin(), tmp.end(),
-                       [](const std::pair<int, int> &a, const std::pair<int, int> &b) { return a.first < b.first; });
-      ci.seg_begin = (int)hb.seg_cam.size();
-      int segs = 0;
+      // camera-sorted order of the chunk's observations, stable: the
+      // chunk's distinct cameras (a stamped table), sorted, then each
+      // observation's position from its camera's running count
+      const int stamp = (int)hb.chunk.size();
+      distinct.clear();
       for (int k = 0; k < nobs; ++k) {
-        if (k == 0 || tmp[k].first != tmp[k - 1].first) {
-          hb.seg_pos.push_back((uint16_t)k);
-          hb.seg_cam.push_back(tmp[k].first);
-          ++segs;
-        }
-        hb.obs_slot[ci.obs_begin + tmp[k].second] = (uint16_t)k;
-        hb.obs_seg[ci.obs_begin + tmp[k].second] = (uint16_t)(segs - 1);
+        const int cam = hb.obs_cam[ci.obs_begin + k];
+        if (cmark[cam] != stamp) cmark[cam] = stamp, ccount[cam] = 0, distinct.push_back(cam);
+        ++ccount[cam];
+      }
+      std::sort(distinct.begin(), distinct.end());
+      ci.seg_begin = (int)hb.seg_cam.size();
+      const int segs = (int)distinct.size();
+      for (int sg = 0, pos = 0; sg < segs; ++sg) {
+        const int cam = distinct[sg];
+        hb.seg_pos.push_back((uint16_t)pos);
+        hb.seg_cam.push_back(cam);
+        cstart[cam] = pos;
+        cseg[cam] = sg;
+        pos += ccount[cam];
+      }
+      for (int k = 0; k < nobs; ++k) {
+        const int cam = hb.obs_cam[ci.obs_begin + k];
+        hb.obs_slot[ci.obs_begin + k] = (uint16_t)cstart[cam]++;
+        hb.obs_seg[ci.obs_begin + k] = (uint16_t)cseg[cam];
       }
       ci.seg_count = segs;
       hb.chunk.push_back(ci);

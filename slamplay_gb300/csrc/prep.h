@@ -46,6 +46,9 @@ struct HostBatch {
   // initial parameters in the internal layout
   std::vector<double> cam_param;  // 9 per camera
   std::vector<double> pt_param;   // 4 per point
+  // Empties the batch but keeps the vectors' storage (a handle re-preparing
+  // problems of similar size touches no fresh pages).
+  void reset();
 };
 
 // Validates and lays out `n` problems.  Returns GBA_OK or an error with a
