@@ -213,11 +213,13 @@ size_t Engine::layout(const HostBatch &hb, char *base, DeviceBatch *db, size_t *
   b.pt_param[1] = cv.take<double>(4 * np);
   b.cam_table = cv.take<double>(kCamTable * nc);
   b.cam_tablef = cv.take<float>(kCamTable * nc);
+  b.cam_tabledf = cv.take<float2>(kCamTable * nc);
   b.jac = cv.take<char>(13 * no * 2 * rs);
   b.pt_C = cv.take<double>(6 * np);
   b.pt_g = cv.take<double>(3 * np);
   b.pt_scale = cv.take<double>(3 * np);
   b.pt_scalef = cv.take<float>(3 * np);
+  b.pt_scaledf = cv.take<float2>(3 * np);
   b.pt_t = cv.take<double>(3 * np);
   b.pt_Cinv = cv.take<char>(6 * np * rs);
   b.pt_Cinv64 = cv.take<double>(6 * np);
@@ -226,6 +228,7 @@ size_t Engine::layout(const HostBatch &hb, char *base, DeviceBatch *db, size_t *
   b.cam_g = cv.take<double>(9 * nc);
   b.cam_scale = cv.take<double>(9 * nc);
   b.cam_scalef = cv.take<float>(9 * nc);
+  b.cam_scaledf = cv.take<float2>(9 * nc);
   b.cam_Minv = cv.take<double>(81 * nc);
   b.cam_Minvf = cv.take<float>(81 * nc);
   b.cam_Bf = cv.take<float>(45 * nc);

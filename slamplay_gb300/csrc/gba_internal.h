@@ -106,6 +106,7 @@ struct DeviceBatch {
   double *pt_param[2];       // np * 4
   double *cam_table;         // nc * kCamTable: R, dR/dw, t, f, k1, k2 of one buffer
   float *cam_tablef;         // nc * kCamTable: FP32 copy for the mixed-form Jacobian
+  float2 *cam_tabledf;       // nc * kCamTable: double-float copy (mixed form: the gradient's Jacobian)
   // Jacobian (scaled, loss-corrected), SoA by column pair; element type by mode
   void *jac;                 // 13 * no of double2 (FP64) or float2 (mixed)
   // per point
@@ -113,6 +114,7 @@ struct DeviceBatch {
   double *pt_g;              // 3
   double *pt_scale;          // 3
   float *pt_scalef;          // 3, FP32 copy
+  float2 *pt_scaledf;        // 3, double-float copy
   double *pt_t;              // 3: Cinv g_p
   void *pt_Cinv;             // 6 sym, double (FP64) or float (mixed)
   double *pt_Cinv64;         // 6 sym, double (both modes, for the back-substitution)
@@ -121,6 +123,7 @@ struct DeviceBatch {
   double *cam_g;             // 9
   double *cam_scale;         // 9
   float *cam_scalef;         // 9, FP32 copy
+  float2 *cam_scaledf;       // 9, double-float copy
   double *cam_Minv;          // 81 block-Jacobi inverse of S_ii
   float *cam_Minvf;          // 81, FP32 copy (mixed form)
   float *cam_Bf;             // 45, FP32 copy of cam_B (mixed form)

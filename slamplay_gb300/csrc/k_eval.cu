@@ -54,7 +54,12 @@ __global__ void k_camera_table(DeviceBatch B) {
   camera_table_entry(B.cam_param[L->parity] + 9 * (size_t)c, tab, true);
   if (B.opt.mixed) {
     float *tf = B.cam_tablef + (size_t)kCamTable * c;
-    for (int k = 0; k < kCamTable; ++k) tf[k] = (float)tab[k];
+    float2 *td = B.cam_tabledf + (size_t)kCamTable * c;
+    for (int k = 0; k < kCamTable; ++k) {
+      const DF d = df_from_double(tab[k]);
+      tf[k] = d.hi;
+      td[k] = make_float2(d.hi, d.lo);
+    }
   }
 }
 
@@ -161,12 +166,115 @@ __device__ __forceinline__ double eval_observation(const DeviceBatch &B, int64_t
 }
 
 // ---------------------------------------------------------------------------
+// The same residual and Jacobian for the mixed form's gradient: the
+// projection (cost, residual) in FP64, the chain rule in double-float (two
+// floats, about 48 bits: GB300 issues FP32 some 64 times faster than FP64)
+// from the double-float copies of the camera table and the Jacobi scales.
+// Returns the FP32 Jacobian (the nearest floats) and residual, and per
+// column J^T r (double-float).
+__device__ __forceinline__ DF operator+(DF a, DF b) { return df_add(a, b); }
+__device__ __forceinline__ DF operator-(DF a, DF b) { return df_add(a, df_neg(b)); }
+__device__ __forceinline__ DF operator*(DF a, DF b) { return df_mul(a, b); }
+__device__ __forceinline__ DF operator-(DF a) { return df_neg(a); }
+
+__device__ __forceinline__ double eval_observation_df(const DeviceBatch &B, int64_t o, int c, int j,
+                                                      const double *X, float2 *Jc, float2 *Jp, float2 &r,
+                                                      DF *gr, bool &bad) {
+  const double *tab = B.cam_table + (size_t)kCamTable * c;
+  const float2 *td = B.cam_tabledf + (size_t)kCamTable * c;
+  auto T = [&](int k) {
+    const float2 v = td[k];
+    return DF{v.x, v.y};
+  };
+  Proj pr;
+  project(tab, X, B.obs_uv[o], pr);
+  const DF iz = df_from_double(pr.iz), xp = df_from_double(pr.xp), yp = df_from_double(pr.yp);
+  const DF r2 = df_from_double(pr.r2), dist = df_from_double(pr.dist);
+  const DF f = T(39), k1 = T(40), k2 = T(41);
+  const DF two{2.f, 0.f};
+  const DF g = k1 + two * k2 * r2;
+  const DF m00 = dist + two * g * xp * xp;
+  const DF m01 = two * g * xp * yp;
+  const DF m11 = dist + two * g * yp * yp;
+  const DF fiz = f * iz;
+  const DF A00 = -(fiz * m00), A01 = -(fiz * m01), A02 = -(fiz * (m00 * xp + m01 * yp));
+  const DF A10 = -(fiz * m01), A11 = -(fiz * m11), A12 = -(fiz * (m01 * xp + m11 * yp));
+  DF ju[12], jv[12];
+  const DF Xd[3] = {df_from_double(X[0]), df_from_double(X[1]), df_from_double(X[2])};
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    // dP/dw_k = dR_k X
+    const int d = 9 + 9 * k;
+    const DF q0 = T(d + 0) * Xd[0] + T(d + 1) * Xd[1] + T(d + 2) * Xd[2];
+    const DF q1 = T(d + 3) * Xd[0] + T(d + 4) * Xd[1] + T(d + 5) * Xd[2];
+    const DF q2 = T(d + 6) * Xd[0] + T(d + 7) * Xd[1] + T(d + 8) * Xd[2];
+    ju[k] = A00 * q0 + A01 * q1 + A02 * q2;
+    jv[k] = A10 * q0 + A11 * q1 + A12 * q2;
+    // dP/dX_k = R[:,k]
+    const DF c0 = T(k), c1 = T(3 + k), c2 = T(6 + k);
+    ju[9 + k] = A00 * c0 + A01 * c1 + A02 * c2;
+    jv[9 + k] = A10 * c0 + A11 * c1 + A12 * c2;
+  }
+  ju[3] = A00, ju[4] = A01, ju[5] = A02;
+  jv[3] = A10, jv[4] = A11, jv[5] = A12;
+  ju[6] = dist * xp, jv[6] = dist * yp;
+  ju[7] = f * r2 * xp, jv[7] = f * r2 * yp;
+  ju[8] = f * (r2 * r2) * xp, jv[8] = f * (r2 * r2) * yp;
+  const int loss = B.opt.loss;
+  const double cost = block_cost(loss, B.opt.loss_scale, pr.ru, pr.rv);
+  double ru = pr.ru, rv = pr.rv;
+  if (loss != GBA_LOSS_TRIVIAL) {
+    const Corrector cr = make_corrector(loss, B.opt.loss_scale, ru, rv);
+    const DF s1 = df_from_double(cr.sqrt_rho1), al = df_from_double(cr.alpha_sq_norm);
+    const DF rur = df_from_double(ru), rvr = df_from_double(rv);
+#pragma unroll
+    for (int k = 0; k < 12; ++k) {
+      const DF rJ = rur * ju[k] + rvr * jv[k];
+      ju[k] = s1 * (ju[k] - al * rur * rJ);
+      jv[k] = s1 * (jv[k] - al * rvr * rJ);
+    }
+    ru *= cr.residual_scaling;
+    rv *= cr.residual_scaling;
+  }
+  bool ok = isfinite(ru) && isfinite(rv) && isfinite(cost);
+  const float2 *sc = B.cam_scaledf + 9 * (size_t)c;
+  const float2 *sp = B.pt_scaledf + 3 * (size_t)j;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    const DF s{sc[k].x, sc[k].y};
+    ju[k] = ju[k] * s;
+    jv[k] = jv[k] * s;
+  }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const DF s{sp[k].x, sp[k].y};
+    ju[9 + k] = ju[9 + k] * s;
+    jv[9 + k] = jv[9 + k] * s;
+  }
+  const DF rdu = df_from_double(ru), rdv = df_from_double(rv);
+#pragma unroll
+  for (int k = 0; k < 12; ++k) {
+    gr[k] = ju[k] * rdu + jv[k] * rdv;
+    ok = ok && isfinite(ju[k].hi) && isfinite(jv[k].hi);
+    const float2 jk = make_float2(ju[k].hi, jv[k].hi);
+    if (k < 9)
+      Jc[k] = jk;
+    else
+      Jp[k - 9] = jk;
+  }
+  r = make_float2(rdu.hi, rdv.hi);
+  bad = !ok;
+  return cost;
+}
+
+// ---------------------------------------------------------------------------
 // K1
-// The mixed form's gradient (G64): the Jacobian is computed in FP64 and only
-// stored in FP32.  The gradient J^T r is a sum of large terms that cancel
-// towards zero as the solve converges, so it is formed from the FP64
-// Jacobian in FP64: per point (g_p) here, and per camera as one FP64 partial
-// per (chunk, camera segment) in seg_grad, summed per camera by K1c.  The
+// The mixed form's gradient (G64): the Jacobian is computed in double-float
+// (eval_observation_df) and only stored in FP32.  The gradient J^T r is a sum
+// of large terms that cancel towards zero as the solve converges, so it is
+// formed from the double-float Jacobian in double-float: per point (g_p)
+// here, and per camera as one partial per (chunk, camera segment) in
+// seg_grad (FP64), summed per camera by K1c.  The
 // LM fixed point (g = 0) is then the FP64 one; the FP32 copies only feed the
 // Schur products and the PCG, i.e. the accuracy of each step, not where the
 // steps lead.
@@ -179,7 +287,7 @@ __global__ void __launch_bounds__(kChunkCap) k_eval_chunk(DeviceBatch B) {
   __shared__ real sm[kChunkCap][9];
   // G64: per observation its FP64 J_c^T r (9, at its camera-sorted slot) and
   // J_p^T r (3, at its position)
-  __shared__ double gsm[G64 ? kChunkCap : 1][12];
+  __shared__ DF gsm[G64 ? kChunkCap : 1][12];
   __shared__ double red[kChunkCap / 32];
   const int t = threadIdx.x;
   for (int ch = blockIdx.x; ch < B.nchunks; ch += gridDim.x) {
@@ -196,22 +304,21 @@ __global__ void __launch_bounds__(kChunkCap) k_eval_chunk(DeviceBatch B) {
       const double X[3] = {Xp[0], Xp[1], Xp[2]};
       real2 Jc[9], Jp[3], r;
       if (G64) {
-        double2 Jc64[9], Jp64[3], r64;
-        cost = eval_observation<false>(B, o, c, j, X, false, Jc64, Jp64, r64, bad);
+        float2 Jcf[9], Jpf[3], rf;
+        DF gr[12];
+        cost = eval_observation_df(B, o, c, j, X, Jcf, Jpf, rf, gr, bad);
         const int slot = B.obs_slot[o];
 #pragma unroll
         for (int k = 0; k < 9; ++k) {
-          Jc[k] = mk2((real)Jc64[k].x, (real)Jc64[k].y);
-          gsm[slot][k] = Jc64[k].x * r64.x + Jc64[k].y * r64.y;
-          bad = bad || !isfinite((float)Jc[k].x) || !isfinite((float)Jc[k].y);
+          Jc[k] = mk2((real)Jcf[k].x, (real)Jcf[k].y);
+          gsm[slot][k] = gr[k];
         }
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-          Jp[k] = mk2((real)Jp64[k].x, (real)Jp64[k].y);
-          gsm[t][9 + k] = Jp64[k].x * r64.x + Jp64[k].y * r64.y;
-          bad = bad || !isfinite((float)Jp[k].x) || !isfinite((float)Jp[k].y);
+          Jp[k] = mk2((real)Jpf[k].x, (real)Jpf[k].y);
+          gsm[t][9 + k] = gr[9 + k];
         }
-        r = mk2((real)r64.x, (real)r64.y);
+        r = mk2((real)rf.x, (real)rf.y);
       } else {
         cost = eval_observation<MIXED>(B, o, c, j, X, NORMS, Jc, Jp, r, bad);
       }
@@ -246,9 +353,9 @@ __global__ void __launch_bounds__(kChunkCap) k_eval_chunk(DeviceBatch B) {
           b1 = (sg + 1 < ci.seg_count) ? B.seg_pos[ci.seg_begin + sg + 1] : ci.obs_count;
           slot9 = B.seg_slot[ci.seg_begin + sg];
         }
-        double a = 0.0;
-        for (int k = b0; k < b1; ++k) a += gsm[k][q];
-        B.seg_grad[9 * (size_t)slot9 + q] = a;
+        DF a = df_zero();
+        for (int k = b0; k < b1; ++k) a = df_add(a, gsm[k][q]);
+        B.seg_grad[9 * (size_t)slot9 + q] = df_value(a);
       }
     }
     double gmax = 0.0, xn2 = 0.0;
@@ -258,13 +365,13 @@ __global__ void __launch_bounds__(kChunkCap) k_eval_chunk(DeviceBatch B) {
       Acc acc[9];
 #pragma unroll
       for (int q = 0; q < 9; ++q) acc[q].init();
-      double g64[3] = {0.0, 0.0, 0.0};
+      DF g64[3] = {df_zero(), df_zero(), df_zero()};
       for (int k = b0; k < b1; ++k) {
 #pragma unroll
         for (int q = 0; q < (G64 ? 6 : 9); ++q) acc[q].add(sm[k][q]);
         if (G64) {
 #pragma unroll
-          for (int q = 0; q < 3; ++q) g64[q] += gsm[k][9 + q];
+          for (int q = 0; q < 3; ++q) g64[q] = df_add(g64[q], gsm[k][9 + q]);
         }
       }
       if (NORMS) {
@@ -278,7 +385,7 @@ __global__ void __launch_bounds__(kChunkCap) k_eval_chunk(DeviceBatch B) {
           const double *x = B.pt_param[parity] + 4 * (size_t)jj;
 #pragma unroll
           for (int q = 0; q < 3; ++q) {
-            const double gq = G64 ? g64[q] : acc[6 + q].value();
+            const double gq = G64 ? df_value(g64[q]) : acc[6 + q].value();
             B.pt_g[3 * (size_t)jj + q] = gq;
             const double gu = gq / B.pt_scale[3 * (size_t)jj + q];
             gmax = fmax(gmax, fabs(x[q] - (x[q] - gu)));
@@ -447,11 +554,15 @@ __global__ void k_scale_init(DeviceBatch B) {
   const int64_t ncam = 9 * (int64_t)B.nc, npt = 3 * (int64_t)B.np;
   if (i < ncam) {
     B.cam_scale[i] = B.opt.jacobi_scaling ? 1.0 / (1.0 + sqrt(B.cam_colnorm[i])) : 1.0;
-    B.cam_scalef[i] = (float)B.cam_scale[i];
+    const DF d = df_from_double(B.cam_scale[i]);
+    B.cam_scalef[i] = d.hi;
+    B.cam_scaledf[i] = make_float2(d.hi, d.lo);
   } else if (i < ncam + npt) {
     const int64_t k = i - ncam;
     B.pt_scale[k] = B.opt.jacobi_scaling ? 1.0 / (1.0 + sqrt(B.pt_colnorm[k])) : 1.0;
-    B.pt_scalef[k] = (float)B.pt_scale[k];
+    const DF d = df_from_double(B.pt_scale[k]);
+    B.pt_scalef[k] = d.hi;
+    B.pt_scaledf[k] = make_float2(d.hi, d.lo);
   }
 }
 
