@@ -188,3 +188,64 @@ def test_cluster_pcg_compute_step():
     assert ok and it > 0
     assert np.linalg.norm(d - do) / np.linalg.norm(do) < 1e-3
     assert abs(m - mo) <= 1e-4 * abs(mo)
+
+
+def _edge_problem():
+    """Configuration-0 cameras plus a camera whose points no other camera
+    sees (a row of S with only its diagonal block) and a camera that sees
+    some points twice (a block with itself)."""
+    b = BALProblem.synthetic(0, seed=6, num_cameras=6, num_points=300)
+    nc, np_ = b.num_cameras(), b.num_points()
+    ci, pi = b.camera_index_.copy(), b.point_index_.copy()
+    obs = b.observations_.reshape(-1, 2).copy()
+    par = b.parameters().copy()
+    cams, pts = par[: 9 * nc].reshape(nc, 9), par[9 * nc:].reshape(np_, 3)
+    # camera nc: a copy of camera 0 that alone sees copies of 12 of camera 0's points
+    rows = np.nonzero(ci == 0)[0][:12]
+    new_pts = pts[pi[rows]]
+    ci = np.concatenate([ci, np.full(len(rows), nc)])
+    pi = np.concatenate([pi, np_ + np.arange(len(rows))])
+    obs = np.concatenate([obs, obs[rows]])
+    # camera 1 sees 10 of its points a second time
+    dup = np.nonzero(ci == 1)[0][:10]
+    ci = np.concatenate([ci, ci[dup]])
+    pi = np.concatenate([pi, pi[dup]])
+    obs = np.concatenate([obs, obs[dup] + 0.3])
+    params = np.concatenate([cams.ravel(), cams[0], pts.ravel(), new_pts.ravel()])
+    return BALProblem.from_arrays(nc + 1, np_ + len(rows), ci, pi, obs, params)
+
+
+def test_cluster_pcg_edge_cameras():
+    """A camera with no co-visible camera and a camera with a block with
+    itself: the cluster PCG and the two-kernel PCG (mixed form, explicit
+    complement) reach final costs within 1e-6 of each other, below the
+    initial cost."""
+    b = _edge_problem()
+    opts = dict(max_num_iterations=10, precision="mixed", schur="explicit", pcg_tolerance=1e-8,
+                max_linear_solver_iterations=200, **FIXED)
+    n1, sc = _launches(b, "pcg_cluster", **opts)
+    _, s2 = _solve(b, persistent_pcg=0, **opts)
+    assert n1 > 0
+    assert np.isfinite(sc.final_cost) and sc.final_cost < sc.initial_cost
+    assert abs(sc.final_cost - s2.final_cost) <= 1e-6 * s2.final_cost, (sc.final_cost, s2.final_cost)
+
+
+def test_cluster_pcg_falls_back_for_large_problem_in_batch():
+    """A mixed batch with a problem of more than 1,024 cameras runs the
+    two-kernel PCG for the whole batch (one launch shape per batch); each
+    problem then gets the bits of its own two-kernel solve."""
+    small = [BALProblem.synthetic(3, index=i, seed=8) for i in range(2)]
+    big = BALProblem.synthetic(0, seed=9, num_cameras=1100, num_points=3000)
+    opts = dict(max_num_iterations=4, precision="mixed", schur="explicit", **FIXED)
+    with Solver(**opts) as s:
+        s.set_profiling(True)
+        qs = [p.copy() for p in small + [big]]
+        sums = s.batch_solve(qs)
+        names = {e["name"]: e["launches"] for e in s.profile()}
+    assert names.get("pcg_cluster", 0) == 0 and names.get("schur_matvec", 0) > 0
+    for p, q, sm in zip(small + [big], qs, sums):
+        g = p.copy()
+        with Solver(persistent_pcg=0, **opts) as s:
+            sa = s.solve(g)
+        assert np.array_equal(g.parameters(), q.parameters())
+        assert sa.final_cost == sm.final_cost
