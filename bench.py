@@ -180,6 +180,46 @@ def ncu_traffic(kernel: str):
     return d.get("kernels", {}).get(kernel)
 
 
+def measure_fp64_peak(torch) -> dict:
+    """FP64 throughput of this GPU: a cuBLAS DGEMM (torch.matmul, float64,
+    8192^3) timed with CUDA events, after warm-up."""
+    n = 8192
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        torch.matmul(a, b)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    reps = 3
+    for _ in range(reps):
+        torch.matmul(a, b)
+    e1.record()
+    e1.synchronize()
+    s = e0.elapsed_time(e1) * 1e-3 / reps
+    del a, b
+    return {"tflops": 2.0 * n ** 3 / s / 1e12, "source": "cuBLAS DGEMM 8192^3 (torch.matmul float64), CUDA events"}
+
+
+def fp64_formation_roofline(problem, prof, peak: dict):
+    """The FP64 form's formation kernel (K3c) against the FP64 roof: 243 FMAs
+    (486 flops) per observation pair on or above the diagonal (sum over
+    points of m (m - 1) / 2 for a problem without repeated observations)."""
+    import numpy as np
+
+    e = next((x for x in prof if x["name"] == "schur_form" and x["launches"] > 0), None)
+    if e is None:
+        return None
+    m = np.bincount(problem.point_index_).astype(np.int64)
+    pairs = int((m * (m - 1) // 2).sum())
+    avg_s = e["total_ms"] / e["launches"] * 1e-3
+    ach = 486.0 * pairs / avg_s / 1e12
+    return {"kernel": "schur_form", "bound": "fp64", "achieved": ach, "peak": peak["tflops"], "unit": "TFLOP/s",
+            "frac": ach / peak["tflops"], "flops_per_launch": 486.0 * pairs, "avg_launch_ms": avg_s * 1e3,
+            "peak_source": peak["source"],
+            "note": "the FP64 form's FP64-bound kernel; its HBM traffic is the mixed form's figure x2 (<5% of HBM)"}
+
+
 def run_gpu(args) -> None:
     import torch
 
@@ -259,6 +299,12 @@ def run_gpu(args) -> None:
     sm.solve(problem.copy())
     sm.set_profiling(False)
     prof = [e for e in sm.profile() if e["launches"] > 0]
+    # the FP64 form: its kernels, and the formation against the FP64 roof
+    sp.set_profiling(True)
+    sp.solve(problem.copy())
+    sp.set_profiling(False)
+    prof_p = [e for e in sp.profile() if e["launches"] > 0]
+    roof_fp64 = fp64_formation_roofline(problem, prof_p, measure_fp64_peak(torch)) if rank == 0 else None
     peaks = measured_peaks()
     peak = peaks.get("hbm_gbs", 6800.0)
     for e in prof:
@@ -295,7 +341,9 @@ def run_gpu(args) -> None:
                           "final_cost": first_m.final_cost},
                 "fp64": {"lm_iters_per_s": value_p, "solves_per_s": world * 1e3 / ms_p, "ms_per_solve": ms_p,
                          "lm_iterations": iters_p, "pcg_iterations": first_p.num_linear_solver_iterations,
-                         "final_cost": first_p.final_cost},
+                         "final_cost": first_p.final_cost, "roofline_fp64": roof_fp64,
+                         "kernels": [{"name": e["name"], "launches": e["launches"],
+                                      "avg_us": 1e3 * e["total_ms"] / e["launches"]} for e in prof_p]},
                 "mixed_vs_fp64_final_cost_rel": abs(first_m.final_cost - first_p.final_cost) / first_p.final_cost,
                 **extra_forms,
             },
