@@ -21,10 +21,11 @@
 //      z_{k+1} + beta p_k for all cameras.
 // Each CTA stores its z and per-camera values into its own shared memory;
 // after the cluster barrier (release/acquire) the others read them from
-// there (distributed shared memory), one load per value.  The dot products are summed per camera (a fixed tree over its
-// nine coordinates) and then over the problem's cameras (a fixed tree over
-// a warp), so the result depends neither on the cluster size nor on the
-// batch: a problem gets the same bits alone and in any batch.
+// there (distributed shared memory), one load per value.  The dot products
+// are summed per camera (a fixed tree over its nine coordinates) and then
+// over the problem's cameras (a fixed tree over a warp), so the result
+// depends neither on the cluster size nor on the batch: a problem gets the
+// same bits alone and in any batch.
 // GB300 issues FP64 some 64 times slower than FP32 (and with a long
 // latency), so the vectors and the PCG scalars are double-float (two
 // floats, about 48 bits); the mixed form's matrix (S, M) is FP32, so this
