@@ -594,18 +594,23 @@ __device__ void finish_lm_body(const DeviceBatch &B, bool count_body) {
 
 // K7: one CTA per problem.
 __global__ void __launch_bounds__(256) k_post_eval(DeviceBatch B, int count_body) {
-  __shared__ double red[8];
+  __shared__ double red[8 * 6];
   const int p = blockIdx.x;
   LMState *L = B.lm + p;
   if (L->active && L->need_jacobian) {
     const ProblemInfo pi = B.prob[p];
     const double *cs = B.chunk_scal;
-    const double cost = block_range_sum(cs + kCS_COST, pi.chunk_begin, pi.chunk_begin + pi.chunk_count, kChunkScal, red);
-    const double bad = block_range_max(cs + kCS_BAD, pi.chunk_begin, pi.chunk_begin + pi.chunk_count, kChunkScal, red);
-    const double gp = block_range_max(cs + kCS_GMAX, pi.chunk_begin, pi.chunk_begin + pi.chunk_count, kChunkScal, red);
-    const double gc = block_range_max(B.cam_scal + kCC_GMAX, pi.cam_begin, pi.cam_begin + pi.cam_count, kCamScal, red);
-    const double xc = block_range_sum(B.cam_scal + kCC_XN2, pi.cam_begin, pi.cam_begin + pi.cam_count, kCamScal, red);
-    const double xp = block_range_sum(cs + kCS_XN2, pi.chunk_begin, pi.chunk_begin + pi.chunk_count, kChunkScal, red);
+    // cost, bad, max |g| (points, cameras), |x|^2 (cameras, points)
+    const int h0 = pi.chunk_begin, h1 = pi.chunk_begin + pi.chunk_count;
+    const int k0 = pi.cam_begin, k1 = pi.cam_begin + pi.cam_count;
+    const double *const a[6] = {cs + kCS_COST, cs + kCS_BAD, cs + kCS_GMAX, B.cam_scal + kCC_GMAX,
+                                B.cam_scal + kCC_XN2, cs + kCS_XN2};
+    const int b[6] = {h0, h0, h0, k0, k0, h0}, e[6] = {h1, h1, h1, k1, k1, h1};
+    const int st[6] = {kChunkScal, kChunkScal, kChunkScal, kCamScal, kCamScal, kChunkScal};
+    const bool mx[6] = {false, true, true, true, false, false};
+    double r[6];
+    block_range_multi<6>(a, b, e, st, mx, r, red);
+    const double cost = r[0], bad = r[1], gp = r[2], gc = r[3], xc = r[4], xp = r[5];
     if (threadIdx.x == 0) {
       const DeviceOptions &o = B.opt;
       L->need_jacobian = 0;

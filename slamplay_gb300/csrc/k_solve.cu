@@ -539,20 +539,28 @@ __device__ __forceinline__ void terminate_(LMState *L, int type, int reason) {
 }
 
 __global__ void __launch_bounds__(256) k_decide(DeviceBatch B) {
-  __shared__ double red[8];
+  __shared__ double red[8 * 6];
   const int p = blockIdx.x;
   LMState *L = B.lm + p;
   if (!L->active) return;
   const ProblemInfo pi = B.prob[p];
   const int c0 = pi.chunk_begin, c1 = pi.chunk_begin + pi.chunk_count;
-  // model cost change -(m.r + |m|^2 / 2) summed; the mixed form adds its
-  // camera part of m.r = step.g here
-  double model = -block_range_sum(B.chunk_scal + kCS_MODEL, c0, c1, kChunkScal, red);
-  if (B.opt.mixed) model -= block_range_sum(B.cam_scal + kCC_YG, pi.cam_begin, pi.cam_begin + pi.cam_count, kCamScal, red);
-  const double cand = block_range_sum(B.chunk_scal + kCS_COST, c0, c1, kChunkScal, red);
-  const double bad = block_range_max(B.chunk_scal + kCS_BAD, c0, c1, kChunkScal, red);
-  const double s2p = block_range_sum(B.chunk_scal + kCS_STEP2, c0, c1, kChunkScal, red);
-  const double s2c = block_range_sum(B.cam_scal + kCC_STEP2, pi.cam_begin, pi.cam_begin + pi.cam_count, kCamScal, red);
+  const int k0 = pi.cam_begin, k1 = pi.cam_begin + pi.cam_count;
+  // model cost change -(m.r + |m|^2 / 2) summed (the mixed form adds its
+  // camera part of m.r = step.g), candidate cost, bad, |step|^2 (points,
+  // cameras): one pass
+  const double *cs = B.chunk_scal;
+  const double *const a[6] = {cs + kCS_MODEL, B.cam_scal + kCC_YG, cs + kCS_COST, cs + kCS_BAD, cs + kCS_STEP2,
+                              B.cam_scal + kCC_STEP2};
+  const int b[6] = {c0, k0, c0, c0, c0, k0};
+  const int e[6] = {c1, B.opt.mixed ? k1 : k0, c1, c1, c1, k1};
+  const int st[6] = {kChunkScal, kCamScal, kChunkScal, kChunkScal, kChunkScal, kCamScal};
+  const bool mx[6] = {false, false, false, true, false, false};
+  double r[6];
+  block_range_multi<6>(a, b, e, st, mx, r, red);
+  double model = -r[0];
+  if (B.opt.mixed) model -= r[1];
+  const double cand = r[2], bad = r[3], s2p = r[4], s2c = r[5];
   if (threadIdx.x != 0) return;
   const DeviceOptions &o = B.opt;
   const int it = ++L->iteration;

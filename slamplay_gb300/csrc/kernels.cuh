@@ -235,6 +235,42 @@ __device__ __forceinline__ double block_range_max(const double *a, int begin, in
   return block_max(s, red);
 }
 
+// N range reductions in one pass (one round of loads, one set of barriers):
+// value j is the sum, or with is_max[j] the maximum (from 0), of a[j][i *
+// stride[j]] over i in [begin[j], end[j]), each in exactly the order of its
+// own block_range_sum / block_range_max (so the same bits).  The totals are
+// valid in thread 0.  `red` needs (blockDim / 32) * N doubles.
+template <int N>
+__device__ __forceinline__ void block_range_multi(const double *const (&a)[N], const int (&begin)[N],
+                                                  const int (&end)[N], const int (&stride)[N],
+                                                  const bool (&is_max)[N], double (&out)[N], double *red) {
+  double v[N];
+#pragma unroll
+  for (int j = 0; j < N; ++j) {
+    v[j] = 0.0;
+#pragma unroll 8
+    for (int i = begin[j] + threadIdx.x; i < end[j]; i += blockDim.x) {
+      const double x = __ldcg(a[j] + (size_t)i * stride[j]);
+      v[j] = is_max[j] ? fmax(v[j], x) : v[j] + x;
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < N; ++j) v[j] = is_max[j] ? warp_max(v[j]) : warp_sum(v[j]);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  __syncthreads();
+  if (lane == 0)
+#pragma unroll
+    for (int j = 0; j < N; ++j) red[N * warp + j] = v[j];
+  __syncthreads();
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+      double s = 0.0;
+      for (int w = 0; w < nw; ++w) s = is_max[j] ? fmax(s, red[N * w + j]) : s + red[N * w + j];
+      out[j] = s;
+    }
+}
+
 // "Last CTA done" detection without waiting: each CTA bumps a counter after
 // a CTA barrier and a device-scope fence by the bumping thread (the barrier
 // orders every thread's earlier writes before that fence, the pattern of a
