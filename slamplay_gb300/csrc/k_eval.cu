@@ -63,8 +63,13 @@ __global__ void k_camera_table(DeviceBatch B) {
   }
 }
 
+// One warp per block: the per-camera work is FP64 (sin, cos, the dual-number
+// derivatives), and GB300's FP64 rate is per SM, so small warps spread the
+// cameras over more SMs.
+constexpr int kCamTableThreads = 32;
+
 void launch_camera_table(const DeviceBatch &b, cudaStream_t s) {
-  k_camera_table<<<(b.nc + 127) / 128, 128, 0, s>>>(b);
+  k_camera_table<<<(b.nc + kCamTableThreads - 1) / kCamTableThreads, kCamTableThreads, 0, s>>>(b);
 }
 
 // ---------------------------------------------------------------------------
@@ -714,7 +719,7 @@ __global__ void __launch_bounds__(kChunkCap) k_cost_chunk(DeviceBatch B) {
 }
 
 void launch_candidate_cost(const DeviceBatch &b, cudaStream_t s) {
-  k_candidate_cameras<<<(b.nc + 127) / 128, 128, 0, s>>>(b);
+  k_candidate_cameras<<<(b.nc + kCamTableThreads - 1) / kCamTableThreads, kCamTableThreads, 0, s>>>(b);
   k_cost_chunk<<<b.nchunks, kChunkCap, 0, s>>>(b);
 }
 
