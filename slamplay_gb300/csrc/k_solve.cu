@@ -56,23 +56,17 @@ struct PointSchurSmem {
 };
 
 // Lower Cholesky factor of a symmetric 3x3 (packed 00 01 02 11 12 22):
-// l00 l10 l11 l20 l21 l22, zero where a pivot is not positive.  In the
-// working precision: the factor only feeds F (stored in that precision), so
-// the mixed form takes FP32 square roots instead of FP64 ones.
-__device__ __forceinline__ double inv_pos(double x) { return recip_nr(x); }
-__device__ __forceinline__ float inv_pos(float x) { return __frcp_rn(x); }
-template <typename real>
-__device__ __forceinline__ void chol3(const real *A, real *L) {
-  const real z = (real)0;
-  const real l00 = A[0] > z ? sqrt(A[0]) : z;
-  const real i00 = l00 > z ? inv_pos(l00) : z;
-  const real l10 = A[1] * i00, l20 = A[2] * i00;
-  const real d1 = A[3] - l10 * l10;
-  const real l11 = d1 > z ? sqrt(d1) : z;
-  const real i11 = l11 > z ? inv_pos(l11) : z;
-  const real l21 = (A[4] - l20 * l10) * i11;
-  const real d2 = A[5] - l20 * l20 - l21 * l21;
-  const real l22 = d2 > z ? sqrt(d2) : z;
+// l00 l10 l11 l20 l21 l22, zero where a pivot is not positive.
+__device__ __forceinline__ void chol3(const double *A, double *L) {
+  const double l00 = A[0] > 0.0 ? sqrt(A[0]) : 0.0;
+  const double i00 = l00 > 0.0 ? recip_nr(l00) : 0.0;
+  const double l10 = A[1] * i00, l20 = A[2] * i00;
+  const double d1 = A[3] - l10 * l10;
+  const double l11 = d1 > 0.0 ? sqrt(d1) : 0.0;
+  const double i11 = l11 > 0.0 ? recip_nr(l11) : 0.0;
+  const double l21 = (A[4] - l20 * l10) * i11;
+  const double d2 = A[5] - l20 * l20 - l21 * l21;
+  const double l22 = d2 > 0.0 ? sqrt(d2) : 0.0;
   L[0] = l00, L[1] = l10, L[2] = l11, L[3] = l20, L[4] = l21, L[5] = l22;
 }
 
@@ -143,12 +137,10 @@ __global__ void __launch_bounds__(kChunkCap) k_point_schur(DeviceBatch B) {
       B.pt_t[3 * (size_t)j + 2] = t2;
       sm.tp[t][0] = (real)t0, sm.tp[t][1] = (real)t1, sm.tp[t][2] = (real)t2;
       if (B.explicit_schur) {
-        real Cr[6], Lc[6];
+        double Lc[6];
+        chol3(Ci, Lc);
 #pragma unroll
-        for (int q = 0; q < 6; ++q) Cr[q] = (real)Ci[q];
-        chol3(Cr, Lc);
-#pragma unroll
-        for (int q = 0; q < 6; ++q) sm.lc[t][q] = Lc[q];
+        for (int q = 0; q < 6; ++q) sm.lc[t][q] = (real)Lc[q];
       }
     }
     // the first (segment, entry) task of this thread: its metadata now
