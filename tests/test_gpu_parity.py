@@ -2,7 +2,7 @@
 
 Tolerances (stated per test):
   FP64 residual / Jacobian: |gpu - oracle| <= 1e-10 (1 + |row|_max) per entry
-  FP64 final cost: relative difference <= 1e-9 (the spec bar)
+  FP64 final cost: relative difference <= 1e-9 (the FP64 parity bar)
   mixed final cost: relative difference <= 1e-6 from the FP64 oracle
 """
 import numpy as np
