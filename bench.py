@@ -323,6 +323,12 @@ def run_gpu(args) -> None:
                           "solve (kernels inside the conditional graph cannot be bracketed one by one)",
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if not peaks.get("fallback")
                 else "fallback 6.8 TB/s (of fallback)"}
+        if top["name"] == "pcg_cluster" and first_m.num_iterations > 0:
+            per_it = 1e3 * avg_ms / max(1.0, first_m.num_linear_solver_iterations / first_m.num_iterations)
+            roof["per_pcg_iteration_us"] = per_it
+            roof["note"] = ("the whole PCG of an LM iteration in one launch: its algorithmic bytes (S, M^-1 and the "
+                            "PCG vectors, once) are small, and its time is the latency of ~2 cluster barriers and "
+                            "2 exchanges per PCG iteration (per_pcg_iteration_us), not HBM bandwidth")
     if rank == 0:
         cb = cpu_baseline() if world == 1 else None
         extra_forms = {}
