@@ -172,12 +172,56 @@ static void project_double(const double *cam, const double *pt, double pred[2]) 
   pred[1] = focal * distortion * yp;
 }
 
-int orc_residual_jacobian(const double cam[9], const double pt[3], const double uv[2],
-                          double r[2], double J[24]) {
+/* The camera update of the g2o variant (VertexPoseAndIntrinsics::oplusImpl,
+ * test_bundle_adjustment_g2o.cpp:84-90): R <- exp(dw) R, the other camera
+ * parameters additive.  In angle-axis form w' = log(exp(dw) exp(w)),
+ * composed through unit quaternions (q(w) = (cos |w|/2, sin(|w|/2) w/|w|),
+ * q' = q(dw) q(w), w' = 2 atan2(|v'|, s') v'/|v'| with s' >= 0). */
+static void aa_to_quat(const double w[3], double q[4]) {
+  const double th2 = w[0] * w[0] + w[1] * w[1] + w[2] * w[2];
+  if (th2 > 0.0) {
+    const double th = sqrt(th2), h = 0.5 * th, sc = sin(h) / th;
+    q[0] = cos(h), q[1] = w[0] * sc, q[2] = w[1] * sc, q[3] = w[2] * sc;
+  } else {
+    q[0] = 1.0, q[1] = 0.5 * w[0], q[2] = 0.5 * w[1], q[3] = 0.5 * w[2];
+  }
+}
+
+void orc_compose_left(const double dw[3], const double w[3], double out[3]) {
+  double a[4], b[4], q[4];
+  aa_to_quat(dw, a);
+  aa_to_quat(w, b);
+  q[0] = a[0] * b[0] - (a[1] * b[1] + a[2] * b[2] + a[3] * b[3]);
+  q[1] = a[0] * b[1] + b[0] * a[1] + (a[2] * b[3] - a[3] * b[2]);
+  q[2] = a[0] * b[2] + b[0] * a[2] + (a[3] * b[1] - a[1] * b[3]);
+  q[3] = a[0] * b[3] + b[0] * a[3] + (a[1] * b[2] - a[2] * b[1]);
+  if (q[0] < 0.0) q[0] = -q[0], q[1] = -q[1], q[2] = -q[2], q[3] = -q[3];
+  const double s2 = q[1] * q[1] + q[2] * q[2] + q[3] * q[3];
+  if (s2 > 0.0) {
+    const double sn = sqrt(s2), f = 2.0 * atan2(sn, q[0]) / sn;
+    out[0] = q[1] * f, out[1] = q[2] * f, out[2] = q[3] * f;
+  } else {
+    out[0] = 0.0, out[1] = 0.0, out[2] = 0.0;
+  }
+}
+
+/* Residual and Jacobian; so3_left: the rotation columns are derivatives
+ * with respect to the left perturbation dw of exp(dw) R(w) at dw = 0 (the
+ * jets rotate R(w) X by exp(dw) with dw = 0 + the unit parts: Rodrigues'
+ * first-order branch, exact for the derivative). */
+static int residual_jacobian_ex(const double cam[9], const double pt[3], const double uv[2], int so3_left,
+                                double r[2], double J[24]) {
   jet c[9], X[3], p[3];
   for (int k = 0; k < 9; ++k) c[k] = jvar(cam[k], k);
   for (int k = 0; k < 3; ++k) X[k] = jvar(pt[k], 9 + k);
-  rotate_jet(c, X, p);
+  if (so3_left) {
+    jet w[3], dw[3], p1[3];
+    for (int k = 0; k < 3; ++k) w[k] = jc(cam[k]), dw[k] = jvar(0.0, k);
+    rotate_jet(w, X, p1);
+    rotate_jet(dw, p1, p);
+  } else {
+    rotate_jet(c, X, p);
+  }
   p[0] = jadd(p[0], c[3]);
   p[1] = jadd(p[1], c[4]);
   p[2] = jadd(p[2], c[5]);
@@ -199,6 +243,11 @@ int orc_residual_jacobian(const double cam[9], const double pt[3], const double 
     ok = ok && isfinite(J[k]) && isfinite(J[NJ + k]);
   }
   return ok;
+}
+
+int orc_residual_jacobian(const double cam[9], const double pt[3], const double uv[2],
+                          double r[2], double J[24]) {
+  return residual_jacobian_ex(cam, pt, uv, 0, r, J);
 }
 
 /* ======================================================================== */
@@ -313,7 +362,7 @@ static int eval_cost(const orc_problem *p, const double *x, int loss, double a, 
 }
 
 /* residuals r (2*no) and Jacobians J (24*no), corrected for the loss; cost */
-static int eval_jacobian(const orc_problem *p, const double *x, int loss, double a, double *r,
+static int eval_jacobian(const orc_problem *p, const double *x, int loss, double a, int so3_left, double *r,
                          double *J, double *cost) {
   const int no = p->no, nb = (no + SUM_BLOCK - 1) / SUM_BLOCK;
   double *part = (double *)calloc((size_t)nb + 1, sizeof(double));
@@ -325,9 +374,8 @@ static int eval_jacobian(const orc_problem *p, const double *x, int loss, double
     const int e = (b + 1) * SUM_BLOCK < no ? (b + 1) * SUM_BLOCK : no;
     for (int i = b * SUM_BLOCK; i < e; ++i) {
       double *ri = r + 2 * (size_t)i, *Ji = J + 24 * (size_t)i;
-      if (!orc_residual_jacobian(x + 9 * (size_t)p->camera_index[i],
-                                 pts + 3 * (size_t)p->point_index[i], p->observations + 2 * i, ri,
-                                 Ji))
+      if (!residual_jacobian_ex(x + 9 * (size_t)p->camera_index[i], pts + 3 * (size_t)p->point_index[i],
+                                p->observations + 2 * i, so3_left, ri, Ji))
         ok = 0;
       acc += correct_block(loss, a, ri, Ji, 12, 12);
     }
@@ -340,17 +388,17 @@ static int eval_jacobian(const orc_problem *p, const double *x, int loss, double
   return ok && isfinite(c);
 }
 
-int orc_evaluate(const orc_problem *p, int loss, double loss_scale, double *residuals,
-                 double *jacobians, double *cost) {
+int orc_evaluate_ex(const orc_problem *p, int loss, double loss_scale, int camera_update, double *residuals,
+                    double *jacobians, double *cost) {
   const int no = p->no;
   double *r = residuals ? residuals : (double *)malloc(sizeof(double) * 2 * (size_t)no);
   double *J = jacobians ? jacobians : (double *)malloc(sizeof(double) * 24 * (size_t)no);
   int ok = 1;
   const double *pts = p->parameters + 9 * (size_t)p->nc;
   for (int i = 0; i < no; ++i)
-    ok &= orc_residual_jacobian(p->parameters + 9 * (size_t)p->camera_index[i],
-                                pts + 3 * (size_t)p->point_index[i], p->observations + 2 * i,
-                                r + 2 * (size_t)i, J + 24 * (size_t)i);
+    ok &= residual_jacobian_ex(p->parameters + 9 * (size_t)p->camera_index[i], pts + 3 * (size_t)p->point_index[i],
+                               p->observations + 2 * i, camera_update == ORC_UPDATE_SO3_LEFT, r + 2 * (size_t)i,
+                               J + 24 * (size_t)i);
   double c = 0.0;
   if (cost) {
     /* same blocked order as eval_cost */
@@ -366,6 +414,11 @@ int orc_evaluate(const orc_problem *p, int loss, double loss_scale, double *resi
   if (!residuals) free(r);
   if (!jacobians) free(J);
   return ok;
+}
+
+int orc_evaluate(const orc_problem *p, int loss, double loss_scale, double *residuals,
+                 double *jacobians, double *cost) {
+  return orc_evaluate_ex(p, loss, loss_scale, ORC_UPDATE_ADDITIVE, residuals, jacobians, cost);
 }
 
 /* ======================================================================== */
@@ -1036,7 +1089,7 @@ int orc_compute_step(const orc_problem *p, const orc_options *o, double radius, 
   double *D = (double *)malloc(sizeof(double) * (size_t)n);
   double *y = (double *)malloc(sizeof(double) * (size_t)n);
   double cost;
-  int ok = eval_jacobian(p, p->parameters, o->loss, o->loss_scale, r, J, &cost);
+  int ok = eval_jacobian(p, p->parameters, o->loss, o->loss_scale, o->camera_update == ORC_UPDATE_SO3_LEFT, r, J, &cost);
   int it = 0;
   if (ok) {
     column_norms(p, &st, J, cn);
@@ -1108,7 +1161,7 @@ int orc_solve(const orc_problem *p, const orc_options *o, orc_summary *s) {
   double x_cost = 0.0, x_norm = used_norm(&st, x), gmax = 0.0;
   int term = -1, reason = 0;
 
-  int ok = eval_jacobian(p, x, o->loss, o->loss_scale, r, J, &x_cost);
+  int ok = eval_jacobian(p, x, o->loss, o->loss_scale, o->camera_update == ORC_UPDATE_SO3_LEFT, r, J, &x_cost);
   if (!ok) {
     term = 2;
     reason = 7;
@@ -1172,11 +1225,17 @@ int orc_solve(const orc_problem *p, const orc_options *o, orc_summary *s) {
       reuse_diagonal = 1;
     } else {
       invalid_run = 0;
-      for (int c = 0; c < p->nc; ++c)
+      for (int c = 0; c < p->nc; ++c) {
         for (int q = 0; q < 9; ++q) {
           const size_t k = 9 * (size_t)c + q;
           xc[k] = st.cam_used[c] ? x[k] + y[k] * scale[k] : x[k];
         }
+        if (o->camera_update == ORC_UPDATE_SO3_LEFT && st.cam_used[c]) {
+          const size_t k = 9 * (size_t)c;
+          const double dw[3] = {y[k] * scale[k], y[k + 1] * scale[k + 1], y[k + 2] * scale[k + 2]};
+          orc_compose_left(dw, x + k, xc + k);
+        }
+      }
       for (int j = 0; j < p->np; ++j)
         for (int q = 0; q < 3; ++q) {
           const size_t k = 9 * (size_t)p->nc + 3 * (size_t)j + q;
@@ -1207,7 +1266,7 @@ int orc_solve(const orc_problem *p, const orc_options *o, orc_summary *s) {
       if (rel > o->min_relative_decrease) {
         memcpy(x, xc, sizeof(double) * (size_t)n);
         x_norm = used_norm(&st, x);
-        if (!eval_jacobian(p, x, o->loss, o->loss_scale, r, J, &x_cost)) {
+        if (!eval_jacobian(p, x, o->loss, o->loss_scale, o->camera_update == ORC_UPDATE_SO3_LEFT, r, J, &x_cost)) {
           term = 2;
           reason = 7;
           break;
@@ -1257,7 +1316,7 @@ done:
   {
     /* final cost and gradient at the returned parameters */
     double fc = 0.0;
-    if (eval_jacobian(p, p->parameters, o->loss, o->loss_scale, r, J, &fc)) {
+    if (eval_jacobian(p, p->parameters, o->loss, o->loss_scale, o->camera_update == ORC_UPDATE_SO3_LEFT, r, J, &fc)) {
       gradient(&st, J, r, g);
       s->gradient_max_norm = gradient_max_norm(&st, p->parameters, g);
     }

@@ -47,6 +47,8 @@ typedef struct orc_problem {
 enum { ORC_LOSS_TRIVIAL = 0, ORC_LOSS_HUBER = 1, ORC_LOSS_CAUCHY = 2 };
 enum { ORC_SOLVER_DENSE_SCHUR = 0, ORC_SOLVER_PCG_SCHUR = 1 };
 enum { ORC_PCG_RESIDUAL = 0, ORC_PCG_QUADRATIC_MODEL = 1 };
+/* camera update: Ceres' additive angle-axis, or g2o's R <- exp(dw) R */
+enum { ORC_UPDATE_ADDITIVE = 0, ORC_UPDATE_SO3_LEFT = 1 };
 
 typedef struct orc_options {
   int max_num_iterations;
@@ -63,6 +65,7 @@ typedef struct orc_options {
   double pcg_tolerance, eta;
   int num_threads; /* 0 = OpenMP default */
   int verbose;
+  int camera_update; /* ORC_UPDATE_* */
 } orc_options;
 
 typedef struct orc_summary {
@@ -87,9 +90,14 @@ void orc_angle_axis_rotate_point(const double aa[3], const double pt[3], double 
 int orc_residual_jacobian(const double cam[9], const double pt[3], const double uv[2],
                           double r[2], double J[24]);
 
+/* w' = log(exp(dw) exp(w)) in angle-axis form (the g2o camera update). */
+void orc_compose_left(const double dw[3], const double w[3], double out[3]);
+
 /* Residuals (2*no) and Jacobians (24*no) of every observation in input order
  * (either may be NULL) and the cost 0.5*sum rho(|r|^2).  Returns 0 on a
  * non-finite evaluation. */
+int orc_evaluate_ex(const orc_problem *p, int loss, double loss_scale, int camera_update, double *residuals,
+                    double *jacobians, double *cost);
 int orc_evaluate(const orc_problem *p, int loss, double loss_scale, double *residuals,
                  double *jacobians, double *cost);
 

@@ -34,7 +34,7 @@ class OrcOptions(C.Structure):
         ("loss", C.c_int), ("loss_scale", C.c_double), ("linear_solver", C.c_int),
         ("pcg_criterion", C.c_int), ("max_linear_solver_iterations", C.c_int),
         ("min_linear_solver_iterations", C.c_int), ("pcg_tolerance", C.c_double), ("eta", C.c_double),
-        ("num_threads", C.c_int), ("verbose", C.c_int),
+        ("num_threads", C.c_int), ("verbose", C.c_int), ("camera_update", C.c_int),
     ]
 
 
@@ -52,6 +52,7 @@ class OrcSummary(C.Structure):
 
 LOSS = {"trivial": 0, "huber": 1, "cauchy": 2}
 SOLVER = {"dense_schur": 0, "pcg_schur": 1}
+CAMERA_UPDATE = {"additive": 0, "so3_left": 1}
 
 _orc = None
 _ref = None
@@ -74,6 +75,9 @@ def oracle():
         L.orc_angle_axis_rotate_point.argtypes = [_f64p, _f64p, _f64p]
         L.orc_evaluate.argtypes = [C.POINTER(OrcProblem), C.c_int, C.c_double, _f64p, _f64p, _f64p]
         L.orc_evaluate.restype = C.c_int
+        L.orc_evaluate_ex.argtypes = [C.POINTER(OrcProblem), C.c_int, C.c_double, C.c_int, _f64p, _f64p, _f64p]
+        L.orc_evaluate_ex.restype = C.c_int
+        L.orc_compose_left.argtypes = [_f64p, _f64p, _f64p]
         L.orc_compute_step.argtypes = [C.POINTER(OrcProblem), C.POINTER(OrcOptions), C.c_double, _f64p, _f64p,
                                        C.POINTER(C.c_int)]
         L.orc_compute_step.restype = C.c_int
@@ -126,6 +130,8 @@ def options(**kw) -> OrcOptions:
             v = LOSS[v]
         if k == "linear_solver" and isinstance(v, str):
             v = SOLVER[v]
+        if k == "camera_update" and isinstance(v, str):
+            v = CAMERA_UPDATE[v]
         if k == "pcg_criterion" and isinstance(v, str):
             v = {"residual": 0, "quadratic_model": 1}[v]
         setattr(o, k, v)
@@ -148,14 +154,23 @@ class Problem:
                    b.parameters())
 
 
-def evaluate(p: Problem, loss="trivial", loss_scale=1.0):
+def evaluate(p: Problem, loss="trivial", loss_scale=1.0, camera_update="additive"):
     no = p.s.no
     r = np.zeros(2 * no)
     J = np.zeros(24 * no)
     c = C.c_double()
-    ok = oracle().orc_evaluate(C.byref(p.s), LOSS[loss] if isinstance(loss, str) else loss, loss_scale, f64(r),
-                               f64(J), C.byref(c))
+    ok = oracle().orc_evaluate_ex(C.byref(p.s), LOSS[loss] if isinstance(loss, str) else loss, loss_scale,
+                                  CAMERA_UPDATE[camera_update], f64(r), f64(J), C.byref(c))
     return r.reshape(no, 2), J.reshape(no, 2, 12), c.value, bool(ok)
+
+
+def compose_left(dw, w):
+    """w' = log(exp(dw) exp(w)) in angle-axis form."""
+    a = np.ascontiguousarray(dw, dtype=np.float64)
+    b = np.ascontiguousarray(w, dtype=np.float64)
+    out = np.zeros(3)
+    oracle().orc_compose_left(f64(a), f64(b), f64(out))
+    return out
 
 
 def compute_step(p: Problem, radius: float, **kw):

@@ -105,3 +105,65 @@ def test_final_cost_matches_scipy_least_squares():
     r = O.solve(p, max_num_iterations=100, linear_solver="dense_schur", function_tolerance=1e-15,
                 parameter_tolerance=1e-15, gradient_tolerance=1e-15)
     assert abs(r["final_cost"] - ls.cost) <= 1e-6 * ls.cost, (r["final_cost"], ls.cost)
+
+
+def _rotate(w, x):
+    out = np.zeros(3)
+    O.oracle().orc_angle_axis_rotate_point(O.f64(np.ascontiguousarray(w, dtype=np.float64)),
+                                           O.f64(np.ascontiguousarray(x, dtype=np.float64)), O.f64(out))
+    return out
+
+
+def _rotation_matrix(w):
+    return np.stack([_rotate(w, e) for e in np.eye(3)], axis=1)
+
+
+@pytest.mark.parametrize("scale", [2.0, 0.3, 1e-5, 0.0])
+def test_compose_left_is_rotation_product(scale):
+    """The g2o camera update R <- exp(dw) R (test_bundle_adjustment_g2o.cpp:84-90) in angle-axis form."""
+    rng = np.random.default_rng(int(scale * 1e6) + 3)
+    for _ in range(200):
+        w = rng.normal(size=3) * scale
+        dw = rng.normal(size=3) * rng.choice([1.0, 1e-3, 1e-9])
+        out = O.compose_left(dw, w)
+        assert np.linalg.norm(out) <= np.pi + 1e-12
+        np.testing.assert_allclose(_rotation_matrix(out), _rotation_matrix(dw) @ _rotation_matrix(w), atol=1e-13)
+    np.testing.assert_array_equal(O.compose_left(np.zeros(3), np.zeros(3)), np.zeros(3))
+
+
+def test_so3_left_jacobian_matches_central_differences():
+    b = BALProblem.synthetic(0, seed=2, num_points=30)
+    p = O.Problem.from_bal(b)
+    r0, Ja, _, ok = O.evaluate(p)
+    r1, Jl, _, ok1 = O.evaluate(p, camera_update="so3_left")
+    assert ok and ok1
+    np.testing.assert_array_equal(r0, r1)
+    np.testing.assert_array_equal(Ja[:, :, 3:], Jl[:, :, 3:])
+    cams = b.cameras().reshape(-1, 9)
+    pts = b.points().reshape(-1, 3)
+    for i in range(0, b.num_observations(), 13):
+        cam = cams[b.camera_index()[i]]
+        pt = np.ascontiguousarray(pts[b.point_index()[i]])
+        uv = np.ascontiguousarray(b.observations()[2 * i: 2 * i + 2])
+        h = 1e-6
+        for k in range(3):
+            rr = []
+            for s in (+1, -1):
+                c = cam.copy()
+                c[:3] = O.compose_left(s * h * np.eye(3)[k], cam[:3])
+                r = np.zeros(2)
+                O.oracle().orc_residual_jacobian(O.f64(c), O.f64(pt), O.f64(uv), O.f64(r), O.f64(np.zeros(24)))
+                rr.append(r)
+            fd = (rr[0] - rr[1]) / (2 * h)
+            assert np.allclose(Jl[i, :, k], fd, rtol=1e-5, atol=1e-5 * (1 + np.abs(Jl[i]).max())), (k, Jl[i, :, k], fd)
+
+
+def test_so3_left_update_reaches_the_additive_minimum():
+    b, truth = BALProblem.synthetic(0, seed=5, num_points=400, pixel_noise=0.0, return_truth=True)
+    r = O.solve(O.Problem.from_bal(b), max_num_iterations=30, linear_solver="dense_schur", camera_update="so3_left")
+    assert r["initial_cost"] > 1e3 and r["final_cost"] < 1e-12 * r["initial_cost"]
+    b = BALProblem.synthetic(0, seed=6, num_points=500)
+    a = O.solve(O.Problem.from_bal(b), max_num_iterations=40, linear_solver="dense_schur")
+    c = O.solve(O.Problem.from_bal(b), max_num_iterations=40, linear_solver="dense_schur", camera_update="so3_left")
+    assert a["final_cost"] < a["initial_cost"] and abs(a["final_cost"] - c["final_cost"]) <= 1e-6 * a["final_cost"]
+    assert not np.array_equal(a["trace_cost"][1:3], c["trace_cost"][1:3])
