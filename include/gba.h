@@ -99,6 +99,18 @@ typedef enum gba_schur {
                              iteration; each PCG iteration multiplies by them    */
 } gba_schur;
 
+/* How an accepted step updates a camera's rotation (the first three camera
+ * parameters, angle-axis w).  ADDITIVE is the Ceres reference's
+ * (test_bundle_adjustment_ceres.cpp: parameters plus step); SO3_LEFT is the
+ * g2o variant's VertexPoseAndIntrinsics::oplusImpl
+ * (test_bundle_adjustment_g2o.cpp:84-90): R <- exp(dw) R, the Jacobian's
+ * rotation columns taken with respect to dw.  Translation, focal length and
+ * distortion are additive in both. */
+typedef enum gba_camera_update {
+  GBA_CAMERA_UPDATE_ADDITIVE = 0,
+  GBA_CAMERA_UPDATE_SO3_LEFT = 1
+} gba_camera_update;
+
 /* ------------------------------------------------------------------------ */
 /* Options.  Defaults (gba_options_init) are Ceres 2.2's Solver::Options     */
 /* defaults for the fields the reference leaves unset                        */
@@ -141,7 +153,8 @@ typedef struct gba_options {
                                          in one launch (a thread-block cluster per
                                          problem) when it fits; 0 = one launch pair per
                                          PCG iteration                               */
-  int32_t reserved[4];
+  int32_t camera_update;              /* gba_camera_update, GBA_CAMERA_UPDATE_ADDITIVE */
+  int32_t reserved[3];
 } gba_options;
 
 /* Per-solve report, the subset of ceres::Solver::Summary the reference

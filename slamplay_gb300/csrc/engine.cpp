@@ -276,6 +276,7 @@ size_t Engine::layout(const HostBatch &hb, char *base, DeviceBatch *db, size_t *
   b.opt.max_pcg_iterations = o_.max_linear_solver_iterations;
   b.opt.min_pcg_iterations = o_.min_linear_solver_iterations;
   b.opt.mixed = mixed_ ? 1 : 0;
+  b.opt.so3_left = o_.camera_update == GBA_CAMERA_UPDATE_SO3_LEFT ? 1 : 0;
   b.lm_cond = 0;
   b.pcg_cond = 0;
   b.use_cond = 0;

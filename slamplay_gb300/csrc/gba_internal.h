@@ -48,6 +48,7 @@ struct DeviceOptions {
   double pcg_tolerance, eta;
   int32_t max_iterations, max_invalid_steps, jacobi_scaling, loss;
   int32_t pcg_criterion, max_pcg_iterations, min_pcg_iterations, mixed;
+  int32_t so3_left;  // camera rotation update R <- exp(dw) R (else additive)
 };
 
 // LM / trust-region state of one problem, resident on the device.

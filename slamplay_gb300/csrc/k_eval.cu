@@ -52,6 +52,7 @@ __global__ void k_camera_table(DeviceBatch B) {
   if (!L->active || !L->need_jacobian) return;
   double *tab = B.cam_table + (size_t)kCamTable * c;
   camera_table_entry(B.cam_param[L->parity] + 9 * (size_t)c, tab, true);
+  if (B.opt.so3_left) so3_left_derivatives(tab);
   if (B.opt.mixed) {
     float *tf = B.cam_tablef + (size_t)kCamTable * c;
     float2 *td = B.cam_tabledf + (size_t)kCamTable * c;
@@ -676,6 +677,14 @@ __global__ void k_candidate_cameras(DeviceBatch B) {
   for (int q = 0; q < 9; ++q) {
     const double step = -B.pcg_x[9 * (size_t)c + q];
     cand[q] = used ? x[q] + step * B.cam_scale[9 * (size_t)c + q] : x[q];
+  }
+  if (B.opt.so3_left && used) {
+    const double dw[3] = {-B.pcg_x[9 * (size_t)c + 0] * B.cam_scale[9 * (size_t)c + 0],
+                          -B.pcg_x[9 * (size_t)c + 1] * B.cam_scale[9 * (size_t)c + 1],
+                          -B.pcg_x[9 * (size_t)c + 2] * B.cam_scale[9 * (size_t)c + 2]};
+    compose_left(dw, x, cand);
+  }
+  for (int q = 0; q < 9; ++q) {
     const double d = x[q] - cand[q];
     s2 += d * d;
     xc[q] = cand[q];

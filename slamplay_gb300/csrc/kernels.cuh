@@ -382,6 +382,57 @@ __device__ inline void camera_table_entry(const double *cam, double *tab, bool d
 }
 
 // ---------------------------------------------------------------------------
+// Left-multiplicative rotation update R <- exp(dw) R (the g2o variant's
+// VertexPoseAndIntrinsics::oplusImpl, test_bundle_adjustment_g2o.cpp:84-90).
+// At dw = 0, d(exp(dw) R X)/d dw_k = e_k x (R X), so dR_k = [e_k]_x R: rows
+// of R moved and negated, exact.  Replaces tab[9..35] of a camera table.
+__device__ inline void so3_left_derivatives(double *tab) {
+  const double *R = tab;
+  double *d0 = tab + 9, *d1 = tab + 18, *d2 = tab + 27;
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    d0[0 + j] = 0.0, d0[3 + j] = -R[6 + j], d0[6 + j] = R[3 + j];
+    d1[0 + j] = R[6 + j], d1[3 + j] = 0.0, d1[6 + j] = -R[0 + j];
+    d2[0 + j] = -R[3 + j], d2[3 + j] = R[0 + j], d2[6 + j] = 0.0;
+  }
+}
+
+// Unit quaternion (s, v) of angle-axis w: (cos(|w|/2), sin(|w|/2) w / |w|);
+// (1, w / 2) at w = 0.
+__device__ inline void aa_quat(const double *w, double q[4]) {
+  const double th2 = w[0] * w[0] + w[1] * w[1] + w[2] * w[2];
+  if (th2 > 0.0) {
+    const double th = sqrt(th2);
+    double sh, ch;
+    sincos(0.5 * th, &sh, &ch);
+    const double sc = sh / th;
+    q[0] = ch, q[1] = w[0] * sc, q[2] = w[1] * sc, q[3] = w[2] * sc;
+  } else {
+    q[0] = 1.0, q[1] = 0.5 * w[0], q[2] = 0.5 * w[1], q[3] = 0.5 * w[2];
+  }
+}
+
+// out = log(exp(dw) exp(w)) in angle-axis form: Hamilton product of the two
+// unit quaternions, sign fixed to s >= 0, w' = 2 atan2(|v|, s) v / |v|.
+__device__ inline void compose_left(const double *dw, const double *w, double *out) {
+  double a[4], b[4], q[4];
+  aa_quat(dw, a);
+  aa_quat(w, b);
+  q[0] = a[0] * b[0] - (a[1] * b[1] + a[2] * b[2] + a[3] * b[3]);
+  q[1] = a[0] * b[1] + b[0] * a[1] + (a[2] * b[3] - a[3] * b[2]);
+  q[2] = a[0] * b[2] + b[0] * a[2] + (a[3] * b[1] - a[1] * b[3]);
+  q[3] = a[0] * b[3] + b[0] * a[3] + (a[1] * b[2] - a[2] * b[1]);
+  const double sg = q[0] < 0.0 ? -1.0 : 1.0;
+  const double s2 = q[1] * q[1] + q[2] * q[2] + q[3] * q[3];
+  if (s2 > 0.0) {
+    const double sn = sqrt(s2), f = sg * 2.0 * atan2(sn, sg * q[0]) / sn;
+    out[0] = q[1] * f, out[1] = q[2] * f, out[2] = q[3] * f;
+  } else {
+    out[0] = 0.0, out[1] = 0.0, out[2] = 0.0;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Snavely projection (utils/camera/SnavelyReprojectionError.h:61-87) on the
 // camera table: P = R X + t; x' = -P_x/P_z; d = 1 + r2 (k1 + k2 r2);
 // prediction = f d x'.  Residual = prediction - observation (:49-50).

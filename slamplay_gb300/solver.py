@@ -87,8 +87,9 @@ def _summary(s: N.Summary, tr: _Trace | None) -> SolveSummary:
 
 def make_options(**kw) -> N.Options:
     """gba_options with Ceres' defaults, overridden by keyword (loss,
-    precision, pcg_criterion and schur accept names: loss='huber',
-    precision='mixed', schur='explicit')."""
+    precision, pcg_criterion, schur and camera_update accept names:
+    loss='huber', precision='mixed', schur='explicit',
+    camera_update='so3_left')."""
     o = N.Options()
     N.lib().gba_options_init(N.C.byref(o))
     for k, v in kw.items():
@@ -100,6 +101,8 @@ def make_options(**kw) -> N.Options:
             v = N.PCG_CRITERION[v]
         elif k == "schur" and isinstance(v, str):
             v = N.SCHUR[v]
+        elif k == "camera_update" and isinstance(v, str):
+            v = N.CAMERA_UPDATE[v]
         elif k == "stream" and v is not None and not isinstance(v, int):
             v = int(v)
         if not hasattr(o, k):

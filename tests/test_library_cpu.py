@@ -42,6 +42,7 @@ def test_option_defaults_are_ceres_defaults():
     assert o.min_relative_decrease == 1e-3 and o.min_lm_diagonal == 1e-6 and o.max_lm_diagonal == 1e32
     assert o.jacobi_scaling == 1 and o.max_num_consecutive_invalid_steps == 5
     assert o.loss == 0 and o.precision == 0
+    assert o.camera_update == 0 and make_options(camera_update="so3_left").camera_update == 1
     with pytest.raises(TypeError):
         make_options(no_such_option=1)
 
@@ -66,6 +67,9 @@ def test_create_without_gpu_fails_cleanly():
 def test_bad_options_rejected_before_device():
     with pytest.raises(GBAError) as ei:
         Solver(loss=7)
+    assert ei.value.status == 1
+    with pytest.raises(GBAError) as ei:
+        Solver(camera_update=2)
     assert ei.value.status == 1
 
 
