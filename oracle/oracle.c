@@ -1127,8 +1127,28 @@ static void trace_put(orc_summary *s, int it, double cost, double radius, int li
   if (it + 1 > s->trace_length) s->trace_length = it + 1;
 }
 
+/* g2o's Levenberg policy (OptimizationAlgorithmLevenberg, g2o tag
+ * 20230223_git, which test_bundle_adjustment_g2o.cpp:174-176 selects; the
+ * library is cloned by build_thirdparty.sh:248-254 and absent here, so this
+ * restates its published algorithm):
+ *   damping H + lambda I on the unscaled normal equations (no Jacobi scaling);
+ *   lambda_0 = tau * max diag(H) at the initial point, tau = 1e-5;
+ *   gain rho = (chi2 - chi2_new) / (dx.(lambda dx + b) + 1e-3), chi2 = 2 cost,
+ *     and dx.(lambda dx + b) = 2 * model_cost_change for the solved step;
+ *   rho > 0: accept, lambda *= max(1/3, min(2/3, 1 - (2 rho - 1)^3)), nu = 2
+ *     (Nielsen's update with the factor capped at 2/3);
+ *   else: reject, lambda *= nu, nu *= 2;
+ *   one outer iteration = trials until the first accepted step, at most 10;
+ *   the solve stops when the 10th trial of an outer iteration has run, when a
+ *   trial gives rho == 0 exactly, when lambda is no longer finite, or after
+ *   max_num_iterations outer iterations.  lambda = 1 / radius below. */
+#define ORC_G2O_TAU 1e-5
+#define ORC_G2O_MAX_TRIALS 10
+
 int orc_solve(const orc_problem *p, const orc_options *o, orc_summary *s) {
   set_threads(o);
+  const int g2o = o->lm_policy == ORC_LM_G2O;
+  int trials = 0, outer = 0;
   structure st;
   build_structure(p, &st);
   const int n = st.n;
@@ -1171,8 +1191,13 @@ int orc_solve(const orc_problem *p, const orc_options *o, orc_summary *s) {
   gradient(&st, J, r, g);
   gmax = gradient_max_norm(&st, x, g);
   column_norms(p, &st, J, cn);
-  jacobi_scale(&st, cn, o->jacobi_scaling, scale);
+  jacobi_scale(&st, cn, o->jacobi_scaling && !g2o, scale);
   scale_columns(p, J, scale);
+  if (g2o) {
+    double hmax = 0.0;
+    for (int k = 0; k < n; ++k) hmax = fmax(hmax, cn[k]);
+    radius = 1.0 / (ORC_G2O_TAU * hmax);
+  }
   s->initial_cost = x_cost;
   double minimum_cost = x_cost;
   trace_put(s, 0, x_cost, radius, 0, 1);
@@ -1183,6 +1208,7 @@ int orc_solve(const orc_problem *p, const orc_options *o, orc_summary *s) {
   if (o->max_num_iterations <= 0) {
     term = 1;
     reason = 1;
+  } else if (g2o) {
   } else if (gmax <= o->gradient_tolerance) {
     term = 0;
     reason = 3;
@@ -1195,7 +1221,7 @@ int orc_solve(const orc_problem *p, const orc_options *o, orc_summary *s) {
     ++iteration;
     if (!reuse_diagonal) {
       column_norms(p, &st, J, cn);
-      for (int k = 0; k < n; ++k) diag[k] = fmin(fmax(cn[k], o->min_lm_diagonal), o->max_lm_diagonal);
+      for (int k = 0; k < n; ++k) diag[k] = g2o ? 1.0 : fmin(fmax(cn[k], o->min_lm_diagonal), o->max_lm_diagonal);
     }
     for (int k = 0; k < n; ++k) D[k] = sqrt(diag[k] / radius);
     int lin_it = 0;
@@ -1210,10 +1236,10 @@ int orc_solve(const orc_problem *p, const orc_options *o, orc_summary *s) {
       valid = mcc > 0.0;
     }
     int successful = 0;
-    double iter_cost = x_cost;
+    double iter_cost = x_cost, rho = -1.0;
     if (!valid) {
       ++s->num_invalid_steps;
-      if (++invalid_run >= o->max_num_consecutive_invalid_steps) {
+      if (!g2o && ++invalid_run >= o->max_num_consecutive_invalid_steps) {
         term = 2;
         reason = 6;
         ++s->num_unsuccessful_steps;
@@ -1247,7 +1273,7 @@ int orc_solve(const orc_problem *p, const orc_options *o, orc_summary *s) {
       if (o->verbose)
         printf("%4d %.6e %.2e %.2e %.2e %.2e %.2e %4d\n", iteration, cand_cost, x_cost - cand_cost,
                gmax, step_norm, (x_cost - cand_cost) / mcc, radius, lin_it);
-      if (step_norm <= o->parameter_tolerance * (x_norm + o->parameter_tolerance)) {
+      if (!g2o && step_norm <= o->parameter_tolerance * (x_norm + o->parameter_tolerance)) {
         term = 0;
         reason = 4;
         ++s->num_unsuccessful_steps;
@@ -1255,7 +1281,7 @@ int orc_solve(const orc_problem *p, const orc_options *o, orc_summary *s) {
         break;
       }
       const double cost_change = x_cost - cand_cost;
-      if (fabs(cost_change) <= o->function_tolerance * x_cost) {
+      if (!g2o && fabs(cost_change) <= o->function_tolerance * x_cost) {
         term = 0;
         reason = 2;
         ++s->num_unsuccessful_steps;
@@ -1263,7 +1289,8 @@ int orc_solve(const orc_problem *p, const orc_options *o, orc_summary *s) {
         break;
       }
       const double rel = (cand_cost >= DBL_MAX) ? -DBL_MAX : (x_cost - cand_cost) / mcc;
-      if (rel > o->min_relative_decrease) {
+      if (g2o) rho = (cand_cost >= DBL_MAX) ? -DBL_MAX : 2.0 * (x_cost - cand_cost) / (2.0 * mcc + 1e-3);
+      if (g2o ? rho > 0.0 : rel > o->min_relative_decrease) {
         memcpy(x, xc, sizeof(double) * (size_t)n);
         x_norm = used_norm(&st, x);
         if (!eval_jacobian(p, x, o->loss, o->loss_scale, o->camera_update == ORC_UPDATE_SO3_LEFT, r, J, &x_cost)) {
@@ -1274,9 +1301,14 @@ int orc_solve(const orc_problem *p, const orc_options *o, orc_summary *s) {
         gradient(&st, J, r, g);
         gmax = gradient_max_norm(&st, x, g);
         scale_columns(p, J, scale);
-        const double t = 2.0 * rel - 1.0;
-        radius = radius / fmax(1.0 / 3.0, 1.0 - t * t * t);
-        radius = fmin(o->max_trust_region_radius, radius);
+        if (g2o) {
+          const double t = 2.0 * rho - 1.0;
+          radius = fmin(DBL_MAX, radius / fmax(1.0 / 3.0, fmin(2.0 / 3.0, 1.0 - t * t * t)));
+        } else {
+          const double t = 2.0 * rel - 1.0;
+          radius = radius / fmax(1.0 / 3.0, 1.0 - t * t * t);
+          radius = fmin(o->max_trust_region_radius, radius);
+        }
         decrease_factor = 2.0;
         reuse_diagonal = 0;
         successful = 1;
@@ -1297,7 +1329,17 @@ int orc_solve(const orc_problem *p, const orc_options *o, orc_summary *s) {
     else
       ++s->num_unsuccessful_steps;
     trace_put(s, iteration, iter_cost, radius, lin_it, successful);
-    if (iteration >= o->max_num_iterations) {
+    if (g2o) {
+      ++trials;
+      if (trials >= ORC_G2O_MAX_TRIALS || (!successful && (rho == 0.0 || radius <= 0.0))) {
+        term = 0;
+        reason = 8;
+      } else if (successful && ++outer >= o->max_num_iterations) {
+        term = 1;
+        reason = 1;
+      }
+      if (successful) trials = 0;
+    } else if (iteration >= o->max_num_iterations) {
       term = 1;
       reason = 1;
     } else if (successful && gmax <= o->gradient_tolerance) {

@@ -49,6 +49,9 @@ enum { ORC_SOLVER_DENSE_SCHUR = 0, ORC_SOLVER_PCG_SCHUR = 1 };
 enum { ORC_PCG_RESIDUAL = 0, ORC_PCG_QUADRATIC_MODEL = 1 };
 /* camera update: Ceres' additive angle-axis, or g2o's R <- exp(dw) R */
 enum { ORC_UPDATE_ADDITIVE = 0, ORC_UPDATE_SO3_LEFT = 1 };
+/* LM damping policy: Ceres' LevenbergMarquardtStrategy, or g2o's
+ * OptimizationAlgorithmLevenberg (g2o tag 20230223_git) */
+enum { ORC_LM_CERES = 0, ORC_LM_G2O = 1 };
 
 typedef struct orc_options {
   int max_num_iterations;
@@ -66,6 +69,7 @@ typedef struct orc_options {
   int num_threads; /* 0 = OpenMP default */
   int verbose;
   int camera_update; /* ORC_UPDATE_* */
+  int lm_policy;     /* ORC_LM_* */
 } orc_options;
 
 typedef struct orc_summary {

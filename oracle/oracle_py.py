@@ -35,6 +35,7 @@ class OrcOptions(C.Structure):
         ("pcg_criterion", C.c_int), ("max_linear_solver_iterations", C.c_int),
         ("min_linear_solver_iterations", C.c_int), ("pcg_tolerance", C.c_double), ("eta", C.c_double),
         ("num_threads", C.c_int), ("verbose", C.c_int), ("camera_update", C.c_int),
+        ("lm_policy", C.c_int),
     ]
 
 
@@ -53,6 +54,8 @@ class OrcSummary(C.Structure):
 LOSS = {"trivial": 0, "huber": 1, "cauchy": 2}
 SOLVER = {"dense_schur": 0, "pcg_schur": 1}
 CAMERA_UPDATE = {"additive": 0, "so3_left": 1}
+LM_POLICY = {"ceres": 0, "g2o": 1}
+G2O_MAX_TRIALS = 10
 
 _orc = None
 _ref = None
@@ -132,6 +135,8 @@ def options(**kw) -> OrcOptions:
             v = SOLVER[v]
         if k == "camera_update" and isinstance(v, str):
             v = CAMERA_UPDATE[v]
+        if k == "lm_policy" and isinstance(v, str):
+            v = LM_POLICY[v]
         if k == "pcg_criterion" and isinstance(v, str):
             v = {"residual": 0, "quadratic_model": 1}[v]
         setattr(o, k, v)
@@ -185,7 +190,7 @@ def compute_step(p: Problem, radius: float, **kw):
 def solve(p: Problem, **kw):
     """Runs the oracle LM; returns a dict with the summary and the trace."""
     o = options(**kw)
-    cap = max(1, o.max_num_iterations + 1)
+    cap = max(1, o.max_num_iterations * (G2O_MAX_TRIALS if o.lm_policy == 1 else 1) + 1)
     tc = np.zeros(cap)
     tr = np.zeros(cap)
     tl = np.zeros(cap, np.int32)

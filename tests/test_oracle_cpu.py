@@ -167,3 +167,70 @@ def test_so3_left_update_reaches_the_additive_minimum():
     c = O.solve(O.Problem.from_bal(b), max_num_iterations=40, linear_solver="dense_schur", camera_update="so3_left")
     assert a["final_cost"] < a["initial_cost"] and abs(a["final_cost"] - c["final_cost"]) <= 1e-6 * a["final_cost"]
     assert not np.array_equal(a["trace_cost"][1:3], c["trace_cost"][1:3])
+
+
+def _dense_jacobian(b, camera_update="additive"):
+    p = O.Problem.from_bal(b)
+    r, J, cost, ok = O.evaluate(p, camera_update=camera_update)
+    assert ok
+    nc, no = b.num_cameras(), b.num_observations()
+    n = 9 * nc + 3 * b.num_points()
+    Jd = np.zeros((2 * no, n))
+    rows = np.arange(no)
+    for k in range(9):
+        Jd[2 * rows, 9 * b.camera_index() + k] = J[:, 0, k]
+        Jd[2 * rows + 1, 9 * b.camera_index() + k] = J[:, 1, k]
+    for k in range(3):
+        Jd[2 * rows, 9 * nc + 3 * b.point_index() + k] = J[:, 0, 9 + k]
+        Jd[2 * rows + 1, 9 * nc + 3 * b.point_index() + k] = J[:, 1, 9 + k]
+    return r.reshape(-1), Jd, cost
+
+
+@pytest.mark.parametrize("camera_update", ["additive", "so3_left"])
+def test_g2o_policy_first_step_is_the_damped_gauss_newton_step(camera_update):
+    """g2o's Levenberg step: (J^T J + lambda_0 I) dx = -J^T r with
+    lambda_0 = 1e-5 max diag(J^T J), unscaled, solved densely here."""
+    b = BALProblem.synthetic(0, seed=3, num_points=60)
+    r, Jd, cost0 = _dense_jacobian(b, camera_update)
+    H = Jd.T @ Jd
+    lam = 1e-5 * np.max(np.diag(H))
+    dx = np.linalg.solve(H + lam * np.eye(H.shape[0]), -Jd.T @ r)
+    x1 = b.parameters().copy()
+    nc = b.num_cameras()
+    x1 += dx
+    if camera_update == "so3_left":
+        for c in range(nc):
+            x1[9 * c: 9 * c + 3] = O.compose_left(dx[9 * c: 9 * c + 3], b.parameters()[9 * c: 9 * c + 3])
+    q = O.Problem(nc, b.num_points(), b.camera_index(), b.point_index(), b.observations(), x1)
+    _, _, cost1, _ = O.evaluate(q)
+    s = O.solve(O.Problem.from_bal(b), linear_solver="dense_schur", max_num_iterations=1, lm_policy="g2o",
+                camera_update=camera_update, **FIXED)
+    assert s["trace_radius"][0] == pytest.approx(1.0 / lam, rel=1e-12)
+    assert s["trace_cost"][1] == pytest.approx(cost1, rel=1e-9)
+    assert s["num_successful_steps"] == 1 and s["termination_reason"] == 1
+
+
+def test_g2o_policy_damping_updates_and_limits():
+    b = BALProblem.synthetic(0, seed=6, num_points=500)
+    s = O.solve(O.Problem.from_bal(b), linear_solver="dense_schur", max_num_iterations=40, lm_policy="g2o",
+                loss="huber", **FIXED)
+    ok = s["trace_successful"]
+    rad = s["trace_radius"]
+    assert s["final_cost"] < s["initial_cost"]
+    for k in range(1, len(rad)):
+        f = rad[k] / rad[k - 1]
+        if ok[k]:
+            assert 1.5 * (1 - 1e-15) <= f <= 3.0 * (1 + 1e-15), (k, f)  # lambda *= [1/3, 2/3]
+        else:
+            assert f <= 0.5 * (1 + 1e-15), (k, f)  # lambda *= nu >= 2
+    # accepted steps never raise the cost
+    c = s["trace_cost"]
+    acc = [c[0]] + [c[k] for k in range(1, len(c)) if ok[k]]
+    assert all(acc[i + 1] < acc[i] for i in range(len(acc) - 1))
+    # max_num_iterations bounds outer iterations (accepted steps), not trials
+    t = O.solve(O.Problem.from_bal(b), linear_solver="dense_schur", max_num_iterations=4, lm_policy="g2o",
+                loss="huber", **FIXED)
+    assert t["num_successful_steps"] == 4 and t["termination_reason"] == 1
+    # same minimum as the Ceres policy
+    a = O.solve(O.Problem.from_bal(b), linear_solver="dense_schur", max_num_iterations=60, loss="huber", **FIXED)
+    assert abs(a["final_cost"] - s["final_cost"]) <= 1e-9 * a["final_cost"]
