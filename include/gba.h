@@ -68,7 +68,10 @@ typedef enum gba_termination_reason {
   GBA_REASON_PARAMETER_TOLERANCE = 4,
   GBA_REASON_MIN_TRUST_REGION_RADIUS = 5,
   GBA_REASON_INVALID_STEPS = 6,
-  GBA_REASON_EVALUATION_FAILED = 7
+  GBA_REASON_EVALUATION_FAILED = 7,
+  GBA_REASON_LM_TRIALS = 8 /* GBA_LM_POLICY_G2O: the damping trials of one
+                              iteration ran out, or a trial left the cost
+                              exactly unchanged                              */
 } gba_termination_reason;
 
 typedef enum gba_loss {
@@ -110,6 +113,23 @@ typedef enum gba_camera_update {
   GBA_CAMERA_UPDATE_ADDITIVE = 0,
   GBA_CAMERA_UPDATE_SO3_LEFT = 1
 } gba_camera_update;
+
+/* Levenberg-Marquardt damping policy.  CERES: LevenbergMarquardtStrategy
+ * (trust-region radius, D^2 = clamp(diag J^T J) / radius, Jacobi scaling,
+ * Ceres' termination tests).  G2O: the g2o variant's
+ * OptimizationAlgorithmLevenberg (test_bundle_adjustment_g2o.cpp:174-176, g2o
+ * tag 20230223_git): lambda I damping of the unscaled normal equations
+ * (jacobi_scaling ignored), lambda_0 = 1e-5 max diag(J^T J), gain
+ * (chi2 - chi2') / (dx.(lambda dx + b) + 1e-3), accept when it is > 0,
+ * lambda *= max(1/3, min(2/3, 1 - (2 rho - 1)^3)) then, else lambda *= nu,
+ * nu *= 2; up to 10 trials per iteration; max_num_iterations counts
+ * iterations (accepted steps), num_iterations in the summary counts trials;
+ * the tolerances and the radius bounds are not used.  final_trust_region_radius
+ * reports 1 / lambda. */
+typedef enum gba_lm_policy {
+  GBA_LM_POLICY_CERES = 0,
+  GBA_LM_POLICY_G2O = 1
+} gba_lm_policy;
 
 /* ------------------------------------------------------------------------ */
 /* Options.  Defaults (gba_options_init) are Ceres 2.2's Solver::Options     */
@@ -154,7 +174,8 @@ typedef struct gba_options {
                                          problem) when it fits; 0 = one launch pair per
                                          PCG iteration                               */
   int32_t camera_update;              /* gba_camera_update, GBA_CAMERA_UPDATE_ADDITIVE */
-  int32_t reserved[3];
+  int32_t lm_policy;                  /* gba_lm_policy, GBA_LM_POLICY_CERES          */
+  int32_t reserved[2];
 } gba_options;
 
 /* Per-solve report, the subset of ceres::Solver::Summary the reference

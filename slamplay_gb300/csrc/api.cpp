@@ -79,6 +79,7 @@ void gba_options_init(gba_options *o) {
   o->schur = GBA_SCHUR_AUTO;
   o->persistent_pcg = 1;
   o->camera_update = GBA_CAMERA_UPDATE_ADDITIVE;
+  o->lm_policy = GBA_LM_POLICY_CERES;
 }
 
 const char *gba_version(void) { return "gba 1 sm_103a"; }
@@ -98,7 +99,7 @@ gba_status gba_create(const gba_options *o, gba_handle **out) {
   }
   if (opt.max_num_iterations < 0 || opt.max_linear_solver_iterations < 0 || opt.loss < 0 || opt.loss > 2 ||
       opt.precision < 0 || opt.precision > 1 || opt.schur < 0 || opt.schur > 2 ||
-      opt.camera_update < 0 || opt.camera_update > 1 ||
+      opt.camera_update < 0 || opt.camera_update > 1 || opt.lm_policy < 0 || opt.lm_policy > 1 ||
       !(opt.initial_trust_region_radius > 0) ||
       !(opt.loss_scale > 0) || opt.max_num_consecutive_invalid_steps < 1) {
     g_create_error = "invalid solver options";

@@ -62,7 +62,7 @@ double now_s() {
 Engine::Engine(const gba_options &o) : o_(o) {
   mixed_ = o.precision == GBA_PRECISION_MIXED;
   device_ = o.device;
-  trace_cap_ = std::max(1, o.max_num_iterations + 1);
+  trace_cap_ = std::max(1, max_lm_bodies() + 1);
   profile_.resize(PF_COUNT);
   for (int i = 0; i < PF_COUNT; ++i) profile_[i].name = kProfNames[i];
 }
@@ -277,6 +277,9 @@ size_t Engine::layout(const HostBatch &hb, char *base, DeviceBatch *db, size_t *
   b.opt.min_pcg_iterations = o_.min_linear_solver_iterations;
   b.opt.mixed = mixed_ ? 1 : 0;
   b.opt.so3_left = o_.camera_update == GBA_CAMERA_UPDATE_SO3_LEFT ? 1 : 0;
+  b.opt.g2o = o_.lm_policy == GBA_LM_POLICY_G2O ? 1 : 0;
+  if (b.opt.g2o) b.opt.jacobi_scaling = 0;
+  b.opt.max_bodies = max_lm_bodies();
   b.lm_cond = 0;
   b.pcg_cond = 0;
   b.use_cond = 0;
@@ -662,7 +665,7 @@ gba_status Engine::run_host_driven(std::string *err) {
   if ((st = read_status()) != GBA_OK) return st;
   int bodies = 0;
   while (hstat[1] && hstat[0] == 0) {
-    if (++bodies > o_.max_num_iterations + 2) break;
+    if (++bodies > max_lm_bodies() + 2) break;
     enqueue_lm_head(stream_);
     if (cl_plan_.cs > 0) {
       if ((st = enqueue_pcg_cluster(stream_, err)) != GBA_OK) return st;

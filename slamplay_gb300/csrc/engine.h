@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include <string>
 #include <vector>
 
@@ -91,6 +93,12 @@ class Engine {
   std::vector<ProfileEntry> profile_;
   double last_setup_ms_ = 0.0, last_solve_ms_ = 0.0;
   int trace_cap_ = 0;
+  // LM bodies (trials) one solve may run: max_num_iterations, times g2o's
+  // trials per iteration under that policy
+  int max_lm_bodies() const {
+    const long long k = (long long)o_.max_num_iterations * (o_.lm_policy == GBA_LM_POLICY_G2O ? kG2oMaxTrials : 1);
+    return (int)std::min<long long>(k, 1 << 28);
+  }
   int sm_count_ = 0;
   bool pdl_ = true;        // programmatic dependent launches inside the PCG body
   ClusterPlan cl_plan_;    // cs > 0: the PCG runs as one cluster launch per LM iteration

@@ -49,7 +49,14 @@ struct DeviceOptions {
   int32_t max_iterations, max_invalid_steps, jacobi_scaling, loss;
   int32_t pcg_criterion, max_pcg_iterations, min_pcg_iterations, mixed;
   int32_t so3_left;  // camera rotation update R <- exp(dw) R (else additive)
+  int32_t g2o;       // g2o's Levenberg policy (else Ceres' trust region)
+  int32_t max_bodies;  // LM bodies (trials) a solve may run
 };
+
+// g2o's OptimizationAlgorithmLevenberg constants: lambda_0 = tau max diag(H),
+// at most this many damping trials per iteration.
+constexpr double kG2oTau = 1e-5;
+constexpr int kG2oMaxTrials = 10;
 
 // LM / trust-region state of one problem, resident on the device.
 // Follows Ceres' TrustRegionMinimizer + LevenbergMarquardtStrategy.
@@ -74,6 +81,7 @@ struct LMState {
   int32_t termination_type, termination_reason;
   int32_t successful_steps, unsuccessful_steps, invalid_steps, invalid_run;
   int32_t pcg_active, pcg_iterations, linear_ok, last_linear_ok;
+  int32_t trials, outer;  // g2o policy: trials of this iteration, iterations done
   int64_t total_pcg_iterations;
 };
 

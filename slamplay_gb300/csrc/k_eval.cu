@@ -588,7 +588,7 @@ __device__ void finish_lm_body(const DeviceBatch &B, bool count_body) {
       for (int p = 0; p < B.num_problems; ++p) any |= __ldcg(&B.lm[p].active);
       uint32_t bodies = B.global_counter[kGC_LMBODIES];
       if (count_body) B.global_counter[kGC_LMBODIES] = ++bodies;
-      if (bodies > (uint32_t)B.opt.max_iterations + 2u) {
+      if (bodies > (uint32_t)B.opt.max_bodies + 2u) {
         if (any) B.status[0] = GBA_ERR_INTERNAL;
         any = 0;
       }
@@ -617,8 +617,19 @@ __global__ void __launch_bounds__(256) k_post_eval(DeviceBatch B, int count_body
     double r[6];
     block_range_multi<6>(a, b, e, st, mx, r, red);
     const double cost = r[0], bad = r[1], gp = r[2], gc = r[3], xc = r[4], xp = r[5];
+    // g2o's Levenberg: lambda_0 = tau max diag(J^T J) over the problem's
+    // cameras and points (the column norms of the first evaluation)
+    double hmax[2] = {0.0, 0.0};
+    if (B.opt.g2o && L->iteration == 0) {
+      const double *const ha[2] = {B.cam_colnorm, B.pt_colnorm};
+      const int hb[2] = {9 * k0, 3 * pi.pt_begin}, he[2] = {9 * k1, 3 * (pi.pt_begin + pi.pt_count)};
+      const int hs[2] = {1, 1};
+      const bool hm[2] = {true, true};
+      block_range_multi<2>(ha, hb, he, hs, hm, hmax, red);
+    }
     if (threadIdx.x == 0) {
       const DeviceOptions &o = B.opt;
+      if (o.g2o && L->iteration == 0) L->radius = 1.0 / (kG2oTau * fmax(hmax[0], hmax[1]));
       L->need_jacobian = 0;
       L->x_cost = cost;
       L->gradient_max_norm = fmax(gp, gc);
@@ -638,7 +649,19 @@ __global__ void __launch_bounds__(256) k_post_eval(DeviceBatch B, int count_body
           L->minimum_cost = cost;
           trace_put(B, p, it, cost, L->radius, L->pcg_iterations, 1);
         }
-        if (it >= o.max_iterations) {
+        if (o.g2o) {
+          // the trials of the iteration that ended with this accepted step
+          if (L->trials >= kG2oMaxTrials) {
+            L->active = 0;
+            L->termination_type = GBA_TERMINATION_CONVERGENCE;
+            L->termination_reason = GBA_REASON_LM_TRIALS;
+          } else if (L->outer >= o.max_iterations) {
+            L->active = 0;
+            L->termination_type = GBA_TERMINATION_NO_CONVERGENCE;
+            L->termination_reason = GBA_REASON_MAX_ITERATIONS;
+          }
+          L->trials = 0;
+        } else if (it >= o.max_iterations) {
           L->active = 0;
           L->termination_type = GBA_TERMINATION_NO_CONVERGENCE;
           L->termination_reason = GBA_REASON_MAX_ITERATIONS;

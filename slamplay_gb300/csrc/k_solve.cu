@@ -27,8 +27,9 @@
 namespace gba {
 
 __device__ __forceinline__ double lm_d2(double colnorm2, double radius, const DeviceOptions &o) {
-  // LevenbergMarquardtStrategy: diag = clamp(|J_col|^2), D = sqrt(diag / radius)
-  const double d = fmin(fmax(colnorm2, o.min_diagonal), o.max_diagonal);
+  // LevenbergMarquardtStrategy: diag = clamp(|J_col|^2), D = sqrt(diag / radius);
+  // g2o's Levenberg: D^2 = lambda = 1 / radius on every parameter
+  const double d = o.g2o ? 1.0 : fmin(fmax(colnorm2, o.min_diagonal), o.max_diagonal);
   const double D = sqrt(d / radius);
   return D * D;
 }
@@ -530,6 +531,46 @@ __device__ __forceinline__ void terminate_(LMState *L, int type, int reason) {
   L->termination_reason = reason;
 }
 
+// g2o's Levenberg trial (OptimizationAlgorithmLevenberg, lambda = 1 / radius):
+// gain rho = (chi2 - chi2') / (dx.(lambda dx + b) + 1e-3) with chi2 = 2 cost
+// and dx.(lambda dx + b) = 2 model_cost_change for the solved step; accept
+// when rho > 0 (lambda *= max(1/3, min(2/3, 1 - (2 rho - 1)^3))), else
+// lambda *= nu, nu *= 2.  The iteration's trials end at the first accepted
+// step (K7 then applies the limits at the new point) or after
+// kG2oMaxTrials; a trial with rho == 0 or lambda no longer finite ends the
+// solve.
+__device__ void decide_g2o(const DeviceBatch &B, int p, LMState *L, int it, int pcg, bool valid, double model,
+                           double cand, double bad, double step2) {
+  double rho = -1.0;
+  if (!valid) {
+    ++L->invalid_steps;
+  } else {
+    const double cost = (bad != 0.0 || !isfinite(cand)) ? DBL_MAX : cand;
+    L->candidate_cost = cost;
+    L->step_norm = sqrt(step2);
+    rho = (cost >= DBL_MAX) ? -DBL_MAX : 2.0 * (L->x_cost - cost) / (2.0 * model + 1e-3);
+    L->relative_decrease = rho;
+    if (rho > 0.0) {
+      L->parity ^= 1;
+      L->need_jacobian = 1;
+      L->x_cost = cost;
+      const double tq = 2.0 * rho - 1.0;
+      L->radius = fmin(DBL_MAX, L->radius / fmax(1.0 / 3.0, fmin(2.0 / 3.0, 1.0 - tq * tq * tq)));
+      L->decrease_factor = 2.0;
+      ++L->successful_steps;
+      ++L->trials;
+      ++L->outer;
+      return;
+    }
+  }
+  ++L->unsuccessful_steps;
+  L->radius /= L->decrease_factor;
+  L->decrease_factor *= 2.0;
+  trace_put(B, p, it, valid ? L->candidate_cost : L->x_cost, L->radius, pcg, 0);
+  if (++L->trials >= kG2oMaxTrials || rho == 0.0 || L->radius <= 0.0)
+    terminate_(L, GBA_TERMINATION_CONVERGENCE, GBA_REASON_LM_TRIALS);
+}
+
 __global__ void __launch_bounds__(256) k_decide(DeviceBatch B) {
   __shared__ double red[8 * 6];
   const int p = blockIdx.x;
@@ -564,6 +605,10 @@ __global__ void __launch_bounds__(256) k_decide(DeviceBatch B) {
   L->pcg_active = 0;
   const bool valid = lin_ok && model > 0.0 && isfinite(model);
   L->model_cost_change = model;
+  if (o.g2o) {
+    decide_g2o(B, p, L, it, pcg, valid, model, cand, bad, s2p + s2c);
+    return;
+  }
   if (!valid) {
     ++L->invalid_steps;
     ++L->unsuccessful_steps;

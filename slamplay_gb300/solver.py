@@ -87,9 +87,9 @@ def _summary(s: N.Summary, tr: _Trace | None) -> SolveSummary:
 
 def make_options(**kw) -> N.Options:
     """gba_options with Ceres' defaults, overridden by keyword (loss,
-    precision, pcg_criterion, schur and camera_update accept names:
-    loss='huber', precision='mixed', schur='explicit',
-    camera_update='so3_left')."""
+    precision, pcg_criterion, schur, camera_update and lm_policy accept
+    names: loss='huber', precision='mixed', schur='explicit',
+    camera_update='so3_left', lm_policy='g2o')."""
     o = N.Options()
     N.lib().gba_options_init(N.C.byref(o))
     for k, v in kw.items():
@@ -103,6 +103,8 @@ def make_options(**kw) -> N.Options:
             v = N.SCHUR[v]
         elif k == "camera_update" and isinstance(v, str):
             v = N.CAMERA_UPDATE[v]
+        elif k == "lm_policy" and isinstance(v, str):
+            v = N.LM_POLICY[v]
         elif k == "stream" and v is not None and not isinstance(v, int):
             v = int(v)
         if not hasattr(o, k):
@@ -139,7 +141,9 @@ class Solver:
         self.close()
 
     def _cap(self) -> int:
-        return max(1, self.options.max_num_iterations + 1)
+        # one trace row per LM trial: g2o's policy runs up to 10 per iteration
+        per = 10 if self.options.lm_policy == N.LM_POLICY["g2o"] else 1
+        return max(1, self.options.max_num_iterations * per + 1)
 
     def solve(self, problem: BALProblem) -> SolveSummary:
         """ceres::Solve replacement; problem.parameters() updated in place."""

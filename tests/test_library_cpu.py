@@ -43,6 +43,7 @@ def test_option_defaults_are_ceres_defaults():
     assert o.jacobi_scaling == 1 and o.max_num_consecutive_invalid_steps == 5
     assert o.loss == 0 and o.precision == 0
     assert o.camera_update == 0 and make_options(camera_update="so3_left").camera_update == 1
+    assert o.lm_policy == 0 and make_options(lm_policy="g2o").lm_policy == 1
     with pytest.raises(TypeError):
         make_options(no_such_option=1)
 
@@ -70,6 +71,9 @@ def test_bad_options_rejected_before_device():
     assert ei.value.status == 1
     with pytest.raises(GBAError) as ei:
         Solver(camera_update=2)
+    assert ei.value.status == 1
+    with pytest.raises(GBAError) as ei:
+        Solver(lm_policy=-1)
     assert ei.value.status == 1
 
 
