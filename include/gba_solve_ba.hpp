@@ -33,6 +33,19 @@ struct SolveBAOptions {
     options.loss = GBA_LOSS_HUBER;  // test_bundle_adjustment_ceres.cpp:78
     options.loss_scale = 1.0;
   }
+  // The g2o variant's SolveBA (test_bundle_adjustment_g2o.cpp:166-232):
+  // SO3 left camera update (:84-90), g2o's Levenberg (:174-176), Huber 1.0
+  // per edge (:213), 40 iterations (:218), no tolerance tests.
+  static SolveBAOptions G2OVariant() {
+    SolveBAOptions o;
+    o.options.camera_update = GBA_CAMERA_UPDATE_SO3_LEFT;
+    o.options.lm_policy = GBA_LM_POLICY_G2O;
+    o.options.max_num_iterations = 40;
+    o.options.function_tolerance = 0.0;
+    o.options.gradient_tolerance = 0.0;
+    o.options.parameter_tolerance = 0.0;
+    return o;
+  }
 };
 
 // Solves in place; returns the status (and fills *summary when given).
@@ -55,7 +68,9 @@ gba_status SolveBA(BALProblemT &bal_problem, const SolveBAOptions &opts = SolveB
     return st;
   }
   gba_summary s{};
-  std::vector<double> cost(opts.options.max_num_iterations + 1);
+  // one trace row per trial: up to 10 per iteration under g2o's policy
+  const int per = opts.options.lm_policy == GBA_LM_POLICY_G2O ? 10 : 1;
+  std::vector<double> cost((size_t)opts.options.max_num_iterations * per + 1);
   s.trace_capacity = (int32_t)cost.size();
   s.trace_cost = cost.data();
   st = gba_solve(h, &v, &s);

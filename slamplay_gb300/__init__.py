@@ -7,7 +7,7 @@ reference's BALProblem and SolveBA.
 """
 from ._native import GBAError
 from .bal_problem import BALProblem
-from .solver import Solver, SolveSummary, estimate_footprint, make_options, solve_ba
+from .solver import G2O_VARIANT, Solver, SolveSummary, estimate_footprint, make_options, solve_ba
 
-__all__ = ["BALProblem", "Solver", "SolveSummary", "solve_ba", "make_options", "estimate_footprint",
+__all__ = ["BALProblem", "Solver", "SolveSummary", "solve_ba", "make_options", "estimate_footprint", "G2O_VARIANT",
            "GBAError"]

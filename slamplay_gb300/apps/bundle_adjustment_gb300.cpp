@@ -3,7 +3,8 @@
 // with SolveBA running on the GPU through libgba:
 //   read BAL -> Normalize -> Perturb(0.1, 0.5, 0.5) -> initial.ply ->
 //   SolveBA -> final.ply
-// Usage: bundle_adjustment_gb300 bal_data.txt [--mixed]
+// Usage: bundle_adjustment_gb300 bal_data.txt [--mixed] [--g2o]
+//   --g2o: the g2o variant's SolveBA (test_bundle_adjustment_g2o.cpp:166-232)
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -12,7 +13,7 @@
 
 int main(int argc, char **argv) {
   if (argc < 2) {
-    std::printf("usage: %s bal_data.txt [--mixed]\n", argv[0]);
+    std::printf("usage: %s bal_data.txt [--mixed] [--g2o]\n", argv[0]);
     return 1;
   }
   try {
@@ -20,8 +21,13 @@ int main(int argc, char **argv) {
     bal_problem.Normalize();
     bal_problem.Perturb(0.1, 0.5, 0.5);
     bal_problem.WriteToPLYFile("initial.ply");
-    slamplay_gb300::SolveBAOptions opts;
-    if (argc > 2 && std::strcmp(argv[2], "--mixed") == 0) opts.options.precision = GBA_PRECISION_MIXED;
+    bool mixed = false, g2o = false;
+    for (int i = 2; i < argc; ++i) {
+      mixed |= std::strcmp(argv[i], "--mixed") == 0;
+      g2o |= std::strcmp(argv[i], "--g2o") == 0;
+    }
+    slamplay_gb300::SolveBAOptions opts = g2o ? slamplay_gb300::SolveBAOptions::G2OVariant() : slamplay_gb300::SolveBAOptions();
+    if (mixed) opts.options.precision = GBA_PRECISION_MIXED;
     const gba_status st = slamplay_gb300::SolveBA(bal_problem, opts);
     bal_problem.WriteToPLYFile("final.ply");
     return st == GBA_OK ? 0 : 2;

@@ -252,6 +252,13 @@ class Solver:
         return {k: getattr(st, k) for k, _ in N.ServerStats._fields_}
 
 
+# The g2o variant's SolveBA (test_bundle_adjustment_g2o.cpp:166-232): SO3 left
+# camera update (:84-90), g2o's Levenberg (:174-176), Huber 1.0 per edge
+# (:213), 40 iterations (:218), no tolerance tests.
+G2O_VARIANT = dict(camera_update="so3_left", lm_policy="g2o", loss="huber", loss_scale=1.0, max_num_iterations=40,
+                   function_tolerance=0.0, gradient_tolerance=0.0, parameter_tolerance=0.0)
+
+
 def solve_ba(bal_problem: BALProblem, **options) -> SolveSummary:
     """Drop-in for SolveBA(BALProblem&) (test_bundle_adjustment_ceres.cpp:58-101):
     HuberLoss(1.0) per observation unless `loss` is given; other options are

@@ -8,7 +8,7 @@ import re
 import numpy as np
 import pytest
 
-from slamplay_gb300 import BALProblem, GBAError, Solver, estimate_footprint, make_options
+from slamplay_gb300 import G2O_VARIANT, BALProblem, GBAError, Solver, estimate_footprint, make_options
 from slamplay_gb300 import _native as N
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -44,6 +44,8 @@ def test_option_defaults_are_ceres_defaults():
     assert o.loss == 0 and o.precision == 0
     assert o.camera_update == 0 and make_options(camera_update="so3_left").camera_update == 1
     assert o.lm_policy == 0 and make_options(lm_policy="g2o").lm_policy == 1
+    g = make_options(**G2O_VARIANT)
+    assert (g.camera_update, g.lm_policy, g.loss, g.max_num_iterations) == (1, 1, 1, 40)
     with pytest.raises(TypeError):
         make_options(no_such_option=1)
 
