@@ -335,7 +335,150 @@ static void set_threads(const orc_options *o) {
 }
 
 /* cost only at parameters x; returns 0 if any residual is non-finite */
-static int eval_cost(const orc_problem *p, const double *x, int loss, double a, double *cost) {
+/* ======================================================================== */
+/* Rig model (local-BA window)                                              */
+/* ======================================================================== */
+static void aa_matrix(const double w[3], double R[9]) {
+  for (int j = 0; j < 3; ++j) {
+    const double e[3] = {j == 0, j == 1, j == 2};
+    double c[3];
+    orc_angle_axis_rotate_point(w, e, c);
+    R[j] = c[0], R[3 + j] = c[1], R[6 + j] = c[2];
+  }
+}
+
+static void mat_vec(const double R[9], const double x[3], double y[3]) {
+  for (int i = 0; i < 3; ++i) y[i] = R[3 * i] * x[0] + R[3 * i + 1] * x[1] + R[3 * i + 2] * x[2];
+}
+
+/* pos_cam = E_k (T X): R_e (R X + t) + t_e */
+static void rig_point(const double pose[9], const double pt[3], const orc_rig *rig, int cam, double R[9], double Re[9],
+                      double Q[3]) {
+  double P[3], RP[3];
+  aa_matrix(pose, R);
+  mat_vec(R, pt, P);
+  for (int i = 0; i < 3; ++i) P[i] += pose[3 + i];
+  aa_matrix(rig->ext[cam], Re);
+  mat_vec(Re, P, RP);
+  for (int i = 0; i < 3; ++i) Q[i] = RP[i] + rig->ext[cam][3 + i];
+}
+
+/* EdgeProjection::computeError (g2o_types.h:137-144): pixel = K pos_cam,
+ * divided by its third entry; error = measurement - pixel. */
+static void rig_residual(const double Q[3], const double uv[2], const orc_rig *rig, double r[2]) {
+  const double pu = rig->fx * Q[0] + rig->cx * Q[2], pv = rig->fy * Q[1] + rig->cy * Q[2];
+  r[0] = uv[0] - pu / Q[2];
+  r[1] = uv[1] - pv / Q[2];
+}
+
+/* EdgeProjection::linearizeOplus (g2o_types.h:146-169), restated: with
+ * (X, Y, Z) = pos_cam and zi = 1 / (Z + 1e-18), the pose columns (translation
+ * first in the reference's order) are
+ *   u: -fx zi, 0, fx X zi^2 | fx X Y zi^2, -fx - fx X^2 zi^2, fx Y zi
+ *   v: 0, -fy zi, fy Y zi^2 | fy + fy Y^2 zi^2, -fy X Y zi^2, -fy X zi
+ * (the derivative of a rotation applied in the rig camera's frame, as the
+ * reference writes it), and the point columns are the translation columns
+ * times R_e R.  Stored with the rotation columns in camera slots 0-2. */
+int orc_rig_residual_jacobian(const double pose[9], const double pt[3], const double uv[2], const orc_rig *rig,
+                              int cam, double r[2], double J[24]) {
+  double R[9], Re[9], Q[3];
+  rig_point(pose, pt, rig, cam, R, Re, Q);
+  rig_residual(Q, uv, rig, r);
+  const double fx = rig->fx, fy = rig->fy, X = Q[0], Y = Q[1], Z = Q[2];
+  const double zi = 1.0 / (Z + 1e-18), zi2 = zi * zi;
+  const double tu[3] = {-fx * zi, 0.0, fx * X * zi2}, tv[3] = {0.0, -fy * zi, fy * Y * zi2};
+  const double ru_[3] = {fx * X * Y * zi2, -fx - fx * X * X * zi2, fx * Y * zi};
+  const double rv_[3] = {fy + fy * Y * Y * zi2, -fy * X * Y * zi2, -fy * X * zi};
+  double ReR[9];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) ReR[3 * i + j] = Re[3 * i] * R[j] + Re[3 * i + 1] * R[3 + j] + Re[3 * i + 2] * R[6 + j];
+  for (int k = 0; k < 3; ++k) {
+    J[k] = ru_[k], J[12 + k] = rv_[k];
+    J[3 + k] = tu[k], J[15 + k] = tv[k];
+    J[6 + k] = 0.0, J[18 + k] = 0.0;
+    J[9 + k] = tu[0] * ReR[k] + tu[1] * ReR[3 + k] + tu[2] * ReR[6 + k];
+    J[21 + k] = tv[0] * ReR[k] + tv[1] * ReR[3 + k] + tv[2] * ReR[6 + k];
+  }
+  int ok = isfinite(r[0]) && isfinite(r[1]);
+  for (int k = 0; k < 24; ++k) ok = ok && isfinite(J[k]);
+  return ok;
+}
+
+/* exp(xi) on SE3 (Sophus convention, xi = (translation u, rotation w)):
+ * rotation exp(w), translation V(w) u with V = I + (1 - cos t)/t^2 [w]x +
+ * (t - sin t)/t^3 [w]x^2, t = |w| (series 1/2 - t^2/24, 1/6 - t^2/120 for
+ * t < 1e-4).  Composed on the left: R' = exp(w) R, t' = exp(w) t + V u. */
+void orc_se3_compose_left(const double dw[3], const double du[3], const double pose[6], double out[6]) {
+  const double th2 = dw[0] * dw[0] + dw[1] * dw[1] + dw[2] * dw[2], th = sqrt(th2);
+  double a, b;
+  if (th < 1e-4) {
+    a = 0.5 - th2 / 24.0;
+    b = 1.0 / 6.0 - th2 / 120.0;
+  } else {
+    a = (1.0 - cos(th)) / th2;
+    b = (th - sin(th)) / (th2 * th);
+  }
+  double c1[3], c2[3], rt[3];
+  c1[0] = dw[1] * du[2] - dw[2] * du[1];
+  c1[1] = dw[2] * du[0] - dw[0] * du[2];
+  c1[2] = dw[0] * du[1] - dw[1] * du[0];
+  c2[0] = dw[1] * c1[2] - dw[2] * c1[1];
+  c2[1] = dw[2] * c1[0] - dw[0] * c1[2];
+  c2[2] = dw[0] * c1[1] - dw[1] * c1[0];
+  orc_angle_axis_rotate_point(dw, pose + 3, rt);
+  double w[3];
+  orc_compose_left(dw, pose, w);
+  for (int i = 0; i < 3; ++i) {
+    out[i] = w[i];
+    out[3 + i] = rt[i] + (du[i] + a * c1[i] + b * c2[i]);
+  }
+}
+
+double orc_window_outliers(const double *chi2, int no, double threshold, int max_doublings, unsigned char *outlier,
+                           int *num_inliers, int *num_outliers) {
+  int in = 0, out = 0;
+  for (int it = 0; it < max_doublings; ++it) {
+    in = out = 0;
+    for (int i = 0; i < no; ++i) chi2[i] > threshold ? ++out : ++in;
+    if ((double)in / (double)(in + out) > 0.5) break;
+    threshold *= 2.0;
+  }
+  if (max_doublings <= 0)
+    for (int i = 0; i < no; ++i) chi2[i] > threshold ? ++out : ++in;
+  for (int i = 0; i < no; ++i)
+    if (outlier) outlier[i] = chi2[i] > threshold;
+  if (num_inliers) *num_inliers = in;
+  if (num_outliers) *num_outliers = out;
+  return threshold;
+}
+
+/* one observation under the problem's camera model */
+typedef struct obs_model {
+  int so3_left;
+  const orc_rig *rig;
+} obs_model;
+
+static int observation_rj(const obs_model *m, const double *cam, const double *pt, const double *uv, int i,
+                          double r[2], double J[24]) {
+  if (m->rig) return orc_rig_residual_jacobian(cam, pt, uv, m->rig, m->rig->obs_camera[i], r, J);
+  return residual_jacobian_ex(cam, pt, uv, m->so3_left, r, J);
+}
+
+static void observation_r(const obs_model *m, const double *cam, const double *pt, const double *uv, int i,
+                          double r[2]) {
+  if (m->rig) {
+    double R[9], Re[9], Q[3];
+    rig_point(cam, pt, m->rig, m->rig->obs_camera[i], R, Re, Q);
+    rig_residual(Q, uv, m->rig, r);
+    return;
+  }
+  double pred[2];
+  project_double(cam, pt, pred);
+  r[0] = pred[0] - uv[0];
+  r[1] = pred[1] - uv[1];
+}
+
+static int eval_cost(const orc_problem *p, const obs_model *m, const double *x, int loss, double a, double *cost) {
   const int no = p->no, nb = (no + SUM_BLOCK - 1) / SUM_BLOCK;
   double *part = (double *)calloc((size_t)nb + 1, sizeof(double));
   int ok = 1;
@@ -345,10 +488,9 @@ static int eval_cost(const orc_problem *p, const double *x, int loss, double a, 
     double acc = 0.0;
     const int e = (b + 1) * SUM_BLOCK < no ? (b + 1) * SUM_BLOCK : no;
     for (int i = b * SUM_BLOCK; i < e; ++i) {
-      double pred[2], r[2];
-      project_double(x + 9 * (size_t)p->camera_index[i], pts + 3 * (size_t)p->point_index[i], pred);
-      r[0] = pred[0] - p->observations[2 * i];
-      r[1] = pred[1] - p->observations[2 * i + 1];
+      double r[2];
+      observation_r(m, x + 9 * (size_t)p->camera_index[i], pts + 3 * (size_t)p->point_index[i],
+                    p->observations + 2 * i, i, r);
       if (!(isfinite(r[0]) && isfinite(r[1]))) ok = 0;
       acc += block_cost(loss, a, r);
     }
@@ -362,7 +504,7 @@ static int eval_cost(const orc_problem *p, const double *x, int loss, double a, 
 }
 
 /* residuals r (2*no) and Jacobians J (24*no), corrected for the loss; cost */
-static int eval_jacobian(const orc_problem *p, const double *x, int loss, double a, int so3_left, double *r,
+static int eval_jacobian(const orc_problem *p, const obs_model *m, const double *x, int loss, double a, double *r,
                          double *J, double *cost) {
   const int no = p->no, nb = (no + SUM_BLOCK - 1) / SUM_BLOCK;
   double *part = (double *)calloc((size_t)nb + 1, sizeof(double));
@@ -374,8 +516,8 @@ static int eval_jacobian(const orc_problem *p, const double *x, int loss, double
     const int e = (b + 1) * SUM_BLOCK < no ? (b + 1) * SUM_BLOCK : no;
     for (int i = b * SUM_BLOCK; i < e; ++i) {
       double *ri = r + 2 * (size_t)i, *Ji = J + 24 * (size_t)i;
-      if (!residual_jacobian_ex(x + 9 * (size_t)p->camera_index[i], pts + 3 * (size_t)p->point_index[i],
-                                p->observations + 2 * i, so3_left, ri, Ji))
+      if (!observation_rj(m, x + 9 * (size_t)p->camera_index[i], pts + 3 * (size_t)p->point_index[i],
+                          p->observations + 2 * i, i, ri, Ji))
         ok = 0;
       acc += correct_block(loss, a, ri, Ji, 12, 12);
     }
@@ -388,17 +530,16 @@ static int eval_jacobian(const orc_problem *p, const double *x, int loss, double
   return ok && isfinite(c);
 }
 
-int orc_evaluate_ex(const orc_problem *p, int loss, double loss_scale, int camera_update, double *residuals,
-                    double *jacobians, double *cost) {
+static int evaluate_model(const orc_problem *p, const obs_model *m, int loss, double loss_scale, double *residuals,
+                          double *jacobians, double *cost) {
   const int no = p->no;
   double *r = residuals ? residuals : (double *)malloc(sizeof(double) * 2 * (size_t)no);
   double *J = jacobians ? jacobians : (double *)malloc(sizeof(double) * 24 * (size_t)no);
   int ok = 1;
   const double *pts = p->parameters + 9 * (size_t)p->nc;
   for (int i = 0; i < no; ++i)
-    ok &= residual_jacobian_ex(p->parameters + 9 * (size_t)p->camera_index[i], pts + 3 * (size_t)p->point_index[i],
-                               p->observations + 2 * i, camera_update == ORC_UPDATE_SO3_LEFT, r + 2 * (size_t)i,
-                               J + 24 * (size_t)i);
+    ok &= observation_rj(m, p->parameters + 9 * (size_t)p->camera_index[i], pts + 3 * (size_t)p->point_index[i],
+                         p->observations + 2 * i, i, r + 2 * (size_t)i, J + 24 * (size_t)i);
   double c = 0.0;
   if (cost) {
     /* same blocked order as eval_cost */
@@ -414,6 +555,18 @@ int orc_evaluate_ex(const orc_problem *p, int loss, double loss_scale, int camer
   if (!residuals) free(r);
   if (!jacobians) free(J);
   return ok;
+}
+
+int orc_evaluate_ex(const orc_problem *p, int loss, double loss_scale, int camera_update, double *residuals,
+                    double *jacobians, double *cost) {
+  const obs_model m = {camera_update == ORC_UPDATE_SO3_LEFT, NULL};
+  return evaluate_model(p, &m, loss, loss_scale, residuals, jacobians, cost);
+}
+
+int orc_evaluate_rig(const orc_problem *p, const orc_rig *rig, int loss, double loss_scale, double *residuals,
+                     double *jacobians, double *cost) {
+  const obs_model m = {0, rig};
+  return evaluate_model(p, &m, loss, loss_scale, residuals, jacobians, cost);
 }
 
 int orc_evaluate(const orc_problem *p, int loss, double loss_scale, double *residuals,
@@ -1079,6 +1232,7 @@ static void jacobi_scale(const structure *st, const double *colnorm2, int on, do
 int orc_compute_step(const orc_problem *p, const orc_options *o, double radius, double *delta,
                      double *mcc_out, int *linear_iterations) {
   set_threads(o);
+  const obs_model model = {o->camera_update == ORC_UPDATE_SO3_LEFT, o->rig};
   structure st;
   build_structure(p, &st);
   const int n = st.n;
@@ -1089,7 +1243,7 @@ int orc_compute_step(const orc_problem *p, const orc_options *o, double radius, 
   double *D = (double *)malloc(sizeof(double) * (size_t)n);
   double *y = (double *)malloc(sizeof(double) * (size_t)n);
   double cost;
-  int ok = eval_jacobian(p, p->parameters, o->loss, o->loss_scale, o->camera_update == ORC_UPDATE_SO3_LEFT, r, J, &cost);
+  int ok = eval_jacobian(p, &model, p->parameters, o->loss, o->loss_scale, r, J, &cost);
   int it = 0;
   if (ok) {
     column_norms(p, &st, J, cn);
@@ -1147,6 +1301,7 @@ static void trace_put(orc_summary *s, int it, double cost, double radius, int li
 
 int orc_solve(const orc_problem *p, const orc_options *o, orc_summary *s) {
   set_threads(o);
+  const obs_model model = {o->camera_update == ORC_UPDATE_SO3_LEFT, o->rig};
   const int g2o = o->lm_policy == ORC_LM_G2O;
   int trials = 0, outer = 0;
   structure st;
@@ -1181,7 +1336,7 @@ int orc_solve(const orc_problem *p, const orc_options *o, orc_summary *s) {
   double x_cost = 0.0, x_norm = used_norm(&st, x), gmax = 0.0;
   int term = -1, reason = 0;
 
-  int ok = eval_jacobian(p, x, o->loss, o->loss_scale, o->camera_update == ORC_UPDATE_SO3_LEFT, r, J, &x_cost);
+  int ok = eval_jacobian(p, &model, x, o->loss, o->loss_scale, r, J, &x_cost);
   if (!ok) {
     term = 2;
     reason = 7;
@@ -1256,7 +1411,13 @@ int orc_solve(const orc_problem *p, const orc_options *o, orc_summary *s) {
           const size_t k = 9 * (size_t)c + q;
           xc[k] = st.cam_used[c] ? x[k] + y[k] * scale[k] : x[k];
         }
-        if (o->camera_update == ORC_UPDATE_SO3_LEFT && st.cam_used[c]) {
+        if (o->rig && st.cam_used[c]) {
+          /* rig model: the pose moves on SE3, T <- exp(xi) T */
+          const size_t k = 9 * (size_t)c;
+          const double dw[3] = {y[k] * scale[k], y[k + 1] * scale[k + 1], y[k + 2] * scale[k + 2]};
+          const double du[3] = {y[k + 3] * scale[k + 3], y[k + 4] * scale[k + 4], y[k + 5] * scale[k + 5]};
+          orc_se3_compose_left(dw, du, x + k, xc + k);
+        } else if (o->camera_update == ORC_UPDATE_SO3_LEFT && st.cam_used[c]) {
           const size_t k = 9 * (size_t)c;
           const double dw[3] = {y[k] * scale[k], y[k + 1] * scale[k + 1], y[k + 2] * scale[k + 2]};
           orc_compose_left(dw, x + k, xc + k);
@@ -1268,7 +1429,7 @@ int orc_solve(const orc_problem *p, const orc_options *o, orc_summary *s) {
           xc[k] = st.pt_used[j] ? x[k] + y[k] * scale[k] : x[k];
         }
       double cand_cost;
-      if (!eval_cost(p, xc, o->loss, o->loss_scale, &cand_cost)) cand_cost = DBL_MAX;
+      if (!eval_cost(p, &model, xc, o->loss, o->loss_scale, &cand_cost)) cand_cost = DBL_MAX;
       const double step_norm = used_diff_norm(&st, x, xc);
       if (o->verbose)
         printf("%4d %.6e %.2e %.2e %.2e %.2e %.2e %4d\n", iteration, cand_cost, x_cost - cand_cost,
@@ -1293,7 +1454,7 @@ int orc_solve(const orc_problem *p, const orc_options *o, orc_summary *s) {
       if (g2o ? rho > 0.0 : rel > o->min_relative_decrease) {
         memcpy(x, xc, sizeof(double) * (size_t)n);
         x_norm = used_norm(&st, x);
-        if (!eval_jacobian(p, x, o->loss, o->loss_scale, o->camera_update == ORC_UPDATE_SO3_LEFT, r, J, &x_cost)) {
+        if (!eval_jacobian(p, &model, x, o->loss, o->loss_scale, r, J, &x_cost)) {
           term = 2;
           reason = 7;
           break;
@@ -1358,7 +1519,7 @@ done:
   {
     /* final cost and gradient at the returned parameters */
     double fc = 0.0;
-    if (eval_jacobian(p, p->parameters, o->loss, o->loss_scale, o->camera_update == ORC_UPDATE_SO3_LEFT, r, J, &fc)) {
+    if (eval_jacobian(p, &model, p->parameters, o->loss, o->loss_scale, r, J, &fc)) {
       gradient(&st, J, r, g);
       s->gradient_max_norm = gradient_max_norm(&st, p->parameters, g);
     }

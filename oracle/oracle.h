@@ -49,6 +49,18 @@ enum { ORC_SOLVER_DENSE_SCHUR = 0, ORC_SOLVER_PCG_SCHUR = 1 };
 enum { ORC_PCG_RESIDUAL = 0, ORC_PCG_QUADRATIC_MODEL = 1 };
 /* camera update: Ceres' additive angle-axis, or g2o's R <- exp(dw) R */
 enum { ORC_UPDATE_ADDITIVE = 0, ORC_UPDATE_SO3_LEFT = 1 };
+/* The local-BA window's camera model (full_slam/include/myslam/g2o_types.h
+ * EdgeProjection, full_slam/src/backend.cpp:67-199): a stereo rig of two
+ * pinhole cameras sharing K, each with its extrinsic E_k (body -> camera);
+ * camera blocks hold a keyframe pose T_cw as angle-axis (3), translation (3)
+ * and three unused slots; obs_camera[i] says which rig camera saw
+ * observation i (0 left, 1 right). */
+typedef struct orc_rig {
+  double fx, fy, cx, cy;
+  double ext[2][6]; /* angle-axis (3), translation (3) of E_0, E_1 */
+  const unsigned char *obs_camera;
+} orc_rig;
+
 /* LM damping policy: Ceres' LevenbergMarquardtStrategy, or g2o's
  * OptimizationAlgorithmLevenberg (g2o tag 20230223_git) */
 enum { ORC_LM_CERES = 0, ORC_LM_G2O = 1 };
@@ -70,6 +82,7 @@ typedef struct orc_options {
   int verbose;
   int camera_update; /* ORC_UPDATE_* */
   int lm_policy;     /* ORC_LM_* */
+  const orc_rig *rig; /* NULL: BAL cameras (Snavely model); else the rig model */
 } orc_options;
 
 typedef struct orc_summary {
@@ -97,11 +110,27 @@ int orc_residual_jacobian(const double cam[9], const double pt[3], const double 
 /* w' = log(exp(dw) exp(w)) in angle-axis form (the g2o camera update). */
 void orc_compose_left(const double dw[3], const double w[3], double out[3]);
 
+/* Rig model: residual (measurement - pixel) and the reference's Jacobian of
+ * one observation seen by rig camera `cam`; J as orc_residual_jacobian
+ * (camera slots: rotation 0-2, translation 3-5, 6-8 zero). */
+int orc_rig_residual_jacobian(const double pose[9], const double pt[3], const double uv[2], const orc_rig *rig,
+                              int cam, double r[2], double J[24]);
+/* T <- exp(xi) T on SE3 (VertexPose::oplusImpl, g2o_types.h:55-60):
+ * xi = (rotation dw, translation du); pose = angle-axis (3), translation (3). */
+void orc_se3_compose_left(const double dw[3], const double du[3], const double pose[6], double out[6]);
+/* backend.cpp:156-187: chi2 threshold doubled (at most max_doublings times)
+ * until more than half the observations are inliers; outlier[i] = chi2[i] >
+ * final threshold.  Returns the final threshold. */
+double orc_window_outliers(const double *chi2, int no, double threshold, int max_doublings, unsigned char *outlier,
+                           int *num_inliers, int *num_outliers);
+
 /* Residuals (2*no) and Jacobians (24*no) of every observation in input order
  * (either may be NULL) and the cost 0.5*sum rho(|r|^2).  Returns 0 on a
  * non-finite evaluation. */
 int orc_evaluate_ex(const orc_problem *p, int loss, double loss_scale, int camera_update, double *residuals,
                     double *jacobians, double *cost);
+int orc_evaluate_rig(const orc_problem *p, const orc_rig *rig, int loss, double loss_scale, double *residuals,
+                     double *jacobians, double *cost);
 int orc_evaluate(const orc_problem *p, int loss, double loss_scale, double *residuals,
                  double *jacobians, double *cost);
 

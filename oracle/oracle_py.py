@@ -23,6 +23,11 @@ class OrcProblem(C.Structure):
                 ("point_index", _i32p), ("observations", _f64p), ("parameters", _f64p)]
 
 
+class OrcRig(C.Structure):
+    _fields_ = [("fx", C.c_double), ("fy", C.c_double), ("cx", C.c_double), ("cy", C.c_double),
+                ("ext", (C.c_double * 6) * 2), ("obs_camera", C.POINTER(C.c_ubyte))]
+
+
 class OrcOptions(C.Structure):
     _fields_ = [
         ("max_num_iterations", C.c_int), ("function_tolerance", C.c_double),
@@ -35,7 +40,7 @@ class OrcOptions(C.Structure):
         ("pcg_criterion", C.c_int), ("max_linear_solver_iterations", C.c_int),
         ("min_linear_solver_iterations", C.c_int), ("pcg_tolerance", C.c_double), ("eta", C.c_double),
         ("num_threads", C.c_int), ("verbose", C.c_int), ("camera_update", C.c_int),
-        ("lm_policy", C.c_int),
+        ("lm_policy", C.c_int), ("rig", C.POINTER(OrcRig)),
     ]
 
 
@@ -81,6 +86,14 @@ def oracle():
         L.orc_evaluate_ex.argtypes = [C.POINTER(OrcProblem), C.c_int, C.c_double, C.c_int, _f64p, _f64p, _f64p]
         L.orc_evaluate_ex.restype = C.c_int
         L.orc_compose_left.argtypes = [_f64p, _f64p, _f64p]
+        L.orc_rig_residual_jacobian.argtypes = [_f64p, _f64p, _f64p, C.POINTER(OrcRig), C.c_int, _f64p, _f64p]
+        L.orc_rig_residual_jacobian.restype = C.c_int
+        L.orc_se3_compose_left.argtypes = [_f64p, _f64p, _f64p, _f64p]
+        L.orc_window_outliers.argtypes = [_f64p, C.c_int, C.c_double, C.c_int, C.POINTER(C.c_ubyte), _i32p, _i32p]
+        L.orc_window_outliers.restype = C.c_double
+        L.orc_evaluate_rig.argtypes = [C.POINTER(OrcProblem), C.POINTER(OrcRig), C.c_int, C.c_double, _f64p, _f64p,
+                                       _f64p]
+        L.orc_evaluate_rig.restype = C.c_int
         L.orc_compute_step.argtypes = [C.POINTER(OrcProblem), C.POINTER(OrcOptions), C.c_double, _f64p, _f64p,
                                        C.POINTER(C.c_int)]
         L.orc_compute_step.restype = C.c_int
@@ -169,6 +182,62 @@ def evaluate(p: Problem, loss="trivial", loss_scale=1.0, camera_update="additive
     return r.reshape(no, 2), J.reshape(no, 2, 12), c.value, bool(ok)
 
 
+def make_rig(fx, fy, cx, cy, extrinsics, obs_camera):
+    """An OrcRig over the given per-observation rig-camera array (kept alive
+    on the returned object)."""
+    r = OrcRig()
+    r.fx, r.fy, r.cx, r.cy = fx, fy, cx, cy
+    e = np.asarray(extrinsics, dtype=np.float64).reshape(2, 6)
+    for k in range(2):
+        for q in range(6):
+            r.ext[k][q] = e[k, q]
+    oc = np.ascontiguousarray(obs_camera, dtype=np.uint8)
+    r._keep = oc
+    r.obs_camera = oc.ctypes.data_as(C.POINTER(C.c_ubyte))
+    return r
+
+
+def rig_from_window(w):
+    return make_rig(w.fx, w.fy, w.cx, w.cy, w.extrinsics, w.rig_camera)
+
+
+def window_problem(w):
+    """The window as an oracle Problem: poses in 9-slot camera blocks
+    (angle-axis, translation, three unused zeros), then the landmarks."""
+    nk = w.num_keyframes
+    cams = np.zeros((nk, 9))
+    cams[:, :6] = np.asarray(w.poses).reshape(nk, 6)
+    params = np.concatenate([cams.reshape(-1), np.asarray(w.landmarks, dtype=np.float64).reshape(-1)])
+    return Problem(nk, w.num_landmarks, w.keyframe_index, w.landmark_index, w.observations, params)
+
+
+def evaluate_rig(p: Problem, rig, loss="trivial", loss_scale=1.0):
+    no = p.s.no
+    r = np.zeros(2 * no)
+    J = np.zeros(24 * no)
+    c = C.c_double()
+    ok = oracle().orc_evaluate_rig(C.byref(p.s), C.byref(rig), LOSS[loss] if isinstance(loss, str) else loss,
+                                   loss_scale, f64(r), f64(J), C.byref(c))
+    return r.reshape(no, 2), J.reshape(no, 2, 12), c.value, bool(ok)
+
+
+def se3_compose_left(dw, du, pose):
+    out = np.zeros(6)
+    oracle().orc_se3_compose_left(f64(np.ascontiguousarray(dw, dtype=np.float64)),
+                                  f64(np.ascontiguousarray(du, dtype=np.float64)),
+                                  f64(np.ascontiguousarray(pose, dtype=np.float64)), f64(out))
+    return out
+
+
+def window_outliers(chi2, threshold=5.991, max_doublings=5):
+    chi2 = np.ascontiguousarray(chi2, dtype=np.float64)
+    out = np.zeros(len(chi2), np.uint8)
+    ni, no_ = C.c_int(), C.c_int()
+    th = oracle().orc_window_outliers(f64(chi2), len(chi2), threshold, max_doublings,
+                                      out.ctypes.data_as(C.POINTER(C.c_ubyte)), C.byref(ni), C.byref(no_))
+    return out, ni.value, no_.value, th
+
+
 def compose_left(dw, w):
     """w' = log(exp(dw) exp(w)) in angle-axis form."""
     a = np.ascontiguousarray(dw, dtype=np.float64)
@@ -187,9 +256,11 @@ def compute_step(p: Problem, radius: float, **kw):
     return d, m.value, it.value, bool(ok)
 
 
-def solve(p: Problem, **kw):
+def solve(p: Problem, rig=None, **kw):
     """Runs the oracle LM; returns a dict with the summary and the trace."""
     o = options(**kw)
+    if rig is not None:
+        o.rig = C.pointer(rig)
     cap = max(1, o.max_num_iterations * (G2O_MAX_TRIALS if o.lm_policy == 1 else 1) + 1)
     tc = np.zeros(cap)
     tr = np.zeros(cap)
