@@ -245,6 +245,61 @@ gba_status gba_solve(gba_handle *h, const gba_problem_view *p, gba_summary *s);
 gba_status gba_batch_solve(gba_handle *h, const gba_problem_view *problems, int32_t n,
                            gba_summary *summaries);
 
+/* ---- local bundle adjustment (full_slam's backend) --------------------- */
+/* The problem Backend::Optimize (full_slam/src/backend.cpp:67-199) hands to
+ * g2o: the active keyframes' poses, the active landmarks and one edge per
+ * feature, seen by the left or right camera of a stereo rig (EdgeProjection,
+ * full_slam/include/myslam/g2o_types.h:127-175):
+ *   pos_cam = E_k (T X),  pixel = K pos_cam / z,  error = measurement - pixel,
+ * with the reference's analytic Jacobian (the pose columns of a rotation
+ * about the rig camera's origin) and the left SE3 update T <- exp(xi) T
+ * (VertexPose::oplusImpl, g2o_types.h:55-60).  Poses and extrinsics are
+ * angle-axis (3) then translation (3); a pose maps world to body
+ * (Frame::Pose(), T_cw), an extrinsic body to camera (Camera::pose()).  The
+ * solve uses the handle's options (full_slam: gba_local_ba_options_init);
+ * its tolerances, loss, LM policy and precision apply as in gba_solve, and
+ * camera_update does not (the pose moves on SE3).  After the solve, the
+ * outlier test of backend.cpp:156-187 runs on chi2 = |error|^2 at the
+ * returned estimate: the threshold starts at chi2_threshold and doubles, at
+ * most max_threshold_doublings times, until more than half the edges are
+ * inliers. */
+typedef struct gba_rig {
+  double fx, fy, cx, cy;   /* K shared by both cameras (backend.cpp:99)     */
+  double extrinsic[2][6];  /* E_0 (left), E_1 (right): angle-axis, translation */
+} gba_rig;
+
+typedef struct gba_window_view {
+  int32_t num_keyframes;
+  int32_t num_landmarks;
+  int32_t num_observations;
+  const int32_t *keyframe_index;  /* [num_observations]                       */
+  const int32_t *landmark_index;  /* [num_observations]                       */
+  const uint8_t *rig_camera;      /* [num_observations] 0 left image, 1 right  */
+  const double *observations;     /* [2 * num_observations] pixel u, v        */
+  double *poses;                  /* [6 * num_keyframes] in/out               */
+  double *landmarks;              /* [3 * num_landmarks] in/out               */
+  gba_rig rig;
+  double chi2_threshold;          /* 5.991 (backend.cpp:104)                  */
+  int32_t max_threshold_doublings;/* 5 (backend.cpp:161)                      */
+  uint8_t *outlier;               /* [num_observations] out: 1 = outlier; may be NULL */
+} gba_window_view;
+
+typedef struct gba_window_result {
+  int32_t num_inliers, num_outliers;  /* of the threshold loop's last pass   */
+  double chi2_threshold;              /* the final threshold                 */
+} gba_window_result;
+
+/* Options of full_slam's local BA: g2o's Levenberg, 10 iterations
+ * (backend.cpp:152), Huber with delta 5.991 (backend.cpp:137-139), no
+ * tolerance tests. */
+void gba_local_ba_options_init(gba_options *o);
+/* Window defaults: chi2_threshold 5.991, max_threshold_doublings 5. */
+void gba_window_view_init(gba_window_view *w);
+/* Solves `n` windows as one batch (each with its own LM state); results may
+ * be NULL, summaries may be NULL. */
+gba_status gba_local_ba(gba_handle *h, gba_window_view *windows, int32_t n, gba_summary *summaries,
+                        gba_window_result *results);
+
 /* ---- serving (continuous batching) ------------------------------------- */
 /* Starts the serving loop on the handle: problems submitted with gba_submit
  * are admitted while their estimated device footprint fits in

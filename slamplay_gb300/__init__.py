@@ -7,7 +7,9 @@ reference's BALProblem and SolveBA.
 """
 from ._native import GBAError
 from .bal_problem import BALProblem
-from .solver import G2O_VARIANT, Solver, SolveSummary, estimate_footprint, make_options, solve_ba
+from .solver import G2O_VARIANT, LOCAL_BA, Solver, SolveSummary, estimate_footprint, make_options, solve_ba
+from .window import LocalBAWindow
 
 __all__ = ["BALProblem", "Solver", "SolveSummary", "solve_ba", "make_options", "estimate_footprint", "G2O_VARIANT",
+           "LOCAL_BA", "LocalBAWindow",
            "GBAError"]

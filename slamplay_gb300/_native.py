@@ -75,6 +75,25 @@ class ProblemView(C.Structure):
     ]
 
 
+class Rig(C.Structure):
+    _fields_ = [("fx", C.c_double), ("fy", C.c_double), ("cx", C.c_double), ("cy", C.c_double),
+                ("extrinsic", (C.c_double * 6) * 2)]
+
+
+class WindowView(C.Structure):
+    _fields_ = [
+        ("num_keyframes", C.c_int32), ("num_landmarks", C.c_int32), ("num_observations", C.c_int32),
+        ("keyframe_index", _i32p), ("landmark_index", _i32p), ("rig_camera", C.POINTER(C.c_uint8)),
+        ("observations", _f64p), ("poses", _f64p), ("landmarks", _f64p), ("rig", Rig),
+        ("chi2_threshold", C.c_double), ("max_threshold_doublings", C.c_int32),
+        ("outlier", C.POINTER(C.c_uint8)),
+    ]
+
+
+class WindowResult(C.Structure):
+    _fields_ = [("num_inliers", C.c_int32), ("num_outliers", C.c_int32), ("chi2_threshold", C.c_double)]
+
+
 class SynthSpec(C.Structure):
     _fields_ = [
         ("layout", C.c_int32), ("num_cameras", C.c_int32), ("num_points", C.c_int32),
@@ -131,6 +150,10 @@ _SIGS = {
     "gba_version": (C.c_char_p, []),
     "gba_solve": (C.c_int, [C.c_void_p, C.POINTER(ProblemView), C.POINTER(Summary)]),
     "gba_batch_solve": (C.c_int, [C.c_void_p, C.POINTER(ProblemView), C.c_int32, C.POINTER(Summary)]),
+    "gba_local_ba_options_init": (None, [C.POINTER(Options)]),
+    "gba_window_view_init": (None, [C.POINTER(WindowView)]),
+    "gba_local_ba": (C.c_int, [C.c_void_p, C.POINTER(WindowView), C.c_int32, C.POINTER(Summary),
+                               C.POINTER(WindowResult)]),
     "gba_server_start": (C.c_int, [C.c_void_p, C.c_size_t, C.c_int32, C.c_int32]),
     "gba_submit": (C.c_int, [C.c_void_p, C.POINTER(ProblemView), C.POINTER(C.c_uint64)]),
     "gba_poll": (C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(Summary), C.POINTER(C.c_int32)]),

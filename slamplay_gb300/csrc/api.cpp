@@ -82,6 +82,23 @@ void gba_options_init(gba_options *o) {
   o->lm_policy = GBA_LM_POLICY_CERES;
 }
 
+void gba_local_ba_options_init(gba_options *o) {
+  gba_options_init(o);
+  o->lm_policy = GBA_LM_POLICY_G2O;  // OptimizationAlgorithmLevenberg, backend.cpp:71-74
+  o->max_num_iterations = 10;        // optimizer.optimize(10), backend.cpp:152
+  o->loss = GBA_LOSS_HUBER;          // RobustKernelHuber, delta 5.991, backend.cpp:137-139
+  o->loss_scale = 5.991;
+  o->function_tolerance = 0.0;
+  o->gradient_tolerance = 0.0;
+  o->parameter_tolerance = 0.0;
+}
+
+void gba_window_view_init(gba_window_view *w) {
+  std::memset(w, 0, sizeof *w);
+  w->chi2_threshold = 5.991;
+  w->max_threshold_doublings = 5;
+}
+
 const char *gba_version(void) { return "gba 1 sm_103a"; }
 
 gba_status gba_create(const gba_options *o, gba_handle **out) {
@@ -148,6 +165,17 @@ gba_status gba_batch_solve(gba_handle *h, const gba_problem_view *problems, int3
   std::string err;
   gba_status st = maybe_autotune(h, problems, n, &err);
   if (st == GBA_OK) st = h->engine->solve(problems, n, summaries, &err);
+  if (st != GBA_OK) return fail(h, st, err);
+  return GBA_OK;
+}
+
+gba_status gba_local_ba(gba_handle *h, gba_window_view *windows, int32_t n, gba_summary *summaries,
+                        gba_window_result *results) {
+  if (!h) return GBA_ERR_INVALID_ARGUMENT;
+  if (!windows || n <= 0) return fail(h, GBA_ERR_INVALID_ARGUMENT, "empty batch");
+  if (h->server && h->server->running()) return fail(h, GBA_ERR_INVALID_ARGUMENT, "handle is serving");
+  std::string err;
+  const gba_status st = h->engine->solve_windows(windows, n, summaries, results, &err);
   if (st != GBA_OK) return fail(h, st, err);
   return GBA_OK;
 }

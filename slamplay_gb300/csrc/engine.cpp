@@ -6,6 +6,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 
@@ -188,6 +189,9 @@ size_t Engine::layout(const HostBatch &hb, char *base, DeviceBatch *db, size_t *
   b.sblk_pair = cv.take<int32_t>(ex ? nup + 1 : 0);
   b.spair = cv.take<int2>(ex ? (size_t)hb.npairs : 0);
   b.obs_fpos = cv.take<int32_t>(ex ? no : 0);
+  const bool rig = !hb.obs_rig.empty();
+  b.obs_rig = cv.take<uint8_t>(rig ? no : 0);
+  b.prob_rig = cv.take<double>(rig ? (size_t)kRig * P : 0);
   *upload_bytes = align_up(cv.off, 256);
   // download
   cv.off = *upload_bytes;
@@ -203,6 +207,7 @@ size_t Engine::layout(const HostBatch &hb, char *base, DeviceBatch *db, size_t *
   b.trace_pcg = cv.take<int32_t>(P * trace_cap_);
   b.trace_succ = cv.take<int32_t>(P * trace_cap_);
   b.status = cv.take<int32_t>(8);
+  b.obs_chi2 = cv.take<double>(rig ? no : 0);
   *download_bytes = align_up(cv.off, 256) - *download_off;
   cv.off = *download_off + *download_bytes;
   // work
@@ -280,6 +285,7 @@ size_t Engine::layout(const HostBatch &hb, char *base, DeviceBatch *db, size_t *
   b.opt.g2o = o_.lm_policy == GBA_LM_POLICY_G2O ? 1 : 0;
   if (b.opt.g2o) b.opt.jacobi_scaling = 0;
   b.opt.max_bodies = max_lm_bodies();
+  b.opt.pinhole = rig ? 1 : 0;
   b.lm_cond = 0;
   b.pcg_cond = 0;
   b.use_cond = 0;
@@ -360,6 +366,10 @@ gba_status Engine::upload(const HostBatch &hb, std::string *err) {
     put(const_cast<int32_t *>(hdb.obs_fpos), hb.obs_fpos);
     if (!hb.spair.empty())
       std::memcpy(const_cast<int2 *>(hdb.spair), hb.spair.data(), hb.spair.size() * sizeof(int32_t));
+  }
+  if (!hb.obs_rig.empty()) {
+    put(const_cast<uint8_t *>(hdb.obs_rig), hb.obs_rig);
+    put(const_cast<double *>(hdb.prob_rig), hb.prob_rig);
   }
   put(const_cast<double *>(hdb.cam_init), hb.cam_param);
   put(const_cast<double *>(hdb.pt_init), hb.pt_param);
@@ -627,8 +637,10 @@ void Engine::end_captures() {
 
 void Engine::enqueue_gather(cudaStream_t s) {
   char *out = d_arena_ + download_off_;
-  launch_gather_results(db_, reinterpret_cast<double *>(out),
-                        reinterpret_cast<double *>(out + align_up(sizeof(double) * 9 * (size_t)db_.nc, 256)), s);
+  double *out_cam = reinterpret_cast<double *>(out);
+  double *out_pt = reinterpret_cast<double *>(out + align_up(sizeof(double) * 9 * (size_t)db_.nc, 256));
+  launch_gather_results(db_, out_cam, out_pt, s);
+  if (db_.opt.pinhole) launch_window_chi2(db_, out_cam, out_pt, s);
 }
 
 gba_status Engine::run_host_driven(std::string *err) {
@@ -811,6 +823,115 @@ gba_status Engine::solve(const gba_problem_view *v, int n, gba_summary *s, std::
                     s[p].trace_successful ? s[p].trace_successful[k] : 0);
     }
   }
+  return GBA_OK;
+}
+
+gba_status Engine::solve_windows(gba_window_view *w, int n, gba_summary *s, gba_window_result *res,
+                                 std::string *err) {
+  const double t0 = now_s();
+  if (n <= 0 || !w) {
+    *err = "empty batch";
+    return GBA_ERR_INVALID_ARGUMENT;
+  }
+  // each window as a BAL-layout problem: a pose in a 9-slot camera block
+  // (angle-axis, translation, three unused zeros), then the landmarks
+  std::vector<std::vector<double>> par(n);
+  std::vector<gba_problem_view> v(n);
+  for (int p = 0; p < n; ++p) {
+    const gba_window_view &x = w[p];
+    if (x.num_keyframes < 0 || x.num_landmarks < 0 || x.num_observations < 0 ||
+        (x.num_keyframes > 0 && !x.poses) || (x.num_landmarks > 0 && !x.landmarks) ||
+        (x.num_observations > 0 && !x.rig_camera)) {
+      *err = "window " + std::to_string(p) + ": missing arrays";
+      return GBA_ERR_INVALID_ARGUMENT;
+    }
+    const double *k = &x.rig.fx;
+    bool fin = std::isfinite(x.chi2_threshold) && x.max_threshold_doublings >= 0;
+    for (int q = 0; q < 4 + 12; ++q) fin = fin && std::isfinite(k[q]);
+    if (!fin) {
+      *err = "window " + std::to_string(p) + ": non-finite rig or threshold";
+      return GBA_ERR_INVALID_ARGUMENT;
+    }
+    for (int i = 0; i < x.num_observations; ++i)
+      if (x.rig_camera[i] > 1) {
+        *err = "window " + std::to_string(p) + ": rig_camera must be 0 or 1";
+        return GBA_ERR_INVALID_ARGUMENT;
+      }
+    par[p].assign(9 * (size_t)x.num_keyframes + 3 * (size_t)x.num_landmarks, 0.0);
+    for (int c = 0; c < x.num_keyframes; ++c)
+      for (int q = 0; q < 6; ++q) par[p][9 * (size_t)c + q] = x.poses[6 * (size_t)c + q];
+    if (x.num_landmarks > 0)
+      std::memcpy(par[p].data() + 9 * (size_t)x.num_keyframes, x.landmarks, sizeof(double) * 3 * (size_t)x.num_landmarks);
+    v[p] = gba_problem_view{x.num_keyframes, x.num_landmarks, x.num_observations, x.keyframe_index,
+                            x.landmark_index, x.observations, par[p].data()};
+  }
+  PrepOptions po = prep_options();
+  HostBatch &hb = hb_;
+  gba_status st = prepare_batch(v.data(), n, po, &hb, err);
+  if (st != GBA_OK) return st;
+  hb.obs_rig.resize(hb.no);
+  hb.prob_rig.assign((size_t)kRig * n, 0.0);
+  for (int p = 0; p < n; ++p) {
+    const ProblemInfo &pi = hb.prob[p];
+    for (int k = pi.obs_begin; k < pi.obs_begin + pi.obs_count; ++k) hb.obs_rig[k] = w[p].rig_camera[hb.obs_orig[k]];
+    double *r = hb.prob_rig.data() + (size_t)kRig * p;
+    r[0] = w[p].rig.fx, r[1] = w[p].rig.fy, r[2] = w[p].rig.cx, r[3] = w[p].rig.cy;
+    for (int e = 0; e < 2; ++e) {
+      double *R = r + 4 + 12 * e;
+      const double *aa = w[p].rig.extrinsic[e];
+      for (int j = 0; j < 3; ++j) {
+        const double ej[3] = {j == 0 ? 1.0 : 0.0, j == 1 ? 1.0 : 0.0, j == 2 ? 1.0 : 0.0};
+        double col[3];
+        gba_angle_axis_rotate_point(aa, ej, col);
+        R[j] = col[0], R[3 + j] = col[1], R[6 + j] = col[2];
+      }
+      R[9] = aa[3], R[10] = aa[4], R[11] = aa[5];
+    }
+  }
+  if ((st = upload(hb, err)) != GBA_OK) return st;
+  const double t1 = now_s();
+  if ((st = run_solve(err)) != GBA_OK) return st;
+  if ((st = download(hb, v.data(), s, err)) != GBA_OK) return st;
+  // results: poses and landmarks back, then the outlier test of
+  // backend.cpp:156-187 on each window's chi2 (GPU-evaluated at the returned
+  // estimate, internal order -> the window's own order)
+  DeviceBatch hdb{};
+  size_t ub, doff, dbytes;
+  layout(hb, h_stage_, &hdb, &ub, &doff, &dbytes);
+  std::vector<double> chi2;
+  for (int p = 0; p < n; ++p) {
+    gba_window_view &x = w[p];
+    for (int c = 0; c < x.num_keyframes; ++c)
+      for (int q = 0; q < 6; ++q) x.poses[6 * (size_t)c + q] = par[p][9 * (size_t)c + q];
+    if (x.num_landmarks > 0)
+      std::memcpy(x.landmarks, par[p].data() + 9 * (size_t)x.num_keyframes, sizeof(double) * 3 * (size_t)x.num_landmarks);
+    const ProblemInfo &pi = hb.prob[p];
+    chi2.assign(x.num_observations, 0.0);
+    for (int k = pi.obs_begin; k < pi.obs_begin + pi.obs_count; ++k) chi2[hb.obs_orig[k]] = hdb.obs_chi2[k];
+    double th = x.chi2_threshold;
+    int in = 0, out = 0;
+    for (int it = 0; it < x.max_threshold_doublings; ++it) {
+      in = out = 0;
+      for (double c2 : chi2) c2 > th ? ++out : ++in;
+      if ((double)in / (double)(in + out) > 0.5) break;
+      th *= 2.0;
+    }
+    if (x.max_threshold_doublings <= 0)
+      for (double c2 : chi2) c2 > th ? ++out : ++in;
+    if (x.outlier)
+      for (int i = 0; i < x.num_observations; ++i) x.outlier[i] = chi2[i] > th ? 1 : 0;
+    if (res) {
+      res[p].num_inliers = in;
+      res[p].num_outliers = out;
+      res[p].chi2_threshold = th;
+    }
+  }
+  const double t2 = now_s();
+  if (s)
+    for (int p = 0; p < n; ++p) {
+      s[p].setup_time_s = t1 - t0;
+      s[p].total_time_s = t2 - t0;
+    }
   return GBA_OK;
 }
 

@@ -32,6 +32,9 @@ class Engine {
                       std::string *err);
   gba_status compute_step(const gba_problem_view *v, double radius, double *delta, double *model,
                           int *pcg_iterations, std::string *err);
+  // Local-BA windows (the rig camera model) solved as one batch, then each
+  // window's outlier test.
+  gba_status solve_windows(gba_window_view *w, int n, gba_summary *s, gba_window_result *res, std::string *err);
 
   void set_profiling(bool on) { profiling_ = on; }
   const std::vector<ProfileEntry> &profile() const { return profile_; }

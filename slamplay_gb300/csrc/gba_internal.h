@@ -51,7 +51,12 @@ struct DeviceOptions {
   int32_t so3_left;  // camera rotation update R <- exp(dw) R (else additive)
   int32_t g2o;       // g2o's Levenberg policy (else Ceres' trust region)
   int32_t max_bodies;  // LM bodies (trials) a solve may run
+  int32_t pinhole;     // local-BA windows: the stereo-rig pinhole model, SE3 poses
 };
+
+// Per problem of a local-BA batch: fx, fy, cx, cy, then R (9, row-major) and
+// t (3) of the rig's two extrinsics.
+constexpr int kRig = 28;
 
 // g2o's OptimizationAlgorithmLevenberg constants: lambda_0 = tau max diag(H),
 // at most this many damping trials per iteration.
@@ -96,6 +101,9 @@ struct DeviceBatch {
   const int32_t *obs_cam;    // global camera
   const int32_t *obs_pt;     // global internal point
   const double2 *obs_uv;
+  const uint8_t *obs_rig;    // local-BA windows: rig camera of each observation
+  const double *prob_rig;    // local-BA windows: kRig per problem
+  double *obs_chi2;          // local-BA windows: |error|^2 at the returned estimate
   const uint16_t *obs_seg;   // local camera-segment index inside its chunk
   const uint16_t *obs_slot;  // position in the chunk's camera-sorted order
   const int32_t *pt_obs_begin;  // np + 1

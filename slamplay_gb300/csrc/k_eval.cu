@@ -74,6 +74,41 @@ void launch_camera_table(const DeviceBatch &b, cudaStream_t s) {
 }
 
 // ---------------------------------------------------------------------------
+// Local-BA windows: residual, the reference's Jacobian (rig_jacobian), the
+// loss corrector and the Jacobi scaling of one observation, in FP64 (the
+// windows are small; both precision forms take their copies from here).
+__device__ __forceinline__ double eval_rig(const DeviceBatch &B, int64_t o, int c, int j, const double *X,
+                                           bool unit_scale, double ju[12], double jv[12], double &ru, double &rv,
+                                           bool &ok) {
+  const double *tab = B.cam_table + (size_t)kCamTable * c;
+  const double *rig = B.prob_rig + (size_t)kRig * B.cam_problem[c];
+  rig_jacobian(tab, rig, B.obs_rig[o], X, B.obs_uv[o], ju, jv, ru, rv);
+  const int loss = B.opt.loss;
+  const double cost = block_cost(loss, B.opt.loss_scale, ru, rv);
+  if (loss != GBA_LOSS_TRIVIAL) {
+    const Corrector cr = make_corrector(loss, B.opt.loss_scale, ru, rv);
+#pragma unroll
+    for (int k = 0; k < 12; ++k) {
+      const double rJ = ru * ju[k] + rv * jv[k];
+      ju[k] = cr.sqrt_rho1 * (ju[k] - cr.alpha_sq_norm * ru * rJ);
+      jv[k] = cr.sqrt_rho1 * (jv[k] - cr.alpha_sq_norm * rv * rJ);
+    }
+    ru *= cr.residual_scaling;
+    rv *= cr.residual_scaling;
+  }
+  ok = isfinite(ru) && isfinite(rv) && isfinite(cost);
+  if (!unit_scale) {
+    const double *sc = B.cam_scale + 9 * (size_t)c, *sp = B.pt_scale + 3 * (size_t)j;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) ju[k] *= sc[k], jv[k] *= sc[k];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) ju[9 + k] *= sp[k], jv[9 + k] *= sp[k];
+  }
+#pragma unroll
+  for (int k = 0; k < 12; ++k) ok = ok && isfinite((float)ju[k]) && isfinite((float)jv[k]);
+  return cost;
+}
+
 // Residual + Jacobian of one observation.  Jc[k] = (d r_u, d r_v)/d cam_k,
 // Jp[k] = (d r_u, d r_v)/d X_k, r = corrected residual; scaled by the Jacobi
 // scaling.  Returns 0.5*rho(|r|^2) (FP64).  *bad = 1 on a non-finite value.
@@ -84,6 +119,18 @@ __device__ __forceinline__ double eval_observation(const DeviceBatch &B, int64_t
                                                    typename Prec<MIXED>::real2 *Jp,
                                                    typename Prec<MIXED>::real2 &r, bool &bad) {
   typedef typename Prec<MIXED>::real real;
+  if (B.opt.pinhole) {
+    double jd[12], kd[12], rud, rvd;
+    bool ok;
+    const double cost = eval_rig(B, o, c, j, X, unit_scale, jd, kd, rud, rvd, ok);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) Jc[k] = mk2((real)jd[k], (real)kd[k]);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) Jp[k] = mk2((real)jd[9 + k], (real)kd[9 + k]);
+    r = mk2((real)rud, (real)rvd);
+    bad = !ok;
+    return cost;
+  }
   const double *tab = B.cam_table + (size_t)kCamTable * c;
   // the Jacobian reads the table and the scales in its own precision (an
   // FP32 copy in the mixed form: no FP64 conversions per observation)
@@ -186,6 +233,23 @@ __device__ __forceinline__ DF operator-(DF a) { return df_neg(a); }
 __device__ __forceinline__ double eval_observation_df(const DeviceBatch &B, int64_t o, int c, int j,
                                                       const double *X, float2 *Jc, float2 *Jp, float2 &r,
                                                       DF *gr, bool &bad) {
+  if (B.opt.pinhole) {
+    double jd[12], kd[12], rud, rvd;
+    bool ok;
+    const double cost = eval_rig(B, o, c, j, X, false, jd, kd, rud, rvd, ok);
+#pragma unroll
+    for (int k = 0; k < 12; ++k) {
+      gr[k] = df_from_double(jd[k] * rud + kd[k] * rvd);
+      const float2 jk = make_float2((float)jd[k], (float)kd[k]);
+      if (k < 9)
+        Jc[k] = jk;
+      else
+        Jp[k - 9] = jk;
+    }
+    r = make_float2((float)rud, (float)rvd);
+    bad = !ok;
+    return cost;
+  }
   const double *tab = B.cam_table + (size_t)kCamTable * c;
   const float2 *td = B.cam_tabledf + (size_t)kCamTable * c;
   auto T = [&](int k) {
@@ -701,7 +765,13 @@ __global__ void k_candidate_cameras(DeviceBatch B) {
     const double step = -B.pcg_x[9 * (size_t)c + q];
     cand[q] = used ? x[q] + step * B.cam_scale[9 * (size_t)c + q] : x[q];
   }
-  if (B.opt.so3_left && used) {
+  if (B.opt.pinhole && used) {
+    // local-BA windows: the pose moves on SE3, T <- exp(xi) T
+    const double *y = B.pcg_x + 9 * (size_t)c, *sc = B.cam_scale + 9 * (size_t)c;
+    const double dw[3] = {-y[0] * sc[0], -y[1] * sc[1], -y[2] * sc[2]};
+    const double du[3] = {-y[3] * sc[3], -y[4] * sc[4], -y[5] * sc[5]};
+    se3_compose_left(dw, du, x, cand);
+  } else if (B.opt.so3_left && used) {
     const double dw[3] = {-B.pcg_x[9 * (size_t)c + 0] * B.cam_scale[9 * (size_t)c + 0],
                           -B.pcg_x[9 * (size_t)c + 1] * B.cam_scale[9 * (size_t)c + 1],
                           -B.pcg_x[9 * (size_t)c + 2] * B.cam_scale[9 * (size_t)c + 2]};
@@ -736,10 +806,18 @@ __global__ void __launch_bounds__(kChunkCap) k_cost_chunk(DeviceBatch B) {
       const int c = B.obs_cam[o], j = B.obs_pt[o];
       const double *Xp = B.pt_param[parity] + 4 * (size_t)j;
       const double X[3] = {Xp[0], Xp[1], Xp[2]};
-      Proj pr;
-      project(B.cam_table + (size_t)kCamTable * c, X, B.obs_uv[o], pr);
-      cost = block_cost(B.opt.loss, B.opt.loss_scale, pr.ru, pr.rv);
-      bad = !(isfinite(pr.ru) && isfinite(pr.rv) && isfinite(cost));
+      double ru, rv;
+      if (B.opt.pinhole) {
+        double Q[3];
+        rig_project(B.cam_table + (size_t)kCamTable * c, B.prob_rig + (size_t)kRig * ci.problem, B.obs_rig[o], X,
+                    B.obs_uv[o], Q, ru, rv);
+      } else {
+        Proj pr;
+        project(B.cam_table + (size_t)kCamTable * c, X, B.obs_uv[o], pr);
+        ru = pr.ru, rv = pr.rv;
+      }
+      cost = block_cost(B.opt.loss, B.opt.loss_scale, ru, rv);
+      bad = !(isfinite(ru) && isfinite(rv) && isfinite(cost));
     }
     const double cs = block_sum(cost, red);
     const double bd = block_max(bad ? 1.0 : 0.0, red);
@@ -812,6 +890,32 @@ __global__ void k_gather_results(DeviceBatch B, double *out_cam, double *out_pt)
 void launch_gather_results(const DeviceBatch &b, double *out_cam, double *out_pt, cudaStream_t s) {
   const int64_t n = 9 * (int64_t)b.nc + 4 * (int64_t)b.np;
   if (n > 0) k_gather_results<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(b, out_cam, out_pt);
+}
+
+// Local-BA windows after the solve: camera tables at the returned estimate,
+// then each observation's chi2 = |error|^2 (EdgeProjection's chi2 with the
+// identity information matrix, backend.cpp:135 and :159).
+__global__ void k_window_tables(DeviceBatch B, const double *out_cam) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= B.nc) return;
+  camera_table_entry(out_cam + 9 * (size_t)c, B.cam_table + (size_t)kCamTable * c, false);
+}
+
+__global__ void k_window_chi2(DeviceBatch B, const double *out_pt) {
+  const int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= B.no) return;
+  const int c = B.obs_cam[o], j = B.obs_pt[o];
+  const double *Xp = out_pt + 4 * (size_t)j;
+  const double X[3] = {Xp[0], Xp[1], Xp[2]};
+  double Q[3], ru, rv;
+  rig_project(B.cam_table + (size_t)kCamTable * c, B.prob_rig + (size_t)kRig * B.cam_problem[c], B.obs_rig[o], X,
+              B.obs_uv[o], Q, ru, rv);
+  B.obs_chi2[o] = ru * ru + rv * rv;
+}
+
+void launch_window_chi2(const DeviceBatch &b, const double *out_cam, const double *out_pt, cudaStream_t s) {
+  if (b.nc > 0) k_window_tables<<<(b.nc + 127) / 128, 128, 0, s>>>(b, out_cam);
+  if (b.no > 0) k_window_chi2<<<(unsigned)((b.no + 255) / 256), 256, 0, s>>>(b, out_pt);
 }
 
 void launch_sync_param_buffers(const DeviceBatch &b, cudaStream_t s) {

@@ -461,6 +461,104 @@ __device__ __forceinline__ void project(const double *tab, const double *X, doub
   o.rv = o.f * o.dist * o.yp - uv.y;
 }
 
+// ---------------------------------------------------------------------------
+// Local-BA windows: full_slam's stereo rig (EdgeProjection,
+// full_slam/include/myslam/g2o_types.h:127-175).  The camera table holds the
+// keyframe pose (R at tab[0..8], t at tab[36..38]); rig = fx, fy, cx, cy,
+// then R_e (9) and t_e (3) of the two rig cameras.
+//   Q = R_e (R X + t) + t_e,  pixel = (K Q) / Q_z,  error = measurement - pixel
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void rig_project(const double *tab, const double *rig, int cam, const double *X,
+                                            double2 uv, double Q[3], double &ru, double &rv) {
+  double P[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) P[i] = tab[3 * i + 0] * X[0] + tab[3 * i + 1] * X[1] + tab[3 * i + 2] * X[2] + tab[36 + i];
+  const double *Re = rig + 4 + 12 * cam;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) Q[i] = Re[3 * i + 0] * P[0] + Re[3 * i + 1] * P[1] + Re[3 * i + 2] * P[2] + Re[9 + i];
+  ru = uv.x - (rig[0] * Q[0] + rig[2] * Q[2]) / Q[2];
+  rv = uv.y - (rig[1] * Q[1] + rig[3] * Q[2]) / Q[2];
+}
+
+// Residual and the reference's Jacobian (EdgeProjection::linearizeOplus,
+// g2o_types.h:146-169) of one observation: with (X, Y, Z) = Q and
+// zi = 1 / (Z + 1e-18), the pose columns
+//   u: rotation fx X Y zi^2, -fx - fx X^2 zi^2, fx Y zi | translation -fx zi, 0, fx X zi^2
+//   v: rotation fy + fy Y^2 zi^2, -fy X Y zi^2, -fy X zi | translation 0, -fy zi, fy Y zi^2
+// (camera slots 0-2 rotation, 3-5 translation, 6-8 zero) and the point
+// columns = the translation columns times R_e R.
+__device__ __forceinline__ void rig_jacobian(const double *tab, const double *rig, int cam, const double *X,
+                                             double2 uv, double ju[12], double jv[12], double &ru, double &rv) {
+  double Q[3];
+  rig_project(tab, rig, cam, X, uv, Q, ru, rv);
+  const double fx = rig[0], fy = rig[1];
+  const double zi = 1.0 / (Q[2] + 1e-18), zi2 = zi * zi;
+  const double tu0 = -fx * zi, tu2 = fx * Q[0] * zi2, tv1 = -fy * zi, tv2 = fy * Q[1] * zi2;
+  ju[0] = fx * Q[0] * Q[1] * zi2, ju[1] = -fx - fx * Q[0] * Q[0] * zi2, ju[2] = fx * Q[1] * zi;
+  jv[0] = fy + fy * Q[1] * Q[1] * zi2, jv[1] = -fy * Q[0] * Q[1] * zi2, jv[2] = -fy * Q[0] * zi;
+  ju[3] = tu0, ju[4] = 0.0, ju[5] = tu2;
+  jv[3] = 0.0, jv[4] = tv1, jv[5] = tv2;
+  ju[6] = ju[7] = ju[8] = 0.0;
+  jv[6] = jv[7] = jv[8] = 0.0;
+  const double *Re = rig + 4 + 12 * cam;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    // column k of R_e R
+    const double a0 = Re[0] * tab[k] + Re[1] * tab[3 + k] + Re[2] * tab[6 + k];
+    const double a1 = Re[3] * tab[k] + Re[4] * tab[3 + k] + Re[5] * tab[6 + k];
+    const double a2 = Re[6] * tab[k] + Re[7] * tab[3 + k] + Re[8] * tab[6 + k];
+    ju[9 + k] = tu0 * a0 + tu2 * a2;
+    jv[9 + k] = tv1 * a1 + tv2 * a2;
+  }
+}
+
+// Rodrigues rotation of p by angle-axis w (utils/geometry/rotation.h:133-199
+// form: the full formula for theta^2 > DBL_EPSILON, p + w x p below).
+__device__ __forceinline__ void aa_rotate(const double *w, const double *p, double *out) {
+  const double th2 = w[0] * w[0] + w[1] * w[1] + w[2] * w[2];
+  const double wxp[3] = {w[1] * p[2] - w[2] * p[1], w[2] * p[0] - w[0] * p[2], w[0] * p[1] - w[1] * p[0]};
+  if (th2 > DBL_EPSILON) {
+    const double th = sqrt(th2), it = 1.0 / th;
+    double s, c;
+    sincos(th, &s, &c);
+    const double k[3] = {w[0] * it, w[1] * it, w[2] * it};
+    const double kd = k[0] * p[0] + k[1] * p[1] + k[2] * p[2];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) out[i] = p[i] * c + wxp[i] * it * s + k[i] * kd * (1.0 - c);
+  } else {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) out[i] = p[i] + wxp[i];
+  }
+}
+
+// T <- exp(xi) T on SE3 (VertexPose::oplusImpl, g2o_types.h:55-60), xi =
+// (rotation dw, translation du): R' = exp(dw) R, t' = exp(dw) t + V(dw) du,
+// V = I + (1 - cos th)/th^2 [dw]x + (th - sin th)/th^3 [dw]x^2 (series below
+// th = 1e-4).  pose = angle-axis (3), translation (3).
+__device__ inline void se3_compose_left(const double *dw, const double *du, const double *pose, double *out) {
+  const double th2 = dw[0] * dw[0] + dw[1] * dw[1] + dw[2] * dw[2], th = sqrt(th2);
+  double a, b;
+  if (th < 1e-4) {
+    a = 0.5 - th2 / 24.0;
+    b = 1.0 / 6.0 - th2 / 120.0;
+  } else {
+    double s, c;
+    sincos(th, &s, &c);
+    a = (1.0 - c) / th2;
+    b = (th - s) / (th2 * th);
+  }
+  const double c1[3] = {dw[1] * du[2] - dw[2] * du[1], dw[2] * du[0] - dw[0] * du[2], dw[0] * du[1] - dw[1] * du[0]};
+  const double c2[3] = {dw[1] * c1[2] - dw[2] * c1[1], dw[2] * c1[0] - dw[0] * c1[2], dw[0] * c1[1] - dw[1] * c1[0]};
+  double rt[3], w[3];
+  aa_rotate(dw, pose + 3, rt);
+  compose_left(dw, pose, w);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    out[i] = w[i];
+    out[3 + i] = rt[i] + (du[i] + a * c1[i] + b * c2[i]);
+  }
+}
+
 // Ceres robust-loss rho(s) (LossFunction::Evaluate) for trivial, Huber(a),
 // Cauchy(a).
 __device__ __forceinline__ void loss_rho(int loss, double a, double s, double rho[3]) {

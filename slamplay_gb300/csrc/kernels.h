@@ -69,5 +69,8 @@ void launch_sync_param_buffers(const DeviceBatch &b, cudaStream_t s);
 // Gathers each problem's current parameters (the buffer its parity selects)
 // into out_cam (9 per camera) / out_pt (4 per point).
 void launch_gather_results(const DeviceBatch &b, double *out_cam, double *out_pt, cudaStream_t s);
+// Local-BA windows: camera tables at the gathered estimate, then each
+// observation's chi2 = |error|^2 (B.obs_chi2).
+void launch_window_chi2(const DeviceBatch &b, const double *out_cam, const double *out_pt, cudaStream_t s);
 
 }  // namespace gba

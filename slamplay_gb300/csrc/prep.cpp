@@ -205,6 +205,8 @@ void HostBatch::reset() {
   for (auto *v : {&obs_uv, &cam_param, &pt_param}) v->clear();
   pt_used.clear();
   cam_used.clear();
+  obs_rig.clear();
+  prob_rig.clear();
   prob.clear();
   chunk.clear();
   camblk.clear();

@@ -46,6 +46,10 @@ struct HostBatch {
   // initial parameters in the internal layout
   std::vector<double> cam_param;  // 9 per camera
   std::vector<double> pt_param;   // 4 per point
+  // local-BA windows (empty otherwise): the rig camera of each internal
+  // observation, and per problem fx, fy, cx, cy, then (R, t) of E_0 and E_1
+  std::vector<uint8_t> obs_rig;
+  std::vector<double> prob_rig;   // kRig per problem
   // Empties the batch but keeps the vectors' storage (a handle re-preparing
   // problems of similar size touches no fresh pages).
   void reset();

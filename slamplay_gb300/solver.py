@@ -164,6 +164,42 @@ class Solver:
         N.check(N.lib().gba_batch_solve(self._h, views, n, sums), self._h, "gba_batch_solve")
         return [_summary(s, t) for s, t in zip(sums, trs)]
 
+    def local_ba(self, windows, chi2_threshold: float = 5.991, max_threshold_doublings: int = 5):
+        """Solves local-BA windows (slamplay_gb300.window.LocalBAWindow; one
+        or a list, solved as one batch) in place and runs full_slam's outlier
+        test on each (full_slam/src/backend.cpp:67-199).  Returns, per window,
+        (summary, {"num_inliers", "num_outliers", "chi2_threshold",
+        "outlier": uint8 per observation})."""
+        single = not isinstance(windows, (list, tuple))
+        ws = [windows] if single else list(windows)
+        n = len(ws)
+        views = (N.WindowView * n)()
+        flags = []
+        for v, w in zip(views, ws):
+            N.lib().gba_window_view_init(N.C.byref(v))
+            v.num_keyframes, v.num_landmarks, v.num_observations = w.num_keyframes, w.num_landmarks, w.num_observations
+            v.keyframe_index, v.landmark_index = N.i32p(w.keyframe_index), N.i32p(w.landmark_index)
+            v.rig_camera = w.rig_camera.ctypes.data_as(N.C.POINTER(N.C.c_uint8))
+            v.observations, v.poses, v.landmarks = N.f64p(w.observations), N.f64p(w.poses), N.f64p(w.landmarks)
+            v.rig.fx, v.rig.fy, v.rig.cx, v.rig.cy = w.fx, w.fy, w.cx, w.cy
+            for k in range(2):
+                for q in range(6):
+                    v.rig.extrinsic[k][q] = float(w.extrinsics[k, q])
+            v.chi2_threshold, v.max_threshold_doublings = chi2_threshold, max_threshold_doublings
+            f = np.zeros(w.num_observations, np.uint8)
+            flags.append(f)
+            v.outlier = f.ctypes.data_as(N.C.POINTER(N.C.c_uint8))
+        sums = (N.Summary * n)()
+        trs = [_Trace(self._cap()) for _ in range(n)]
+        for s, t in zip(sums, trs):
+            t.attach(s)
+        res = (N.WindowResult * n)()
+        N.check(N.lib().gba_local_ba(self._h, views, n, sums, res), self._h, "gba_local_ba")
+        out = [(_summary(s, t), {"num_inliers": r.num_inliers, "num_outliers": r.num_outliers,
+                                 "chi2_threshold": r.chi2_threshold, "outlier": f})
+               for s, t, r, f in zip(sums, trs, res, flags)]
+        return out[0] if single else out
+
     def autotune(self, problems: BALProblem | Sequence[BALProblem]) -> dict:
         """Picks the fastest launch shapes (tile size, PCG iterations per
         graph body) for these problems by timed trial solves; later solves on
@@ -257,6 +293,13 @@ class Solver:
 # (:213), 40 iterations (:218), no tolerance tests.
 G2O_VARIANT = dict(camera_update="so3_left", lm_policy="g2o", loss="huber", loss_scale=1.0, max_num_iterations=40,
                    function_tolerance=0.0, gradient_tolerance=0.0, parameter_tolerance=0.0)
+
+
+# full_slam's local BA (Backend::Optimize, full_slam/src/backend.cpp:67-199):
+# g2o's Levenberg, 10 iterations, Huber with delta 5.991, no tolerance tests
+# (the same set gba_local_ba_options_init fills in).
+LOCAL_BA = dict(lm_policy="g2o", max_num_iterations=10, loss="huber", loss_scale=5.991, function_tolerance=0.0,
+                gradient_tolerance=0.0, parameter_tolerance=0.0)
 
 
 def solve_ba(bal_problem: BALProblem, **options) -> SolveSummary:

@@ -8,7 +8,7 @@ import re
 import numpy as np
 import pytest
 
-from slamplay_gb300 import G2O_VARIANT, BALProblem, GBAError, Solver, estimate_footprint, make_options
+from slamplay_gb300 import G2O_VARIANT, LOCAL_BA, BALProblem, GBAError, Solver, estimate_footprint, make_options
 from slamplay_gb300 import _native as N
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -48,6 +48,19 @@ def test_option_defaults_are_ceres_defaults():
     assert (g.camera_update, g.lm_policy, g.loss, g.max_num_iterations) == (1, 1, 1, 40)
     with pytest.raises(TypeError):
         make_options(no_such_option=1)
+
+
+def test_local_ba_defaults():
+    o = N.Options()
+    N.lib().gba_local_ba_options_init(N.C.byref(o))
+    ref = make_options(**LOCAL_BA)
+    for k in ("lm_policy", "max_num_iterations", "loss", "loss_scale", "function_tolerance", "gradient_tolerance",
+              "parameter_tolerance"):
+        assert getattr(o, k) == getattr(ref, k), k
+    assert (o.lm_policy, o.max_num_iterations, o.loss, o.loss_scale) == (1, 10, 1, 5.991)
+    v = N.WindowView()
+    N.lib().gba_window_view_init(N.C.byref(v))
+    assert v.chi2_threshold == 5.991 and v.max_threshold_doublings == 5 and v.num_observations == 0
 
 
 def _gpu_present():
