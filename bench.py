@@ -336,6 +336,7 @@ def run_gpu(args) -> None:
             extra_forms["large"] = large_form()
             extra_forms["batched"] = batched_form()
             extra_forms["serving"] = serving_form()
+            extra_forms["local_ba"] = local_ba_form()
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_m, "higher_is_better": True, "scaling": "weak",
@@ -432,6 +433,57 @@ def batched_form(n_problems: int = 1024, repeats: int = 2, seq_sample: int = 32)
     out["mixed_vs_fp64_final_cost_rel"] = {"max": rel[-1], "median": rel[len(rel) // 2],
                                           "p99": rel[int(0.99 * (len(rel) - 1))],
                                           "within_1e-6": sum(1 for r in rel if r <= 1e-6), "problems": len(rel)}
+    return out
+
+
+def local_ba_form(n_windows: int = 256, repeats: int = 2, oracle_sample: int = 16) -> dict:
+    """full_slam's local BA (Backend::Optimize, full_slam/src/backend.cpp:67-199)
+    on a batch of synthetic stereo windows (7 keyframes, ~580 landmarks,
+    ~5.7k edges each, 5 % gross outliers): g2o's Levenberg, 10 iterations,
+    Huber 5.991, then the outlier-threshold test, all windows as one batch
+    through gba_local_ba.  e2e = the whole call (host prep, copies, solve,
+    chi2, outlier test); resident = device re-runs of the uploaded batch.
+    The oracle solves the first `oracle_sample` windows (dense Schur) for the
+    CPU rate and the parity of the final costs."""
+    from oracle import oracle_py as O
+    from slamplay_gb300 import LOCAL_BA, LocalBAWindow, Solver
+
+    ws = [LocalBAWindow.synthetic(seed=1000 + i) for i in range(n_windows)]
+    nobs = sum(w.num_observations for w in ws)
+    out = {"workload": f"{n_windows} windows, 7 keyframes each, {nobs} edges", "options": "g2o LM, 10 iterations, "
+           "Huber 5.991, exact-ish PCG (residual 1e-10, <= 500)"}
+    for prec in ("mixed", "fp64"):
+        with Solver(precision=prec, **LOCAL_BA) as s:
+            gs = [w.copy() for w in ws]
+            s.local_ba(gs)  # warm-up: graph capture, workspace
+            gs = [w.copy() for w in ws]
+            t0 = time.perf_counter()
+            res = s.local_ba(gs)
+            e2e = time.perf_counter() - t0
+            ts = []
+            for _ in range(repeats):
+                t1 = time.perf_counter()
+                s.solve_resident(1)
+                s.synchronize()
+                ts.append(time.perf_counter() - t1)
+        t = min(ts)
+        its = sum(sm.num_iterations for sm, _ in res)
+        out[prec] = {"windows_per_s": n_windows / t, "lm_trials_per_s": its / t, "s_per_batch": t,
+                     "e2e_windows_per_s": n_windows / e2e, "e2e_s": e2e,
+                     "outliers": sum(r["num_outliers"] for _, r in res),
+                     "final_costs_head": [sm.final_cost for sm, _ in res[:oracle_sample]]}
+    t0 = time.perf_counter()
+    orc = []
+    for w in ws[:oracle_sample]:
+        so = O.solve(O.window_problem(w), rig=O.rig_from_window(w), linear_solver="dense_schur", **LOCAL_BA)
+        orc.append(so["final_cost"])
+    dt = time.perf_counter() - t0
+    import os as _os
+    out["cpu_oracle"] = {"windows_per_s": oracle_sample / dt, "sample": f"first {oracle_sample} windows",
+                         "cores": _os.cpu_count(), "kind": "port"}
+    for prec in ("mixed", "fp64"):
+        rel = [abs(a - b) / b for a, b in zip(out[prec]["final_costs_head"], orc)]
+        out[prec]["final_cost_rel_vs_oracle_max"] = max(rel)
     return out
 
 
