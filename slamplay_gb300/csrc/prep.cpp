@@ -7,15 +7,17 @@
 // chunks of whole points; per chunk the camera-sorted order of its
 // observations and its camera segments; per camera its segments and its
 // observations.  All orderings are deterministic functions of the input.
+// The data-parallel loops run on host threads; no result depends on how
+// their work is split.
 #include "prep.h"
 
-#include <functional>
-#include <thread>
-
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <functional>
+#include <thread>
 
 namespace gba {
 
@@ -24,6 +26,50 @@ static std::string fmt(const char *f, long long a, long long b = 0, long long c 
   std::snprintf(buf, sizeof buf, f, a, b, c);
   return buf;
 }
+
+// ---------------------------------------------------------------------------
+// Host threads for the prep's data-parallel loops: up to the hardware
+// threads (at most 32), started per loop and joined before it returns, the
+// calling thread working too; tasks are taken from a shared counter, and no
+// result depends on which thread runs a task.
+int host_threads() { return (int)std::min(std::max(1u, std::thread::hardware_concurrency()), 32u); }
+
+void host_parallel(int ntasks, const std::function<void(int)> &fn) {
+  const int nth = std::min(host_threads(), ntasks);
+  if (nth <= 1) {
+    for (int t = 0; t < ntasks; ++t) fn(t);
+    return;
+  }
+  std::atomic<int> next{0};
+  auto work = [&] {
+    for (int t; (t = next.fetch_add(1, std::memory_order_relaxed)) < ntasks;) fn(t);
+  };
+  std::vector<std::thread> th;
+  for (int w = 1; w < nth; ++w) th.emplace_back(work);
+  work();
+  for (auto &x : th) x.join();
+}
+
+// Runs fn(begin, end) over [0, n) in contiguous runs (one run when n is
+// small); fn must write disjoint outputs per index.
+static void parallel_runs(long long n, long long min_per_run, const std::function<void(long long, long long)> &fn) {
+  const long long runs =
+      std::min<long long>(4LL * host_threads(), std::max<long long>(1, n / std::max(1LL, min_per_run)));
+  if (runs <= 1) {
+    fn(0, n);
+    return;
+  }
+  host_parallel((int)runs, [&](int r) { fn(n * r / runs, n * (r + 1) / runs); });
+}
+
+static inline void atomic_min_i64(std::atomic<long long> &a, long long v) {
+  long long cur = a.load(std::memory_order_relaxed);
+  while (v < cur && !a.compare_exchange_weak(cur, v, std::memory_order_relaxed)) {
+  }
+}
+
+// Loops with fewer elements than this run on the calling thread.
+constexpr long long kParMin = 32768;
 
 gba_status validate_problem(const gba_problem_view *v, std::string *err) {
   if (!v) {
@@ -40,7 +86,31 @@ gba_status validate_problem(const gba_problem_view *v, std::string *err) {
   if ((v->num_cameras > 0 || v->num_points > 0) && !v->parameters)
     return *err = "null parameter array", GBA_ERR_INVALID_ARGUMENT;
   const int nc = v->num_cameras, np = v->num_points;
-  for (int i = 0; i < v->num_observations; ++i) {
+  // the first bad observation and the first bad parameter (runs in
+  // parallel; the reported one is the lowest index, as a sequential scan)
+  auto bad_obs = [&](long long i) {
+    const int c = v->camera_index[i], p = v->point_index[i];
+    return c < 0 || c >= nc || p < 0 || p >= np || !std::isfinite(v->observations[2 * i]) ||
+           !std::isfinite(v->observations[2 * i + 1]);
+  };
+  const long long no = v->num_observations, npar = 9LL * nc + 3LL * np;
+  std::atomic<long long> first_obs{no}, first_par{npar};
+  parallel_runs(no, kParMin, [&](long long b, long long e) {
+    for (long long i = b; i < e && i < first_obs.load(std::memory_order_relaxed); ++i)
+      if (bad_obs(i)) {
+        atomic_min_i64(first_obs, i);
+        return;
+      }
+  });
+  parallel_runs(npar, 4 * kParMin, [&](long long b, long long e) {
+    for (long long k = b; k < e && k < first_par.load(std::memory_order_relaxed); ++k)
+      if (!std::isfinite(v->parameters[k])) {
+        atomic_min_i64(first_par, k);
+        return;
+      }
+  });
+  if (first_obs.load() < no) {
+    const long long i = first_obs.load();
     const int c = v->camera_index[i], p = v->point_index[i];
     if (c < 0 || c >= nc) {
       *err = fmt("observation %lld: camera index %lld out of range [0, %lld)", i, c, nc);
@@ -50,33 +120,37 @@ gba_status validate_problem(const gba_problem_view *v, std::string *err) {
       *err = fmt("observation %lld: point index %lld out of range [0, %lld)", i, p, np);
       return GBA_ERR_INVALID_ARGUMENT;
     }
-    if (!std::isfinite(v->observations[2 * i]) || !std::isfinite(v->observations[2 * i + 1])) {
-      *err = fmt("observation %lld is not finite", i);
-      return GBA_ERR_NON_FINITE;
-    }
+    *err = fmt("observation %lld is not finite", i);
+    return GBA_ERR_NON_FINITE;
   }
-  const long long npar = 9LL * nc + 3LL * np;
-  for (long long k = 0; k < npar; ++k)
-    if (!std::isfinite(v->parameters[k])) {
-      *err = fmt("parameter %lld is not finite", k);
-      return GBA_ERR_NON_FINITE;
-    }
+  if (first_par.load() < npar) {
+    *err = fmt("parameter %lld is not finite", first_par.load());
+    return GBA_ERR_NON_FINITE;
+  }
   return GBA_OK;
 }
 
-// Runs fn(begin, end) over [0, n) in runs on host threads (one run when n
-// is small); fn must write disjoint outputs per index.
-static void parallel_runs(long long n, long long min_per_thread, const std::function<void(long long, long long)> &fn) {
-  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-  const long long nth = std::min<long long>(std::min(hw, 32u), std::max<long long>(1, n / std::max(1LL, min_per_thread)));
-  if (nth <= 1) {
-    fn(0, n);
-    return;
+// Per-thread scratch tables indexed by camera, stamped so that they need no
+// clearing between uses: a slot is valid when its stamp is the caller's.
+namespace {
+std::atomic<long long> g_stamp_base{0};
+struct CamScratch {
+  std::vector<long long> mark;
+  std::vector<int32_t> a, b, c;
+};
+CamScratch &cam_scratch(int n) {
+  static thread_local CamScratch s;
+  if ((int)s.mark.size() < n) {
+    s.mark.resize(n, -1);
+    s.a.resize(n);
+    s.b.resize(n);
+    s.c.resize(n);
   }
-  std::vector<std::thread> th;
-  for (long long w = 0; w < nth; ++w) th.emplace_back([&, w] { fn(n * w / nth, n * (w + 1) / nth); });
-  for (auto &x : th) x.join();
+  return s;
 }
+// A fresh range of 2^32 stamps.
+long long new_stamps() { return g_stamp_base.fetch_add(1, std::memory_order_relaxed) << 32; }
+}  // namespace
 
 // The explicit Schur complement's structure, row camera by row camera: the
 // row's co-visible cameras (sorted; the row's own camera when it observes a
@@ -88,40 +162,49 @@ static void parallel_runs(long long n, long long min_per_thread, const std::func
 // so the formation sums have a fixed order.  A camera's observations
 // (cam_obs_list) are in point order, so walking them and each point's
 // observations lists every block's pairs in that order.  O(pairs) with a
-// per-row lookup table; the rows are independent, so host threads take runs
-// of rows (the result does not depend on the thread count).
+// per-row lookup table; the rows are independent, so the pool's threads
+// take runs of rows (the result does not depend on the split).
 static void build_schur_structure(HostBatch *hbp) {
   HostBatch &hb = *hbp;
   const int nc = hb.nc;
   // F rows are stored camera-major (a camera's observations together, in
   // point order): the pairs of a block read two cameras' runs of rows
   hb.obs_fpos.resize(hb.no);
-  for (int i = 0; i < hb.no; ++i) hb.obs_fpos[hb.cam_obs_list[i]] = i;
+  parallel_runs(hb.no, kParMin, [&](long long b, long long e) {
+    for (long long i = b; i < e; ++i) hb.obs_fpos[hb.cam_obs_list[i]] = (int32_t)i;
+  });
   std::vector<std::vector<int32_t>> rows(nc), cnts(nc);  // per row: columns; pair counts of its upper blocks
   std::vector<int32_t> first_up(nc, 0);                  // per row: index of its first column >= the row
-  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-  const int nth = (int)std::min<long long>(std::min(hw, 32u), std::max<long long>(1, (long long)hb.no / 20000));
-  auto for_rows = [&](const std::function<void(int, int, std::vector<int32_t> &, std::vector<int32_t> &)> &fn) {
-    std::vector<std::thread> th;
-    for (int w = 0; w < nth; ++w) {
-      const int c0 = (int)((long long)nc * w / nth), c1 = (int)((long long)nc * (w + 1) / nth);
-      th.emplace_back([&, c0, c1] {
-        std::vector<int32_t> mark(nc, -1), pos(nc, 0);
-        fn(c0, c1, mark, pos);
-      });
+  // runs of rows of about equal observation counts
+  std::vector<int> rb(1, 0);
+  {
+    const long long target = std::max<long long>(4096, (long long)hb.no / (8LL * host_threads()) + 1);
+    for (int c = 0; c < nc;) {
+      long long acc = 0;
+      int c1 = c;
+      do {
+        acc += hb.cam_obs_begin[c1 + 1] - hb.cam_obs_begin[c1];
+        ++c1;
+      } while (c1 < nc && acc < target);
+      rb.push_back(c1);
+      c = c1;
     }
-    for (auto &x : th) x.join();
-  };
+  }
+  const int nruns = (int)rb.size() - 1;
   // 1. per row: sorted co-visible cameras, pair counts of the upper blocks
-  for_rows([&](int c0, int c1, std::vector<int32_t> &mark, std::vector<int32_t> &pos) {
-    for (int c = c0; c < c1; ++c) {
+  const long long stamp = new_stamps();
+  host_parallel(nruns, [&](int r) {
+    CamScratch &s = cam_scratch(nc);
+    std::vector<int32_t> &pos = s.a;
+    for (int c = rb[r]; c < rb[r + 1]; ++c) {
+      const long long mk = stamp | c;
       const int a0 = hb.cam_obs_begin[c], a1 = hb.cam_obs_begin[c + 1];
       std::vector<int32_t> &row = rows[c];
       for (int ia = a0; ia < a1; ++ia) {
         const int a = hb.cam_obs_list[ia], j = hb.obs_pt[a];
         for (int b = hb.pt_obs_begin[j]; b < hb.pt_obs_begin[j + 1]; ++b) {
           const int k = hb.obs_cam[b];
-          if (b != a && mark[k] != c) mark[k] = c, row.push_back(k);
+          if (b != a && s.mark[k] != mk) s.mark[k] = mk, row.push_back(k);
         }
       }
       std::sort(row.begin(), row.end());
@@ -143,26 +226,28 @@ static void build_schur_structure(HostBatch *hbp) {
   for (int c = 0; c < nc; ++c) hb.sblk_row[c + 1] = hb.sblk_row[c] + (int32_t)rows[c].size();
   hb.nblk = hb.sblk_row[nc];
   hb.sblk_col.resize(hb.nblk);
-  hb.sblk_up.clear();
-  hb.sblk_pair.assign(1, 0);
   std::vector<long long> up_begin(nc + 1, 0);  // per row: its first upper block (index into sblk_up)
+  for (int c = 0; c < nc; ++c) up_begin[c + 1] = up_begin[c] + (long long)cnts[c].size();
+  hb.nup = up_begin[nc];
+  hb.sblk_up.resize(hb.nup);
+  hb.sblk_pair.resize(hb.nup + 1);
+  hb.sblk_pair[0] = 0;
   for (int c = 0; c < nc; ++c) {
     std::copy(rows[c].begin(), rows[c].end(), hb.sblk_col.begin() + hb.sblk_row[c]);
-    up_begin[c] = (long long)hb.sblk_up.size();
     for (size_t u = 0; u < cnts[c].size(); ++u) {
-      hb.sblk_up.push_back(hb.sblk_row[c] + first_up[c] + (int32_t)u);
-      hb.sblk_pair.push_back(hb.sblk_pair.back() + cnts[c][u]);
+      const long long k = up_begin[c] + (long long)u;
+      hb.sblk_up[k] = hb.sblk_row[c] + first_up[c] + (int32_t)u;
+      hb.sblk_pair[k + 1] = hb.sblk_pair[k] + cnts[c][u];
     }
   }
-  up_begin[nc] = (long long)hb.sblk_up.size();
-  hb.nup = (long long)hb.sblk_up.size();
-  hb.npairs = hb.sblk_pair.back();
+  hb.npairs = hb.sblk_pair[hb.nup];
   hb.spair.resize(2 * (size_t)hb.npairs);
   // 3. the pairs, in point order per block
-  for_rows([&](int c0, int c1, std::vector<int32_t> &mark, std::vector<int32_t> &pos) {
-    (void)mark;
+  host_parallel(nruns, [&](int r) {
+    CamScratch &s = cam_scratch(nc);
+    std::vector<int32_t> &pos = s.a;
     std::vector<int32_t> next;
-    for (int c = c0; c < c1; ++c) {
+    for (int c = rb[r]; c < rb[r + 1]; ++c) {
       const std::vector<int32_t> &row = rows[c];
       const int u0 = first_up[c], nu = (int)row.size() - u0;
       next.resize(nu);
@@ -183,8 +268,8 @@ static void build_schur_structure(HostBatch *hbp) {
   });
   // 4. the transpose of block (c, k) is block (k, c), in row k
   hb.sblk_tr.resize(hb.nblk);
-  for_rows([&](int c0, int c1, std::vector<int32_t> &, std::vector<int32_t> &) {
-    for (int c = c0; c < c1; ++c)
+  host_parallel(nruns, [&](int r) {
+    for (int c = rb[r]; c < rb[r + 1]; ++c)
       for (int e = hb.sblk_row[c]; e < hb.sblk_row[c + 1]; ++e) {
         const int k = hb.sblk_col[e];
         const auto b0 = hb.sblk_col.begin() + hb.sblk_row[k], b1 = hb.sblk_col.begin() + hb.sblk_row[k + 1];
@@ -193,17 +278,16 @@ static void build_schur_structure(HostBatch *hbp) {
   });
 }
 
+// Counts, offsets and appended arrays start empty; the arrays prepare_batch
+// overwrites entirely keep their size, so a batch of the same size is laid
+// out without re-zeroing them.
 void HostBatch::reset() {
   P = nc = np = no = nchunks = nseg = cam_blocks = 0;
   explicit_schur = false;
   nblk = nup = npairs = 0;
-  for (auto *v : {&obs_cam, &obs_pt, &pt_obs_begin, &pt_problem, &cam_problem, &seg_cam, &cam_seg_begin, &seg_slot,
-                  &cam_obs_begin, &cam_obs_list, &sblk_row, &sblk_col, &sblk_tr, &sblk_up, &sblk_pair, &spair,
-                  &obs_fpos, &obs_orig, &pt_orig})
+  for (auto *v : {&pt_obs_begin, &seg_cam, &cam_seg_begin, &cam_obs_begin, &sblk_row, &sblk_up, &sblk_pair})
     v->clear();
-  for (auto *v : {&obs_seg, &obs_slot, &seg_pos}) v->clear();
-  for (auto *v : {&obs_uv, &cam_param, &pt_param}) v->clear();
-  pt_used.clear();
+  seg_pos.clear();
   cam_used.clear();
   obs_rig.clear();
   prob_rig.clear();
@@ -250,19 +334,16 @@ gba_status prepare_batch(const gba_problem_view *views, int n, const PrepOptions
   hb.pt_obs_begin.assign(tp + 1, 0);
   hb.pt_problem.resize(tp);
   hb.cam_problem.resize(tc);
-  hb.pt_used.assign(tp, 0);
+  hb.pt_used.resize(tp);
   hb.cam_used.assign(tc, 0);
   hb.pt_orig.resize(tp);
   hb.cam_param.resize(9 * tc);
-  hb.pt_param.assign(4 * tp, 0.0);
+  hb.pt_param.resize(4 * tp);
   hb.cam_obs_begin.assign(tc + 1, 0);
   hb.cam_obs_list.resize(to);
 
   int cam0 = 0, pt0 = 0, obs0 = 0;
-  std::vector<int32_t> deg, key, order, inv, fill, cams;
-  // per camera of the batch, for the chunks' camera-sorted orders: the
-  // chunk that last saw it, its count, next position, segment
-  std::vector<int32_t> cmark(tc, -1), ccount(tc), cstart(tc), cseg(tc), distinct;
+  std::vector<int32_t> deg, key, order, inv, fill;
   for (int p = 0; p < n; ++p) {
     const gba_problem_view &v = views[p];
     const int nc = v.num_cameras, np = v.num_points, no = v.num_observations;
@@ -274,7 +355,6 @@ gba_status prepare_batch(const gba_problem_view *views, int n, const PrepOptions
     pi.obs_begin = obs0;
     pi.obs_count = no;
     pi.chunk_begin = (int)hb.chunk.size();
-    pi.seg_begin = (int)hb.seg_cam.size();
     // degrees, first camera of each point
     deg.assign(np, 0);
     key.assign(np, nc);
@@ -304,7 +384,9 @@ gba_status prepare_batch(const gba_problem_view *views, int n, const PrepOptions
       hb.pt_problem[pt0 + ji] = p;
       hb.pt_used[pt0 + ji] = deg[j] > 0;
       hb.pt_obs_begin[pt0 + ji + 1] = deg[j];
-      for (int q = 0; q < 3; ++q) hb.pt_param[4 * (size_t)(pt0 + ji) + q] = v.parameters[9 * (size_t)nc + 3 * (size_t)j + q];
+      double *x = hb.pt_param.data() + 4 * (size_t)(pt0 + ji);
+      for (int q = 0; q < 3; ++q) x[q] = v.parameters[9 * (size_t)nc + 3 * (size_t)j + q];
+      x[3] = 0.0;
     }
     hb.pt_obs_begin[pt0] = obs0;
     for (int ji = 0; ji < np; ++ji) hb.pt_obs_begin[pt0 + ji + 1] += hb.pt_obs_begin[pt0 + ji];
@@ -336,11 +418,9 @@ gba_status prepare_batch(const gba_problem_view *views, int n, const PrepOptions
         hb.obs_uv[2 * (size_t)k + 1] = v.observations[2 * (size_t)i + 1];
       }
     });
-    for (int c = 0; c < nc; ++c) {
-      hb.cam_problem[cam0 + c] = p;
-      for (int q = 0; q < 9; ++q) hb.cam_param[9 * (size_t)(cam0 + c) + q] = v.parameters[9 * (size_t)c + q];
-    }
-    // chunks of whole points
+    for (int c = 0; c < nc; ++c) hb.cam_problem[cam0 + c] = p;
+    if (nc > 0) std::memcpy(hb.cam_param.data() + 9 * (size_t)cam0, v.parameters, sizeof(double) * 9 * (size_t)nc);
+    // chunks of whole points (their camera orders below, for the whole batch)
     int ji = 0;
     while (ji < np) {
       ChunkInfo ci;
@@ -363,37 +443,9 @@ gba_status prepare_batch(const gba_problem_view *views, int n, const PrepOptions
       }
       ci.obs_count = nobs;
       ci.pt_count = npts;
-      // camera-sorted order of the chunk's observations, stable: the
-      // chunk's distinct cameras (a stamped table), sorted, then each
-      // observation's position from its camera's running count
-      const int stamp = (int)hb.chunk.size();
-      distinct.clear();
-      for (int k = 0; k < nobs; ++k) {
-        const int cam = hb.obs_cam[ci.obs_begin + k];
-        if (cmark[cam] != stamp) cmark[cam] = stamp, ccount[cam] = 0, distinct.push_back(cam);
-        ++ccount[cam];
-      }
-      std::sort(distinct.begin(), distinct.end());
-      ci.seg_begin = (int)hb.seg_cam.size();
-      const int segs = (int)distinct.size();
-      for (int sg = 0, pos = 0; sg < segs; ++sg) {
-        const int cam = distinct[sg];
-        hb.seg_pos.push_back((uint16_t)pos);
-        hb.seg_cam.push_back(cam);
-        cstart[cam] = pos;
-        cseg[cam] = sg;
-        pos += ccount[cam];
-      }
-      for (int k = 0; k < nobs; ++k) {
-        const int cam = hb.obs_cam[ci.obs_begin + k];
-        hb.obs_slot[ci.obs_begin + k] = (uint16_t)cstart[cam]++;
-        hb.obs_seg[ci.obs_begin + k] = (uint16_t)cseg[cam];
-      }
-      ci.seg_count = segs;
       hb.chunk.push_back(ci);
     }
     pi.chunk_count = (int)hb.chunk.size() - pi.chunk_begin;
-    pi.seg_count = (int)hb.seg_cam.size() - pi.seg_begin;
     // camera blocks of the PCG kernels
     pi.cam_block_begin = (int)hb.camblk.size();
     for (int c = 0; c < nc; c += kPcgBlockCams) {
@@ -410,8 +462,74 @@ gba_status prepare_batch(const gba_problem_view *views, int n, const PrepOptions
     obs0 += no;
   }
   hb.nchunks = (int)hb.chunk.size();
-  hb.nseg = (int)hb.seg_cam.size();
   hb.cam_blocks = (int)hb.camblk.size();
+  // per chunk, the camera-sorted order of its observations, stable: the
+  // chunk's distinct cameras (a stamped table), sorted, then each
+  // observation's position from its camera's running count.  Two passes
+  // over runs of chunks: the segment counts, then (at their offsets) the
+  // segments and the orders.
+  const int nch = hb.nchunks;
+  const long long chunk_runs = std::max<long long>(1, std::min<long long>(4LL * host_threads(), (long long)to / 8192));
+  std::vector<int32_t> seg_off(nch + 1, 0);
+  {
+    const long long st = new_stamps();
+    host_parallel((int)chunk_runs, [&](int r) {
+      CamScratch &s = cam_scratch((int)tc);
+      for (int ch = (int)((long long)nch * r / chunk_runs); ch < (int)((long long)nch * (r + 1) / chunk_runs); ++ch) {
+        const ChunkInfo &ci = hb.chunk[ch];
+        const long long mk = st | ch;
+        int segs = 0;
+        for (int k = 0; k < ci.obs_count; ++k) {
+          const int cam = hb.obs_cam[ci.obs_begin + k];
+          if (s.mark[cam] != mk) s.mark[cam] = mk, ++segs;
+        }
+        seg_off[ch + 1] = segs;
+      }
+    });
+  }
+  for (int ch = 0; ch < nch; ++ch) seg_off[ch + 1] += seg_off[ch];
+  hb.nseg = seg_off[nch];
+  hb.seg_pos.resize(hb.nseg);
+  hb.seg_cam.resize(hb.nseg);
+  {
+    const long long st = new_stamps();
+    host_parallel((int)chunk_runs, [&](int r) {
+      CamScratch &s = cam_scratch((int)tc);
+      std::vector<int32_t> distinct;
+      int32_t *count = s.a.data(), *start = s.b.data(), *segi = s.c.data();
+      for (int ch = (int)((long long)nch * r / chunk_runs); ch < (int)((long long)nch * (r + 1) / chunk_runs); ++ch) {
+        ChunkInfo &ci = hb.chunk[ch];
+        const long long mk = st | ch;
+        distinct.clear();
+        for (int k = 0; k < ci.obs_count; ++k) {
+          const int cam = hb.obs_cam[ci.obs_begin + k];
+          if (s.mark[cam] != mk) s.mark[cam] = mk, count[cam] = 0, distinct.push_back(cam);
+          ++count[cam];
+        }
+        std::sort(distinct.begin(), distinct.end());
+        ci.seg_begin = seg_off[ch];
+        ci.seg_count = (int)distinct.size();
+        for (int sg = 0, pos = 0; sg < ci.seg_count; ++sg) {
+          const int cam = distinct[sg];
+          hb.seg_pos[ci.seg_begin + sg] = (uint16_t)pos;
+          hb.seg_cam[ci.seg_begin + sg] = cam;
+          start[cam] = pos;
+          segi[cam] = sg;
+          pos += count[cam];
+        }
+        for (int k = 0; k < ci.obs_count; ++k) {
+          const int cam = hb.obs_cam[ci.obs_begin + k];
+          hb.obs_slot[ci.obs_begin + k] = (uint16_t)start[cam]++;
+          hb.obs_seg[ci.obs_begin + k] = (uint16_t)segi[cam];
+        }
+      }
+    });
+  }
+  for (int p = 0; p < n; ++p) {
+    ProblemInfo &pi = hb.prob[p];
+    pi.seg_begin = seg_off[pi.chunk_begin];
+    pi.seg_count = seg_off[pi.chunk_begin + pi.chunk_count] - pi.seg_begin;
+  }
   // per camera: its segments (chunk order) and its observations (internal order)
   hb.cam_seg_begin.assign(hb.nc + 1, 0);
   for (int s = 0; s < hb.nseg; ++s) ++hb.cam_seg_begin[hb.seg_cam[s] + 1];
@@ -426,23 +544,54 @@ gba_status prepare_batch(const gba_problem_view *views, int n, const PrepOptions
   // kExplicitPairsPerObs per observation (forming S then costs less than the
   // implicit mat-vec saves over a PCG solve)
   {
-    long long pairs = 0;
-    for (int j = 0; j < hb.np; ++j) {
-      const long long m = hb.pt_obs_begin[j + 1] - hb.pt_obs_begin[j];
-      pairs += m * (m - 1);
-    }
+    std::atomic<long long> pairs{0};
+    parallel_runs(hb.np, kParMin, [&](long long j0, long long j1) {
+      long long s = 0;
+      for (long long j = j0; j < j1; ++j) {
+        const long long m = hb.pt_obs_begin[j + 1] - hb.pt_obs_begin[j];
+        s += m * (m - 1);
+      }
+      pairs.fetch_add(s, std::memory_order_relaxed);
+    });
     hb.explicit_schur = opt.schur == GBA_SCHUR_EXPLICIT ||
-                        (opt.schur == GBA_SCHUR_AUTO && pairs <= kExplicitPairsPerObs * (long long)hb.no);
-    if (hb.explicit_schur && pairs > kExplicitPairsMax) {
-      *err = fmt("the explicit Schur complement needs %lld observation pairs; at most %lld are supported", pairs,
-                 (long long)kExplicitPairsMax);
+                        (opt.schur == GBA_SCHUR_AUTO && pairs.load() <= kExplicitPairsPerObs * (long long)hb.no);
+    if (hb.explicit_schur && pairs.load() > kExplicitPairsMax) {
+      *err = fmt("the explicit Schur complement needs %lld observation pairs; at most %lld are supported",
+                 pairs.load(), (long long)kExplicitPairsMax);
       return GBA_ERR_INVALID_ARGUMENT;
     }
   }
-  for (int k = 0; k < hb.no; ++k) ++hb.cam_obs_begin[hb.obs_cam[k] + 1];
-  for (int c = 0; c < hb.nc; ++c) hb.cam_obs_begin[c + 1] += hb.cam_obs_begin[c];
-  fill.assign(hb.cam_obs_begin.begin(), hb.cam_obs_begin.end());
-  for (int k = 0; k < hb.no; ++k) hb.cam_obs_list[fill[hb.obs_cam[k]]++] = k;
+  // each camera's observations in internal order: a stable counting sort by
+  // camera over runs of observations (per-run counts, then offsets)
+  {
+    const long long runs = std::min<long long>(std::max<long long>(1, to / kParMin), 2LL * host_threads());
+    if (runs <= 1 || runs * tc > (1LL << 24)) {
+      for (int k = 0; k < hb.no; ++k) ++hb.cam_obs_begin[hb.obs_cam[k] + 1];
+      for (int c = 0; c < hb.nc; ++c) hb.cam_obs_begin[c + 1] += hb.cam_obs_begin[c];
+      fill.assign(hb.cam_obs_begin.begin(), hb.cam_obs_begin.end());
+      for (int k = 0; k < hb.no; ++k) hb.cam_obs_list[fill[hb.obs_cam[k]]++] = k;
+    } else {
+      std::vector<int32_t> cnt((size_t)runs * tc, 0);
+      host_parallel((int)runs, [&](int r) {
+        int32_t *c = cnt.data() + (size_t)r * tc;
+        for (long long k = to * r / runs; k < to * (r + 1) / runs; ++k) ++c[hb.obs_cam[k]];
+      });
+      long long acc = 0;
+      for (long long c = 0; c < tc; ++c) {
+        hb.cam_obs_begin[c] = (int32_t)acc;
+        for (long long r = 0; r < runs; ++r) {
+          const int32_t x = cnt[(size_t)r * tc + c];
+          cnt[(size_t)r * tc + c] = (int32_t)acc;
+          acc += x;
+        }
+      }
+      hb.cam_obs_begin[tc] = (int32_t)acc;
+      host_parallel((int)runs, [&](int r) {
+        int32_t *c = cnt.data() + (size_t)r * tc;
+        for (long long k = to * r / runs; k < to * (r + 1) / runs; ++k) hb.cam_obs_list[c[hb.obs_cam[k]]++] = (int32_t)k;
+      });
+    }
+  }
   if (hb.explicit_schur) build_schur_structure(&hb);
   return GBA_OK;
 }
@@ -452,10 +601,12 @@ void scatter_parameters(const HostBatch &hb, int p, const double *cam_param, con
   const ProblemInfo &pi = hb.prob[p];
   std::memcpy(out, cam_param + 9 * (size_t)pi.cam_begin, sizeof(double) * 9 * (size_t)pi.cam_count);
   double *pts = out + 9 * (size_t)pi.cam_count;
-  for (int ji = 0; ji < pi.pt_count; ++ji) {
-    const int j = hb.pt_orig[pi.pt_begin + ji];
-    for (int q = 0; q < 3; ++q) pts[3 * (size_t)j + q] = pt_param[4 * (size_t)(pi.pt_begin + ji) + q];
-  }
+  parallel_runs(pi.pt_count, kParMin, [&](long long j0, long long j1) {
+    for (long long ji = j0; ji < j1; ++ji) {
+      const int j = hb.pt_orig[pi.pt_begin + ji];
+      for (int q = 0; q < 3; ++q) pts[3 * (size_t)j + q] = pt_param[4 * (size_t)(pi.pt_begin + ji) + q];
+    }
+  });
 }
 
 }  // namespace gba

@@ -3,6 +3,7 @@
 // segments).  Pure host code, testable without a GPU.
 #pragma once
 
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -50,10 +51,19 @@ struct HostBatch {
   // observation, and per problem fx, fy, cx, cy, then (R, t) of E_0 and E_1
   std::vector<uint8_t> obs_rig;
   std::vector<double> prob_rig;   // kRig per problem
-  // Empties the batch but keeps the vectors' storage (a handle re-preparing
-  // problems of similar size touches no fresh pages).
+  // Starts a new batch: counts, offsets and appended arrays emptied; the
+  // arrays prepare_batch overwrites entirely keep their size and storage (a
+  // handle re-preparing problems of similar size neither touches fresh
+  // pages nor re-zeroes them).
   void reset();
 };
+
+// The host thread pool of the prep (and of other host-side data-parallel
+// copies): fn(task) for task in [0, ntasks), on the pool's threads and the
+// caller's; fn must write disjoint outputs per task.  Runs on the calling
+// thread alone when the pool is busy.
+int host_threads();
+void host_parallel(int ntasks, const std::function<void(int)> &fn);
 
 // Validates and lays out `n` problems.  Returns GBA_OK or an error with a
 // message in *err.
