@@ -10,6 +10,10 @@ iterations/s of the mixed-precision form with the problem resident in HBM
 public C ABI call (gba_solve) with host buffers, host prep and transfers
 inside the timed region.
 
+Beside them (rank 0, one GPU): `forms.large` (configuration 2), `batched`
+(configuration 3), `serving` (configuration 4) and `local_ba` (full_slam's
+local-BA windows, the g2o policy; `--local-ba-only` prints that form alone).
+
 --impl reference times the CPU oracle (the C restatement of the reference's
 Ceres path: exact Schur + dense Cholesky) on this host's cores instead.
 
@@ -625,12 +629,16 @@ def main():
     ap.add_argument("--lm-iterations", type=int, default=0,
                     help="with --profile-solve: LM iterations (0 = the workload's 50)")
     ap.add_argument("--no-extra-forms", action="store_true",
-                    help="skip the batched (configuration 3) and serving (configuration 4) forms")
+                    help="skip the large, batched, serving and local-BA forms")
+    ap.add_argument("--local-ba-only", action="store_true",
+                    help="print only the local-BA form (full_slam's windows) as one JSON line")
     args = ap.parse_args()
     from slamplay_gb300 import build as B
 
     B.build()
-    if args.profile_solve:
+    if args.local_ba_only:
+        print(json.dumps({"form": "local_ba", **local_ba_form()}), flush=True)
+    elif args.profile_solve:
         run_profile_solve(args)
     elif args.impl == "reference":
         from oracle import oracle_py
