@@ -165,3 +165,29 @@ def test_footprint_estimate_monotone():
     c = estimate_footprint(1800, 1000000, 5000000, "mixed")
     assert b < a < c
     assert 50e6 < a < 400e6
+
+
+def test_c_abi_header_is_plain_c():
+    """include/gba.h is the C ABI: it compiles as C99 with every warning on,
+    and a C caller can fill the window view and the options."""
+    import shutil
+    import subprocess
+    import tempfile
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc missing")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    src = ("#include \"gba.h\"\n"
+           "int main(void) {\n"
+           "  gba_options o; gba_window_view w; gba_window_result r;\n"
+           "  gba_local_ba_options_init(&o); gba_window_view_init(&w);\n"
+           "  o.camera_update = GBA_CAMERA_UPDATE_SO3_LEFT; o.lm_policy = GBA_LM_POLICY_G2O;\n"
+           "  w.rig.extrinsic[1][3] = -0.5; r.num_inliers = 0;\n"
+           "  return (int)(w.max_threshold_doublings + r.num_inliers - 5);\n"
+           "}\n")
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "t.c")
+        with open(c, "w") as f:
+            f.write(src)
+        r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-fsyntax-only",
+                            "-I", os.path.join(root, "include"), c], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
