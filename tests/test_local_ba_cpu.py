@@ -3,6 +3,8 @@ full_slam/include/myslam/g2o_types.h:127-175), the SE3 left update (VertexPose,
 :48-66) and the outlier-threshold loop (full_slam/src/backend.cpp:156-187),
 checked against independent restatements (numpy, scipy's matrix exponential,
 central differences)."""
+import os
+
 import numpy as np
 import pytest
 
@@ -150,3 +152,40 @@ def test_oracle_window_flags_the_planted_outliers():
     # the 20-60 px outliers are all flagged; the rest is chi2 with 2 dof
     # of unit pixel noise (about 5 % above 5.991)
     assert 0.05 <= no_ / w.num_observations <= 0.13
+
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _fixture_window(g):
+    K = g["window_K"]
+    return LocalBAWindow(g["window_keyframe_index"], g["window_landmark_index"], g["window_rig_camera"],
+                         g["window_observations"], g["window_poses"], g["window_landmarks"], K[0], K[1], K[2],
+                         K[3], g["window_extrinsics"])
+
+
+def test_oracle_reproduces_the_variant_fixtures():
+    """The oracle's g2o-variant solve and local-BA solve against the stored
+    ones (tests/golden/make_golden.py): a change to either restatement shows
+    here first."""
+    from slamplay_gb300 import G2O_VARIANT, LOCAL_BA
+    g = np.load(os.path.join(GOLDEN, "variants.npz"))
+    gs = np.load(os.path.join(GOLDEN, "small_problem.npz"))
+    p = O.Problem(int(gs["num_cameras"]), int(gs["num_points"]), gs["camera_index"], gs["point_index"],
+                  gs["observations"], gs["parameters"])
+    r = O.solve(p, linear_solver="dense_schur", **dict(G2O_VARIANT, max_num_iterations=15))
+    np.testing.assert_allclose(r["trace_cost"], g["g2o_trace_cost"], rtol=1e-12)
+    np.testing.assert_allclose(r["trace_radius"], g["g2o_trace_radius"], rtol=1e-12)
+    np.testing.assert_allclose(r["parameters"], g["g2o_final_parameters"], rtol=1e-9, atol=1e-9)
+    w = _fixture_window(g)
+    rig = O.rig_from_window(w)
+    r = O.solve(O.window_problem(w), rig=rig, linear_solver="dense_schur", **LOCAL_BA)
+    np.testing.assert_allclose(r["trace_cost"], g["window_trace_cost"], rtol=1e-12)
+    np.testing.assert_allclose(r["parameters"], g["window_final_parameters"], rtol=1e-9, atol=1e-9)
+    q = O.window_problem(w)
+    q.params[:] = r["parameters"]
+    res, _, _, ok = O.evaluate_rig(q, rig)
+    chi2 = np.sum(res * res, axis=1)
+    np.testing.assert_allclose(chi2, g["window_chi2"], rtol=1e-9, atol=1e-12)
+    flags, _, _, th = O.window_outliers(chi2)
+    assert th == g["window_threshold"][0] and np.array_equal(flags, g["window_outlier"])
