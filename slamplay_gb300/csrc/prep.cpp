@@ -195,7 +195,7 @@ static void build_schur_structure(HostBatch *hbp) {
   const long long stamp = new_stamps();
   host_parallel(nruns, [&](int r) {
     CamScratch &s = cam_scratch(nc);
-    std::vector<int32_t> &pos = s.a;
+    int32_t *pairs_of = s.a.data();  // per column camera: the row's pair count
     for (int c = rb[r]; c < rb[r + 1]; ++c) {
       const long long mk = stamp | c;
       const int a0 = hb.cam_obs_begin[c], a1 = hb.cam_obs_begin[c + 1];
@@ -204,7 +204,9 @@ static void build_schur_structure(HostBatch *hbp) {
         const int a = hb.cam_obs_list[ia], j = hb.obs_pt[a];
         for (int b = hb.pt_obs_begin[j]; b < hb.pt_obs_begin[j + 1]; ++b) {
           const int k = hb.obs_cam[b];
-          if (b != a && s.mark[k] != mk) s.mark[k] = mk, row.push_back(k);
+          if (b == a) continue;
+          if (s.mark[k] != mk) s.mark[k] = mk, row.push_back(k), pairs_of[k] = 0;
+          ++pairs_of[k];
         }
       }
       std::sort(row.begin(), row.end());
@@ -212,13 +214,8 @@ static void build_schur_structure(HostBatch *hbp) {
       const int u0 = (int)(std::lower_bound(row.begin(), row.end(), c) - row.begin());
       first_up[c] = u0;
       std::vector<int32_t> &cnt = cnts[c];
-      cnt.assign(nb - u0, 0);
-      for (int u = u0; u < nb; ++u) pos[row[u]] = u - u0;
-      for (int ia = a0; ia < a1; ++ia) {
-        const int a = hb.cam_obs_list[ia], j = hb.obs_pt[a];
-        for (int b = hb.pt_obs_begin[j]; b < hb.pt_obs_begin[j + 1]; ++b)
-          if (b != a && hb.obs_cam[b] >= c) ++cnt[pos[hb.obs_cam[b]]];
-      }
+      cnt.resize(nb - u0);
+      for (int u = u0; u < nb; ++u) cnt[u - u0] = pairs_of[row[u]];
     }
   });
   // 2. prefix sums: the CSR, the upper blocks, their pair ranges
@@ -343,7 +340,8 @@ gba_status prepare_batch(const gba_problem_view *views, int n, const PrepOptions
   hb.cam_obs_list.resize(to);
 
   int cam0 = 0, pt0 = 0, obs0 = 0;
-  std::vector<int32_t> deg, key, order, inv, fill;
+  std::vector<int32_t> deg, key, order, inv, fill, part_deg, part_key;
+  std::vector<uint8_t> part_used;
   for (int p = 0; p < n; ++p) {
     const gba_problem_view &v = views[p];
     const int nc = v.num_cameras, np = v.num_points, no = v.num_observations;
@@ -355,14 +353,50 @@ gba_status prepare_batch(const gba_problem_view *views, int n, const PrepOptions
     pi.obs_begin = obs0;
     pi.obs_count = no;
     pi.chunk_begin = (int)hb.chunk.size();
-    // degrees, first camera of each point
+    // degrees, first camera of each point.  A large problem takes runs of
+    // its observations on host threads, each counting into its own
+    // per-point arrays (merged over the runs); the same runs then place
+    // their observations in the points' ranges after the earlier runs', so
+    // each point keeps its input order as in one sequential pass.
+    const long long runs =
+        std::min<long long>({(long long)host_threads(), (long long)no / 16384, (1LL << 22) / std::max(1, np)});
+    auto run_begin = [&](long long r) { return (int)((long long)no * r / runs); };
     deg.assign(np, 0);
     key.assign(np, nc);
-    for (int i = 0; i < no; ++i) {
-      const int c = v.camera_index[i], j = v.point_index[i];
-      ++deg[j];
-      if (c < key[j]) key[j] = c;
-      hb.cam_used[cam0 + c] = 1;
+    if (runs > 1) {
+      part_deg.assign((size_t)runs * np, 0);
+      part_key.assign((size_t)runs * np, nc);
+      part_used.assign((size_t)runs * nc, 0);
+      host_parallel((int)runs, [&](int r) {
+        int32_t *d = part_deg.data() + (size_t)r * np, *k = part_key.data() + (size_t)r * np;
+        uint8_t *u = part_used.data() + (size_t)r * nc;
+        for (int i = run_begin(r); i < run_begin(r + 1); ++i) {
+          const int c = v.camera_index[i], j = v.point_index[i];
+          ++d[j];
+          if (c < k[j]) k[j] = c;
+          u[c] = 1;
+        }
+      });
+      parallel_runs(np, 8192, [&](long long j0, long long j1) {
+        for (long long j = j0; j < j1; ++j) {
+          int32_t dj = 0, kj = nc;
+          for (long long r = 0; r < runs; ++r) {
+            dj += part_deg[(size_t)r * np + j];
+            kj = std::min(kj, part_key[(size_t)r * np + j]);
+          }
+          deg[j] = dj;
+          key[j] = kj;
+        }
+      });
+      for (int c = 0; c < nc; ++c)
+        for (long long r = 0; r < runs; ++r) hb.cam_used[cam0 + c] |= part_used[(size_t)r * nc + c];
+    } else {
+      for (int i = 0; i < no; ++i) {
+        const int c = v.camera_index[i], j = v.point_index[i];
+        ++deg[j];
+        if (c < key[j]) key[j] = c;
+        hb.cam_used[cam0 + c] = 1;
+      }
     }
     // internal point order: by first camera (locality of the camera
     // segments in the chunk kernels), stable in the input index
@@ -376,22 +410,42 @@ gba_status prepare_batch(const gba_problem_view *views, int n, const PrepOptions
       for (int j = 0; j < np; ++j) order[j] = j;
     }
     inv.resize(np);
-    for (int ji = 0; ji < np; ++ji) inv[order[ji]] = ji;
     // CSR by internal point, observations stable in input index
-    for (int ji = 0; ji < np; ++ji) {
-      const int j = order[ji];
-      hb.pt_orig[pt0 + ji] = j;
-      hb.pt_problem[pt0 + ji] = p;
-      hb.pt_used[pt0 + ji] = deg[j] > 0;
-      hb.pt_obs_begin[pt0 + ji + 1] = deg[j];
-      double *x = hb.pt_param.data() + 4 * (size_t)(pt0 + ji);
-      for (int q = 0; q < 3; ++q) x[q] = v.parameters[9 * (size_t)nc + 3 * (size_t)j + q];
-      x[3] = 0.0;
-    }
+    parallel_runs(np, 8192, [&](long long j0, long long j1) {
+      for (int ji = (int)j0; ji < (int)j1; ++ji) {
+        const int j = order[ji];
+        inv[j] = ji;
+        hb.pt_orig[pt0 + ji] = j;
+        hb.pt_problem[pt0 + ji] = p;
+        hb.pt_used[pt0 + ji] = deg[j] > 0;
+        hb.pt_obs_begin[pt0 + ji + 1] = deg[j];
+        double *x = hb.pt_param.data() + 4 * (size_t)(pt0 + ji);
+        for (int q = 0; q < 3; ++q) x[q] = v.parameters[9 * (size_t)nc + 3 * (size_t)j + q];
+        x[3] = 0.0;
+      }
+    });
     hb.pt_obs_begin[pt0] = obs0;
     for (int ji = 0; ji < np; ++ji) hb.pt_obs_begin[pt0 + ji + 1] += hb.pt_obs_begin[pt0 + ji];
-    fill.assign(hb.pt_obs_begin.begin() + pt0, hb.pt_obs_begin.begin() + pt0 + np + 1);
-    for (int i = 0; i < no; ++i) hb.obs_orig[fill[inv[v.point_index[i]]]++] = i;
+    if (runs > 1) {
+      // per (run, point): where the run's observations of the point start
+      parallel_runs(np, 8192, [&](long long j0, long long j1) {
+        for (long long j = j0; j < j1; ++j) {
+          int32_t base = hb.pt_obs_begin[pt0 + inv[j]];
+          for (long long r = 0; r < runs; ++r) {
+            const int32_t d = part_deg[(size_t)r * np + j];
+            part_deg[(size_t)r * np + j] = base;
+            base += d;
+          }
+        }
+      });
+      host_parallel((int)runs, [&](int r) {
+        int32_t *at = part_deg.data() + (size_t)r * np;
+        for (int i = run_begin(r); i < run_begin(r + 1); ++i) hb.obs_orig[at[v.point_index[i]]++] = i;
+      });
+    } else {
+      fill.assign(hb.pt_obs_begin.begin() + pt0, hb.pt_obs_begin.begin() + pt0 + np + 1);
+      for (int i = 0; i < no; ++i) hb.obs_orig[fill[inv[v.point_index[i]]]++] = i;
+    }
     // within a point: by camera, then input index (insertion sort, stable);
     // points and observations are independent (host threads)
     parallel_runs(np, 20000, [&](long long j0, long long j1) {
