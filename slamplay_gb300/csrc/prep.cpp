@@ -7,16 +7,20 @@
 // chunks of whole points; per chunk the camera-sorted order of its
 // observations and its camera segments; per camera its segments and its
 // observations.  All orderings are deterministic functions of the input.
-// The data-parallel loops run on host threads; no result depends on how
-// their work is split.
+// The data-parallel loops run on a pool of host threads; no result depends
+// on how their work is split.
 #include "prep.h"
+
+#include <unistd.h>
 
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <condition_variable>
 #include <cstdio>
 #include <cstring>
 #include <functional>
+#include <mutex>
 #include <thread>
 
 namespace gba {
@@ -28,27 +32,101 @@ static std::string fmt(const char *f, long long a, long long b = 0, long long c 
 }
 
 // ---------------------------------------------------------------------------
-// Host threads for the prep's data-parallel loops: up to the hardware
-// threads (at most 32), started per loop and joined before it returns, the
-// calling thread working too; tasks are taken from a shared counter, and no
-// result depends on which thread runs a task.
-int host_threads() { return (int)std::min(std::max(1u, std::thread::hardware_concurrency()), 32u); }
+// Host thread pool for the data-parallel loops: hardware threads (at most
+// 32) made on first use and kept (starting threads costs far more than a
+// loop's wake-up), the calling thread working too; tasks are taken from a
+// shared counter, and no result depends on which thread runs a task.  A loop
+// that finds the pool busy (another handle preparing at the same time), runs
+// inside a task, or runs in a forked child works on the calling thread alone.
+namespace {
+thread_local bool tl_in_task = false;  // this thread is running a pool task
 
-void host_parallel(int ntasks, const std::function<void(int)> &fn) {
-  const int nth = std::min(host_threads(), ntasks);
-  if (nth <= 1) {
-    for (int t = 0; t < ntasks; ++t) fn(t);
-    return;
+class Pool {
+ public:
+  static Pool &get() {
+    static Pool p;
+    return p;
   }
-  std::atomic<int> next{0};
-  auto work = [&] {
-    for (int t; (t = next.fetch_add(1, std::memory_order_relaxed)) < ntasks;) fn(t);
-  };
-  std::vector<std::thread> th;
-  for (int w = 1; w < nth; ++w) th.emplace_back(work);
-  work();
-  for (auto &x : th) x.join();
-}
+  int threads() const { return (int)workers_.size() + 1; }
+  void run(int ntasks, const std::function<void(int)> &fn) {
+    if (ntasks <= 0) return;
+    std::unique_lock<std::mutex> busy(run_mu_, std::defer_lock);
+    if (ntasks == 1 || workers_.empty() || tl_in_task || getpid() != pid_ || !busy.try_lock()) {
+      for (int t = 0; t < ntasks; ++t) fn(t);
+      return;
+    }
+    {
+      std::lock_guard<std::mutex> g(mu_);
+      fn_ = &fn;
+      ntasks_ = ntasks;
+      next_.store(0, std::memory_order_relaxed);
+      done_ = 0;
+      ++gen_;
+    }
+    cv_.notify_all();
+    work();
+    std::unique_lock<std::mutex> g(mu_);
+    done_cv_.wait(g, [&] { return done_ == (int)workers_.size(); });
+    fn_ = nullptr;
+  }
+
+ private:
+  Pool() : pid_(getpid()) {
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const int n = (int)std::min(hw, 32u) - 1;
+    try {
+      for (int i = 0; i < n; ++i) workers_.emplace_back([this] { loop(); });
+    } catch (...) {
+      // fewer threads than asked: the loop counts only those that started
+    }
+  }
+  ~Pool() {
+    {
+      std::lock_guard<std::mutex> g(mu_);
+      stop_ = true;
+    }
+    cv_.notify_all();
+    for (auto &t : workers_)
+      if (t.joinable()) t.join();
+  }
+  void work() {
+    tl_in_task = true;
+    for (;;) {
+      const int t = next_.fetch_add(1, std::memory_order_relaxed);
+      if (t >= ntasks_) break;
+      (*fn_)(t);
+    }
+    tl_in_task = false;
+  }
+  void loop() {
+    long long seen = 0;
+    std::unique_lock<std::mutex> g(mu_);
+    for (;;) {
+      cv_.wait(g, [&] { return stop_ || gen_ != seen; });
+      if (stop_) return;
+      seen = gen_;
+      g.unlock();
+      work();
+      g.lock();
+      if (++done_ == (int)workers_.size()) done_cv_.notify_one();
+    }
+  }
+  std::vector<std::thread> workers_;
+  std::mutex run_mu_, mu_;
+  std::condition_variable cv_, done_cv_;
+  const std::function<void(int)> *fn_ = nullptr;
+  int ntasks_ = 0;
+  std::atomic<int> next_{0};
+  int done_ = 0;
+  long long gen_ = 0;
+  bool stop_ = false;
+  const pid_t pid_;
+};
+}  // namespace
+
+int host_threads() { return Pool::get().threads(); }
+
+void host_parallel(int ntasks, const std::function<void(int)> &fn) { Pool::get().run(ntasks, fn); }
 
 // Runs fn(begin, end) over [0, n) in contiguous runs (one run when n is
 // small); fn must write disjoint outputs per index.
@@ -523,7 +601,7 @@ gba_status prepare_batch(const gba_problem_view *views, int n, const PrepOptions
   // over runs of chunks: the segment counts, then (at their offsets) the
   // segments and the orders.
   const int nch = hb.nchunks;
-  const long long chunk_runs = std::max<long long>(1, std::min<long long>(4LL * host_threads(), (long long)to / 8192));
+  const long long chunk_runs = std::max<long long>(1, std::min<long long>(4LL * host_threads(), (long long)to / 16384));
   std::vector<int32_t> seg_off(nch + 1, 0);
   {
     const long long st = new_stamps();
