@@ -18,6 +18,7 @@
 #include <cmath>
 #include <condition_variable>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <functional>
 #include <mutex>
@@ -33,7 +34,7 @@ static std::string fmt(const char *f, long long a, long long b = 0, long long c 
 
 // ---------------------------------------------------------------------------
 // Host thread pool for the data-parallel loops: hardware threads (at most
-// 32) made on first use and kept (starting threads costs far more than a
+// 32, or GBA_HOST_THREADS) made on first use and kept (starting threads costs far more than a
 // loop's wake-up), the calling thread working too; tasks are taken from a
 // shared counter, and no result depends on which thread runs a task.  A loop
 // that finds the pool busy (another handle preparing at the same time), runs
@@ -72,7 +73,12 @@ class Pool {
 
  private:
   Pool() : pid_(getpid()) {
-    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    // GBA_HOST_THREADS caps the host threads (1: every loop on the caller's)
+    if (const char *env = std::getenv("GBA_HOST_THREADS")) {
+      const long v = std::strtol(env, nullptr, 10);
+      if (v >= 1) hw = std::min<unsigned>(hw, (unsigned)v);
+    }
     const int n = (int)std::min(hw, 32u) - 1;
     try {
       for (int i = 0; i < n; ++i) workers_.emplace_back([this] { loop(); });
