@@ -189,3 +189,34 @@ def test_oracle_reproduces_the_variant_fixtures():
     np.testing.assert_allclose(chi2, g["window_chi2"], rtol=1e-9, atol=1e-12)
     flags, _, _, th = O.window_outliers(chi2)
     assert th == g["window_threshold"][0] and np.array_equal(flags, g["window_outlier"])
+
+
+def test_se3_left_update_inverse_and_identity():
+    rng = np.random.default_rng(11)
+    for _ in range(100):
+        pose = np.concatenate([rng.normal(size=3) * 0.7, rng.normal(size=3) * 3])
+        dw, du = rng.normal(size=3) * rng.choice([1.0, 1e-3, 1e-7]), rng.normal(size=3)
+        # the identity: translation exact, rotation through the quaternion round trip
+        same = O.se3_compose_left(np.zeros(3), np.zeros(3), pose)
+        np.testing.assert_array_equal(same[3:], pose[3:])
+        np.testing.assert_allclose(same[:3], pose[:3], rtol=1e-14, atol=1e-15)
+        # exp(-xi) exp(xi) T = T
+        back = O.se3_compose_left(-dw, -du, O.se3_compose_left(dw, du, pose))
+        np.testing.assert_allclose(_R(back[:3]), _R(pose[:3]), atol=1e-12)
+        np.testing.assert_allclose(back[3:], pose[3:], atol=1e-11)
+
+
+def test_synthetic_window_is_deterministic_and_in_spec():
+    a, ta = LocalBAWindow.synthetic(seed=12, return_truth=True)
+    b = LocalBAWindow.synthetic(seed=12)
+    for k in ("keyframe_index", "landmark_index", "rig_camera", "observations", "poses", "landmarks"):
+        np.testing.assert_array_equal(getattr(a, k), getattr(b, k))
+    assert a.num_keyframes == 7 and set(np.unique(a.rig_camera)) <= {0, 1}
+    assert np.all(np.bincount(a.landmark_index, minlength=a.num_landmarks) >= 2)
+    # the truth projects every edge in front of its camera and inside the image
+    uv, depth = ta.project()
+    ideal = uv.copy()
+    assert np.all(depth > 1.0) and np.all((ideal[:, 0] > 0) & (ideal[:, 0] < 1241) & (ideal[:, 1] > 0) & (ideal[:, 1] < 376))
+    # the first keyframe is not perturbed (the others are)
+    np.testing.assert_array_equal(a.poses[:6], ta.poses[:6])
+    assert not np.array_equal(a.poses[6:], ta.poses[6:])
