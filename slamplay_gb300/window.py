@@ -45,6 +45,17 @@ class LocalBAWindow:
         self.landmarks = np.array(landmarks, dtype=np.float64).reshape(-1)
         self.fx, self.fy, self.cx, self.cy = float(fx), float(fy), float(cx), float(cy)
         self.extrinsics = np.array(extrinsics, dtype=np.float64).reshape(2, 6)
+        no = self.keyframe_index.size
+        if self.landmark_index.size != no or self.rig_camera.size != no or self.observations.size != 2 * no:
+            raise ValueError("keyframe_index, landmark_index, rig_camera and observations must describe the same "
+                             "observations (observations: 2 per observation)")
+        if self.poses.size % 6 or self.landmarks.size % 3:
+            raise ValueError("poses are 6 numbers per keyframe, landmarks 3 per landmark")
+        if no and (self.keyframe_index.min() < 0 or self.keyframe_index.max() >= self.num_keyframes or
+                   self.landmark_index.min() < 0 or self.landmark_index.max() >= self.num_landmarks):
+            raise ValueError("keyframe or landmark index out of range")
+        if no and self.rig_camera.max() > 1:
+            raise ValueError("rig_camera must be 0 (left) or 1 (right)")
 
     @property
     def num_keyframes(self) -> int:

@@ -220,3 +220,23 @@ def test_synthetic_window_is_deterministic_and_in_spec():
     # the first keyframe is not perturbed (the others are)
     np.testing.assert_array_equal(a.poses[:6], ta.poses[:6])
     assert not np.array_equal(a.poses[6:], ta.poses[6:])
+
+
+def test_window_rejects_inconsistent_arrays():
+    w = LocalBAWindow.synthetic(seed=1, num_landmarks=60)
+    args = [w.keyframe_index, w.landmark_index, w.rig_camera, w.observations, w.poses, w.landmarks,
+            w.fx, w.fy, w.cx, w.cy, w.extrinsics]
+    LocalBAWindow(*args)  # consistent
+    bad = list(args)
+    bad[2] = np.full_like(w.rig_camera, 2)
+    with pytest.raises(ValueError):
+        LocalBAWindow(*bad)
+    bad = list(args)
+    bad[0] = w.keyframe_index.copy()
+    bad[0][0] = w.num_keyframes
+    with pytest.raises(ValueError):
+        LocalBAWindow(*bad)
+    bad = list(args)
+    bad[3] = w.observations[:-2]
+    with pytest.raises(ValueError):
+        LocalBAWindow(*bad)
