@@ -3,19 +3,27 @@
 Workload (default): benchmark configuration 1 — one synthetic BAL problem,
 250 cameras on a random walk, 60,000 points, ~296k observations, 50 LM
 iterations (tolerances off so all 50 run), PCG capped at 100 iterations
-(residual criterion 1e-6).  A step is one full solve.  `value` = LM
-iterations/s of the mixed-precision form with the problem resident in HBM
-(re-solved from its initial point on the device, L2 flushed between steps);
-`forms` also reports the plain FP64 form; `e2e` = the same metric through the
-public C ABI call (gba_solve) with host buffers, host prep and transfers
-inside the timed region.
+(residual criterion 1e-6).  A step is one full solve.  The headline `value`
+is the plain FP64 form (the reference's arithmetic) with the problem
+resident in HBM (re-solved from its initial point on the device, L2 flushed
+between steps); `e2e` is the same metric through the public C ABI call
+(gba_solve) with host buffers: host prep, the host->device copy of the
+problem, the solve and the device->host copy of the parameters inside the
+timed region.  `forms.mixed` is the FP32/FP64 mixed form on the same
+problem, with its accuracy against the FP64 CPU oracle.
 
 Beside them (rank 0, one GPU): `forms.large` (configuration 2), `batched`
-(configuration 3), `serving` (configuration 4) and `local_ba` (full_slam's
-local-BA windows, the g2o policy; `--local-ba-only` prints that form alone).
+(configuration 3), `serving` (configuration 4), `g2o_variant` and
+`local_ba` (full_slam's local-BA windows; `--local-ba-only` prints that form
+alone).  The full per-kernel tables go to a detail line printed before the
+headline line.
 
 --impl reference times the CPU oracle (the C restatement of the reference's
-Ceres path: exact Schur + dense Cholesky) on this host's cores instead.
+Ceres path: LM + exact Schur complement + Cholesky of the reduced camera
+matrix) on this host's cores: each step is one full 50-iteration solve of
+the same problem on all cores, generated by the oracle's own generator
+(the product library is never loaded on that arm); one more solve on a
+single thread (Ceres' default num_threads) is reported beside it.
 
 Multi-GPU (torchrun, N>1): replicas only — each rank solves its own copy of
 the workload (weak scaling); value = all ranks' LM iterations / max time.
@@ -36,24 +44,28 @@ sys.path.insert(0, ROOT)
 
 METRIC = "LM iters/s and solves/s per GB300 (mixed vs plain FP64 GPU); p50/p99 latency"
 UNIT = "LM iter/s"
+LM_ITERATIONS = 50
 
 
 def workload_options(precision: str) -> dict:
-    return dict(max_num_iterations=50, function_tolerance=0.0, gradient_tolerance=0.0, parameter_tolerance=0.0,
-                max_linear_solver_iterations=100, pcg_tolerance=1e-6, precision=precision, loss="trivial")
+    return dict(max_num_iterations=LM_ITERATIONS, function_tolerance=0.0, gradient_tolerance=0.0,
+                parameter_tolerance=0.0, max_linear_solver_iterations=100, pcg_tolerance=1e-6, precision=precision,
+                loss="trivial")
 
 
-def config_dict(problem, extra=None) -> dict:
-    d = {"workload": "config1: synthetic BAL, 250 cams random walk, 60k points, "
-                     f"{problem.num_observations()} obs, 50 LM iters, PCG<=100",
-         "num_cameras": problem.num_cameras(), "num_points": problem.num_points(),
-         "num_observations": problem.num_observations(), "lm_iterations": 50, "pcg_cap": 100,
-         "pcg": "residual criterion 1e-6, at most 100 iterations per LM step",
-         "l2": "flushed between steps (256 MiB write on the solver stream, outside the timed events)",
-         "parallelism": "replicas"}
-    if extra:
-        d.update(extra)
-    return d
+def config_dict(nc: int, np_: int, no: int) -> dict:
+    return {"workload": f"config1: synthetic BAL, 250 cams random walk, 60k points, {no} obs, 50 LM iters, PCG<=100",
+            "num_cameras": nc, "num_points": np_, "num_observations": no, "lm_iterations": LM_ITERATIONS,
+            "pcg_cap": 100, "pcg": "residual criterion 1e-6, at most 100 iterations per LM step",
+            "l2": "flushed between steps (256 MiB write on the solver stream, outside the timed events)",
+            "parallelism": "replicas"}
+
+
+def host_cores() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
 
 
 class ClockSampler:
@@ -116,45 +128,76 @@ def measured_peaks() -> dict:
     return {"hbm_gbs": 6800.0, "fallback": True}
 
 
-def cpu_baseline(seconds_budget: float = 20.0) -> dict:
-    """The oracle (C restatement of the reference path, exact Schur + dense
-    Cholesky, OpenMP on all host cores) on a bounded sample of the workload:
-    the first LM iterations of the same problem."""
+def oracle_solve(threads: int = 0, iterations: int = LM_ITERATIONS) -> dict:
+    """One solve of the configuration 1 problem by the CPU oracle (the C
+    restatement of the reference's Ceres SPARSE_SCHUR path: LM, points
+    eliminated, Cholesky of the reduced camera matrix in its envelope), on
+    `threads` host threads (0 = all).  The problem comes from the oracle's
+    own generator, bitwise the product's."""
     from oracle import oracle_py as O
-    from slamplay_gb300 import BALProblem
 
-    b = BALProblem.synthetic(1, seed=0)
-    iters = 2
+    p = O.Problem.synthetic(1, seed=0)
     t0 = time.perf_counter()
-    res = O.solve(O.Problem.from_bal(b), max_num_iterations=iters, function_tolerance=0.0, gradient_tolerance=0.0,
-                  parameter_tolerance=0.0, linear_solver="dense_schur")
-    dt = time.perf_counter() - t0
-    cores = os.cpu_count() or 1
-    return {"value": res["num_iterations"] / dt, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"config1 problem, first {res['num_iterations']} LM iterations (+ initial evaluation), "
-                      f"oracle dense-Schur LM, {dt:.1f} s"}
+    res = O.solve(p, max_num_iterations=iterations, function_tolerance=0.0, gradient_tolerance=0.0,
+                  parameter_tolerance=0.0, linear_solver="dense_schur", num_threads=threads)
+    res["seconds"] = time.perf_counter() - t0
+    res["threads"] = threads if threads > 0 else host_cores()
+    res["sizes"] = (p.num_cameras(), p.num_points(), p.num_observations())
+    return res
+
+
+def cpu_baseline() -> tuple[dict, dict]:
+    """The oracle on all host cores, one full 50-iteration solve of the same
+    problem (a few seconds of CPU work)."""
+    r = oracle_solve()
+    cb = {"value": r["num_iterations"] / r["seconds"], "unit": UNIT, "cores": r["threads"], "kind": "port",
+          "sample": f"one full {r['num_iterations']}-iteration solve of the config1 problem (oracle LM, exact Schur "
+                    f"complement, envelope Cholesky), {r['seconds']:.2f} s on {r['threads']} threads"}
+    return cb, r
+
+
+def accuracy_vs(oracle_res: dict, params, final_cost: float, nc: int, no: int) -> dict:
+    """Final cost, RMS reprojection error and parameter RMS differences of a
+    GPU result against the oracle's result on the same problem."""
+    import numpy as np
+
+    po = oracle_res["parameters"]
+    pg = np.asarray(params, dtype=np.float64).reshape(-1)
+    co = oracle_res["final_cost"]
+    return {"final_cost": final_cost, "oracle_final_cost": co, "final_cost_rel": abs(final_cost - co) / co,
+            "rms_reprojection_px": (2.0 * final_cost / no) ** 0.5, "oracle_rms_reprojection_px": (2.0 * co / no) ** 0.5,
+            "camera_rms_diff": float(np.sqrt(np.mean((pg[:9 * nc] - po[:9 * nc]) ** 2))),
+            "point_rms_diff": float(np.sqrt(np.mean((pg[9 * nc:] - po[9 * nc:]) ** 2)))}
 
 
 def run_reference(args) -> None:
+    """The CPU oracle on this host's cores, on the GPU arm's config, metric
+    and unit.  Rank 0 only; the product library is not loaded."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     for _ in range(args.warmup):
-        pass  # the CPU oracle has no warm-up state worth timing
-    vals = []
-    for _ in range(args.steps):
-        cb = cpu_baseline()
-        vals.append(cb["value"])
-    v = statistics.median(vals)
-    from slamplay_gb300 import BALProblem
-
-    b = BALProblem.synthetic(1, seed=0)
+        oracle_solve(iterations=1)  # thread pool, page faults
+    runs = [oracle_solve() for _ in range(args.steps)]
+    secs = [r["seconds"] for r in runs]
+    its = runs[0]["num_iterations"]
+    ms = 1e3 * statistics.median(secs)
+    v = its / (ms * 1e-3)
+    one = oracle_solve(threads=1)
+    nc, np_, no = runs[0]["sizes"]
     line = {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * 2 / v if v else None,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": config_dict(b, {"reference": "CPU oracle port (Ceres' path restated: LM + exact Schur + "
-                                                   "dense Cholesky); the Ceres build is unavailable here"}),
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cb["cores"], "kind": "port", "sample": cb["sample"]},
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config_dict(nc, np_, no),
+            "reference_impl": "CPU oracle port of the reference's Ceres path (LM + exact Schur complement + "
+                              "Cholesky of the reduced camera matrix); Ceres itself is not in the reference tree",
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": runs[0]["threads"], "kind": "port",
+                             "sample": f"each step one full {its}-iteration solve of the config1 problem on "
+                                       f"{runs[0]['threads']} threads"},
+            "cpu_1thread": {"value": one["num_iterations"] / one["seconds"], "unit": UNIT, "cores": 1,
+                            "seconds_per_solve": one["seconds"],
+                            "sample": "one full solve on one thread (Ceres' default num_threads)"},
+            "final_cost": runs[0]["final_cost"],
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -205,23 +248,33 @@ def measure_fp64_peak(torch) -> dict:
     return {"tflops": 2.0 * n ** 3 / s / 1e12, "source": "cuBLAS DGEMM 8192^3 (torch.matmul float64), CUDA events"}
 
 
-def fp64_formation_roofline(problem, prof, peak: dict):
-    """The FP64 form's formation kernel (K3c) against the FP64 roof: 243 FMAs
-    (486 flops) per observation pair on or above the diagonal (sum over
-    points of m (m - 1) / 2 for a problem without repeated observations)."""
+def fp64_rooflines(problem, prof, peak: dict) -> dict:
+    """The FP64 form's kernels against the FP64 roof (the measured DGEMM
+    rate), for the kernels whose FP64 work is counted: the formation of the
+    explicit Schur complement (243 FMAs = 486 flops per observation pair on or
+    above the diagonal: sum over points of m (m - 1) / 2 pairs for m views)."""
     import numpy as np
 
-    e = next((x for x in prof if x["name"] == "schur_form" and x["launches"] > 0), None)
-    if e is None:
-        return None
-    m = np.bincount(problem.point_index_).astype(np.int64)
+    out = {"peak": peak["tflops"], "unit": "TFLOP/s", "peak_source": peak["source"]}
+    m = np.bincount(problem.point_index()).astype(np.int64)
     pairs = int((m * (m - 1) // 2).sum())
-    avg_s = e["total_ms"] / e["launches"] * 1e-3
-    ach = 486.0 * pairs / avg_s / 1e12
-    return {"kernel": "schur_form", "bound": "fp64", "achieved": ach, "peak": peak["tflops"], "unit": "TFLOP/s",
-            "frac": ach / peak["tflops"], "flops_per_launch": 486.0 * pairs, "avg_launch_ms": avg_s * 1e3,
-            "peak_source": peak["source"],
-            "note": "the FP64 form's FP64-bound kernel; its HBM traffic is the mixed form's figure x2 (<5% of HBM)"}
+    for e in prof:
+        if e["name"] == "schur_form":
+            avg_s = e["total_ms"] / e["launches"] * 1e-3
+            ach = 486.0 * pairs / avg_s / 1e12
+            out["schur_form"] = {"achieved": ach, "frac": ach / peak["tflops"], "flops_per_launch": 486.0 * pairs,
+                                 "avg_launch_ms": avg_s * 1e3}
+    return out
+
+
+def kernel_table(prof: list[dict]) -> list[dict]:
+    out = []
+    for e in prof:
+        avg_us = 1e3 * e["total_ms"] / e["launches"]
+        out.append({"name": e["name"], "launches": e["launches"], "total_ms": e["total_ms"], "avg_us": avg_us,
+                    "bytes_per_launch": e["bytes"] / e["launches"],
+                    "gbs": e["bytes"] / e["launches"] / (avg_us * 1e-6) / 1e9 if avg_us > 0 else None})
+    return out
 
 
 def run_gpu(args) -> None:
@@ -239,14 +292,14 @@ def run_gpu(args) -> None:
     from slamplay_gb300 import BALProblem, Solver
 
     problem = BALProblem.synthetic(1, seed=0)
+    nc, np_, no = problem.num_cameras(), problem.num_points(), problem.num_observations()
     stream = torch.cuda.Stream()
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
     def timed_form(precision: str):
         s = Solver(device=local, stream=stream.cuda_stream, **workload_options(precision))
         p0 = problem.copy()
-        first = s.solve(p0)  # uploads the problem, builds the graph
-        iters = first.num_iterations
+        first = s.solve(p0)  # uploads the problem, builds the graph; p0 holds the result
         for _ in range(args.warmup):
             s.solve_resident(1)
         s.synchronize()
@@ -261,7 +314,19 @@ def run_gpu(args) -> None:
             e1.record(stream)
             e1.synchronize()
             times.append(e0.elapsed_time(e1))
-        return s, first, iters, times
+        return s, first, p0, times
+
+    def e2e_form(s) -> tuple[float, object]:
+        # through gba_solve: host arrays in, host prep + H2D + solve + D2H
+        ts = []
+        su = None
+        for _ in range(args.steps):
+            p = problem.copy()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            su = s.solve(p)
+            ts.append(time.perf_counter() - t0)
+        return statistics.median(ts), su
 
     if dist:
         dist.barrier()
@@ -269,52 +334,38 @@ def run_gpu(args) -> None:
     clocks = ClockSampler(local)
     clocks.start()
     t_wall0 = time.perf_counter()
-    sm, first_m, iters_m, times_m = timed_form("mixed")
+    sp, first_p, res_p, times_p = timed_form("fp64")
     t_wall1 = time.perf_counter()
     clk = clocks.stop()
     torch.cuda.synchronize()
-    sp, first_p, iters_p, times_p = timed_form("fp64")
-    ms_m = sum(times_m) / len(times_m)
     ms_p = sum(times_p) / len(times_p)
+    e2e_s, su_p = e2e_form(sp)
+    sm, first_m, res_m, times_m = timed_form("mixed")
+    ms_m = sum(times_m) / len(times_m)
+    e2e_m, _ = e2e_form(sm)
     if dist:
-        t = torch.tensor([ms_m, ms_p], device="cuda")
+        t = torch.tensor([ms_p, ms_m, e2e_s], device="cuda", dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_m, ms_p = t.tolist()
-    value = world * iters_m / (ms_m * 1e-3)
-    value_p = world * iters_p / (ms_p * 1e-3)
-
-    # e2e through gba_solve: host arrays in, host prep + H2D + solve + D2H
-    e2e_times = []
-    h2d = d2h = 0
-    for _ in range(max(1, min(args.steps, 5))):
-        p = problem.copy()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        su = sm.solve(p)
-        e2e_times.append(time.perf_counter() - t0)
-    no, nc, np_ = problem.num_observations(), problem.num_cameras(), problem.num_points()
+        ms_p, ms_m, e2e_s = t.tolist()
+    iters_p, iters_m = first_p.num_iterations, first_m.num_iterations
+    value = world * iters_p / (ms_p * 1e-3)
+    value_m = world * iters_m / (ms_m * 1e-3)
     h2d = 24 * no + 8 * (9 * nc + 3 * np_)
     d2h = 8 * (9 * nc + 3 * np_)
-    e2e_s = statistics.median(e2e_times)
-    e2e_val = world * su.num_iterations / e2e_s
+    e2e_val = world * su_p.num_iterations / e2e_s
 
     # per-kernel device times (host-driven pass with CUDA events per launch)
-    sm.set_profiling(True)
-    sm.solve(problem.copy())
-    sm.set_profiling(False)
-    prof = [e for e in sm.profile() if e["launches"] > 0]
-    # the FP64 form: its kernels, and the formation against the FP64 roof
-    sp.set_profiling(True)
-    sp.solve(problem.copy())
-    sp.set_profiling(False)
-    prof_p = [e for e in sp.profile() if e["launches"] > 0]
-    roof_fp64 = fp64_formation_roofline(problem, prof_p, measure_fp64_peak(torch)) if rank == 0 else None
+    def profile(s):
+        s.set_profiling(True)
+        s.solve(problem.copy())
+        s.set_profiling(False)
+        return [e for e in s.profile() if e["launches"] > 0]
+
+    prof_p, prof_m = profile(sp), profile(sm)
     peaks = measured_peaks()
     peak = peaks.get("hbm_gbs", 6800.0)
-    for e in prof:
-        e["avg_us"] = 1e3 * e["total_ms"] / e["launches"]
-        e["gbs"] = e["bytes"] / e["launches"] / (e["avg_us"] * 1e-6) / 1e9 if e["avg_us"] > 0 else None
-    top = max(prof, key=lambda e: e["total_ms"]) if prof else None
+    fp64_peak = measure_fp64_peak(torch) if rank == 0 else None
+    top = max(prof_p, key=lambda e: e["total_ms"]) if prof_p else None
     roof = None
     if top:
         avg_ms = top["total_ms"] / top["launches"]
@@ -327,14 +378,11 @@ def run_gpu(args) -> None:
                           "solve (kernels inside the conditional graph cannot be bracketed one by one)",
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if not peaks.get("fallback")
                 else "fallback 6.8 TB/s (of fallback)"}
-        if top["name"] == "pcg_cluster" and first_m.num_iterations > 0:
-            per_it = 1e3 * avg_ms / max(1.0, first_m.num_linear_solver_iterations / first_m.num_iterations)
-            roof["per_pcg_iteration_us"] = per_it
-            roof["note"] = ("the whole PCG of an LM iteration in one launch: its algorithmic bytes (S, M^-1 and the "
-                            "PCG vectors, once) are small, and its time is the latency of ~2 cluster barriers and "
-                            "2 exchanges per PCG iteration (per_pcg_iteration_us), not HBM bandwidth")
+    roof_fp64 = fp64_rooflines(problem, prof_p, fp64_peak) if fp64_peak else None
     if rank == 0:
-        cb = cpu_baseline() if world == 1 else None
+        cb, orc = cpu_baseline() if world == 1 else (None, None)
+        acc_p = accuracy_vs(orc, res_p.parameters(), first_p.final_cost, nc, no) if orc else None
+        acc_m = accuracy_vs(orc, res_m.parameters(), first_m.final_cost, nc, no) if orc else None
         extra_forms = {}
         if world == 1 and not args.no_extra_forms:
             for name, form in (("large", large_form), ("batched", batched_form), ("serving", serving_form),
@@ -343,33 +391,32 @@ def run_gpu(args) -> None:
                     extra_forms[name] = form()
                 except Exception as e:  # a side form never takes the headline line down
                     extra_forms[name] = {"error": repr(e)}
+        forms = {
+            "fp64": {"lm_iters_per_s": value, "solves_per_s": world * 1e3 / ms_p, "ms_per_solve": ms_p,
+                     "lm_iterations": iters_p, "pcg_iterations": first_p.num_linear_solver_iterations,
+                     "vs_oracle": acc_p},
+            "mixed": {"lm_iters_per_s": value_m, "solves_per_s": world * 1e3 / ms_m, "ms_per_solve": ms_m,
+                      "lm_iterations": iters_m, "pcg_iterations": first_m.num_linear_solver_iterations,
+                      "e2e_lm_iters_per_s": world * iters_m / e2e_m, "vs_oracle": acc_m,
+                      "final_cost_rel_vs_fp64_gpu": abs(first_m.final_cost - first_p.final_cost) / first_p.final_cost,
+                      "vs_fp64": value_m / value},
+        }
+        detail = {"detail": "bench", "kernels_fp64": kernel_table(prof_p), "kernels_mixed": kernel_table(prof_m),
+                  "forms": {**forms, **extra_forms}}
+        print(json.dumps(detail), flush=True)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms_m, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32+f64 (mixed)", "data": "synthetic",
-            "config": config_dict(problem),
-            "forms": {
-                "mixed": {"lm_iters_per_s": value, "solves_per_s": world * 1e3 / ms_m, "ms_per_solve": ms_m,
-                          "lm_iterations": iters_m, "pcg_iterations": first_m.num_linear_solver_iterations,
-                          "final_cost": first_m.final_cost},
-                "fp64": {"lm_iters_per_s": value_p, "solves_per_s": world * 1e3 / ms_p, "ms_per_solve": ms_p,
-                         "lm_iterations": iters_p, "pcg_iterations": first_p.num_linear_solver_iterations,
-                         "final_cost": first_p.final_cost, "roofline_fp64": roof_fp64,
-                         "kernels": [{"name": e["name"], "launches": e["launches"],
-                                      "avg_us": 1e3 * e["total_ms"] / e["launches"]} for e in prof_p]},
-                "mixed_vs_fp64_final_cost_rel": abs(first_m.final_cost - first_p.final_cost) / first_p.final_cost,
-                **extra_forms,
-            },
+            "warmup": args.warmup, "ms_per_step": ms_p, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config_dict(nc, np_, no),
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": 1e3 * e2e_s},
             "roofline": roof,
-            "kernels": prof,
+            "roofline_fp64": roof_fp64,
             "cpu_baseline": cb,
-            "gpu_launches": args.steps * launches_per_solve(first_m, {e["name"]: e["launches"] for e in prof}),
-            "linear_solver": {"schur": "explicit" if any(e["name"] == "schur_form" for e in prof) else "implicit",
-                              "pcg": "cluster (one launch per LM iteration)"
-                              if any(e["name"] == "pcg_cluster" for e in prof) else "two kernels per PCG iteration"},
+            "gpu_launches": args.steps * launches_per_solve(first_p, {e["name"]: e["launches"] for e in prof_p}),
             "clocks": clk,
+            "forms": {**forms, **{k: compact_form(k, v) for k, v in extra_forms.items()}},
+            "linear_solver": linear_solver_name(prof_p),
             "wall_s_timed": t_wall1 - t_wall0,
         }
         print(json.dumps(line), flush=True)
@@ -378,6 +425,44 @@ def run_gpu(args) -> None:
     if dist:
         dist.barrier()
         dist.destroy_process_group()
+
+
+def linear_solver_name(prof: list[dict]) -> dict:
+    names = {e["name"] for e in prof}
+    pcg = "two kernels per PCG iteration"
+    if "pcg_cluster" in names:
+        pcg = "cluster (one launch per LM iteration)"
+    elif "pcg_grid" in names:
+        pcg = "grid (one launch per LM iteration)"
+    return {"schur": "explicit" if "schur_form" in names else "implicit", "pcg": pcg}
+
+
+def compact_form(name: str, f: dict) -> dict:
+    """The side forms' headline figures, for the final JSON line."""
+    if "error" in f:
+        return f
+    try:
+        if name == "large":
+            return {k: {"lm_iters_per_s": f[k]["lm_iters_per_s"], "pcg_iterations": f[k]["pcg_iterations"]}
+                    for k in ("mixed", "fp64")} | {"mixed_vs_fp64_final_cost_rel": f.get("mixed_vs_fp64_final_cost_rel")}
+        if name == "batched":
+            return {"mixed_solves_per_s": f["mixed"]["solves_per_s"], "fp64_solves_per_s": f["fp64"]["solves_per_s"],
+                    "sequential_fp64_solves_per_s": f["sequential_fp64"]["solves_per_s"],
+                    "mixed_vs_fp64_final_cost_rel": f["mixed_vs_fp64_final_cost_rel"]}
+        if name == "serving":
+            return {"sweep": [{k: x[k] for k in ("arrival_rate_per_s", "solves_per_s", "p50_ms", "p99_ms")}
+                              for x in f["sweep"]], "requests_per_rate": f.get("requests_per_rate"),
+                    "sequential_fp64_solves_per_s": f["sequential_fp64_solves_per_s"]}
+        if name == "g2o_variant":
+            return {k: {"solves_per_s": f[k]["solves_per_s"], "final_cost": f[k]["final_cost"]}
+                    for k in ("mixed", "fp64")} | {"mixed_vs_fp64_final_cost_rel": f["mixed_vs_fp64_final_cost_rel"]}
+        if name == "local_ba":
+            return {k: {"windows_per_s": f[k]["windows_per_s"], "e2e_windows_per_s": f[k]["e2e_windows_per_s"],
+                        "final_cost_rel_vs_oracle_max": f[k]["final_cost_rel_vs_oracle_max"]}
+                    for k in ("mixed", "fp64")} | {"cpu_oracle_windows_per_s": f["cpu_oracle"]["windows_per_s"]}
+    except (KeyError, TypeError) as e:
+        return {"error": f"summary: {e!r}"}
+    return f
 
 
 PCG_SMALL = dict(pcg_criterion="residual", pcg_tolerance=1e-6, max_linear_solver_iterations=100)
@@ -663,6 +748,13 @@ def main():
     ap.add_argument("--local-ba-only", action="store_true",
                     help="print only the local-BA form (full_slam's windows) as one JSON line")
     args = ap.parse_args()
+    if args.impl == "reference":
+        # the CPU oracle alone: the product library is neither built nor loaded
+        from oracle import oracle_py
+
+        oracle_py.ensure_built()
+        run_reference(args)
+        return
     from slamplay_gb300 import build as B
 
     B.build()
@@ -670,11 +762,6 @@ def main():
         print(json.dumps({"form": "local_ba", **local_ba_form()}), flush=True)
     elif args.profile_solve:
         run_profile_solve(args)
-    elif args.impl == "reference":
-        from oracle import oracle_py
-
-        oracle_py.ensure_built()
-        run_reference(args)
     else:
         run_gpu(args)
 

@@ -14,7 +14,7 @@ CFLAGS="-O2 -fPIC -ffp-contract=off -fopenmp"
 
 if [[ "$WHAT" == "oracle" || "$WHAT" == "all" ]]; then
   mkdir -p "$HERE/_build"
-  gcc -std=c11 $CFLAGS -shared "$HERE/oracle.c" -o "$HERE/_build/liboracle.so.tmp" -lm
+  gcc -std=c11 $CFLAGS -shared "$HERE/oracle.c" "$HERE/synth.c" -o "$HERE/_build/liboracle.so.tmp" -lm
   mv -f "$HERE/_build/liboracle.so.tmp" "$HERE/_build/liboracle.so"
 fi
 

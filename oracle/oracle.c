@@ -732,8 +732,30 @@ static int spd_inverse(const double *A, double *Ainv, int n) {
 }
 
 /* Lower Cholesky of a dense row-major n x n matrix in place (blocked,
- * right-looking).  Returns 0 when not positive definite. */
-static int chol_dense(double *A, int n) {
+ * right-looking), restricted to the matrix's envelope: first[i] is the first
+ * non-zero column of row i of the lower triangle, and every entry left of it
+ * stays zero through the factorisation (no fill outside the envelope).  The
+ * work skipped is exactly the terms that are products with those zeros, in
+ * an unchanged order for the rest, so the factor is bitwise the one of the
+ * plain dense loops; a banded reduced camera matrix (a trajectory's cameras
+ * see points with their neighbours) costs about n bw^2 / 2 instead of n^3 / 6.
+ * This is the role the sparse Cholesky plays in SPARSE_SCHUR.  Returns 0 when
+ * not positive definite. */
+static void envelope(const double *A, int n, int *first) {
+#pragma omp parallel for schedule(static)
+  for (int i = 0; i < n; ++i) {
+    const double *Ai = A + (size_t)i * n;
+    int f = i;
+    for (int k = 0; k < i; ++k)
+      if (Ai[k] != 0.0) {
+        f = k;
+        break;
+      }
+    first[i] = f;
+  }
+}
+
+static int chol_dense(double *A, int n, const int *first) {
   const int NB = 48;
   for (int k0 = 0; k0 < n; k0 += NB) {
     const int k1 = (k0 + NB < n) ? k0 + NB : n;
@@ -750,16 +772,20 @@ static int chol_dense(double *A, int n) {
       }
     }
 #pragma omp parallel for schedule(static)
-    for (int i = k1; i < n; ++i)
+    for (int i = k1; i < n; ++i) {
+      if (first[i] >= k1) continue; /* row i is zero in columns k0..k1-1 */
       for (int j = k0; j < k1; ++j) {
         double t = A[(size_t)i * n + j];
         for (int k = k0; k < j; ++k) t -= A[(size_t)i * n + k] * A[(size_t)j * n + k];
         A[(size_t)i * n + j] = t / A[(size_t)j * n + j];
       }
+    }
 #pragma omp parallel for schedule(dynamic, 4)
     for (int i = k1; i < n; ++i) {
+      if (first[i] >= k1) continue;
       const double *Li = A + (size_t)i * n;
       for (int j = k1; j <= i; ++j) {
+        if (first[j] >= k1) continue;
         const double *Lj = A + (size_t)j * n;
         double t = 0.0;
         for (int k = k0; k < k1; ++k) t += Li[k] * Lj[k];
@@ -770,16 +796,17 @@ static int chol_dense(double *A, int n) {
   return 1;
 }
 
-static void chol_solve(const double *L, int n, double *b) {
+static void chol_solve(const double *L, int n, const int *first, double *b) {
   for (int i = 0; i < n; ++i) {
     double t = b[i];
     const double *Li = L + (size_t)i * n;
-    for (int k = 0; k < i; ++k) t -= Li[k] * b[k];
+    for (int k = first[i]; k < i; ++k) t -= Li[k] * b[k];
     b[i] = t / Li[i];
   }
   for (int i = n - 1; i >= 0; --i) {
     double t = b[i];
-    for (int k = i + 1; k < n; ++k) t -= L[(size_t)k * n + i] * b[k];
+    for (int k = i + 1; k < n; ++k)
+      if (first[k] <= i) t -= L[(size_t)k * n + i] * b[k];
     b[i] = t / L[(size_t)i * n + i];
   }
 }
@@ -927,11 +954,18 @@ static int solve_dense_schur(const lsys *L, double *y) {
   }
   double *v = y; /* camera part of y first holds the rhs */
   reduced_rhs(L, v);
-  const int ok = chol_dense(S, m);
+  int *first = (int *)malloc((size_t)m * sizeof(int));
+  if (!first) {
+    free(S);
+    return 0;
+  }
+  envelope(S, m, first);
+  const int ok = chol_dense(S, m, first);
   if (ok) {
-    chol_solve(S, m, v);
+    chol_solve(S, m, first, v);
     back_substitute(L, v, y + m);
   }
+  free(first);
   free(S);
   return ok;
 }

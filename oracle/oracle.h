@@ -143,6 +143,14 @@ int orc_compute_step(const orc_problem *p, const orc_options *o, double radius, 
 /* Full solve; p->parameters updated in place.  Returns 0 on success. */
 int orc_solve(const orc_problem *p, const orc_options *o, orc_summary *s);
 
+/* The benchmark configurations' seeded synthetic problems (synth.c): sizes,
+ * then the arrays (caller-allocated; parameters = the perturbed initial
+ * guess).  config 0-4, `index` selects a window (3) or a request (4).
+ * Return 0 on an unknown configuration, a size mismatch or no memory. */
+int orc_synth_size(int config, int index, uint64_t seed, int *nc, int *np, int *no);
+int orc_synth_generate(int config, int index, uint64_t seed, int nc, int np, int no, int *camera_index,
+                       int *point_index, double *observations, double *parameters);
+
 #ifdef __cplusplus
 }
 #endif

@@ -66,8 +66,17 @@ _orc = None
 _ref = None
 
 
+def _stale(lib: str, sources: list[str]) -> bool:
+    if not os.path.exists(lib):
+        return True
+    t = os.path.getmtime(lib)
+    return any(os.path.getmtime(os.path.join(HERE, f)) > t for f in sources if os.path.exists(os.path.join(HERE, f)))
+
+
 def ensure_built(reference: bool = False) -> None:
-    if not os.path.exists(ORACLE_LIB) or (reference and not os.path.exists(REF_LIB)):
+    """Builds the oracle (and with `reference` the reference-built checker)
+    when missing or older than its sources."""
+    if _stale(ORACLE_LIB, ["oracle.c", "synth.c", "oracle.h"]) or (reference and not os.path.exists(REF_LIB)):
         import subprocess
         subprocess.run(["bash", os.path.join(HERE, "build_ref.sh"), "all" if reference else "oracle"], check=True)
 
@@ -99,6 +108,11 @@ def oracle():
         L.orc_compute_step.restype = C.c_int
         L.orc_solve.argtypes = [C.POINTER(OrcProblem), C.POINTER(OrcOptions), C.POINTER(OrcSummary)]
         L.orc_solve.restype = C.c_int
+        L.orc_synth_size.argtypes = [C.c_int, C.c_int, C.c_uint64, _i32p, _i32p, _i32p]
+        L.orc_synth_size.restype = C.c_int
+        L.orc_synth_generate.argtypes = [C.c_int, C.c_int, C.c_uint64, C.c_int, C.c_int, C.c_int, _i32p, _i32p,
+                                         _f64p, _f64p]
+        L.orc_synth_generate.restype = C.c_int
         _orc = L
     return _orc
 
@@ -170,6 +184,35 @@ class Problem:
     def from_bal(cls, b):
         return cls(b.num_cameras(), b.num_points(), b.camera_index(), b.point_index(), b.observations(),
                    b.parameters())
+
+    @classmethod
+    def synthetic(cls, config: int, index: int = 0, seed: int = 0) -> "Problem":
+        """Benchmark configuration `config`'s seeded problem, generated by the
+        oracle's own generator (synth.c; the same bytes as the product's
+        gba_synth_generate)."""
+        L = oracle()
+        nc, np_, no = C.c_int(), C.c_int(), C.c_int()
+        if not L.orc_synth_size(config, index, seed, C.byref(nc), C.byref(np_), C.byref(no)):
+            raise ValueError(f"oracle synth: bad configuration {config}")
+        cam = np.zeros(no.value, np.int32)
+        pt = np.zeros(no.value, np.int32)
+        obs = np.zeros(2 * no.value)
+        par = np.zeros(9 * nc.value + 3 * np_.value)
+        if not L.orc_synth_generate(config, index, seed, nc, np_, no, i32(cam), i32(pt), f64(obs), f64(par)):
+            raise RuntimeError("oracle synth: generation failed")
+        return cls(nc.value, np_.value, cam, pt, obs, par)
+
+    def copy(self) -> "Problem":
+        return Problem(self.s.nc, self.s.np, self.cam, self.pt, self.obs, self.params)
+
+    def num_cameras(self) -> int:
+        return self.s.nc
+
+    def num_points(self) -> int:
+        return self.s.np
+
+    def num_observations(self) -> int:
+        return self.s.no
 
 
 def evaluate(p: Problem, loss="trivial", loss_scale=1.0, camera_update="additive"):
