@@ -208,11 +208,11 @@ def launches_per_solve(s, prof_launches: dict) -> int:
     the gather = 10; per LM iteration point/Schur chunk, camera Schur, back-
     substitution, candidate cameras, candidate cost, decide, camera table,
     evaluation (chunk + camera), post-evaluation = 10, + 1 for the formation
-    of the explicit Schur complement; the PCG either as one cluster launch
-    per LM iteration or as two kernels per PCG iteration.  prof_launches:
+    of the explicit Schur complement; the PCG either as one launch per LM
+    iteration (cluster or grid form) or as two kernels per PCG iteration.  prof_launches:
     launches per profile entry of a host-driven pass of the same solve."""
     per_lm = 10 + (1 if prof_launches.get("schur_form") else 0)
-    pcg = prof_launches.get("pcg_cluster") or 2 * s.num_linear_solver_iterations
+    pcg = prof_launches.get("pcg_cluster") or prof_launches.get("pcg_grid") or 2 * s.num_linear_solver_iterations
     return 10 + per_lm * s.num_iterations + pcg
 
 

@@ -168,11 +168,13 @@ typedef struct gba_options {
   int32_t autotune;                   /* 1 = run gba_autotune on the first solve of a
                                          new problem-size bucket                     */
   int32_t schur;                      /* gba_schur, GBA_SCHUR_AUTO                   */
-  int32_t persistent_pcg;             /* 1 = with the mixed precision and the explicit
-                                         Schur complement, run each problem's whole PCG
-                                         in one launch (a thread-block cluster per
-                                         problem) when it fits; 0 = one launch pair per
-                                         PCG iteration                               */
+  int32_t persistent_pcg;             /* 1 = with the explicit Schur complement, run
+                                         the whole PCG of an LM iteration in one
+                                         launch where the form allows: the mixed
+                                         precision as a thread-block cluster per
+                                         problem, the FP64 form of a single problem
+                                         over the whole GPU (grid-wide barriers);
+                                         0 = one launch pair per PCG iteration      */
   int32_t camera_update;              /* gba_camera_update, GBA_CAMERA_UPDATE_ADDITIVE */
   int32_t lm_policy;                  /* gba_lm_policy, GBA_LM_POLICY_CERES          */
   int32_t reserved[2];

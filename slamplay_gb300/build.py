@@ -22,7 +22,7 @@ INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libgba.so")
 
-CUDA_SOURCES = ["k_eval.cu", "k_solve.cu", "k_pcg.cu", "k_schur.cu", "k_pcg_cluster.cu", "k_noalloc.cu"]
+CUDA_SOURCES = ["k_eval.cu", "k_solve.cu", "k_pcg.cu", "k_schur.cu", "k_pcg_cluster.cu", "k_pcg_grid.cu", "k_noalloc.cu"]
 CXX_SOURCES = ["engine.cpp", "prep.cpp", "api.cpp", "server.cpp", "bal_io.cpp", "synth.cpp", "tune.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

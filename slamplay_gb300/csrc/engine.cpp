@@ -47,12 +47,13 @@ enum ProfSlot {
   PF_SETUP_MISC,
   PF_FORM,
   PF_CLUSTER,
+  PF_GRID,
   PF_COUNT
 };
 const char *kProfNames[PF_COUNT] = {"eval_jacobian",  "post_eval", "point_schur",  "camera_schur",
                                     "schur_matvec",   "pcg_camera", "back_substitute", "candidate_cost",
                                     "decide",         "camera_table", "setup_misc", "schur_form",
-                                    "pcg_cluster"};
+                                    "pcg_cluster",    "pcg_grid"};
 
 double now_s() {
   return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
@@ -258,6 +259,8 @@ size_t Engine::layout(const HostBatch &hb, char *base, DeviceBatch *db, size_t *
   b.cam_Sii = cv.take<char>(ex ? 81 * nc * rs : 0);
   b.pcg_q = cv.take<double>(ex ? 9 * nc : 0);
   b.spmv_red = cv.take<double>(ex ? nc : 0);
+  b.pcg_p2 = cv.take<double>(ex ? 9 * nc : 0);
+  b.grid_ctl = cv.take<uint32_t>(8);
   b.prob_counter = cv.take<uint32_t>(4 * P);
   b.global_counter = cv.take<uint32_t>(8);
   b.chunk_counter = cv.take<uint32_t>(nch);
@@ -408,12 +411,20 @@ gba_status Engine::upload(const HostBatch &hb, std::string *err) {
   if (mixed_ && hb.explicit_schur && o_.persistent_pcg &&
       !pcg_cluster_plan(hb.prob.data(), (int)hb.prob.size(), hb.sblk_row.data(), &cl_plan_))
     cl_plan_ = ClusterPlan();
+  // the PCG as one grid-wide launch per LM iteration: FP64 form, explicit
+  // Schur complement, one problem
+  gr_plan_ = GridPlan();
+  if (o_.persistent_pcg && !pcg_grid_plan((int)hb.prob.size(), mixed_, hb.explicit_schur, hb.nc,
+                                          hb.explicit_schur ? hb.sblk_row.data() : nullptr, &gr_plan_))
+    gr_plan_ = GridPlan();
   // current batch shape + pointers + options + PCG form = graph key
   DeviceBatch k = db_;
   cur_key_.assign(reinterpret_cast<const char *>(&k), reinterpret_cast<const char *>(&k) + sizeof k);
   cur_key_.push_back(cl_plan_.cs);
   cur_key_.push_back(cl_plan_.threads);
   cur_key_.push_back(cl_plan_.cache_blocks);
+  cur_key_.push_back(gr_plan_.grid);
+  cur_key_.push_back(gr_plan_.cap_blocks);
   return GBA_OK;
 }
 
@@ -615,16 +626,20 @@ gba_status Engine::build_graph(std::string *err) {
   cudaGraph_t lmbody = nullptr, pcgbody = nullptr, tmp = nullptr;
   if ((e = add_while(stream_, lmh, &lmbody)) != cudaSuccess) return fail(e, "LM conditional node");
   // (a conditional handle must belong to a node: none for the cluster PCG)
-  if (cl_plan_.cs == 0 &&
+  const bool one_launch = cl_plan_.cs > 0 || gr_plan_.grid > 0;
+  if (!one_launch &&
       (e = cudaGraphConditionalHandleCreate(&pcgh, lmbody, 1, cudaGraphCondAssignDefault)) != cudaSuccess)
     return fail(e, "PCG conditional handle");
-  db_.pcg_cond = cl_plan_.cs > 0 ? 0 : pcgh;
+  db_.pcg_cond = one_launch ? 0 : pcgh;
   e = cudaStreamBeginCaptureToGraph(cap_[0], lmbody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) return fail(e, "capture LM body");
   enqueue_lm_head(cap_[0]);
   if (cl_plan_.cs > 0) {
     // the whole PCG of every problem in one cluster launch
     if ((e = launch_pcg_cluster(db_, cl_plan_, cap_[0])) != cudaSuccess) return fail(e, "PCG cluster kernel");
+  } else if (gr_plan_.grid > 0) {
+    // the whole PCG of the problem in one grid-wide launch
+    if ((e = launch_pcg_grid(db_, gr_plan_, cap_[0])) != cudaSuccess) return fail(e, "PCG grid kernel");
   } else {
     if ((e = add_while(cap_[0], pcgh, &pcgbody)) != cudaSuccess) return fail(e, "PCG conditional node");
     e = cudaStreamBeginCaptureToGraph(cap_[1], pcgbody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
@@ -705,8 +720,8 @@ gba_status Engine::run_host_driven(std::string *err) {
   while (hstat[1] && hstat[0] == 0) {
     if (++bodies > max_lm_bodies() + 2) break;
     enqueue_lm_head(stream_);
-    if (cl_plan_.cs > 0) {
-      if ((st = enqueue_pcg_cluster(stream_, err)) != GBA_OK) return st;
+    if (cl_plan_.cs > 0 || gr_plan_.grid > 0) {
+      if ((st = enqueue_pcg_one_launch(stream_, err)) != GBA_OK) return st;
       enqueue_lm_tail(stream_);
       if ((st = read_status()) != GBA_OK) return st;
       continue;
@@ -738,8 +753,20 @@ static double bytes_pcg_cluster(const DeviceBatch &b) {
   return ((double)b.nblk + b.nc) * 81.0 * 4.0 + (double)b.nc * 81.0 * 4.0 + (double)b.nc * 9.0 * (3 * 8.0 + 4.0 + 4 * 8.0);
 }
 
-gba_status Engine::enqueue_pcg_cluster(cudaStream_t s, std::string *err) {
+// Algorithmic bytes of one grid-PCG launch: the blocks of S (off-diagonal
+// and diagonal) and M^-1 once (FP64), v, r, z, x in and x, r, z, p out per
+// camera coordinate; the per-iteration exchanges stay in L2.
+static double bytes_pcg_grid(const DeviceBatch &b) {
+  return ((double)b.nblk + b.nc) * 81.0 * 8.0 + (double)b.nc * 81.0 * 8.0 + (double)b.nc * 9.0 * 8 * 8.0;
+}
+
+gba_status Engine::enqueue_pcg_one_launch(cudaStream_t s, std::string *err) {
   prof_begin(s);
+  if (gr_plan_.grid > 0) {
+    const gba_status st = check(launch_pcg_grid(db_, gr_plan_, s), "PCG grid kernel", err);
+    prof_end(s, PF_GRID, bytes_pcg_grid(db_));
+    return st;
+  }
   const gba_status st = check(launch_pcg_cluster(db_, cl_plan_, s), "PCG cluster kernel", err);
   prof_end(s, PF_CLUSTER, bytes_pcg_cluster(db_));
   return st;
@@ -786,6 +813,10 @@ gba_status Engine::download(const HostBatch &hb, const gba_problem_view *v, gba_
   size_t ub, doff, dbytes;
   layout(hb, h_stage_, &hdb, &ub, &doff, &dbytes);
   const int32_t *hstat = hdb.status;
+  if (hstat[0] == GBA_ERR_TIMEOUT) {
+    *err = "a bounded device-side wait of the grid PCG ran out (the solve was stopped)";
+    return GBA_ERR_TIMEOUT;
+  }
   if (hstat[0] != 0) {
     *err = "device-side loop guard tripped (internal error)";
     return GBA_ERR_INTERNAL;
@@ -1048,8 +1079,8 @@ gba_status Engine::compute_step(const gba_problem_view *v, double radius, double
   launch_camera_schur(db_, mixed_, stream_);
   launch_schur_form(db_, mixed_, stream_);
   if ((st = read_status()) != GBA_OK) return st;
-  if (cl_plan_.cs > 0) {
-    if ((st = enqueue_pcg_cluster(stream_, err)) != GBA_OK) return st;
+  if (cl_plan_.cs > 0 || gr_plan_.grid > 0) {
+    if ((st = enqueue_pcg_one_launch(stream_, err)) != GBA_OK) return st;
   } else {
     int pcg = 0;
     while (hstat[2] && pcg <= o_.max_linear_solver_iterations) {

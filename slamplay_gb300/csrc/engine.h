@@ -105,8 +105,9 @@ class Engine {
   int sm_count_ = 0;
   bool pdl_ = true;        // programmatic dependent launches inside the PCG body
   ClusterPlan cl_plan_;    // cs > 0: the PCG runs as one cluster launch per LM iteration
+  GridPlan gr_plan_;       // grid > 0: the PCG runs as one grid-wide launch per LM iteration
   HostBatch hb_;           // the last solve's prepared batch (storage reused)
-  gba_status enqueue_pcg_cluster(cudaStream_t s, std::string *err);
+  gba_status enqueue_pcg_one_launch(cudaStream_t s, std::string *err);
 };
 
 }  // namespace gba

@@ -198,6 +198,11 @@ struct DeviceBatch {
   void *cam_Sii;             // 81 * nc
   double *pcg_q;             // 9 * nc
   double *spmv_red;          // nc
+  // the grid PCG (FP64, one problem): the second direction buffer (the
+  // directions alternate between pcg_p and pcg_p2 by iteration parity) and
+  // its control words (kGrid* slots), zeroed by K3b before each launch
+  double *pcg_p2;            // 9 * nc
+  uint32_t *grid_ctl;        // 8
 };
 
 constexpr int kCamTable = 44;    // R(9) dR(27) t(3) f k1 k2 + pad
@@ -225,5 +230,11 @@ constexpr int kObsF = 28;  // reals per observation of obs_F (27 + pad: 16-byte 
 constexpr int kPC_SCHUR = 0, kPC_REDUCE = 1, kPC_UPDATE = 2;
 constexpr int kGC_SCHUR = 0, kGC_UPDATE = 1, kGC_POST = 2, kGC_LMBODIES = 3;
 // status words: [0] error, [1] any LM active, [2] any PCG active, [3] PCG-active problem count
+// grid PCG: threads per CTA (16 warps: four per SM sub-partition, so up to
+// 128 registers a thread) and the control words: registration (64-bit:
+// count, and the closed bit), the published participant count + 1, the
+// barrier counter, the abort word
+constexpr int kPcgGridThreads = 512;
+constexpr int kGridReg = 0, kGridCount = 2, kGridBar = 3, kGridAbort = 4;
 
 }  // namespace gba

@@ -594,8 +594,18 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg_camera(DeviceBatch B) {
       }
       psub[sub][m] = a;
     }
-    // p.q over the CTA (fixed order); thread 0 forms alpha once
-    if (dfs) {
+    // p.q over the CTA (fixed order); thread 0 forms alpha once.  The FP64
+    // form with the explicit complement sums the cameras' values in warp 0
+    // (warp_strided_sum: the grid PCG's order)
+    if (ex && !MIXED) {
+      if (t < 32) {
+        const double s2 = warp_strided_sum(cv, n);
+        if (t == 0) {
+          sc[0] = s2;
+          sc[1] = rz_k * recip_nr(s2);
+        }
+      }
+    } else if (dfs) {
 #pragma unroll
       for (int j = 0; j < kCv; ++j) psf = df_add(psf, cvf[j]);
       psf = df_warp_sum(psf);
@@ -607,7 +617,7 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg_camera(DeviceBatch B) {
       if ((t & 31) == 0) red[t >> 5] = psm;
     }
     __syncthreads();  // also publishes psub
-    if (t == 0) {
+    if (t == 0 && !(ex && !MIXED)) {
       double s2 = 0.0;
       if (dfs) {
         DF sf = dfred[0];

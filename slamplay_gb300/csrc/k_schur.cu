@@ -253,6 +253,54 @@ __global__ void __launch_bounds__(kSpmvThreads) k_schur_spmv(DeviceBatch B) {
   }
 }
 
+// K4a' of the FP64 form: one warp per camera, three groups of kSpmvSub
+// lanes, each group rows g, g + 3, g + 6 of the camera's blocks
+// (spmv_triplet_fp64: the grid PCG's arithmetic), then the camera's share of
+// p.q (the nine rows' p_i q_i in row order).
+__global__ void __launch_bounds__(32) k_schur_spmv64(DeviceBatch B) {
+  __shared__ double pqs[9];
+  const int c = blockIdx.x, t = threadIdx.x;
+  const int prob = B.cam_problem[c];
+  pdl_wait_s();
+  pdl_launch_dependents_s();
+  const LMState *L = B.lm + prob;
+  if (!(L->active && L->pcg_active)) return;  // uniform over the CTA
+  const int k = L->pcg_iterations;
+  const double beta = L->beta;
+  const double *zv = B.pcg_z, *pvv = B.pcg_p;
+  auto pdir = [&](size_t idx) -> double {
+    const double z = zv[idx];
+    if (k == 0) return z;
+    return fma(beta, pvv[idx], z);
+  };
+  const int r0 = B.sblk_row[c], nb = B.sblk_row[c + 1] - r0;
+  const double *vals = reinterpret_cast<const double *>(B.sblk_val);
+  const double *diag = reinterpret_cast<const double *>(B.cam_Sii) + 81 * (size_t)c;
+  const int g = t / kSpmvSub, j = t - kSpmvSub * g;
+  if (g < 3) {
+    double q[3];
+    spmv_triplet_fp64(
+        nb, j, 0x00ffffffu,
+        [&](int v, int rr) { return (v < nb ? vals + 81 * (size_t)(r0 + v) : diag) + 9 * (g + 3 * rr); },
+        [&](int v, int cc) { return pdir(9 * (size_t)(v < nb ? B.sblk_col[r0 + v] : c) + cc); }, q);
+    if (j == 0) {
+#pragma unroll
+      for (int rr = 0; rr < 3; ++rr) {
+        const size_t i = 9 * (size_t)c + g + 3 * rr;
+        B.pcg_q[i] = q[rr];
+        pqs[g + 3 * rr] = pdir(i) * q[rr];
+      }
+    }
+  }
+  __syncwarp();
+  if (t == 0) {
+    double s = 0.0;
+#pragma unroll
+    for (int r = 0; r < 9; ++r) s += pqs[r];
+    B.spmv_red[c] = s;
+  }
+}
+
 cudaError_t launch_schur_spmv(const DeviceBatch &b, bool mixed, cudaStream_t s, bool pdl) {
   if (b.nc == 0) return cudaSuccess;
   cudaLaunchConfig_t cfg = {};
@@ -265,7 +313,8 @@ cudaError_t launch_schur_spmv(const DeviceBatch &b, bool mixed, cudaStream_t s, 
   cfg.attrs = attr;
   cfg.numAttrs = pdl ? 1 : 0;
   if (mixed) return cudaLaunchKernelEx(&cfg, k_schur_spmv<true>, b);
-  return cudaLaunchKernelEx(&cfg, k_schur_spmv<false>, b);
+  cfg.blockDim = dim3(32);
+  return cudaLaunchKernelEx(&cfg, k_schur_spmv64, b);
 }
 
 }  // namespace gba

@@ -392,6 +392,7 @@ __global__ void __launch_bounds__(kSchurThreads) k_camera_schur(DeviceBatch B) {
     for (int q = t; q < B.num_problems; q += blockDim.x)
       cnt += (__ldcg(&B.lm[q].active) && __ldcg(&B.lm[q].pcg_active)) ? 1.0 : 0.0;
     const int count = (int)block_sum(cnt, red);
+    if (B.grid_ctl && t < 8) B.grid_ctl[t] = 0u;  // the grid PCG's control words, before its launch
     if (t == 0) {
       B.status[2] = count > 0 ? 1 : 0;
       B.status[3] = count;

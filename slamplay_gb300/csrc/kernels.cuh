@@ -184,6 +184,74 @@ __device__ __forceinline__ double warp_max(double v) {
   return v;
 }
 
+// Sum of n values v[0..n) in a fixed order: lane l of one warp adds values
+// l, l + 32, ... in order (L2 loads, several in flight per lane), then the
+// xor butterfly; the total in every lane of the warp.  Call from one whole
+// warp.
+__device__ __forceinline__ double warp_strided_sum(const double *v, int n) {
+  constexpr int kBatch = 8;  // loads in flight per lane
+  const int lane = (int)(threadIdx.x & 31);
+  double s = 0.0;
+  for (int e0 = 0; e0 < n; e0 += 32 * kBatch) {
+    double x[kBatch];
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) {
+      const int e = e0 + lane + 32 * u;
+      x[u] = e < n ? __ldcg(v + e) : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u)
+      if (e0 + lane + 32 * u < n) s += x[u];
+  }
+  return warp_sum(s);
+}
+
+// The FP64 explicit Schur product of one camera's row triplet (rows g, g + 3,
+// g + 6) by one of kSpmvSub lanes: lane j takes the camera's blocks v = j,
+// j + kSpmvSub, ... (v == nb: the diagonal block); each block's three row
+// dots are FMA chains over the nine columns in order, the lane adds its
+// blocks' dots in block order (four blocks' chains in flight at a time:
+// FP64 has a long dependent latency on GB300), then an xor butterfly over
+// the kSpmvSub lanes (a fixed tree).  row(v, rr) points at row g + 3 rr of
+// block v, col(v, cc) gives the direction's value at column cc of block v.
+// Both FP64 PCG forms (the two-kernel product and the grid kernel) call
+// this, so they agree bitwise.  `mask`: the warp's lanes that take part
+// (whole groups).
+constexpr int kSpmvSub = 8;
+template <class Row, class Col>
+__device__ __forceinline__ void spmv_triplet_fp64(int nb, int j, unsigned mask, Row row, Col col, double q[3]) {
+  constexpr int kIlp = 4;
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+  for (int v0 = j; v0 <= nb; v0 += kIlp * kSpmvSub) {
+    double d[kIlp][3];
+#pragma unroll
+    for (int u = 0; u < kIlp; ++u) {
+      const int v = v0 + u * kSpmvSub;
+      d[u][0] = d[u][1] = d[u][2] = 0.0;
+      if (v <= nb) {
+        const double *r0 = row(v, 0), *r1 = row(v, 1), *r2 = row(v, 2);
+#pragma unroll
+        for (int cc = 0; cc < 9; ++cc) {
+          const double p = col(v, cc);
+          d[u][0] = fma(r0[cc], p, d[u][0]);
+          d[u][1] = fma(r1[cc], p, d[u][1]);
+          d[u][2] = fma(r2[cc], p, d[u][2]);
+        }
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kIlp; ++u)
+      if (v0 + u * kSpmvSub <= nb) a0 += d[u][0], a1 += d[u][1], a2 += d[u][2];
+  }
+#pragma unroll
+  for (int o = 1; o < kSpmvSub; o <<= 1) {
+    a0 += __shfl_xor_sync(mask, a0, o);
+    a1 += __shfl_xor_sync(mask, a1, o);
+    a2 += __shfl_xor_sync(mask, a2, o);
+  }
+  q[0] = a0, q[1] = a1, q[2] = a2;
+}
+
 // Sum over the CTA; result valid in every thread.  `red` needs blockDim/32
 // doubles.  Contains __syncthreads(): call from all threads.  Thread 0 adds
 // the warp sums in warp order and broadcasts the total (GB300 issues FP64 at

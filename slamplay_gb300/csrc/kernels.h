@@ -49,6 +49,20 @@ struct ClusterPlan {
 // form does not apply or cannot be launched.
 bool pcg_cluster_plan(const ProblemInfo *prob, int num_problems, const int32_t *sblk_row, ClusterPlan *plan);
 cudaError_t launch_pcg_cluster(const DeviceBatch &b, const ClusterPlan &plan, cudaStream_t s);
+// K4 grid form: the whole PCG of one problem in one launch, one CTA per SM
+// with grid-wide barriers (FP64 form, explicit Schur complement).
+struct GridPlan {
+  int grid = 0;        // CTAs launched (the ones that register share the work)
+  int cap_blocks = 0;  // blocks of S a CTA's shared-memory layout holds
+  int cache_s = 0;     // 1: the blocks' values too (else only the staged direction)
+  size_t smem = 0;
+};
+// Sizes the launch from the problem's explicit-complement rows (sblk_row,
+// nc + 1); false when the form does not apply (a batch, the mixed form,
+// the implicit complement) or its kernel cannot be resident.
+bool pcg_grid_plan(int num_problems, bool mixed, bool explicit_schur, int nc, const int32_t *sblk_row,
+                   GridPlan *plan);
+cudaError_t launch_pcg_grid(const DeviceBatch &b, const GridPlan &plan, cudaStream_t s);
 // K4a-b: one PCG iteration (implicit Schur mat-vec, camera-side update).
 void launch_pcg_iteration(const DeviceBatch &b, bool mixed, cudaStream_t s);
 cudaError_t launch_schur_matvec(const DeviceBatch &b, bool mixed, cudaStream_t s, bool pdl);
