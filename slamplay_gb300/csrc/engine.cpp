@@ -184,6 +184,9 @@ size_t Engine::layout(const HostBatch &hb, char *base, DeviceBatch *db, size_t *
   b.nup = (int32_t)nup;
   b.npairs = ex ? hb.npairs : 0;
   b.sblk_row = cv.take<int32_t>(ex ? nc + 1 : 0);
+  b.sblk_max = 0;
+  if (ex)
+    for (size_t c = 0; c < nc; ++c) b.sblk_max = std::max(b.sblk_max, hb.sblk_row[c + 1] - hb.sblk_row[c] + 1);
   b.sblk_col = cv.take<int32_t>(nsb);
   b.sblk_tr = cv.take<int32_t>(nsb);
   b.sblk_up = cv.take<int32_t>(nup);
@@ -260,6 +263,7 @@ size_t Engine::layout(const HostBatch &hb, char *base, DeviceBatch *db, size_t *
   b.pcg_q = cv.take<double>(ex ? 9 * nc : 0);
   b.spmv_red = cv.take<double>(ex ? nc : 0);
   b.pcg_p2 = cv.take<double>(ex ? 9 * nc : 0);
+  b.pq_row = cv.take<double>(ex ? 9 * nc : 0);
   b.grid_ctl = cv.take<uint32_t>(8);
   b.prob_counter = cv.take<uint32_t>(4 * P);
   b.global_counter = cv.take<uint32_t>(8);
@@ -425,6 +429,7 @@ gba_status Engine::upload(const HostBatch &hb, std::string *err) {
   cur_key_.push_back(cl_plan_.cache_blocks);
   cur_key_.push_back(gr_plan_.grid);
   cur_key_.push_back(gr_plan_.cap_blocks);
+  cur_key_.push_back(gr_plan_.cap_pairs);
   return GBA_OK;
 }
 

@@ -186,6 +186,7 @@ struct DeviceBatch {
   int32_t explicit_schur;
   int32_t nblk, nup;
   long long npairs;
+  int32_t sblk_max;          // the most blocks of a row of S (the diagonal one included)
   const int32_t *sblk_row;   // nc + 1
   const int32_t *sblk_col;   // nblk
   const int32_t *sblk_tr;    // nblk
@@ -202,6 +203,7 @@ struct DeviceBatch {
   // directions alternate between pcg_p and pcg_p2 by iteration parity) and
   // its control words (kGrid* slots), zeroed by K3b before each launch
   double *pcg_p2;            // 9 * nc
+  double *pq_row;            // 9 * nc: each row's p_i q_i, [row of the camera][camera of the problem]
   uint32_t *grid_ctl;        // 8
 };
 
@@ -235,6 +237,9 @@ constexpr int kGC_SCHUR = 0, kGC_UPDATE = 1, kGC_POST = 2, kGC_LMBODIES = 3;
 // count, and the closed bit), the published participant count + 1, the
 // barrier counter, the abort word
 constexpr int kPcgGridThreads = 512;
+// chunk sums (32 cameras each) of the explicit FP64 form's p.q in the camera
+// kernel: problems of up to 32 * kPcgChunkSums cameras
+constexpr int kPcgChunkSums = 1024;
 constexpr int kGridReg = 0, kGridCount = 2, kGridBar = 3, kGridAbort = 4;
 
 }  // namespace gba

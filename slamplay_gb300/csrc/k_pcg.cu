@@ -492,6 +492,7 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg_camera(DeviceBatch B) {
   __shared__ DF dfred[kPcgWarps];
   __shared__ double red3[kPcgWarps][3];
   __shared__ double sc[2];
+  __shared__ double chs[kPcgChunkSums];  // the explicit FP64 form's p.q chunk sums
   __shared__ int flag;
   constexpr int kLeadWarps = (kPcgCoords + 31) / 32;  // the warps holding sub-lane 0
   const int4 cb = B.camblk[blockIdx.x];  // (problem, first camera, count, 0)
@@ -595,15 +596,14 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg_camera(DeviceBatch B) {
       psub[sub][m] = a;
     }
     // p.q over the CTA (fixed order); thread 0 forms alpha once.  The FP64
-    // form with the explicit complement sums the cameras' values in warp 0
-    // (warp_strided_sum: the grid PCG's order)
+    // form with the explicit complement sums the cameras' values in chunks
+    // of 32 and a pairwise tree (cta_chunked_sum: the grid PCG's order)
     if (ex && !MIXED) {
-      if (t < 32) {
-        const double s2 = warp_strided_sum(cv, n);
-        if (t == 0) {
-          sc[0] = s2;
-          sc[1] = rz_k * recip_nr(s2);
-        }
+      cta_chunked_sum<true>(cv, n, chs);
+      if (t == 0) {
+        const double s2 = chs[0];
+        sc[0] = s2;
+        sc[1] = rz_k * recip_nr(s2);
       }
     } else if (dfs) {
 #pragma unroll

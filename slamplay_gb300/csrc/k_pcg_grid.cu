@@ -9,27 +9,32 @@
 // kernel) the iteration costs two kernel boundaries (~27 us).  Here one CTA
 // per SM runs every iteration of the problem's PCG, with a grid-wide
 // barrier after each reduction:
-//   A. q = S p_k for the cameras the CTA owns (runs of about equal numbers
-//      of blocks of S): p_k = z_k + beta_k p_{k-1} of the owned blocks'
-//      columns staged in shared memory, then per camera three row triplets
-//      of eight lanes each over the blocks (spmv_triplet_fp64); each owned
-//      camera's p.q.                                             barrier
-//   B. p.q over the cameras (one warp), alpha; for the camera blocks (8
-//      cameras) the CTA owns: p_k, x, r, z = M r, each block's r.z, r.r,
-//      x.(v + r).                                                barrier
+//   A. q = S p_k for the rows the CTA owns (runs of about equal numbers of
+//      row blocks of S): p_k = z_k + beta_k p_{k-1} at the columns of the
+//      touched cameras' blocks staged in shared memory; a thread per (row,
+//      block) pair of the owned rows (a nine-column FMA chain), each row's
+//      block dots summed by the pairwise tree (the additions of each tree
+//      level listed once per launch and spread over all threads); each
+//      row's p_i q_i.                                           barrier
+//   B. every CTA: each camera's p.q (sum9_tree of its rows), their sum
+//      (chunks of 32 and a tree), alpha; for the camera blocks (8 cameras)
+//      the CTA owns: p_k, x, r, z = M r, each block's r.z, r.r, x.(v + r).
+//                                                                barrier
 //   C. in every CTA: the stopping test and beta_{k+1} from the blocks'
-//      values (one warp), while the other warps load what the next
-//      iteration's staged direction needs.
-// The owned rows of S stay in shared memory for the launch (S is fixed
-// during the PCG) when they fit; a CTA with more blocks than the layout
-// holds reads them from L2.  GB300's FP64 pipe retires about two lanes per
-// clock per SM, so the kernel keeps FP64 instructions off idle lanes: the
-// reductions over cameras run in one warp, the direction is formed once
-// per (block, column) and not once per row.
+//      values (three warps, one sum each), while the other warps load what
+//      the next iteration's staged direction needs.
+// The touched cameras' blocks of S stay in shared memory for the launch (S
+// is fixed during the PCG) when they fit; a CTA with more than the layout
+// holds reads them from L2.  GB300's FP64 pipe retires about one warp
+// instruction per 64 clocks per SM sub-partition, so the work is split by
+// rows (not cameras) for an even load over the CTAs and spread over all 16
+// warps of a CTA, and the direction is formed once per (block, column), not
+// once per row.
 // Every CTA takes the same decisions from the same values, so all reach the
 // same barriers.  The arithmetic is the two-kernel FP64 PCG's, operation
-// for operation (the same product, the same reduction trees), so both forms
-// give the same bits, and no result depends on how many CTAs took part.
+// for operation (the fixed trees of kernels.cuh, k_schur.cu's product and
+// the camera kernel's reductions), so both forms give the same bits, and no
+// result depends on how many CTAs took part.
 //
 // Participation.  The CTAs that start register on a counter; the first one
 // closes the registration once every CTA of the launch has registered, or
@@ -55,13 +60,14 @@ namespace {
 
 constexpr int kGThreads = kPcgGridThreads;
 constexpr int kGWarps = kGThreads / 32;
-constexpr int kGCamThreads = 3 * kSpmvSub;                // threads per camera in the product
-constexpr int kGCamsPerRound = kGThreads / kGCamThreads;  // cameras per round of the product
-constexpr int kGMaxOwn = 64;                               // cameras a CTA's shared-memory layout indexes
-constexpr int kGBlkSlot = 96;                              // threads per camera block in the update (3 warps)
+constexpr int kGMaxOwn = 64;    // touched cameras a CTA's shared-memory layout indexes
+constexpr int kGRows = 64;      // rows of one pass of the product (tables in shared memory)
+constexpr int kGLevels = 24;    // levels of the pairwise tree (rows of up to 2^24 blocks)
+constexpr int kGBlkSlot = 96;   // threads per camera block in the update (3 warps)
 constexpr int kGBlksPerRound = kGThreads / kGBlkSlot;
-static_assert(kGCamsPerRound >= 1 && kGBlksPerRound >= 1 && kGThreads % 32 == 0, "whole warps, at least one slot");
-static_assert(kGBlkSlot % 32 == 0 && kGCamThreads % kSpmvSub == 0, "block slots of whole warps, camera groups of whole lane groups");
+constexpr int kGPreThreads = kGThreads - 96;  // threads that prefetch while warps 0-2 decide
+static_assert(kGBlksPerRound >= 1 && kGThreads % 32 == 0 && kGWarps >= 4, "whole warps, at least one slot");
+static_assert(kGBlkSlot % 32 == 0, "block slots of whole warps");
 static_assert(9 * kPcgBlockCams <= kGBlkSlot, "a camera block's coordinates fit its slot");
 
 constexpr unsigned long long kClosed = 1ull << 63;
@@ -135,33 +141,52 @@ __device__ __forceinline__ bool grid_barrier(const DeviceBatch &B, unsigned gen,
 }
 
 // Dynamic shared memory: the rows of the block-Jacobi inverse of the
-// update's coordinates (one row per thread), per owned camera its first
-// block (boff, the diagonal block last in each camera's run), per owned
-// block its column camera, its 81 values (when cached) and the direction
-// at its nine columns.
+// update's coordinates (one row per thread), the cameras' p.q chunk sums,
+// per touched camera its first block (boff, the diagonal block last in each
+// camera's run), per touched block its column camera, its 81 values (when
+// cached) and the direction at its nine columns; for the product's pass
+// (at most kGRows rows, cap_pairs (row, block) pairs): each pair's dot and
+// (row, block), each row's first pair, the tree's additions by level.
 struct GridSmem {
-  size_t mrow, boff, scol, sval, pst, total;
+  size_t mrow, chs, boff, scol, sval, pst, pd, pinfo, ldst, roff, lbeg, total;
 };
 __host__ __device__ inline size_t grid_align(size_t x) { return (x + 15) & ~size_t(15); }
-__host__ __device__ inline GridSmem grid_smem(int cap_blocks, bool cache_s) {
+__host__ __device__ inline GridSmem grid_smem(int n, int cap_blocks, bool cache_s, int cap_pairs) {
   GridSmem l;
   size_t o = 0;
   l.mrow = o, o = grid_align(o + 8 * 9 * (size_t)kGThreads);
+  l.chs = o, o = grid_align(o + 8 * (size_t)((n + 31) / 32 + 1));
   l.boff = o, o = grid_align(o + 4 * (size_t)(kGMaxOwn + 1));
   l.scol = o, o = grid_align(o + 4 * (size_t)cap_blocks);
   l.sval = o, o = grid_align(o + (cache_s ? 8 * 81 * (size_t)cap_blocks : 0));
   l.pst = o, o = grid_align(o + 8 * 9 * (size_t)cap_blocks);
+  l.pd = o, o = grid_align(o + 8 * (size_t)cap_pairs);
+  l.pinfo = o, o = grid_align(o + 4 * (size_t)cap_pairs);
+  l.ldst = o, o = grid_align(o + 4 * (size_t)cap_pairs);
+  l.roff = o, o = grid_align(o + 4 * (size_t)(kGRows + 1));
+  l.lbeg = o, o = grid_align(o + 4 * (size_t)(kGLevels + 1));
   l.total = o;
   return l;
 }
 
+// The rows of a CTA: row rho (camera rho / 9, row rho % 9 of the problem)
+// costs the camera's blocks m_c (off-diagonal + diagonal); the 9 n rows are
+// cut into P runs of about equal cost.  Rows of camera c before the cost
+// bound t: min(9, ceil((t - 9 before_c) / m_c)), 0 when t <= 9 before_c.
+__host__ __device__ inline int rows_below(long long t, long long before9, long long m) {
+  if (t <= before9) return 0;
+  const long long r = (t - before9 + m - 1) / m;
+  return r > 9 ? 9 : (int)r;
+}
+
 }  // namespace
 
-__global__ void __launch_bounds__(kGThreads, 1) k_pcg_grid(DeviceBatch B, int cap_blocks, int cache_s) {
+__global__ void __launch_bounds__(kGThreads, 1) k_pcg_grid(DeviceBatch B, int cap_blocks, int cache_s,
+                                                         int cap_pairs) {
   extern __shared__ __align__(16) unsigned char g_smem[];
-  __shared__ int s_ticket, s_P, s_ok, s_own0, s_own1, s_stop;
-  __shared__ double pqs[kGCamsPerRound][9];
+  __shared__ int s_ticket, s_P, s_ok, s_ra, s_rb, s_stop, s_pass_end, s_npairs, s_nlev;
   __shared__ double sc[4];
+  __shared__ double tot3[3];
   __shared__ double rv[kGThreads];  // r_{k+1} of the update's coordinates, for M r
   __shared__ double red3[kGWarps][3];
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
@@ -200,59 +225,124 @@ __global__ void __launch_bounds__(kGThreads, 1) k_pcg_grid(DeviceBatch B, int ca
     }
     s_ticket = ticket;
     s_P = P;
+    s_ra = 0;
+    s_rb = 0;
   }
   __syncthreads();
   const int w = s_ticket, P = s_P;
   if (w < 0) return;  // arrived after the closing (or the closing never came)
 
   // ---- ownership -------------------------------------------------------------
-  // product: cameras in P runs of about equal blocks (off-diagonal + diagonal)
+  // product: the problem's rows in P runs of about equal cost (rows_below)
   const int n = pi.cam_count, c0 = pi.cam_begin;
+  const int r0 = B.sblk_row[c0];
   {
-    const int r0 = B.sblk_row[c0];
     const long long wtot = (long long)(B.sblk_row[c0 + n] - r0) + n;
-    const long long ta = ((long long)w * wtot + P - 1) / P, tb = ((long long)(w + 1) * wtot + P - 1) / P;
+    const long long ta = ((long long)w * 9 * wtot + P - 1) / P, tb = ((long long)(w + 1) * 9 * wtot + P - 1) / P;
     int a = 0, b = 0;
-    for (int cb = 0; cb < n; cb += kGThreads) {
-      const int c = cb + t;
-      const long long before = c < n ? (long long)(B.sblk_row[c0 + c] - r0) + c : wtot;
-      a += __syncthreads_count(before < ta);
-      b += __syncthreads_count(before < tb);
+    for (int c = t; c < n; c += kGThreads) {
+      const long long before = (long long)(B.sblk_row[c0 + c] - r0) + c;
+      const long long m = (long long)(B.sblk_row[c0 + c + 1] - B.sblk_row[c0 + c]) + 1;
+      a += rows_below(ta, 9 * before, m);
+      b += rows_below(tb, 9 * before, m);
     }
-    if (t == 0) s_own0 = a, s_own1 = b;
+    if (a) atomicAdd(&s_ra, a);
+    if (b) atomicAdd(&s_rb, b);
   }
   // update: camera blocks in P equal runs
   const int nblk = pi.cam_block_count;
   const int kb0 = pi.cam_block_begin + (int)((long long)w * nblk / P);
   const int kb1 = pi.cam_block_begin + (int)((long long)(w + 1) * nblk / P);
   __syncthreads();
-  const int own0 = c0 + s_own0, own1 = c0 + s_own1, own_n = own1 - own0;
+  const int ra = s_ra, rb = s_rb, own_rows = rb - ra;  // rows of the problem (local)
+  const int cA = ra / 9, cB = own_rows > 0 ? (rb - 1) / 9 : cA - 1;  // touched cameras (local)
+  const int ntc = cB - cA + 1;
   const double *vals = reinterpret_cast<const double *>(B.sblk_val);
   const double *Sii = reinterpret_cast<const double *>(B.cam_Sii);
-  // the owned blocks in shared memory: staged directions (and cached values)
-  // when they fit the layout, else everything from L2
-  const GridSmem lay = grid_smem(cap_blocks, cache_s != 0);
+  // the touched blocks in shared memory: staged directions (and cached
+  // values) when they fit the layout, else everything from L2
+  const GridSmem lay = grid_smem(n, cap_blocks, cache_s != 0, cap_pairs);
+  double *chs = reinterpret_cast<double *>(g_smem + lay.chs);
   int *boff = reinterpret_cast<int *>(g_smem + lay.boff);
   int *scol = reinterpret_cast<int *>(g_smem + lay.scol);
   double *sval = reinterpret_cast<double *>(g_smem + lay.sval);
   double *pst = reinterpret_cast<double *>(g_smem + lay.pst);
-  const int nbo = own_n > 0 ? (B.sblk_row[own1] - B.sblk_row[own0]) + own_n : 0;
-  const bool staged = own_n <= kGMaxOwn && nbo <= cap_blocks;
+  double *pd = reinterpret_cast<double *>(g_smem + lay.pd);
+  int *pinfo = reinterpret_cast<int *>(g_smem + lay.pinfo);
+  int *ldst = reinterpret_cast<int *>(g_smem + lay.ldst);
+  int *roff = reinterpret_cast<int *>(g_smem + lay.roff);
+  int *lbeg = reinterpret_cast<int *>(g_smem + lay.lbeg);
+  const int nbo = ntc > 0 ? (B.sblk_row[c0 + cB + 1] - B.sblk_row[c0 + cA]) + ntc : 0;
+  const bool staged = ntc <= kGMaxOwn && nbo <= cap_blocks;
   const bool cached = staged && cache_s != 0;
   if (staged) {
-    if (t <= own_n) boff[t] = B.sblk_row[own0 + t] - B.sblk_row[own0] + t;
+    if (t <= ntc) boff[t] = B.sblk_row[c0 + cA + t] - B.sblk_row[c0 + cA] + t;
     __syncthreads();
-    for (int lc = 0; lc < own_n; ++lc) {
-      const int c = own0 + lc;
-      const int r0 = B.sblk_row[c], nb = B.sblk_row[c + 1] - r0, b0 = boff[lc];
-      for (int v = t; v <= nb; v += kGThreads) scol[b0 + v] = v < nb ? B.sblk_col[r0 + v] : c;
+    for (int lc = 0; lc < ntc; ++lc) {
+      const int c = c0 + cA + lc;
+      const int rr0 = B.sblk_row[c], nb = B.sblk_row[c + 1] - rr0, b0 = boff[lc];
+      for (int v = t; v <= nb; v += kGThreads) scol[b0 + v] = v < nb ? B.sblk_col[rr0 + v] : c;
       if (cached)
         for (int e = t; e < 81 * (nb + 1); e += kGThreads) {
           const int v = e / 81, el = e - 81 * v;
-          sval[81 * (size_t)(b0 + v) + el] = v < nb ? vals[81 * (size_t)(r0 + v) + el] : Sii[81 * (size_t)c + el];
+          sval[81 * (size_t)(b0 + v) + el] = v < nb ? vals[81 * (size_t)(rr0 + v) + el] : Sii[81 * (size_t)c + el];
         }
     }
     __syncthreads();
+  }
+  // The product's pass over local rows [rl0, s_pass_end): at most kGRows rows
+  // and cap_pairs (row, block) pairs; its tables: each row's first pair
+  // (roff), each pair's (row, block) (pinfo), the tree's additions of each
+  // level (their destinations, ldst[lbeg[L] ..]).
+  auto row_m = [&](int rl) -> int {
+    const int c = c0 + (ra + rl) / 9;
+    return B.sblk_row[c + 1] - B.sblk_row[c] + 1;
+  };
+  auto build_pass = [&](int rl0) {
+    if (t == 0) {
+      int rl = rl0, np = 0, mx = 1;
+      roff[0] = 0;
+      while (rl < own_rows && rl - rl0 < kGRows) {
+        const int m = row_m(rl);
+        if (rl > rl0 && np + m > cap_pairs) break;
+        np += m;
+        mx = max(mx, m);
+        roff[rl - rl0 + 1] = np;
+        ++rl;
+      }
+      int nl = 0;
+      while ((1 << nl) < mx) ++nl;
+      int o = 0;
+      for (int L2 = 0; L2 < nl; ++L2) {
+        lbeg[L2] = o;
+        for (int j = 0; j < rl - rl0; ++j) o += tree_adds(roff[j + 1] - roff[j], 1 << L2);
+      }
+      lbeg[nl] = o;
+      s_pass_end = rl, s_npairs = np, s_nlev = nl;
+    }
+    __syncthreads();
+    const int nr = s_pass_end - rl0, nl = s_nlev;
+    for (int j = 0; j < nr; ++j)
+      for (int v = t; v < roff[j + 1] - roff[j]; v += kGThreads) pinfo[roff[j] + v] = (j << 20) | v;
+    for (int L2 = 0; L2 < nl; ++L2) {
+      const int sp = 1 << L2, base = lbeg[L2], cnt = lbeg[L2 + 1] - base;
+      for (int kk = t; kk < cnt; kk += kGThreads) {
+        int j = 0, acc = 0;
+        for (;;) {
+          const int a = tree_adds(roff[j + 1] - roff[j], sp);
+          if (kk < acc + a) break;
+          acc += a;
+          ++j;
+        }
+        ldst[base + kk] = roff[j] + 2 * sp * (kk - acc);
+      }
+    }
+    __syncthreads();
+  };
+  bool one_pass = true;
+  if (own_rows > 0) {
+    build_pass(0);
+    one_pass = s_pass_end == own_rows;
   }
 
   const DeviceOptions &o = B.opt;
@@ -292,7 +382,7 @@ __global__ void __launch_bounds__(kGThreads, 1) k_pcg_grid(DeviceBatch B, int ca
       uv = B.pcg_v[u_i];
     }
   }
-  // the staged direction of the owned blocks' columns: p_0 = z_0
+  // the staged direction of the touched blocks' columns: p_0 = z_0
   if (staged) {
     for (int e = t; e < 9 * nbo; e += kGThreads) {
       const int bl = e / 9, cc = e - 9 * bl;
@@ -301,81 +391,91 @@ __global__ void __launch_bounds__(kGThreads, 1) k_pcg_grid(DeviceBatch B, int ca
   }
   __syncthreads();
   for (;;) {
-    // ---- A. q = S p_k, each owned camera's p.q -------------------------------
+    // ---- A. q = S p_k for the owned rows, each row's p_i q_i ---------------
     const double *pprev = pbuf(k + 1);  // p_{k-1}
     auto pdir = [&](size_t idx) -> double {
       const double z = __ldcg(B.pcg_z + idx);
       if (k == 0) return z;
       return fma(beta, __ldcg(pprev + idx), z);
     };
-    for (int cb = 0; cb < own_n; cb += kGCamsPerRound) {
-      const int slot = t / kGCamThreads, m = t - kGCamThreads * slot;
-      const int g = m / kSpmvSub, j = m - kSpmvSub * g;
-      const int lc = cb + slot, c = own0 + lc;
-      if (slot < kGCamsPerRound && lc < own_n) {
-        const unsigned gmask = 0xffu << (lane & ~(kSpmvSub - 1));
-        double q[3];
+    for (int rl0 = 0; rl0 < own_rows;) {
+      if (!one_pass) build_pass(rl0);
+      const int pend = one_pass ? own_rows : s_pass_end, np = s_npairs, nl = s_nlev;
+      // the pairs' block dots (nine-column FMA chains)
+      for (int e = t; e < np; e += kGThreads) {
+        const int j = pinfo[e] >> 20, v = pinfo[e] & 0xfffff;
+        const int rho = ra + rl0 + j, cl = rho / 9, q = rho - 9 * cl, c = c0 + cl;
+        double d = 0.0;
         if (staged) {
-          const int b0 = boff[lc], nb = boff[lc + 1] - b0 - 1;
-          if (cached)
-            spmv_triplet_fp64(
-                nb, j, gmask, [&](int v, int rr) { return sval + 81 * (size_t)(b0 + v) + 9 * (g + 3 * rr); },
-                [&](int v, int cc) { return pst[9 * (b0 + v) + cc]; }, q);
-          else {
-            const int r0 = B.sblk_row[c];
-            spmv_triplet_fp64(
-                nb, j, gmask,
-                [&](int v, int rr) {
-                  return (v < nb ? vals + 81 * (size_t)(r0 + v) : Sii + 81 * (size_t)c) + 9 * (g + 3 * rr);
-                },
-                [&](int v, int cc) { return pst[9 * (b0 + v) + cc]; }, q);
-          }
+          const int b0 = boff[cl - cA], nb = boff[cl - cA + 1] - b0 - 1;
+          const double *row = cached ? sval + 81 * (size_t)(b0 + v) + 9 * q
+                                     : (v < nb ? vals + 81 * (size_t)(B.sblk_row[c] + v) : Sii + 81 * (size_t)c) + 9 * q;
+          const double *pp = pst + 9 * (b0 + v);
+#pragma unroll
+          for (int cc = 0; cc < 9; ++cc) d = fma(row[cc], pp[cc], d);
         } else {
-          const int r0 = B.sblk_row[c], nb = B.sblk_row[c + 1] - r0;
-          spmv_triplet_fp64(
-              nb, j, gmask,
-              [&](int v, int rr) {
-                return (v < nb ? vals + 81 * (size_t)(r0 + v) : Sii + 81 * (size_t)c) + 9 * (g + 3 * rr);
-              },
-              [&](int v, int cc) { return pdir(9 * (size_t)(v < nb ? B.sblk_col[r0 + v] : c) + cc); }, q);
-        }
-        if (j == 0) {
+          const int rr0 = B.sblk_row[c], nb = B.sblk_row[c + 1] - rr0;
+          const double *row = (v < nb ? vals + 81 * (size_t)(rr0 + v) : Sii + 81 * (size_t)c) + 9 * q;
+          const int col = v < nb ? B.sblk_col[rr0 + v] : c;
 #pragma unroll
-          for (int rr = 0; rr < 3; ++rr) {
-            const int row = g + 3 * rr;
-            const size_t i = 9 * (size_t)c + row;
-            B.pcg_q[i] = q[rr];
-            // p_k at the camera's own coordinate: its diagonal block's column
-            const double pk = staged ? pst[9 * (boff[lc + 1] - 1) + row] : pdir(i);
-            pqs[slot][row] = pk * q[rr];
-          }
+          for (int cc = 0; cc < 9; ++cc) d = fma(row[cc], pdir(9 * (size_t)col + cc), d);
         }
+        pd[e] = d;
       }
       __syncthreads();
-      if (t < kGCamsPerRound && cb + t < own_n) {
-        double s2 = 0.0;
-#pragma unroll
-        for (int r = 0; r < 9; ++r) s2 += pqs[t][r];
-        B.spmv_red[own0 + cb + t] = s2;
+      // each row's pairwise tree, level by level
+      for (int L2 = 0; L2 < nl; ++L2) {
+        const int sp = 1 << L2;
+        for (int kk = lbeg[L2] + t; kk < lbeg[L2 + 1]; kk += kGThreads) {
+          const int dst = ldst[kk];
+          pd[dst] += pd[dst + sp];
+        }
+        __syncthreads();
       }
-      __syncthreads();
+      if (t < pend - rl0) {
+        const int rho = ra + rl0 + t, cl = rho / 9, q = rho - 9 * cl, c = c0 + cl;
+        const size_t i = 9 * (size_t)c + q;
+        const double qv = pd[roff[t]];
+        // p_k at the row's own coordinate: the diagonal block's column
+        const double pk = staged ? pst[9 * (boff[cl - cA + 1] - 1) + q] : pdir(i);
+        B.pcg_q[i] = qv;
+        B.pq_row[(size_t)q * n + cl] = pk * qv;  // row-major by row index: a camera's rows n apart
+      }
+      __syncthreads();  // pd and the pass tables are used again
+      rl0 = pend;
     }
     if (!grid_barrier(B, ++gen, (unsigned)P, &s_ok)) {
       aborted = true;
       break;
     }
-    // ---- B. p.q over the cameras (warp 0), alpha; the update ------------------
+    // ---- B. each camera's p.q (sum9_tree), their sum (chunks of 32 and the
+    // pairwise tree: cta_chunked_sum's order), alpha; the update ---------------
     double qv_pre = 0.0;
-    if (t < 32) {
-      const double s2 = warp_strided_sum(B.spmv_red + c0, n);
+    if (one_round && u_lead) qv_pre = __ldcg(B.pcg_q + u_i);  // in flight while the cameras are summed
+    {
+      const int nch = (n + 31) / 32;
+      for (int j = warp; j < nch; j += kGWarps) {
+        const int c = 32 * j + lane;
+        double x = 0.0;
+        if (c < n) {
+          double x9[9];  // coalesced over the lanes' cameras
+#pragma unroll
+          for (int r = 0; r < 9; ++r) x9[r] = __ldcg(B.pq_row + (size_t)r * n + c);
+          x = sum9_tree(x9);
+        }
+        x = warp_sum(x);
+        if (lane == 0) chs[j] = x;
+      }
+      if (nch == 0 && t == 0) chs[0] = 0.0;
+      __syncthreads();
+      cta_pairwise_tree(chs, nch);
       if (t == 0) {
+        const double s2 = chs[0];
         sc[0] = s2;
         sc[1] = rz_k * recip_nr(s2);
       }
-    } else if (one_round && u_lead) {
-      qv_pre = __ldcg(B.pcg_q + u_i);  // in flight while warp 0 sums
+      __syncthreads();
     }
-    __syncthreads();
     const double pq = sc[0], alpha = sc[1];
     const bool good = pq > 0.0 && isfinite(pq);  // else S is not positive definite along p_k
     if (!good) {                                  // the PCG ends with x_k
@@ -384,7 +484,6 @@ __global__ void __launch_bounds__(kGThreads, 1) k_pcg_grid(DeviceBatch B, int ca
     }
     if (one_round) {
       if (u_lead) {
-        if (t < 32) qv_pre = __ldcg(B.pcg_q + u_i);
         up = k == 0 ? uz : fma(beta, up, uz);  // p_k from p_{k-1}
         ux = fma(alpha, up, ux);
         ur = fma(-alpha, qv_pre, ur);
@@ -470,48 +569,48 @@ __global__ void __launch_bounds__(kGThreads, 1) k_pcg_grid(DeviceBatch B, int ca
       aborted = true;
       break;
     }
-    // ---- C. the stopping test on (x_{k+1}, r_{k+1}) and beta_{k+1} (warp 0),
-    // while the other warps load z_{k+1} and p_k of the staged columns --------
+    // ---- C. the stopping test on (x_{k+1}, r_{k+1}) and beta_{k+1}: warp j < 3
+    // sums quantity j over the blocks (the camera kernel's order), while the
+    // other warps load z_{k+1} and p_k of the staged columns ------------------
     constexpr int kPre = 2;
     double zpre[kPre], ppre[kPre];
-    if (t < 32) {
-      double a3[3] = {0.0, 0.0, 0.0};
-      for (int bb = t; bb < nblk; bb += 32) {
-        const double *bv = B.blk_red + 3 * (size_t)(pi.cam_block_begin + bb);
-        a3[0] += __ldcg(bv), a3[1] += __ldcg(bv + 1), a3[2] += __ldcg(bv + 2);
-      }
-      a3[0] = warp_sum(a3[0]), a3[1] = warp_sum(a3[1]), a3[2] = warp_sum(a3[2]);
-      if (t == 0) {
-        const double rz1 = a3[0], rr1 = a3[1], qk = -a3[2];  // Q(x) = x'Sx - 2 v'x = -x.(v + r)
-        const int k1 = k + 1;
-        bool stop = false;
-        if (o.pcg_criterion == GBA_PCG_QUADRATIC_MODEL) {
-          const double lhs = k1 * (qk - q0), rhs = o.eta * qk;
-          const bool below = qk > 0.0 ? lhs < rhs : (qk < 0.0 ? lhs > rhs : q0 > 0.0);
-          if (below && k1 >= o.min_pcg_iterations) stop = true;
-        } else {
-          if (rr1 <= lim * lim && k1 >= o.min_pcg_iterations) stop = true;
-        }
-        if (k1 >= o.max_pcg_iterations) stop = true;
-        if (!(rz1 != 0.0 && isfinite(rz1))) stop = true;
-        sc[0] = rz1 * recip_nr(rz_k);  // beta_{k+1}
-        sc[1] = rz1;
-        sc[2] = rr1;
-        sc[3] = qk;
-        s_stop = stop ? 1 : 0;
-      }
+    if (warp < 3) {
+      double a = 0.0;
+      for (int bb = lane; bb < nblk; bb += 32) a += __ldcg(B.blk_red + 3 * (size_t)(pi.cam_block_begin + bb) + warp);
+      a = warp_sum(a);
+      if (lane == 0) tot3[warp] = a;
     } else if (staged) {
-      const double *pk = pbuf(k);
+      const double *pkb = pbuf(k);
 #pragma unroll
       for (int u = 0; u < kPre; ++u) {
-        const int e = (t - 32) + u * (kGThreads - 32);
+        const int e = (t - 96) + u * kGPreThreads;
         zpre[u] = ppre[u] = 0.0;
         if (e < 9 * nbo) {
           const size_t gi = 9 * (size_t)scol[e / 9] + e % 9;
           zpre[u] = __ldcg(B.pcg_z + gi);
-          ppre[u] = __ldcg(pk + gi);
+          ppre[u] = __ldcg(pkb + gi);
         }
       }
+    }
+    __syncthreads();
+    if (t == 0) {
+      const double rz1 = tot3[0], rr1 = tot3[1], qk = -tot3[2];  // Q(x) = x'Sx - 2 v'x = -x.(v + r)
+      const int k1 = k + 1;
+      bool stop = false;
+      if (o.pcg_criterion == GBA_PCG_QUADRATIC_MODEL) {
+        const double lhs = k1 * (qk - q0), rhs = o.eta * qk;
+        const bool below = qk > 0.0 ? lhs < rhs : (qk < 0.0 ? lhs > rhs : q0 > 0.0);
+        if (below && k1 >= o.min_pcg_iterations) stop = true;
+      } else {
+        if (rr1 <= lim * lim && k1 >= o.min_pcg_iterations) stop = true;
+      }
+      if (k1 >= o.max_pcg_iterations) stop = true;
+      if (!(rz1 != 0.0 && isfinite(rz1))) stop = true;
+      sc[0] = rz1 * recip_nr(rz_k);  // beta_{k+1}
+      sc[1] = rz1;
+      sc[2] = rr1;
+      sc[3] = qk;
+      s_stop = stop ? 1 : 0;
     }
     __syncthreads();
     beta = sc[0];
@@ -524,14 +623,14 @@ __global__ void __launch_bounds__(kGThreads, 1) k_pcg_grid(DeviceBatch B, int ca
     if (stop) break;
     // p_k = z_k + beta_k p_{k-1} at the staged columns
     if (staged) {
-      if (t >= 32) {
+      if (t >= 96) {
 #pragma unroll
         for (int u = 0; u < kPre; ++u) {
-          const int e = (t - 32) + u * (kGThreads - 32);
+          const int e = (t - 96) + u * kGPreThreads;
           if (e < 9 * nbo) pst[e] = fma(beta, ppre[u], zpre[u]);
         }
       }
-      for (int e = kPre * (kGThreads - 32) + t; e < 9 * nbo; e += kGThreads) {  // beyond the prefetched ones
+      for (int e = kPre * kGPreThreads + t; e < 9 * nbo; e += kGThreads) {  // beyond the prefetched ones
         const size_t gi = 9 * (size_t)scol[e / 9] + e % 9;
         pst[e] = fma(beta, __ldcg(pbuf(k + 1) + gi), __ldcg(B.pcg_z + gi));
       }
@@ -588,24 +687,44 @@ bool pcg_grid_plan(int num_problems, bool mixed, bool explicit_schur, int nc, co
     cudaGetLastError();
     return false;
   }
-  // one CTA per SM, and no more CTAs than cameras
-  const int grid = std::max(1, std::min(sms, nc));
-  // the kernel's split (all CTAs registered): the most blocks a CTA owns
+  // one CTA per SM, and no more CTAs than rows
+  const int grid = std::max(1, std::min(sms, 9 * nc));
+  // the kernel's split of the rows (all CTAs registered): the most blocks of
+  // touched cameras a CTA stages, the most touched cameras, the most (row,
+  // block) pairs, the longest row
   const long long wtot = (long long)(sblk_row[nc] - sblk_row[0]) + nc;
-  int most = 0, a = 0;
+  auto m_of = [&](int c) { return (long long)(sblk_row[c + 1] - sblk_row[c]) + 1; };
+  auto rows_before = [&](long long tb) {
+    long long r = 0;
+    for (int c = 0; c < nc; ++c) r += rows_below(tb, 9 * ((long long)(sblk_row[c] - sblk_row[0]) + c), m_of(c));
+    return r;
+  };
+  long long most = 0, most_pairs = 0, m_max = 0;
+  int most_cams = 0;
+  for (int c = 0; c < nc; ++c) m_max = std::max(m_max, m_of(c));
+  long long ra = 0;
   for (int r = 0; r < grid; ++r) {
-    const long long tb = ((long long)(r + 1) * wtot + grid - 1) / grid;
-    int b = a;
-    while (b < nc && (long long)(sblk_row[b] - sblk_row[0]) + b < tb) ++b;
-    most = std::max(most, (int)(sblk_row[b] - sblk_row[a]) + (b - a));
-    a = b;
+    const long long rb = rows_before(((long long)(r + 1) * 9 * wtot + grid - 1) / grid);
+    if (rb > ra) {
+      const int cA = (int)(ra / 9), cB = (int)((rb - 1) / 9);
+      most = std::max(most, (long long)(sblk_row[cB + 1] - sblk_row[cA]) + (cB - cA + 1));
+      most_cams = std::max(most_cams, cB - cA + 1);
+      long long pairs = 0;
+      for (long long rho = ra; rho < rb; ++rho) pairs += m_of((int)(rho / 9));
+      most_pairs = std::max(most_pairs, pairs);
+    }
+    ra = rb;
   }
   const size_t static_bytes = fa.sharedSizeBytes + 1024;  // the kernel's static shared memory, with margin
-  int cap = most + most / 4 + 8;  // room for a few CTAs fewer than launched
-  const bool cache = grid_smem(cap, true).total + static_bytes <= (size_t)optin;
-  while (!cache && cap > most && grid_smem(cap, false).total + static_bytes > (size_t)optin) cap = cap * 3 / 4;
-  if (!cache && grid_smem(cap, false).total + static_bytes > (size_t)optin) cap = 0;
-  const size_t smem = grid_smem(cap, cache).total;
+  auto fits = [&](int cap, bool cache, int pairs) { return grid_smem(nc, cap, cache, pairs).total + static_bytes <= (size_t)optin; };
+  // room for a few CTAs fewer than launched; a pass holds one whole row at least
+  int cap_pairs = (int)std::max<long long>(m_max, most_pairs + most_pairs / 4 + 64);
+  while (cap_pairs > m_max && !fits(0, false, cap_pairs)) cap_pairs = std::max<int>((int)m_max, cap_pairs * 3 / 4);
+  if (!fits(0, false, cap_pairs)) return false;
+  int cap = most_cams <= kGMaxOwn ? (int)(most + most / 4 + 16) : 0;
+  const bool cache = cap > 0 && fits(cap, true, cap_pairs);
+  while (!cache && cap > 0 && !fits(cap, false, cap_pairs)) cap = cap * 3 / 4;
+  const size_t smem = grid_smem(nc, cap, cache, cap_pairs).total;
   if (cudaFuncSetAttribute(k_pcg_grid, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
     cudaGetLastError();
     return false;
@@ -618,13 +737,14 @@ bool pcg_grid_plan(int num_problems, bool mixed, bool explicit_schur, int nc, co
   plan->grid = grid;
   plan->cap_blocks = cap;
   plan->cache_s = cache ? 1 : 0;
+  plan->cap_pairs = cap_pairs;
   plan->smem = smem;
   return true;
 }
 
 cudaError_t launch_pcg_grid(const DeviceBatch &b, const GridPlan &plan, cudaStream_t s) {
   if (plan.grid <= 0) return cudaSuccess;
-  k_pcg_grid<<<plan.grid, kGThreads, plan.smem, s>>>(b, plan.cap_blocks, plan.cache_s);
+  k_pcg_grid<<<plan.grid, kGThreads, plan.smem, s>>>(b, plan.cap_blocks, plan.cache_s, plan.cap_pairs);
   return cudaGetLastError();
 }
 

@@ -33,6 +33,8 @@
 //                     wait on the preceding camera kernel.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "kernels.cuh"
 #include "kernels.h"
 
@@ -253,11 +255,12 @@ __global__ void __launch_bounds__(kSpmvThreads) k_schur_spmv(DeviceBatch B) {
   }
 }
 
-// K4a' of the FP64 form: one warp per camera, three groups of kSpmvSub
-// lanes, each group rows g, g + 3, g + 6 of the camera's blocks
-// (spmv_triplet_fp64: the grid PCG's arithmetic), then the camera's share of
-// p.q (the nine rows' p_i q_i in row order).
-__global__ void __launch_bounds__(32) k_schur_spmv64(DeviceBatch B) {
+// K4a' of the FP64 form: one CTA per camera; the block dots of its rows
+// (nine-column FMA chains) into shared memory, `rpp` rows at a time, each
+// row summed by the pairwise tree, then the camera's p.q (sum9_tree of its
+// rows' p_i q_i): the grid PCG's arithmetic, so both forms agree bitwise.
+__global__ void __launch_bounds__(kSpmvThreads) k_schur_spmv64(DeviceBatch B, int rpp) {
+  extern __shared__ double sp_d[];  // [rpp][m]
   __shared__ double pqs[9];
   const int c = blockIdx.x, t = threadIdx.x;
   const int prob = B.cam_problem[c];
@@ -267,38 +270,56 @@ __global__ void __launch_bounds__(32) k_schur_spmv64(DeviceBatch B) {
   if (!(L->active && L->pcg_active)) return;  // uniform over the CTA
   const int k = L->pcg_iterations;
   const double beta = L->beta;
-  const double *zv = B.pcg_z, *pvv = B.pcg_p;
   auto pdir = [&](size_t idx) -> double {
-    const double z = zv[idx];
+    const double z = B.pcg_z[idx];
     if (k == 0) return z;
-    return fma(beta, pvv[idx], z);
+    return fma(beta, B.pcg_p[idx], z);
   };
-  const int r0 = B.sblk_row[c], nb = B.sblk_row[c + 1] - r0;
+  const int r0 = B.sblk_row[c], nb = B.sblk_row[c + 1] - r0, m = nb + 1;
   const double *vals = reinterpret_cast<const double *>(B.sblk_val);
   const double *diag = reinterpret_cast<const double *>(B.cam_Sii) + 81 * (size_t)c;
-  const int g = t / kSpmvSub, j = t - kSpmvSub * g;
-  if (g < 3) {
-    double q[3];
-    spmv_triplet_fp64(
-        nb, j, 0x00ffffffu,
-        [&](int v, int rr) { return (v < nb ? vals + 81 * (size_t)(r0 + v) : diag) + 9 * (g + 3 * rr); },
-        [&](int v, int cc) { return pdir(9 * (size_t)(v < nb ? B.sblk_col[r0 + v] : c) + cc); }, q);
-    if (j == 0) {
+  for (int q0 = 0; q0 < 9; q0 += rpp) {
+    const int nr = min(rpp, 9 - q0);
+    for (int e = t; e < nr * m; e += kSpmvThreads) {
+      const int rr = e / m, v = e - rr * m;
+      const double *row = (v < nb ? vals + 81 * (size_t)(r0 + v) : diag) + 9 * (q0 + rr);
+      const int col = v < nb ? B.sblk_col[r0 + v] : c;
+      double d = 0.0;
 #pragma unroll
-      for (int rr = 0; rr < 3; ++rr) {
-        const size_t i = 9 * (size_t)c + g + 3 * rr;
-        B.pcg_q[i] = q[rr];
-        pqs[g + 3 * rr] = pdir(i) * q[rr];
-      }
+      for (int cc = 0; cc < 9; ++cc) d = fma(row[cc], pdir(9 * (size_t)col + cc), d);
+      sp_d[e] = d;
     }
+    __syncthreads();
+    for (int s = 1; s < m; s <<= 1) {
+      const int na = tree_adds(m, s);
+      for (int e = t; e < nr * na; e += kSpmvThreads) {
+        const int rr = e / na, i = 2 * s * (e - rr * na);
+        sp_d[rr * m + i] += sp_d[rr * m + i + s];
+      }
+      __syncthreads();
+    }
+    if (t < nr) {
+      const int q = q0 + t;
+      const size_t i = 9 * (size_t)c + q;
+      const double qv = sp_d[t * m];
+      B.pcg_q[i] = qv;
+      pqs[q] = pdir(i) * qv;
+    }
+    __syncthreads();
   }
-  __syncwarp();
-  if (t == 0) {
-    double s = 0.0;
-#pragma unroll
-    for (int r = 0; r < 9; ++r) s += pqs[r];
-    B.spmv_red[c] = s;
-  }
+  if (t == 0) B.spmv_red[c] = sum9_tree(pqs);
+}
+
+// Rows per pass of k_schur_spmv64 and its shared memory, from the longest
+// row (in blocks, the diagonal one included).
+static int spmv64_rows(int m_max, size_t *smem) {
+  int optin = 48 * 1024, dev = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  const size_t budget = (size_t)optin - 4096;
+  int rpp = 9;
+  while (rpp > 1 && 8 * (size_t)rpp * m_max > budget) --rpp;
+  *smem = 8 * (size_t)rpp * std::max(m_max, 1);
+  return rpp;
 }
 
 cudaError_t launch_schur_spmv(const DeviceBatch &b, bool mixed, cudaStream_t s, bool pdl) {
@@ -313,8 +334,11 @@ cudaError_t launch_schur_spmv(const DeviceBatch &b, bool mixed, cudaStream_t s, 
   cfg.attrs = attr;
   cfg.numAttrs = pdl ? 1 : 0;
   if (mixed) return cudaLaunchKernelEx(&cfg, k_schur_spmv<true>, b);
-  cfg.blockDim = dim3(32);
-  return cudaLaunchKernelEx(&cfg, k_schur_spmv64, b);
+  size_t smem = 0;
+  const int rpp = spmv64_rows(b.sblk_max, &smem);
+  if (smem > 48 * 1024) cudaFuncSetAttribute(k_schur_spmv64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cfg.dynamicSmemBytes = smem;
+  return cudaLaunchKernelEx(&cfg, k_schur_spmv64, b, rpp);
 }
 
 }  // namespace gba

@@ -184,72 +184,57 @@ __device__ __forceinline__ double warp_max(double v) {
   return v;
 }
 
-// Sum of n values v[0..n) in a fixed order: lane l of one warp adds values
-// l, l + 32, ... in order (L2 loads, several in flight per lane), then the
-// xor butterfly; the total in every lane of the warp.  Call from one whole
-// warp.
-__device__ __forceinline__ double warp_strided_sum(const double *v, int n) {
-  constexpr int kBatch = 8;  // loads in flight per lane
-  const int lane = (int)(threadIdx.x & 31);
-  double s = 0.0;
-  for (int e0 = 0; e0 < n; e0 += 32 * kBatch) {
-    double x[kBatch];
-#pragma unroll
-    for (int u = 0; u < kBatch; ++u) {
-      const int e = e0 + lane + 32 * u;
-      x[u] = e < n ? __ldcg(v + e) : 0.0;
-    }
-#pragma unroll
-    for (int u = 0; u < kBatch; ++u)
-      if (e0 + lane + 32 * u < n) s += x[u];
-  }
-  return warp_sum(s);
+// The FP64 explicit Schur product's fixed summation trees (both FP64 PCG
+// forms, the two-kernel product in k_schur.cu and the grid kernel, use
+// them, so they agree bitwise):
+//  * a row of S times p: each block's dot over its nine columns is an FMA
+//    chain in column order; the row's m block dots (the diagonal block
+//    last) are summed by the pairwise tree: at level s = 1, 2, 4, ...,
+//    d[i] += d[i + s] for every i that is a multiple of 2 s with
+//    i + s < m; the sum is d[0];
+//  * a camera's p.q from its nine rows' p_i q_i: sum9_tree;
+//  * the problem's p.q from its cameras' values: chunks of 32 cameras, each
+//    summed by an xor butterfly over the lanes, then the pairwise tree over
+//    the chunks (cta_chunked_sum).
+// Number of additions level s of the pairwise tree does on m values.
+__host__ __device__ __forceinline__ int tree_adds(int m, int s) { return m > s ? (m - 1 - s) / (2 * s) + 1 : 0; }
+
+__device__ __forceinline__ double sum9_tree(const double x[9]) {
+  const double a = (x[0] + x[1]) + (x[2] + x[3]);
+  const double b = (x[4] + x[5]) + (x[6] + x[7]);
+  return (a + b) + x[8];
 }
 
-// The FP64 explicit Schur product of one camera's row triplet (rows g, g + 3,
-// g + 6) by one of kSpmvSub lanes: lane j takes the camera's blocks v = j,
-// j + kSpmvSub, ... (v == nb: the diagonal block); each block's three row
-// dots are FMA chains over the nine columns in order, the lane adds its
-// blocks' dots in block order (four blocks' chains in flight at a time:
-// FP64 has a long dependent latency on GB300), then an xor butterfly over
-// the kSpmvSub lanes (a fixed tree).  row(v, rr) points at row g + 3 rr of
-// block v, col(v, cc) gives the direction's value at column cc of block v.
-// Both FP64 PCG forms (the two-kernel product and the grid kernel) call
-// this, so they agree bitwise.  `mask`: the warp's lanes that take part
-// (whole groups).
-constexpr int kSpmvSub = 8;
-template <class Row, class Col>
-__device__ __forceinline__ void spmv_triplet_fp64(int nb, int j, unsigned mask, Row row, Col col, double q[3]) {
-  constexpr int kIlp = 4;
-  double a0 = 0.0, a1 = 0.0, a2 = 0.0;
-  for (int v0 = j; v0 <= nb; v0 += kIlp * kSpmvSub) {
-    double d[kIlp][3];
-#pragma unroll
-    for (int u = 0; u < kIlp; ++u) {
-      const int v = v0 + u * kSpmvSub;
-      d[u][0] = d[u][1] = d[u][2] = 0.0;
-      if (v <= nb) {
-        const double *r0 = row(v, 0), *r1 = row(v, 1), *r2 = row(v, 2);
-#pragma unroll
-        for (int cc = 0; cc < 9; ++cc) {
-          const double p = col(v, cc);
-          d[u][0] = fma(r0[cc], p, d[u][0]);
-          d[u][1] = fma(r1[cc], p, d[u][1]);
-          d[u][2] = fma(r2[cc], p, d[u][2]);
-        }
-      }
-    }
-#pragma unroll
-    for (int u = 0; u < kIlp; ++u)
-      if (v0 + u * kSpmvSub <= nb) a0 += d[u][0], a1 += d[u][1], a2 += d[u][2];
+// The pairwise tree over x[0..m) in shared memory, levels s = 1, 2, 4, ...
+// (the additions of a level spread over the CTA's threads, a barrier after
+// each level); the sum ends in x[0].  Call from every thread of the CTA.
+__device__ __forceinline__ void cta_pairwise_tree(double *x, int m) {
+  for (int s = 1; s < m; s <<= 1) {
+    for (int k = (int)threadIdx.x; k < tree_adds(m, s); k += (int)blockDim.x) x[2 * s * k] += x[2 * s * k + s];
+    __syncthreads();
   }
-#pragma unroll
-  for (int o = 1; o < kSpmvSub; o <<= 1) {
-    a0 += __shfl_xor_sync(mask, a0, o);
-    a1 += __shfl_xor_sync(mask, a1, o);
-    a2 += __shfl_xor_sync(mask, a2, o);
+}
+
+// The CTA's sum of v[0..n) (global memory, read with __ldcg, or shared
+// memory): chunks of 32 values, each an xor butterfly over a warp's lanes,
+// then the pairwise tree over the chunk sums; `scratch` holds
+// (n + 31) / 32 doubles of shared memory.  Call from every thread of the
+// CTA (whole warps); the total is in scratch[0] after the call (which ends
+// with a barrier), 0 for n = 0.
+template <bool GLOBAL>
+__device__ __forceinline__ void cta_chunked_sum(const double *v, int n, double *scratch) {
+  const int lane = (int)(threadIdx.x & 31), warp = (int)(threadIdx.x >> 5), nw = (int)(blockDim.x >> 5);
+  const int nch = (n + 31) / 32;
+  for (int j = warp; j < nch; j += nw) {
+    const int e = 32 * j + lane;
+    double x = 0.0;
+    if (e < n) x = GLOBAL ? __ldcg(v + e) : v[e];
+    x = warp_sum(x);
+    if (lane == 0) scratch[j] = x;
   }
-  q[0] = a0, q[1] = a1, q[2] = a2;
+  if (nch == 0 && threadIdx.x == 0) scratch[0] = 0.0;
+  __syncthreads();
+  cta_pairwise_tree(scratch, nch);
 }
 
 // Sum over the CTA; result valid in every thread.  `red` needs blockDim/32

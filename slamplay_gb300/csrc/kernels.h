@@ -55,6 +55,7 @@ struct GridPlan {
   int grid = 0;        // CTAs launched (the ones that register share the work)
   int cap_blocks = 0;  // blocks of S a CTA's shared-memory layout holds
   int cache_s = 0;     // 1: the blocks' values too (else only the staged direction)
+  int cap_pairs = 0;   // (row, block) pairs of one pass of the product
   size_t smem = 0;
 };
 // Sizes the launch from the problem's explicit-complement rows (sblk_row,

@@ -698,6 +698,17 @@ gba_status prepare_batch(const gba_problem_view *views, int n, const PrepOptions
                  pairs.load(), (long long)kExplicitPairsMax);
       return GBA_ERR_INVALID_ARGUMENT;
     }
+    // the FP64 explicit form sums a problem's cameras' p.q in chunks of 32
+    // held in shared memory: at most 32 kPcgChunkSums cameras a problem
+    int most_cams = 0;
+    for (const ProblemInfo &pi : hb.prob) most_cams = std::max(most_cams, (int)pi.cam_count);
+    if (most_cams > 32 * kPcgChunkSums) {
+      if (opt.schur == GBA_SCHUR_EXPLICIT) {
+        *err = fmt("the explicit Schur complement supports problems of at most %d cameras", 32 * kPcgChunkSums);
+        return GBA_ERR_INVALID_ARGUMENT;
+      }
+      hb.explicit_schur = false;
+    }
   }
   // each camera's observations in internal order: a stable counting sort by
   // camera over runs of observations (per-run counts, then offsets)
