@@ -398,16 +398,18 @@ typedef struct gba_device_problem {
 /* Residuals (device, 2 per observation, may be NULL) and cost (device, one
  * double) of a device-resident problem, computed without allocating any
  * memory.  No counterpart in the reference: it exists for callers that
- * cannot call cudaMalloc — code running during CUDA graph capture, real-time
- * threads that must not take cudaMalloc's implicit synchronisation, hosts
+ * cannot call cudaMalloc — real-time tracking threads that must not take
+ * cudaMalloc's implicit device synchronisation and unbounded latency, hosts
  * that own every device byte through their own pool.  Scratch lives in a
  * fixed file-scope device array (~6.3 MB, held by every GPU that loads the
  * library until exit); at most 16384 cameras and 16777216 observations per
  * call, larger problems are rejected with GBA_ERR_INVALID_ARGUMENT.  The
  * first call on a device sets up the array's address for that device (make
  * it before any stream capture).  Calls share the array: calls that overlap
- * on the GPU race.  Asynchronous on `stream` (a cudaStream_t, NULL = the
- * default stream); errors via gba_last_error(NULL). */
+ * on the GPU race.  The array's address is looked up once per device and
+ * kept for the life of the process: do not call this after a
+ * cudaDeviceReset of that device.  Asynchronous on `stream` (a
+ * cudaStream_t, NULL = the default stream); errors via gba_last_error(NULL). */
 gba_status gba_evaluate_noalloc(const gba_device_problem *p, int32_t loss, double loss_scale,
                                 double *residuals, double *cost, void *stream);
 

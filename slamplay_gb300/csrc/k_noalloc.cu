@@ -1,10 +1,9 @@
 // k_noalloc.cu — gba_evaluate_noalloc: residuals and cost of a problem whose
 // arrays already live on the device, without allocating anything.
 //
-// Who needs it: callers that cannot call cudaMalloc — code that runs while a
-// CUDA graph is being captured (an allocation would break the capture), a
-// real-time tracking thread that must not take cudaMalloc's implicit device
-// synchronisation and unbounded latency, or a host framework that owns all
+// Who needs it: callers that cannot call cudaMalloc — a real-time tracking
+// thread that must not take cudaMalloc's implicit device synchronisation and
+// unbounded latency, or a host framework that owns all
 // device memory through its own pool and forbids a library from allocating
 // outside it.  They pass device inputs and outputs; the only scratch this
 // entry point needs (per-camera rotation tables and per-CTA partial costs)
@@ -23,7 +22,10 @@
 //
 // Set-up: the first call on a device (with that device current) looks up the
 // device address of the array with cudaGetSymbolAddress and caches it per
-// device; make that first call before any stream capture starts.
+// device; make that first call before any stream capture starts.  The cached
+// address is the one of the module loaded in that device's primary context:
+// after a cudaDeviceReset the module is loaded again and the array may move,
+// so the entry point must not be used across a device reset.
 #include <cuda_runtime.h>
 
 #include <mutex>

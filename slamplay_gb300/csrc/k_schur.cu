@@ -128,7 +128,10 @@ __global__ void __launch_bounds__(kFormThreads) k_schur_form(DeviceBatch B) {
     if (sub < kFormSub)
       for (int u = sub; u < n; u += kFormSub) {
         const real *fa = &Fs[u][0][3 * ei], *fb = &Fs[u][1][3 * ek];
-        acc.add(fa[0] * fb[0] + fa[1] * fb[1] + fa[2] * fb[2]);
+        if constexpr (MIXED)
+          acc.add(fa[0] * fb[0] + fa[1] * fb[1] + fa[2] * fb[2]);
+        else  // FP64: one FMA chain through the accumulator (three FP64 operations a pair, not four)
+          acc.s = fma(fa[2], fb[2], fma(fa[1], fb[1], fma(fa[0], fb[0], acc.s)));
       }
     __syncthreads();  // the stage is reused
     if (more) store_round(g + kFormPairs);

@@ -20,6 +20,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <exception>
 #include <functional>
 #include <mutex>
 #include <thread>
@@ -39,14 +40,18 @@ static std::string fmt(const char *f, long long a, long long b = 0, long long c 
 // shared counter, and no result depends on which thread runs a task.  A loop
 // that finds the pool busy (another handle preparing at the same time), runs
 // inside a task, or runs in a forked child works on the calling thread alone.
+// The pool is never destroyed: a forked child (which has none of the
+// parent's threads) and the parent at exit end without joining or locking
+// anything.  An exception from a task ends the loop's other tasks early and
+// is rethrown by run() once every worker has left the loop.
 namespace {
 thread_local bool tl_in_task = false;  // this thread is running a pool task
 
 class Pool {
  public:
   static Pool &get() {
-    static Pool p;
-    return p;
+    static Pool *p = new Pool;  // never destroyed
+    return *p;
   }
   int threads() const { return (int)workers_.size() + 1; }
   void run(int ntasks, const std::function<void(int)> &fn) {
@@ -62,13 +67,20 @@ class Pool {
       ntasks_ = ntasks;
       next_.store(0, std::memory_order_relaxed);
       done_ = 0;
+      error_ = nullptr;
       ++gen_;
     }
     cv_.notify_all();
     work();
-    std::unique_lock<std::mutex> g(mu_);
-    done_cv_.wait(g, [&] { return done_ == (int)workers_.size(); });
-    fn_ = nullptr;
+    std::exception_ptr err;
+    {
+      std::unique_lock<std::mutex> g(mu_);
+      done_cv_.wait(g, [&] { return done_ == (int)workers_.size(); });
+      fn_ = nullptr;
+      err = error_;
+      error_ = nullptr;
+    }
+    if (err) std::rethrow_exception(err);
   }
 
  private:
@@ -86,30 +98,30 @@ class Pool {
       // fewer threads than asked: the loop counts only those that started
     }
   }
-  ~Pool() {
-    {
-      std::lock_guard<std::mutex> g(mu_);
-      stop_ = true;
-    }
-    cv_.notify_all();
-    for (auto &t : workers_)
-      if (t.joinable()) t.join();
-  }
+  // the tasks of the current loop, until none is left; a task's exception
+  // is kept (the first one) and the remaining tasks are skipped
   void work() {
-    tl_in_task = true;
+    struct InTask {
+      InTask() { tl_in_task = true; }
+      ~InTask() { tl_in_task = false; }
+    } in_task;
     for (;;) {
       const int t = next_.fetch_add(1, std::memory_order_relaxed);
       if (t >= ntasks_) break;
-      (*fn_)(t);
+      try {
+        (*fn_)(t);
+      } catch (...) {
+        std::lock_guard<std::mutex> g(mu_);
+        if (!error_) error_ = std::current_exception();
+        next_.store(ntasks_, std::memory_order_relaxed);
+      }
     }
-    tl_in_task = false;
   }
   void loop() {
     long long seen = 0;
     std::unique_lock<std::mutex> g(mu_);
     for (;;) {
-      cv_.wait(g, [&] { return stop_ || gen_ != seen; });
-      if (stop_) return;
+      cv_.wait(g, [&] { return gen_ != seen; });
       seen = gen_;
       g.unlock();
       work();
@@ -125,7 +137,7 @@ class Pool {
   std::atomic<int> next_{0};
   int done_ = 0;
   long long gen_ = 0;
-  bool stop_ = false;
+  std::exception_ptr error_;
   const pid_t pid_;
 };
 }  // namespace

@@ -39,7 +39,10 @@ class LocalBAWindow:
                  fx, fy, cx, cy, extrinsics):
         self.keyframe_index = np.ascontiguousarray(keyframe_index, dtype=np.int32)
         self.landmark_index = np.ascontiguousarray(landmark_index, dtype=np.int32)
-        self.rig_camera = np.ascontiguousarray(rig_camera, dtype=np.uint8)
+        rc = np.asarray(rig_camera)
+        if rc.size and (not np.all(np.isfinite(rc)) or rc.min() < 0 or rc.max() > 1 or np.any(rc != np.round(rc))):
+            raise ValueError("rig_camera must be 0 (left) or 1 (right)")
+        self.rig_camera = np.ascontiguousarray(rc, dtype=np.uint8)
         self.observations = np.ascontiguousarray(observations, dtype=np.float64).reshape(-1)
         self.poses = np.array(poses, dtype=np.float64).reshape(-1)
         self.landmarks = np.array(landmarks, dtype=np.float64).reshape(-1)

@@ -9,6 +9,8 @@
 #include <unistd.h>
 
 #include <algorithm>
+#include <atomic>
+#include <stdexcept>
 #include <cstdio>
 #include <cstring>
 #include <random>
@@ -128,6 +130,26 @@ int main() {
     printf("concurrent prepares: %d differ\n", fails);
     return 1;
   }
+  // a task that throws: the loop's other tasks stop early, run() rethrows
+  // once every worker has left, and the pool keeps working afterwards
+  {
+    std::atomic<int> ran{0};
+    bool caught = false;
+    try {
+      gba::host_parallel(64, [&](int t) {
+        ran.fetch_add(1);
+        if (t == 3) throw std::runtime_error("task 3");
+      });
+    } catch (const std::runtime_error &) {
+      caught = true;
+    }
+    std::atomic<int> after{0};
+    gba::host_parallel(64, [&](int) { after.fetch_add(1); });
+    if (!caught || ran.load() < 1 || after.load() != 64) {
+      printf("pool exception: caught %d ran %d after %d\n", (int)caught, ran.load(), after.load());
+      return 1;
+    }
+  }
   const pid_t pid = fork();
   if (pid == 0) {
     HostBatch hb;
@@ -135,7 +157,7 @@ int main() {
     int bad = 0;
     for (int s = 0; s < 2; ++s)
       if (prepare_batch(sets[s].data(), (int)sets[s].size(), po, &hb, &e) != GBA_OK || !same(hb, ref[s])) ++bad;
-    _exit(bad ? 1 : 0);
+    exit(bad ? 1 : 0);  // through the static destructors: the pool holds no threads here
   }
   int status = 0;
   if (pid < 0 || waitpid(pid, &status, 0) != pid || !WIFEXITED(status) || WEXITSTATUS(status) != 0) {

@@ -227,10 +227,11 @@ def test_window_rejects_inconsistent_arrays():
     args = [w.keyframe_index, w.landmark_index, w.rig_camera, w.observations, w.poses, w.landmarks,
             w.fx, w.fy, w.cx, w.cy, w.extrinsics]
     LocalBAWindow(*args)  # consistent
-    bad = list(args)
-    bad[2] = np.full_like(w.rig_camera, 2)
-    with pytest.raises(ValueError):
-        LocalBAWindow(*bad)
+    for v in (2, 256, 257, -1):  # integers that a byte cast would wrap into 0 or 1 are rejected too
+        bad = list(args)
+        bad[2] = np.full(w.rig_camera.shape, v, dtype=np.int64)
+        with pytest.raises(ValueError):
+            LocalBAWindow(*bad)
     bad = list(args)
     bad[0] = w.keyframe_index.copy()
     bad[0][0] = w.num_keyframes

@@ -1,8 +1,8 @@
 """gba_evaluate_noalloc: the allocation-free evaluation entry point.
 
-It serves callers that cannot call cudaMalloc (code running during CUDA
-graph capture, real-time threads, hosts that own every device byte through
-their own pool): they hand in device inputs and outputs and the library
+It serves callers that cannot call cudaMalloc (real-time tracking threads
+that must not take its implicit synchronisation, hosts that own every
+device byte through their own pool): they hand in device inputs and outputs and the library
 uses only a fixed file-scope device array as scratch.  This test (collected
 last on purpose) allocates the caller's device buffers with torch, calls the
 entry point through the C ABI twice in a row on two different problems, and
