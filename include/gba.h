@@ -114,6 +114,18 @@ typedef enum gba_camera_update {
   GBA_CAMERA_UPDATE_SO3_LEFT = 1
 } gba_camera_update;
 
+/* Camera parameter layout of gba_problem_view::parameters (gba_solve,
+ * gba_batch_solve): BALProblem's 9 angle-axis parameters per camera, or its
+ * use_quaternions layout of 10 (unit quaternion, translation, f, k1, k2;
+ * utils/datasets/BALProblem.cpp:117-138, camera_block_size() == 10 at
+ * BALProblem.h:55).  Quaternion cameras are converted to angle-axis for the
+ * solve and back afterwards, with the reference's own conversions
+ * (utils/geometry/rotation.h:72-131), as BALProblem does on load and write. */
+typedef enum gba_camera_layout {
+  GBA_CAMERA_ANGLE_AXIS = 0,
+  GBA_CAMERA_QUATERNION = 1
+} gba_camera_layout;
+
 /* Levenberg-Marquardt damping policy.  CERES: LevenbergMarquardtStrategy
  * (trust-region radius, D^2 = clamp(diag J^T J) / radius, Jacobi scaling,
  * Ceres' termination tests).  G2O: the g2o variant's
@@ -177,7 +189,8 @@ typedef struct gba_options {
                                          0 = one launch pair per PCG iteration      */
   int32_t camera_update;              /* gba_camera_update, GBA_CAMERA_UPDATE_ADDITIVE */
   int32_t lm_policy;                  /* gba_lm_policy, GBA_LM_POLICY_CERES          */
-  int32_t reserved[2];
+  int32_t camera_layout;              /* gba_camera_layout, GBA_CAMERA_ANGLE_AXIS    */
+  int32_t reserved[1];
 } gba_options;
 
 /* Per-solve report, the subset of ceres::Solver::Summary the reference

@@ -5,9 +5,12 @@
 // Works with any type exposing the accessors of slamplay::BALProblem
 // (utils/datasets/BALProblem.h:55-98): num_cameras(), num_points(),
 // num_observations(), camera_block_size(), camera_index(), point_index(),
-// observations(), mutable_cameras().  Cameras must be in the 9-parameter
-// angle-axis layout (camera_block_size() == 9), as the reference's
-// AutoDiffCostFunction<SnavelyReprojectionError, 2, 9, 3> assumes.
+// observations(), mutable_cameras().  Cameras in the 9-parameter angle-axis
+// layout (camera_block_size() == 9, what the reference's
+// AutoDiffCostFunction<SnavelyReprojectionError, 2, 9, 3> assumes) or in
+// BALProblem's use_quaternions layout (camera_block_size() == 10,
+// BALProblem.cpp:117-138), which the library converts to angle-axis for the
+// solve and back (gba_options::camera_layout).
 //
 // Like the reference: one Snavely residual block per observation with
 // HuberLoss(1.0) (:78), Levenberg-Marquardt with the points eliminated
@@ -52,7 +55,10 @@ struct SolveBAOptions {
 template <typename BALProblemT>
 gba_status SolveBA(BALProblemT &bal_problem, const SolveBAOptions &opts = SolveBAOptions(),
                    gba_summary *summary = nullptr) {
-  if (bal_problem.camera_block_size() != 9) return GBA_ERR_INVALID_ARGUMENT;
+  const int cbs = bal_problem.camera_block_size();
+  if (cbs != 9 && cbs != 10) return GBA_ERR_INVALID_ARGUMENT;
+  gba_options options = opts.options;
+  options.camera_layout = cbs == 10 ? GBA_CAMERA_QUATERNION : GBA_CAMERA_ANGLE_AXIS;
   gba_problem_view v;
   v.num_cameras = bal_problem.num_cameras();
   v.num_points = bal_problem.num_points();
@@ -62,7 +68,7 @@ gba_status SolveBA(BALProblemT &bal_problem, const SolveBAOptions &opts = SolveB
   v.observations = bal_problem.observations();
   v.parameters = bal_problem.mutable_cameras();  // cameras, then points, contiguous
   gba_handle *h = nullptr;
-  gba_status st = gba_create(&opts.options, &h);
+  gba_status st = gba_create(&options, &h);
   if (st != GBA_OK) {
     std::fprintf(stderr, "gba_create: %s\n", gba_last_error(nullptr));
     return st;

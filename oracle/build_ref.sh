@@ -5,11 +5,16 @@
 #       rotation and BALProblem.cpp compiled from where they lie in the
 #       reference tree, with declaration shims for Ceres/Eigen; only when the
 #       reference tree is present (REF_ROOT, default /root/reference).
-# Usage: oracle/build_ref.sh [oracle|ref|all]
+# Usage: oracle/build_ref.sh [oracle|ref|all|root]   (root: prints the
+# reference tree's path when it is present, nothing otherwise)
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
 REF_ROOT="${REF_ROOT:-/root/reference}"
 WHAT="${1:-all}"
+if [[ "$WHAT" == "root" ]]; then
+  if [[ -f "$REF_ROOT/utils/datasets/BALProblem.cpp" ]]; then echo "$REF_ROOT"; fi
+  exit 0
+fi
 CFLAGS="-O2 -fPIC -ffp-contract=off -fopenmp"
 
 if [[ "$WHAT" == "oracle" || "$WHAT" == "all" ]]; then

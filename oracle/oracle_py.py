@@ -81,6 +81,15 @@ def ensure_built(reference: bool = False) -> None:
         subprocess.run(["bash", os.path.join(HERE, "build_ref.sh"), "all" if reference else "oracle"], check=True)
 
 
+def reference_root():
+    """The reference tree's path where this machine has it (the environment
+    variable REF_ROOT, else build_ref.sh's default), or None."""
+    import subprocess
+    r = subprocess.run(["bash", os.path.join(HERE, "build_ref.sh"), "root"], stdout=subprocess.PIPE, text=True)
+    p = r.stdout.strip()
+    return p if p and os.path.isdir(p) else None
+
+
 def oracle():
     global _orc
     if _orc is None:

@@ -28,6 +28,7 @@ PCG_CRITERION = {"residual": 0, "quadratic_model": 1}
 SCHUR = {"auto": 0, "implicit": 1, "explicit": 2}
 CAMERA_UPDATE = {"additive": 0, "so3_left": 1}
 LM_POLICY = {"ceres": 0, "g2o": 1}
+CAMERA_LAYOUT = {"angle_axis": 0, "quaternion": 1}
 
 _i32p = C.POINTER(C.c_int32)
 _f64p = C.POINTER(C.c_double)
@@ -48,7 +49,7 @@ class Options(C.Structure):
         ("minimizer_progress_to_stdout", C.c_int32), ("device", C.c_int32), ("stream", C.c_void_p),
         ("chunk_observations", C.c_int32), ("reorder_points", C.c_int32), ("use_graphs", C.c_int32),
         ("pcg_unroll", C.c_int32), ("autotune", C.c_int32), ("schur", C.c_int32), ("persistent_pcg", C.c_int32),
-        ("camera_update", C.c_int32), ("lm_policy", C.c_int32), ("reserved", C.c_int32 * 2),
+        ("camera_update", C.c_int32), ("lm_policy", C.c_int32), ("camera_layout", C.c_int32), ("reserved", C.c_int32 * 1),
     ]
 
 

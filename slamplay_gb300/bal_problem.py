@@ -151,11 +151,14 @@ class BALProblem:
         v.parameters = N.f64p(self.parameters_)
         return v
 
-    def view(self) -> N.ProblemView:
-        """gba_problem_view over this problem's arrays (angle-axis layout)."""
-        if self.use_quaternions:
-            raise ValueError("the solver takes the 9-parameter angle-axis camera layout "
-                             "(SnavelyReprojectionError.h:89-92); convert with to_angle_axis()")
+    def view(self, allow_quaternions: bool = False) -> N.ProblemView:
+        """gba_problem_view over this problem's arrays: the angle-axis layout,
+        or the quaternion one (10 per camera) for a solver created with
+        camera_layout='quaternion' (allow_quaternions)."""
+        if self.use_quaternions and not allow_quaternions:
+            raise ValueError("this entry point takes the 9-parameter angle-axis camera layout "
+                             "(SnavelyReprojectionError.h:89-92); convert with to_angle_axis(), or solve with "
+                             "camera_layout='quaternion'")
         for a in (self.camera_index_, self.point_index_):
             assert a.dtype == np.int32 and a.flags.c_contiguous
         for a in (self.observations_, self.parameters_):

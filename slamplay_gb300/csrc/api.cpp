@@ -1,8 +1,10 @@
 // api.cpp — the extern "C" surface of libgba (declared in include/gba.h).
+#include <algorithm>
 #include <cstring>
 #include <memory>
 #include <new>
 #include <string>
+#include <vector>
 
 #include "engine.h"
 #include "gba.h"
@@ -117,6 +119,7 @@ gba_status gba_create(const gba_options *o, gba_handle **out) {
   if (opt.max_num_iterations < 0 || opt.max_linear_solver_iterations < 0 || opt.loss < 0 || opt.loss > 2 ||
       opt.precision < 0 || opt.precision > 1 || opt.schur < 0 || opt.schur > 2 ||
       opt.camera_update < 0 || opt.camera_update > 1 || opt.lm_policy < 0 || opt.lm_policy > 1 ||
+      opt.camera_layout < 0 || opt.camera_layout > 1 ||
       !(opt.initial_trust_region_radius > 0) ||
       !(opt.loss_scale > 0) || opt.max_num_consecutive_invalid_steps < 1) {
     g_create_error = "invalid solver options";
@@ -147,13 +150,56 @@ const char *gba_last_error(const gba_handle *h) {
   return h->last_error.c_str();
 }
 
+// Solves n problems; with the quaternion camera layout the cameras are
+// converted to angle-axis copies first and the results converted back into
+// the callers' arrays (BALProblem.cpp:117-138 loads and writes the same way).
+static gba_status solve_views(gba_handle *h, const gba_problem_view *problems, int32_t n, gba_summary *summaries,
+                              std::string *err) {
+  if (h->engine->options().camera_layout != GBA_CAMERA_QUATERNION) {
+    gba_status st = maybe_autotune(h, problems, n, err);
+    if (st == GBA_OK) st = h->engine->solve(problems, n, summaries, err);
+    return st;
+  }
+  std::vector<gba_problem_view> views(problems, problems + n);
+  std::vector<std::vector<double>> aa((size_t)n);
+  for (int32_t p = 0; p < n; ++p) {
+    const gba_problem_view &v = problems[p];
+    if (v.num_cameras < 0 || v.num_points < 0 || ((v.num_cameras > 0 || v.num_points > 0) && !v.parameters)) {
+      *err = "invalid problem view";
+      return GBA_ERR_INVALID_ARGUMENT;
+    }
+    const size_t nc = (size_t)v.num_cameras, np = (size_t)v.num_points;
+    aa[p].resize(9 * nc + 3 * np);
+    for (size_t c = 0; c < nc; ++c) {
+      const double *q = v.parameters + 10 * c;
+      gba_quaternion_to_angle_axis(q, &aa[p][9 * c]);
+      std::copy(q + 4, q + 10, &aa[p][9 * c + 3]);
+    }
+    std::copy(v.parameters + 10 * nc, v.parameters + 10 * nc + 3 * np, aa[p].begin() + 9 * nc);
+    views[p].parameters = aa[p].data();
+  }
+  gba_status st = maybe_autotune(h, views.data(), n, err);
+  if (st == GBA_OK) st = h->engine->solve(views.data(), n, summaries, err);
+  if (st != GBA_OK) return st;
+  for (int32_t p = 0; p < n; ++p) {
+    const gba_problem_view &v = problems[p];
+    const size_t nc = (size_t)v.num_cameras, np = (size_t)v.num_points;
+    for (size_t c = 0; c < nc; ++c) {
+      double *q = v.parameters + 10 * c;
+      gba_angle_axis_to_quaternion(&aa[p][9 * c], q);
+      std::copy(&aa[p][9 * c + 3], &aa[p][9 * c + 9], q + 4);
+    }
+    std::copy(aa[p].begin() + 9 * nc, aa[p].begin() + 9 * nc + 3 * np, v.parameters + 10 * nc);
+  }
+  return GBA_OK;
+}
+
 gba_status gba_solve(gba_handle *h, const gba_problem_view *p, gba_summary *s) {
   if (!h) return GBA_ERR_INVALID_ARGUMENT;
   if (!p) return fail(h, GBA_ERR_INVALID_ARGUMENT, "null problem");
   if (h->server && h->server->running()) return fail(h, GBA_ERR_INVALID_ARGUMENT, "handle is serving");
   std::string err;
-  gba_status st = maybe_autotune(h, p, 1, &err);
-  if (st == GBA_OK) st = h->engine->solve(p, 1, s, &err);
+  const gba_status st = solve_views(h, p, 1, s, &err);
   if (st != GBA_OK) return fail(h, st, err);
   return GBA_OK;
 }
@@ -163,8 +209,7 @@ gba_status gba_batch_solve(gba_handle *h, const gba_problem_view *problems, int3
   if (!problems || n <= 0) return fail(h, GBA_ERR_INVALID_ARGUMENT, "empty batch");
   if (h->server && h->server->running()) return fail(h, GBA_ERR_INVALID_ARGUMENT, "handle is serving");
   std::string err;
-  gba_status st = maybe_autotune(h, problems, n, &err);
-  if (st == GBA_OK) st = h->engine->solve(problems, n, summaries, &err);
+  const gba_status st = solve_views(h, problems, n, summaries, &err);
   if (st != GBA_OK) return fail(h, st, err);
   return GBA_OK;
 }
@@ -172,6 +217,8 @@ gba_status gba_batch_solve(gba_handle *h, const gba_problem_view *problems, int3
 gba_status gba_local_ba(gba_handle *h, gba_window_view *windows, int32_t n, gba_summary *summaries,
                         gba_window_result *results) {
   if (!h) return GBA_ERR_INVALID_ARGUMENT;
+  if (h->engine->options().camera_layout == GBA_CAMERA_QUATERNION)
+    return fail(h, GBA_ERR_INVALID_ARGUMENT, "the quaternion camera layout is taken by gba_solve and gba_batch_solve only");
   if (!windows || n <= 0) return fail(h, GBA_ERR_INVALID_ARGUMENT, "empty batch");
   if (h->server && h->server->running()) return fail(h, GBA_ERR_INVALID_ARGUMENT, "handle is serving");
   std::string err;
@@ -198,6 +245,8 @@ gba_status gba_autotune(gba_handle *h, const gba_problem_view *problems, int32_t
 gba_status gba_evaluate(gba_handle *h, const gba_problem_view *p, double *residuals, double *jacobians,
                         double *cost) {
   if (!h) return GBA_ERR_INVALID_ARGUMENT;
+  if (h->engine->options().camera_layout == GBA_CAMERA_QUATERNION)
+    return fail(h, GBA_ERR_INVALID_ARGUMENT, "the quaternion camera layout is taken by gba_solve and gba_batch_solve only");
   if (!p) return fail(h, GBA_ERR_INVALID_ARGUMENT, "null problem");
   std::string err;
   const gba_status st = h->engine->evaluate(p, residuals, jacobians, cost, &err);
@@ -208,6 +257,8 @@ gba_status gba_evaluate(gba_handle *h, const gba_problem_view *p, double *residu
 gba_status gba_compute_step(gba_handle *h, const gba_problem_view *p, double radius, double *delta,
                             double *model_cost_change, int32_t *pcg_iterations) {
   if (!h) return GBA_ERR_INVALID_ARGUMENT;
+  if (h->engine->options().camera_layout == GBA_CAMERA_QUATERNION)
+    return fail(h, GBA_ERR_INVALID_ARGUMENT, "the quaternion camera layout is taken by gba_solve and gba_batch_solve only");
   if (!p || !delta || !(radius > 0)) return fail(h, GBA_ERR_INVALID_ARGUMENT, "invalid step arguments");
   std::string err;
   int it = 0;
@@ -275,6 +326,8 @@ gba_status gba_server_start(gba_handle *h, size_t budget, int32_t max_live, int3
 
 gba_status gba_submit(gba_handle *h, const gba_problem_view *p, uint64_t *ticket) {
   if (!h || !ticket) return GBA_ERR_INVALID_ARGUMENT;
+  if (h->engine->options().camera_layout == GBA_CAMERA_QUATERNION)
+    return fail(h, GBA_ERR_INVALID_ARGUMENT, "the quaternion camera layout is taken by gba_solve and gba_batch_solve only");
   if (!h->server || !h->server->running()) return fail(h, GBA_ERR_INVALID_ARGUMENT, "server not started");
   std::string err;
   const gba_status st = h->server->submit(p, ticket, &err);

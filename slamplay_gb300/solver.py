@@ -87,9 +87,10 @@ def _summary(s: N.Summary, tr: _Trace | None) -> SolveSummary:
 
 def make_options(**kw) -> N.Options:
     """gba_options with Ceres' defaults, overridden by keyword (loss,
-    precision, pcg_criterion, schur, camera_update and lm_policy accept
-    names: loss='huber', precision='mixed', schur='explicit',
-    camera_update='so3_left', lm_policy='g2o')."""
+    precision, pcg_criterion, schur, camera_update, lm_policy and
+    camera_layout accept names: loss='huber', precision='mixed',
+    schur='explicit', camera_update='so3_left', lm_policy='g2o',
+    camera_layout='quaternion')."""
     o = N.Options()
     N.lib().gba_options_init(N.C.byref(o))
     for k, v in kw.items():
@@ -105,6 +106,8 @@ def make_options(**kw) -> N.Options:
             v = N.CAMERA_UPDATE[v]
         elif k == "lm_policy" and isinstance(v, str):
             v = N.LM_POLICY[v]
+        elif k == "camera_layout" and isinstance(v, str):
+            v = N.CAMERA_LAYOUT[v]
         elif k == "stream" and v is not None and not isinstance(v, int):
             v = int(v)
         if not hasattr(o, k):
@@ -145,9 +148,17 @@ class Solver:
         per = 10 if self.options.lm_policy == N.LM_POLICY["g2o"] else 1
         return max(1, self.options.max_num_iterations * per + 1)
 
+    def _view(self, problem: BALProblem) -> N.ProblemView:
+        quat = self.options.camera_layout == N.CAMERA_LAYOUT["quaternion"]
+        if problem.use_quaternions != quat:
+            raise ValueError("the problem's camera layout (use_quaternions=%s) differs from the solver's "
+                             "camera_layout option" % problem.use_quaternions)
+        return problem.view(allow_quaternions=quat)
+
     def solve(self, problem: BALProblem) -> SolveSummary:
-        """ceres::Solve replacement; problem.parameters() updated in place."""
-        v = problem.view()
+        """ceres::Solve replacement; problem.parameters() updated in place.
+        A use_quaternions problem needs camera_layout='quaternion'."""
+        v = self._view(problem)
         s = N.Summary()
         tr = _Trace(self._cap())
         tr.attach(s)
@@ -156,7 +167,7 @@ class Solver:
 
     def batch_solve(self, problems: Sequence[BALProblem]) -> list[SolveSummary]:
         n = len(problems)
-        views = (N.ProblemView * n)(*[p.view() for p in problems])
+        views = (N.ProblemView * n)(*[self._view(p) for p in problems])
         sums = (N.Summary * n)()
         trs = [_Trace(self._cap()) for _ in range(n)]
         for s, t in zip(sums, trs):

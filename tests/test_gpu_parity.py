@@ -60,7 +60,7 @@ def test_evaluate_mixed_matches_oracle():
     assert abs(cost - co) <= 1e-12 * co  # cost is FP64 in both modes
 
 
-@pytest.mark.parametrize("loss", ["trivial", "huber"])
+@pytest.mark.parametrize("loss", ["trivial", "huber", "cauchy"])
 def test_compute_step_matches_oracle(loss):
     b = small_problem()
     radius = 1e4
@@ -88,7 +88,7 @@ def _solve_pair(b, gpu_opts, orc_opts):
     return g, sg, so
 
 
-@pytest.mark.parametrize("loss", ["trivial", "huber"])
+@pytest.mark.parametrize("loss", ["trivial", "huber", "cauchy"])
 def test_solve_fp64_matches_oracle(loss):
     b = small_problem()
     opts = dict(max_num_iterations=20, loss=loss, **FIXED)

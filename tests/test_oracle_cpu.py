@@ -59,12 +59,33 @@ def test_zero_noise_problem_converges_to_zero_cost():
     assert r["final_cost"] < 1e-12 * r["initial_cost"]
 
 
-def test_dense_and_pcg_schur_agree():
+@pytest.mark.parametrize("loss", ["trivial", "cauchy"])
+def test_dense_and_pcg_schur_agree(loss):
     b = BALProblem.synthetic(0, seed=6, num_points=500)
-    a = O.solve(O.Problem.from_bal(b), max_num_iterations=10, linear_solver="dense_schur", **FIXED)
+    a = O.solve(O.Problem.from_bal(b), max_num_iterations=10, linear_solver="dense_schur", loss=loss, **FIXED)
     c = O.solve(O.Problem.from_bal(b), max_num_iterations=10, linear_solver="pcg_schur", pcg_tolerance=1e-13,
-                max_linear_solver_iterations=2000, **FIXED)
+                max_linear_solver_iterations=2000, loss=loss, **FIXED)
+    assert a["final_cost"] < 0.1 * a["initial_cost"]
     assert abs(a["final_cost"] - c["final_cost"]) <= 1e-10 * a["final_cost"]
+
+
+def test_cauchy_cost_formula_and_corrector():
+    """CauchyLoss(a) (backend/ceres/test_ceres_bundle_adjuster_simple.cpp:193):
+    rho(s) = a^2 log(1 + s / a^2) of each observation's squared residual
+    norm.  The evaluation returns the raw residuals and Jacobians (the
+    solver applies the corrector; the GPU parity tests solve with it)."""
+    b = BALProblem.synthetic(0, seed=7, num_points=100)
+    p = O.Problem.from_bal(b)
+    r, J, c_triv, _ = O.evaluate(p, "trivial")
+    for a in (1.0, 2.5):
+        rc, Jc, c_cau, ok = O.evaluate(p, "cauchy", a)
+        assert ok
+        s = (r ** 2).sum(axis=1)
+        b2 = a * a
+        assert abs(c_cau - 0.5 * (b2 * np.log1p(s / b2)).sum()) <= 1e-9 * c_cau
+        np.testing.assert_array_equal(rc, r)
+        np.testing.assert_array_equal(Jc, J)
+        assert c_cau < c_triv
 
 
 def test_huber_cost_formula():

@@ -13,10 +13,10 @@ from oracle import oracle_py as O
 from slamplay_gb300 import BALProblem
 from slamplay_gb300 import _native as N
 
-REF_ROOT = "/root/reference"
-LADYBUG = os.path.join(REF_ROOT, "data", "bal", "ladybug49.txt")
+REF_ROOT = O.reference_root()
+LADYBUG = os.path.join(REF_ROOT, "data", "bal", "ladybug49.txt") if REF_ROOT else ""
 
-ref = O.reference_lib() if os.path.isdir(REF_ROOT) else None
+ref = O.reference_lib() if REF_ROOT else None
 pytestmark = pytest.mark.skipif(ref is None, reason="reference tree / oracle/_ref unavailable")
 
 
