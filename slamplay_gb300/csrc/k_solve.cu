@@ -228,6 +228,150 @@ __global__ void __launch_bounds__(kChunkCap) k_point_schur(DeviceBatch B) {
   }
 }
 
+// K3a of the FP64 form with the explicit Schur complement.  Per point: C,
+// its inverse, t = C^-1 g_p, the factor L (L L^T = C^-1) and u = L^-1 t;
+// per observation the rows F = J_c^T (J_p L) (9x3), written for the
+// formation kernel K3c and kept by slot; per (camera segment, entry) the
+// segment's share of the diagonal block, sum_obs F_a . F_b over its rows
+// (W C^-1 W^T = F F^T), and of the reduced rhs, sum_obs F_a . u
+// (J_c^T J_p t = F L^-1 t): three FMAs an entry and observation where the
+// general kernel's J_c^T A J_c takes seven, GB300's FP64 pipe being what
+// bounds this kernel.
+struct PointSchurEx64Smem {
+  double F[kChunkCap][27];  // F by slot
+  double ci[kChunkCap][6];  // C^-1 by chunk point
+  double u[kChunkCap][3];   // L^-1 t by chunk point
+  double lc[kChunkCap][6];  // L by chunk point
+  int spt[kChunkCap];       // chunk point of each slot
+};
+
+__global__ void __launch_bounds__(kChunkCap) k_point_schur_ex64(DeviceBatch B) {
+  extern __shared__ __align__(16) unsigned char k3x_smem[];
+  PointSchurEx64Smem &sm = *reinterpret_cast<PointSchurEx64Smem *>(k3x_smem);
+  const int t = threadIdx.x;
+  for (int ch = blockIdx.x; ch < B.nchunks; ch += gridDim.x) {
+    const ChunkInfo ci = B.chunk[ch];
+    LMState *L = B.lm + ci.problem;
+    if (!L->active) continue;  // uniform over the CTA
+    const bool valid = t < ci.obs_count;
+    double2 Jc[9], Jp[3];
+    int lp = 0, slot = 0;
+    if (valid) {
+      const int64_t o = ci.obs_begin + t;
+#pragma unroll
+      for (int q = 0; q < 9; ++q) Jc[q] = jload<double2>(B.jac, B.no, q, o);
+#pragma unroll
+      for (int q = 0; q < 3; ++q) Jp[q] = jload<double2>(B.jac, B.no, 9 + q, o);
+      slot = B.obs_slot[o];
+      lp = B.obs_pt[o] - ci.pt_begin;
+      sm.spt[slot] = lp;
+    }
+    if (t < ci.pt_count) {
+      const int j = ci.pt_begin + t;
+      const double radius = L->radius;
+      double C[6];
+#pragma unroll
+      for (int q = 0; q < 6; ++q) C[q] = B.pt_C[6 * (size_t)j + q];
+      C[0] += lm_d2(C[0], radius, B.opt);
+      C[3] += lm_d2(C[3], radius, B.opt);
+      C[5] += lm_d2(C[5], radius, B.opt);
+      double Ci[6];
+      if (!spd_inverse3(C, Ci)) {
+        L->linear_ok = 0;  // benign race: every writer stores 0
+#pragma unroll
+        for (int q = 0; q < 6; ++q) Ci[q] = 0.0;
+      }
+      double *cio = reinterpret_cast<double *>(B.pt_Cinv) + 6 * (size_t)j;
+#pragma unroll
+      for (int q = 0; q < 6; ++q) {
+        cio[q] = Ci[q];
+        B.pt_Cinv64[6 * (size_t)j + q] = Ci[q];
+        sm.ci[t][q] = Ci[q];
+      }
+      const double *g = B.pt_g + 3 * (size_t)j;
+      const double g0 = g[0], g1 = g[1], g2 = g[2];
+      const double t0 = Ci[0] * g0 + Ci[1] * g1 + Ci[2] * g2;
+      const double t1 = Ci[1] * g0 + Ci[3] * g1 + Ci[4] * g2;
+      const double t2 = Ci[2] * g0 + Ci[4] * g1 + Ci[5] * g2;
+      B.pt_t[3 * (size_t)j + 0] = t0;
+      B.pt_t[3 * (size_t)j + 1] = t1;
+      B.pt_t[3 * (size_t)j + 2] = t2;
+      double Lc[6];
+      chol3(Ci, Lc);
+#pragma unroll
+      for (int q = 0; q < 6; ++q) sm.lc[t][q] = Lc[q];
+      // u = L^-1 t (forward substitution; a zero pivot gives a zero component)
+      const double i00 = Lc[0] > 0.0 ? recip_nr(Lc[0]) : 0.0;
+      const double i11 = Lc[2] > 0.0 ? recip_nr(Lc[2]) : 0.0;
+      const double i22 = Lc[5] > 0.0 ? recip_nr(Lc[5]) : 0.0;
+      const double u0 = t0 * i00;
+      const double u1 = (t1 - Lc[1] * u0) * i11;
+      const double u2 = (t2 - Lc[3] * u0 - Lc[4] * u1) * i22;
+      sm.u[t][0] = u0, sm.u[t][1] = u1, sm.u[t][2] = u2;
+    }
+    // the first (segment, entry) task of this thread: its metadata now
+    int f_b0 = 0, f_b1 = 0, f_slot = 0;
+    if (t < ci.seg_count * 54) {
+      const int sg = t / 54;
+      f_b0 = B.seg_pos[ci.seg_begin + sg];
+      f_b1 = (sg + 1 < ci.seg_count) ? B.seg_pos[ci.seg_begin + sg + 1] : ci.obs_count;
+      f_slot = B.seg_slot[ci.seg_begin + sg];
+    }
+    __syncthreads();
+    if (valid) {
+      const double *Lc = sm.lc[lp];
+      double P[2][3];
+#pragma unroll
+      for (int r = 0; r < 2; ++r) {
+        const double j0 = r ? Jp[0].y : Jp[0].x, j1 = r ? Jp[1].y : Jp[1].x, j2 = r ? Jp[2].y : Jp[2].x;
+        P[r][0] = j0 * Lc[0] + j1 * Lc[1] + j2 * Lc[3];
+        P[r][1] = j1 * Lc[2] + j2 * Lc[4];
+        P[r][2] = j2 * Lc[5];
+      }
+      double F[kObsF];
+#pragma unroll
+      for (int q = 0; q < 9; ++q)
+#pragma unroll
+        for (int m = 0; m < 3; ++m) F[3 * q + m] = Jc[q].x * P[0][m] + Jc[q].y * P[1][m];
+      F[27] = 0.0;
+#pragma unroll
+      for (int e = 0; e < 27; ++e) sm.F[slot][e] = F[e];
+      double2 *dst = reinterpret_cast<double2 *>(reinterpret_cast<double *>(B.obs_F) +
+                                                 (size_t)kObsF * B.obs_fpos[ci.obs_begin + t]);
+#pragma unroll
+      for (int e = 0; e < kObsF / 2; ++e) dst[e] = *reinterpret_cast<const double2 *>(&F[2 * e]);
+    }
+    __syncthreads();
+    double *part = reinterpret_cast<double *>(B.schur_partial);
+    for (int i = t; i < ci.seg_count * 54; i += blockDim.x) {
+      const int sg = i / 54, en = i - 54 * sg;
+      int b0 = f_b0, b1 = f_b1, sl = f_slot;
+      if (i != t) {
+        b0 = B.seg_pos[ci.seg_begin + sg];
+        b1 = (sg + 1 < ci.seg_count) ? B.seg_pos[ci.seg_begin + sg + 1] : ci.obs_count;
+        sl = B.seg_slot[ci.seg_begin + sg];
+      }
+      double acc = 0.0;
+      if (en < 45) {
+        int a, b;
+        sym9_pair(en, a, b);
+        for (int k = b0; k < b1; ++k) {
+          const double *fa = sm.F[k] + 3 * a, *fb = sm.F[k] + 3 * b;
+          acc = fma(fa[2], fb[2], fma(fa[1], fb[1], fma(fa[0], fb[0], acc)));
+        }
+      } else {
+        const int a = en - 45;
+        for (int k = b0; k < b1; ++k) {
+          const double *fa = sm.F[k] + 3 * a, *u = sm.u[sm.spt[k]];
+          acc = fma(fa[2], u[2], fma(fa[1], u[1], fma(fa[0], u[0], acc)));
+        }
+      }
+      part[54 * (size_t)sl + en] = acc;
+    }
+    __syncthreads();
+  }
+}
+
 size_t point_schur_smem(bool mixed) {
   return mixed ? sizeof(PointSchurSmem<float>) : sizeof(PointSchurSmem<double>);
 }
@@ -238,6 +382,8 @@ void launch_point_prepare(const DeviceBatch &b, bool mixed, cudaStream_t s) {
   const size_t lcb = b.explicit_schur ? 0 : kChunkCap * 6 * (mixed ? sizeof(float) : sizeof(double));
   if (mixed)
     k_point_schur<true><<<b.nchunks, kChunkCap, point_schur_smem(true) - lcb, s>>>(b);
+  else if (b.explicit_schur)
+    k_point_schur_ex64<<<b.nchunks, kChunkCap, sizeof(PointSchurEx64Smem), s>>>(b);
   else
     k_point_schur<false><<<b.nchunks, kChunkCap, point_schur_smem(false) - lcb, s>>>(b);
 }
@@ -412,6 +558,7 @@ void launch_camera_schur(const DeviceBatch &b, bool mixed, cudaStream_t s) {
 void point_schur_init() {
   cudaFuncSetAttribute(k_point_schur<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)point_schur_smem(true));
   cudaFuncSetAttribute(k_point_schur<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)point_schur_smem(false));
+  cudaFuncSetAttribute(k_point_schur_ex64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(PointSchurEx64Smem));
 }
 
 
