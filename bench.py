@@ -450,7 +450,7 @@ def compact_form(name: str, f: dict) -> dict:
                     "sequential_fp64_solves_per_s": f["sequential_fp64"]["solves_per_s"],
                     "mixed_vs_fp64_final_cost_rel": f["mixed_vs_fp64_final_cost_rel"]}
         if name == "serving":
-            return {"sweep": [{k: x[k] for k in ("arrival_rate_per_s", "solves_per_s", "p50_ms", "p99_ms")}
+            return {"sweep": [{k: x[k] for k in ("arrival_rate_per_s", "solves_per_s", "p50_ms", "p99_ms", "reforms")}
                               for x in f["sweep"]], "requests_per_rate": f.get("requests_per_rate"),
                     "sequential_fp64_solves_per_s": f["sequential_fp64_solves_per_s"]}
         if name == "g2o_variant":
@@ -649,30 +649,46 @@ def large_form(lm_iterations: int = 10) -> dict:
     return out
 
 
-def serving_form(n_requests: int = 48, rate_mults=(2.0, 5.0, 10.0), seq_sample: int = 16) -> dict:
+def _request_copy(r):
+    """A request over a pool problem: its own parameter array (the solve
+    writes it), the observations and indices shared."""
+    from slamplay_gb300 import BALProblem
+
+    b = BALProblem()
+    b.use_quaternions = r.use_quaternions
+    b.num_cameras_, b.num_points_, b.num_observations_ = r.num_cameras_, r.num_points_, r.num_observations_
+    b.camera_index_, b.point_index_, b.observations_ = r.camera_index_, r.point_index_, r.observations_
+    b.parameters_ = r.parameters_.copy()
+    return b
+
+
+def serving_form(n_requests: int = 1000, pool: int = 64, rate_mults=(2.0, 5.0, 10.0), seq_sample: int = 16) -> dict:
     """Configuration 4: requests generated as configuration 1 with 10-400
     cameras and 1k-150k points (log-uniform), solved to relative cost
-    decrease < 1e-6 or 50 iterations.  A sequential plain FP64 loop sets the
-    reference rate; the mixed-precision server then takes `n_requests`
-    Poisson arrivals at each multiple of that rate (continuous batching over
-    four engine slots); latency = completion seen by the client - submit."""
+    decrease < 1e-6 or 50 iterations.  `pool` distinct problems are
+    generated; the `n_requests` requests of a rate cycle through them (each
+    request its own parameter array).  A sequential plain FP64 loop over the
+    first `seq_sample` problems sets the reference rate; the mixed-precision
+    server then takes `n_requests` Poisson arrivals at each multiple of that
+    rate (continuous batching over four engine slots, requests joining
+    running cohorts at LM-iteration boundaries); latency = completion seen by
+    the client - submit."""
     import numpy as np
 
     from slamplay_gb300 import BALProblem, Solver
 
-    reqs = [BALProblem.synthetic(4, index=i, seed=0) for i in range(n_requests)]
+    problems = [BALProblem.synthetic(4, index=i, seed=0) for i in range(pool)]
     opts = dict(max_num_iterations=50, function_tolerance=1e-6, **PCG_SMALL)
     with Solver(precision="fp64", **opts) as s:
         t0 = time.perf_counter()
-        for r in reqs[:seq_sample]:
-            s.solve(r.copy())
+        for r in problems[:seq_sample]:
+            s.solve(_request_copy(r))
         seq = seq_sample / (time.perf_counter() - t0)
     sweep = []
     rng = np.random.default_rng(1)
     for mult in rate_mults:
         rate = seq * mult
         gaps = rng.exponential(1.0 / rate, size=n_requests)
-        work = [r.copy() for r in reqs]
         sub_t, done_t = {}, {}
         with Solver(precision="mixed", **opts) as s:
             s.start_server()
@@ -681,7 +697,7 @@ def serving_form(n_requests: int = 48, rate_mults=(2.0, 5.0, 10.0), seq_sample: 
             while i < n_requests or pending:
                 now = time.perf_counter()
                 while i < n_requests and now >= next_t:
-                    tk = s.submit(work[i])
+                    tk = s.submit(_request_copy(problems[i % pool]))
                     sub_t[tk] = now
                     pending.add(tk)
                     next_t += gaps[i]
@@ -695,13 +711,15 @@ def serving_form(n_requests: int = 48, rate_mults=(2.0, 5.0, 10.0), seq_sample: 
             st = s.server_stats()
             s.stop_server()
         lat = np.array([done_t[k] - sub_t[k] for k in done_t])
-        sweep.append({"arrival_rate_per_s": rate, "solves_per_s": n_requests / total,
+        sweep.append({"arrival_rate_per_s": rate, "requests": n_requests, "solves_per_s": n_requests / total,
                       "p50_ms": 1e3 * float(np.percentile(lat, 50)), "p99_ms": 1e3 * float(np.percentile(lat, 99)),
-                      "peak_live": st.get("peak_live")})
+                      "peak_live": st.get("peak_live"), "batched_lm_iterations": st.get("steps"),
+                      "reforms": st.get("reforms")})
     best = max(sweep, key=lambda x: x["solves_per_s"])
-    return {"workload": f"config4: {n_requests} Poisson requests per rate, mean "
-                        f"{int(np.mean([r.num_observations() for r in reqs]))} obs",
-            "sweep": sweep, "sequential_fp64_solves_per_s": seq, "sequential_sample": f"first {seq_sample} requests",
+    return {"workload": f"config4: {n_requests} Poisson requests per rate over a pool of {pool} problems, mean "
+                        f"{int(np.mean([r.num_observations() for r in problems]))} obs",
+            "requests_per_rate": n_requests, "sweep": sweep, "sequential_fp64_solves_per_s": seq,
+            "sequential_sample": f"first {seq_sample} problems",
             "best_solves_per_s": best["solves_per_s"], "best_vs_sequential_fp64": best["solves_per_s"] / seq}
 
 

@@ -190,7 +190,8 @@ typedef struct gba_options {
   int32_t camera_update;              /* gba_camera_update, GBA_CAMERA_UPDATE_ADDITIVE */
   int32_t lm_policy;                  /* gba_lm_policy, GBA_LM_POLICY_CERES          */
   int32_t camera_layout;              /* gba_camera_layout, GBA_CAMERA_ANGLE_AXIS    */
-  int32_t reserved[1];
+  int32_t server_slots;               /* serving: cohorts solved concurrently (engine
+                                         slots, one stream each), 1..16, 0 = 4     */
 } gba_options;
 
 /* Per-solve report, the subset of ceres::Solver::Summary the reference
@@ -336,6 +337,8 @@ typedef struct gba_server_stats {
   int32_t live, queued, peak_live;
   int64_t steps;                 /* batched LM iterations run */
   size_t device_bytes_in_use, device_bytes_peak;
+  int64_t reforms;               /* cohorts re-formed at an LM-iteration boundary
+                                    (finished members out, queued requests in) */
 } gba_server_stats;
 gba_status gba_server_get_stats(gba_handle *h, gba_server_stats *st);
 

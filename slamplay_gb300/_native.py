@@ -49,7 +49,7 @@ class Options(C.Structure):
         ("minimizer_progress_to_stdout", C.c_int32), ("device", C.c_int32), ("stream", C.c_void_p),
         ("chunk_observations", C.c_int32), ("reorder_points", C.c_int32), ("use_graphs", C.c_int32),
         ("pcg_unroll", C.c_int32), ("autotune", C.c_int32), ("schur", C.c_int32), ("persistent_pcg", C.c_int32),
-        ("camera_update", C.c_int32), ("lm_policy", C.c_int32), ("camera_layout", C.c_int32), ("reserved", C.c_int32 * 1),
+        ("camera_update", C.c_int32), ("lm_policy", C.c_int32), ("camera_layout", C.c_int32), ("server_slots", C.c_int32),
     ]
 
 
@@ -120,7 +120,7 @@ class ServerStats(C.Structure):
         ("submitted", C.c_int64), ("admitted", C.c_int64), ("completed", C.c_int64),
         ("rejected", C.c_int64), ("live", C.c_int32), ("queued", C.c_int32),
         ("peak_live", C.c_int32), ("steps", C.c_int64), ("device_bytes_in_use", C.c_size_t),
-        ("device_bytes_peak", C.c_size_t),
+        ("device_bytes_peak", C.c_size_t), ("reforms", C.c_int64),
     ]
 
 

@@ -119,7 +119,7 @@ gba_status gba_create(const gba_options *o, gba_handle **out) {
   if (opt.max_num_iterations < 0 || opt.max_linear_solver_iterations < 0 || opt.loss < 0 || opt.loss > 2 ||
       opt.precision < 0 || opt.precision > 1 || opt.schur < 0 || opt.schur > 2 ||
       opt.camera_update < 0 || opt.camera_update > 1 || opt.lm_policy < 0 || opt.lm_policy > 1 ||
-      opt.camera_layout < 0 || opt.camera_layout > 1 ||
+      opt.camera_layout < 0 || opt.camera_layout > 1 || opt.server_slots < 0 || opt.server_slots > 16 ||
       !(opt.initial_trust_region_radius > 0) ||
       !(opt.loss_scale > 0) || opt.max_num_consecutive_invalid_steps < 1) {
     g_create_error = "invalid solver options";

@@ -196,6 +196,12 @@ size_t Engine::layout(const HostBatch &hb, char *base, DeviceBatch *db, size_t *
   const bool rig = !hb.obs_rig.empty();
   b.obs_rig = cv.take<uint8_t>(rig ? no : 0);
   b.prob_rig = cv.take<double>(rig ? (size_t)kRig * P : 0);
+  const bool res = !hb.resume.empty();
+  b.prob_resume = cv.take<int32_t>(res ? P : 0);
+  b.lm_resume = cv.take<LMState>(res ? P : 0);
+  b.cam_scale_in = cv.take<double>(res ? 9 * nc : 0);
+  b.pt_scale_in = cv.take<double>(res ? 3 * np : 0);
+  if (!res) b.prob_resume = nullptr, b.lm_resume = nullptr, b.cam_scale_in = nullptr, b.pt_scale_in = nullptr;
   *upload_bytes = align_up(cv.off, 256);
   // download
   cv.off = *upload_bytes;
@@ -292,6 +298,7 @@ size_t Engine::layout(const HostBatch &hb, char *base, DeviceBatch *db, size_t *
   b.opt.g2o = o_.lm_policy == GBA_LM_POLICY_G2O ? 1 : 0;
   if (b.opt.g2o) b.opt.jacobi_scaling = 0;
   b.opt.max_bodies = max_lm_bodies();
+  b.opt.bodies_cap = 0;  // set per graph by the segment runs
   b.opt.pinhole = rig ? 1 : 0;
   b.lm_cond = 0;
   b.pcg_cond = 0;
@@ -403,6 +410,12 @@ gba_status Engine::upload(const HostBatch &hb, std::string *err) {
     sc.put(hdb.obs_rig, hb.obs_rig);
     sc.put(hdb.prob_rig, hb.prob_rig);
   }
+  if (!hb.resume.empty()) {
+    sc.put(hdb.prob_resume, hb.resume);
+    sc.put(hdb.lm_resume, hb.resume_lm);
+    sc.put(hdb.cam_scale_in, hb.resume_cam_scale);
+    sc.put(hdb.pt_scale_in, hb.resume_pt_scale);
+  }
   sc.put(hdb.cam_init, hb.cam_param);
   sc.put(hdb.pt_init, hb.pt_param);
   sc.run();
@@ -439,6 +452,11 @@ void Engine::destroy_graph() {
   exec_ = nullptr;
   graph_ = nullptr;
   graph_key_.clear();
+  if (exec_c_) cudaGraphExecDestroy(exec_c_);
+  if (graph_c_) cudaGraphDestroy(graph_c_);
+  exec_c_ = nullptr;
+  graph_c_ = nullptr;
+  graph_c_key_.clear();
 }
 
 // Profiling runs one launch at a time and waits for it, so the GPU is idle
@@ -582,28 +600,41 @@ void Engine::enqueue_lm_tail(cudaStream_t s) {
   prof_end(s, PF_POST, 0.0);
 }
 
-gba_status Engine::build_graph(std::string *err) {
-  destroy_graph();
+// The solve as one graph: setup, WHILE(LM) { head; PCG; tail }, gather.
+// cont: the continue graph of segment runs (counters zeroed, no setup).
+// With a segment length k the loop of one launch stops after k LM bodies
+// (k + 1 counted bodies with the setup's evaluation).
+gba_status Engine::build_graph(std::string *err, bool cont) {
+  cudaGraph_t &graph = cont ? graph_c_ : graph_;
+  cudaGraphExec_t &exec = cont ? exec_c_ : exec_;
+  if (exec) cudaGraphExecDestroy(exec);
+  if (graph) cudaGraphDestroy(graph);
+  exec = nullptr;
+  graph = nullptr;
   gba_status st;
   cudaGraphConditionalHandle lmh = 0, pcgh = 0;
-  if ((st = check(cudaGraphCreate(&graph_, 0), "cudaGraphCreate", err)) != GBA_OK) return st;
-  if ((st = check(cudaGraphConditionalHandleCreate(&lmh, graph_, 1, cudaGraphCondAssignDefault),
+  cudaGetLastError();  // the launches below report their own errors only
+  if ((st = check(cudaGraphCreate(&graph, 0), "cudaGraphCreate", err)) != GBA_OK) return st;
+  if ((st = check(cudaGraphConditionalHandleCreate(&lmh, graph, 1, cudaGraphCondAssignDefault),
                   "conditional handle", err)) != GBA_OK)
     return st;
+  const DeviceBatch saved = db_;
   db_.use_cond = 1;
   db_.lm_cond = lmh;
   db_.pcg_cond = 0;
+  db_.opt.bodies_cap = segment_bodies_ > 0 ? segment_bodies_ + (cont ? 0 : 1) : 0;
   const bool prof = profiling_;
   profiling_ = false;
+  // a failed build: the captures are ended and the graph is dropped, not
+  // destroyed (a capture that failed may have left it unusable)
   auto fail = [&](cudaError_t e, const char *what) {
     profiling_ = prof;
     end_captures();
     cudaGetLastError();
     const gba_status r = check(e, what, err);
-    destroy_graph();
-    db_.use_cond = 0;
-    db_.lm_cond = 0;
-    db_.pcg_cond = 0;
+    exec = nullptr;
+    graph = nullptr;
+    db_ = saved;
     return r;
   };
   auto add_while = [&](cudaStream_t s, cudaGraphConditionalHandle h, cudaGraph_t *body) -> cudaError_t {
@@ -625,9 +656,12 @@ gba_status Engine::build_graph(std::string *err) {
     return cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
   };
   // setup, then WHILE(LM) { head; WHILE(PCG) { mat-vec; camera side } tail }, then gather
-  cudaError_t e = cudaStreamBeginCaptureToGraph(stream_, graph_, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+  cudaError_t e = cudaStreamBeginCaptureToGraph(stream_, graph, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) return fail(e, "capture setup");
-  enqueue_setup(stream_);
+  if (cont)
+    zero_counters(stream_);
+  else
+    enqueue_setup(stream_);
   cudaGraph_t lmbody = nullptr, pcgbody = nullptr, tmp = nullptr;
   if ((e = add_while(stream_, lmh, &lmbody)) != cudaSuccess) return fail(e, "LM conditional node");
   // (a conditional handle must belong to a node: none for the cluster PCG)
@@ -664,19 +698,29 @@ gba_status Engine::build_graph(std::string *err) {
   if ((e = cudaStreamEndCapture(cap_[0], &tmp)) != cudaSuccess) return fail(e, "end capture LM body");
   enqueue_gather(stream_);
   if ((e = cudaStreamEndCapture(stream_, &tmp)) != cudaSuccess) return fail(e, "end capture");
-  if ((e = cudaGraphInstantiate(&exec_, graph_, 0)) != cudaSuccess) return fail(e, "cudaGraphInstantiate");
+  if ((e = cudaGraphInstantiate(&exec, graph, 0)) != cudaSuccess) return fail(e, "cudaGraphInstantiate");
   profiling_ = prof;
-  graph_key_ = cur_key_;
+  if (cont) {
+    graph_c_key_ = cur_key_;
+    graph_c_segment_ = segment_bodies_;
+  } else {
+    graph_key_ = cur_key_;
+    graph_segment_ = segment_bodies_;
+  }
+  db_ = saved;
   return GBA_OK;
 }
 
+// Ends the captures a failed graph build left open.  Every capture goes
+// into a graph that is already owned (the graph being built, or a body of
+// one of its conditional nodes), so nothing returned here is destroyed: the
+// caller destroys the graph being built, which owns the bodies.
 void Engine::end_captures() {
   cudaStreamCaptureStatus cs;
   for (cudaStream_t s : {cap_[1], cap_[0], stream_}) {
     if (cudaStreamIsCapturing(s, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) {
       cudaGraph_t g = nullptr;
       cudaStreamEndCapture(s, &g);
-      if (g && g != graph_) cudaGraphDestroy(g);
     }
   }
 }
@@ -789,7 +833,7 @@ gba_status Engine::run_solve(std::string *err) {
   gba_status st;
   if ((st = check(cudaEventRecord(ev_start_, stream_), "event", err)) != GBA_OK) return st;
   if (o_.use_graphs && !profiling_) {
-    if (!exec_ || graph_key_ != cur_key_) {
+    if (!exec_ || graph_key_ != cur_key_ || graph_segment_ != segment_bodies_) {
       st = build_graph(err);
       if (st != GBA_OK && pdl_) {
         pdl_ = false;  // a driver without programmatic edges in conditional bodies
@@ -802,6 +846,128 @@ gba_status Engine::run_solve(std::string *err) {
     if ((st = run_host_driven(err)) != GBA_OK) return st;
   }
   return check(cudaEventRecord(ev_stop_, stream_), "event", err);
+}
+
+gba_status Engine::run_segment(bool cont, std::string *err) {
+  if (!cont) return run_solve(err);
+  gba_status st;
+  if (!exec_c_ || graph_c_key_ != cur_key_ || graph_c_segment_ != segment_bodies_) {
+    st = build_graph(err, true);
+    if (st != GBA_OK && pdl_) {
+      pdl_ = false;
+      st = build_graph(err, true);
+    }
+    if (st != GBA_OK) return st;
+  }
+  return check(cudaGraphLaunch(exec_c_, stream_), "cudaGraphLaunch", err);
+}
+
+gba_status Engine::fetch_states(std::string *err) {
+  const size_t off = reinterpret_cast<char *>(db_.lm) - d_arena_;
+  const size_t soff = reinterpret_cast<char *>(db_.status) - d_arena_;
+  gba_status st = check(cudaMemcpyAsync(h_stage_ + off, db_.lm, sizeof(LMState) * (size_t)db_.num_problems,
+                                        cudaMemcpyDeviceToHost, stream_),
+                        "state read", err);
+  if (st != GBA_OK) return st;
+  return check(cudaMemcpyAsync(h_stage_ + soff, db_.status, 8 * sizeof(int32_t), cudaMemcpyDeviceToHost, stream_),
+               "status read", err);
+}
+
+const LMState *Engine::states(const HostBatch &hb) {
+  (void)hb;
+  return reinterpret_cast<const LMState *>(h_stage_ + (reinterpret_cast<char *>(db_.lm) - d_arena_));
+}
+
+// The device-side error word of the batch (as last downloaded or fetched).
+gba_status Engine::device_status(std::string *err) {
+  const int32_t s0 = *reinterpret_cast<const int32_t *>(h_stage_ + (reinterpret_cast<char *>(db_.status) - d_arena_));
+  if (s0 == GBA_ERR_TIMEOUT) {
+    *err = "a bounded device-side wait of the grid PCG ran out (the solve was stopped)";
+    return GBA_ERR_TIMEOUT;
+  }
+  if (s0 != 0) {
+    *err = "device-side loop guard tripped (internal error)";
+    return GBA_ERR_INTERNAL;
+  }
+  return GBA_OK;
+}
+
+void Engine::summarize(const DeviceBatch &hdb, int p, double solve_s, gba_summary *out) {
+  const LMState &L = hdb.lm[p];
+  gba_summary &S = *out;
+  S.initial_cost = L.initial_cost;
+  S.final_cost = L.x_cost;
+  S.num_iterations = L.iteration;
+  S.num_successful_steps = L.successful_steps;
+  S.num_unsuccessful_steps = L.unsuccessful_steps;
+  S.num_invalid_steps = L.invalid_steps;
+  S.num_linear_solver_iterations = L.total_pcg_iterations;
+  S.termination_type = L.termination_type < 0 ? GBA_TERMINATION_NO_CONVERGENCE : L.termination_type;
+  S.termination_reason = L.termination_reason;
+  S.final_trust_region_radius = L.radius;
+  S.gradient_max_norm = L.gradient_max_norm;
+  S.solve_time_s = solve_s;
+  const int n = std::min(L.iteration + 1, trace_cap_);
+  S.trace_length = std::min(n, S.trace_capacity > 0 ? S.trace_capacity : 0);
+  for (int k = 0; k < S.trace_length; ++k) {
+    const size_t i = (size_t)p * trace_cap_ + k;
+    if (S.trace_cost) S.trace_cost[k] = hdb.trace_cost[i];
+    if (S.trace_radius) S.trace_radius[k] = hdb.trace_radius[i];
+    if (S.trace_linear_iterations) S.trace_linear_iterations[k] = hdb.trace_pcg[i];
+    if (S.trace_successful) S.trace_successful[k] = hdb.trace_succ[i];
+  }
+}
+
+gba_status Engine::deliver(const HostBatch &hb, const std::vector<int> &probs, const gba_problem_view *v,
+                           gba_summary *s, std::string *err) {
+  if (probs.empty()) return GBA_OK;
+  const size_t cam_off = download_off_;
+  const size_t pt_off = download_off_ + align_up(sizeof(double) * 9 * (size_t)hb.nc, 256);
+  gba_status st;
+  for (int p : probs) {
+    const ProblemInfo &pi = hb.prob[p];
+    const size_t oc = cam_off + sizeof(double) * 9 * (size_t)pi.cam_begin;
+    const size_t op = pt_off + sizeof(double) * 4 * (size_t)pi.pt_begin;
+    if ((st = check(cudaMemcpyAsync(h_stage_ + oc, d_arena_ + oc, sizeof(double) * 9 * (size_t)pi.cam_count,
+                                    cudaMemcpyDeviceToHost, stream_),
+                    "result read", err)) != GBA_OK ||
+        (st = check(cudaMemcpyAsync(h_stage_ + op, d_arena_ + op, sizeof(double) * 4 * (size_t)pi.pt_count,
+                                    cudaMemcpyDeviceToHost, stream_),
+                    "result read", err)) != GBA_OK)
+      return st;
+  }
+  if ((st = check(cudaStreamSynchronize(stream_), "solver kernels", err)) != GBA_OK) return st;
+  DeviceBatch hdb{};
+  size_t ub, doff, dbytes;
+  layout(hb, h_stage_, &hdb, &ub, &doff, &dbytes);
+  const double *out_cam = reinterpret_cast<const double *>(h_stage_ + cam_off);
+  const double *out_pt = reinterpret_cast<const double *>(h_stage_ + pt_off);
+  for (int p : probs) {
+    if (v[p].parameters) scatter_parameters(hb, p, out_cam, out_pt, v[p].parameters);
+    if (s) summarize(hdb, p, 0.0, &s[p]);
+  }
+  return GBA_OK;
+}
+
+gba_status Engine::download_states(const HostBatch &hb, std::vector<ProblemState> *out, std::string *err) {
+  std::vector<double> cs(9 * (size_t)hb.nc), ps(3 * (size_t)hb.np);
+  gba_status st;
+  if (hb.nc && (st = check(cudaMemcpyAsync(cs.data(), db_.cam_scale, cs.size() * sizeof(double),
+                                           cudaMemcpyDeviceToHost, stream_),
+                           "scale read", err)) != GBA_OK)
+    return st;
+  if (hb.np && (st = check(cudaMemcpyAsync(ps.data(), db_.pt_scale, ps.size() * sizeof(double),
+                                           cudaMemcpyDeviceToHost, stream_),
+                           "scale read", err)) != GBA_OK)
+    return st;
+  if ((st = check(cudaStreamSynchronize(stream_), "scale read", err)) != GBA_OK) return st;
+  const LMState *lm = states(hb);
+  out->resize((size_t)hb.P);
+  for (int p = 0; p < hb.P; ++p) {
+    (*out)[p].lm = lm[p];
+    gather_scales(hb, p, cs.data(), ps.data(), &(*out)[p]);
+  }
+  return GBA_OK;
 }
 
 gba_status Engine::download(const HostBatch &hb, const gba_problem_view *v, gba_summary *s, std::string *err) {
@@ -831,30 +997,7 @@ gba_status Engine::download(const HostBatch &hb, const gba_problem_view *v, gba_
       reinterpret_cast<const double *>(h_stage_ + download_off_ + align_up(sizeof(double) * 9 * (size_t)hb.nc, 256));
   for (int p = 0; p < hb.P; ++p) {
     if (v[p].parameters) scatter_parameters(hb, p, out_cam, out_pt, v[p].parameters);
-    if (!s) continue;
-    const LMState &L = hdb.lm[p];
-    gba_summary &S = s[p];
-    S.initial_cost = L.initial_cost;
-    S.final_cost = L.x_cost;
-    S.num_iterations = L.iteration;
-    S.num_successful_steps = L.successful_steps;
-    S.num_unsuccessful_steps = L.unsuccessful_steps;
-    S.num_invalid_steps = L.invalid_steps;
-    S.num_linear_solver_iterations = L.total_pcg_iterations;
-    S.termination_type = L.termination_type < 0 ? GBA_TERMINATION_NO_CONVERGENCE : L.termination_type;
-    S.termination_reason = L.termination_reason;
-    S.final_trust_region_radius = L.radius;
-    S.gradient_max_norm = L.gradient_max_norm;
-    S.solve_time_s = ms * 1e-3;
-    const int n = std::min(L.iteration + 1, trace_cap_);
-    S.trace_length = std::min(n, S.trace_capacity > 0 ? S.trace_capacity : 0);
-    for (int k = 0; k < S.trace_length; ++k) {
-      const size_t i = (size_t)p * trace_cap_ + k;
-      if (S.trace_cost) S.trace_cost[k] = hdb.trace_cost[i];
-      if (S.trace_radius) S.trace_radius[k] = hdb.trace_radius[i];
-      if (S.trace_linear_iterations) S.trace_linear_iterations[k] = hdb.trace_pcg[i];
-      if (S.trace_successful) S.trace_successful[k] = hdb.trace_succ[i];
-    }
+    if (s) summarize(hdb, p, ms * 1e-3, &s[p]);
   }
   return GBA_OK;
 }

@@ -49,6 +49,26 @@ class Engine {
   // Prepared-batch level entry points (used by the serving loop).
   gba_status upload(const HostBatch &hb, std::string *err);
   gba_status run_solve(std::string *err);
+  // Segment runs (the serving loop): at most `lm_bodies` LM iterations a
+  // launch (0 = to the end); run_segment(false) starts the uploaded batch
+  // (setup, then the loop), run_segment(true) continues it from the device
+  // state.  fetch_states() queues the copy of the problems' LM states to the
+  // host staging area, states() reads them once the stream has passed it.
+  void set_segment(int lm_bodies) { segment_bodies_ = std::max(0, lm_bodies); }
+  gba_status run_segment(bool cont, std::string *err);
+  gba_status fetch_states(std::string *err);
+  const LMState *states(const HostBatch &hb);
+  // The batch's device-side error word as fetched (GBA_OK when clear).
+  gba_status device_status(std::string *err);
+  // Once the stream has passed a segment: the parameters of problems
+  // `probs` into their views (their current point; for a finished problem
+  // its result) and, if s, their summaries from the fetched LM states.  The
+  // batch stays on the device.
+  gba_status deliver(const HostBatch &hb, const std::vector<int> &probs, const gba_problem_view *v, gba_summary *s,
+                     std::string *err);
+  // Each problem's state for a resumed upload: the fetched LM state and the
+  // Jacobi scales in user order.
+  gba_status download_states(const HostBatch &hb, std::vector<ProblemState> *out, std::string *err);
   // Re-runs the last uploaded batch from its initial point (device only,
   // asynchronous on the handle's stream).
   gba_status rerun(std::string *err);
@@ -58,7 +78,8 @@ class Engine {
   gba_status ensure_capacity(size_t dev_bytes, size_t host_bytes, std::string *err);
   size_t layout(const HostBatch &hb, char *dbase, DeviceBatch *db, size_t *upload_bytes,
                 size_t *download_off, size_t *download_bytes);
-  gba_status build_graph(std::string *err);
+  gba_status build_graph(std::string *err, bool cont = false);
+  void summarize(const DeviceBatch &hdb, int p, double solve_s, gba_summary *out);
   void end_captures();
   void enqueue_gather(cudaStream_t s);
   void destroy_graph();
@@ -89,6 +110,12 @@ class Engine {
   cudaGraph_t graph_ = nullptr;
   cudaGraphExec_t exec_ = nullptr;
   std::vector<long long> graph_key_;
+  // the continue graph (no setup) of segment runs, and the segment length
+  cudaGraph_t graph_c_ = nullptr;
+  cudaGraphExec_t exec_c_ = nullptr;
+  std::vector<long long> graph_c_key_;
+  int segment_bodies_ = 0;
+  int graph_segment_ = -1, graph_c_segment_ = -1;
   std::vector<long long> cur_key_;
   // events
   cudaEvent_t ev_start_ = nullptr, ev_stop_ = nullptr;

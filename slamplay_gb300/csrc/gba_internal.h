@@ -52,6 +52,8 @@ struct DeviceOptions {
   int32_t g2o;       // g2o's Levenberg policy (else Ceres' trust region)
   int32_t max_bodies;  // LM bodies (trials) a solve may run
   int32_t pinhole;     // local-BA windows: the stereo-rig pinhole model, SE3 poses
+  int32_t bodies_cap;  // > 0: the LM loop of one launch stops after this many counted bodies
+                       // (the problems stay active; a later launch continues them)
 };
 
 // Per problem of a local-BA batch: fx, fy, cx, cy, then R (9, row-major) and
@@ -87,6 +89,8 @@ struct LMState {
   int32_t successful_steps, unsuccessful_steps, invalid_steps, invalid_run;
   int32_t pcg_active, pcg_iterations, linear_ok, last_linear_ok;
   int32_t trials, outer;  // g2o policy: trials of this iteration, iterations done
+  int32_t resumed;        // 1 from a resumed upload until its first evaluation
+  int32_t pad_;
   int64_t total_pcg_iterations;
 };
 
@@ -203,6 +207,13 @@ struct DeviceBatch {
   // directions alternate between pcg_p and pcg_p2 by iteration parity) and
   // its control words (kGrid* slots), zeroed by K3b before each launch
   double *pcg_p2;            // 9 * nc
+  // a resumed batch (a problem continued in a new batch at an LM-iteration
+  // boundary): per problem a flag and the LM state to continue from, per
+  // camera / point the Jacobi scales of its first evaluation (internal
+  // order); all null when no problem of the batch is resumed
+  const int32_t *prob_resume;
+  const LMState *lm_resume;
+  const double *cam_scale_in, *pt_scale_in;
   double *pq_row;            // 9 * nc: each row's p_i q_i, [row of the camera][camera of the problem]
   uint32_t *grid_ctl;        // 8
 };

@@ -36,6 +36,15 @@ __global__ void k_init_state(DeviceBatch B) {
   L.parity = 0;
   L.linear_ok = 1;
   L.last_linear_ok = 1;
+  if (B.prob_resume && B.prob_resume[p]) {
+    // a problem continued from an LM-iteration boundary of another batch:
+    // its state as it was, the Jacobian to be evaluated again at its current
+    // point (uploaded as this batch's initial point)
+    L = B.lm_resume[p];
+    L.need_jacobian = 1;
+    L.parity = 0;
+    L.resumed = 1;
+  }
   B.lm[p] = L;
 }
 
@@ -623,13 +632,15 @@ __global__ void k_scale_init(DeviceBatch B) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t ncam = 9 * (int64_t)B.nc, npt = 3 * (int64_t)B.np;
   if (i < ncam) {
-    B.cam_scale[i] = B.opt.jacobi_scaling ? 1.0 / (1.0 + sqrt(B.cam_colnorm[i])) : 1.0;
+    const bool res = B.prob_resume && B.prob_resume[B.cam_problem[i / 9]];
+    B.cam_scale[i] = res ? B.cam_scale_in[i] : B.opt.jacobi_scaling ? 1.0 / (1.0 + sqrt(B.cam_colnorm[i])) : 1.0;
     const DF d = df_from_double(B.cam_scale[i]);
     B.cam_scalef[i] = d.hi;
     B.cam_scaledf[i] = make_float2(d.hi, d.lo);
   } else if (i < ncam + npt) {
     const int64_t k = i - ncam;
-    B.pt_scale[k] = B.opt.jacobi_scaling ? 1.0 / (1.0 + sqrt(B.pt_colnorm[k])) : 1.0;
+    const bool res = B.prob_resume && B.prob_resume[B.pt_problem[k / 3]];
+    B.pt_scale[k] = res ? B.pt_scale_in[k] : B.opt.jacobi_scaling ? 1.0 / (1.0 + sqrt(B.pt_colnorm[k])) : 1.0;
     const DF d = df_from_double(B.pt_scale[k]);
     B.pt_scalef[k] = d.hi;
     B.pt_scaledf[k] = make_float2(d.hi, d.lo);
@@ -657,7 +668,10 @@ __device__ void finish_lm_body(const DeviceBatch &B, bool count_body) {
         any = 0;
       }
       B.status[1] = any;
-      if (B.use_cond && B.lm_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)B.lm_cond, any ? 1u : 0u);
+      // a segment run stops its loop after bodies_cap counted bodies; the
+      // problems stay active for the next launch
+      const bool more = any && !(B.opt.bodies_cap > 0 && bodies >= (uint32_t)B.opt.bodies_cap);
+      if (B.use_cond && B.lm_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)B.lm_cond, more ? 1u : 0u);
     }
   }
 }
@@ -693,13 +707,18 @@ __global__ void __launch_bounds__(256) k_post_eval(DeviceBatch B, int count_body
     }
     if (threadIdx.x == 0) {
       const DeviceOptions &o = B.opt;
-      if (o.g2o && L->iteration == 0) L->radius = 1.0 / (kG2oTau * fmax(hmax[0], hmax[1]));
+      const bool resumed = L->resumed != 0;
+      if (o.g2o && L->iteration == 0 && !resumed) L->radius = 1.0 / (kG2oTau * fmax(hmax[0], hmax[1]));
       L->need_jacobian = 0;
       L->x_cost = cost;
       L->gradient_max_norm = fmax(gp, gc);
       L->x_norm = sqrt(xc + xp);
+      L->resumed = 0;
       const int it = L->iteration;
-      if (bad != 0.0 || !isfinite(cost)) {
+      if (resumed) {
+        // the state was carried over at an LM-iteration boundary: the same
+        // point evaluated again (the same bits), nothing else to decide
+      } else if (bad != 0.0 || !isfinite(cost)) {
         L->active = 0;
         L->termination_type = GBA_TERMINATION_FAILURE;
         L->termination_reason = GBA_REASON_EVALUATION_FAILED;

@@ -488,7 +488,7 @@ bool pcg_cluster_plan(const ProblemInfo *prob, int num_problems, const int32_t *
   if ((long long)num_problems * cs <= sms && cl_layout(n_max, own, mb).total <= (size_t)optin) cache = mb;
   const ClLayout l = cl_layout(n_max, own, cache);
   if (l.total > (size_t)optin) return false;
-  if (cudaFuncSetAttribute(k_pcg_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)l.total) != cudaSuccess ||
+  if (raise_smem_limit((const void *)k_pcg_cluster, l.total) != cudaSuccess ||
       (cs > 8 && cudaFuncSetAttribute(k_pcg_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)) {
     cudaGetLastError();
     return false;

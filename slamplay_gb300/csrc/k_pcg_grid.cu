@@ -725,7 +725,7 @@ bool pcg_grid_plan(int num_problems, bool mixed, bool explicit_schur, int nc, co
   const bool cache = cap > 0 && fits(cap, true, cap_pairs);
   while (!cache && cap > 0 && !fits(cap, false, cap_pairs)) cap = cap * 3 / 4;
   const size_t smem = grid_smem(nc, cap, cache, cap_pairs).total;
-  if (cudaFuncSetAttribute(k_pcg_grid, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+  if (raise_smem_limit((const void *)k_pcg_grid, smem) != cudaSuccess) {
     cudaGetLastError();
     return false;
   }

@@ -339,7 +339,10 @@ cudaError_t launch_schur_spmv(const DeviceBatch &b, bool mixed, cudaStream_t s, 
   if (mixed) return cudaLaunchKernelEx(&cfg, k_schur_spmv<true>, b);
   size_t smem = 0;
   const int rpp = spmv64_rows(b.sblk_max, &smem);
-  if (smem > 48 * 1024) cudaFuncSetAttribute(k_schur_spmv64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (smem > 48 * 1024) {
+    const cudaError_t e = raise_smem_limit((const void *)k_schur_spmv64, smem);
+    if (e != cudaSuccess) return e;
+  }
   cfg.dynamicSmemBytes = smem;
   return cudaLaunchKernelEx(&cfg, k_schur_spmv64, b, rpp);
 }

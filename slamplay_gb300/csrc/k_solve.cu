@@ -19,7 +19,10 @@
 //  K6  k_decide          per problem: Ceres' accept / reject / radius update
 #include <cuda_runtime.h>
 
+#include <map>
+#include <mutex>
 #include <type_traits>
+#include <utility>
 
 #include "kernels.cuh"
 #include "kernels.h"
@@ -552,6 +555,20 @@ void launch_camera_schur(const DeviceBatch &b, bool mixed, cudaStream_t s) {
     k_camera_schur<true><<<b.nc, kSchurThreads, 0, s>>>(b);
   else
     k_camera_schur<false><<<b.nc, kSchurThreads, 0, s>>>(b);
+}
+
+cudaError_t raise_smem_limit(const void *func, size_t bytes) {
+  static std::mutex mu;
+  static auto *limits = new std::map<std::pair<const void *, int>, size_t>;  // never destroyed
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> g(mu);
+  size_t &cur = (*limits)[{func, dev}];
+  if (bytes <= cur) return cudaSuccess;
+  e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess) cur = bytes;
+  return e;
 }
 
 // Large dynamic shared memory of the point-Schur kernel (FP64 form).

@@ -71,6 +71,11 @@ cudaError_t launch_schur_matvec(const DeviceBatch &b, bool mixed, cudaStream_t s
 cudaError_t launch_pcg_camera(const DeviceBatch &b, bool mixed, cudaStream_t s, bool pdl);
 void launch_prof_delay(cudaStream_t s);
 void point_schur_init();
+// Raises a kernel's dynamic shared memory limit on the current device to at
+// least `bytes`, never lowering it: the limit is process-wide, and several
+// engines (the serving slots) plan and capture launches of the same kernel
+// with different sizes at different times.
+cudaError_t raise_smem_limit(const void *func, size_t bytes);
 // Kernel attributes of the PCG kernels (once per device).
 void pcg_init();
 // K5: point back-substitution, model cost change, candidate points.

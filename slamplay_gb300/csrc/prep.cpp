@@ -384,6 +384,10 @@ void HostBatch::reset() {
   cam_used.clear();
   obs_rig.clear();
   prob_rig.clear();
+  resume.clear();
+  resume_lm.clear();
+  resume_cam_scale.clear();
+  resume_pt_scale.clear();
   prob.clear();
   chunk.clear();
   camblk.clear();
@@ -755,6 +759,34 @@ gba_status prepare_batch(const gba_problem_view *views, int n, const PrepOptions
   }
   if (hb.explicit_schur) build_schur_structure(&hb);
   return GBA_OK;
+}
+
+void set_resume(HostBatch &hb, int p, const ProblemState &st) {
+  if (hb.resume.empty()) {
+    hb.resume.assign((size_t)hb.P, 0);
+    hb.resume_lm.assign((size_t)hb.P, LMState{});
+    hb.resume_cam_scale.assign(9 * (size_t)hb.nc, 1.0);
+    hb.resume_pt_scale.assign(3 * (size_t)hb.np, 1.0);
+  }
+  const ProblemInfo &pi = hb.prob[p];
+  hb.resume[p] = 1;
+  hb.resume_lm[p] = st.lm;
+  std::copy(st.cam_scale.begin(), st.cam_scale.begin() + 9 * (size_t)pi.cam_count,
+            hb.resume_cam_scale.begin() + 9 * (size_t)pi.cam_begin);
+  for (int ji = 0; ji < pi.pt_count; ++ji) {
+    const int j = hb.pt_orig[pi.pt_begin + ji];
+    for (int q = 0; q < 3; ++q) hb.resume_pt_scale[3 * (size_t)(pi.pt_begin + ji) + q] = st.pt_scale[3 * (size_t)j + q];
+  }
+}
+
+void gather_scales(const HostBatch &hb, int p, const double *cam_scale, const double *pt_scale, ProblemState *st) {
+  const ProblemInfo &pi = hb.prob[p];
+  st->cam_scale.assign(cam_scale + 9 * (size_t)pi.cam_begin, cam_scale + 9 * (size_t)(pi.cam_begin + pi.cam_count));
+  st->pt_scale.assign(3 * (size_t)pi.pt_count, 1.0);
+  for (int ji = 0; ji < pi.pt_count; ++ji) {
+    const int j = hb.pt_orig[pi.pt_begin + ji];
+    for (int q = 0; q < 3; ++q) st->pt_scale[3 * (size_t)j + q] = pt_scale[3 * (size_t)(pi.pt_begin + ji) + q];
+  }
 }
 
 void scatter_parameters(const HostBatch &hb, int p, const double *cam_param, const double *pt_param,

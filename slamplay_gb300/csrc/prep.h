@@ -51,6 +51,12 @@ struct HostBatch {
   // observation, and per problem fx, fy, cx, cy, then (R, t) of E_0 and E_1
   std::vector<uint8_t> obs_rig;
   std::vector<double> prob_rig;   // kRig per problem
+  // resumed problems (set_resume; empty when none): per problem a flag and
+  // the LM state to continue from, the Jacobi scales in the internal layout
+  std::vector<int32_t> resume;
+  std::vector<LMState> resume_lm;
+  std::vector<double> resume_cam_scale;  // 9 per camera
+  std::vector<double> resume_pt_scale;   // 3 per point
   // Starts a new batch: counts, offsets and appended arrays emptied; the
   // arrays prepare_batch overwrites entirely keep their size and storage (a
   // handle re-preparing problems of similar size neither touches fresh
@@ -72,6 +78,19 @@ gba_status prepare_batch(const gba_problem_view *views, int n, const PrepOptions
 
 // Checks one problem view (sizes, pointers, indices, finiteness).
 gba_status validate_problem(const gba_problem_view *v, std::string *err);
+
+// The state of a problem at an LM-iteration boundary, enough to continue its
+// solve in another batch with the same bits: the LM state and the Jacobi
+// scales of its first evaluation (user order: 9 per camera, 3 per point);
+// its current parameters are the problem view's.
+struct ProblemState {
+  LMState lm;
+  std::vector<double> cam_scale, pt_scale;
+};
+// Marks problem p of a prepared batch as resumed from `st`.
+void set_resume(HostBatch &hb, int p, const ProblemState &st);
+// Maps the internal-layout scales of problem p to user order.
+void gather_scales(const HostBatch &hb, int p, const double *cam_scale, const double *pt_scale, ProblemState *st);
 
 // Writes the internal-layout parameters of problem p back to the caller's array.
 void scatter_parameters(const HostBatch &hb, int p, const double *cam_param, const double *pt_param,

@@ -1,12 +1,19 @@
-// server.cpp — continuous batching: requests arrive at any time; the loop
-// admits queued requests into a free engine slot as long as their estimated
-// device footprint fits the remaining budget and the live-problem cap, lays
-// them out as one batch (problems batched per LM iteration inside one CUDA
-// graph), and launches it on the slot's own stream while other slots are
-// still running, so cohorts overlap on the device.  A finished cohort is
-// retired (results written back, memory budget returned) as soon as its
-// completion event fires.  Each problem's arithmetic depends only on the
-// problem, never on its cohort, so a result is the same alone and in the mix.
+// server.cpp — continuous batching at LM-iteration granularity.  Requests
+// arrive at any time.  A cohort (the problems of one engine slot, laid out
+// as one batch of at most kCohortObs observations) runs one LM iteration
+// per launch on the slot's own stream, the cohorts of the slots overlapping
+// on the device.  Free slots take queued requests as new cohorts.  At each
+// iteration boundary the loop reads the members' LM states: members that
+// finished get their results at once (their parameters and summaries are
+// copied out while the batch stays on the device).  When queued requests
+// are waiting, no slot is free and the change is worth a re-layout (the
+// finished members and the joining requests are at least 1/kReformDiv of
+// the cohort), the cohort is re-formed: finished members leave, queued
+// requests join, and the members still running continue in the new batch
+// from their exact state (LM state, Jacobi scales, current point), so a
+// request joins a running batch at an LM-iteration boundary and every
+// result keeps the bits of the problem solved alone.  Otherwise the cohort
+// continues on the device (a graph without the setup).
 #include "server.h"
 
 #include <algorithm>
@@ -19,7 +26,10 @@ namespace {
 double now_s() {
   return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
-constexpr int kSlots = 4;
+constexpr int kDefaultSlots = 4;
+constexpr int kSegmentBodies = 1;            // LM iterations a cohort runs between boundaries
+constexpr long long kCohortObs = 1LL << 22;  // observations a cohort takes in (one request more if alone)
+constexpr int kReformDiv = 4;                // re-form when leavers + joiners >= 1/kReformDiv of the cohort
 }  // namespace
 
 size_t Server::estimate_footprint(int nc, int np, int no, bool mixed, bool explicit_bound) {
@@ -129,65 +139,215 @@ void Server::stats(gba_server_stats *out) {
   *out = st_;
 }
 
-bool Server::launch_cohort(Slot &s, std::vector<std::shared_ptr<Request>> &&reqs) {
-  s.reqs = std::move(reqs);
+auto Server::take_queued(long long max_obs, size_t *bytes) -> std::vector<std::shared_ptr<Request>> {
+  std::vector<std::shared_ptr<Request>> take;
+  *bytes = 0;
+  long long obs = 0;
+  std::lock_guard<std::mutex> lk(mu_);
+  while (!queue_.empty()) {
+    const auto &r = queue_.front();
+    if (st_.live + (int)take.size() >= max_live_) break;
+    if (st_.device_bytes_in_use + *bytes + r->footprint > budget_) break;
+    if (!take.empty() && obs + r->view.num_observations > max_obs) break;
+    *bytes += r->footprint;
+    obs += r->view.num_observations;
+    take.push_back(r);
+    queue_.pop_front();
+  }
+  if (!take.empty()) {
+    st_.live += (int32_t)take.size();
+    st_.peak_live = std::max(st_.peak_live, st_.live);
+    st_.admitted += (int64_t)take.size();
+    st_.device_bytes_in_use += *bytes;
+    st_.device_bytes_peak = std::max(st_.device_bytes_peak, st_.device_bytes_in_use);
+    st_.queued = (int32_t)queue_.size();
+  }
+  return take;
+}
+
+int Server::peek_queued(long long max_obs, long long *obs) {
+  std::lock_guard<std::mutex> lk(mu_);
+  int n = 0;
+  size_t bytes = 0;
+  *obs = 0;
+  for (const auto &r : queue_) {
+    if (st_.live + n >= max_live_) break;
+    if (st_.device_bytes_in_use + bytes + r->footprint > budget_) break;
+    if (*obs + r->view.num_observations > max_obs) break;
+    bytes += r->footprint;
+    *obs += r->view.num_observations;
+    ++n;
+  }
+  return n;
+}
+
+bool Server::launch_cohort(Slot &s, std::vector<std::shared_ptr<Request>> &&keep, std::vector<double> &&keep_t,
+                           const std::vector<ProblemState> &states, std::vector<std::shared_ptr<Request>> &&fresh) {
+  const double t = now_s();
+  s.reqs = std::move(keep);
+  s.t_start = std::move(keep_t);
+  const size_t nkeep = s.reqs.size();
+  for (auto &r : fresh) {
+    s.reqs.push_back(r);
+    s.t_start.push_back(t);
+  }
+  s.delivered.assign(s.reqs.size(), 0);
   s.views.clear();
   for (auto &r : s.reqs) s.views.push_back(r->view);
   std::string err;
   const PrepOptions po = s.engine->prep_options();
   gba_status st = prepare_batch(s.views.data(), (int)s.views.size(), po, &s.hb, &err);
+  if (st == GBA_OK)
+    for (size_t i = 0; i < nkeep; ++i) set_resume(s.hb, (int)i, states[i]);
   if (st == GBA_OK) st = s.engine->upload(s.hb, &err);
-  if (st == GBA_OK) st = s.engine->run_solve(&err);
+  if (st == GBA_OK) st = s.engine->run_segment(false, &err);
+  if (st == GBA_OK) st = s.engine->fetch_states(&err);
   if (st == GBA_OK && cudaEventRecord(s.done_ev, s.engine->stream()) != cudaSuccess) {
     st = GBA_ERR_CUDA;
     err = "event record";
   }
   if (st != GBA_OK) {
-    std::lock_guard<std::mutex> lk(mu_);
-    for (auto &r : s.reqs) {
-      r->status = st;
-      r->error = err;
-      r->done = true;
-      ++st_.completed;
-    }
-    s.reqs.clear();
-    done_cv_.notify_all();
+    fail_cohort(s, st, err);
     return false;
   }
   s.busy = true;
-  s.t_start = now_s();
+  std::lock_guard<std::mutex> lk(mu_);
+  ++st_.steps;
   return true;
 }
 
-void Server::retire(Slot &s) {
-  std::string err;
-  std::vector<gba_summary> sums(s.reqs.size());
-  for (auto &x : sums) std::memset(&x, 0, sizeof x);
-  const gba_status st = s.engine->download(s.hb, s.views.data(), sums.data(), &err);
-  const double t = now_s();
+// Every member not yet delivered fails with `st`; the slot is emptied.
+void Server::fail_cohort(Slot &s, gba_status st, const std::string &err) {
   std::lock_guard<std::mutex> lk(mu_);
   for (size_t i = 0; i < s.reqs.size(); ++i) {
+    if (i < s.delivered.size() && s.delivered[i]) continue;
     Request &r = *s.reqs[i];
-    r.summary = sums[i];
-    r.summary.total_time_s = t - s.t_start;
     r.status = st;
     r.error = err;
     r.done = true;
     ++st_.completed;
+    --st_.live;
   }
-  st_.live -= (int32_t)s.reqs.size();
   st_.device_bytes_in_use -= s.bytes;
   s.reqs.clear();
+  s.views.clear();
+  s.t_start.clear();
+  s.delivered.clear();
   s.busy = false;
   s.bytes = 0;
   done_cv_.notify_all();
+}
+
+void Server::finish(Slot &s, const std::vector<int> &members, const std::vector<gba_summary> &sums) {
+  const double t = now_s();
+  std::lock_guard<std::mutex> lk(mu_);
+  for (int i : members) {
+    Request &r = *s.reqs[i];
+    r.summary = sums[i];
+    r.summary.total_time_s = t - s.t_start[i];
+    r.summary.solve_time_s = r.summary.total_time_s;
+    r.status = GBA_OK;
+    r.done = true;
+    s.delivered[i] = 1;
+    ++st_.completed;
+    --st_.live;
+    st_.device_bytes_in_use -= r.footprint;
+    s.bytes -= r.footprint;
+  }
+  done_cv_.notify_all();
+}
+
+void Server::boundary(Slot &s) {
+  std::string err;
+  gba_status st = s.engine->device_status(&err);
+  if (st != GBA_OK) {
+    fail_cohort(s, st, err);
+    return;
+  }
+  const LMState *lm = s.engine->states(s.hb);
+  const int n = (int)s.reqs.size();
+  std::vector<int> newly, live_m;
+  long long live_obs = 0, gone_obs = 0;
+  for (int i = 0; i < n; ++i) {
+    const long long o = s.reqs[i]->view.num_observations;
+    if (lm[i].active) {
+      live_m.push_back(i);
+      live_obs += o;
+    } else {
+      if (!s.delivered[i]) newly.push_back(i);
+      gone_obs += o;
+    }
+  }
+  // results of the members that finished in this segment
+  if (!newly.empty()) {
+    std::vector<gba_summary> sums(n);
+    for (auto &x : sums) std::memset(&x, 0, sizeof x);
+    if ((st = s.engine->deliver(s.hb, newly, s.views.data(), sums.data(), &err)) != GBA_OK) {
+      fail_cohort(s, st, err);
+      return;
+    }
+    finish(s, newly, sums);
+  }
+  if (live_m.empty()) {
+    // every member done: the slot is free
+    s.reqs.clear();
+    s.views.clear();
+    s.t_start.clear();
+    s.delivered.clear();
+    s.busy = false;
+    s.bytes = 0;
+    return;
+  }
+  long long join_obs = 0;
+  const int joiners = peek_queued(kCohortObs - live_obs, &join_obs);
+  if (joiners > 0 && (gone_obs + join_obs) * kReformDiv >= live_obs + gone_obs) {
+    // re-form: the running members' current point into their views, their
+    // states carried over; the finished ones leave, queued requests join
+    std::vector<ProblemState> states;
+    if ((st = s.engine->deliver(s.hb, live_m, s.views.data(), nullptr, &err)) != GBA_OK ||
+        (st = s.engine->download_states(s.hb, &states, &err)) != GBA_OK) {
+      fail_cohort(s, st, err);
+      return;
+    }
+    std::vector<std::shared_ptr<Request>> keep;
+    std::vector<double> keep_t;
+    std::vector<ProblemState> keep_states;
+    for (int i : live_m) {
+      keep.push_back(s.reqs[i]);
+      keep_t.push_back(s.t_start[i]);
+      keep_states.push_back(std::move(states[i]));
+    }
+    size_t bytes = 0;
+    std::vector<std::shared_ptr<Request>> fresh = take_queued(kCohortObs - live_obs, &bytes);
+    s.bytes += bytes;
+    s.busy = false;
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      ++st_.reforms;
+    }
+    launch_cohort(s, std::move(keep), std::move(keep_t), keep_states, std::move(fresh));
+    return;
+  }
+  // nothing joins: the next LM iteration on the device
+  st = s.engine->run_segment(true, &err);
+  if (st == GBA_OK) st = s.engine->fetch_states(&err);
+  if (st == GBA_OK && cudaEventRecord(s.done_ev, s.engine->stream()) != cudaSuccess) {
+    st = GBA_ERR_CUDA;
+    err = "event record";
+  }
+  if (st != GBA_OK) {
+    fail_cohort(s, st, err);
+    return;
+  }
+  std::lock_guard<std::mutex> lk(mu_);
+  ++st_.steps;
 }
 
 void Server::loop() {
   // engines are created on this thread, bound to the configured device
   {
     std::lock_guard<std::mutex> lk(mu_);
-    slots_.resize(kSlots);
+    slots_.resize(o_.server_slots > 0 ? o_.server_slots : kDefaultSlots);
     for (Slot &s : slots_) {
       gba_options so = o_;
       so.stream = nullptr;
@@ -200,6 +360,7 @@ void Server::loop() {
         init_error_ = err;
         break;
       }
+      s.engine->set_segment(kSegmentBodies);
       cudaEventCreateWithFlags(&s.done_ev, cudaEventDisableTiming);
     }
     if (init_status_ == GBA_OK && budget_ == 0) {
@@ -218,53 +379,29 @@ void Server::loop() {
   }
   for (;;) {
     bool did = false;
-    // retire finished cohorts
-    for (Slot &s : slots_)
-      if (s.busy && cudaEventQuery(s.done_ev) == cudaSuccess) {
-        retire(s);
-        did = true;
-      }
-    // admit queued requests into free slots
+    // free slots take queued requests as new cohorts
     for (Slot &s : slots_) {
       if (s.busy) continue;
-      std::vector<std::shared_ptr<Request>> take;
       size_t bytes = 0;
-      {
-        std::lock_guard<std::mutex> lk(mu_);
-        while (!queue_.empty()) {
-          const auto &r = queue_.front();
-          if (st_.live + (int)take.size() >= max_live_) break;
-          if (st_.device_bytes_in_use + bytes + r->footprint > budget_) break;
-          bytes += r->footprint;
-          take.push_back(r);
-          queue_.pop_front();
-        }
-        if (take.empty()) break;
-        st_.live += (int32_t)take.size();
-        st_.peak_live = std::max(st_.peak_live, st_.live);
-        st_.admitted += (int64_t)take.size();
-        st_.device_bytes_in_use += bytes;
-        st_.device_bytes_peak = std::max(st_.device_bytes_peak, st_.device_bytes_in_use);
-        st_.queued = (int32_t)queue_.size();
-        ++st_.steps;
-      }
+      std::vector<std::shared_ptr<Request>> take = take_queued(kCohortObs, &bytes);
+      if (take.empty()) break;
       s.bytes = bytes;
-      const int32_t count = (int32_t)take.size();
-      if (!launch_cohort(s, std::move(take))) {
-        std::lock_guard<std::mutex> lk(mu_);
-        st_.live -= count;
-        st_.device_bytes_in_use -= bytes;
-        s.bytes = 0;
-      }
+      launch_cohort(s, {}, {}, {}, std::move(take));
       did = true;
     }
+    // cohorts at an LM-iteration boundary: results out, continue or re-form
+    for (Slot &s : slots_)
+      if (s.busy && cudaEventQuery(s.done_ev) == cudaSuccess) {
+        boundary(s);
+        did = true;
+      }
     std::unique_lock<std::mutex> lk(mu_);
     bool any_busy = false;
     for (Slot &s : slots_) any_busy |= s.busy;
     if (stopping_ && queue_.empty() && !any_busy) break;
     if (!did) {
       if (any_busy)
-        cv_.wait_for(lk, std::chrono::microseconds(50));
+        cv_.wait_for(lk, std::chrono::microseconds(20));
       else
         cv_.wait_for(lk, std::chrono::milliseconds(5), [this] { return !queue_.empty() || stopping_; });
     }

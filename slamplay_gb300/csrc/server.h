@@ -46,15 +46,29 @@ class Server {
     std::unique_ptr<Engine> engine;
     std::vector<std::shared_ptr<Request>> reqs;
     std::vector<gba_problem_view> views;
+    std::vector<double> t_start;  // per member: when it was admitted
+    std::vector<char> delivered;  // per member: finished, result delivered
     HostBatch hb;
     cudaEvent_t done_ev = nullptr;
     size_t bytes = 0;
     bool busy = false;
-    double t_start = 0.0;
   };
   void loop();
-  bool launch_cohort(Slot &s, std::vector<std::shared_ptr<Request>> &&reqs);
-  void retire(Slot &s);
+  // The queued requests (in order) that fit the live cap, the device budget
+  // and `max_obs` observations (the first one always, if it fits the
+  // budget): take_queued removes and admits them (their bytes in *bytes),
+  // peek_queued counts them and their observations.
+  std::vector<std::shared_ptr<Request>> take_queued(long long max_obs, size_t *bytes);
+  int peek_queued(long long max_obs, long long *obs);
+  // Lays out and starts a cohort: `keep` members continue from `states`
+  // (their views hold their current parameters), `fresh` ones start.
+  bool launch_cohort(Slot &s, std::vector<std::shared_ptr<Request>> &&keep, std::vector<double> &&keep_t,
+                     const std::vector<ProblemState> &states, std::vector<std::shared_ptr<Request>> &&fresh);
+  // At a segment boundary: continue, re-form (finished members out, queued
+  // requests in) or retire the whole cohort.
+  void boundary(Slot &s);
+  void finish(Slot &s, const std::vector<int> &members, const std::vector<gba_summary> &sums);
+  void fail_cohort(Slot &s, gba_status st, const std::string &err);
 
   gba_options o_;
   std::thread thread_;
