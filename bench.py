@@ -714,7 +714,8 @@ def serving_form(n_requests: int = 1000, pool: int = 64, rate_mults=(2.0, 5.0, 1
         sweep.append({"arrival_rate_per_s": rate, "requests": n_requests, "solves_per_s": n_requests / total,
                       "p50_ms": 1e3 * float(np.percentile(lat, 50)), "p99_ms": 1e3 * float(np.percentile(lat, 99)),
                       "peak_live": st.get("peak_live"), "batched_lm_iterations": st.get("steps"),
-                      "reforms": st.get("reforms")})
+                      "reforms": st.get("reforms"), "host_prep_s": st.get("host_prep_s"),
+                      "wall_s": total})
     best = max(sweep, key=lambda x: x["solves_per_s"])
     return {"workload": f"config4: {n_requests} Poisson requests per rate over a pool of {pool} problems, mean "
                         f"{int(np.mean([r.num_observations() for r in problems]))} obs",

@@ -339,6 +339,8 @@ typedef struct gba_server_stats {
   size_t device_bytes_in_use, device_bytes_peak;
   int64_t reforms;               /* cohorts re-formed at an LM-iteration boundary
                                     (finished members out, queued requests in) */
+  double host_prep_s;            /* host time laying out and uploading cohorts, on
+                                    worker threads beside the serving loop      */
 } gba_server_stats;
 gba_status gba_server_get_stats(gba_handle *h, gba_server_stats *st);
 

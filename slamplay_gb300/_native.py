@@ -120,7 +120,7 @@ class ServerStats(C.Structure):
         ("submitted", C.c_int64), ("admitted", C.c_int64), ("completed", C.c_int64),
         ("rejected", C.c_int64), ("live", C.c_int32), ("queued", C.c_int32),
         ("peak_live", C.c_int32), ("steps", C.c_int64), ("device_bytes_in_use", C.c_size_t),
-        ("device_bytes_peak", C.c_size_t), ("reforms", C.c_int64),
+        ("device_bytes_peak", C.c_size_t), ("reforms", C.c_int64), ("host_prep_s", C.c_double),
     ]
 
 

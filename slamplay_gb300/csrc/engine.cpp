@@ -848,17 +848,20 @@ gba_status Engine::run_solve(std::string *err) {
   return check(cudaEventRecord(ev_stop_, stream_), "event", err);
 }
 
+gba_status Engine::prepare_continue(std::string *err) {
+  if (exec_c_ && graph_c_key_ == cur_key_ && graph_c_segment_ == segment_bodies_) return GBA_OK;
+  gba_status st = build_graph(err, true);
+  if (st != GBA_OK && pdl_) {
+    pdl_ = false;
+    st = build_graph(err, true);
+  }
+  return st;
+}
+
 gba_status Engine::run_segment(bool cont, std::string *err) {
   if (!cont) return run_solve(err);
-  gba_status st;
-  if (!exec_c_ || graph_c_key_ != cur_key_ || graph_c_segment_ != segment_bodies_) {
-    st = build_graph(err, true);
-    if (st != GBA_OK && pdl_) {
-      pdl_ = false;
-      st = build_graph(err, true);
-    }
-    if (st != GBA_OK) return st;
-  }
+  const gba_status st = prepare_continue(err);
+  if (st != GBA_OK) return st;
   return check(cudaGraphLaunch(exec_c_, stream_), "cudaGraphLaunch", err);
 }
 

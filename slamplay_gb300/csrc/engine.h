@@ -56,6 +56,9 @@ class Engine {
   // host staging area, states() reads them once the stream has passed it.
   void set_segment(int lm_bodies) { segment_bodies_ = std::max(0, lm_bodies); }
   gba_status run_segment(bool cont, std::string *err);
+  // Builds the continue graph of the uploaded batch ahead of its use (the
+  // capture does not wait for the stream).
+  gba_status prepare_continue(std::string *err);
   gba_status fetch_states(std::string *err);
   const LMState *states(const HostBatch &hb);
   // The batch's device-side error word as fetched (GBA_OK when clear).

@@ -181,12 +181,12 @@ int Server::peek_queued(long long max_obs, long long *obs) {
   return n;
 }
 
-bool Server::launch_cohort(Slot &s, std::vector<std::shared_ptr<Request>> &&keep, std::vector<double> &&keep_t,
-                           const std::vector<ProblemState> &states, std::vector<std::shared_ptr<Request>> &&fresh) {
+void Server::launch_cohort(Slot &s, std::vector<std::shared_ptr<Request>> &&keep, std::vector<double> &&keep_t,
+                           std::vector<ProblemState> &&states, std::vector<std::shared_ptr<Request>> &&fresh) {
   const double t = now_s();
   s.reqs = std::move(keep);
   s.t_start = std::move(keep_t);
-  const size_t nkeep = s.reqs.size();
+  s.resume = std::move(states);
   for (auto &r : fresh) {
     s.reqs.push_back(r);
     s.t_start.push_back(t);
@@ -194,26 +194,40 @@ bool Server::launch_cohort(Slot &s, std::vector<std::shared_ptr<Request>> &&keep
   s.delivered.assign(s.reqs.size(), 0);
   s.views.clear();
   for (auto &r : s.reqs) s.views.push_back(r->view);
+  s.state = SlotState::kPreparing;
+  s.prep_done.store(0, std::memory_order_relaxed);
+  s.worker = std::thread([this, &s] { prepare_and_start(s); });
+}
+
+// On the slot's worker thread: the loop does not touch the slot until
+// prep_done is set.
+void Server::prepare_and_start(Slot &s) {
   std::string err;
+  const double t0 = now_s();
   const PrepOptions po = s.engine->prep_options();
   gba_status st = prepare_batch(s.views.data(), (int)s.views.size(), po, &s.hb, &err);
   if (st == GBA_OK)
-    for (size_t i = 0; i < nkeep; ++i) set_resume(s.hb, (int)i, states[i]);
+    for (size_t i = 0; i < s.resume.size(); ++i) set_resume(s.hb, (int)i, s.resume[i]);
+  s.resume.clear();
   if (st == GBA_OK) st = s.engine->upload(s.hb, &err);
+  const double t1 = now_s();
   if (st == GBA_OK) st = s.engine->run_segment(false, &err);
   if (st == GBA_OK) st = s.engine->fetch_states(&err);
   if (st == GBA_OK && cudaEventRecord(s.done_ev, s.engine->stream()) != cudaSuccess) {
     st = GBA_ERR_CUDA;
     err = "event record";
   }
-  if (st != GBA_OK) {
-    fail_cohort(s, st, err);
-    return false;
+  // the graph of the next segments, built while the first one runs
+  if (st == GBA_OK) st = s.engine->prepare_continue(&err);
+  s.prep_status = st;
+  s.prep_error = err;
+  {
+    std::lock_guard<std::mutex> lk(mu_);
+    st_.host_prep_s += t1 - t0;
+    if (st == GBA_OK) ++st_.steps;
+    s.prep_done.store(1, std::memory_order_release);
   }
-  s.busy = true;
-  std::lock_guard<std::mutex> lk(mu_);
-  ++st_.steps;
-  return true;
+  cv_.notify_all();
 }
 
 // Every member not yet delivered fails with `st`; the slot is emptied.
@@ -233,7 +247,7 @@ void Server::fail_cohort(Slot &s, gba_status st, const std::string &err) {
   s.views.clear();
   s.t_start.clear();
   s.delivered.clear();
-  s.busy = false;
+  s.state = SlotState::kIdle;
   s.bytes = 0;
   done_cv_.notify_all();
 }
@@ -294,7 +308,7 @@ void Server::boundary(Slot &s) {
     s.views.clear();
     s.t_start.clear();
     s.delivered.clear();
-    s.busy = false;
+    s.state = SlotState::kIdle;
     s.bytes = 0;
     return;
   }
@@ -320,12 +334,11 @@ void Server::boundary(Slot &s) {
     size_t bytes = 0;
     std::vector<std::shared_ptr<Request>> fresh = take_queued(kCohortObs - live_obs, &bytes);
     s.bytes += bytes;
-    s.busy = false;
     {
       std::lock_guard<std::mutex> lk(mu_);
       ++st_.reforms;
     }
-    launch_cohort(s, std::move(keep), std::move(keep_t), keep_states, std::move(fresh));
+    launch_cohort(s, std::move(keep), std::move(keep_t), std::move(keep_states), std::move(fresh));
     return;
   }
   // nothing joins: the next LM iteration on the device
@@ -347,8 +360,10 @@ void Server::loop() {
   // engines are created on this thread, bound to the configured device
   {
     std::lock_guard<std::mutex> lk(mu_);
-    slots_.resize(o_.server_slots > 0 ? o_.server_slots : kDefaultSlots);
-    for (Slot &s : slots_) {
+    const int n = o_.server_slots > 0 ? o_.server_slots : kDefaultSlots;
+    for (int i = 0; i < n; ++i) {
+      slots_.emplace_back(new Slot);
+      Slot &s = *slots_.back();
       gba_options so = o_;
       so.stream = nullptr;
       so.use_graphs = 1;
@@ -371,17 +386,29 @@ void Server::loop() {
     init_done_ = true;
     done_cv_.notify_all();
     if (init_status_ != GBA_OK) {
-      for (Slot &s : slots_)
-        if (s.done_ev) cudaEventDestroy(s.done_ev);
+      for (auto &s : slots_)
+        if (s->done_ev) cudaEventDestroy(s->done_ev);
       slots_.clear();
       return;
     }
   }
   for (;;) {
     bool did = false;
+    // cohorts whose worker finished laying out and starting them
+    for (auto &sp : slots_) {
+      Slot &s = *sp;
+      if (s.state != SlotState::kPreparing || !s.prep_done.load(std::memory_order_acquire)) continue;
+      s.worker.join();
+      if (s.prep_status != GBA_OK)
+        fail_cohort(s, s.prep_status, s.prep_error);
+      else
+        s.state = SlotState::kRunning;
+      did = true;
+    }
     // free slots take queued requests as new cohorts
-    for (Slot &s : slots_) {
-      if (s.busy) continue;
+    for (auto &sp : slots_) {
+      Slot &s = *sp;
+      if (s.state != SlotState::kIdle) continue;
       size_t bytes = 0;
       std::vector<std::shared_ptr<Request>> take = take_queued(kCohortObs, &bytes);
       if (take.empty()) break;
@@ -390,14 +417,16 @@ void Server::loop() {
       did = true;
     }
     // cohorts at an LM-iteration boundary: results out, continue or re-form
-    for (Slot &s : slots_)
-      if (s.busy && cudaEventQuery(s.done_ev) == cudaSuccess) {
+    for (auto &sp : slots_) {
+      Slot &s = *sp;
+      if (s.state == SlotState::kRunning && cudaEventQuery(s.done_ev) == cudaSuccess) {
         boundary(s);
         did = true;
       }
+    }
     std::unique_lock<std::mutex> lk(mu_);
     bool any_busy = false;
-    for (Slot &s : slots_) any_busy |= s.busy;
+    for (auto &s : slots_) any_busy |= s->state != SlotState::kIdle;
     if (stopping_ && queue_.empty() && !any_busy) break;
     if (!did) {
       if (any_busy)
@@ -406,9 +435,9 @@ void Server::loop() {
         cv_.wait_for(lk, std::chrono::milliseconds(5), [this] { return !queue_.empty() || stopping_; });
     }
   }
-  for (Slot &s : slots_) {
-    if (s.done_ev) cudaEventDestroy(s.done_ev);
-    s.engine.reset();
+  for (auto &s : slots_) {
+    if (s->done_ev) cudaEventDestroy(s->done_ev);
+    s->engine.reset();
   }
   slots_.clear();
 }

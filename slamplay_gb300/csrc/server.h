@@ -1,6 +1,7 @@
 // server.h — continuous-batching request loop over several engine slots.
 #pragma once
 
+#include <atomic>
 #include <condition_variable>
 #include <deque>
 #include <map>
@@ -42,16 +43,25 @@ class Server {
     std::string error;
     bool done = false;
   };
+  // A slot is idle, preparing (a worker thread lays out, uploads and starts
+  // its cohort while the loop serves the other slots) or running (its
+  // segment's completion event pending).
+  enum class SlotState { kIdle, kPreparing, kRunning };
   struct Slot {
     std::unique_ptr<Engine> engine;
     std::vector<std::shared_ptr<Request>> reqs;
     std::vector<gba_problem_view> views;
     std::vector<double> t_start;  // per member: when it was admitted
     std::vector<char> delivered;  // per member: finished, result delivered
+    std::vector<ProblemState> resume;  // the continuing members' states, for the worker
     HostBatch hb;
     cudaEvent_t done_ev = nullptr;
     size_t bytes = 0;
-    bool busy = false;
+    SlotState state = SlotState::kIdle;
+    std::thread worker;
+    std::atomic<int> prep_done{0};
+    gba_status prep_status = GBA_OK;
+    std::string prep_error;
   };
   void loop();
   // The queued requests (in order) that fit the live cap, the device budget
@@ -60,10 +70,12 @@ class Server {
   // peek_queued counts them and their observations.
   std::vector<std::shared_ptr<Request>> take_queued(long long max_obs, size_t *bytes);
   int peek_queued(long long max_obs, long long *obs);
-  // Lays out and starts a cohort: `keep` members continue from `states`
-  // (their views hold their current parameters), `fresh` ones start.
-  bool launch_cohort(Slot &s, std::vector<std::shared_ptr<Request>> &&keep, std::vector<double> &&keep_t,
-                     const std::vector<ProblemState> &states, std::vector<std::shared_ptr<Request>> &&fresh);
+  // Starts a cohort on a worker thread: `keep` members continue from
+  // `states` (their views hold their current parameters), `fresh` ones
+  // start.
+  void launch_cohort(Slot &s, std::vector<std::shared_ptr<Request>> &&keep, std::vector<double> &&keep_t,
+                     std::vector<ProblemState> &&states, std::vector<std::shared_ptr<Request>> &&fresh);
+  void prepare_and_start(Slot &s);
   // At a segment boundary: continue, re-form (finished members out, queued
   // requests in) or retire the whole cohort.
   void boundary(Slot &s);
@@ -77,7 +89,7 @@ class Server {
   std::condition_variable done_cv_;
   std::deque<std::shared_ptr<Request>> queue_;
   std::map<uint64_t, std::shared_ptr<Request>> tickets_;
-  std::vector<Slot> slots_;
+  std::vector<std::unique_ptr<Slot>> slots_;
   uint64_t next_ticket_ = 1;
   size_t budget_ = 0;
   int max_live_ = 0, max_queue_ = 0;
