@@ -377,24 +377,43 @@ gba_status gba_solve_resident(gba_handle *h, int32_t repeats);
 gba_status gba_synchronize(gba_handle *h);
 
 /* ---- autotuner ------------------------------------------------------------
- * Times short trial solves (3 LM iterations, tolerances off, PCG capped at
- * 20 iterations) of the given problem(s) over a grid of launch shapes --
- * point-segment tile size (observations per CTA: 256, 192, 128) x PCG
- * iterations per graph body (1, 2, 4) -- on a scratch engine, keeps the
- * fastest, and sets it on the handle (later solves use it).  The problems
- * are not modified.  Results are cached per size bucket (number of
- * problems, log2 of observations and cameras, precision) for the process.
- * No counterpart in the reference (Ceres has no launch shapes to tune). */
-#define GBA_TUNE_MAX_TRIALS 16
+ * Times short trial solves of the given problem(s) on a scratch engine and
+ * sets the fastest choices on the handle (later solves use them), one knob
+ * after another:
+ *  1. launch shapes (3 LM iterations, tolerances off, PCG capped at 20
+ *     iterations): the point-segment tile, i.e. the observations (and so
+ *     the warps, 32 observations a warp) that one CTA of the point kernels
+ *     takes (256, 192, 128), x PCG iterations per graph body (1, 2, 4; one
+ *     value when the PCG runs as one launch);
+ *  2. with the cluster PCG (mixed form, explicit Schur complement): the
+ *     cameras of a problem that one CTA of its cluster takes (16, 32, 64);
+ *  3. only when the handle's options.autotune is 2: the PCG iteration cap
+ *     (5 LM iterations at the handle's PCG tolerance): the configured cap
+ *     and its halvings down to 10; a smaller cap is taken only when its
+ *     trial ends within 1e-6 relative of the configured cap's cost, and
+ *     then the fastest such one.
+ * Steps 1-2 change which thread adds which partial sum, never what is
+ * solved; step 3 changes how far each linear solve goes.  The problems are
+ * not modified.  Results are cached per size bucket (number of problems,
+ * log2 of observations and cameras, precision) for the process.  No
+ * counterpart in the reference (Ceres has no launch shapes to tune). */
+#define GBA_TUNE_MAX_TRIALS 32
 typedef struct gba_tune_result {
   int32_t chunk_observations; /* chosen tile size                           */
   int32_t pcg_unroll;         /* chosen PCG iterations per graph body       */
   int32_t num_trials;         /* 0 when the answer came from the cache      */
   int32_t from_cache;
-  double best_ms;             /* device time of the chosen trial solve      */
+  double best_ms;             /* device time of the chosen launch-shape trial */
+  int32_t pcg_cameras_per_cta; /* chosen cameras per CTA of the cluster PCG
+                                  (0: not a cluster PCG, defaults kept)     */
+  int32_t pcg_cap;            /* chosen PCG iteration cap (0: not tuned)    */
   double trial_ms[GBA_TUNE_MAX_TRIALS];
+  int32_t trial_step[GBA_TUNE_MAX_TRIALS];   /* 1, 2 or 3 (the knob above) */
   int32_t trial_chunk[GBA_TUNE_MAX_TRIALS];
   int32_t trial_unroll[GBA_TUNE_MAX_TRIALS];
+  int32_t trial_cameras_per_cta[GBA_TUNE_MAX_TRIALS];
+  int32_t trial_cap[GBA_TUNE_MAX_TRIALS];
+  double trial_final_cost[GBA_TUNE_MAX_TRIALS];
 } gba_tune_result;
 gba_status gba_autotune(gba_handle *h, const gba_problem_view *problems, int32_t num_problems,
                         gba_tune_result *result);

@@ -124,11 +124,17 @@ class ServerStats(C.Structure):
     ]
 
 
+TUNE_MAX_TRIALS = 32
+
+
 class TuneResult(C.Structure):
     _fields_ = [
         ("chunk_observations", C.c_int32), ("pcg_unroll", C.c_int32), ("num_trials", C.c_int32),
-        ("from_cache", C.c_int32), ("best_ms", C.c_double), ("trial_ms", C.c_double * 16),
-        ("trial_chunk", C.c_int32 * 16), ("trial_unroll", C.c_int32 * 16),
+        ("from_cache", C.c_int32), ("best_ms", C.c_double), ("pcg_cameras_per_cta", C.c_int32),
+        ("pcg_cap", C.c_int32), ("trial_ms", C.c_double * TUNE_MAX_TRIALS),
+        ("trial_step", C.c_int32 * TUNE_MAX_TRIALS), ("trial_chunk", C.c_int32 * TUNE_MAX_TRIALS),
+        ("trial_unroll", C.c_int32 * TUNE_MAX_TRIALS), ("trial_cameras_per_cta", C.c_int32 * TUNE_MAX_TRIALS),
+        ("trial_cap", C.c_int32 * TUNE_MAX_TRIALS), ("trial_final_cost", C.c_double * TUNE_MAX_TRIALS),
     ]
 
 

@@ -31,7 +31,6 @@ namespace gba {
 // The calling thread's handle-less error message (gba_last_error(NULL)).
 std::string &thread_error_message() { return g_create_error; }
 gba_status autotune(Engine &target, const gba_problem_view *problems, int n, gba_tune_result *out, std::string *err);
-bool tune_cached(const gba_problem_view *problems, int n, int precision);
 }  // namespace gba
 
 namespace {

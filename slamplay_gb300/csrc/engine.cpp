@@ -132,9 +132,11 @@ PrepOptions Engine::prep_options() const {
   return po;
 }
 
-void Engine::set_tuning(int chunk_observations, int pcg_unroll) {
+void Engine::set_tuning(int chunk_observations, int pcg_unroll, int cluster_cams, int pcg_cap) {
   o_.chunk_observations = chunk_observations;
   o_.pcg_unroll = pcg_unroll;
+  cluster_cams_ = std::max(0, cluster_cams);
+  if (pcg_cap > 0) o_.max_linear_solver_iterations = pcg_cap;
   destroy_graph();
   cur_key_.clear();
 }
@@ -426,7 +428,7 @@ gba_status Engine::upload(const HostBatch &hb, std::string *err) {
   // Schur complement, every problem small enough
   cl_plan_ = ClusterPlan();
   if (mixed_ && hb.explicit_schur && o_.persistent_pcg &&
-      !pcg_cluster_plan(hb.prob.data(), (int)hb.prob.size(), hb.sblk_row.data(), &cl_plan_))
+      !pcg_cluster_plan(hb.prob.data(), (int)hb.prob.size(), hb.sblk_row.data(), cluster_cams_, &cl_plan_))
     cl_plan_ = ClusterPlan();
   // the PCG as one grid-wide launch per LM iteration: FP64 form, explicit
   // Schur complement, one problem

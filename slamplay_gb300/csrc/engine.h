@@ -40,7 +40,12 @@ class Engine {
   const std::vector<ProfileEntry> &profile() const { return profile_; }
   const gba_options &options() const { return o_; }
   // Launch shapes chosen by the autotuner (takes effect on the next upload).
-  void set_tuning(int chunk_observations, int pcg_unroll);
+  // The autotuner's choices: tile size, PCG iterations per graph body, the
+  // cameras per CTA of the cluster PCG (0 = default) and, when > 0, the PCG
+  // iteration cap.
+  void set_tuning(int chunk_observations, int pcg_unroll, int cluster_cams = 0, int pcg_cap = 0);
+  bool cluster_pcg() const { return cl_plan_.cs > 0; }
+  bool one_launch_pcg() const { return cl_plan_.cs > 0 || gr_plan_.grid > 0; }
   double last_solve_ms() const { return last_solve_ms_; }
   PrepOptions prep_options() const;
   cudaStream_t stream() const { return stream_; }
@@ -118,6 +123,7 @@ class Engine {
   cudaGraphExec_t exec_c_ = nullptr;
   std::vector<long long> graph_c_key_;
   int segment_bodies_ = 0;
+  int cluster_cams_ = 0;  // cameras per CTA of the cluster PCG (0 = default)
   int graph_segment_ = -1, graph_c_segment_ = -1;
   std::vector<long long> cur_key_;
   // events

@@ -449,7 +449,8 @@ __global__ void __launch_bounds__(kClThreads, 1) k_pcg_cluster(DeviceBatch B, in
   cl.sync();
 }
 
-bool pcg_cluster_plan(const ProblemInfo *prob, int num_problems, const int32_t *sblk_row, ClusterPlan *plan) {
+bool pcg_cluster_plan(const ProblemInfo *prob, int num_problems, const int32_t *sblk_row, int cams_per_cta,
+                      ClusterPlan *plan) {
   *plan = ClusterPlan();
   int n_max = 0;
   for (int p = 0; p < num_problems; ++p) n_max = std::max(n_max, (int)prob[p].cam_count);
@@ -457,7 +458,7 @@ bool pcg_cluster_plan(const ProblemInfo *prob, int num_problems, const int32_t *
   // a single problem spreads over up to 16 SMs (16 cameras per CTA); a batch
   // takes fewer CTAs per problem (64 cameras per CTA) and more problems at once
   const bool single = num_problems == 1;
-  const int target = single ? 16 : 64;
+  const int target = cams_per_cta > 0 ? cams_per_cta : single ? 16 : 64;
   int cs = 1;
   while (cs < kClMaxCS && (n_max + cs - 1) / cs > target) cs *= 2;
   const int threads = 512;

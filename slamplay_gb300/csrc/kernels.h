@@ -47,7 +47,10 @@ struct ClusterPlan {
 // in shared memory, from the batch's problems (camera ranges) and the
 // explicit complement's row structure (sblk_row, nc + 1); false when the
 // form does not apply or cannot be launched.
-bool pcg_cluster_plan(const ProblemInfo *prob, int num_problems, const int32_t *sblk_row, ClusterPlan *plan);
+// cams_per_cta: the cameras of a problem one CTA of its cluster takes (the
+// cluster size follows); 0 = 16 for a single problem, 64 for a batch.
+bool pcg_cluster_plan(const ProblemInfo *prob, int num_problems, const int32_t *sblk_row, int cams_per_cta,
+                      ClusterPlan *plan);
 cudaError_t launch_pcg_cluster(const DeviceBatch &b, const ClusterPlan &plan, cudaStream_t s);
 // K4 grid form: the whole PCG of one problem in one launch, one CTA per SM
 // with grid-wide barriers (FP64 form, explicit Schur complement).

@@ -213,18 +213,23 @@ class Solver:
 
     def autotune(self, problems: BALProblem | Sequence[BALProblem]) -> dict:
         """Picks the fastest launch shapes (tile size, PCG iterations per
-        graph body) for these problems by timed trial solves; later solves on
-        this handle use them.  The problems are not modified."""
+        graph body, cameras per CTA of the cluster PCG) and, with
+        autotune=2, the PCG iteration cap for these problems by timed trial
+        solves; later solves on this handle use them.  The problems are not
+        modified."""
         if isinstance(problems, BALProblem):
             problems = [problems]
         views = (N.ProblemView * len(problems))(*[p.view() for p in problems])
         r = N.TuneResult()
         N.check(N.lib().gba_autotune(self._h, views, len(problems), N.C.byref(r)), self._h, "gba_autotune")
-        n = min(r.num_trials, 16)
+        n = min(r.num_trials, N.TUNE_MAX_TRIALS)
         return {"chunk_observations": r.chunk_observations, "pcg_unroll": r.pcg_unroll, "best_ms": r.best_ms,
+                "pcg_cameras_per_cta": r.pcg_cameras_per_cta, "pcg_cap": r.pcg_cap,
                 "from_cache": bool(r.from_cache),
-                "trials": [{"chunk_observations": r.trial_chunk[i], "pcg_unroll": r.trial_unroll[i],
-                            "ms": r.trial_ms[i]} for i in range(n)]}
+                "trials": [{"step": r.trial_step[i], "chunk_observations": r.trial_chunk[i],
+                            "pcg_unroll": r.trial_unroll[i], "pcg_cameras_per_cta": r.trial_cameras_per_cta[i],
+                            "pcg_cap": r.trial_cap[i], "ms": r.trial_ms[i], "final_cost": r.trial_final_cost[i]}
+                           for i in range(n)]}
 
     def evaluate(self, problem: BALProblem):
         """(residuals [no,2], jacobians [no,2,12], cost) evaluated on the GPU."""

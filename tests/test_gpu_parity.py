@@ -265,7 +265,38 @@ def test_autotune_picks_a_shape_and_keeps_the_solution():
         r = s.autotune(b)
         assert np.array_equal(b.parameters(), before)
         assert r["chunk_observations"] in (128, 192, 256) and r["pcg_unroll"] in (1, 2, 4)
-        assert len(r["trials"]) == 9 and min(t["ms"] for t in r["trials"]) == r["best_ms"]
+        shapes = [t for t in r["trials"] if t["step"] == 1]
+        assert len(shapes) in (3, 9) and min(t["ms"] for t in shapes) == r["best_ms"]
+        assert r["pcg_cap"] == 0  # the cap is tuned only with autotune=2
         tuned = s.solve(b.copy())
         assert s.autotune(b)["from_cache"]
     assert abs(tuned.final_cost - ref.final_cost) <= 1e-9 * ref.final_cost
+
+
+def test_autotune_cluster_split_and_pcg_cap():
+    """A mixed batch on the cluster PCG: the tuner also picks the cameras
+    per CTA (16, 32, 64, or 0 = the default split) and, with autotune=2, the
+    PCG cap: a smaller cap only when its 5-iteration trial ends within 1e-6
+    relative of the configured cap's, and then the fastest such one.  The
+    tuned solve ends within 1e-6 relative of the untuned one (10 LM
+    iterations; a smaller cap changes each linear solve's length)."""
+    probs = [BALProblem.synthetic(0, seed=20 + i, num_points=600) for i in range(8)]
+    opts = dict(precision="mixed", max_num_iterations=10, pcg_tolerance=1e-6, max_linear_solver_iterations=80,
+                persistent_pcg=1, **FIXED)
+    with Solver(**opts) as s:
+        ref = s.batch_solve([p.copy() for p in probs])
+    with Solver(autotune=2, **opts) as s:
+        r = s.autotune(probs)
+        steps = {t["step"] for t in r["trials"]}
+        assert steps >= {1, 3}
+        if 2 in steps:
+            assert r["pcg_cameras_per_cta"] in (0, 16, 32, 64)
+        caps = [t for t in r["trials"] if t["step"] == 3]
+        assert caps[0]["pcg_cap"] == 80 and r["pcg_cap"] in [t["pcg_cap"] for t in caps]
+        chosen = next(t for t in caps if t["pcg_cap"] == r["pcg_cap"])
+        assert chosen["final_cost"] <= caps[0]["final_cost"] * (1 + 1e-6)
+        tuned = s.batch_solve([p.copy() for p in probs])
+    print("tune:", {k: r[k] for k in ("chunk_observations", "pcg_unroll", "pcg_cameras_per_cta", "pcg_cap")},
+          [(t["step"], t["pcg_cap"], round(t["ms"], 3)) for t in r["trials"]])
+    for a, b in zip(tuned, ref):
+        assert abs(a.final_cost - b.final_cost) <= 1e-6 * b.final_cost
