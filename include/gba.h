@@ -387,6 +387,8 @@ gba_status gba_synchronize(gba_handle *h);
  *     value when the PCG runs as one launch);
  *  2. with the cluster PCG (mixed form, explicit Schur complement): the
  *     cameras of a problem that one CTA of its cluster takes (16, 32, 64);
+ *     with the grid PCG (FP64 form, one problem): its CTAs (every SM, 3/4,
+ *     1/2, 1/4 of them; the result does not depend on the count);
  *  3. only when the handle's options.autotune is 2: the PCG iteration cap
  *     (5 LM iterations at the handle's PCG tolerance): the configured cap
  *     and its halvings down to 10; a smaller cap is taken only when its
@@ -407,12 +409,16 @@ typedef struct gba_tune_result {
   int32_t pcg_cameras_per_cta; /* chosen cameras per CTA of the cluster PCG
                                   (0: not a cluster PCG, defaults kept)     */
   int32_t pcg_cap;            /* chosen PCG iteration cap (0: not tuned)    */
+  int32_t pcg_grid_ctas;      /* chosen CTAs of the grid PCG (0: not a grid
+                                 PCG, every SM kept)                        */
+  int32_t reserved_;
   double trial_ms[GBA_TUNE_MAX_TRIALS];
   int32_t trial_step[GBA_TUNE_MAX_TRIALS];   /* 1, 2 or 3 (the knob above) */
   int32_t trial_chunk[GBA_TUNE_MAX_TRIALS];
   int32_t trial_unroll[GBA_TUNE_MAX_TRIALS];
   int32_t trial_cameras_per_cta[GBA_TUNE_MAX_TRIALS];
   int32_t trial_cap[GBA_TUNE_MAX_TRIALS];
+  int32_t trial_grid_ctas[GBA_TUNE_MAX_TRIALS];
   double trial_final_cost[GBA_TUNE_MAX_TRIALS];
 } gba_tune_result;
 gba_status gba_autotune(gba_handle *h, const gba_problem_view *problems, int32_t num_problems,

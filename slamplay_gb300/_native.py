@@ -131,10 +131,12 @@ class TuneResult(C.Structure):
     _fields_ = [
         ("chunk_observations", C.c_int32), ("pcg_unroll", C.c_int32), ("num_trials", C.c_int32),
         ("from_cache", C.c_int32), ("best_ms", C.c_double), ("pcg_cameras_per_cta", C.c_int32),
-        ("pcg_cap", C.c_int32), ("trial_ms", C.c_double * TUNE_MAX_TRIALS),
+        ("pcg_cap", C.c_int32), ("pcg_grid_ctas", C.c_int32), ("reserved_", C.c_int32),
+        ("trial_ms", C.c_double * TUNE_MAX_TRIALS),
         ("trial_step", C.c_int32 * TUNE_MAX_TRIALS), ("trial_chunk", C.c_int32 * TUNE_MAX_TRIALS),
         ("trial_unroll", C.c_int32 * TUNE_MAX_TRIALS), ("trial_cameras_per_cta", C.c_int32 * TUNE_MAX_TRIALS),
-        ("trial_cap", C.c_int32 * TUNE_MAX_TRIALS), ("trial_final_cost", C.c_double * TUNE_MAX_TRIALS),
+        ("trial_cap", C.c_int32 * TUNE_MAX_TRIALS), ("trial_grid_ctas", C.c_int32 * TUNE_MAX_TRIALS),
+        ("trial_final_cost", C.c_double * TUNE_MAX_TRIALS),
     ]
 
 

@@ -132,10 +132,11 @@ PrepOptions Engine::prep_options() const {
   return po;
 }
 
-void Engine::set_tuning(int chunk_observations, int pcg_unroll, int cluster_cams, int pcg_cap) {
+void Engine::set_tuning(int chunk_observations, int pcg_unroll, int cluster_cams, int pcg_cap, int grid_ctas) {
   o_.chunk_observations = chunk_observations;
   o_.pcg_unroll = pcg_unroll;
   cluster_cams_ = std::max(0, cluster_cams);
+  grid_ctas_ = std::max(0, grid_ctas);
   if (pcg_cap > 0) o_.max_linear_solver_iterations = pcg_cap;
   destroy_graph();
   cur_key_.clear();
@@ -434,7 +435,7 @@ gba_status Engine::upload(const HostBatch &hb, std::string *err) {
   // Schur complement, one problem
   gr_plan_ = GridPlan();
   if (o_.persistent_pcg && !pcg_grid_plan((int)hb.prob.size(), mixed_, hb.explicit_schur, hb.nc,
-                                          hb.explicit_schur ? hb.sblk_row.data() : nullptr, &gr_plan_))
+                                          hb.explicit_schur ? hb.sblk_row.data() : nullptr, grid_ctas_, &gr_plan_))
     gr_plan_ = GridPlan();
   // current batch shape + pointers + options + PCG form = graph key
   DeviceBatch k = db_;

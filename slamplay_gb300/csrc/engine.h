@@ -41,10 +41,11 @@ class Engine {
   const gba_options &options() const { return o_; }
   // Launch shapes chosen by the autotuner (takes effect on the next upload).
   // The autotuner's choices: tile size, PCG iterations per graph body, the
-  // cameras per CTA of the cluster PCG (0 = default) and, when > 0, the PCG
-  // iteration cap.
-  void set_tuning(int chunk_observations, int pcg_unroll, int cluster_cams = 0, int pcg_cap = 0);
+  // cameras per CTA of the cluster PCG (0 = default), when > 0 the PCG
+  // iteration cap, and the CTAs of the grid PCG (0 = every SM).
+  void set_tuning(int chunk_observations, int pcg_unroll, int cluster_cams = 0, int pcg_cap = 0, int grid_ctas = 0);
   bool cluster_pcg() const { return cl_plan_.cs > 0; }
+  int grid_pcg_ctas() const { return gr_plan_.grid; }
   bool one_launch_pcg() const { return cl_plan_.cs > 0 || gr_plan_.grid > 0; }
   double last_solve_ms() const { return last_solve_ms_; }
   PrepOptions prep_options() const;
@@ -124,6 +125,7 @@ class Engine {
   std::vector<long long> graph_c_key_;
   int segment_bodies_ = 0;
   int cluster_cams_ = 0;  // cameras per CTA of the cluster PCG (0 = default)
+  int grid_ctas_ = 0;     // CTAs of the grid PCG (0 = every SM)
   int graph_segment_ = -1, graph_c_segment_ = -1;
   std::vector<long long> cur_key_;
   // events

@@ -105,15 +105,17 @@ __device__ void grid_abort(const DeviceBatch &B) {
 
 // Grid-wide barrier of the P registered CTAs (generation `gen`, from 1):
 // every thread's earlier writes are ordered before thread 0's release
-// increment; after thread 0's acquire wait and the CTA barrier every thread
-// reads the other CTAs' writes (with __ldcg: L2, not a stale L1 line).
+// increment by the CTA barrier (causality order is transitive: CTA barrier,
+// then the gpu-scope release, the other CTA's gpu-scope acquire, its CTA
+// barrier), so no separate fence is needed on either side; after thread 0's
+// acquire wait and the CTA barrier every thread reads the other CTAs'
+// writes (with __ldcg: L2, not a stale L1 line).
 // Returns false (in every thread) when the wait ran out or was aborted.
 __device__ __forceinline__ bool grid_barrier(const DeviceBatch &B, unsigned gen, unsigned P, int *s_ok) {
   __syncthreads();
   if (threadIdx.x == 0) {
     int ok = 1;
     unsigned *bar = B.grid_ctl + kGridBar;
-    __threadfence();
     red_release_add_u32(bar, 1u);
     const unsigned target = gen * P;
     if (ld_acquire_u32(bar) < target) {
@@ -133,7 +135,6 @@ __device__ __forceinline__ bool grid_barrier(const DeviceBatch &B, unsigned gen,
         }
       }
     }
-    __threadfence();
     *s_ok = ok;
   }
   __syncthreads();
@@ -675,7 +676,7 @@ __global__ void __launch_bounds__(kGThreads, 1) k_pcg_grid(DeviceBatch B, int ca
   }
 }
 
-bool pcg_grid_plan(int num_problems, bool mixed, bool explicit_schur, int nc, const int32_t *sblk_row,
+bool pcg_grid_plan(int num_problems, bool mixed, bool explicit_schur, int nc, const int32_t *sblk_row, int ctas,
                    GridPlan *plan) {
   *plan = GridPlan();
   if (num_problems != 1 || mixed || !explicit_schur || nc <= 0 || !sblk_row) return false;
@@ -687,8 +688,8 @@ bool pcg_grid_plan(int num_problems, bool mixed, bool explicit_schur, int nc, co
     cudaGetLastError();
     return false;
   }
-  // one CTA per SM, and no more CTAs than rows
-  const int grid = std::max(1, std::min(sms, 9 * nc));
+  // one CTA per SM at most, and no more CTAs than rows
+  const int grid = std::max(1, std::min(ctas > 0 ? std::min(ctas, sms) : sms, 9 * nc));
   // the kernel's split of the rows (all CTAs registered): the most blocks of
   // touched cameras a CTA stages, the most touched cameras, the most (row,
   // block) pairs, the longest row

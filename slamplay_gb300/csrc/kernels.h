@@ -63,8 +63,9 @@ struct GridPlan {
 };
 // Sizes the launch from the problem's explicit-complement rows (sblk_row,
 // nc + 1); false when the form does not apply (a batch, the mixed form,
-// the implicit complement) or its kernel cannot be resident.
-bool pcg_grid_plan(int num_problems, bool mixed, bool explicit_schur, int nc, const int32_t *sblk_row,
+// the implicit complement) or its kernel cannot be resident.  ctas: the
+// CTAs of the launch (one per SM at most; 0 = every SM).
+bool pcg_grid_plan(int num_problems, bool mixed, bool explicit_schur, int nc, const int32_t *sblk_row, int ctas,
                    GridPlan *plan);
 cudaError_t launch_pcg_grid(const DeviceBatch &b, const GridPlan &plan, cudaStream_t s);
 // K4a-b: one PCG iteration (implicit Schur mat-vec, camera-side update).

@@ -65,7 +65,8 @@ gba_status autotune(Engine &target, const gba_problem_view *problems, int n, gba
       *out = it->second;
       out->num_trials = 0;
       out->from_cache = 1;
-      target.set_tuning(out->chunk_observations, out->pcg_unroll, out->pcg_cameras_per_cta, out->pcg_cap);
+      target.set_tuning(out->chunk_observations, out->pcg_unroll, out->pcg_cameras_per_cta, out->pcg_cap,
+                        out->pcg_grid_ctas);
       return GBA_OK;
     }
   }
@@ -81,9 +82,9 @@ gba_status autotune(Engine &target, const gba_problem_view *problems, int n, gba
   int t = 0;
   // one trial: the solve twice (the first run also builds the graph), the
   // second one's device time; the summed final cost
-  auto trial = [&](Engine &eng, int step, int chunk, int unroll, int cams, int cap, double *ms,
+  auto trial = [&](Engine &eng, int step, int chunk, int unroll, int cams, int cap, int ctas, double *ms,
                    double *cost) -> gba_status {
-    eng.set_tuning(chunk, unroll, cams, cap);
+    eng.set_tuning(chunk, unroll, cams, cap, ctas);
     for (int rep = 0; rep < 2; ++rep) {
       for (int i = 0; i < n; ++i)
         std::memcpy(params[i].data(), problems[i].parameters, params[i].size() * sizeof(double));
@@ -101,6 +102,7 @@ gba_status autotune(Engine &target, const gba_problem_view *problems, int n, gba
       out->trial_unroll[t] = unroll;
       out->trial_cameras_per_cta[t] = cams;
       out->trial_cap[t] = cap;
+      out->trial_grid_ctas[t] = ctas;
       out->trial_final_cost[t] = *cost;
     }
     ++t;
@@ -128,7 +130,7 @@ gba_status autotune(Engine &target, const gba_problem_view *problems, int n, gba
     for (int c : chunks)
       for (size_t k = 0; k < unrolls.size(); ++k) {
         const int u = unrolls[k];
-        if ((st = trial(eng, 1, c, u, 0, 0, &ms, &cost)) != GBA_OK) return st;
+        if ((st = trial(eng, 1, c, u, 0, 0, 0, &ms, &cost)) != GBA_OK) return st;
         if (eng.one_launch_pcg()) unrolls.assign(1, u);
         if (ms < best) {
           best = ms;
@@ -137,15 +139,28 @@ gba_status autotune(Engine &target, const gba_problem_view *problems, int n, gba
           out->best_ms = ms;
         }
       }
-    // 2. cameras per CTA of the cluster PCG (the default split is step 1's
-    //    best trial)
+    // 2. cameras per CTA of the cluster PCG, or the CTAs of the grid PCG
+    //    (the defaults are step 1's best trial)
     if (eng.cluster_pcg()) {
       double best2 = best;
       for (int cams : {16, 32, 64}) {
-        if ((st = trial(eng, 2, out->chunk_observations, out->pcg_unroll, cams, 0, &ms, &cost)) != GBA_OK) return st;
+        if ((st = trial(eng, 2, out->chunk_observations, out->pcg_unroll, cams, 0, 0, &ms, &cost)) != GBA_OK)
+          return st;
         if (ms < best2) {
           best2 = ms;
           out->pcg_cameras_per_cta = cams;
+        }
+      }
+    } else if (eng.grid_pcg_ctas() > 0) {
+      const int full = eng.grid_pcg_ctas();
+      double best2 = best;
+      for (int ctas : {3 * full / 4, full / 2, full / 4}) {
+        if (ctas < 1) continue;
+        if ((st = trial(eng, 2, out->chunk_observations, out->pcg_unroll, 0, 0, ctas, &ms, &cost)) != GBA_OK)
+          return st;
+        if (ms < best2) {
+          best2 = ms;
+          out->pcg_grid_ctas = ctas;
         }
       }
     }
@@ -159,15 +174,15 @@ gba_status autotune(Engine &target, const gba_problem_view *problems, int n, gba
     if ((st = eng.init(err)) != GBA_OK) return st;
     const int cap0 = std::max(1, (int)base.max_linear_solver_iterations);
     double ms0 = 0.0, cost0 = 0.0;
-    if ((st = trial(eng, 3, out->chunk_observations, out->pcg_unroll, out->pcg_cameras_per_cta, cap0, &ms0,
-                    &cost0)) != GBA_OK)
+    if ((st = trial(eng, 3, out->chunk_observations, out->pcg_unroll, out->pcg_cameras_per_cta, cap0,
+                    out->pcg_grid_ctas, &ms0, &cost0)) != GBA_OK)
       return st;
     out->pcg_cap = cap0;
     double best3 = ms0;
     for (int cap = cap0 / 2; cap >= 10; cap /= 2) {
       double ms = 0.0, cost = 0.0;
-      if ((st = trial(eng, 3, out->chunk_observations, out->pcg_unroll, out->pcg_cameras_per_cta, cap, &ms,
-                      &cost)) != GBA_OK)
+      if ((st = trial(eng, 3, out->chunk_observations, out->pcg_unroll, out->pcg_cameras_per_cta, cap,
+                      out->pcg_grid_ctas, &ms, &cost)) != GBA_OK)
         return st;
       if (!(cost <= cost0 * (1.0 + kCapCostTol))) break;  // smaller caps go further off
       if (ms < best3) {
@@ -181,7 +196,8 @@ gba_status autotune(Engine &target, const gba_problem_view *problems, int n, gba
     std::lock_guard<std::mutex> lk(g_tune_mu);
     g_tune_cache[key] = *out;
   }
-  target.set_tuning(out->chunk_observations, out->pcg_unroll, out->pcg_cameras_per_cta, out->pcg_cap);
+  target.set_tuning(out->chunk_observations, out->pcg_unroll, out->pcg_cameras_per_cta, out->pcg_cap,
+                    out->pcg_grid_ctas);
   return GBA_OK;
 }
 

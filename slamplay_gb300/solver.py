@@ -224,11 +224,12 @@ class Solver:
         N.check(N.lib().gba_autotune(self._h, views, len(problems), N.C.byref(r)), self._h, "gba_autotune")
         n = min(r.num_trials, N.TUNE_MAX_TRIALS)
         return {"chunk_observations": r.chunk_observations, "pcg_unroll": r.pcg_unroll, "best_ms": r.best_ms,
-                "pcg_cameras_per_cta": r.pcg_cameras_per_cta, "pcg_cap": r.pcg_cap,
+                "pcg_cameras_per_cta": r.pcg_cameras_per_cta, "pcg_cap": r.pcg_cap, "pcg_grid_ctas": r.pcg_grid_ctas,
                 "from_cache": bool(r.from_cache),
                 "trials": [{"step": r.trial_step[i], "chunk_observations": r.trial_chunk[i],
                             "pcg_unroll": r.trial_unroll[i], "pcg_cameras_per_cta": r.trial_cameras_per_cta[i],
-                            "pcg_cap": r.trial_cap[i], "ms": r.trial_ms[i], "final_cost": r.trial_final_cost[i]}
+                            "pcg_cap": r.trial_cap[i], "pcg_grid_ctas": r.trial_grid_ctas[i], "ms": r.trial_ms[i],
+                            "final_cost": r.trial_final_cost[i]}
                            for i in range(n)]}
 
     def evaluate(self, problem: BALProblem):
