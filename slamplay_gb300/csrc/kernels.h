@@ -63,7 +63,8 @@ struct GridPlan {
 };
 // Sizes the launch from the problem's explicit-complement rows (sblk_row,
 // nc + 1); false when the form does not apply (a batch, the mixed form,
-// the implicit complement) or its kernel cannot be resident.  ctas: the
+// the implicit complement), when the CTAs' blocks of S would not stay in
+// shared memory, or when its kernel cannot be resident.  ctas: the
 // CTAs of the launch (one per SM at most; 0 = every SM).
 bool pcg_grid_plan(int num_problems, bool mixed, bool explicit_schur, int nc, const int32_t *sblk_row, int ctas,
                    GridPlan *plan);
