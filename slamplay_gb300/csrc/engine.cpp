@@ -177,6 +177,9 @@ size_t Engine::layout(const HostBatch &hb, char *base, DeviceBatch *db, size_t *
   b.seg_slot = cv.take<int32_t>(ns);
   b.cam_obs_begin = cv.take<int32_t>(nc + 1);
   b.cam_obs_list = cv.take<int32_t>(no);
+  const int npieces = hb.cam_piece_begin.empty() ? 0 : hb.cam_piece_begin.back();
+  b.cam_piece_begin = cv.take<int32_t>(hb.cam_piece_begin.size());
+  b.npieces = npieces;
   b.camblk = cv.take<int4>(nb);
   b.cam_init = cv.take<double>(9 * nc);
   b.pt_init = cv.take<double>(4 * np);
@@ -259,6 +262,8 @@ size_t Engine::layout(const HostBatch &hb, char *base, DeviceBatch *db, size_t *
   b.pcg_zf = cv.take<float>(9 * nc);
   b.pcg_pf = cv.take<float>(9 * nc);
   b.cam_colnorm = cv.take<double>(9 * nc);
+  b.piece_part = cv.take<double>(mixed_ ? 0 : 54 * (size_t)npieces);
+  b.cam_counter = cv.take<uint32_t>(mixed_ ? 0 : nc);
   b.seg_partial = cv.take<double>(9 * ns);
   b.schur_partial = cv.take<char>(54 * ns * rs);
   b.seg_grad = cv.take<double>(mixed_ ? 9 * ns : 0);
@@ -399,6 +404,7 @@ gba_status Engine::upload(const HostBatch &hb, std::string *err) {
   sc.put(hdb.seg_slot, hb.seg_slot);
   sc.put(hdb.cam_obs_begin, hb.cam_obs_begin);
   sc.put(hdb.cam_obs_list, hb.cam_obs_list);
+  sc.put(hdb.cam_piece_begin, hb.cam_piece_begin);
   sc.put(hdb.camblk, hb.camblk);
   if (hb.explicit_schur) {
     sc.put(hdb.sblk_row, hb.sblk_row);
@@ -554,6 +560,7 @@ void Engine::zero_counters(cudaStream_t s) {
   cudaMemsetAsync(db_.prob_counter, 0, 4 * sizeof(uint32_t) * (size_t)db_.num_problems, s);
   cudaMemsetAsync(db_.global_counter, 0, 8 * sizeof(uint32_t), s);
   if (db_.nchunks > 0) cudaMemsetAsync(db_.chunk_counter, 0, sizeof(uint32_t) * (size_t)db_.nchunks, s);
+  if (!mixed_ && db_.nc > 0) cudaMemsetAsync(db_.cam_counter, 0, sizeof(uint32_t) * (size_t)db_.nc, s);
 }
 
 void Engine::enqueue_setup(cudaStream_t s) {

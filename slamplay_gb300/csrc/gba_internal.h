@@ -15,6 +15,7 @@ namespace gba {
 // thread per observation.  A chunk is a run of consecutive points (in the
 // internal point order) whose observations fit in kChunkCap.
 constexpr int kChunkCap = 256;
+constexpr int kCamPieceObs = 256;  // observations of one piece of a camera's list (FP64 K1c)
 constexpr int kChunkCapLarge = 1024;  // problems with a point seen > 256 times
 
 // Per-chunk metadata (all indices global over the batch).
@@ -119,6 +120,13 @@ struct DeviceBatch {
   const int32_t *cam_seg_begin;  // nc + 1: each camera's run of partials (camera-major)
   const int32_t *seg_slot;       // camera-major position of each segment's partial
   const int32_t *cam_obs_begin, *cam_obs_list;
+  // the FP64 camera kernel's pieces: camera c's observation list in pieces
+  // of kCamPieceObs, pieces [cam_piece_begin[c], cam_piece_begin[c + 1]);
+  // per piece its 54 sums, per camera the count of its pieces done
+  const int32_t *cam_piece_begin;
+  int32_t npieces;
+  double *piece_part;
+  uint32_t *cam_counter;
   // parameters: the uploaded initial point, and two working buffers of
   // which LMState::parity picks the current one
   const double *cam_init;    // nc * 9

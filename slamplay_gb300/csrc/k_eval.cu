@@ -604,6 +604,95 @@ __global__ void __launch_bounds__(kCamThreads) k_eval_camera(DeviceBatch B) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// K1c, FP64 form: J_c^T J_c and J_c^T r of a camera over pieces of its
+// observation list (kCamPieceObs each), a CTA per piece, so the work of a
+// few hundred cameras spreads over all SMs (one CTA per camera left most of
+// them idle behind the cameras with the most observations).  Each thread
+// sums its observations with FMA chains (2 FP64 FMAs per entry); the
+// piece's sums are the threads' values added in thread order (a column per
+// thread, shared memory); the camera's last piece to finish (a counter per
+// camera, reset by it) adds the pieces' sums in piece order and writes the
+// camera's values.  Every sum has a fixed order.
+constexpr int kPieceThreads = 64;
+
+__global__ void __launch_bounds__(kPieceThreads) k_eval_camera_pieces(DeviceBatch B) {
+  __shared__ double part[kPieceThreads][55];
+  __shared__ double tot[54];
+  __shared__ int last;
+  const int piece = blockIdx.x, t = threadIdx.x;
+  // the camera of the piece: cam_piece_begin[c] <= piece < cam_piece_begin[c + 1]
+  int lo = 0, hi = B.nc;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (B.cam_piece_begin[mid] <= piece)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  const int c = lo;
+  const LMState *L = B.lm + B.cam_problem[c];
+  if (!L->active || !L->need_jacobian) return;
+  const int k0 = B.cam_piece_begin[c], npc = B.cam_piece_begin[c + 1] - k0;
+  const int e1 = B.cam_obs_begin[c + 1];
+  const int o0 = B.cam_obs_begin[c] + (piece - k0) * kCamPieceObs, o1 = min(o0 + kCamPieceObs, e1);
+  double acc[54];
+#pragma unroll
+  for (int q = 0; q < 54; ++q) acc[q] = 0.0;
+  for (int k = o0 + t; k < o1; k += kPieceThreads) {
+    const int64_t o = B.cam_obs_list[k];
+    double2 J[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) J[q] = jload<double2>(B.jac, B.no, q, o);
+    const double2 r = jload<double2>(B.jac, B.no, 12, o);
+#pragma unroll
+    for (int a = 0; a < 9; ++a) {
+#pragma unroll
+      for (int b = a; b < 9; ++b) acc[sym9(a, b)] = fma(J[a].y, J[b].y, fma(J[a].x, J[b].x, acc[sym9(a, b)]));
+      acc[45 + a] = fma(J[a].y, r.y, fma(J[a].x, r.x, acc[45 + a]));
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < 54; ++q) part[t][q] = acc[q];
+  __syncthreads();
+  double s = 0.0;
+  if (t < 54)
+    for (int i = 0; i < kPieceThreads; ++i) s += part[i][t];
+  if (npc > 1) {
+    // the piece's sums to the camera's slots; the last piece adds them up
+    if (t < 54) B.piece_part[54 * (size_t)piece + t] = s;
+    __threadfence();
+    __syncthreads();
+    if (t == 0) last = atomicAdd(B.cam_counter + c, 1u) == (unsigned)(npc - 1);
+    __syncthreads();
+    if (!last) return;
+    if (t < 54) {
+      s = 0.0;
+      for (int q = 0; q < npc; ++q) s += __ldcg(B.piece_part + 54 * (size_t)(k0 + q) + t);
+    }
+    if (t == 0) B.cam_counter[c] = 0u;  // ready for the next evaluation
+  }
+  if (t < 54) tot[t] = s;
+  __syncthreads();
+  if (t == 0) {
+    for (int q = 0; q < 45; ++q) B.cam_B[45 * (size_t)c + q] = tot[q];
+    double gmax = 0.0, xn2 = 0.0;
+    const bool used = B.cam_used[c] != 0;
+    const double *x = B.cam_param[L->parity] + 9 * (size_t)c;
+    for (int q = 0; q < 9; ++q) {
+      const double gq = used ? tot[45 + q] : 0.0;
+      B.cam_g[9 * (size_t)c + q] = gq;
+      if (used) {
+        const double gu = gq / B.cam_scale[9 * (size_t)c + q];
+        gmax = fmax(gmax, fabs(x[q] - (x[q] - gu)));
+        xn2 += x[q] * x[q];
+      }
+    }
+    B.cam_scal[(size_t)kCamScal * c + kCC_GMAX] = gmax;
+    B.cam_scal[(size_t)kCamScal * c + kCC_XN2] = xn2;
+  }
+}
+
 void launch_eval_jacobian(const DeviceBatch &b, bool mixed, bool norms, cudaStream_t s) {
   const int gc = b.nchunks;
   if (mixed) {
@@ -620,7 +709,8 @@ void launch_eval_jacobian(const DeviceBatch &b, bool mixed, bool norms, cudaStre
       k_eval_camera<false, true><<<b.nc, kCamThreads, 0, s>>>(b);
     } else {
       k_eval_chunk<false, false><<<gc, kChunkCap, 0, s>>>(b);
-      k_eval_camera<false, false><<<b.nc, kCamThreads, 0, s>>>(b);
+      const int npieces = b.nc > 0 ? (int)b.npieces : 0;
+      if (npieces > 0) k_eval_camera_pieces<<<npieces, kPieceThreads, 0, s>>>(b);
     }
   }
 }

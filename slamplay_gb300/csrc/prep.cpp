@@ -378,7 +378,8 @@ void HostBatch::reset() {
   P = nc = np = no = nchunks = nseg = cam_blocks = 0;
   explicit_schur = false;
   nblk = nup = npairs = 0;
-  for (auto *v : {&pt_obs_begin, &seg_cam, &cam_seg_begin, &cam_obs_begin, &sblk_row, &sblk_up, &sblk_pair})
+  for (auto *v : {&pt_obs_begin, &seg_cam, &cam_seg_begin, &cam_obs_begin, &cam_piece_begin, &sblk_row, &sblk_up,
+                  &sblk_pair})
     v->clear();
   seg_pos.clear();
   cam_used.clear();
@@ -756,6 +757,11 @@ gba_status prepare_batch(const gba_problem_view *views, int n, const PrepOptions
         for (long long k = to * r / runs; k < to * (r + 1) / runs; ++k) hb.cam_obs_list[c[hb.obs_cam[k]]++] = (int32_t)k;
       });
     }
+  }
+  hb.cam_piece_begin.assign((size_t)tc + 1, 0);
+  for (long long c = 0; c < tc; ++c) {
+    const int n = hb.cam_obs_begin[c + 1] - hb.cam_obs_begin[c];
+    hb.cam_piece_begin[c + 1] = hb.cam_piece_begin[c] + std::max(1, (n + kCamPieceObs - 1) / kCamPieceObs);
   }
   if (hb.explicit_schur) build_schur_structure(&hb);
   return GBA_OK;

@@ -29,6 +29,7 @@ struct HostBatch {
   std::vector<uint16_t> seg_pos;
   std::vector<int32_t> seg_cam;
   std::vector<int32_t> cam_seg_begin, seg_slot, cam_obs_begin, cam_obs_list;
+  std::vector<int32_t> cam_piece_begin;  // nc + 1: pieces of kCamPieceObs of each camera's list
   std::vector<int4> camblk;
   // explicit Schur complement (explicit_schur): the off-diagonal camera-camera
   // blocks of S by row camera (CSR over the batch's cameras; a block with
