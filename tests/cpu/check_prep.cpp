@@ -4,7 +4,12 @@
 //    diagonal with their observation pairs (camera-major F positions) in
 //    point order;
 //  - each chunk's camera-sorted observation order is stable and its
-//    segments are the chunk's distinct cameras in increasing order.
+//    segments are the chunk's distinct cameras in increasing order;
+//  - each camera's observation list in pieces of kCamPieceObs (at least
+//    one piece a camera);
+//  - a resumed problem's state: the Jacobi scales gathered to user order
+//    and set back into a batch land where they were (set_resume inverts
+//    gather_scales), the LM state carried.
 // Usage: check_prep <num_cameras> <num_points> <seed>; prints "ok" or the
 // first mismatch and exits non-zero.
 #include <algorithm>
@@ -122,6 +127,42 @@ int main(int argc, char **argv) {
       printf("chunk %d segment count\n", ch);
       return 1;
     }
+  }
+  // pieces of the cameras' observation lists
+  if ((int)hb.cam_piece_begin.size() != hb.nc + 1 || hb.cam_piece_begin[0] != 0) {
+    printf("piece table size\n");
+    return 1;
+  }
+  for (int c = 0; c < hb.nc; ++c) {
+    const int n = hb.cam_obs_begin[c + 1] - hb.cam_obs_begin[c];
+    const int want = std::max(1, (n + kCamPieceObs - 1) / kCamPieceObs);
+    if (hb.cam_piece_begin[c + 1] - hb.cam_piece_begin[c] != want) {
+      printf("camera %d pieces\n", c);
+      return 1;
+    }
+  }
+  // resume: gather_scales then set_resume is the identity on the scales
+  {
+    std::vector<double> cs(9 * (size_t)hb.nc), ps(3 * (size_t)hb.np);
+    for (size_t i = 0; i < cs.size(); ++i) cs[i] = 1.0 + 0.001 * (double)i;
+    for (size_t i = 0; i < ps.size(); ++i) ps[i] = 2.0 + 0.001 * (double)i;
+    ProblemState st;
+    gather_scales(hb, 0, cs.data(), ps.data(), &st);
+    st.lm.iteration = 7;
+    st.lm.radius = 123.5;
+    set_resume(hb, 0, st);
+    if (hb.resume.size() != 1 || hb.resume[0] != 1 || hb.resume_lm[0].iteration != 7 ||
+        hb.resume_lm[0].radius != 123.5 || hb.resume_cam_scale != cs || hb.resume_pt_scale != ps) {
+      printf("resume round trip\n");
+      return 1;
+    }
+    // user order: point j of the input is internal point inv(j)
+    for (int ji = 0; ji < hb.np; ++ji)
+      for (int q = 0; q < 3; ++q)
+        if (st.pt_scale[3 * (size_t)hb.pt_orig[ji] + q] != ps[3 * (size_t)ji + q]) {
+          printf("resume point order\n");
+          return 1;
+        }
   }
   printf("ok nblk %lld nup %lld npairs %lld chunks %d\n", hb.nblk, hb.nup, hb.npairs, hb.nchunks);
   return 0;

@@ -60,7 +60,8 @@ static bool same(const HostBatch &a, const HostBatch &b) {
   ok = ok && eq(a.obs_cam, b.obs_cam) && eq(a.obs_pt, b.obs_pt) && eq(a.obs_uv, b.obs_uv) &&
        eq(a.obs_seg, b.obs_seg) && eq(a.obs_slot, b.obs_slot) && eq(a.pt_obs_begin, b.pt_obs_begin) &&
        eq(a.seg_cam, b.seg_cam) && eq(a.seg_pos, b.seg_pos) && eq(a.seg_slot, b.seg_slot) &&
-       eq(a.cam_obs_begin, b.cam_obs_begin) && eq(a.cam_obs_list, b.cam_obs_list) && eq(a.pt_param, b.pt_param) &&
+       eq(a.cam_obs_begin, b.cam_obs_begin) && eq(a.cam_obs_list, b.cam_obs_list) &&
+       eq(a.cam_piece_begin, b.cam_piece_begin) && eq(a.pt_param, b.pt_param) &&
        eq(a.cam_param, b.cam_param) && eq(a.cam_used, b.cam_used) && eq(a.pt_used, b.pt_used) &&
        eq(a.pt_orig, b.pt_orig);
   if (ok && a.explicit_schur)
