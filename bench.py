@@ -674,7 +674,7 @@ def serving_form(n_requests: int = 1000, pool: int = 64, rate_mults=(2.0, 5.0, 1
     request its own parameter array).  A sequential plain FP64 loop over the
     first `seq_sample` problems sets the reference rate; the mixed-precision
     server then takes `n_requests` Poisson arrivals at each multiple of that
-    rate (continuous batching over four engine slots, requests joining
+    rate (continuous batching over eight engine slots, requests joining
     running cohorts at LM-iteration boundaries); latency = completion seen by
     the client - submit."""
     import numpy as np

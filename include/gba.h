@@ -191,7 +191,7 @@ typedef struct gba_options {
   int32_t lm_policy;                  /* gba_lm_policy, GBA_LM_POLICY_CERES          */
   int32_t camera_layout;              /* gba_camera_layout, GBA_CAMERA_ANGLE_AXIS    */
   int32_t server_slots;               /* serving: cohorts solved concurrently (engine
-                                         slots, one stream each), 1..16, 0 = 4     */
+                                         slots, one stream each), 1..16, 0 = 8     */
 } gba_options;
 
 /* Per-solve report, the subset of ceres::Solver::Summary the reference

@@ -26,9 +26,9 @@ namespace {
 double now_s() {
   return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
-constexpr int kDefaultSlots = 4;
+constexpr int kDefaultSlots = 8;
 constexpr int kSegmentBodies = 1;            // LM iterations a cohort runs between boundaries
-constexpr long long kCohortObs = 1LL << 22;  // observations a cohort takes in (one request more if alone)
+constexpr long long kCohortObs = 1LL << 21;  // observations a cohort takes in (one request more if alone)
 constexpr int kReformDiv = 4;                // re-form when leavers + joiners >= 1/kReformDiv of the cohort
 }  // namespace
 
