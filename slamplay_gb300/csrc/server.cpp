@@ -19,6 +19,8 @@
 #include <algorithm>
 #include <chrono>
 #include <cstring>
+#include <new>
+#include <stdexcept>
 
 namespace gba {
 
@@ -194,9 +196,9 @@ void Server::launch_cohort(Slot &s, std::vector<std::shared_ptr<Request>> &&keep
   s.delivered.assign(s.reqs.size(), 0);
   s.views.clear();
   for (auto &r : s.reqs) s.views.push_back(r->view);
-  s.state = SlotState::kPreparing;
   s.prep_done.store(0, std::memory_order_relaxed);
-  s.worker = std::thread([this, &s] { prepare_and_start(s); });
+  s.worker = std::thread([this, &s] { prepare_and_start(s); });  // may throw: the slot is not marked yet
+  s.state = SlotState::kPreparing;
 }
 
 // On the slot's worker thread: the loop does not touch the slot until
@@ -204,13 +206,23 @@ void Server::launch_cohort(Slot &s, std::vector<std::shared_ptr<Request>> &&keep
 void Server::prepare_and_start(Slot &s) {
   std::string err;
   const double t0 = now_s();
-  const PrepOptions po = s.engine->prep_options();
-  gba_status st = prepare_batch(s.views.data(), (int)s.views.size(), po, &s.hb, &err);
-  if (st == GBA_OK)
-    for (size_t i = 0; i < s.resume.size(); ++i) set_resume(s.hb, (int)i, s.resume[i]);
-  s.resume.clear();
-  if (st == GBA_OK) st = s.engine->upload(s.hb, &err);
-  const double t1 = now_s();
+  double t1 = t0;
+  gba_status st = GBA_OK;
+  try {
+    const PrepOptions po = s.engine->prep_options();
+    st = prepare_batch(s.views.data(), (int)s.views.size(), po, &s.hb, &err);
+    if (st == GBA_OK)
+      for (size_t i = 0; i < s.resume.size(); ++i) set_resume(s.hb, (int)i, s.resume[i]);
+    s.resume.clear();
+    if (st == GBA_OK) st = s.engine->upload(s.hb, &err);
+  } catch (const std::bad_alloc &) {
+    st = GBA_ERR_OUT_OF_MEMORY;
+    err = "host memory exhausted while laying out a cohort";
+  } catch (const std::exception &e) {
+    st = GBA_ERR_INTERNAL;
+    err = std::string("laying out a cohort: ") + e.what();
+  }
+  t1 = now_s();
   if (st == GBA_OK) st = s.engine->run_segment(false, &err);
   if (st == GBA_OK) st = s.engine->fetch_states(&err);
   if (st == GBA_OK && cudaEventRecord(s.done_ev, s.engine->stream()) != cudaSuccess) {
@@ -356,6 +368,21 @@ void Server::boundary(Slot &s) {
   ++st_.steps;
 }
 
+// Runs a step of the loop for slot s; a host exception (memory, thread
+// creation) fails the slot's requests instead of ending the process.  The
+// steps start a worker only as their last action, so no worker is running
+// when one throws.
+template <typename F>
+void Server::guarded(Slot &s, F &&f) {
+  try {
+    f();
+  } catch (const std::bad_alloc &) {
+    if (s.state != SlotState::kPreparing) fail_cohort(s, GBA_ERR_OUT_OF_MEMORY, "host memory exhausted");
+  } catch (const std::exception &e) {
+    if (s.state != SlotState::kPreparing) fail_cohort(s, GBA_ERR_INTERNAL, e.what());
+  }
+}
+
 void Server::loop() {
   // engines are created on this thread, bound to the configured device
   {
@@ -413,14 +440,14 @@ void Server::loop() {
       std::vector<std::shared_ptr<Request>> take = take_queued(kCohortObs, &bytes);
       if (take.empty()) break;
       s.bytes = bytes;
-      launch_cohort(s, {}, {}, {}, std::move(take));
+      guarded(s, [&] { launch_cohort(s, {}, {}, {}, std::move(take)); });
       did = true;
     }
     // cohorts at an LM-iteration boundary: results out, continue or re-form
     for (auto &sp : slots_) {
       Slot &s = *sp;
       if (s.state == SlotState::kRunning && cudaEventQuery(s.done_ev) == cudaSuccess) {
-        boundary(s);
+        guarded(s, [&] { boundary(s); });
         did = true;
       }
     }

@@ -81,6 +81,8 @@ class Server {
   void boundary(Slot &s);
   void finish(Slot &s, const std::vector<int> &members, const std::vector<gba_summary> &sums);
   void fail_cohort(Slot &s, gba_status st, const std::string &err);
+  template <typename F>
+  void guarded(Slot &s, F &&f);
 
   gba_options o_;
   std::thread thread_;
