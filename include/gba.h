@@ -209,8 +209,10 @@ typedef struct gba_summary {
   double final_trust_region_radius;
   double gradient_max_norm;       /* at the returned parameters                   */
   double setup_time_s;            /* host prep + H2D + device setup               */
-  double solve_time_s;            /* device LM loop (CUDA events)                 */
-  double total_time_s;            /* wall time of the call                        */
+  double solve_time_s;            /* device LM loop (CUDA events); for a served
+                                     request, as total_time_s                    */
+  double total_time_s;            /* wall time of the call; for a served request,
+                                     from admission to delivery                  */
   /* Optional per-iteration trace, caller-allocated; may be NULL.  Entry k is
    * iteration k (0 = initial point): cost, trust radius, PCG iterations and
    * step_is_successful, as in Ceres' IterationSummary. */

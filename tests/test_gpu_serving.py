@@ -50,6 +50,7 @@ def test_served_results_equal_alone():
         s.stop_server()
     assert len(results) == len(tickets)
     assert stats["peak_live"] > 1  # requests were on the device together
+    assert stats["host_prep_s"] > 0.0  # cohorts laid out on the slots' worker threads
     for i, t in enumerate(tickets):
         assert np.array_equal(served[i].parameters(), alone[i][0]), i
         assert results[t].final_cost == alone[i][1]
