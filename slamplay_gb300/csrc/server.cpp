@@ -229,8 +229,12 @@ void Server::prepare_and_start(Slot &s) {
     st = GBA_ERR_CUDA;
     err = "event record";
   }
-  // the graph of the next segments, built while the first one runs
-  if (st == GBA_OK) st = s.engine->prepare_continue(&err);
+  // the graph of the next segments, built while the first one runs (a
+  // failure here is not the cohort's: the first continue builds it again)
+  if (st == GBA_OK) {
+    std::string ignored;
+    s.engine->prepare_continue(&ignored);
+  }
   s.prep_status = st;
   s.prep_error = err;
   {
