@@ -185,7 +185,11 @@ typedef struct gba_options {
                                          launch where the form allows: the mixed
                                          precision as a thread-block cluster per
                                          problem, the FP64 form of a single problem
-                                         over the whole GPU (grid-wide barriers);
+                                         over the whole GPU (grid-wide barriers; it
+                                         expects the GPU to itself: beside other
+                                         kernels it runs on the SMs it finds free,
+                                         correct but slower; the server's slots
+                                         keep the two-kernel FP64 PCG);
                                          0 = one launch pair per PCG iteration      */
   int32_t camera_update;              /* gba_camera_update, GBA_CAMERA_UPDATE_ADDITIVE */
   int32_t lm_policy;                  /* gba_lm_policy, GBA_LM_POLICY_CERES          */

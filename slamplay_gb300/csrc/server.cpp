@@ -398,6 +398,12 @@ void Server::loop() {
       gba_options so = o_;
       so.stream = nullptr;
       so.use_graphs = 1;
+      // the FP64 grid PCG spreads one problem over every SM; cohorts of
+      // other slots run beside it, and a grid launch that finds the SMs
+      // taken proceeds with the CTAs that start (correct, but slow), so the
+      // slots keep the two-kernel FP64 PCG (the mixed form's clusters hold
+      // 16 SMs each and share the GPU)
+      if (so.precision == GBA_PRECISION_FP64) so.persistent_pcg = 0;
       s.engine.reset(new Engine(so));
       std::string err;
       const gba_status st = s.engine->init(&err);
