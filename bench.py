@@ -389,7 +389,9 @@ def run_gpu(args) -> None:
         acc_m = accuracy_vs(orc, res_m.parameters(), first_m.final_cost, nc, no) if orc else None
         extra_forms = {}
         if world == 1 and not args.no_extra_forms:
-            for name, form in (("large", large_form), ("batched", batched_form), ("serving", serving_form),
+            serving = lambda: serving_form(n_requests=args.serving_requests,
+                                           rate_mults=tuple(float(x) for x in args.serving_rates.split(",")))
+            for name, form in (("large", large_form), ("batched", batched_form), ("serving", serving),
                                ("g2o_variant", g2o_variant_form), ("local_ba", local_ba_form)):
                 try:
                     extra_forms[name] = form()
@@ -766,6 +768,10 @@ def main():
                     help="with --profile-solve: the cluster PCG (1) or two kernels per PCG iteration (0)")
     ap.add_argument("--lm-iterations", type=int, default=0,
                     help="with --profile-solve: LM iterations (0 = the workload's 50)")
+    ap.add_argument("--serving-requests", type=int, default=1000,
+                    help="Poisson requests per arrival rate in the serving form")
+    ap.add_argument("--serving-rates", default="2,5,10",
+                    help="arrival rates of the serving form, as multiples of the sequential FP64 rate")
     ap.add_argument("--no-extra-forms", action="store_true",
                     help="skip the large, batched, serving and local-BA forms")
     ap.add_argument("--local-ba-only", action="store_true",
