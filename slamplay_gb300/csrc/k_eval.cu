@@ -238,10 +238,24 @@ __device__ __forceinline__ DF operator+(DF a, DF b) { return df_add(a, b); }
 __device__ __forceinline__ DF operator-(DF a, DF b) { return df_add(a, df_neg(b)); }
 __device__ __forceinline__ DF operator*(DF a, DF b) { return df_mul(a, b); }
 __device__ __forceinline__ DF operator-(DF a) { return df_neg(a); }
+// 1 / b in double-float: a float quotient and one correction step
+__device__ __forceinline__ DF df_recip(DF b) {
+  const float q1 = __fdiv_rn(1.f, b.hi);
+  const DF r = df_add(DF{1.f, 0.f}, df_neg(df_mul_f(b, q1)));
+  const float q2 = __fdiv_rn(r.hi, b.hi);
+  return df_fast_two_sum(q1, q2);
+}
 
+// cost64: the projection and the cost in FP64 (the first evaluation of a
+// problem, whose cost starts the LM); otherwise the projection runs in
+// double-float from the double-float camera table and the cost is not
+// formed (0): the LM keeps the FP64 cost of the candidate evaluation (K2)
+// that made this point current.  The residual then carries ~2^-44 of the
+// predicted pixel, far below what the FP32-stored Jacobian and Schur
+// products resolve.
 __device__ __forceinline__ double eval_observation_df(const DeviceBatch &B, int64_t o, int c, int j,
                                                       const double *X, float2 *Jc, float2 *Jp, float2 &r,
-                                                      DF *gr, bool &bad) {
+                                                      DF *gr, bool &bad, bool cost64) {
   if (B.opt.pinhole) {
     double jd[12], kd[12], rud, rvd;
     bool ok;
@@ -265,11 +279,30 @@ __device__ __forceinline__ double eval_observation_df(const DeviceBatch &B, int6
     const float2 v = td[k];
     return DF{v.x, v.y};
   };
-  Proj pr;
-  project(tab, X, B.obs_uv[o], pr);
-  const DF iz = df_from_double(pr.iz), xp = df_from_double(pr.xp), yp = df_from_double(pr.yp);
-  const DF r2 = df_from_double(pr.r2), dist = df_from_double(pr.dist);
   const DF f = T(39), k1 = T(40), k2 = T(41);
+  const DF Xd[3] = {df_from_double(X[0]), df_from_double(X[1]), df_from_double(X[2])};
+  DF iz, xp, yp, r2, dist;
+  double ru, rv, cost = 0.0;
+  if (cost64) {
+    Proj pr;
+    project(tab, X, B.obs_uv[o], pr);
+    iz = df_from_double(pr.iz), xp = df_from_double(pr.xp), yp = df_from_double(pr.yp);
+    r2 = df_from_double(pr.r2), dist = df_from_double(pr.dist);
+    ru = pr.ru, rv = pr.rv;
+    cost = block_cost(B.opt.loss, B.opt.loss_scale, ru, rv);
+  } else {
+    DF P[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) P[i] = T(3 * i) * Xd[0] + T(3 * i + 1) * Xd[1] + T(3 * i + 2) * Xd[2] + T(36 + i);
+    iz = df_recip(P[2]);
+    xp = -(P[0] * iz), yp = -(P[1] * iz);
+    r2 = xp * xp + yp * yp;
+    dist = DF{1.f, 0.f} + r2 * (k1 + k2 * r2);
+    const DF fd = f * dist;
+    const double2 uv = B.obs_uv[o];
+    ru = df_value(fd * xp - df_from_double(uv.x));
+    rv = df_value(fd * yp - df_from_double(uv.y));
+  }
   const DF two{2.f, 0.f};
   const DF g = k1 + two * k2 * r2;
   const DF m00 = dist + two * g * xp * xp;
@@ -279,7 +312,6 @@ __device__ __forceinline__ double eval_observation_df(const DeviceBatch &B, int6
   const DF A00 = -(fiz * m00), A01 = -(fiz * m01), A02 = -(fiz * (m00 * xp + m01 * yp));
   const DF A10 = -(fiz * m01), A11 = -(fiz * m11), A12 = -(fiz * (m01 * xp + m11 * yp));
   DF ju[12], jv[12];
-  const DF Xd[3] = {df_from_double(X[0]), df_from_double(X[1]), df_from_double(X[2])};
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     // dP/dw_k = dR_k X
@@ -300,8 +332,6 @@ __device__ __forceinline__ double eval_observation_df(const DeviceBatch &B, int6
   ju[7] = f * r2 * xp, jv[7] = f * r2 * yp;
   ju[8] = f * (r2 * r2) * xp, jv[8] = f * (r2 * r2) * yp;
   const int loss = B.opt.loss;
-  const double cost = block_cost(loss, B.opt.loss_scale, pr.ru, pr.rv);
-  double ru = pr.ru, rv = pr.rv;
   if (loss != GBA_LOSS_TRIVIAL) {
     const Corrector cr = make_corrector(loss, B.opt.loss_scale, ru, rv);
     const DF s1 = df_from_double(cr.sqrt_rho1), al = df_from_double(cr.alpha_sq_norm);
@@ -353,10 +383,12 @@ __device__ __forceinline__ double eval_observation_df(const DeviceBatch &B, int6
 // of large terms that cancel towards zero as the solve converges, so it is
 // formed from the double-float Jacobian in double-float: per point (g_p)
 // here, and per camera as one partial per (chunk, camera segment) in
-// seg_grad (FP64), summed per camera by K1c.  The
-// LM fixed point (g = 0) is then the FP64 one; the FP32 copies only feed the
-// Schur products and the PCG, i.e. the accuracy of each step, not where the
-// steps lead.
+// seg_grad (FP64), summed per camera by K1c.  After a problem's first
+// evaluation the residual itself is projected in double-float (the cost
+// then comes from the FP64 candidate evaluation), so the LM fixed point
+// (g = 0) is the FP64 one to double-float rounding; the FP32 copies only
+// feed the Schur products and the PCG, i.e. the accuracy of each step, not
+// where the steps lead.
 template <bool MIXED, bool NORMS>
 __global__ void __launch_bounds__(kChunkCap) k_eval_chunk(DeviceBatch B) {
   typedef typename Prec<MIXED>::real real;
@@ -385,7 +417,7 @@ __global__ void __launch_bounds__(kChunkCap) k_eval_chunk(DeviceBatch B) {
       if (G64) {
         float2 Jcf[9], Jpf[3], rf;
         DF gr[12];
-        cost = eval_observation_df(B, o, c, j, X, Jcf, Jpf, rf, gr, bad);
+        cost = eval_observation_df(B, o, c, j, X, Jcf, Jpf, rf, gr, bad, L->iteration == 0 && L->resumed == 0);
         const int slot = B.obs_slot[o];
 #pragma unroll
         for (int k = 0; k < 9; ++k) {
@@ -477,7 +509,9 @@ __global__ void __launch_bounds__(kChunkCap) k_eval_chunk(DeviceBatch B) {
       }
     }
     if (!NORMS) {
-      const double cs = block_sum(cost, red);
+      // the mixed form's later evaluations form no cost (eval_observation_df)
+      const bool with_cost = !G64 || (L->iteration == 0 && !L->resumed);
+      const double cs = with_cost ? block_sum(cost, red) : 0.0;
       const double gm = block_max(gmax, red);
       const double xs = block_sum(xn2, red);
       const double bd = block_max(bad ? 1.0 : 0.0, red);
@@ -800,7 +834,11 @@ __global__ void __launch_bounds__(256) k_post_eval(DeviceBatch B, int count_body
       const bool resumed = L->resumed != 0;
       if (o.g2o && L->iteration == 0 && !resumed) L->radius = 1.0 / (kG2oTau * fmax(hmax[0], hmax[1]));
       L->need_jacobian = 0;
-      L->x_cost = cost;
+      // the mixed form forms the FP64 cost only at a problem's first
+      // evaluation; later the current point's cost is the FP64 cost of the
+      // candidate evaluation that was accepted (already in x_cost)
+      const bool cost_here = !o.mixed || (L->iteration == 0 && !resumed);
+      if (cost_here) L->x_cost = cost;
       L->gradient_max_norm = fmax(gp, gc);
       L->x_norm = sqrt(xc + xp);
       L->resumed = 0;
@@ -808,7 +846,7 @@ __global__ void __launch_bounds__(256) k_post_eval(DeviceBatch B, int count_body
       if (resumed) {
         // the state was carried over at an LM-iteration boundary: the same
         // point evaluated again (the same bits), nothing else to decide
-      } else if (bad != 0.0 || !isfinite(cost)) {
+      } else if (bad != 0.0 || !isfinite(L->x_cost)) {
         L->active = 0;
         L->termination_type = GBA_TERMINATION_FAILURE;
         L->termination_reason = GBA_REASON_EVALUATION_FAILED;
@@ -819,8 +857,8 @@ __global__ void __launch_bounds__(256) k_post_eval(DeviceBatch B, int count_body
           L->minimum_cost = cost;
           trace_put(B, p, 0, cost, L->radius, 0, 1);
         } else {
-          L->minimum_cost = cost;
-          trace_put(B, p, it, cost, L->radius, L->pcg_iterations, 1);
+          L->minimum_cost = L->x_cost;
+          trace_put(B, p, it, L->x_cost, L->radius, L->pcg_iterations, 1);
         }
         if (o.g2o) {
           // the trials of the iteration that ended with this accepted step
