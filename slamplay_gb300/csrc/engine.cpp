@@ -8,6 +8,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 
 #include "kernels.h"
@@ -105,6 +106,10 @@ gba_status Engine::init(std::string *err) {
   }
   gba_status st;
   if ((st = check(cudaSetDevice(device_), "cudaSetDevice", err)) != GBA_OK) return st;
+  {
+    const char *e = std::getenv("GBA_TEST_GRID_WAIT");
+    grid_wait_test_ = e && e[0] == '1';
+  }
   if ((st = check(probe_kernel_image(), "loading the sm_103a kernels", err)) != GBA_OK) return st;
   if (o_.stream) {
     stream_ = static_cast<cudaStream_t>(o_.stream);
@@ -307,6 +312,7 @@ size_t Engine::layout(const HostBatch &hb, char *base, DeviceBatch *db, size_t *
   if (b.opt.g2o) b.opt.jacobi_scaling = 0;
   b.opt.max_bodies = max_lm_bodies();
   b.opt.bodies_cap = 0;  // set per graph by the segment runs
+  b.opt.grid_wait_test = grid_wait_test_ ? 1 : 0;
   b.opt.pinhole = rig ? 1 : 0;
   b.lm_cond = 0;
   b.pcg_cond = 0;

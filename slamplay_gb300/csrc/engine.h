@@ -126,6 +126,7 @@ class Engine {
   int segment_bodies_ = 0;
   int cluster_cams_ = 0;  // cameras per CTA of the cluster PCG (0 = default)
   int grid_ctas_ = 0;     // CTAs of the grid PCG (0 = every SM)
+  bool grid_wait_test_ = false;  // the grid PCG's wait-runs-out test (DeviceOptions::grid_wait_test)
   int graph_segment_ = -1, graph_c_segment_ = -1;
   std::vector<long long> cur_key_;
   // events

@@ -54,6 +54,9 @@ struct DeviceOptions {
   int32_t max_bodies;  // LM bodies (trials) a solve may run
   int32_t pinhole;     // local-BA windows: the stereo-rig pinhole model, SE3 poses
   int32_t bodies_cap;  // > 0: the LM loop of one launch stops after this many counted bodies
+  int32_t grid_wait_test;  // failure test of the grid PCG (environment GBA_TEST_GRID_WAIT=1 at
+                           // handle creation): every barrier waits for one CTA more than
+                           // registered, so its bounded wait runs out (GBA_ERR_TIMEOUT)
                        // (the problems stay active; a later launch continues them)
 };
 

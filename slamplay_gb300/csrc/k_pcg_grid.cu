@@ -355,6 +355,8 @@ __global__ void __launch_bounds__(kGThreads, 1) k_pcg_grid(DeviceBatch B, int ca
   int k = 0;
   bool linear_ok = true, aborted = false;
   unsigned gen = 0;
+  // CTAs a barrier waits for (one more under the wait-runs-out test)
+  const unsigned bar_n = (unsigned)P + (B.opt.grid_wait_test ? 1u : 0u);
 
   // the update's coordinate of this thread (the camera kernel's lead
   // threads: coordinate m of a camera block in the lanes of 3 warps); with
@@ -445,7 +447,7 @@ __global__ void __launch_bounds__(kGThreads, 1) k_pcg_grid(DeviceBatch B, int ca
       __syncthreads();  // pd and the pass tables are used again
       rl0 = pend;
     }
-    if (!grid_barrier(B, ++gen, (unsigned)P, &s_ok)) {
+    if (!grid_barrier(B, ++gen, bar_n, &s_ok)) {
       aborted = true;
       break;
     }
@@ -566,7 +568,7 @@ __global__ void __launch_bounds__(kGThreads, 1) k_pcg_grid(DeviceBatch B, int ca
         __syncthreads();
       }
     }
-    if (!grid_barrier(B, ++gen, (unsigned)P, &s_ok)) {
+    if (!grid_barrier(B, ++gen, bar_n, &s_ok)) {
       aborted = true;
       break;
     }

@@ -117,3 +117,35 @@ def test_config1_fp64_converged_matches_oracle():
           f"{np.sqrt(2 * sg.final_cost / b.num_observations()):.4f} px")
     assert rel <= 1e-8
     assert sg.termination_type == "CONVERGENCE" and so["termination_type"] == 0
+
+
+def test_grid_pcg_wait_runs_out_and_context_survives(monkeypatch):
+    """The failure path of the grid PCG's bounded waits, without a GPU
+    fault: with GBA_TEST_GRID_WAIT=1 at handle creation every grid barrier
+    waits for one CTA more than registered; the wait runs out after about a
+    second, the abort word ends the other CTAs' waits, the solve reports
+    GBA_ERR_TIMEOUT, and handles created afterwards in the same process
+    solve normally, with the bits of an unaffected solve (the context stays
+    usable)."""
+    import time
+
+    from slamplay_gb300 import GBAError
+
+    b = BALProblem.synthetic(0, seed=3, num_points=600)
+    opts = dict(max_num_iterations=3, pcg_tolerance=1e-6, max_linear_solver_iterations=100, schur="explicit",
+                persistent_pcg=1, **FIXED)
+    monkeypatch.setenv("GBA_TEST_GRID_WAIT", "1")
+    with Solver(**opts) as s:
+        t0 = time.time()
+        with pytest.raises(GBAError) as ei:
+            s.solve(b.copy())
+        waited = time.time() - t0
+        assert ei.value.status == 5, ei.value  # GBA_ERR_TIMEOUT
+        assert 0.5 < waited < 30.0, waited
+    monkeypatch.delenv("GBA_TEST_GRID_WAIT")
+    ref_g, ref, _ = _solve_profiled(b, **opts)
+    with Solver(**opts) as s:
+        g = b.copy()
+        sm = s.solve(g)
+    assert sm.final_cost == ref.final_cost and np.array_equal(g.parameters(), ref_g.parameters())
+    print(f"grid wait ran out after {waited:.2f} s; the next solves are normal")
