@@ -454,7 +454,9 @@ def compact_form(name: str, f: dict) -> dict:
         if name == "batched":
             return {"mixed_solves_per_s": f["mixed"]["solves_per_s"], "fp64_solves_per_s": f["fp64"]["solves_per_s"],
                     "sequential_fp64_solves_per_s": f["sequential_fp64"]["solves_per_s"],
-                    "mixed_vs_fp64_final_cost_rel": f["mixed_vs_fp64_final_cost_rel"]}
+                    "mixed_vs_fp64_final_cost_rel": f["mixed_vs_fp64_final_cost_rel"],
+                    "rms_reprojection_px_median": {k: v["median"] for k, v in f.get("rms_reprojection_px", {}).items()},
+                    "mixed_vs_fp64_camera_rms_diff_median": f.get("mixed_vs_fp64_camera_rms_diff", {}).get("median")}
         if name == "serving":
             return {"sweep": [{k: x[k] for k in ("arrival_rate_per_s", "solves_per_s", "p50_ms", "p99_ms", "reforms")}
                               for x in f["sweep"]], "requests_per_rate": f.get("requests_per_rate"),
@@ -486,8 +488,13 @@ def batched_form(n_problems: int = 1024, repeats: int = 2, seq_sample: int = 32)
     probs = [BALProblem.synthetic(3, index=i, seed=0) for i in range(n_problems)]
     out = {"workload": f"config3: {n_problems} problems, {sum(p.num_observations() for p in probs)} obs",
            "pcg": "residual 1e-6, <= 100"}
-    def timed(s):
-        sums = s.batch_solve([p.copy() for p in probs])
+    solved = {}
+
+    def timed(s, prec=None):
+        work = [p.copy() for p in probs]
+        sums = s.batch_solve(work)
+        if prec:
+            solved[prec] = work
         ts = []
         for _ in range(repeats):
             t0 = time.perf_counter()
@@ -499,7 +506,7 @@ def batched_form(n_problems: int = 1024, repeats: int = 2, seq_sample: int = 32)
     finals = {}
     for prec in ("mixed", "fp64"):
         with Solver(precision=prec, max_num_iterations=50, **PCG_SMALL) as s:
-            sums, t = timed(s)
+            sums, t = timed(s, prec)
             finals[prec] = [x.final_cost for x in sums]
             tune = None
             if prec == "mixed":
@@ -530,6 +537,26 @@ def batched_form(n_problems: int = 1024, repeats: int = 2, seq_sample: int = 32)
     out["mixed_vs_fp64_final_cost_rel"] = {"max": rel[-1], "median": rel[len(rel) // 2],
                                           "p99": rel[int(0.99 * (len(rel) - 1))],
                                           "within_1e-6": sum(1 for r in rel if r <= 1e-6), "problems": len(rel)}
+    # RMS reprojection error of each result and the parameter RMS differences
+    # of the mixed results against the FP64 ones (the FP64 GPU solve as the
+    # reference of this size), as medians / p99 / max over the problems
+    import numpy as np
+
+    def dist(v):
+        v = np.sort(np.asarray(v))
+        return {"median": float(v[len(v) // 2]), "p99": float(v[int(0.99 * (len(v) - 1))]), "max": float(v[-1])}
+
+    rms = {prec: [(2.0 * c / p.num_observations()) ** 0.5 for c, p in zip(finals[prec], probs)]
+           for prec in ("mixed", "fp64")}
+    cam_d, pt_d = [], []
+    for a, b, p in zip(solved["mixed"], solved["fp64"], probs):
+        n9 = 9 * p.num_cameras()
+        pa, pb = a.parameters(), b.parameters()
+        cam_d.append(float(np.sqrt(np.mean((pa[:n9] - pb[:n9]) ** 2))))
+        pt_d.append(float(np.sqrt(np.mean((pa[n9:] - pb[n9:]) ** 2))))
+    out["rms_reprojection_px"] = {prec: dist(v) for prec, v in rms.items()}
+    out["mixed_vs_fp64_camera_rms_diff"] = dist(cam_d)
+    out["mixed_vs_fp64_point_rms_diff"] = dist(pt_d)
     return out
 
 
@@ -652,6 +679,10 @@ def large_form(lm_iterations: int = 10) -> dict:
                      "final_cost": first.final_cost, "kernels": kern}
     out["peak_gbs"] = peak
     out["mixed_vs_fp64_lm_iters"] = out["mixed"]["lm_iters_per_s"] / out["fp64"]["lm_iters_per_s"]
+    # the FP64 GPU solve is this size's reference (the dense oracle does not scale to it)
+    out["mixed_vs_fp64_final_cost_rel"] = abs(finals["mixed"] - finals["fp64"]) / finals["fp64"]
+    for prec in ("mixed", "fp64"):
+        out[prec]["rms_reprojection_px"] = (2.0 * finals[prec] / b.num_observations()) ** 0.5
     return out
 
 
