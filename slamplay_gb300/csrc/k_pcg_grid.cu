@@ -186,7 +186,7 @@ __global__ void __launch_bounds__(kGThreads, 1) k_pcg_grid(DeviceBatch B, int ca
                                                          int cap_pairs) {
   extern __shared__ __align__(16) unsigned char g_smem[];
   __shared__ int s_ticket, s_P, s_ok, s_ra, s_rb, s_stop, s_pass_end, s_npairs, s_nlev;
-  __shared__ double sc[4];
+  __shared__ double sc[4], s_inv_rz;
   __shared__ double tot3[3];
   __shared__ double rv[kGThreads];  // r_{k+1} of the update's coordinates, for M r
   __shared__ double red3[kGWarps][3];
@@ -471,11 +471,18 @@ __global__ void __launch_bounds__(kGThreads, 1) k_pcg_grid(DeviceBatch B, int ca
       }
       if (nch == 0 && t == 0) chs[0] = 0.0;
       __syncthreads();
-      cta_pairwise_tree(chs, nch);
-      if (t == 0) {
-        const double s2 = chs[0];
-        sc[0] = s2;
-        sc[1] = rz_k * recip_nr(s2);
+      if (nch <= 32) {  // the tree by one warp's shuffles (no barrier per level)
+        if (warp == 0) {
+          const double s2 = warp_pairwise_tree(lane < nch ? chs[lane] : 0.0, nch);
+          if (lane == 0) sc[0] = s2, sc[1] = rz_k * recip_nr(s2);
+        }
+      } else {
+        cta_pairwise_tree(chs, nch);
+        if (t == 0) {
+          const double s2 = chs[0];
+          sc[0] = s2;
+          sc[1] = rz_k * recip_nr(s2);
+        }
       }
       __syncthreads();
     }
@@ -582,18 +589,22 @@ __global__ void __launch_bounds__(kGThreads, 1) k_pcg_grid(DeviceBatch B, int ca
       for (int bb = lane; bb < nblk; bb += 32) a += __ldcg(B.blk_red + 3 * (size_t)(pi.cam_block_begin + bb) + warp);
       a = warp_sum(a);
       if (lane == 0) tot3[warp] = a;
-    } else if (staged) {
-      const double *pkb = pbuf(k);
+    } else {
+      if (staged) {
+        const double *pkb = pbuf(k);
 #pragma unroll
-      for (int u = 0; u < kPre; ++u) {
-        const int e = (t - 96) + u * kGPreThreads;
-        zpre[u] = ppre[u] = 0.0;
-        if (e < 9 * nbo) {
-          const size_t gi = 9 * (size_t)scol[e / 9] + e % 9;
-          zpre[u] = __ldcg(B.pcg_z + gi);
-          ppre[u] = __ldcg(pkb + gi);
+        for (int u = 0; u < kPre; ++u) {
+          const int e = (t - 96) + u * kGPreThreads;
+          zpre[u] = ppre[u] = 0.0;
+          if (e < 9 * nbo) {
+            const size_t gi = 9 * (size_t)scol[e / 9] + e % 9;
+            zpre[u] = __ldcg(B.pcg_z + gi);
+            ppre[u] = __ldcg(pkb + gi);
+          }
         }
       }
+      // 1 / r_k.z_k for beta, off the deciding warps' dependent chain
+      if (t == 96) s_inv_rz = recip_nr(rz_k);
     }
     __syncthreads();
     if (t == 0) {
@@ -609,7 +620,7 @@ __global__ void __launch_bounds__(kGThreads, 1) k_pcg_grid(DeviceBatch B, int ca
       }
       if (k1 >= o.max_pcg_iterations) stop = true;
       if (!(rz1 != 0.0 && isfinite(rz1))) stop = true;
-      sc[0] = rz1 * recip_nr(rz_k);  // beta_{k+1}
+      sc[0] = rz1 * s_inv_rz;  // beta_{k+1} (the reciprocal as recip_nr(rz_k))
       sc[1] = rz1;
       sc[2] = rr1;
       sc[3] = qk;

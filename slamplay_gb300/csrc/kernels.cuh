@@ -215,6 +215,17 @@ __device__ __forceinline__ void cta_pairwise_tree(double *x, int m) {
   }
 }
 
+// cta_pairwise_tree's additions over x[0..m), m <= 32, by one warp: lane l
+// holds x[l] (0 beyond m); the sum ends in lane 0.  Call from a whole warp.
+__device__ __forceinline__ double warp_pairwise_tree(double v, int m) {
+  const int lane = (int)(threadIdx.x & 31);
+  for (int s = 1; s < m; s <<= 1) {
+    const double o = __shfl_down_sync(0xffffffffu, v, s);
+    if ((lane & (2 * s - 1)) == 0 && lane + s < m) v += o;
+  }
+  return v;
+}
+
 // The CTA's sum of v[0..n) (global memory, read with __ldcg, or shared
 // memory): chunks of 32 values, each an xor butterfly over a warp's lanes,
 // then the pairwise tree over the chunk sums; `scratch` holds
