@@ -669,7 +669,7 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg_camera(DeviceBatch B) {
     // the block's r.z, r.r, x.(v + r): warp butterflies in the warps that
     // hold the coordinates, then those warps in order (one value per thread)
     if ((t >> 5) < kLeadWarps) {
-      rz = warp_sum(rz), rr = warp_sum(rr), qx = warp_sum(qx);
+      warp_sum3(rz, rr, qx);
       if ((t & 31) == 0) red3[t >> 5][0] = rz, red3[t >> 5][1] = rr, red3[t >> 5][2] = qx;
     }
     __syncthreads();
@@ -693,7 +693,7 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg_camera(DeviceBatch B) {
           const double *bv = B.blk_red + 3 * (size_t)(pi.cam_block_begin + b);
           a3[0] += __ldcg(bv), a3[1] += __ldcg(bv + 1), a3[2] += __ldcg(bv + 2);
         }
-        a3[0] = warp_sum(a3[0]), a3[1] = warp_sum(a3[1]), a3[2] = warp_sum(a3[2]);
+        warp_sum3(a3[0], a3[1], a3[2]);
       }
       if (t == 0) {
         // the stopping test on (x_{k+1}, r_{k+1}) and beta_{k+1}, without

@@ -453,8 +453,11 @@ __global__ void __launch_bounds__(kGThreads, 1) k_pcg_grid(DeviceBatch B, int ca
     }
     // ---- B. each camera's p.q (sum9_tree), their sum (chunks of 32 and the
     // pairwise tree: cta_chunked_sum's order), alpha; the update ---------------
-    double qv_pre = 0.0;
-    if (one_round && u_lead) qv_pre = __ldcg(B.pcg_q + u_i);  // in flight while the cameras are summed
+    double qv_pre = 0.0, up_k = 0.0;
+    if (one_round && u_lead) {
+      qv_pre = __ldcg(B.pcg_q + u_i);         // in flight while the cameras are summed
+      up_k = k == 0 ? uz : fma(beta, up, uz);  // p_k from p_{k-1} (alpha not needed)
+    }
     {
       const int nch = (n + 31) / 32;
       for (int j = warp; j < nch; j += kGWarps) {
@@ -494,7 +497,7 @@ __global__ void __launch_bounds__(kGThreads, 1) k_pcg_grid(DeviceBatch B, int ca
     }
     if (one_round) {
       if (u_lead) {
-        up = k == 0 ? uz : fma(beta, up, uz);  // p_k from p_{k-1}
+        up = up_k;
         ux = fma(alpha, up, ux);
         ur = fma(-alpha, qv_pre, ur);
         rv[t] = ur;
@@ -513,7 +516,7 @@ __global__ void __launch_bounds__(kGThreads, 1) k_pcg_grid(DeviceBatch B, int ca
         }
         // the block's r.z, r.r, x.(v + r): butterflies in its three warps,
         // then the warps in order
-        rz = warp_sum(rz), rr = warp_sum(rr), qx = warp_sum(qx);
+        warp_sum3(rz, rr, qx);
         if (lane == 0) red3[warp][0] = rz, red3[warp][1] = rr, red3[warp][2] = qx;
       }
       __syncthreads();
@@ -563,7 +566,7 @@ __global__ void __launch_bounds__(kGThreads, 1) k_pcg_grid(DeviceBatch B, int ca
             B.pcg_z[i] = z;
             rz = r * z, rr = r * r, qx = x * (v + r);
           }
-          rz = warp_sum(rz), rr = warp_sum(rr), qx = warp_sum(qx);
+          warp_sum3(rz, rr, qx);
           if (lane == 0) red3[warp][0] = rz, red3[warp][1] = rr, red3[warp][2] = qx;
         }
         __syncthreads();

@@ -178,6 +178,30 @@ __device__ __forceinline__ double warp_sum(double v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
+// Three warp_sum calls at once, with the same additions (and bits): the
+// first two butterfly levels split the lanes between the values (after xor
+// 16 lanes 0-15 hold a and b, lanes 16-31 c; after xor 8 lanes 0-7 a, 8-15
+// b, 16-23 c), each lane adding only what its group keeps, so a lane issues
+// 6 FP64 additions instead of 15 (GB300 issues FP64 at one warp
+// instruction per 64 clocks per sub-partition).  Every lane after xor s
+// holds the butterfly's value of its lane, and the butterfly ends with the
+// same value in all lanes.  Every lane gets the three sums.
+__device__ __forceinline__ void warp_sum3(double &a, double &b, double &c) {
+  const unsigned full = 0xffffffffu;
+  const int lane = (int)(threadIdx.x & 31);
+  const bool lo = lane < 16, lo8 = (lane & 8) == 0;
+  const double s1 = __shfl_xor_sync(full, lo ? c : a, 16);
+  const double s2 = __shfl_xor_sync(full, lo ? 0.0 : b, 16);
+  const double k1 = (lo ? a : c) + s1;
+  const double k2 = (lo ? b : 0.0) + s2;
+  double v = (lo8 ? k1 : k2) + __shfl_xor_sync(full, lo8 ? k2 : k1, 8);
+  v += __shfl_xor_sync(full, v, 4);
+  v += __shfl_xor_sync(full, v, 2);
+  v += __shfl_xor_sync(full, v, 1);
+  a = __shfl_sync(full, v, 0);
+  b = __shfl_sync(full, v, 8);
+  c = __shfl_sync(full, v, 16);
+}
 __device__ __forceinline__ double warp_max(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
