@@ -258,12 +258,15 @@ __global__ void __launch_bounds__(kSpmvThreads) k_schur_spmv(DeviceBatch B) {
   }
 }
 
-// K4a' of the FP64 form: one CTA per camera; the block dots of its rows
-// (nine-column FMA chains) into shared memory, `rpp` rows at a time, each
-// row summed by the pairwise tree, then the camera's p.q (sum9_tree of its
-// rows' p_i q_i): the grid PCG's arithmetic, so both forms agree bitwise.
-__global__ void __launch_bounds__(kSpmvThreads) k_schur_spmv64(DeviceBatch B, int rpp) {
-  extern __shared__ double sp_d[];  // [rpp][m]
+// K4a' of the FP64 form: one CTA per camera; the direction p_k = z_k +
+// beta_k p_{k-1} at the columns of the camera's blocks formed once into
+// shared memory (`stage`; else formed at each use, nine times per block),
+// the block dots of its rows (nine-column FMA chains) into shared memory,
+// `rpp` rows at a time, each row summed by the pairwise tree, then the
+// camera's p.q (sum9_tree of its rows' p_i q_i): the grid PCG's arithmetic,
+// so both forms agree bitwise.
+__global__ void __launch_bounds__(kSpmvThreads) k_schur_spmv64(DeviceBatch B, int rpp, int stage) {
+  extern __shared__ double sp_smem[];  // [m][9] staged direction (stage), then [rpp][m]
   __shared__ double pqs[9];
   const int c = blockIdx.x, t = threadIdx.x;
   const int prob = B.cam_problem[c];
@@ -281,15 +284,29 @@ __global__ void __launch_bounds__(kSpmvThreads) k_schur_spmv64(DeviceBatch B, in
   const int r0 = B.sblk_row[c], nb = B.sblk_row[c + 1] - r0, m = nb + 1;
   const double *vals = reinterpret_cast<const double *>(B.sblk_val);
   const double *diag = reinterpret_cast<const double *>(B.cam_Sii) + 81 * (size_t)c;
+  double *sp_p = sp_smem, *sp_d = sp_smem + (stage ? 9 * (size_t)m : 0);
+  if (stage) {  // the diagonal block's column (the camera's own) last
+    for (int e = t; e < 9 * m; e += kSpmvThreads) {
+      const int v = e / 9, cc = e - 9 * v;
+      sp_p[e] = pdir(9 * (size_t)(v < nb ? B.sblk_col[r0 + v] : c) + cc);
+    }
+    __syncthreads();
+  }
   for (int q0 = 0; q0 < 9; q0 += rpp) {
     const int nr = min(rpp, 9 - q0);
     for (int e = t; e < nr * m; e += kSpmvThreads) {
       const int rr = e / m, v = e - rr * m;
       const double *row = (v < nb ? vals + 81 * (size_t)(r0 + v) : diag) + 9 * (q0 + rr);
-      const int col = v < nb ? B.sblk_col[r0 + v] : c;
       double d = 0.0;
+      if (stage) {
+        const double *pp = sp_p + 9 * v;
 #pragma unroll
-      for (int cc = 0; cc < 9; ++cc) d = fma(row[cc], pdir(9 * (size_t)col + cc), d);
+        for (int cc = 0; cc < 9; ++cc) d = fma(row[cc], pp[cc], d);
+      } else {
+        const int col = v < nb ? B.sblk_col[r0 + v] : c;
+#pragma unroll
+        for (int cc = 0; cc < 9; ++cc) d = fma(row[cc], pdir(9 * (size_t)col + cc), d);
+      }
       sp_d[e] = d;
     }
     __syncthreads();
@@ -306,7 +323,7 @@ __global__ void __launch_bounds__(kSpmvThreads) k_schur_spmv64(DeviceBatch B, in
       const size_t i = 9 * (size_t)c + q;
       const double qv = sp_d[t * m];
       B.pcg_q[i] = qv;
-      pqs[q] = pdir(i) * qv;
+      pqs[q] = (stage ? sp_p[9 * nb + q] : pdir(i)) * qv;
     }
     __syncthreads();
   }
@@ -315,13 +332,17 @@ __global__ void __launch_bounds__(kSpmvThreads) k_schur_spmv64(DeviceBatch B, in
 
 // Rows per pass of k_schur_spmv64 and its shared memory, from the longest
 // row (in blocks, the diagonal one included).
-static int spmv64_rows(int m_max, size_t *smem) {
+static int spmv64_rows(int m_max, size_t *smem, int *stage) {
   int optin = 48 * 1024, dev = 0;
   if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   const size_t budget = (size_t)optin - 4096;
+  const size_t mm = (size_t)std::max(m_max, 1);
+  // the staged direction when it leaves room for one row's block dots
+  *stage = 8 * 10 * mm <= budget ? 1 : 0;
+  const size_t rows_budget = budget - (*stage ? 8 * 9 * mm : 0);
   int rpp = 9;
-  while (rpp > 1 && 8 * (size_t)rpp * m_max > budget) --rpp;
-  *smem = 8 * (size_t)rpp * std::max(m_max, 1);
+  while (rpp > 1 && 8 * (size_t)rpp * mm > rows_budget) --rpp;
+  *smem = 8 * (size_t)rpp * mm + (*stage ? 8 * 9 * mm : 0);
   return rpp;
 }
 
@@ -338,13 +359,14 @@ cudaError_t launch_schur_spmv(const DeviceBatch &b, bool mixed, cudaStream_t s, 
   cfg.numAttrs = pdl ? 1 : 0;
   if (mixed) return cudaLaunchKernelEx(&cfg, k_schur_spmv<true>, b);
   size_t smem = 0;
-  const int rpp = spmv64_rows(b.sblk_max, &smem);
+  int stage = 0;
+  const int rpp = spmv64_rows(b.sblk_max, &smem, &stage);
   if (smem > 48 * 1024) {
     const cudaError_t e = raise_smem_limit((const void *)k_schur_spmv64, smem);
     if (e != cudaSuccess) return e;
   }
   cfg.dynamicSmemBytes = smem;
-  return cudaLaunchKernelEx(&cfg, k_schur_spmv64, b, rpp);
+  return cudaLaunchKernelEx(&cfg, k_schur_spmv64, b, rpp, stage);
 }
 
 }  // namespace gba
