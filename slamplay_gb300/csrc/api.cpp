@@ -152,8 +152,8 @@ const char *gba_last_error(const gba_handle *h) {
 // Solves n problems; with the quaternion camera layout the cameras are
 // converted to angle-axis copies first and the results converted back into
 // the callers' arrays (BALProblem.cpp:117-138 loads and writes the same way).
-static gba_status solve_views(gba_handle *h, const gba_problem_view *problems, int32_t n, gba_summary *summaries,
-                              std::string *err) {
+static gba_status solve_nonempty(gba_handle *h, const gba_problem_view *problems, int32_t n, gba_summary *summaries,
+                                 std::string *err) {
   if (h->engine->options().camera_layout != GBA_CAMERA_QUATERNION) {
     gba_status st = maybe_autotune(h, problems, n, err);
     if (st == GBA_OK) st = h->engine->solve(problems, n, summaries, err);
@@ -189,6 +189,47 @@ static gba_status solve_views(gba_handle *h, const gba_problem_view *problems, i
       std::copy(&aa[p][9 * c + 3], &aa[p][9 * c + 9], q + 4);
     }
     std::copy(aa[p].begin() + 9 * nc, aa[p].begin() + 9 * nc + 3 * np, v.parameters + 10 * nc);
+  }
+  return GBA_OK;
+}
+
+// Problems without observations are answered on the host
+// (empty_problem_summary); the others are solved together, in their order.
+static gba_status solve_views(gba_handle *h, const gba_problem_view *problems, int32_t n, gba_summary *summaries,
+                              std::string *err) {
+  std::vector<int32_t> live;
+  live.reserve((size_t)n);
+  for (int32_t p = 0; p < n; ++p) {
+    const gba_problem_view &v = problems[p];
+    if (v.num_observations != 0) {
+      live.push_back(p);
+      continue;
+    }
+    const gba_status vs = gba::validate_problem(&v, err);
+    if (vs != GBA_OK) return vs;
+  }
+  if ((int32_t)live.size() == n) return solve_nonempty(h, problems, n, summaries, err);
+  if (!live.empty()) {
+    std::vector<gba_problem_view> lv;
+    std::vector<gba_summary> ls;
+    for (int32_t p : live) {
+      lv.push_back(problems[p]);
+      if (summaries) ls.push_back(summaries[p]);
+    }
+    const gba_status st = solve_nonempty(h, lv.data(), (int32_t)lv.size(), summaries ? ls.data() : nullptr, err);
+    if (st != GBA_OK) return st;
+    if (summaries)
+      for (size_t j = 0; j < live.size(); ++j) summaries[live[j]] = ls[j];
+  }
+  if (summaries) {
+    const double radius = h->engine->options().initial_trust_region_radius;
+    for (int32_t p = 0, j = 0; p < n; ++p) {
+      if (j < (int32_t)live.size() && live[j] == p) {
+        ++j;
+        continue;
+      }
+      gba::empty_problem_summary(&summaries[p], radius);
+    }
   }
   return GBA_OK;
 }

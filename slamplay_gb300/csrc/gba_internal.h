@@ -16,7 +16,6 @@ namespace gba {
 // internal point order) whose observations fit in kChunkCap.
 constexpr int kChunkCap = 256;
 constexpr int kCamPieceObs = 256;  // observations of one piece of a camera's list (FP64 K1c)
-constexpr int kChunkCapLarge = 1024;  // problems with a point seen > 256 times
 
 // Per-chunk metadata (all indices global over the batch).
 struct ChunkInfo {
@@ -263,5 +262,32 @@ constexpr int kPcgGridThreads = 512;
 // kernel: problems of up to 32 * kPcgChunkSums cameras
 constexpr int kPcgChunkSums = 1024;
 constexpr int kGridReg = 0, kGridCount = 2, kGridBar = 3, kGridAbort = 4;
+
+// A problem without observations has no parameter blocks in the
+// reference's problem (each observation adds its camera and point through
+// AddResidualBlock, test_bundle_adjustment_ceres.cpp:70-87), and Ceres'
+// Solver::Solve returns before the minimizer for such a problem: CONVERGENCE
+// ("Function tolerance reached.  No non-constant parameter blocks found."),
+// cost 0, no iterations.  The library does the same without touching the
+// device; the parameters are left as they are.  The caller's trace buffers
+// are kept (no entries).
+inline void empty_problem_summary(gba_summary *s, double radius) {
+  if (!s) return;
+  s->initial_cost = 0.0;
+  s->final_cost = 0.0;
+  s->num_iterations = 0;
+  s->num_successful_steps = 0;
+  s->num_unsuccessful_steps = 0;
+  s->num_invalid_steps = 0;
+  s->num_linear_solver_iterations = 0;
+  s->termination_type = GBA_TERMINATION_CONVERGENCE;
+  s->termination_reason = GBA_REASON_FUNCTION_TOLERANCE;
+  s->final_trust_region_radius = radius;
+  s->gradient_max_norm = 0.0;
+  s->setup_time_s = 0.0;
+  s->solve_time_s = 0.0;
+  s->total_time_s = 0.0;
+  s->trace_length = 0;
+}
 
 }  // namespace gba

@@ -101,11 +101,18 @@ gba_status Server::submit(const gba_problem_view *p, uint64_t *ticket, std::stri
   r->view = *p;
   r->footprint = fp;
   std::memset(&r->summary, 0, sizeof r->summary);
-  queue_.push_back(r);
   tickets_[r->ticket] = r;
   ++st_.submitted;
-  st_.queued = (int32_t)queue_.size();
   *ticket = r->ticket;
+  if (p->num_observations == 0) {  // nothing to solve: done at once, as gba_solve
+    empty_problem_summary(&r->summary, o_.initial_trust_region_radius);
+    r->done = true;
+    ++st_.completed;
+    done_cv_.notify_all();
+    return GBA_OK;
+  }
+  queue_.push_back(r);
+  st_.queued = (int32_t)queue_.size();
   cv_.notify_all();
   return GBA_OK;
 }

@@ -181,10 +181,50 @@ def test_invalid_inputs_raise():
         with pytest.raises(GBAError) as ei:
             s.solve(bad)
         assert ei.value.status == 3
+        # a point observed more than 256 times does not fit a chunk
+        k = 300
+        ci = np.concatenate([b.camera_index(), np.arange(k, dtype=np.int32) % b.num_cameras()])
+        pi = np.concatenate([b.point_index(), np.zeros(k, np.int32)])
+        uv = np.concatenate([b.observations(), np.tile(b.observations()[:2], k)])
+        big = BALProblem.from_arrays(b.num_cameras(), b.num_points(), ci, pi, uv, b.parameters().copy())
+        with pytest.raises(GBAError) as ei:
+            s.solve(big)
+        assert ei.value.status == 1 and "observed" in str(ei.value)
         # the handle stays usable after an error
         ok = b.copy()
         sm = s.solve(ok)
         assert sm.final_cost < sm.initial_cost
+
+
+def test_problem_without_observations():
+    """A problem without observations has no parameter blocks in the
+    reference's problem, and Ceres returns at once for it (CONVERGENCE, cost
+    0, no iterations): so do gba_solve, gba_batch_solve (the other problems
+    of the batch get the bits they get alone) and the server (the ticket is
+    done at once).  The parameters are left as they are."""
+    b = small_problem(num_points=300)
+    none = np.zeros(0, np.int32)
+    e = BALProblem.from_arrays(b.num_cameras(), b.num_points(), none, none, np.zeros(0), b.parameters().copy())
+    z = BALProblem.from_arrays(0, 0, none, none, np.zeros(0), np.zeros(0))
+    before = e.parameters().copy()
+    with Solver(max_num_iterations=5) as s:
+        sm = s.solve(e)
+        alone = b.copy()
+        sa = s.solve(alone)
+        mix = [e.copy(), b.copy(), z.copy()]
+        sums = s.batch_solve(mix)
+    assert sm.termination_type == "CONVERGENCE" and sm.num_iterations == 0
+    assert sm.initial_cost == 0.0 and sm.final_cost == 0.0
+    np.testing.assert_array_equal(e.parameters(), before)
+    assert np.array_equal(mix[1].parameters(), alone.parameters()) and sums[1].final_cost == sa.final_cost
+    assert sums[0].num_iterations == 0 and sums[2].num_iterations == 0 and sums[2].final_cost == 0.0
+    np.testing.assert_array_equal(mix[0].parameters(), before)
+    with Solver(max_num_iterations=5) as s:
+        s.start_server()
+        t = s.submit(e.copy())
+        r = s.poll(t)
+        s.stop_server()
+    assert r is not None and r.num_iterations == 0 and r.termination_type == "CONVERGENCE"
 
 
 @pytest.mark.parametrize("crit", ["residual", "quadratic_model"])
