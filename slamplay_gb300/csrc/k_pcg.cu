@@ -493,7 +493,7 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg_camera(DeviceBatch B) {
   __shared__ double red3[kPcgWarps][3];
   __shared__ double sc[2];
   __shared__ double chs[kPcgChunkSums];  // the explicit FP64 form's p.q chunk sums
-  __shared__ int flag;
+  __shared__ int flag, sgood;
   constexpr int kLeadWarps = (kPcgCoords + 31) / 32;  // the warps holding sub-lane 0
   const int4 cb = B.camblk[blockIdx.x];  // (problem, first camera, count, 0)
   const int prob = cb.x;
@@ -604,6 +604,7 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg_camera(DeviceBatch B) {
         const double s2 = chs[0];
         sc[0] = s2;
         sc[1] = rz_k * recip_nr(s2);
+        sgood = s2 > 0.0 && isfinite(s2);
       }
     } else if (dfs) {
 #pragma unroll
@@ -628,11 +629,15 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg_camera(DeviceBatch B) {
       }
       sc[0] = s2;
       sc[1] = rz_k * recip_nr(s2);
+      sgood = s2 > 0.0 && isfinite(s2);
     }
     __syncthreads();
     pq = sc[0];
   }
-  const bool good = pq > 0.0 && isfinite(pq);  // else S is not positive definite along p_k
+  // pq > 0 and finite (else S is not positive definite along p_k), tested
+  // once by thread 0: an FP64 comparison in every warp would queue on the
+  // FP64 pipes
+  const bool good = live && sgood != 0;
   if (live && good) {
     const double alpha = sc[1];
     double p = 0.0;

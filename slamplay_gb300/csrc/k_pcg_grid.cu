@@ -185,7 +185,7 @@ __host__ __device__ inline int rows_below(long long t, long long before9, long l
 __global__ void __launch_bounds__(kGThreads, 1) k_pcg_grid(DeviceBatch B, int cap_blocks, int cache_s,
                                                          int cap_pairs) {
   extern __shared__ __align__(16) unsigned char g_smem[];
-  __shared__ int s_ticket, s_P, s_ok, s_ra, s_rb, s_stop, s_pass_end, s_npairs, s_nlev;
+  __shared__ int s_ticket, s_P, s_ok, s_ra, s_rb, s_stop, s_pass_end, s_npairs, s_nlev, s_good;
   __shared__ double sc[4], s_inv_rz;
   __shared__ double tot3[3];
   __shared__ double rv[kGThreads];  // r_{k+1} of the update's coordinates, for M r
@@ -477,7 +477,7 @@ __global__ void __launch_bounds__(kGThreads, 1) k_pcg_grid(DeviceBatch B, int ca
       if (nch <= 32) {  // the tree by one warp's shuffles (no barrier per level)
         if (warp == 0) {
           const double s2 = warp_pairwise_tree(lane < nch ? chs[lane] : 0.0, nch);
-          if (lane == 0) sc[0] = s2, sc[1] = rz_k * recip_nr(s2);
+          if (lane == 0) sc[0] = s2, sc[1] = rz_k * recip_nr(s2), s_good = s2 > 0.0 && isfinite(s2);
         }
       } else {
         cta_pairwise_tree(chs, nch);
@@ -485,12 +485,15 @@ __global__ void __launch_bounds__(kGThreads, 1) k_pcg_grid(DeviceBatch B, int ca
           const double s2 = chs[0];
           sc[0] = s2;
           sc[1] = rz_k * recip_nr(s2);
+          s_good = s2 > 0.0 && isfinite(s2);
         }
       }
       __syncthreads();
     }
     const double pq = sc[0], alpha = sc[1];
-    const bool good = pq > 0.0 && isfinite(pq);  // else S is not positive definite along p_k
+    // pq > 0 and finite, tested once (else S is not positive definite along
+    // p_k): an FP64 comparison in every warp would queue on the FP64 pipes
+    const bool good = s_good != 0;
     if (!good) {                                  // the PCG ends with x_k
       if (k == 0) linear_ok = false;
       break;
