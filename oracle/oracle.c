@@ -1,7 +1,7 @@
 /*
  * oracle.c — CPU oracle for the bundle-adjustment hot path.
  *
- * TEST INFRASTRUCTURE ONLY: the checker the GPU solver is compared against
+ * TEST INFRASTRUCTURE ONLY: the reference the GPU solver is compared against
  * (tests/, __graft_entry__.smoke(), bench.py's CPU-baseline leg).  Never
  * linked into libgba.  See oracle.h for what it restates and where from.
  *

@@ -1,8 +1,8 @@
 /*
  * oracle.h — CPU oracle for the bundle-adjustment hot path.
  *
- * TEST INFRASTRUCTURE ONLY.  This is the checker that the GPU solver in
- * slamplay_gb300/ is compared against; nothing in the product links it.
+ * TEST INFRASTRUCTURE ONLY.  The GPU solver in slamplay_gb300/ is compared
+ * against this oracle; nothing in the product links it.
  *
  * What it restates (file:line in luigifreda/slamplay):
  *   - residual model: utils/camera/SnavelyReprojectionError.h:42-53, :61-87

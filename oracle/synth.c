@@ -1,6 +1,6 @@
 /*
  * synth.c — the benchmark configurations' synthetic problems, generated on
- * the CPU side of the checker.
+ * the oracle's side.
  *
  * TEST INFRASTRUCTURE ONLY.  The reference ships one real BAL file and no
  * generator; the benchmark workloads are seeded synthetic BAL problems that
