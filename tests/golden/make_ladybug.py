@@ -10,8 +10,8 @@ utils/datasets/BALProblem.cpp compiled into oracle/_ref (oracle/build_ref.sh):
       the C library's rand() in its initial state (main() never seeds it:
       srand(1)).
 
-The GPU machine has no reference tree, so the fixture carries these arrays to
-the tests there.  Run from the repository root where the reference tree is
+A machine that runs the GPU tests need not have the reference tree, so the
+fixture carries these arrays to the tests there.  Run from the repository root where the reference tree is
 present: python tests/golden/make_ladybug.py
 """
 import os

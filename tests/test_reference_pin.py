@@ -2,7 +2,7 @@
 reference's OWN sources (utils/camera/SnavelyReprojectionError.h,
 utils/geometry/rotation.h, utils/datasets/BALProblem.cpp), compiled by
 oracle/build_ref.sh into oracle/_ref with declaration shims for Ceres/Eigen.
-Skipped where the reference tree is not available (e.g. the GPU machine)."""
+Skipped where the reference tree is not available."""
 import ctypes
 import os
 
