@@ -86,12 +86,13 @@ gba_status Server::submit(const gba_problem_view *p, uint64_t *ticket, std::stri
     *err = "server not running";
     return GBA_ERR_INVALID_ARGUMENT;
   }
-  if (fp > budget_) {
+  const bool empty = p->num_observations == 0;  // nothing to solve: done at once, as gba_solve
+  if (!empty && fp > budget_) {
     ++st_.rejected;
     *err = "problem footprint exceeds the device budget";
     return GBA_ERR_OUT_OF_MEMORY;
   }
-  if ((int)queue_.size() >= max_queue_) {
+  if (!empty && (int)queue_.size() >= max_queue_) {
     ++st_.rejected;
     *err = "request queue full";
     return GBA_ERR_QUEUE_FULL;
@@ -104,7 +105,7 @@ gba_status Server::submit(const gba_problem_view *p, uint64_t *ticket, std::stri
   tickets_[r->ticket] = r;
   ++st_.submitted;
   *ticket = r->ticket;
-  if (p->num_observations == 0) {  // nothing to solve: done at once, as gba_solve
+  if (empty) {
     empty_problem_summary(&r->summary, o_.initial_trust_region_radius);
     r->done = true;
     ++st_.completed;
