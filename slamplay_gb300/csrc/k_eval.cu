@@ -389,8 +389,11 @@ __device__ __forceinline__ double eval_observation_df(const DeviceBatch &B, int6
 // (g = 0) is the FP64 one to double-float rounding; the FP32 copies only
 // feed the Schur products and the PCG, i.e. the accuracy of each step, not
 // where the steps lead.
+// The mixed form's per-iteration pass waits mostly at its CTA barriers:
+// three CTAs per SM (80 registers a thread, a few spilled) instead of two
+// (128) take 13 % off it on configuration 2.
 template <bool MIXED, bool NORMS>
-__global__ void __launch_bounds__(kChunkCap) k_eval_chunk(DeviceBatch B) {
+__global__ void __launch_bounds__(kChunkCap, (MIXED && !NORMS) ? 3 : 1) k_eval_chunk(DeviceBatch B) {
   typedef typename Prec<MIXED>::real real;
   typedef typename Prec<MIXED>::real2 real2;
   typedef typename Acc<MIXED>::type Acc;
