@@ -85,8 +85,8 @@ __device__ __forceinline__ void sym9_pair(int e, int &a, int &b) {
   b = a + e;
 }
 
-template <bool MIXED>
 // (the mixed form at four CTAs per SM: 64 registers a thread)
+template <bool MIXED>
 __global__ void __launch_bounds__(kChunkCap, MIXED ? 4 : 1) k_point_schur(DeviceBatch B) {
   typedef typename Prec<MIXED>::real real;
   typedef typename Prec<MIXED>::real2 real2;
