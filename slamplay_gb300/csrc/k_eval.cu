@@ -389,11 +389,13 @@ __device__ __forceinline__ double eval_observation_df(const DeviceBatch &B, int6
 // (g = 0) is the FP64 one to double-float rounding; the FP32 copies only
 // feed the Schur products and the PCG, i.e. the accuracy of each step, not
 // where the steps lead.
-// The mixed form's per-iteration pass waits mostly at its CTA barriers:
-// three CTAs per SM (80 registers a thread, a few spilled) instead of two
-// (128) take 13 % off it on configuration 2.
+// The per-iteration pass (not the first evaluation's column norms) at three
+// CTAs per SM (80 registers a thread, a few spilled) instead of two (122-128):
+// the mixed pass waits mostly at its CTA barriers (13 % off on configuration
+// 2), the FP64 pass hides more of its FP64 latency (6 % off on configuration
+// 2, 1.5 % on configuration 1).
 template <bool MIXED, bool NORMS>
-__global__ void __launch_bounds__(kChunkCap, (MIXED && !NORMS) ? 3 : 1) k_eval_chunk(DeviceBatch B) {
+__global__ void __launch_bounds__(kChunkCap, !NORMS ? 3 : 1) k_eval_chunk(DeviceBatch B) {
   typedef typename Prec<MIXED>::real real;
   typedef typename Prec<MIXED>::real2 real2;
   typedef typename Acc<MIXED>::type Acc;
