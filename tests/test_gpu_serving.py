@@ -125,6 +125,12 @@ def test_server_rejects_oversize_and_survives():
 
         with pytest.raises(GBAError):
             s.submit(_requests(1)[0])
+        # a request without observations needs no device memory: done at once
+        b = _requests(1)[0]
+        none = np.zeros(0, np.int32)
+        e = BALProblem.from_arrays(b.num_cameras(), b.num_points(), none, none, np.zeros(0), b.parameters().copy())
+        r = s.poll(s.submit(e))
         st = s.server_stats()
         s.stop_server()
     assert st["rejected"] == 1
+    assert r is not None and r.num_iterations == 0 and r.final_cost == 0.0
